@@ -1,0 +1,1199 @@
+/* Oracle (test infrastructure only): the per-step world pipeline restated from the reference.
+ *
+ *   StepFixed order                    src/World/PhysicsWorld.cpp:245-329
+ *   UpdateBroadPhase                   PhysicsWorld.cpp:334-345
+ *   dynamic AABB tree + UpdatePairs    src/BroadPhase/BroadPhase.cpp:13-270,368-381,
+ *                                      include/Kizuri/BroadPhase/BroadPhase.h:62-104
+ *   Collide                            PhysicsWorld.cpp:350-400 (MakePairKey :13-18, SwapManifold :22-29)
+ *   manifold cache                     PhysicsWorld.cpp:405-452
+ *   BuildContactConstraints            PhysicsWorld.cpp:454-535
+ *   IntegrateVelocities                PhysicsWorld.cpp:757-783
+ *   Prepare / WarmStart / bias pass    src/Solver/ContactSolver.cpp:18-132, 257-290
+ *   BuildIslands / SolveIsland         PhysicsWorld.cpp:587-743
+ *   SIMD velocity batch (lane order)   src/Solver/ContactSolverSIMD.cpp:93-256
+ *   IntegratePositions / pseudo / inertia  PhysicsWorld.cpp:276-290, 785-802, 854-861
+ *   ComputeStateHash                   PhysicsWorld.cpp:1145-1175
+ *
+ * Lanes of the 4-wide SSE batch never interact, so the batch is evaluated lane by lane with
+ * the same per-lane operation sequence; -ffp-contract=off keeps every a*b+c unfused.
+ */
+#include "kzo.h"
+#include "kzo_internal.h"
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define NUL 0xFFFFFFFFu
+
+static char g_err[256];
+const char* kzo_error(void) { return g_err; }
+static void set_err(const char* m) { snprintf(g_err, sizeof g_err, "%s", m); }
+
+/* ----------------------------------------------------------------------------- */
+typedef struct { aabb fat, tight; uint32_t parent, c1, c2, user, next; int32_t height; } node_t;
+
+typedef struct {
+    v3 pA, pB, rA, rB, laA, laB, n, t1, t2;
+    float nm, tm1, tm2, ni, ti1, ti2, sep, rbias, pbias, bimp, fric, rest, nvel;
+    uint32_t feature;
+} cpc_t;
+
+typedef struct {
+    int a, b;
+    uint32_t npts;
+    cpc_t p[KZO_MAX_MANIFOLD];
+    float friction, restitution;
+    int sensor, dynA, dynB;
+} con_t;
+
+typedef struct {
+    uint64_t key;
+    uint32_t frame, npts;
+    v3 pos[KZO_MAX_MANIFOLD];
+    float ni[KZO_MAX_MANIFOLD], ti1[KZO_MAX_MANIFOLD], ti2[KZO_MAX_MANIFOLD];
+} cache_t;
+
+typedef struct { int con; uint32_t pt; } pref_t;
+typedef struct { pref_t ref[4]; int a[4], b[4]; uint32_t count; } batch_t;
+
+struct kzo_world {
+    /* settings (WorldSettings / SolverSettings) */
+    v3 gravity;
+    float fixed_dt, baumgarte, slop, rest_thresh, max_bias, ws_factor;
+    uint32_t vel_iters, pos_iters;
+    int vel_bias, no_ws, threads, pair_mode, sched_stats;
+    /* shapes */
+    int nshapes;
+    kzo_shape* shapes;
+    /* bodies (slot order) */
+    int nb;
+    uint32_t *packed, *layer, *mask, *proxy;
+    int* shape;
+    uint8_t *motion, *sensor;
+    v3 *pos, *lv, *av, *plv, *pav, *force, *torque;
+    qt* rot;
+    float *inv_mass, *lin_damp, *ang_damp, *grav, *max_lin, *max_ang, *fric, *rest;
+    m3 *iil, *iiw;
+    int* active;
+    int nactive;
+    /* broad phase tree */
+    node_t* nodes;
+    uint32_t nnodes, node_cap, root, free_list, nproxies;
+    uint32_t *bp_layer, *bp_mask;
+    uint32_t bp_layer_cap;
+    /* manifold cache */
+    cache_t* cache;
+    uint32_t cache_cap, cache_count, frame;
+    /* per step */
+    uint32_t* pairs; /* packed A, packed B */
+    uint32_t npairs, pairs_cap;
+    uint32_t* ext_pairs;
+    uint32_t next_pairs;
+    kzo_manifold* man;
+    uint64_t* keys;
+    uint32_t man_cap;
+    con_t* cons;
+    uint32_t ncons, cons_cap;
+    /* islands */
+    uint32_t nislands;
+    uint32_t* isl_off; /* nislands+1 */
+    uint32_t* isl_con;
+    int* island_index;
+    /* stats */
+    uint32_t st_points, st_batches, st_max_vl, st_max_bl, st_max_isl_pts, st_sum_vl;
+};
+
+/* ----------------------------------------------------------------------------- */
+/* Utilities                                                                     */
+/* ----------------------------------------------------------------------------- */
+static void* xrealloc(void* p, size_t n) {
+    void* q = realloc(p, n ? n : 1);
+    if (!q) { fprintf(stderr, "kzo: out of memory\n"); abort(); }
+    return q;
+}
+
+static int body_of(const kzo_world* w, uint32_t packed) {
+    uint32_t slot = packed & 0x00FFFFFFu;
+    if (slot >= (uint32_t)w->nb || w->packed[slot] != packed) return -1;
+    return (int)slot;
+}
+
+static uint64_t pair_key(uint32_t pa, uint32_t pb) {
+    if (pa > pb) { uint32_t t = pa; pa = pb; pb = t; }
+    return ((uint64_t)pa << 32) | (uint64_t)pb;
+}
+
+/* ----------------------------------------------------------------------------- */
+/* Dynamic AABB tree (BroadPhase.cpp)                                             */
+/* ----------------------------------------------------------------------------- */
+static node_t node_default(void) {
+    node_t n;
+    n.fat = aabb_empty();
+    n.tight = aabb_empty();
+    n.parent = n.c1 = n.c2 = NUL;
+    n.user = 0;
+    n.next = NUL;
+    n.height = -1;
+    return n;
+}
+static int is_leaf(const kzo_world* w, uint32_t i) { return w->nodes[i].c1 == NUL; }
+
+static uint32_t alloc_node(kzo_world* w) {
+    if (w->free_list != NUL) {
+        uint32_t id = w->free_list;
+        w->free_list = w->nodes[id].next;
+        w->nodes[id] = node_default();
+        w->nodes[id].next = NUL;
+        return id;
+    }
+    if (w->nnodes == w->node_cap) {
+        w->node_cap = w->node_cap ? w->node_cap * 2 : 1024;
+        w->nodes = (node_t*)xrealloc(w->nodes, sizeof(node_t) * w->node_cap);
+    }
+    w->nodes[w->nnodes] = node_default();
+    return w->nnodes++;
+}
+static void free_node(kzo_world* w, uint32_t id) {
+    w->nodes[id] = node_default();
+    w->nodes[id].next = w->free_list;
+    w->nodes[id].height = -1;
+    w->free_list = id;
+}
+
+static int32_t imax(int32_t a, int32_t b) { return a > b ? a : b; }
+
+static uint32_t balance(kzo_world* w, uint32_t iA) {
+    node_t* N = w->nodes;
+    node_t* A = &N[iA];
+    if (A->c1 == NUL || A->height < 2) return iA;
+    uint32_t iB = A->c1, iC = A->c2;
+    node_t *B = &N[iB], *C = &N[iC];
+    int32_t bal = C->height - B->height;
+    if (bal > 1) {
+        uint32_t iF = C->c1, iG = C->c2;
+        node_t *F = &N[iF], *G = &N[iG];
+        C->c1 = iA;
+        C->parent = A->parent;
+        A->parent = iC;
+        if (C->parent != NUL) {
+            if (N[C->parent].c1 == iA) N[C->parent].c1 = iC;
+            else N[C->parent].c2 = iC;
+        } else {
+            w->root = iC;
+        }
+        if (F->height > G->height) {
+            C->c2 = iF; A->c2 = iG; G->parent = iA;
+            A->fat = aabb_merge(B->fat, G->fat);
+            C->fat = aabb_merge(A->fat, F->fat);
+            A->height = 1 + imax(B->height, G->height);
+            C->height = 1 + imax(A->height, F->height);
+        } else {
+            C->c2 = iG; A->c2 = iF; F->parent = iA;
+            A->fat = aabb_merge(B->fat, F->fat);
+            C->fat = aabb_merge(A->fat, G->fat);
+            A->height = 1 + imax(B->height, F->height);
+            C->height = 1 + imax(A->height, G->height);
+        }
+        return iC;
+    }
+    if (bal < -1) {
+        uint32_t iD = B->c1, iE = B->c2;
+        node_t *D = &N[iD], *E = &N[iE];
+        B->c1 = iA;
+        B->parent = A->parent;
+        A->parent = iB;
+        if (B->parent != NUL) {
+            if (N[B->parent].c1 == iA) N[B->parent].c1 = iB;
+            else N[B->parent].c2 = iB;
+        } else {
+            w->root = iB;
+        }
+        if (D->height > E->height) {
+            B->c2 = iD; A->c1 = iE; E->parent = iA;
+            A->fat = aabb_merge(C->fat, E->fat);
+            B->fat = aabb_merge(A->fat, D->fat);
+            A->height = 1 + imax(C->height, E->height);
+            B->height = 1 + imax(A->height, D->height);
+        } else {
+            B->c2 = iE; A->c1 = iD; D->parent = iA;
+            A->fat = aabb_merge(C->fat, D->fat);
+            B->fat = aabb_merge(A->fat, E->fat);
+            A->height = 1 + imax(C->height, D->height);
+            B->height = 1 + imax(A->height, E->height);
+        }
+        return iB;
+    }
+    return iA;
+}
+
+static void insert_leaf(kzo_world* w, uint32_t leaf) {
+    if (w->root == NUL) { w->root = leaf; w->nodes[leaf].parent = NUL; return; }
+    aabb la = w->nodes[leaf].fat;
+    uint32_t index = w->root;
+    while (!is_leaf(w, index)) {
+        uint32_t c1 = w->nodes[index].c1, c2 = w->nodes[index].c2;
+        float area = aabb_area(w->nodes[index].fat);
+        aabb comb = aabb_merge(w->nodes[index].fat, la);
+        float ca = aabb_area(comb);
+        float cost = 2.0f * ca;
+        float inh = 2.0f * (ca - area);
+        float cost1, cost2;
+        {
+            aabb m = aabb_merge(la, w->nodes[c1].fat);
+            cost1 = is_leaf(w, c1) ? aabb_area(m) + inh : (aabb_area(m) - aabb_area(w->nodes[c1].fat)) + inh;
+        }
+        {
+            aabb m = aabb_merge(la, w->nodes[c2].fat);
+            cost2 = is_leaf(w, c2) ? aabb_area(m) + inh : (aabb_area(m) - aabb_area(w->nodes[c2].fat)) + inh;
+        }
+        if (cost < cost1 && cost < cost2) break;
+        index = (cost1 < cost2) ? c1 : c2;
+    }
+    uint32_t sib = index;
+    uint32_t old_parent = w->nodes[sib].parent;
+    uint32_t np = alloc_node(w);
+    w->nodes[np].parent = old_parent;
+    w->nodes[np].fat = aabb_merge(la, w->nodes[sib].fat);
+    w->nodes[np].tight = w->nodes[np].fat;
+    w->nodes[np].height = w->nodes[sib].height + 1;
+    w->nodes[np].user = 0;
+    if (old_parent != NUL) {
+        if (w->nodes[old_parent].c1 == sib) w->nodes[old_parent].c1 = np;
+        else w->nodes[old_parent].c2 = np;
+    } else {
+        w->root = np;
+    }
+    w->nodes[np].c1 = sib;
+    w->nodes[np].c2 = leaf;
+    w->nodes[sib].parent = np;
+    w->nodes[leaf].parent = np;
+    index = w->nodes[leaf].parent;
+    while (index != NUL) {
+        index = balance(w, index);
+        uint32_t c1 = w->nodes[index].c1, c2 = w->nodes[index].c2;
+        w->nodes[index].height = 1 + imax(w->nodes[c1].height, w->nodes[c2].height);
+        w->nodes[index].fat = aabb_merge(w->nodes[c1].fat, w->nodes[c2].fat);
+        index = w->nodes[index].parent;
+    }
+}
+
+static void remove_leaf(kzo_world* w, uint32_t leaf) {
+    if (leaf == w->root) { w->root = NUL; return; }
+    uint32_t parent = w->nodes[leaf].parent;
+    uint32_t gp = w->nodes[parent].parent;
+    uint32_t sib = (w->nodes[parent].c1 == leaf) ? w->nodes[parent].c2 : w->nodes[parent].c1;
+    if (gp != NUL) {
+        if (w->nodes[gp].c1 == parent) w->nodes[gp].c1 = sib;
+        else w->nodes[gp].c2 = sib;
+        w->nodes[sib].parent = gp;
+        free_node(w, parent);
+        uint32_t index = gp;
+        while (index != NUL) {
+            index = balance(w, index);
+            uint32_t c1 = w->nodes[index].c1, c2 = w->nodes[index].c2;
+            w->nodes[index].fat = aabb_merge(w->nodes[c1].fat, w->nodes[c2].fat);
+            w->nodes[index].height = 1 + imax(w->nodes[c1].height, w->nodes[c2].height);
+            index = w->nodes[index].parent;
+        }
+    } else {
+        w->root = sib;
+        w->nodes[sib].parent = NUL;
+        free_node(w, parent);
+    }
+}
+
+static uint32_t create_proxy(kzo_world* w, aabb b, uint32_t user, uint32_t layer, uint32_t mask) {
+    uint32_t id = alloc_node(w);
+    v3 margin = V(0.1f, 0.1f, 0.1f);
+    w->nodes[id].fat = AB(vsub(b.mn, margin), vadd(b.mx, margin));
+    w->nodes[id].tight = b;
+    w->nodes[id].user = user;
+    w->nodes[id].height = 0;
+    w->nodes[id].c1 = w->nodes[id].c2 = NUL;
+    w->nodes[id].parent = NUL;
+    insert_leaf(w, id);
+    ++w->nproxies;
+    if (id >= w->bp_layer_cap) {
+        uint32_t nc = w->bp_layer_cap ? w->bp_layer_cap : 256;
+        while (nc <= id) nc *= 2;
+        w->bp_layer = (uint32_t*)xrealloc(w->bp_layer, sizeof(uint32_t) * nc);
+        w->bp_mask = (uint32_t*)xrealloc(w->bp_mask, sizeof(uint32_t) * nc);
+        for (uint32_t i = w->bp_layer_cap; i < nc; ++i) w->bp_layer[i] = w->bp_mask[i] = 0;
+        w->bp_layer_cap = nc;
+    }
+    w->bp_layer[id] = layer;
+    w->bp_mask[id] = mask;
+    return id;
+}
+
+static void move_proxy(kzo_world* w, uint32_t id, aabb b, v3 disp) {
+    w->nodes[id].tight = b;
+    if (aabb_contains(w->nodes[id].fat, b)) return;
+    remove_leaf(w, id);
+    v3 margin = V(0.1f, 0.1f, 0.1f);
+    v3 d = vabs(disp);
+    w->nodes[id].fat = AB(vsub(vsub(b.mn, margin), d), vadd(vadd(b.mx, margin), d));
+    insert_leaf(w, id);
+}
+
+static void push_pair(kzo_world* w, uint32_t a, uint32_t b) {
+    if (w->npairs == w->pairs_cap) {
+        w->pairs_cap = w->pairs_cap ? w->pairs_cap * 2 : 1024;
+        w->pairs = (uint32_t*)xrealloc(w->pairs, sizeof(uint32_t) * 2 * w->pairs_cap);
+    }
+    w->pairs[2 * w->npairs] = a;
+    w->pairs[2 * w->npairs + 1] = b;
+    ++w->npairs;
+}
+
+/* QueryPairs (BroadPhase.h:62-104) + UpdatePairs filter (BroadPhase.cpp:368-381). */
+static void tree_pairs(kzo_world* w) {
+    w->npairs = 0;
+    if (w->root == NUL) return;
+    uint32_t cap = 1024, sz = 0;
+    uint32_t* st = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * 2 * cap);
+#define PUSH(a, b)                                                            \
+    do {                                                                      \
+        if (sz == cap) { cap *= 2; st = (uint32_t*)xrealloc(st, sizeof(uint32_t) * 2 * cap); } \
+        st[2 * sz] = (a); st[2 * sz + 1] = (b); ++sz;                         \
+    } while (0)
+    PUSH(w->root, w->root);
+    while (sz > 0) {
+        --sz;
+        uint32_t n1 = st[2 * sz], n2 = st[2 * sz + 1];
+        const node_t* a = &w->nodes[n1];
+        if (n1 == n2) {
+            if (a->c1 == NUL) continue;
+            uint32_t c1 = a->c1, c2 = a->c2;
+            PUSH(c1, c1);
+            PUSH(c2, c2);
+            PUSH(c1, c2);
+            continue;
+        }
+        const node_t* b = &w->nodes[n2];
+        if (!aabb_overlaps(a->fat, b->fat)) continue;
+        int la = a->c1 == NUL, lb = b->c1 == NUL;
+        if (la && lb) {
+            if (n1 < n2) {
+                if ((w->bp_layer[n1] & w->bp_mask[n2]) == 0) continue;
+                if ((w->bp_layer[n2] & w->bp_mask[n1]) == 0) continue;
+                if (!aabb_overlaps(w->nodes[n1].tight, w->nodes[n2].tight)) continue;
+                push_pair(w, w->nodes[n1].user, w->nodes[n2].user);
+            }
+            continue;
+        }
+        uint32_t ac1 = a->c1, ac2 = a->c2, bc1 = b->c1, bc2 = b->c2;
+        if (la || (!lb && a->height < b->height)) {
+            PUSH(n1, bc1);
+            PUSH(n1, bc2);
+        } else {
+            PUSH(ac1, n2);
+            PUSH(ac2, n2);
+        }
+    }
+#undef PUSH
+    free(st);
+}
+
+/* Canonical pairs: every overlapping pair (tight AABBs, layer filter), MakePairKey order. */
+typedef struct { float mnx; int i; } sweep_t;
+static int cmp_sweep(const void* a, const void* b) {
+    const sweep_t *x = (const sweep_t*)a, *y = (const sweep_t*)b;
+    if (x->mnx < y->mnx) return -1;
+    if (x->mnx > y->mnx) return 1;
+    return x->i - y->i;
+}
+static int cmp_key(const void* a, const void* b) {
+    const uint32_t *x = (const uint32_t*)a, *y = (const uint32_t*)b;
+    if (x[0] != y[0]) return x[0] < y[0] ? -1 : 1;
+    if (x[1] != y[1]) return x[1] < y[1] ? -1 : 1;
+    return 0;
+}
+static void canonical_pairs(kzo_world* w) {
+    w->npairs = 0;
+    aabb* bb = (aabb*)xrealloc(NULL, sizeof(aabb) * (size_t)w->nb);
+    sweep_t* sw = (sweep_t*)xrealloc(NULL, sizeof(sweep_t) * (size_t)w->nb);
+    for (int i = 0; i < w->nb; ++i) {
+        bb[i] = kzo_world_bounds(&w->shapes[w->shape[i]], w->rot[i], w->pos[i]);
+        sw[i].mnx = bb[i].mn.x;
+        sw[i].i = i;
+    }
+    qsort(sw, (size_t)w->nb, sizeof(sweep_t), cmp_sweep);
+    for (int s = 0; s < w->nb; ++s) {
+        int i = sw[s].i;
+        for (int t = s + 1; t < w->nb && sw[t].mnx <= bb[i].mx.x; ++t) {
+            int j = sw[t].i;
+            if ((w->layer[i] & w->mask[j]) == 0 || (w->layer[j] & w->mask[i]) == 0) continue;
+            if (!aabb_overlaps(bb[i], bb[j])) continue;
+            uint32_t pa = w->packed[i], pb = w->packed[j];
+            if (pa < pb) push_pair(w, pa, pb); else push_pair(w, pb, pa);
+        }
+    }
+    qsort(w->pairs, w->npairs, sizeof(uint32_t) * 2, cmp_key);
+    free(bb);
+    free(sw);
+}
+
+/* ----------------------------------------------------------------------------- */
+/* Manifold cache (PhysicsWorld.cpp:405-452)                                       */
+/* ----------------------------------------------------------------------------- */
+static cache_t* find_cached(kzo_world* w, uint64_t key) {
+    if (w->cache_cap == 0) return NULL;
+    uint32_t mask = w->cache_cap - 1;
+    uint32_t slot = (uint32_t)(key ^ (key >> 32)) & mask;
+    for (uint32_t p = 0; p < w->cache_cap; ++p) {
+        cache_t* e = &w->cache[slot];
+        if (e->key == key && e->frame != 0) return e;
+        if (e->frame == 0) return NULL;
+        slot = (slot + 1) & mask;
+    }
+    return NULL;
+}
+
+static cache_t* get_or_create_cached(kzo_world* w, uint64_t key) {
+    if (w->cache_count * 10u >= w->cache_cap * 7u) {
+        uint32_t ncap = w->cache_cap * 2;
+        cache_t* nc = (cache_t*)calloc(ncap, sizeof(cache_t));
+        uint32_t mask = ncap - 1;
+        for (uint32_t i = 0; i < w->cache_cap; ++i) {
+            cache_t* e = &w->cache[i];
+            if (e->frame == 0) continue;
+            uint32_t slot = (uint32_t)(e->key ^ (e->key >> 32)) & mask;
+            while (nc[slot].frame != 0) slot = (slot + 1) & mask;
+            nc[slot] = *e;
+        }
+        free(w->cache);
+        w->cache = nc;
+        w->cache_cap = ncap;
+    }
+    uint32_t mask = w->cache_cap - 1;
+    uint32_t slot = (uint32_t)(key ^ (key >> 32)) & mask;
+    for (;;) {
+        cache_t* e = &w->cache[slot];
+        if (e->frame == 0) {
+            memset(e, 0, sizeof *e);
+            e->key = key;
+            e->frame = w->frame;
+            ++w->cache_count;
+            return e;
+        }
+        if (e->key == key) { e->frame = w->frame; return e; }
+        slot = (slot + 1) & mask;
+    }
+}
+
+/* ----------------------------------------------------------------------------- */
+/* Solver pieces (ContactSolver.cpp, ContactSolverSIMD.cpp)                         */
+/* ----------------------------------------------------------------------------- */
+static float effective_mass(const kzo_world* w, int a, int b, v3 rA, v3 rB, v3 dir) {
+    v3 ra = vcross(rA, dir), rb = vcross(rB, dir);
+    float k = w->inv_mass[a] + w->inv_mass[b];
+    k += vdot(ra, mmulv(&w->iiw[a], ra));
+    k += vdot(rb, mmulv(&w->iiw[b], rb));
+    return k > KZO_EPS ? 1.0f / k : 0.0f;
+}
+
+static void prepare(kzo_world* w, con_t* c, float dt) {
+    int A = c->a, B = c->b;
+    c->dynA = w->motion[A] == KZO_DYNAMIC;
+    c->dynB = w->motion[B] == KZO_DYNAMIC;
+    for (uint32_t i = 0; i < c->npts; ++i) {
+        cpc_t* p = &c->p[i];
+        p->rA = vsub(p->pA, w->pos[A]);
+        p->rB = vsub(p->pB, w->pos[B]);
+        p->laA = qinv_rotate(w->rot[A], p->rA);
+        p->laB = qinv_rotate(w->rot[B], p->rB);
+        v3 n = vnormalized_or(p->n, V(0, 1, 0));
+        p->n = n;
+        v3 t1 = vperp_normalized(n);
+        p->t1 = t1;
+        p->t2 = vcross(n, t1);
+        p->nm = effective_mass(w, A, B, p->rA, p->rB, n);
+        p->tm1 = effective_mass(w, A, B, p->rA, p->rB, p->t1);
+        p->tm2 = effective_mass(w, A, B, p->rA, p->rB, p->t2);
+        v3 vA = vadd(w->lv[A], vcross(w->av[A], vsub(p->pA, w->pos[A])));
+        v3 vB = vadd(w->lv[B], vcross(w->av[B], vsub(p->pB, w->pos[B])));
+        v3 vr = vsub(vA, vB);
+        p->nvel = vdot(vr, n);
+        p->rbias = 0;
+        if (p->nvel < -w->rest_thresh) p->rbias = -p->rest * p->nvel;
+        p->pbias = 0;
+        if (p->sep < -w->slop) {
+            p->pbias = w->baumgarte / dt * (-p->sep - w->slop);
+            p->pbias = fmin_r(p->pbias, w->max_bias);
+        }
+        p->bimp = 0;
+        float mf = p->fric * p->ni;
+        p->ti1 = fclamp_r(p->ti1, -mf, mf);
+        p->ti2 = fclamp_r(p->ti2, -mf, mf);
+        p->ni = fmax_r(p->ni, 0.0f);
+    }
+}
+
+static void apply_pair(kzo_world* w, int a, int b, v3 rA, v3 rB, v3 imp, int dynA, int dynB) {
+    if (dynA) {
+        w->lv[a] = vadd(w->lv[a], vmul(imp, w->inv_mass[a]));
+        w->av[a] = vadd(w->av[a], mmulv(&w->iiw[a], vcross(rA, imp)));
+    }
+    if (dynB) {
+        w->lv[b] = vsub(w->lv[b], vmul(imp, w->inv_mass[b]));
+        w->av[b] = vsub(w->av[b], mmulv(&w->iiw[b], vcross(rB, imp)));
+    }
+}
+
+static void warm_start(kzo_world* w, con_t* c) {
+    for (uint32_t i = 0; i < c->npts; ++i) {
+        cpc_t* p = &c->p[i];
+        v3 imp = vadd(vadd(vmul(p->n, p->ni), vmul(p->t1, p->ti1)), vmul(p->t2, p->ti2));
+        imp = vmul(imp, w->ws_factor);
+        apply_pair(w, c->a, c->b, p->rA, p->rB, imp, c->dynA, c->dynB);
+    }
+}
+
+/* One lane of SolveVelocityBatchSIMD (ContactSolverSIMD.cpp:93-256). */
+static void solve_lane(kzo_world* w, con_t* c, cpc_t* p) {
+    int A = c->a, B = c->b;
+    v3 rA = qrotate(w->rot[A], p->laA);
+    v3 rB = qrotate(w->rot[B], p->laB);
+    v3 vA = w->lv[A], wA = w->av[A], vB = w->lv[B], wB = w->av[B];
+    const float invA = w->inv_mass[A], invB = w->inv_mass[B];
+    const m3* IA = &w->iiw[A];
+    const m3* IB = &w->iiw[B];
+    const float nb = p->rbias + (w->vel_bias ? p->pbias : 0.0f);
+    float nacc = p->ni, t1acc = p->ti1, t2acc = p->ti2;
+    for (int t = 0; t < 3; ++t) {
+        v3 dir = t == 0 ? p->t1 : (t == 1 ? p->t2 : p->n);
+        v3 wa = vcross(wA, rA), wb = vcross(wB, rB);
+        v3 rel = V((vA.x + wa.x) - (vB.x + wb.x), (vA.y + wa.y) - (vB.y + wb.y), (vA.z + wa.z) - (vB.z + wb.z));
+        float vdir = vdot(rel, dir);
+        float dl;
+        if (t < 2) {
+            float mass = t == 0 ? p->tm1 : p->tm2;
+            float acc = t == 0 ? t1acc : t2acc;
+            float lambda = (0.0f - mass) * vdir;
+            float maxf = p->fric * nacc;
+            float na = acc + lambda;
+            float lo = 0.0f - maxf;
+            na = na > lo ? na : lo;          /* _mm_max_ps(na, -maxFric) */
+            na = na < maxf ? na : maxf;      /* _mm_min_ps(na, maxFric) */
+            dl = na - acc;
+            if (t == 0) t1acc = na; else t2acc = na;
+        } else {
+            float lambda = (0.0f - p->nm) * (vdir - nb);
+            float na = nacc + lambda;
+            na = na > 0.0f ? na : 0.0f;      /* _mm_max_ps(na, 0) */
+            dl = na - nacc;
+            nacc = na;
+        }
+        v3 imp = V(dir.x * dl, dir.y * dl, dir.z * dl);
+        vA = V(vA.x + imp.x * invA, vA.y + imp.y * invA, vA.z + imp.z * invA);
+        v3 cA = vcross(rA, imp);
+        wA = vadd(wA, mmulv(IA, cA));
+        vB = V(vB.x - imp.x * invB, vB.y - imp.y * invB, vB.z - imp.z * invB);
+        v3 cB = vcross(rB, imp);
+        wB = vsub(wB, mmulv(IB, cB));
+    }
+    if (c->dynA) { w->lv[A] = vA; w->av[A] = wA; }
+    if (c->dynB) { w->lv[B] = vB; w->av[B] = wB; }
+    p->ni = nacc;
+    p->ti1 = t1acc;
+    p->ti2 = t2acc;
+}
+
+/* SolveBiasConstraint, ContactSolver.cpp:257-290 */
+static void solve_bias(kzo_world* w, con_t* c) {
+    int A = c->a, B = c->b;
+    if (w->inv_mass[A] <= 0.0f && w->inv_mass[B] <= 0.0f) return;
+    for (uint32_t i = 0; i < c->npts; ++i) {
+        cpc_t* p = &c->p[i];
+        if (p->pbias <= 0.0f) continue;
+        v3 rA = qrotate(w->rot[A], p->laA);
+        v3 rB = qrotate(w->rot[B], p->laB);
+        v3 vr = vsub(vadd(w->plv[A], vcross(w->pav[A], rA)), vadd(w->plv[B], vcross(w->pav[B], rB)));
+        float lambda = -p->nm * (vdot(vr, p->n) - p->pbias);
+        float ni = fmax_r(p->bimp + lambda, 0.0f);
+        lambda = ni - p->bimp;
+        p->bimp = ni;
+        v3 imp = vmul(p->n, lambda);
+        if (c->dynA) {
+            w->plv[A] = vadd(w->plv[A], vmul(imp, w->inv_mass[A]));
+            w->pav[A] = vadd(w->pav[A], mmulv(&w->iiw[A], vcross(rA, imp)));
+        }
+        if (c->dynB) {
+            w->plv[B] = vsub(w->plv[B], vmul(imp, w->inv_mass[B]));
+            w->pav[B] = vsub(w->pav[B], mmulv(&w->iiw[B], vcross(rB, imp)));
+        }
+    }
+}
+
+/* SolveIsland, PhysicsWorld.cpp:666-743 (SIMD path, no joints). */
+static void solve_island(kzo_world* w, uint32_t isl, uint32_t* out_batches, uint32_t* out_vl, uint32_t* out_bl,
+                         uint32_t* out_pts) {
+    const uint32_t* list = w->isl_con + w->isl_off[isl];
+    uint32_t nc = w->isl_off[isl + 1] - w->isl_off[isl];
+    if (nc == 0) return;
+    for (uint32_t i = 0; i < nc; ++i) warm_start(w, &w->cons[list[i]]);
+
+    uint32_t npts = 0;
+    for (uint32_t i = 0; i < nc; ++i) npts += w->cons[list[i]].npts;
+    batch_t* bt = (batch_t*)xrealloc(NULL, sizeof(batch_t) * (npts ? npts : 1));
+    uint32_t nbt = 0;
+    for (uint32_t i = 0; i < nc; ++i) {
+        con_t* c = &w->cons[list[i]];
+        if (c->sensor) continue;
+        for (uint32_t p = 0; p < c->npts; ++p) {
+            int placed = 0;
+            for (uint32_t bi = 0; bi < nbt && !placed; ++bi) {
+                batch_t* b = &bt[bi];
+                if (b->count >= 4) continue;
+                int conflict = 0;
+                for (uint32_t k = 0; k < b->count; ++k)
+                    if (b->a[k] == c->a || b->a[k] == c->b || b->b[k] == c->a || b->b[k] == c->b) { conflict = 1; break; }
+                if (conflict) continue;
+                b->ref[b->count].con = (int)list[i];
+                b->ref[b->count].pt = p;
+                b->a[b->count] = c->a;
+                b->b[b->count] = c->b;
+                ++b->count;
+                placed = 1;
+            }
+            if (!placed) {
+                batch_t* b = &bt[nbt++];
+                b->count = 1;
+                b->ref[0].con = (int)list[i];
+                b->ref[0].pt = p;
+                b->a[0] = c->a;
+                b->b[0] = c->b;
+            }
+        }
+    }
+    for (uint32_t it = 0; it < w->vel_iters; ++it)
+        for (uint32_t bi = 0; bi < nbt; ++bi)
+            for (uint32_t k = 0; k < bt[bi].count; ++k) {
+                con_t* c = &w->cons[bt[bi].ref[k].con];
+                solve_lane(w, c, &c->p[bt[bi].ref[k].pt]);
+            }
+    if (!w->vel_bias)
+        for (uint32_t it = 0; it < w->pos_iters; ++it)
+            for (uint32_t i = 0; i < nc; ++i) solve_bias(w, &w->cons[list[i]]);
+
+    if (w->sched_stats) {
+        /* Dependency levels of the two Gauss-Seidel sweeps, counting only dynamic bodies. */
+        uint32_t* last = (uint32_t*)calloc((size_t)w->nb, sizeof(uint32_t));
+        uint32_t vl = 0;
+        for (uint32_t bi = 0; bi < nbt; ++bi)
+            for (uint32_t k = 0; k < bt[bi].count; ++k) {
+                con_t* c = &w->cons[bt[bi].ref[k].con];
+                uint32_t l = 0;
+                if (c->dynA && last[c->a] > l) l = last[c->a];
+                if (c->dynB && last[c->b] > l) l = last[c->b];
+                ++l;
+                if (c->dynA) last[c->a] = l;
+                if (c->dynB) last[c->b] = l;
+                if (l > vl) vl = l;
+            }
+        memset(last, 0, sizeof(uint32_t) * (size_t)w->nb);
+        uint32_t bl = 0;
+        for (uint32_t i = 0; i < nc; ++i) {
+            con_t* c = &w->cons[list[i]];
+            if (w->inv_mass[c->a] <= 0.0f && w->inv_mass[c->b] <= 0.0f) continue;
+            for (uint32_t p = 0; p < c->npts; ++p) {
+                if (c->p[p].pbias <= 0.0f) continue;
+                uint32_t l = 0;
+                if (c->dynA && last[c->a] > l) l = last[c->a];
+                if (c->dynB && last[c->b] > l) l = last[c->b];
+                ++l;
+                if (c->dynA) last[c->a] = l;
+                if (c->dynB) last[c->b] = l;
+                if (l > bl) bl = l;
+            }
+        }
+        free(last);
+        *out_vl = vl;
+        *out_bl = bl;
+    }
+    *out_batches = nbt;
+    *out_pts = npts;
+    free(bt);
+}
+
+/* ----------------------------------------------------------------------------- */
+/* Step                                                                           */
+/* ----------------------------------------------------------------------------- */
+static uint32_t uf_find(uint32_t* par, uint32_t x) {
+    while (par[x] != x) { par[x] = par[par[x]]; x = par[x]; }
+    return x;
+}
+static void uf_union(uint32_t* par, uint32_t* rank, uint32_t a, uint32_t b) {
+    a = uf_find(par, a);
+    b = uf_find(par, b);
+    if (a == b) return;
+    if (rank[a] < rank[b]) { uint32_t t = a; a = b; b = t; }
+    par[b] = a;
+    if (rank[a] == rank[b]) ++rank[a];
+}
+
+static void build_islands(kzo_world* w) {
+    uint32_t numDyn = 0;
+    for (int i = 0; i < w->nactive; ++i) {
+        int b = w->active[i];
+        w->island_index[b] = w->motion[b] == KZO_DYNAMIC ? (int)numDyn++ : -1;
+    }
+    w->nislands = 0;
+    if (numDyn == 0) return;
+    uint32_t* par = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * numDyn);
+    uint32_t* rank = (uint32_t*)calloc(numDyn, sizeof(uint32_t));
+    for (uint32_t i = 0; i < numDyn; ++i) par[i] = i;
+    for (uint32_t ci = 0; ci < w->ncons; ++ci) {
+        con_t* c = &w->cons[ci];
+        if (w->motion[c->a] != KZO_DYNAMIC || w->motion[c->b] != KZO_DYNAMIC) continue;
+        int ia = w->island_index[c->a], ib = w->island_index[c->b];
+        if (ia >= 0 && ib >= 0) uf_union(par, rank, (uint32_t)ia, (uint32_t)ib);
+    }
+    uint32_t* r2i = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * numDyn);
+    for (uint32_t i = 0; i < numDyn; ++i) r2i[i] = NUL;
+    uint32_t ni = 0;
+    for (uint32_t i = 0; i < numDyn; ++i) {
+        uint32_t r = uf_find(par, i);
+        if (r2i[r] == NUL) r2i[r] = ni++;
+    }
+    w->nislands = ni;
+    uint32_t* isl = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * (w->ncons ? w->ncons : 1));
+    w->isl_off = (uint32_t*)xrealloc(w->isl_off, sizeof(uint32_t) * (ni + 1));
+    memset(w->isl_off, 0, sizeof(uint32_t) * (ni + 1));
+    for (uint32_t ci = 0; ci < w->ncons; ++ci) {
+        con_t* c = &w->cons[ci];
+        uint32_t is = NUL;
+        if (w->motion[c->a] == KZO_DYNAMIC && w->island_index[c->a] >= 0) is = r2i[uf_find(par, (uint32_t)w->island_index[c->a])];
+        if (is == NUL && w->motion[c->b] == KZO_DYNAMIC && w->island_index[c->b] >= 0)
+            is = r2i[uf_find(par, (uint32_t)w->island_index[c->b])];
+        isl[ci] = is;
+        if (is != NUL) w->isl_off[is + 1]++;
+    }
+    for (uint32_t i = 0; i < ni; ++i) w->isl_off[i + 1] += w->isl_off[i];
+    w->isl_con = (uint32_t*)xrealloc(w->isl_con, sizeof(uint32_t) * (w->ncons ? w->ncons : 1));
+    uint32_t* fill = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * (ni ? ni : 1));
+    for (uint32_t i = 0; i < ni; ++i) fill[i] = w->isl_off[i];
+    for (uint32_t ci = 0; ci < w->ncons; ++ci)
+        if (isl[ci] != NUL) w->isl_con[fill[isl[ci]]++] = ci;
+    free(fill);
+    free(isl);
+    free(r2i);
+    free(rank);
+    free(par);
+}
+
+static void collide_one(kzo_world* w, uint32_t i) {
+    uint32_t ida = w->pairs[2 * i], idb = w->pairs[2 * i + 1];
+    int A = body_of(w, ida), B = body_of(w, idb);
+    w->man[i].n = 0;
+    w->keys[i] = 0;
+    if (A < 0 || B < 0) return;
+    if (w->motion[A] != KZO_DYNAMIC && w->motion[B] != KZO_DYNAMIC) return;
+    int swapped = ida > idb;
+    int first = swapped ? B : A, second = swapped ? A : B;
+    w->keys[i] = pair_key(ida, idb);
+    kzo_collide(&w->shapes[w->shape[first]], w->rot[first], w->pos[first], &w->shapes[w->shape[second]],
+                w->rot[second], w->pos[second], 0.02f, 1.0e-4f, &w->man[i]);
+    if (swapped) {
+        kzo_manifold* m = &w->man[i];
+        for (uint32_t k = 0; k < m->n; ++k) {
+            v3 t = m->pts[k].pA;
+            m->pts[k].pA = m->pts[k].pB;
+            m->pts[k].pB = t;
+            m->pts[k].n = vneg(m->pts[k].n);
+        }
+    }
+}
+
+static void build_constraints(kzo_world* w) {
+    w->ncons = 0;
+    for (uint32_t i = 0; i < w->npairs; ++i) {
+        kzo_manifold* m = &w->man[i];
+        if (m->n == 0) continue;
+        uint64_t key = w->keys[i];
+        if (key == 0) continue;
+        int A = body_of(w, w->pairs[2 * i]), B = body_of(w, w->pairs[2 * i + 1]);
+        if (A < 0 || B < 0) continue;
+        if (w->packed[A] > w->packed[B]) { int t = A; A = B; B = t; }
+        cache_t* cached = w->no_ws ? NULL : find_cached(w, key);
+        if (w->ncons == w->cons_cap) {
+            w->cons_cap = w->cons_cap ? w->cons_cap * 2 : 1024;
+            w->cons = (con_t*)xrealloc(w->cons, sizeof(con_t) * w->cons_cap);
+        }
+        con_t* c = &w->cons[w->ncons++];
+        memset(c, 0, sizeof *c);
+        c->a = A;
+        c->b = B;
+        c->sensor = w->sensor[A] || w->sensor[B];
+        c->friction = sqrtf(w->fric[A] * w->fric[B]);
+        c->restitution = fmax_r(w->rest[A], w->rest[B]);
+        c->npts = m->n;
+        for (uint32_t p = 0; p < m->n; ++p) {
+            cpc_t* q = &c->p[p];
+            const kzo_cpoint* s = &m->pts[p];
+            q->pA = s->pA; q->pB = s->pB; q->n = s->n; q->sep = s->sep; q->feature = s->feature;
+            q->fric = c->friction;
+            q->rest = c->restitution;
+            q->ni = q->ti1 = q->ti2 = 0;
+            if (cached) {
+                float best = 0.10f * 0.10f;
+                uint32_t bi = NUL;
+                for (uint32_t k = 0; k < cached->npts; ++k) {
+                    float d = vlen2(vsub(cached->pos[k], s->pA));
+                    if (d < best) { best = d; bi = k; }
+                }
+                if (bi != NUL) { q->ni = cached->ni[bi]; q->ti1 = cached->ti1[bi]; q->ti2 = cached->ti2[bi]; }
+            }
+        }
+    }
+}
+
+static void integrate_velocities(kzo_world* w, float dt) {
+    for (int k = 0; k < w->nactive; ++k) {
+        int i = w->active[k];
+        if (w->motion[i] != KZO_DYNAMIC) continue;
+        v3 acc = vadd(vmul(w->gravity, w->grav[i]), vmul(w->force[i], w->inv_mass[i]));
+        w->lv[i] = vadd(w->lv[i], vmul(acc, dt));
+        w->av[i] = vadd(w->av[i], vmul(mmulv(&w->iiw[i], w->torque[i]), dt));
+        w->lv[i] = vmul(w->lv[i], 1.0f / (1.0f + w->lin_damp[i] * dt));
+        w->av[i] = vmul(w->av[i], 1.0f / (1.0f + w->ang_damp[i] * dt));
+        w->lv[i] = vclamp_len(w->lv[i], w->max_lin[i]);
+        w->av[i] = vclamp_len(w->av[i], w->max_ang[i]);
+        if (!visfinite(w->lv[i]) || !visfinite(w->av[i])) { w->lv[i] = V(0, 0, 0); w->av[i] = V(0, 0, 0); }
+    }
+}
+
+static void update_world_inertia(kzo_world* w, int i) {
+    m3 r = qtomat(w->rot[i]);
+    m3 ri = mmul(&r, &w->iil[i]);
+    m3 rt = mtranspose(&r);
+    w->iiw[i] = mmul(&ri, &rt);
+}
+
+int kzo_step(kzo_world* w, float dt) {
+    ++w->frame;
+    if (w->frame == 0) w->frame = 1;
+
+    /* 1. broad phase */
+    if (w->pair_mode == KZO_PAIRS_TREE) {
+        for (int k = 0; k < w->nactive; ++k) {
+            int i = w->active[k];
+            if (w->motion[i] == KZO_STATIC) continue;
+            aabb b = kzo_world_bounds(&w->shapes[w->shape[i]], w->rot[i], w->pos[i]);
+            move_proxy(w, w->proxy[i], b, vmul(w->lv[i], w->fixed_dt));
+        }
+        tree_pairs(w);
+    } else if (w->pair_mode == KZO_PAIRS_CANONICAL) {
+        canonical_pairs(w);
+    } else {
+        w->npairs = 0;
+        for (uint32_t i = 0; i < w->next_pairs; ++i) push_pair(w, w->ext_pairs[2 * i], w->ext_pairs[2 * i + 1]);
+    }
+
+    /* 2. narrow phase */
+    if (w->npairs > w->man_cap) {
+        w->man_cap = w->npairs;
+        w->man = (kzo_manifold*)xrealloc(w->man, sizeof(kzo_manifold) * w->man_cap);
+        w->keys = (uint64_t*)xrealloc(w->keys, sizeof(uint64_t) * w->man_cap);
+    }
+    int np = (int)w->npairs;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 32) num_threads(w->threads) if (w->threads > 1 && np > 64)
+#endif
+    for (int i = 0; i < np; ++i) collide_one(w, (uint32_t)i);
+
+    /* 3. constraints with warm start */
+    build_constraints(w);
+    /* 4. velocities */
+    integrate_velocities(w, dt);
+    /* 5. solve */
+    for (uint32_t ci = 0; ci < w->ncons; ++ci) prepare(w, &w->cons[ci], dt);
+    build_islands(w);
+    w->st_batches = w->st_max_vl = w->st_max_bl = w->st_max_isl_pts = w->st_sum_vl = 0;
+    int ni = (int)w->nislands;
+    uint32_t* ib = (uint32_t*)calloc((size_t)(ni ? ni : 1) * 4, sizeof(uint32_t));
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) num_threads(w->threads) if (w->threads > 1 && ni > 1)
+#endif
+    for (int i = 0; i < ni; ++i) solve_island(w, (uint32_t)i, &ib[4 * i], &ib[4 * i + 1], &ib[4 * i + 2], &ib[4 * i + 3]);
+    for (int i = 0; i < ni; ++i) {
+        w->st_batches += ib[4 * i];
+        if (ib[4 * i + 1] > w->st_max_vl) w->st_max_vl = ib[4 * i + 1];
+        if (ib[4 * i + 2] > w->st_max_bl) w->st_max_bl = ib[4 * i + 2];
+        if (ib[4 * i + 3] > w->st_max_isl_pts) w->st_max_isl_pts = ib[4 * i + 3];
+        w->st_sum_vl += ib[4 * i + 1];
+    }
+    free(ib);
+    for (uint32_t ci = 0; ci < w->ncons; ++ci) {
+        con_t* c = &w->cons[ci];
+        cache_t* e = get_or_create_cached(w, pair_key(w->packed[c->a], w->packed[c->b]));
+        e->npts = c->npts;
+        for (uint32_t p = 0; p < c->npts; ++p) {
+            e->pos[p] = c->p[p].pA;
+            e->ni[p] = c->p[p].ni;
+            e->ti1[p] = c->p[p].ti1;
+            e->ti2[p] = c->p[p].ti2;
+        }
+    }
+    /* 6. positions, split-impulse pseudo velocities, inertia */
+    for (int k = 0; k < w->nactive; ++k) {
+        int i = w->active[k];
+        if (w->motion[i] == KZO_STATIC) continue;
+        w->pos[i] = vadd(w->pos[i], vmul(w->lv[i], dt));
+        if (vlen2(w->av[i]) > 0.0f) w->rot[i] = q_integrate(w->rot[i], w->av[i], dt);
+    }
+    if (!w->vel_bias) {
+        for (int k = 0; k < w->nactive; ++k) {
+            int i = w->active[k];
+            if (w->motion[i] == KZO_STATIC) continue;
+            if (vlen2(w->plv[i]) > 0.0f) w->pos[i] = vadd(w->pos[i], vmul(w->plv[i], dt));
+            if (vlen2(w->pav[i]) > 0.0f) w->rot[i] = q_integrate(w->rot[i], w->pav[i], dt);
+            w->plv[i] = V(0, 0, 0);
+            w->pav[i] = V(0, 0, 0);
+        }
+    }
+    for (int k = 0; k < w->nactive; ++k) {
+        int i = w->active[k];
+        if (w->motion[i] == KZO_DYNAMIC) update_world_inertia(w, i);
+    }
+    /* 9. clear forces */
+    for (int i = 0; i < w->nb; ++i) { w->force[i] = V(0, 0, 0); w->torque[i] = V(0, 0, 0); }
+    uint32_t pts = 0;
+    for (uint32_t ci = 0; ci < w->ncons; ++ci) pts += w->cons[ci].npts;
+    w->st_points = pts;
+    return 0;
+}
+
+/* ----------------------------------------------------------------------------- */
+/* Creation / API                                                                 */
+/* ----------------------------------------------------------------------------- */
+typedef struct { const uint8_t* p; size_t n, off; int bad; } rd_t;
+static void rd(rd_t* r, void* dst, size_t k) {
+    if (r->off + k > r->n) { r->bad = 1; memset(dst, 0, k); return; }
+    memcpy(dst, r->p + r->off, k);
+    r->off += k;
+}
+static uint32_t rd_u32(rd_t* r) { uint32_t v; rd(r, &v, 4); return v; }
+static float rd_f32(rd_t* r) { float v; rd(r, &v, 4); return v; }
+
+kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* resolved, size_t resolved_len) {
+    rd_t r = {scene, scene_len, 0, 0};
+    if (rd_u32(&r) != 0x43535A4Bu || rd_u32(&r) != 1u) { set_err("bad scene header"); return NULL; }
+    kzo_world* w = (kzo_world*)calloc(1, sizeof(kzo_world));
+    w->gravity.x = rd_f32(&r); w->gravity.y = rd_f32(&r); w->gravity.z = rd_f32(&r);
+    (void)rd_f32(&r); /* scene dt: the caller passes dt to kzo_step */
+    w->vel_iters = rd_u32(&r);
+    w->pos_iters = rd_u32(&r);
+    uint32_t wflags = rd_u32(&r);
+    w->baumgarte = rd_f32(&r);
+    w->slop = rd_f32(&r);
+    w->rest_thresh = rd_f32(&r);
+    w->max_bias = rd_f32(&r);
+    w->ws_factor = rd_f32(&r);
+    if (wflags & 1u) { set_err("sleeping is not supported by the oracle"); free(w); return NULL; }
+    w->vel_bias = (wflags & 2u) != 0;
+    w->no_ws = (wflags & 4u) != 0;
+    w->fixed_dt = (float)(1.0 / 60.0); /* WorldSettings::fixedTimestep, PhysicsWorld.h:32 */
+    w->threads = 1;
+    w->root = NUL;
+    w->free_list = NUL;
+
+    rd_t rr = {resolved, resolved_len, 0, 0};
+    w->nshapes = (int)rd_u32(&r);
+    w->shapes = (kzo_shape*)calloc((size_t)w->nshapes, sizeof(kzo_shape));
+    for (int i = 0; i < w->nshapes; ++i) {
+        kzo_shape* s = &w->shapes[i];
+        s->type = (int)rd_u32(&r);
+        for (int k = 0; k < 4; ++k) s->p[k] = rd_f32(&r);
+        uint32_t npts = rd_u32(&r);
+        r.off += 12u * npts; /* hull input cloud: the resolved blob carries the built hull */
+        switch (s->type) {
+            case KZO_SPHERE: { v3 e = V(s->p[0], s->p[0], s->p[0]); s->local = AB(vneg(e), e); break; }
+            case KZO_BOX: { v3 e = V(s->p[0], s->p[1], s->p[2]); s->local = AB(vneg(e), e); break; }
+            case KZO_CAPSULE: { v3 e = V(s->p[1], s->p[0] + s->p[1], s->p[1]); s->local = AB(vneg(e), e); break; }
+            case KZO_PLANE: {
+                const float big = 1.0e6f;
+                v3 n = V(s->p[0], s->p[1], s->p[2]);
+                v3 ext = vsub(V(big, big, big), vmul(vabs(n), big));
+                v3 c = vmul(n, s->p[3]);
+                s->local = AB(vsub(c, ext), vadd(c, ext));
+                break;
+            }
+            case KZO_HULL: {
+                s->nverts = (int)rd_u32(&rr);
+                s->verts = (v3*)calloc((size_t)s->nverts, sizeof(v3));
+                for (int k = 0; k < s->nverts; ++k) { s->verts[k].x = rd_f32(&rr); s->verts[k].y = rd_f32(&rr); s->verts[k].z = rd_f32(&rr); }
+                s->nfaces = (int)rd_u32(&rr);
+                s->sizes = (uint8_t*)calloc((size_t)s->nfaces + 4, 1);
+                rd(&rr, s->sizes, (size_t)s->nfaces);
+                rr.off = (rr.off + 3u) & ~(size_t)3u;
+                s->nidx = (int)rd_u32(&rr);
+                s->idx = (uint32_t*)calloc((size_t)s->nidx, sizeof(uint32_t));
+                rd(&rr, s->idx, 4u * (size_t)s->nidx);
+                aabb b = aabb_empty();
+                for (int k = 0; k < s->nverts; ++k) { b.mn = vmin(b.mn, s->verts[k]); b.mx = vmax(b.mx, s->verts[k]); }
+                s->local = b;
+                break;
+            }
+            default: set_err("unsupported shape type"); kzo_destroy(w); return NULL;
+        }
+    }
+    int nb = (int)rd_u32(&r);
+    w->nb = nb;
+#define ALLOC(f, T) w->f = (T*)calloc((size_t)(nb ? nb : 1), sizeof(T))
+    ALLOC(packed, uint32_t); ALLOC(layer, uint32_t); ALLOC(mask, uint32_t); ALLOC(proxy, uint32_t);
+    ALLOC(shape, int); ALLOC(motion, uint8_t); ALLOC(sensor, uint8_t);
+    ALLOC(pos, v3); ALLOC(lv, v3); ALLOC(av, v3); ALLOC(plv, v3); ALLOC(pav, v3); ALLOC(force, v3); ALLOC(torque, v3);
+    ALLOC(rot, qt);
+    ALLOC(inv_mass, float); ALLOC(lin_damp, float); ALLOC(ang_damp, float); ALLOC(grav, float);
+    ALLOC(max_lin, float); ALLOC(max_ang, float); ALLOC(fric, float); ALLOC(rest, float);
+    ALLOC(iil, m3); ALLOC(iiw, m3); ALLOC(active, int); ALLOC(island_index, int);
+#undef ALLOC
+    for (int i = 0; i < nb; ++i) {
+        w->shape[i] = (int)rd_u32(&r);
+        w->motion[i] = (uint8_t)rd_u32(&r);
+        w->pos[i].x = rd_f32(&r); w->pos[i].y = rd_f32(&r); w->pos[i].z = rd_f32(&r);
+        w->rot[i].x = rd_f32(&r); w->rot[i].y = rd_f32(&r); w->rot[i].z = rd_f32(&r); w->rot[i].w = rd_f32(&r);
+        w->lv[i].x = rd_f32(&r); w->lv[i].y = rd_f32(&r); w->lv[i].z = rd_f32(&r);
+        w->av[i].x = rd_f32(&r); w->av[i].y = rd_f32(&r); w->av[i].z = rd_f32(&r);
+        w->fric[i] = rd_f32(&r); w->rest[i] = rd_f32(&r);
+        w->lin_damp[i] = rd_f32(&r); w->ang_damp[i] = rd_f32(&r); w->grav[i] = rd_f32(&r);
+        w->max_lin[i] = rd_f32(&r); w->max_ang[i] = rd_f32(&r);
+        (void)rd_f32(&r); (void)rd_f32(&r); /* density, mass override: resolved mass comes in the blob */
+        w->layer[i] = rd_u32(&r); w->mask[i] = rd_u32(&r);
+        uint32_t fl = rd_u32(&r);
+        w->sensor[i] = (fl & 1u) != 0;
+        w->packed[i] = (uint32_t)i; /* BodyID(index, sequence 0).Packed() */
+        w->active[i] = i;
+        w->inv_mass[i] = rd_f32(&rr);
+        for (int c = 0; c < 3; ++c) { w->iil[i].c[c].x = rd_f32(&rr); w->iil[i].c[c].y = rd_f32(&rr); w->iil[i].c[c].z = rd_f32(&rr); }
+        if (w->shape[i] < 0 || w->shape[i] >= w->nshapes) { set_err("bad shape index"); kzo_destroy(w); return NULL; }
+    }
+    w->nactive = nb;
+    if (r.bad || rr.bad) { set_err("truncated scene or resolved data"); kzo_destroy(w); return NULL; }
+    for (int i = 0; i < nb; ++i) {
+        if (w->motion[i] == KZO_DYNAMIC && w->inv_mass[i] > 0.0f) update_world_inertia(w, i);
+        aabb b = kzo_world_bounds(&w->shapes[w->shape[i]], w->rot[i], w->pos[i]);
+        w->proxy[i] = create_proxy(w, b, w->packed[i], w->layer[i], w->mask[i]);
+    }
+    w->cache_cap = 1024;
+    w->cache = (cache_t*)calloc(w->cache_cap, sizeof(cache_t));
+    return w;
+}
+
+void kzo_destroy(kzo_world* w) {
+    if (!w) return;
+    for (int i = 0; i < w->nshapes; ++i) { free(w->shapes[i].verts); free(w->shapes[i].sizes); free(w->shapes[i].idx); }
+    free(w->shapes);
+    void* ptrs[] = {w->packed, w->layer, w->mask, w->proxy, w->shape, w->motion, w->sensor, w->pos, w->lv, w->av,
+                    w->plv, w->pav, w->force, w->torque, w->rot, w->inv_mass, w->lin_damp, w->ang_damp, w->grav,
+                    w->max_lin, w->max_ang, w->fric, w->rest, w->iil, w->iiw, w->active, w->island_index,
+                    w->nodes, w->bp_layer, w->bp_mask, w->cache, w->pairs, w->ext_pairs, w->man, w->keys,
+                    w->cons, w->isl_off, w->isl_con};
+    for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; ++i) free(ptrs[i]);
+    free(w);
+}
+
+void kzo_set_threads(kzo_world* w, int t) { w->threads = t > 0 ? t : 1; }
+void kzo_set_pair_mode(kzo_world* w, int m) { w->pair_mode = m; }
+void kzo_set_schedule_stats(kzo_world* w, int e) { w->sched_stats = e; }
+int kzo_set_external_pairs(kzo_world* w, const uint32_t* p, uint32_t n) {
+    w->ext_pairs = (uint32_t*)xrealloc(w->ext_pairs, sizeof(uint32_t) * 2 * (n ? n : 1));
+    memcpy(w->ext_pairs, p, sizeof(uint32_t) * 2 * n);
+    w->next_pairs = n;
+    return 0;
+}
+uint32_t kzo_num_bodies(const kzo_world* w) { return (uint32_t)w->nb; }
+
+void kzo_get_state(const kzo_world* w, float* o) {
+    for (int i = 0; i < w->nb; ++i) {
+        float* q = o + KZO_STATE_FLOATS * i;
+        q[0] = w->pos[i].x; q[1] = w->pos[i].y; q[2] = w->pos[i].z;
+        q[3] = w->rot[i].x; q[4] = w->rot[i].y; q[5] = w->rot[i].z; q[6] = w->rot[i].w;
+        q[7] = w->lv[i].x; q[8] = w->lv[i].y; q[9] = w->lv[i].z;
+        q[10] = w->av[i].x; q[11] = w->av[i].y; q[12] = w->av[i].z;
+    }
+}
+void kzo_set_state(kzo_world* w, const float* in) {
+    for (int i = 0; i < w->nb; ++i) {
+        const float* q = in + KZO_STATE_FLOATS * i;
+        w->pos[i] = V(q[0], q[1], q[2]);
+        w->rot[i] = Q(q[3], q[4], q[5], q[6]);
+        w->lv[i] = V(q[7], q[8], q[9]);
+        w->av[i] = V(q[10], q[11], q[12]);
+        if (w->motion[i] == KZO_DYNAMIC) update_world_inertia(w, i);
+    }
+}
+
+uint64_t kzo_hash(const kzo_world* w) {
+    uint64_t h = 1469598103934665603ull;
+#define MIX(v) do { h ^= (uint64_t)(v); h *= 1099511628211ull; } while (0)
+#define QZ(f) ((uint64_t)(int64_t)((f) * 100000.0f))
+    for (int i = 0; i < w->nb; ++i) {
+        MIX(w->packed[i]);
+        MIX(QZ(w->pos[i].x)); MIX(QZ(w->pos[i].y)); MIX(QZ(w->pos[i].z));
+        MIX(QZ(w->rot[i].x)); MIX(QZ(w->rot[i].y)); MIX(QZ(w->rot[i].z)); MIX(QZ(w->rot[i].w));
+        MIX(QZ(w->lv[i].x)); MIX(QZ(w->lv[i].y)); MIX(QZ(w->lv[i].z));
+        MIX(QZ(w->av[i].x)); MIX(QZ(w->av[i].y)); MIX(QZ(w->av[i].z));
+    }
+#undef MIX
+#undef QZ
+    return h;
+}
+
+uint32_t kzo_num_pairs(const kzo_world* w) { return w->npairs; }
+void kzo_get_pairs(const kzo_world* w, uint32_t* out) { memcpy(out, w->pairs, sizeof(uint32_t) * 2 * w->npairs); }
+uint32_t kzo_num_constraints(const kzo_world* w) { return w->ncons; }
+
+static void put3(float* o, v3 v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; }
+void kzo_get_constraints(const kzo_world* w, uint32_t* hdr, float* pts, float* fr) {
+    for (uint32_t ci = 0; ci < w->ncons; ++ci) {
+        const con_t* c = &w->cons[ci];
+        hdr[3 * ci] = w->packed[c->a];
+        hdr[3 * ci + 1] = w->packed[c->b];
+        hdr[3 * ci + 2] = c->npts;
+        if (fr) { fr[2 * ci] = c->friction; fr[2 * ci + 1] = c->restitution; }
+        for (uint32_t p = 0; p < KZO_MAX_MANIFOLD; ++p) {
+            float* o = pts + ((size_t)ci * KZO_MAX_MANIFOLD + p) * KZO_PT_FLOATS;
+            if (p >= c->npts) { memset(o, 0, sizeof(float) * KZO_PT_FLOATS); continue; }
+            const cpc_t* q = &c->p[p];
+            put3(o, q->pA); put3(o + 3, q->pB); put3(o + 6, q->n); o[9] = q->sep;
+            memcpy(&o[10], &q->feature, 4);
+            put3(o + 11, q->rA); put3(o + 14, q->rB); put3(o + 17, q->laA); put3(o + 20, q->laB);
+            put3(o + 23, q->t1); put3(o + 26, q->t2);
+            o[29] = q->nm; o[30] = q->tm1; o[31] = q->tm2;
+            o[32] = q->ni; o[33] = q->ti1; o[34] = q->ti2;
+            o[35] = q->rbias; o[36] = q->pbias; o[37] = q->bimp; o[38] = q->nvel;
+        }
+    }
+}
+
+void kzo_get_stats(const kzo_world* w, uint32_t* o) {
+    o[0] = w->npairs; o[1] = w->ncons; o[2] = w->st_points; o[3] = w->nislands;
+    o[4] = w->st_batches; o[5] = w->st_max_vl; o[6] = w->st_max_bl; o[7] = w->st_max_isl_pts; o[8] = w->st_sum_vl;
+}
+
+void kzo_get_mass(const kzo_world* w, float* im, float* iw) {
+    for (int i = 0; i < w->nb; ++i) {
+        im[i] = w->inv_mass[i];
+        for (int c = 0; c < 3; ++c) { iw[9 * i + 3 * c] = w->iiw[i].c[c].x; iw[9 * i + 3 * c + 1] = w->iiw[i].c[c].y; iw[9 * i + 3 * c + 2] = w->iiw[i].c[c].z; }
+    }
+}
+
+uint32_t kzo_collide_bodies(const kzo_world* w, uint32_t a, uint32_t b, float max_sep, float* out) {
+    kzo_manifold m;
+    uint32_t n = kzo_collide(&w->shapes[w->shape[a]], w->rot[a], w->pos[a], &w->shapes[w->shape[b]], w->rot[b],
+                             w->pos[b], max_sep, 1.0e-4f, &m);
+    for (uint32_t i = 0; i < m.n; ++i) {
+        float* o = out + 11 * i;
+        put3(o, m.pts[i].pA); put3(o + 3, m.pts[i].pB); put3(o + 6, m.pts[i].n); o[9] = m.pts[i].sep;
+        memcpy(&o[10], &m.pts[i].feature, 4);
+    }
+    (void)n;
+    return m.n;
+}

@@ -1,0 +1,247 @@
+// Trace exporter for the reference engine (test infrastructure, never shipped).
+//
+// Drives the UNMODIFIED reference through its public API only:
+//   PhysicsWorld::CreateBody / StepFixed / GetBody / GetBroadPhase().GetPairs() /
+//   GetContactConstraints() / ComputeStateHash()   (include/Kizuri/World/PhysicsWorld.h:82-239)
+// and writes a binary trace that the oracle and the GPU parity tests are pinned to.
+//
+// Built only by oracle/Makefile.ref, from the reference's own sources, into oracle/_ref/.
+//
+// usage: ref_trace <scene.kzsc> <out.kztr> <steps> [detail_steps] [--st]
+//   detail_steps : number of leading steps that also dump pairs and contact constraints
+//   --st         : WorldSettings::useMultithreading = false
+#include "Kizuri/Kizuri.h"
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cstdint>
+#include <chrono>
+#include <vector>
+
+using namespace kizuri;
+
+namespace {
+
+struct Reader {
+    std::vector<uint8_t> buf;
+    size_t off = 0;
+    template <typename T> T get() {
+        T v;
+        std::memcpy(&v, buf.data() + off, sizeof(T));
+        off += sizeof(T);
+        return v;
+    }
+};
+
+struct Writer {
+    FILE* f;
+    template <typename T> void put(const T& v) { std::fwrite(&v, sizeof(T), 1, f); }
+    void putv(const Vec3& v) { put(v.x); put(v.y); put(v.z); }
+};
+
+struct SceneShape {
+    uint32_t type;
+    float p[4];
+    std::vector<Vec3> pts;
+};
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 4) {
+        std::fprintf(stderr, "usage: %s scene out steps [detail_steps] [--st]\n", argv[0]);
+        return 2;
+    }
+    const char* scenePath = argv[1];
+    const char* outPath = argv[2];
+    int steps = std::atoi(argv[3]);
+    int detail = argc > 4 ? std::atoi(argv[4]) : 0;
+    bool singleThread = false;
+    for (int i = 1; i < argc; ++i)
+        if (std::strcmp(argv[i], "--st") == 0) singleThread = true;
+
+    Reader rd;
+    {
+        FILE* f = std::fopen(scenePath, "rb");
+        if (!f) { std::perror("scene"); return 1; }
+        std::fseek(f, 0, SEEK_END);
+        long n = std::ftell(f);
+        std::fseek(f, 0, SEEK_SET);
+        rd.buf.resize(size_t(n));
+        if (std::fread(rd.buf.data(), 1, size_t(n), f) != size_t(n)) return 1;
+        std::fclose(f);
+    }
+    if (rd.get<uint32_t>() != 0x43535A4Bu || rd.get<uint32_t>() != 1u) {
+        std::fprintf(stderr, "bad scene\n");
+        return 1;
+    }
+
+    PhysicsWorld world;
+    WorldSettings& ws = world.GetSettings();
+    ws.gravity.x = rd.get<float>(); ws.gravity.y = rd.get<float>(); ws.gravity.z = rd.get<float>();
+    float dt = rd.get<float>();
+    ws.solver.velocityIterations = rd.get<uint32_t>();
+    ws.solver.positionIterations = rd.get<uint32_t>();
+    uint32_t wflags = rd.get<uint32_t>();
+    ws.solver.baumgarte = rd.get<float>();
+    ws.solver.penetrationSlop = rd.get<float>();
+    ws.solver.restitutionThreshold = rd.get<float>();
+    ws.solver.maxBiasVelocity = rd.get<float>();
+    ws.solver.warmStartFactor = rd.get<float>();
+    ws.allowSleeping = (wflags & 1u) != 0;
+    ws.solver.useVelocityBias = (wflags & 2u) != 0;
+    ws.useMultithreading = !singleThread;
+    if (wflags & 4u) setenv("KZ_NOWS", "1", 1);
+
+    uint32_t ns = rd.get<uint32_t>();
+    std::vector<ShapeRef> shapes(ns);
+    std::vector<SceneShape> sdesc(ns);
+    for (uint32_t i = 0; i < ns; ++i) {
+        SceneShape& s = sdesc[i];
+        s.type = rd.get<uint32_t>();
+        for (float& p : s.p) p = rd.get<float>();
+        uint32_t np = rd.get<uint32_t>();
+        for (uint32_t k = 0; k < np; ++k) {
+            float x = rd.get<float>(), y = rd.get<float>(), z = rd.get<float>();
+            s.pts.push_back(Vec3(x, y, z));
+        }
+        switch (s.type) {
+            case 0: shapes[i] = ShapeRef(new SphereShape(s.p[0])); break;
+            case 1: shapes[i] = ShapeRef(new BoxShape(Vec3(s.p[0], s.p[1], s.p[2]))); break;
+            case 2: shapes[i] = ShapeRef(new CapsuleShape(s.p[0], s.p[1])); break;
+            case 4: {
+                Ref<ConvexHullShape> h = ConvexHullShape::Create(ArrayView<const Vec3>(s.pts.data(), s.pts.size()));
+                if (!h) { std::fprintf(stderr, "hull %u degenerate\n", i); return 1; }
+                shapes[i] = ShapeRef(h.Get());
+                break;
+            }
+            case 8: shapes[i] = ShapeRef(new PlaneShape(Plane(Vec3(s.p[0], s.p[1], s.p[2]), s.p[3]))); break;
+            default: std::fprintf(stderr, "shape type %u unsupported\n", s.type); return 1;
+        }
+    }
+
+    uint32_t nb = rd.get<uint32_t>();
+    std::vector<BodyID> ids(nb);
+    for (uint32_t i = 0; i < nb; ++i) {
+        BodySettings bs;
+        uint32_t shape = rd.get<uint32_t>();
+        uint32_t motion = rd.get<uint32_t>();
+        float v[13];
+        for (float& x : v) x = rd.get<float>();
+        float m[9];
+        for (float& x : m) x = rd.get<float>();
+        uint32_t layer = rd.get<uint32_t>(), mask = rd.get<uint32_t>(), flags = rd.get<uint32_t>();
+        bs.shape = shapes[shape];
+        bs.motionType = MotionType(motion);
+        bs.position = Vec3(v[0], v[1], v[2]);
+        bs.rotation = Quat(v[3], v[4], v[5], v[6]);
+        bs.linearVelocity = Vec3(v[7], v[8], v[9]);
+        bs.angularVelocity = Vec3(v[10], v[11], v[12]);
+        bs.friction = m[0]; bs.restitution = m[1]; bs.linearDamping = m[2]; bs.angularDamping = m[3];
+        bs.gravityFactor = m[4]; bs.maxLinearVelocity = m[5]; bs.maxAngularVelocity = m[6];
+        bs.density = m[7]; bs.massOverride = m[8];
+        bs.objectLayer = layer; bs.collisionMask = mask;
+        bs.isSensor = (flags & 1u) != 0;
+        bs.allowSleeping = (flags & 2u) != 0;
+        ids[i] = world.CreateBody(bs);
+        if (ids[i].IsInvalid()) { std::fprintf(stderr, "body %u invalid\n", i); return 1; }
+    }
+
+    FILE* f = std::fopen(outPath, "wb");
+    if (!f) { std::perror("out"); return 1; }
+    Writer w{f};
+    w.put(uint32_t(0x52545A4Bu));  // 'KZTR'
+    w.put(uint32_t(1));
+    w.put(nb);
+    w.put(uint32_t(steps));
+    w.put(uint32_t(detail));
+
+    // Setup: packed ids and mass properties exactly as the reference computed them.
+    for (uint32_t i = 0; i < nb; ++i) {
+        const Body* b = world.GetBody(ids[i]);
+        const MotionProperties& mp = b->GetMotionProperties();
+        w.put(uint32_t(ids[i].Packed()));
+        w.put(mp.inverseMass);
+        for (int c = 0; c < 3; ++c) w.putv(mp.inverseInertiaLocal.col[c]);
+        for (int c = 0; c < 3; ++c) w.putv(mp.inverseInertiaWorld.col[c]);
+    }
+    // Hulls as built by ConvexHullShape::Create.
+    uint32_t nh = 0;
+    for (uint32_t i = 0; i < ns; ++i) nh += sdesc[i].type == 4 ? 1u : 0u;
+    w.put(nh);
+    for (uint32_t i = 0; i < ns; ++i) {
+        if (sdesc[i].type != 4) continue;
+        const ConvexHullShape* h = static_cast<const ConvexHullShape*>(shapes[i].Get());
+        w.put(i);
+        auto pts = h->GetPoints();
+        auto sizes = h->GetFaceSizes();
+        auto idx = h->GetFaceIndices();
+        w.put(uint32_t(pts.Size()));
+        for (usize k = 0; k < pts.Size(); ++k) w.putv(pts[k]);
+        w.put(uint32_t(sizes.Size()));
+        for (usize k = 0; k < sizes.Size(); ++k) w.put(uint8_t(sizes[k]));
+        w.put(uint32_t(idx.Size()));
+        for (usize k = 0; k < idx.Size(); ++k) w.put(uint32_t(idx[k]));
+        w.put(h->GetVolume());
+    }
+
+    auto dumpState = [&]() {
+        for (uint32_t i = 0; i < nb; ++i) {
+            const Body* b = world.GetBody(ids[i]);
+            w.putv(b->GetPosition());
+            const Quat& q = b->GetRotation();
+            w.put(q.x); w.put(q.y); w.put(q.z); w.put(q.w);
+            w.putv(b->GetLinearVelocity());
+            w.putv(b->GetAngularVelocity());
+        }
+    };
+    dumpState();
+
+    double totalMs = 0;
+    for (int s = 0; s < steps; ++s) {
+        auto t0 = std::chrono::steady_clock::now();
+        world.StepFixed(dt);
+        auto t1 = std::chrono::steady_clock::now();
+        totalMs += std::chrono::duration<double, std::milli>(t1 - t0).count();
+        w.put(uint32_t(s));
+        w.put(uint64_t(world.ComputeStateHash()));
+        const WorldStats& st = world.GetStats();
+        w.put(st.numBroadPhasePairs); w.put(st.numContactConstraints);
+        w.put(st.numContactPoints); w.put(st.numIslands);
+        dumpState();
+        if (s < detail) {
+            auto pairs = world.GetBroadPhase().GetPairs();
+            w.put(uint32_t(pairs.Size()));
+            for (usize k = 0; k < pairs.Size(); ++k) {
+                w.put(uint32_t(world.GetBroadPhase().GetUserData(pairs[k].proxyA)));
+                w.put(uint32_t(world.GetBroadPhase().GetUserData(pairs[k].proxyB)));
+            }
+            auto cons = world.GetContactConstraints();
+            w.put(uint32_t(cons.Size()));
+            for (usize k = 0; k < cons.Size(); ++k) {
+                const ContactConstraint& c = cons[k];
+                w.put(uint32_t(c.bodyA->GetID().Packed()));
+                w.put(uint32_t(c.bodyB->GetID().Packed()));
+                w.put(uint32_t(c.numPoints));
+                w.put(c.friction); w.put(c.restitution);
+                for (u32 p = 0; p < c.numPoints; ++p) {
+                    const ContactPointConstraint& q = c.points[p];
+                    w.putv(q.pointOnA); w.putv(q.pointOnB); w.putv(q.normal);
+                    w.put(q.separation); w.put(uint32_t(q.featureId));
+                    w.putv(q.rA); w.putv(q.rB); w.putv(q.localAnchorA); w.putv(q.localAnchorB);
+                    w.putv(q.tangent1); w.putv(q.tangent2);
+                    w.put(q.normalMass); w.put(q.tangentMass1); w.put(q.tangentMass2);
+                    w.put(q.normalImpulse); w.put(q.tangentImpulse1); w.put(q.tangentImpulse2);
+                    w.put(q.restitutionBias); w.put(q.positionBias); w.put(q.biasImpulse);
+                    w.put(q.normalVelocity);
+                }
+            }
+        }
+    }
+    w.put(totalMs);
+    std::fclose(f);
+    std::fprintf(stderr, "ref_trace: %u bodies, %d steps, %.3f ms/step, hash %016llx\n", nb, steps,
+                 steps ? totalMs / steps : 0.0, (unsigned long long)world.ComputeStateHash());
+    return 0;
+}
