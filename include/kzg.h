@@ -1,0 +1,211 @@
+/* kzg.h - C-ABI of the GB300-native contact pipeline (libkzg.so).
+ *
+ * This is the drop-in boundary for the reference's per-step pipeline behind
+ * PhysicsWorld::Step / StepFixed (reference: include/Kizuri/World/PhysicsWorld.h:82-239,
+ * src/World/PhysicsWorld.cpp:245-329).  The reference has no FFI of its own; every entry point
+ * below replaces one piece of its C++ API, cited beside it, and keeps that piece's argument
+ * meaning.  Plain pointers and sizes only; every call returns a kzg_status and records a
+ * message retrievable with kzg_last_error().  One context = one device-resident world (or a
+ * batch of independent worlds), owned by one host thread, running on one CUDA stream.
+ *
+ * Body state (positions, quaternions, velocities, inverse mass and inertia) and the manifold
+ * cache stay resident in device memory between steps.  There is no CPU fallback: when no
+ * suitable GPU is present, kzg_create fails with KZG_ERR_CUDA.
+ */
+#ifndef KZG_H
+#define KZG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct kzg_ctx kzg_ctx;
+typedef int kzg_status;
+
+#define KZG_OK 0
+#define KZG_ERR_INVALID (-1)     /* bad argument or call order */
+#define KZG_ERR_CUDA (-2)        /* CUDA runtime failure or no usable device */
+#define KZG_ERR_CAPACITY (-3)    /* a device table or buffer is full; raise the kzg_config limit */
+#define KZG_ERR_UNSUPPORTED (-4) /* feature outside the accelerated path (e.g. sleeping) */
+#define KZG_ERR_DEVICE (-5)      /* a kernel raised its error word (see kzg_stats.device_error) */
+
+/* Shape types: numbering of ShapeType (reference include/Kizuri/Geometry/Shape.h:13-25). */
+#define KZG_SHAPE_SPHERE 0
+#define KZG_SHAPE_BOX 1
+#define KZG_SHAPE_CAPSULE 2
+#define KZG_SHAPE_HULL 4
+#define KZG_SHAPE_PLANE 8
+
+/* Motion types: MotionType (reference include/Kizuri/Body/Body.h:37-41). */
+#define KZG_MOTION_STATIC 0
+#define KZG_MOTION_KINEMATIC 1
+#define KZG_MOTION_DYNAMIC 2
+
+#define KZG_BODY_SENSOR 1u         /* BodySettings::isSensor */
+#define KZG_BODY_ALLOW_SLEEPING 2u /* BodySettings::allowSleeping */
+
+/* Broad-phase pair order of kzg_step (production mode). */
+#define KZG_PAIRS_CANONICAL 0 /* every overlapping pair, sorted by MakePairKey (PhysicsWorld.cpp:13-18) */
+
+/* Solver schedules. */
+#define KZG_SCHEDULE_REFERENCE 0 /* the reference's greedy 4-wide batches (PhysicsWorld.cpp:680-717): bit-exact */
+
+/* Device capacities, fixed at creation (no reallocation while stepping). */
+typedef struct {
+    uint32_t max_bodies;
+    uint32_t max_shapes;
+    uint32_t max_hull_vertices;
+    uint32_t max_hull_indices;
+    uint32_t max_pairs;         /* broad-phase pairs per step */
+    uint32_t max_cache_entries; /* manifold cache slots (power of two; entries are never evicted) */
+    int device;                 /* CUDA ordinal */
+} kzg_config;
+
+/* Mirrors SolverSettings (reference include/Kizuri/Solver/ContactSolver.h:67-82). */
+typedef struct {
+    uint32_t velocity_iterations;
+    uint32_t position_iterations;
+    float baumgarte;
+    float penetration_slop;
+    float restitution_threshold;
+    float max_bias_velocity;
+    float warm_start_factor;
+    int use_velocity_bias;
+    int schedule; /* KZG_SCHEDULE_* */
+} kzg_solver_settings;
+
+/* Mirrors the WorldSettings fields the step reads (reference PhysicsWorld.h:20-43). */
+typedef struct {
+    float gravity[3];
+    float fixed_timestep;   /* used for the broad-phase displacement, PhysicsWorld.cpp:342 */
+    int allow_sleeping;     /* must be 0: sleeping is outside the accelerated path */
+    int warm_start;         /* 0 reproduces the reference's KZ_NOWS switch (PhysicsWorld.cpp:493) */
+} kzg_world_settings;
+
+/* One shape. params: sphere {r}; box {hx,hy,hz}; capsule {halfHeight, radius}
+ * (CapsuleShape(halfHeight, radius), Shape.h:206); plane {nx,ny,nz,d}.  Hulls reference a
+ * range of the vertex / face-size / face-index pools given to kzg_upload_shapes. */
+typedef struct {
+    uint32_t type;
+    float params[4];
+    uint32_t first_vertex, num_vertices;
+    uint32_t first_face, num_faces;
+    uint32_t first_index, num_indices;
+} kzg_shape_desc;
+
+/* Bodies in creation order (reference BodyManager::CreateBody, src/Body/BodyManager.cpp:15-61).
+ * Arrays of n entries; vectors packed xyz / xyzw; inertia 9 floats column-major.  inv_mass and
+ * inv_inertia_local are the resolved mass properties (kzg_mass_properties). world_id separates
+ * independent worlds stepped together (pairs never cross worlds); 0 for a single world. */
+typedef struct {
+    const uint32_t* shape;
+    const uint32_t* motion;
+    const uint32_t* flags;
+    const float* position;
+    const float* rotation;
+    const float* linear_velocity;
+    const float* angular_velocity;
+    const float* friction;
+    const float* restitution;
+    const float* linear_damping;
+    const float* angular_damping;
+    const float* gravity_factor;
+    const float* max_linear_velocity;
+    const float* max_angular_velocity;
+    const float* inv_mass;
+    const float* inv_inertia_local;
+    const uint32_t* object_layer;
+    const uint32_t* collision_mask;
+    const uint32_t* world_id; /* may be NULL */
+} kzg_body_soa;
+
+/* Counters of the last step (reference WorldStats, PhysicsWorld.h:66-77, with honest stage
+ * labels) plus device-side diagnostics. */
+typedef struct {
+    uint32_t num_bodies;
+    uint32_t num_broadphase_pairs;
+    uint32_t num_contact_constraints;
+    uint32_t num_contact_points;
+    uint32_t num_islands;
+    uint32_t num_batches;
+    uint32_t max_velocity_levels;
+    uint32_t max_bias_levels;
+    uint32_t cache_entries;
+    uint32_t device_error;  /* bit mask of KZG_DEVERR_* raised by kernels */
+    float broadphase_ms, narrowphase_ms, constraints_ms, solve_ms, integrate_ms, step_ms;
+} kzg_stats;
+
+#define KZG_DEVERR_PAIRS 1u     /* pair buffer overflow */
+#define KZG_DEVERR_CACHE 2u     /* cache table full */
+#define KZG_DEVERR_EPA 4u       /* EPA polytope exceeded its face capacity */
+#define KZG_DEVERR_MANIFOLD 8u  /* a manifold produced more than 4 points */
+
+/* ---- lifecycle (PhysicsWorld ctor/dtor, PhysicsWorld.cpp:64-78) ----------------------------- */
+kzg_status kzg_create(const kzg_config* cfg, kzg_ctx** out);
+kzg_status kzg_destroy(kzg_ctx* ctx);
+const char* kzg_last_error(const kzg_ctx* ctx); /* ctx may be NULL: last creation error */
+/* All work is issued on this stream (cudaStream_t passed as void*; NULL = the context's own). */
+kzg_status kzg_set_stream(kzg_ctx* ctx, void* stream);
+kzg_status kzg_synchronize(kzg_ctx* ctx);
+
+/* ---- settings (PhysicsWorld::GetSettings, PhysicsWorld.h:91-95) ----------------------------- */
+kzg_status kzg_set_world_settings(kzg_ctx* ctx, const kzg_world_settings* s);
+kzg_status kzg_set_solver_settings(kzg_ctx* ctx, const kzg_solver_settings* s);
+void kzg_default_settings(kzg_world_settings* ws, kzg_solver_settings* ss);
+
+/* ---- scene setup (PhysicsWorld::CreateBody, PhysicsWorld.cpp:83-93) ------------------------- */
+kzg_status kzg_upload_shapes(kzg_ctx* ctx, const kzg_shape_desc* shapes, uint32_t num_shapes,
+                             const float* hull_vertices, uint32_t num_vertices, const uint8_t* face_sizes,
+                             uint32_t num_faces, const uint32_t* face_indices, uint32_t num_indices);
+/* Appends bodies; *first_slot receives the slot (BodyID index) of the first one. */
+kzg_status kzg_add_bodies(kzg_ctx* ctx, uint32_t n, const kzg_body_soa* bodies, uint32_t* first_slot);
+
+/* ---- stepping (PhysicsWorld::StepFixed, PhysicsWorld.cpp:245-329) --------------------------- */
+/* nsteps fixed steps with the GPU broad phase (canonical pair order). */
+kzg_status kzg_step(kzg_ctx* ctx, float dt, uint32_t nsteps);
+/* One step using the caller's broad-phase pairs, in order (2 packed BodyIDs per pair, host
+ * memory).  With the reference's own pair list this reproduces the reference bit for bit. */
+kzg_status kzg_step_with_pairs(kzg_ctx* ctx, const uint32_t* packed_pairs, uint32_t num_pairs, float dt);
+
+/* ---- state access (Body getters/setters, Body.h:146-178) ------------------------------------ */
+/* 13 floats per body in slot order: position xyz, rotation xyzw, linear xyz, angular xyz. */
+kzg_status kzg_download_state(kzg_ctx* ctx, float* out, uint32_t first, uint32_t count);
+kzg_status kzg_upload_state(kzg_ctx* ctx, const float* in, uint32_t first, uint32_t count);
+/* 7 floats per body: position xyz + rotation xyzw (what a renderer reads each frame). */
+kzg_status kzg_download_transforms(kzg_ctx* ctx, float* out, uint32_t first, uint32_t count);
+/* Force and torque accumulators for the next step (Body::ApplyForce / ApplyTorque); 6 floats per
+ * body (force xyz, torque xyz); cleared after every step like Body::ClearForces. */
+kzg_status kzg_upload_forces(kzg_ctx* ctx, const float* force_torque, uint32_t first, uint32_t count);
+kzg_status kzg_download_mass(kzg_ctx* ctx, float* inv_mass, float* inv_inertia_world);
+
+/* ---- diagnostics (ComputeStateHash / GetStats / GetContactConstraints / GetPairs) ----------- */
+kzg_status kzg_state_hash(kzg_ctx* ctx, uint64_t* out); /* PhysicsWorld.cpp:1145-1175 */
+kzg_status kzg_get_stats(kzg_ctx* ctx, kzg_stats* out);
+kzg_status kzg_num_pairs(kzg_ctx* ctx, uint32_t* n);
+kzg_status kzg_download_pairs(kzg_ctx* ctx, uint32_t* packed_pairs, uint32_t capacity);
+kzg_status kzg_num_constraints(kzg_ctx* ctx, uint32_t* n);
+/* Per constraint: hdr 3 u32 (packed A, packed B, numPoints), fr 2 floats (friction, restitution),
+ * pts 8*39 floats in the layout: pA3 pB3 n3 sep feature(bits) rA3 rB3 localA3 localB3 t1_3 t2_3
+ * nMass t1Mass t2Mass nImp t1Imp t2Imp restitutionBias positionBias biasImpulse normalVelocity
+ * (the fields of ContactPointConstraint, reference ContactSolver.h:13-43). */
+kzg_status kzg_download_constraints(kzg_ctx* ctx, uint32_t* hdr, float* fr, float* pts, uint32_t capacity);
+
+/* ---- host-side setup helpers (no device needed) ---------------------------------------------- */
+/* ConvexHullShape::Create (reference src/Geometry/Shapes.cpp:331-471): builds the hull of a point
+ * cloud keeping the reference's vertex order.  Returns KZG_ERR_INVALID for degenerate clouds.
+ * Output capacities: vertices max_points*3 floats, sizes/indices see kzg_hull_capacity. */
+kzg_status kzg_hull_build(const float* points, uint32_t num_points, uint32_t max_points, float* out_vertices,
+                          uint32_t* out_num_vertices, uint8_t* out_face_sizes, uint32_t* out_num_faces,
+                          uint32_t* out_face_indices, uint32_t* out_num_indices, uint32_t capacity_faces);
+/* BodyManager::RecomputeMassProperties (reference BodyManager.cpp:63-99) for one body. */
+kzg_status kzg_mass_properties(const kzg_shape_desc* shape, const float* hull_vertices, const uint8_t* face_sizes,
+                               const uint32_t* face_indices, uint32_t motion, float density, float mass_override,
+                               float* out_inv_mass, float* out_inv_inertia_local);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

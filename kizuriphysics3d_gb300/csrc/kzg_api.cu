@@ -1,0 +1,675 @@
+// kzg_api.cu - the exported C-ABI (include/kzg.h): context lifetime, scene upload, stepping entry
+// points and state/diagnostic downloads.  Every call returns a kzg_status and leaves a message
+// in kzg_last_error() on failure; no C++ exception crosses the boundary.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "kzg_ctx.h"
+#include "kzg_internal.h"
+
+using namespace kzg;
+
+namespace {
+
+std::string g_create_error;
+
+#define CK(x)                                                            \
+    do {                                                                 \
+        cudaError_t e_ = (x);                                            \
+        if (e_ != cudaSuccess) {                                         \
+            ctx->err = std::string(#x) + ": " + cudaGetErrorString(e_);  \
+            return KZG_ERR_CUDA;                                         \
+        }                                                                \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+    return cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+}
+
+kzg_status alloc_all(Ctx* ctx) {
+    const kzg_config& c = ctx->cfg;
+    const size_t B = c.max_bodies, P = c.max_pairs, R = 4ull * c.max_pairs, H = c.max_cache_entries;
+    DeviceBodies& b = ctx->b;
+    float4** f4b[] = {&b.pos, &b.rot, &b.lv, &b.av, &b.plv, &b.pav, &b.force, &b.torque, &b.prm0, &b.prm1,
+                      &b.aabb_mn, &b.aabb_mx};
+    for (float4** p : f4b) CK(dalloc(p, B));
+    CK(dalloc(&b.iiw, 3 * B));
+    CK(dalloc(&b.iil, 3 * B));
+    CK(dalloc(&b.inv_mass, B));
+    uint32_t** u32b[] = {&b.shape, &b.motion, &b.flags, &b.layer, &b.mask, &b.world, &b.packed};
+    for (uint32_t** p : u32b) CK(dalloc(p, B));
+    CK(cudaMemset(b.plv, 0, sizeof(float4) * B));
+    CK(cudaMemset(b.pav, 0, sizeof(float4) * B));
+    CK(cudaMemset(b.force, 0, sizeof(float4) * B));
+    CK(cudaMemset(b.torque, 0, sizeof(float4) * B));
+    CK(dalloc(&ctx->is_large, B));
+    CK(dalloc(&ctx->large_list, B));
+    CK(dalloc(&ctx->large_off, 65537));  // world ids are < 65536
+    CK(dalloc(&ctx->cell_keys, B));
+    CK(dalloc(&ctx->cell_keys_sorted, B));
+    CK(dalloc(&ctx->cell_vals, B));
+    CK(dalloc(&ctx->cell_vals_sorted, B));
+    CK(dalloc(&ctx->pair_keys, P));
+    CK(dalloc(&ctx->pair_keys_sorted, P));
+    CK(dalloc(&ctx->pairs, P));
+    CK(dalloc(&ctx->m_count, P));
+    CK(dalloc(&ctx->m_data, 12 * P));
+    CK(dalloc(&ctx->m_key, P));
+    CK(dalloc(&ctx->con_flag, P));
+    CK(dalloc(&ctx->con_index, P));
+    CK(dalloc(&ctx->con_pair, P));
+    CK(dalloc(&ctx->con_a, P));
+    CK(dalloc(&ctx->con_b, P));
+    CK(dalloc(&ctx->con_np, P));
+    CK(dalloc(&ctx->con_bits, P));
+    CK(dalloc(&ctx->con_fr, P));
+    CK(dalloc(&ctx->con_key, P));
+    DeviceRows& r = ctx->r;
+    float4** rows[] = {&r.pA, &r.pB, &r.n, &r.t1, &r.t2, &r.rA, &r.rB, &r.rAr, &r.rBr, &r.laA, &r.laB,
+                       &r.mass, &r.imp, &r.bias};
+    for (float4** p : rows) {
+        CK(dalloc(p, R));
+        CK(cudaMemset(*p, 0, sizeof(float4) * R));
+    }
+    CK(dalloc(&ctx->uf, B));
+    CK(dalloc(&ctx->isl_key, P));
+    CK(dalloc(&ctx->isl_key_sorted, P));
+    CK(dalloc(&ctx->isl_con_in, P));
+    CK(dalloc(&ctx->isl_con, P));
+    CK(dalloc(&ctx->isl_head, P));
+    CK(dalloc(&ctx->isl_start, P + 1));
+    CK(dalloc(&ctx->isl_pts, P));
+    CK(dalloc(&ctx->lvl_count, R + P + 1));
+    CK(dalloc(&ctx->last_lvl, B));
+    CK(cudaMemset(ctx->last_lvl, 0, sizeof(uint32_t) * B));
+    CK(dalloc(&ctx->batch_cnt, R));
+    CK(dalloc(&ctx->batch_body, 8 * R));
+    CK(dalloc(&ctx->batch_mem, 4 * R));
+    CK(dalloc(&ctx->lvl_tmp, R));
+    CK(dalloc(&ctx->ids_tmp, R));
+    CK(dalloc(&ctx->wl_list, R));
+    CK(dalloc(&ctx->vl_list, R));
+    CK(dalloc(&ctx->bl_list, R));
+    CK(dalloc(&ctx->wl_off, R + P + 1));
+    CK(dalloc(&ctx->vl_off, R + P + 1));
+    CK(dalloc(&ctx->bl_off, R + P + 1));
+    CK(dalloc(&ctx->isl_meta, 4 * P));
+    CK(dalloc(&ctx->c_key, H));
+    CK(cudaMemset(ctx->c_key, 0, sizeof(unsigned long long) * H));
+    CK(dalloc(&ctx->c_np, H));
+    CK(dalloc(&ctx->c_pos, 4 * H));
+    CK(dalloc(&ctx->c_imp, 4 * H));
+    CK(dalloc(&ctx->dcnt, 1));
+    CK(cudaMemset(ctx->dcnt, 0, sizeof(Counters)));
+    CK(cudaMallocHost((void**)&ctx->hcnt, sizeof(Counters)));
+    std::memset(ctx->hcnt, 0, sizeof(Counters));
+    ctx->cub_tmp_bytes = cub_temp_bytes(std::max<uint32_t>(c.max_pairs, c.max_bodies));
+    CK(cudaMalloc(&ctx->cub_tmp, ctx->cub_tmp_bytes));
+    CK(dalloc(&ctx->hash_words, 14 * B));
+    for (cudaEvent_t& e : ctx->ev) CK(cudaEventCreate(&e));
+    return KZG_OK;
+}
+
+void free_all(Ctx* ctx) {
+    DeviceBodies& b = ctx->b;
+    void* ptrs[] = {b.pos, b.rot, b.lv, b.av, b.plv, b.pav, b.force, b.torque, b.prm0, b.prm1, b.aabb_mn, b.aabb_mx,
+                    b.iiw, b.iil, b.inv_mass, b.shape, b.motion, b.flags, b.layer, b.mask, b.world, b.packed,
+                    ctx->is_large, ctx->large_list, ctx->large_off, ctx->cell_keys, ctx->cell_keys_sorted,
+                    ctx->cell_vals, ctx->cell_vals_sorted, ctx->pair_keys, ctx->pair_keys_sorted, ctx->pairs,
+                    ctx->m_count, ctx->m_data, ctx->m_key, ctx->con_flag, ctx->con_index, ctx->con_pair, ctx->con_a,
+                    ctx->con_b, ctx->con_np, ctx->con_bits, ctx->con_fr, ctx->con_key, ctx->r.pA, ctx->r.pB, ctx->r.n,
+                    ctx->r.t1, ctx->r.t2, ctx->r.rA, ctx->r.rB, ctx->r.rAr, ctx->r.rBr, ctx->r.laA, ctx->r.laB,
+                    ctx->r.mass, ctx->r.imp, ctx->r.bias, ctx->uf, ctx->isl_key, ctx->isl_key_sorted,
+                    ctx->isl_con_in, ctx->isl_con, ctx->isl_head, ctx->isl_start, ctx->isl_pts, ctx->lvl_count,
+                    ctx->last_lvl, ctx->batch_cnt, ctx->batch_body, ctx->batch_mem, ctx->lvl_tmp, ctx->ids_tmp,
+                    ctx->wl_list, ctx->vl_list, ctx->bl_list, ctx->wl_off, ctx->vl_off, ctx->bl_off, ctx->isl_meta,
+                    ctx->c_key, ctx->c_np, ctx->c_pos, ctx->c_imp, ctx->dcnt, ctx->cub_tmp, ctx->hash_words,
+                    ctx->shapes, ctx->hull_verts, ctx->face_sizes, ctx->face_idx};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (ctx->hcnt) cudaFreeHost(ctx->hcnt);
+    for (cudaEvent_t e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+}
+
+struct HostShape {
+    kzg_shape_desc d;
+    float radius;  // bounds every rotated world-AABB half size of the shape
+};
+
+struct HostSide {
+    std::vector<HostShape> shapes;
+    std::vector<uint32_t> shape, motion, world;
+    bool dirty = true;
+};
+
+}  // namespace
+
+// Host-side mirror kept next to each context.
+struct kzg_ctx {
+    Ctx c;
+    HostSide h;
+};
+
+namespace {
+
+// Large bodies (planes, and bodies far larger than the typical one) bypass the uniform grid and
+// are tested against every body of their world; the grid cell fits every other body's AABB.
+kzg_status finalize_bodies(kzg_ctx* k) {
+    Ctx* ctx = &k->c;
+    HostSide& h = k->h;
+    if (!h.dirty) return KZG_OK;
+    const uint32_t n = ctx->nbodies;
+    std::vector<float> rad;
+    for (uint32_t i = 0; i < n; ++i) {
+        const HostShape& s = h.shapes[h.shape[i]];
+        if (s.d.type != KZG_SHAPE_PLANE) rad.push_back(s.radius);
+    }
+    float r90 = 0.0f;
+    if (!rad.empty()) {
+        std::vector<float> t = rad;
+        size_t q = (t.size() * 9) / 10;
+        std::nth_element(t.begin(), t.begin() + q, t.end());
+        r90 = t[q];
+    }
+    std::vector<uint8_t> large(n, 0);
+    float rmax_small = 0.0f;
+    uint32_t nworlds = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const HostShape& s = h.shapes[h.shape[i]];
+        bool lg = s.d.type == KZG_SHAPE_PLANE || (r90 > 0.0f && s.radius > 4.0f * r90);
+        large[i] = lg ? 1 : 0;
+        if (!lg) rmax_small = std::max(rmax_small, s.radius);
+        nworlds = std::max(nworlds, h.world[i] + 1);
+    }
+    ctx->cell_size = rmax_small > 0.0f ? 2.02f * rmax_small : 1.0f;
+    std::vector<uint32_t> off(nworlds + 1, 0), list;
+    for (uint32_t i = 0; i < n; ++i)
+        if (large[i]) off[h.world[i] + 1]++;
+    for (uint32_t w = 0; w < nworlds; ++w) off[w + 1] += off[w];
+    list.resize(off[nworlds]);
+    std::vector<uint32_t> fill(off.begin(), off.end() - 1);
+    for (uint32_t i = 0; i < n; ++i)
+        if (large[i]) list[fill[h.world[i]]++] = i;
+    ctx->nlarge = (uint32_t)list.size();
+    ctx->nworlds = nworlds;
+    CK(cudaMemcpy(ctx->is_large, large.data(), n, cudaMemcpyHostToDevice));
+    if (!list.empty()) CK(cudaMemcpy(ctx->large_list, list.data(), sizeof(uint32_t) * list.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->large_off, off.data(), sizeof(uint32_t) * off.size(), cudaMemcpyHostToDevice));
+    h.dirty = false;
+    return KZG_OK;
+}
+
+kzg_status check(kzg_ctx* c) { return c ? KZG_OK : KZG_ERR_INVALID; }
+}  // namespace
+
+extern "C" {
+
+void kzg_default_settings(kzg_world_settings* ws, kzg_solver_settings* ss) {
+    if (ws) {
+        ws->gravity[0] = 0.0f; ws->gravity[1] = -9.81f; ws->gravity[2] = 0.0f;
+        ws->fixed_timestep = (float)(1.0 / 60.0);
+        ws->allow_sleeping = 0;
+        ws->warm_start = 1;
+    }
+    if (ss) {  // SolverSettings defaults, ContactSolver.h:67-82
+        ss->velocity_iterations = 16;
+        ss->position_iterations = 6;
+        ss->baumgarte = 0.2f;
+        ss->penetration_slop = 0.005f;
+        ss->restitution_threshold = 1.0f;
+        ss->max_bias_velocity = 3.0f;
+        ss->warm_start_factor = 1.0f;
+        ss->use_velocity_bias = 0;
+        ss->schedule = KZG_SCHEDULE_REFERENCE;
+    }
+}
+
+kzg_status kzg_create(const kzg_config* cfg, kzg_ctx** out) {
+    if (!cfg || !out) { g_create_error = "null argument"; return KZG_ERR_INVALID; }
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        g_create_error = "no CUDA device: the contact pipeline has no CPU fallback";
+        return KZG_ERR_CUDA;
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) { g_create_error = "bad device ordinal"; return KZG_ERR_INVALID; }
+    if (cfg->max_cache_entries == 0 || (cfg->max_cache_entries & (cfg->max_cache_entries - 1)) != 0) {
+        g_create_error = "max_cache_entries must be a power of two";
+        return KZG_ERR_INVALID;
+    }
+    if (cfg->max_bodies == 0 || cfg->max_bodies > 0x00FFFFFFu || cfg->max_pairs == 0) {
+        g_create_error = "max_bodies must be in [1, 2^24) and max_pairs > 0";
+        return KZG_ERR_INVALID;
+    }
+    kzg_ctx* k = new (std::nothrow) kzg_ctx();
+    if (!k) { g_create_error = "out of host memory"; return KZG_ERR_INVALID; }
+    Ctx* ctx = &k->c;
+    ctx->cfg = *cfg;
+    ctx->device = cfg->device;
+    kzg_default_settings(&ctx->ws, &ctx->ss);
+    if (cudaSetDevice(cfg->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        g_create_error = "cannot open the CUDA device";
+        delete k;
+        return KZG_ERR_CUDA;
+    }
+    ctx->own_stream = true;
+    kzg_status s = alloc_all(ctx);
+    if (s != KZG_OK) {
+        g_create_error = ctx->err;
+        free_all(ctx);
+        delete k;
+        return s;
+    }
+    *out = k;
+    return KZG_OK;
+}
+
+kzg_status kzg_destroy(kzg_ctx* k) {
+    if (!k) return KZG_ERR_INVALID;
+    cudaSetDevice(k->c.device);
+    cudaStreamSynchronize(k->c.stream);
+    free_all(&k->c);
+    delete k;
+    return KZG_OK;
+}
+
+const char* kzg_last_error(const kzg_ctx* k) { return k ? k->c.err.c_str() : g_create_error.c_str(); }
+
+kzg_status kzg_set_stream(kzg_ctx* k, void* stream) {
+    if (check(k)) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    ctx->own_stream = false;
+    ctx->stream = (cudaStream_t)stream;
+    if (!stream) {
+        CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        ctx->own_stream = true;
+    }
+    return KZG_OK;
+}
+
+kzg_status kzg_synchronize(kzg_ctx* k) {
+    if (check(k)) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return KZG_OK;
+}
+
+kzg_status kzg_set_world_settings(kzg_ctx* k, const kzg_world_settings* s) {
+    if (check(k) || !s) return KZG_ERR_INVALID;
+    if (s->allow_sleeping) {
+        k->c.err = "sleeping (WorldSettings::allowSleeping) is outside the accelerated path";
+        return KZG_ERR_UNSUPPORTED;
+    }
+    k->c.ws = *s;
+    return KZG_OK;
+}
+
+kzg_status kzg_set_solver_settings(kzg_ctx* k, const kzg_solver_settings* s) {
+    if (check(k) || !s) return KZG_ERR_INVALID;
+    if (s->schedule != KZG_SCHEDULE_REFERENCE) {
+        k->c.err = "unknown solver schedule";
+        return KZG_ERR_INVALID;
+    }
+    k->c.ss = *s;
+    return KZG_OK;
+}
+
+kzg_status kzg_upload_shapes(kzg_ctx* k, const kzg_shape_desc* shapes, uint32_t ns, const float* hv, uint32_t nv,
+                             const uint8_t* fs, uint32_t nf, const uint32_t* fi, uint32_t ni) {
+    if (check(k) || (ns && !shapes)) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    if (ctx->shapes_uploaded) { ctx->err = "shapes are uploaded once per context"; return KZG_ERR_INVALID; }
+    if (ns > ctx->cfg.max_shapes || nv > ctx->cfg.max_hull_vertices || ni > ctx->cfg.max_hull_indices) {
+        ctx->err = "shape tables exceed kzg_config capacities";
+        return KZG_ERR_CAPACITY;
+    }
+    std::vector<ShapeDev> dev(ns);
+    HostSide& h = k->h;
+    h.shapes.resize(ns);
+    for (uint32_t i = 0; i < ns; ++i) {
+        const kzg_shape_desc& d = shapes[i];
+        if (d.type != KZG_SHAPE_SPHERE && d.type != KZG_SHAPE_BOX && d.type != KZG_SHAPE_CAPSULE &&
+            d.type != KZG_SHAPE_HULL && d.type != KZG_SHAPE_PLANE) {
+            ctx->err = "shape " + std::to_string(i) + ": type outside the accelerated set";
+            return KZG_ERR_UNSUPPORTED;
+        }
+        if (d.type == KZG_SHAPE_HULL) {
+            bool ok = d.num_vertices > 0 && d.num_faces > 0 && d.first_vertex + d.num_vertices <= nv &&
+                      d.first_face + d.num_faces <= nf && d.first_index + d.num_indices <= ni && hv && fs && fi;
+            uint64_t total = 0;
+            for (uint32_t f = 0; ok && f < d.num_faces; ++f) {
+                ok = fs[d.first_face + f] >= 3;
+                total += fs[d.first_face + f];
+            }
+            ok = ok && total == d.num_indices;
+            for (uint32_t q = 0; ok && q < d.num_indices; ++q) ok = fi[d.first_index + q] < d.num_vertices;
+            if (!ok) {
+                ctx->err = "shape " + std::to_string(i) + ": inconsistent hull ranges, face sizes or indices";
+                return KZG_ERR_INVALID;
+            }
+        }
+        ShapeDev& s = dev[i];
+        std::memset(&s, 0, sizeof s);
+        s.type = d.type;
+        s.vfirst = d.first_vertex; s.vnum = d.num_vertices;
+        s.ffirst = d.first_face; s.fnum = d.num_faces;
+        s.ifirst = d.first_index; s.inum = d.num_indices;
+        for (int q = 0; q < 4; ++q) s.p[q] = d.params[q];
+        shape_local_bounds(d, hv, s.lmn, s.lmx);
+        h.shapes[i].d = d;
+        float ex = 0.5f * (s.lmx[0] - s.lmn[0]), ey = 0.5f * (s.lmx[1] - s.lmn[1]), ez = 0.5f * (s.lmx[2] - s.lmn[2]);
+        float cx = 0.5f * (s.lmx[0] + s.lmn[0]), cy = 0.5f * (s.lmx[1] + s.lmn[1]), cz = 0.5f * (s.lmx[2] + s.lmn[2]);
+        h.shapes[i].radius = std::sqrt(ex * ex + ey * ey + ez * ez) + std::sqrt(cx * cx + cy * cy + cz * cz);
+    }
+    CK(dalloc(&ctx->shapes, ns));
+    CK(cudaMemcpy(ctx->shapes, dev.data(), sizeof(ShapeDev) * ns, cudaMemcpyHostToDevice));
+    std::vector<float4> v4(nv);
+    for (uint32_t i = 0; i < nv; ++i) v4[i] = make_float4(hv[3 * i], hv[3 * i + 1], hv[3 * i + 2], 0.0f);
+    CK(dalloc(&ctx->hull_verts, nv));
+    CK(dalloc(&ctx->face_sizes, nf));
+    CK(dalloc(&ctx->face_idx, ni));
+    if (nv) CK(cudaMemcpy(ctx->hull_verts, v4.data(), sizeof(float4) * nv, cudaMemcpyHostToDevice));
+    if (nf) CK(cudaMemcpy(ctx->face_sizes, fs, nf, cudaMemcpyHostToDevice));
+    if (ni) CK(cudaMemcpy(ctx->face_idx, fi, sizeof(uint32_t) * ni, cudaMemcpyHostToDevice));
+    ctx->nshapes = ns;
+    ctx->shapes_uploaded = true;
+    return KZG_OK;
+}
+
+kzg_status kzg_add_bodies(kzg_ctx* k, uint32_t n, const kzg_body_soa* b, uint32_t* first_slot) {
+    if (check(k) || !b) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    if (!ctx->shapes_uploaded) { ctx->err = "upload shapes before bodies"; return KZG_ERR_INVALID; }
+    const uint32_t base = ctx->nbodies;
+    if (base + n > ctx->cfg.max_bodies) { ctx->err = "kzg_config.max_bodies exceeded"; return KZG_ERR_CAPACITY; }
+    if (!b->shape || !b->motion || !b->position || !b->rotation || !b->inv_mass || !b->inv_inertia_local) {
+        ctx->err = "missing required body arrays";
+        return KZG_ERR_INVALID;
+    }
+    HostSide& h = k->h;
+    std::vector<float4> pos(n), rot(n), lv(n), av(n), p0(n), p1(n), iil(3 * n), iiw(3 * n);
+    std::vector<uint32_t> flags(n), layer(n), mask(n), world(n), packed(n), motion(n), shape(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (b->shape[i] >= ctx->nshapes || b->motion[i] > KZG_MOTION_DYNAMIC) {
+            ctx->err = "body " + std::to_string(i) + ": bad shape index or motion type";
+            return KZG_ERR_INVALID;
+        }
+        if (b->flags && (b->flags[i] & ~(KZG_BODY_SENSOR | KZG_BODY_ALLOW_SLEEPING))) {
+            ctx->err = "unknown body flag";
+            return KZG_ERR_INVALID;
+        }
+        auto f = [&](const float* a, uint32_t k_, float dflt) { return a ? a[k_] : dflt; };
+        shape[i] = b->shape[i];
+        motion[i] = b->motion[i];
+        pos[i] = make_float4(b->position[3 * i], b->position[3 * i + 1], b->position[3 * i + 2], 0.0f);
+        Quat q(b->rotation[4 * i], b->rotation[4 * i + 1], b->rotation[4 * i + 2], b->rotation[4 * i + 3]);
+        rot[i] = make_float4(q.x, q.y, q.z, q.w);
+        lv[i] = make_float4(f(b->linear_velocity, 3 * i, 0.0f), f(b->linear_velocity, 3 * i + 1, 0.0f),
+                            f(b->linear_velocity, 3 * i + 2, 0.0f), 0.0f);
+        av[i] = make_float4(f(b->angular_velocity, 3 * i, 0.0f), f(b->angular_velocity, 3 * i + 1, 0.0f),
+                            f(b->angular_velocity, 3 * i + 2, 0.0f), 0.0f);
+        // BodySettings defaults, Body.h:62-90
+        p0[i] = make_float4(f(b->linear_damping, i, 0.05f), f(b->angular_damping, i, 0.05f),
+                            f(b->gravity_factor, i, 1.0f), f(b->max_linear_velocity, i, 500.0f));
+        p1[i] = make_float4(f(b->max_angular_velocity, i, 50.0f), f(b->friction, i, 0.5f), f(b->restitution, i, 0.0f),
+                            0.0f);
+        const float* L = b->inv_inertia_local + 9 * i;
+        Mat3 IL{Vec3(L[0], L[1], L[2]), Vec3(L[3], L[4], L[5]), Vec3(L[6], L[7], L[8])};
+        for (int c = 0; c < 3; ++c) iil[3 * i + c] = make_float4(L[3 * c], L[3 * c + 1], L[3 * c + 2], 0.0f);
+        // World inertia at creation: MotionProperties::UpdateWorldInertia (Body.h:122-125) for
+        // dynamic bodies with mass, zero otherwise (BodyManager.cpp:65-79).
+        Mat3 W{Vec3(), Vec3(), Vec3()};
+        if (motion[i] == KZG_MOTION_DYNAMIC && b->inv_mass[i] > 0.0f) {
+            Mat3 R = q.to_mat3();
+            W = (R * IL) * R.transposed();
+        }
+        iiw[3 * i] = make_float4(W.c0.x, W.c0.y, W.c0.z, 0.0f);
+        iiw[3 * i + 1] = make_float4(W.c1.x, W.c1.y, W.c1.z, 0.0f);
+        iiw[3 * i + 2] = make_float4(W.c2.x, W.c2.y, W.c2.z, 0.0f);
+        flags[i] = b->flags ? b->flags[i] : KZG_BODY_ALLOW_SLEEPING;
+        layer[i] = b->object_layer ? b->object_layer[i] : 1u;
+        mask[i] = b->collision_mask ? b->collision_mask[i] : 0xFFFFFFFFu;
+        world[i] = b->world_id ? b->world_id[i] : 0u;
+        if (world[i] > 0xFFFFu) { ctx->err = "world_id must be < 65536"; return KZG_ERR_INVALID; }
+        packed[i] = base + i;  // BodyID(index, sequence 0).Packed()
+    }
+    DeviceBodies& d = ctx->b;
+    auto up4 = [&](float4* dst, const std::vector<float4>& src, size_t per) {
+        return cudaMemcpy(dst + per * base, src.data(), sizeof(float4) * src.size(), cudaMemcpyHostToDevice);
+    };
+    auto up32 = [&](uint32_t* dst, const std::vector<uint32_t>& src) {
+        return cudaMemcpy(dst + base, src.data(), sizeof(uint32_t) * src.size(), cudaMemcpyHostToDevice);
+    };
+    CK(up4(d.pos, pos, 1)); CK(up4(d.rot, rot, 1)); CK(up4(d.lv, lv, 1)); CK(up4(d.av, av, 1));
+    CK(up4(d.prm0, p0, 1)); CK(up4(d.prm1, p1, 1)); CK(up4(d.iil, iil, 3)); CK(up4(d.iiw, iiw, 3));
+    CK(cudaMemcpy(d.inv_mass + base, b->inv_mass, sizeof(float) * n, cudaMemcpyHostToDevice));
+    CK(up32(d.shape, shape)); CK(up32(d.motion, motion)); CK(up32(d.flags, flags)); CK(up32(d.layer, layer));
+    CK(up32(d.mask, mask)); CK(up32(d.world, world)); CK(up32(d.packed, packed));
+    h.shape.insert(h.shape.end(), shape.begin(), shape.end());
+    h.motion.insert(h.motion.end(), motion.begin(), motion.end());
+    h.world.insert(h.world.end(), world.begin(), world.end());
+    h.dirty = true;
+    ctx->nbodies += n;
+    if (first_slot) *first_slot = base;
+    return KZG_OK;
+}
+
+kzg_status kzg_step(kzg_ctx* k, float dt, uint32_t nsteps) {
+    if (check(k)) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    if (!(dt > 0.0f)) return KZG_OK;  // PhysicsWorld::Step ignores dt <= 0 (PhysicsWorld.cpp:226)
+    CK(cudaSetDevice(ctx->device));
+    kzg_status s = finalize_bodies(k);
+    if (s != KZG_OK) return s;
+    for (uint32_t i = 0; i < nsteps; ++i) {
+        s = step_canonical(*ctx, dt);
+        if (s != KZG_OK) return s;
+    }
+    return KZG_OK;
+}
+
+kzg_status kzg_step_with_pairs(kzg_ctx* k, const uint32_t* pairs, uint32_t np, float dt) {
+    if (check(k) || (np && !pairs)) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    CK(cudaSetDevice(ctx->device));
+    kzg_status s = finalize_bodies(k);
+    if (s != KZG_OK) return s;
+    return step_external(*ctx, pairs, np, dt);
+}
+
+kzg_status kzg_download_state(kzg_ctx* k, float* out, uint32_t first, uint32_t count) {
+    if (check(k) || !out) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    if (first + count > ctx->nbodies) { ctx->err = "range outside the body array"; return KZG_ERR_INVALID; }
+    std::vector<float4> p(count), q(count), l(count), a(count);
+    CK(cudaMemcpyAsync(p.data(), ctx->b.pos + first, sizeof(float4) * count, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(q.data(), ctx->b.rot + first, sizeof(float4) * count, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(l.data(), ctx->b.lv + first, sizeof(float4) * count, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(a.data(), ctx->b.av + first, sizeof(float4) * count, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (uint32_t i = 0; i < count; ++i) {
+        float* o = out + 13 * i;
+        o[0] = p[i].x; o[1] = p[i].y; o[2] = p[i].z;
+        o[3] = q[i].x; o[4] = q[i].y; o[5] = q[i].z; o[6] = q[i].w;
+        o[7] = l[i].x; o[8] = l[i].y; o[9] = l[i].z;
+        o[10] = a[i].x; o[11] = a[i].y; o[12] = a[i].z;
+    }
+    return KZG_OK;
+}
+
+kzg_status kzg_upload_state(kzg_ctx* k, const float* in, uint32_t first, uint32_t count) {
+    if (check(k) || !in) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    if (first + count > ctx->nbodies) { ctx->err = "range outside the body array"; return KZG_ERR_INVALID; }
+    std::vector<float4> p(count), q(count), l(count), a(count), il(3 * count), iw(3 * count);
+    std::vector<float> im(count);
+    CK(cudaMemcpy(il.data(), ctx->b.iil + 3ull * first, sizeof(float4) * 3 * count, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(im.data(), ctx->b.inv_mass + first, sizeof(float) * count, cudaMemcpyDeviceToHost));
+    HostSide& h = k->h;
+    for (uint32_t i = 0; i < count; ++i) {
+        const float* s = in + 13 * i;
+        p[i] = make_float4(s[0], s[1], s[2], 0.0f);
+        q[i] = make_float4(s[3], s[4], s[5], s[6]);
+        l[i] = make_float4(s[7], s[8], s[9], 0.0f);
+        a[i] = make_float4(s[10], s[11], s[12], 0.0f);
+        Mat3 W{Vec3(), Vec3(), Vec3()};
+        if (h.motion[first + i] == KZG_MOTION_DYNAMIC && im[i] > 0.0f) {
+            Quat qq(s[3], s[4], s[5], s[6]);
+            Mat3 R = qq.to_mat3();
+            Mat3 IL{Vec3(il[3 * i].x, il[3 * i].y, il[3 * i].z), Vec3(il[3 * i + 1].x, il[3 * i + 1].y, il[3 * i + 1].z),
+                    Vec3(il[3 * i + 2].x, il[3 * i + 2].y, il[3 * i + 2].z)};
+            W = (R * IL) * R.transposed();
+        }
+        iw[3 * i] = make_float4(W.c0.x, W.c0.y, W.c0.z, 0.0f);
+        iw[3 * i + 1] = make_float4(W.c1.x, W.c1.y, W.c1.z, 0.0f);
+        iw[3 * i + 2] = make_float4(W.c2.x, W.c2.y, W.c2.z, 0.0f);
+    }
+    CK(cudaMemcpy(ctx->b.pos + first, p.data(), sizeof(float4) * count, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->b.rot + first, q.data(), sizeof(float4) * count, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->b.lv + first, l.data(), sizeof(float4) * count, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->b.av + first, a.data(), sizeof(float4) * count, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->b.iiw + 3ull * first, iw.data(), sizeof(float4) * 3 * count, cudaMemcpyHostToDevice));
+    return KZG_OK;
+}
+
+kzg_status kzg_download_transforms(kzg_ctx* k, float* out, uint32_t first, uint32_t count) {
+    if (check(k) || !out) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    if (first + count > ctx->nbodies) { ctx->err = "range outside the body array"; return KZG_ERR_INVALID; }
+    // pos.xyz + rot.xyzw: 7 floats per body gathered straight from the float4 arrays
+    CK(cudaMemcpy2DAsync(out, 7 * sizeof(float), ctx->b.pos + first, sizeof(float4), 3 * sizeof(float), count,
+                         cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpy2DAsync(out + 3, 7 * sizeof(float), ctx->b.rot + first, sizeof(float4), 4 * sizeof(float), count,
+                         cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return KZG_OK;
+}
+
+kzg_status kzg_upload_forces(kzg_ctx* k, const float* ft, uint32_t first, uint32_t count) {
+    if (check(k) || !ft) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    if (first + count > ctx->nbodies) { ctx->err = "range outside the body array"; return KZG_ERR_INVALID; }
+    CK(cudaMemcpy2DAsync(ctx->b.force + first, sizeof(float4), ft, 6 * sizeof(float), 3 * sizeof(float), count,
+                         cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpy2DAsync(ctx->b.torque + first, sizeof(float4), ft + 3, 6 * sizeof(float), 3 * sizeof(float), count,
+                         cudaMemcpyHostToDevice, ctx->stream));
+    return KZG_OK;
+}
+
+kzg_status kzg_download_mass(kzg_ctx* k, float* im, float* iw) {
+    if (check(k)) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    const uint32_t n = ctx->nbodies;
+    if (im) CK(cudaMemcpy(im, ctx->b.inv_mass, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    if (iw) {
+        std::vector<float4> w(3ull * n);
+        CK(cudaMemcpy(w.data(), ctx->b.iiw, sizeof(float4) * w.size(), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < w.size(); ++i) { iw[3 * i] = w[i].x; iw[3 * i + 1] = w[i].y; iw[3 * i + 2] = w[i].z; }
+    }
+    return KZG_OK;
+}
+
+kzg_status kzg_state_hash(kzg_ctx* k, uint64_t* out) {
+    if (check(k) || !out) return KZG_ERR_INVALID;
+    return hash_state(k->c, out);
+}
+
+kzg_status kzg_get_stats(kzg_ctx* k, kzg_stats* out) {
+    if (check(k) || !out) return KZG_ERR_INVALID;
+    *out = k->c.stats;
+    return KZG_OK;
+}
+
+kzg_status kzg_num_pairs(kzg_ctx* k, uint32_t* n) {
+    if (check(k) || !n) return KZG_ERR_INVALID;
+    *n = k->c.hcnt->npairs;
+    return KZG_OK;
+}
+
+kzg_status kzg_download_pairs(kzg_ctx* k, uint32_t* out, uint32_t cap) {
+    if (check(k) || !out) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    uint32_t n = std::min(ctx->hcnt->npairs, cap);
+    std::vector<uint2> p(n);
+    std::vector<uint32_t> packed(ctx->nbodies);
+    if (n) CK(cudaMemcpy(p.data(), ctx->pairs, sizeof(uint2) * n, cudaMemcpyDeviceToHost));
+    if (ctx->nbodies) CK(cudaMemcpy(packed.data(), ctx->b.packed, 4 * ctx->nbodies, cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < n; ++i) {
+        out[2 * i] = p[i].x == 0xFFFFFFFFu ? 0xFFFFFFFFu : packed[p[i].x];
+        out[2 * i + 1] = p[i].y == 0xFFFFFFFFu ? 0xFFFFFFFFu : packed[p[i].y];
+    }
+    return KZG_OK;
+}
+
+kzg_status kzg_num_constraints(kzg_ctx* k, uint32_t* n) {
+    if (check(k) || !n) return KZG_ERR_INVALID;
+    *n = k->c.hcnt->ncons;
+    return KZG_OK;
+}
+
+kzg_status kzg_download_constraints(kzg_ctx* k, uint32_t* hdr, float* fr, float* pts, uint32_t cap) {
+    if (check(k)) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    const uint32_t n = std::min(ctx->hcnt->ncons, cap);
+    if (!n) return KZG_OK;
+    std::vector<uint32_t> a(n), b(n), np(n);
+    std::vector<float2> f(n);
+    CK(cudaMemcpy(a.data(), ctx->con_a, 4 * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(b.data(), ctx->con_b, 4 * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(np.data(), ctx->con_np, 4 * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(f.data(), ctx->con_fr, sizeof(float2) * n, cudaMemcpyDeviceToHost));
+    const size_t R = 4ull * n;
+    const DeviceRows& r = ctx->r;
+    std::vector<float4> pA(R), pB(R), nn(R), t1(R), t2(R), rA(R), rB(R), laA(R), laB(R), m(R), im(R), bi(R);
+    float4* srcs[] = {r.pA, r.pB, r.n, r.t1, r.t2, r.rA, r.rB, r.laA, r.laB, r.mass, r.imp, r.bias};
+    std::vector<float4>* dsts[] = {&pA, &pB, &nn, &t1, &t2, &rA, &rB, &laA, &laB, &m, &im, &bi};
+    for (int q = 0; q < 12; ++q) CK(cudaMemcpy(dsts[q]->data(), srcs[q], sizeof(float4) * R, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> packed(ctx->nbodies);
+    CK(cudaMemcpy(packed.data(), ctx->b.packed, 4 * ctx->nbodies, cudaMemcpyDeviceToHost));
+    for (uint32_t c = 0; c < n; ++c) {
+        if (hdr) { hdr[3 * c] = packed[a[c]]; hdr[3 * c + 1] = packed[b[c]]; hdr[3 * c + 2] = np[c]; }
+        if (fr) { fr[2 * c] = f[c].x; fr[2 * c + 1] = f[c].y; }
+        if (!pts) continue;
+        for (uint32_t p = 0; p < 8; ++p) {
+            float* o = pts + (8ull * c + p) * 39;
+            std::memset(o, 0, sizeof(float) * 39);
+            if (p >= np[c]) continue;
+            size_t j = 4ull * c + p;
+            auto put = [&](int at, const float4& v) { o[at] = v.x; o[at + 1] = v.y; o[at + 2] = v.z; };
+            put(0, pA[j]); put(3, pB[j]); put(6, nn[j]); o[9] = pA[j].w;
+            std::memcpy(&o[10], &pB[j].w, 4);
+            put(11, rA[j]); put(14, rB[j]); put(17, laA[j]); put(20, laB[j]); put(23, t1[j]); put(26, t2[j]);
+            o[29] = m[j].x; o[30] = m[j].y; o[31] = m[j].z;
+            o[32] = im[j].x; o[33] = im[j].y; o[34] = im[j].z;
+            o[35] = bi[j].x; o[36] = bi[j].y; o[37] = im[j].w; o[38] = bi[j].z;
+        }
+    }
+    return KZG_OK;
+}
+
+kzg_status kzg_hull_build(const float* pts, uint32_t n, uint32_t max_points, float* ov, uint32_t* onv, uint8_t* osz,
+                          uint32_t* onf, uint32_t* oidx, uint32_t* oni, uint32_t cap_faces) {
+    if (!pts || !ov || !onv || !osz || !onf || !oidx || !oni) return KZG_ERR_INVALID;
+    int r = hull_build(pts, n, max_points ? max_points : 256, ov, onv, osz, onf, oidx, oni, cap_faces);
+    if (r == -2) return KZG_ERR_CAPACITY;
+    return r == 0 ? KZG_OK : KZG_ERR_INVALID;
+}
+
+kzg_status kzg_mass_properties(const kzg_shape_desc* shape, const float* hv, const uint8_t* fs, const uint32_t* fi,
+                               uint32_t motion, float density, float mass_override, float* out_inv_mass,
+                               float* out_iil) {
+    if (!shape || !out_inv_mass || !out_iil) return KZG_ERR_INVALID;
+    if (shape->type == KZG_SHAPE_HULL && (!hv || !fs || !fi)) return KZG_ERR_INVALID;
+    mass_properties(*shape, hv, fs, fi, motion, density, mass_override, out_inv_mass, out_iil);
+    return KZG_OK;
+}
+
+}  // extern "C"

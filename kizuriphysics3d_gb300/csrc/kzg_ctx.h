@@ -1,0 +1,141 @@
+// kzg_ctx.h - internal state of one kzg context (not part of the C-ABI).
+//
+// Device layout (slot order = BodyID index order, reference BodyManager::mBodies):
+//   bodies   : float4 SoA - pos, rot, lin/ang velocity, split-impulse pseudo velocities,
+//              force/torque accumulators, world/local inverse inertia as 3 float4 columns,
+//              two float4 parameter packs; u32 SoA for shape, motion, flags, layer, mask,
+//              world, packed id.  One float4 load per vector keeps pair gathers coalesced.
+//   pairs    : uint2 (slot A, slot B) in broad-phase order, + u64 MakePairKey per pair.
+//   manifold : per pair a count and 4 contact points (pA|sep, pB|feature, n).
+//   rows     : per constraint 4 point rows (stride 4), SoA float4 fields.
+//   cache    : open-addressing table keyed by the u64 pair key, entries never evicted
+//              (the reference keeps every entry forever, PhysicsWorld.cpp:418-452).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/kzg.h"
+#include "kzg_narrow.cuh"
+
+namespace kzg {
+
+struct DeviceBodies {
+    float4 *pos, *rot, *lv, *av, *plv, *pav, *force, *torque;
+    float4 *iiw, *iil;    // 3 columns per body
+    float4 *prm0, *prm1;  // (linDamp, angDamp, gravityFactor, maxLin), (maxAng, friction, restitution, -)
+    float* inv_mass;
+    uint32_t *shape, *motion, *flags, *layer, *mask, *world, *packed;
+    float4 *aabb_mn, *aabb_mx;
+};
+
+struct DeviceRows {  // per point row, index = 4 * constraint + point
+    float4 *pA, *pB, *n;       // pA.w = separation, pB.w = feature (bits), n.w = combinedRestitution
+    float4 *t1, *t2;           // t1.w = combinedFriction
+    float4 *rA, *rB;           // world offsets used by the warm start (pointOnA - posA)
+    float4 *rAr, *rBr;         // Rotate(localAnchor): offsets used by the velocity/bias solves
+    float4 *laA, *laB;         // local anchors (exported only)
+    float4 *mass;              // normalMass, tangentMass1, tangentMass2, -
+    float4 *imp;               // normalImpulse, tangentImpulse1, tangentImpulse2, biasImpulse
+    float4 *bias;              // restitutionBias, positionBias, normalVelocity, -
+};
+
+struct Counters {  // device-side counters, copied back after each stage that sizes the next
+    uint32_t npairs;
+    uint32_t ncons;
+    uint32_t nislands;
+    uint32_t batches;
+    uint32_t max_vlev;
+    uint32_t max_blev;
+    uint32_t error;
+    uint32_t cache_entries;
+};
+
+struct Ctx {
+    kzg_config cfg{};
+    kzg_world_settings ws{};
+    kzg_solver_settings ss{};
+    std::string err;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int device = 0;
+
+    // host mirrors needed for launches
+    uint32_t nbodies = 0, nshapes = 0, nlarge = 0;
+    float cell_size = 1.0f;
+    bool shapes_uploaded = false;
+
+    // shapes
+    ShapeDev* shapes = nullptr;
+    float4* hull_verts = nullptr;
+    uint8_t* face_sizes = nullptr;
+    uint32_t* face_idx = nullptr;
+
+    DeviceBodies b{};
+    uint32_t* large_list = nullptr;  // slots of bodies that bypass the grid (planes), grouped by world
+    uint32_t* large_off = nullptr;   // per world: range in large_list (nworlds + 1 entries)
+    uint32_t nworlds = 0;
+    uint8_t* is_large = nullptr;
+
+    // broad phase
+    unsigned long long* cell_keys = nullptr;
+    unsigned long long* cell_keys_sorted = nullptr;
+    uint32_t* cell_vals = nullptr;
+    uint32_t* cell_vals_sorted = nullptr;
+    unsigned long long* pair_keys = nullptr;
+    unsigned long long* pair_keys_sorted = nullptr;
+    uint2* pairs = nullptr;
+
+    // narrow phase
+    uint32_t* m_count = nullptr;
+    float4* m_data = nullptr;  // 12 float4 per pair
+    unsigned long long* m_key = nullptr;
+
+    // constraints
+    uint32_t* con_flag = nullptr;    // per pair: 1 if it makes a constraint
+    uint32_t* con_index = nullptr;   // per pair: exclusive scan of con_flag
+    uint32_t *con_pair = nullptr, *con_a = nullptr, *con_b = nullptr, *con_np = nullptr, *con_bits = nullptr;
+    float2* con_fr = nullptr;
+    unsigned long long* con_key = nullptr;
+    DeviceRows r{};
+
+    // islands and schedule
+    uint32_t* uf = nullptr;
+    uint32_t* isl_key = nullptr;
+    uint32_t* isl_key_sorted = nullptr;
+    uint32_t* isl_con_in = nullptr;
+    uint32_t* isl_con = nullptr;      // constraints grouped by island, ascending within each
+    uint32_t* isl_head = nullptr;
+    uint32_t* isl_start = nullptr;    // nislands + 1
+    uint32_t* isl_pts = nullptr;      // first point slot of each island in the level lists
+    uint32_t* lvl_count = nullptr;    // per island level counters (4*ncons + nislands + 1)
+    uint32_t* last_lvl = nullptr;     // per body: level of its last update in the current sweep
+    uint32_t* batch_cnt = nullptr;    // per batch member count (batches <= points)
+    uint32_t* batch_body = nullptr;   // 8 body slots per batch
+    uint32_t* batch_mem = nullptr;    // 4 point rows per batch
+    uint32_t* lvl_tmp = nullptr;      // per point level of the sweep being sorted
+    uint32_t* ids_tmp = nullptr;      // per point row id of the sweep being sorted
+    uint32_t *wl_list = nullptr, *vl_list = nullptr, *bl_list = nullptr;   // per island point lists by level
+    uint32_t *wl_off = nullptr, *vl_off = nullptr, *bl_off = nullptr;      // level offsets
+    uint32_t* isl_meta = nullptr;     // per island: nw, nv, nb levels, level offset base
+
+    // cache
+    unsigned long long* c_key = nullptr;
+    uint32_t* c_np = nullptr;
+    float4* c_pos = nullptr;
+    float4* c_imp = nullptr;
+
+    // misc
+    Counters* dcnt = nullptr;
+    Counters* hcnt = nullptr;  // pinned
+    void* cub_tmp = nullptr;
+    size_t cub_tmp_bytes = 0;
+    unsigned long long* hash_words = nullptr;
+    cudaEvent_t ev[8] = {};
+    kzg_stats stats{};
+    uint32_t frame = 0;
+};
+
+}  // namespace kzg

@@ -1,0 +1,26 @@
+// kzg_internal.h - functions shared between the translation units of libkzg (not exported).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/kzg.h"
+
+namespace kzg {
+
+struct Ctx;
+
+size_t cub_temp_bytes(uint32_t max_items);
+kzg_status step_canonical(Ctx& ctx, float dt);
+kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t num_pairs, float dt);
+kzg_status hash_state(Ctx& ctx, uint64_t* out);
+
+// host setup (kzg_hull.cpp)
+int hull_build(const float* pts, uint32_t n, uint32_t max_points, float* out_v, uint32_t* out_nv, uint8_t* out_sizes,
+               uint32_t* out_nf, uint32_t* out_idx, uint32_t* out_ni, uint32_t cap_faces);
+void mass_properties(const kzg_shape_desc& s, const float* hull_vertices, const uint8_t* face_sizes,
+                     const uint32_t* face_indices, uint32_t motion, float density, float mass_override,
+                     float* out_inv_mass, float* out_iil);
+void shape_local_bounds(const kzg_shape_desc& s, const float* hull_vertices, float* mn, float* mx);
+
+}  // namespace kzg

@@ -1,0 +1,776 @@
+// kzg_narrow.cuh - device narrow phase: one thread computes one pair's manifold.
+//
+// Follows the reference's NarrowPhase::Collide routing and numerics
+// (src/Collision/CollideShape.cpp:30-430, 480-592; GJK src/Collision/GJK.cpp:11-244;
+// EPA src/Collision/EPA.cpp:16-296; support functions include/Kizuri/Geometry/Shape.h:152-226
+// and src/Geometry/Shapes.cpp:538-547).  Iteration caps, tolerances, tie-breaks (first maximum /
+// first minimum wins) and polytope face order are the reference's, so manifolds match it bit
+// for bit.  Shapes supported on the device: sphere, box, capsule, convex hull, plane.
+#pragma once
+
+#include "kzg_math.cuh"
+
+namespace kzg {
+
+enum : uint32_t { kSphere = 0, kBox = 1, kCapsule = 2, kHull = 4, kPlane = 8 };
+
+// Device shape record: 64 bytes.
+struct ShapeDev {
+    uint32_t type, vfirst, vnum, ffirst, fnum, ifirst, inum, pad0;
+    float p[4];
+    float lmn[3], lmx[3];
+    float pad1[2];
+};
+
+// Read-only view of the shape tables.
+struct ShapeTables {
+    const ShapeDev* shapes;
+    const float4* hull_verts;
+    const uint8_t* face_sizes;
+    const uint32_t* face_idx;
+};
+
+constexpr uint32_t kMaxManifold = 4;  // every routine here reduces to at most 4 points
+
+struct ContactPt {
+    Vec3 pA, pB, n;
+    float sep;
+    uint32_t feature;
+};
+
+struct Manifold {
+    ContactPt pts[kMaxManifold];
+    uint32_t n;
+};
+
+struct SP {  // SupportPoint (GJK.h:108-118)
+    Vec3 pA, pB, p;
+};
+
+struct Body {  // pose + shape of one side of a pair
+    const ShapeDev* s;
+    Quat q;
+    Vec3 t;
+};
+
+__device__ __forceinline__ Vec3 hv(const ShapeTables& T, uint32_t i) {
+    float4 v = __ldg(&T.hull_verts[i]);
+    return Vec3(v.x, v.y, v.z);
+}
+
+__device__ inline Vec3 support_local(const ShapeTables& T, const ShapeDev* s, const Vec3& d) {
+    switch (s->type) {
+        case kSphere: return d.normalized_or(Vec3(0.0f, 1.0f, 0.0f)) * s->p[0];
+        case kBox:
+            return Vec3(d.x >= 0.0f ? s->p[0] : -s->p[0], d.y >= 0.0f ? s->p[1] : -s->p[1],
+                        d.z >= 0.0f ? s->p[2] : -s->p[2]);
+        case kCapsule: {
+            float sg = d.y >= 0.0f ? s->p[0] : -s->p[0];
+            return Vec3(0.0f, sg, 0.0f) + d.normalized_or(Vec3(0.0f, 1.0f, 0.0f)) * s->p[1];
+        }
+        case kHull: {
+            float best_dot = -INFINITY;
+            Vec3 best = hv(T, s->vfirst);
+            for (uint32_t i = 0; i < s->vnum; ++i) {
+                Vec3 v = hv(T, s->vfirst + i);
+                float dd = v.dot(d);
+                if (dd > best_dot) { best_dot = dd; best = v; }
+            }
+            return best;
+        }
+        case kPlane: return Vec3(s->p[0], s->p[1], s->p[2]) * s->p[3] + d * 1.0e6f;
+        default: return Vec3();
+    }
+}
+
+struct SupportMap {
+    const ShapeTables* T;
+    Body a, b;
+    __device__ SP operator()(const Vec3& d) const {
+        Vec3 la = a.q.inv_rotate(d);
+        Vec3 lb = b.q.inv_rotate(-d);
+        SP sp;
+        sp.pA = xform(a.q, a.t, support_local(*T, a.s, la));
+        sp.pB = xform(b.q, b.t, support_local(*T, b.s, lb));
+        sp.p = sp.pA - sp.pB;
+        return sp;
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// GJK (GJK.cpp:11-244)
+// ---------------------------------------------------------------------------------------------
+__device__ inline Vec3 closest_on_triangle(const Vec3& p, const Vec3& a, const Vec3& b, const Vec3& c, float& u,
+                                           float& v, float& w) {
+    Vec3 ab = b - a, ac = c - a, ap = p - a;
+    float d1 = ab.dot(ap), d2 = ac.dot(ap);
+    if (d1 <= 0.0f && d2 <= 0.0f) { u = 1.0f; v = 0.0f; w = 0.0f; return a; }
+    Vec3 bp = p - b;
+    float d3 = ab.dot(bp), d4 = ac.dot(bp);
+    if (d3 >= 0.0f && d4 <= d3) { u = 0.0f; v = 1.0f; w = 0.0f; return b; }
+    float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f) {
+        float t = rdiv(d1, d1 - d3);
+        u = 1.0f - t; v = t; w = 0.0f;
+        return a + ab * t;
+    }
+    Vec3 cp = p - c;
+    float d5 = ab.dot(cp), d6 = ac.dot(cp);
+    if (d6 >= 0.0f && d5 <= d6) { u = 0.0f; v = 0.0f; w = 1.0f; return c; }
+    float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f) {
+        float t = rdiv(d2, d2 - d6);
+        u = 1.0f - t; v = 0.0f; w = t;
+        return a + ac * t;
+    }
+    float va = d3 * d6 - d5 * d4;
+    if (va <= 0.0f && (d4 - d3) >= 0.0f && (d5 - d6) >= 0.0f) {
+        float t = rdiv(d4 - d3, (d4 - d3) + (d5 - d6));
+        u = 0.0f; v = 1.0f - t; w = t;
+        return b + (c - b) * t;
+    }
+    float denom = rdiv(1.0f, va + vb + vc);
+    v = vb * denom;
+    w = vc * denom;
+    u = 1.0f - v - w;
+    return (a + ab * v) + ac * w;
+}
+
+__device__ __forceinline__ bool gjk_outside(const Vec3& p0, const Vec3& p1, const Vec3& p2, const Vec3& opp) {
+    Vec3 n = (p1 - p0).cross(p2 - p0);
+    if (n.dot(opp - p0) > 0.0f) n = -n;
+    return n.dot(Vec3() - p0) > 0.0f;
+}
+
+__device__ inline bool reduce_simplex(SP* s, uint32_t& count, Vec3& closest) {
+    if (count == 1) {
+        closest = s[0].p;
+    } else if (count == 2) {
+        Vec3 a = s[0].p, b = s[1].p, ab = b - a;
+        float t = -a.dot(ab);
+        if (t <= 0.0f) { closest = a; count = 1; }
+        else if (t >= ab.len2()) { s[0] = s[1]; closest = b; count = 1; }
+        else { closest = a + ab * rdiv(t, ab.len2()); }
+    } else if (count == 3) {
+        float u, v, w;
+        closest = closest_on_triangle(Vec3(), s[0].p, s[1].p, s[2].p, u, v, w);
+        SP k[3] = {SP{}, SP{}, SP{}};
+        uint32_t n = 0;
+        if (u > 0.0f) k[n++] = s[0];
+        if (v > 0.0f) k[n++] = s[1];
+        if (w > 0.0f) k[n++] = s[2];
+        if (n == 0) n = 1;
+        for (uint32_t i = 0; i < n; ++i) s[i] = k[i];
+        count = n;
+    } else if (count == 4) {
+        Vec3 a = s[0].p, b = s[1].p, c = s[2].p, d = s[3].p;
+        bool o[4] = {gjk_outside(a, b, c, d), gjk_outside(a, c, d, b), gjk_outside(a, d, b, c),
+                     gjk_outside(b, d, c, a)};
+        if (!o[0] && !o[1] && !o[2] && !o[3]) return true;
+        const uint8_t F[4][3] = {{0, 1, 2}, {0, 2, 3}, {0, 3, 1}, {1, 3, 2}};
+        float best = INFINITY;
+        SP bt[3] = {SP{}, SP{}, SP{}};
+        uint32_t bc = 0;
+        for (int f = 0; f < 4; ++f) {
+            if (!o[f]) continue;
+            float u, v, w;
+            Vec3 p = closest_on_triangle(Vec3(), s[F[f][0]].p, s[F[f][1]].p, s[F[f][2]].p, u, v, w);
+            float d2 = p.len2();
+            if (d2 < best) {
+                best = d2;
+                uint32_t n = 0;
+                if (u > 0.0f) bt[n++] = s[F[f][0]];
+                if (v > 0.0f) bt[n++] = s[F[f][1]];
+                if (w > 0.0f) bt[n++] = s[F[f][2]];
+                bc = n;
+                closest = p;
+            }
+        }
+        for (uint32_t i = 0; i < bc; ++i) s[i] = bt[i];
+        count = bc;
+    }
+    return false;
+}
+
+struct GjkOut {
+    bool intersect;
+    float distance;
+    Vec3 pA, pB, normal;
+    uint32_t ns;
+    SP simplex[4];
+};
+
+__device__ inline void gjk(const SupportMap& map, float tol, uint32_t max_iter, GjkOut& r) {
+    r.intersect = false;
+    r.distance = 0.0f;
+    r.pA = r.pB = r.normal = Vec3();
+    SP s[4];
+    uint32_t count = 0;
+    s[count++] = map(Vec3(1.0f, 0.0f, 0.0f));
+    Vec3 closest = s[0].p;
+    const float tol2 = tol * tol;
+    for (uint32_t it = 0; it < max_iter; ++it) {
+        if (closest.len2() <= tol2) { r.intersect = true; r.distance = 0.0f; break; }
+        Vec3 d = -closest;
+        SP w = map(d);
+        float progress = closest.len2() - closest.dot(w.p);
+        if (progress <= tol * closest.len2()) break;
+        bool dup = false;
+        for (uint32_t i = 0; i < count; ++i)
+            if ((s[i].p - w.p).len2() < tol2) { dup = true; break; }
+        if (dup) break;
+        s[count++] = w;
+        if (reduce_simplex(s, count, closest)) { r.intersect = true; r.distance = 0.0f; break; }
+    }
+    r.ns = count;
+    for (uint32_t i = 0; i < count; ++i) r.simplex[i] = s[i];
+    if (!r.intersect) {
+        float dist = closest.len();
+        r.distance = dist;
+        if (dist < kEps) r.intersect = true;
+        else r.normal = (-closest) / dist;
+        if (count == 1) {
+            r.pA = s[0].pA; r.pB = s[0].pB;
+        } else if (count == 2) {
+            Vec3 a = s[0].p, b = s[1].p, ab = b - a;
+            float t = rclamp(rdiv(-a.dot(ab), rmax(ab.len2(), kEps)), 0.0f, 1.0f);
+            r.pA = lerp(s[0].pA, s[1].pA, t);
+            r.pB = lerp(s[0].pB, s[1].pB, t);
+        } else if (count == 3) {
+            float u, v, w;
+            closest_on_triangle(Vec3(), s[0].p, s[1].p, s[2].p, u, v, w);
+            r.pA = (s[0].pA * u + s[1].pA * v) + s[2].pA * w;
+            r.pB = (s[0].pB * u + s[1].pB * v) + s[2].pB * w;
+        } else {
+            r.pA = s[0].pA; r.pB = s[0].pB;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// EPA (EPA.cpp:16-296).  Polytope capacities are the reference's (256 vertices are never
+// reached: 4 + 64 iterations; 512 faces; 256 horizon edges).
+// ---------------------------------------------------------------------------------------------
+constexpr uint32_t kEpaVerts = 72;
+constexpr uint32_t kEpaFaces = 512;
+constexpr uint32_t kEpaHorizon = 256;
+
+struct EpaFace {
+    uint32_t a, b, c;
+    Vec3 n;
+    float dist;
+    uint32_t alive;
+};
+
+struct EpaOut {
+    bool valid;
+    float depth;
+    Vec3 normal, pA, pB;
+};
+
+__device__ __forceinline__ bool epa_build_face(EpaFace& f, const SP* vs) {
+    Vec3 A = vs[f.a].p, B = vs[f.b].p, C = vs[f.c].p;
+    Vec3 n = (B - A).cross(C - A);
+    float len = n.len();
+    if (len < 1.0e-12f) return false;
+    n = n / len;
+    float d = n.dot(A);
+    if (d < 0.0f) {
+        n = -n;
+        d = -d;
+        uint32_t t = f.b; f.b = f.c; f.c = t;
+    }
+    f.n = n;
+    f.dist = d;
+    return true;
+}
+
+__device__ __forceinline__ Vec3 epa_perp(const Vec3& v) {
+    if (rabs(v.x) <= rabs(v.y) && rabs(v.x) <= rabs(v.z)) return Vec3(0.0f, -v.z, v.y);
+    if (rabs(v.y) <= rabs(v.z)) return Vec3(-v.z, 0.0f, v.x);
+    return Vec3(-v.y, v.x, 0.0f);
+}
+
+__device__ __forceinline__ bool tet_face_ok(const Vec3& a, const Vec3& b, const Vec3& c, const Vec3& d) {
+    Vec3 n = (b - a).cross(c - a);
+    if (n.dot(d - a) > 0.0f) n = -n;
+    return n.dot(Vec3() - a) < -1.0e-9f;
+}
+__device__ __forceinline__ bool origin_in_tetra(const SP* v) {
+    return tet_face_ok(v[0].p, v[1].p, v[2].p, v[3].p) && tet_face_ok(v[0].p, v[2].p, v[3].p, v[1].p) &&
+           tet_face_ok(v[0].p, v[3].p, v[1].p, v[2].p) && tet_face_ok(v[1].p, v[3].p, v[2].p, v[0].p);
+}
+
+__device__ inline bool epa_initial_tetra(const SupportMap& map, const GjkOut& g, SP* out) {
+    uint32_t n = 0;
+    for (uint32_t i = 0; i < g.ns && n < 4; ++i) {
+        bool dup = false;
+        for (uint32_t j = 0; j < n; ++j)
+            if ((out[j].p - g.simplex[i].p).len2() < 1.0e-12f) dup = true;
+        if (!dup) out[n++] = g.simplex[i];
+    }
+    if (n == 0) out[n++] = map(Vec3(1.0f, 0.0f, 0.0f));
+    if (n == 4 && !origin_in_tetra(out)) n = 3;
+    if (n == 1) {
+        out[n] = map(-out[0].p);
+        if ((out[1].p - out[0].p).len2() > 1.0e-12f) ++n;
+    }
+    if (n == 2) {
+        Vec3 ab = out[1].p - out[0].p;
+        if (ab.len2() > 1.0e-12f) {
+            Vec3 d1 = epa_perp(ab).normalized();
+            Vec3 d2 = ab.cross(d1).normalized();
+            SP k0 = out[0], k1 = out[1];
+            out[0] = map(d1);
+            out[1] = map(-d1);
+            out[2] = map(d2);
+            out[3] = map(-d2);
+            if (origin_in_tetra(out)) return true;
+            out[0] = k0;
+            out[1] = k1;
+        }
+        SP s = map(epa_perp(ab));
+        if ((s.p - out[0].p).len2() > 1.0e-12f && (s.p - out[1].p).len2() > 1.0e-12f) out[n++] = s;
+    }
+    if (n == 3) {
+        Vec3 tn = (out[1].p - out[0].p).cross(out[2].p - out[0].p);
+        float len = tn.len();
+        if (len > 1.0e-12f) {
+            tn = tn / len;
+            float sd = tn.dot(Vec3() - out[0].p);
+            SP a = map(sd > 0.0f ? -tn : tn);
+            SP b = map(sd > 0.0f ? tn : -tn);
+            out[3] = a;
+            if (!origin_in_tetra(out)) out[3] = b;
+            if (origin_in_tetra(out)) return true;
+        }
+        n = 3;
+    }
+    if (n == 4 && origin_in_tetra(out)) return true;
+
+    SP cand[16];
+    uint32_t nc = 0;
+    auto add = [&](const SP& sp) {
+        for (uint32_t i = 0; i < nc; ++i)
+            if ((cand[i].p - sp.p).len2() < 1.0e-12f) return;
+        if (nc < 16) cand[nc++] = sp;
+    };
+    for (uint32_t i = 0; i < g.ns && i < 4; ++i) add(g.simplex[i]);
+    const float s = 0.5773502692f;
+    const float D[14][3] = {{1, 0, 0},   {-1, 0, 0},  {0, 1, 0},  {0, -1, 0}, {0, 0, 1},  {0, 0, -1}, {s, s, s},
+                            {s, s, -s},  {s, -s, s},  {-s, s, s}, {-s, -s, s}, {-s, s, -s}, {s, -s, -s}, {-s, -s, -s}};
+    for (int i = 0; i < 14; ++i) add(map(Vec3(D[i][0], D[i][1], D[i][2])));
+    for (uint32_t i = 0; i + 3 < nc; ++i)
+        for (uint32_t j = i + 1; j + 2 < nc; ++j)
+            for (uint32_t k = j + 1; k + 1 < nc; ++k)
+                for (uint32_t l = k + 1; l < nc; ++l) {
+                    SP t[4] = {cand[i], cand[j], cand[k], cand[l]};
+                    float vol = (t[1].p - t[0].p).cross(t[2].p - t[0].p).dot(t[3].p - t[0].p);
+                    if (rabs(vol) < 1.0e-12f) continue;
+                    if (origin_in_tetra(t)) {
+                        for (int m = 0; m < 4; ++m) out[m] = t[m];
+                        return true;
+                    }
+                }
+    return false;
+}
+
+__device__ inline void epa_finish(const EpaFace& f, const SP* vs, EpaOut& r) {
+    Vec3 proj = f.n * f.dist;
+    Vec3 a = vs[f.a].p, b = vs[f.b].p, c = vs[f.c].p;
+    Vec3 v0 = b - a, v1 = c - a, v2 = proj - a;
+    float d00 = v0.dot(v0), d01 = v0.dot(v1), d11 = v1.dot(v1);
+    float d20 = v2.dot(v0), d21 = v2.dot(v1);
+    float denom = d00 * d11 - d01 * d01;
+    float u, v, w;
+    if (rabs(denom) < 1.0e-18f) { u = 1.0f; v = 0.0f; w = 0.0f; }
+    else {
+        v = rdiv(d11 * d20 - d01 * d21, denom);
+        w = rdiv(d00 * d21 - d01 * d20, denom);
+        u = 1.0f - v - w;
+    }
+    r.valid = true;
+    r.depth = f.dist;
+    r.normal = -f.n;
+    r.pA = (vs[f.a].pA * u + vs[f.b].pA * v) + vs[f.c].pA * w;
+    r.pB = (vs[f.a].pB * u + vs[f.b].pB * v) + vs[f.c].pB * w;
+}
+
+// Scratch for one EPA run (thread-local memory).
+struct EpaScratch {
+    SP verts[kEpaVerts];
+    EpaFace faces[kEpaFaces];
+    uint16_t vis[kEpaFaces];
+    uint8_t hu[kEpaHorizon], hv[kEpaHorizon];
+};
+
+__device__ inline void epa(const SupportMap& map, const GjkOut& g, float tol, uint32_t max_iter, EpaScratch& S,
+                           EpaOut& r, uint32_t* err) {
+    r.valid = false;
+    r.depth = 0.0f;
+    r.normal = Vec3(0.0f, 1.0f, 0.0f);
+    r.pA = r.pB = Vec3();
+    SP tet[4];
+    if (!epa_initial_tetra(map, g, tet)) return;
+    uint32_t nv = 0;
+    for (int i = 0; i < 4; ++i) S.verts[nv++] = tet[i];
+    uint32_t nf = 0;
+    const uint8_t T4[4][3] = {{0, 1, 2}, {0, 2, 3}, {0, 3, 1}, {1, 3, 2}};
+    for (int i = 0; i < 4; ++i) {
+        EpaFace f{T4[i][0], T4[i][1], T4[i][2], Vec3(0.0f, 1.0f, 0.0f), 0.0f, 1u};
+        if (epa_build_face(f, S.verts)) S.faces[nf++] = f;
+    }
+    if (nf < 4) return;
+    const float eps = tol;
+    for (uint32_t it = 0; it < max_iter; ++it) {
+        float bd = INFINITY;
+        uint32_t bf = 0xFFFFFFFFu;
+        for (uint32_t i = 0; i < nf; ++i)
+            if (S.faces[i].alive && S.faces[i].dist < bd) { bd = S.faces[i].dist; bf = i; }
+        if (bf == 0xFFFFFFFFu) break;
+        EpaFace face = S.faces[bf];
+        SP w = map(face.n);
+        float d = w.p.dot(face.n);
+        if (d - face.dist < eps || nv >= 256) {
+            epa_finish(face, S.verts, r);
+            return;
+        }
+        if (nv >= kEpaVerts) {  // unreachable with max_iter <= 64
+            atomicOr(err, 4u);
+            epa_finish(face, S.verts, r);
+            return;
+        }
+        uint32_t ni = nv;
+        S.verts[nv++] = w;
+        uint32_t nvis = 0;
+        for (uint32_t i = 0; i < nf; ++i)
+            if (S.faces[i].alive && S.faces[i].n.dot(w.p) - S.faces[i].dist > eps) {
+                S.faces[i].alive = 0;
+                S.vis[nvis++] = (uint16_t)i;
+            }
+        uint32_t nh = 0;
+        for (uint32_t vi = 0; vi < nvis; ++vi) {
+            const EpaFace& fi = S.faces[S.vis[vi]];
+            uint32_t ev[3][2] = {{fi.a, fi.b}, {fi.b, fi.c}, {fi.c, fi.a}};
+            for (int e = 0; e < 3; ++e) {
+                bool shared = false;
+                for (uint32_t vj = 0; vj < nvis && !shared; ++vj) {
+                    if (vj == vi) continue;
+                    const EpaFace& fj = S.faces[S.vis[vj]];
+                    if ((fj.a == ev[e][1] && fj.b == ev[e][0]) || (fj.b == ev[e][1] && fj.c == ev[e][0]) ||
+                        (fj.c == ev[e][1] && fj.a == ev[e][0]))
+                        shared = true;
+                }
+                if (!shared && nh < kEpaHorizon) {
+                    S.hu[nh] = (uint8_t)ev[e][0];
+                    S.hv[nh] = (uint8_t)ev[e][1];
+                    ++nh;
+                }
+            }
+        }
+        uint32_t wi = 0;
+        for (uint32_t i = 0; i < nf; ++i)
+            if (S.faces[i].alive) S.faces[wi++] = S.faces[i];
+        nf = wi;
+        for (uint32_t i = 0; i < nh; ++i) {
+            if (nf >= kEpaFaces) break;
+            EpaFace f{S.hv[i], S.hu[i], ni, Vec3(0.0f, 1.0f, 0.0f), 0.0f, 1u};
+            if (epa_build_face(f, S.verts)) S.faces[nf++] = f;
+        }
+    }
+    float bd = INFINITY;
+    uint32_t bf = 0xFFFFFFFFu;
+    for (uint32_t i = 0; i < nf; ++i)
+        if (S.faces[i].alive && S.faces[i].dist < bd) { bd = S.faces[i].dist; bf = i; }
+    if (bf != 0xFFFFFFFFu) epa_finish(S.faces[bf], S.verts, r);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Face clipping (CollideShape.cpp:30-228)
+// ---------------------------------------------------------------------------------------------
+constexpr uint32_t kMaxFaceVerts = 16;
+
+__device__ inline bool shape_face(const ShapeTables& T, const Body& b, const Vec3& wdir, Vec3* out, uint32_t& cnt,
+                                  Vec3& nworld) {
+    const ShapeDev* s = b.s;
+    if (s->type == kBox) {
+        Vec3 ld = b.q.inv_rotate(wdir);
+        int axis = ld.abs().max_comp_index();
+        float sg = ld[axis] >= 0.0f ? 1.0f : -1.0f;
+        Vec3 he(s->p[0], s->p[1], s->p[2]);
+        Vec3 n;
+        n.set(axis, sg);
+        Vec3 c(he.x * n.x, he.y * n.y, he.z * n.z);
+        int a0 = (axis + 1) % 3, a1 = (axis + 2) % 3;
+        float s0 = he[a0], s1 = he[a1];
+        Vec3 cr[4] = {c, c, c, c};
+        cr[0].set(a0, s0); cr[0].set(a1, s1);
+        cr[1].set(a0, -s0); cr[1].set(a1, s1);
+        cr[2].set(a0, -s0); cr[2].set(a1, -s1);
+        cr[3].set(a0, s0); cr[3].set(a1, -s1);
+        for (int i = 0; i < 4; ++i) out[i] = xform(b.q, b.t, cr[i]);
+        cnt = 4;
+        nworld = b.q.rotate(n);
+        return true;
+    }
+    if (s->type == kHull) {
+        Vec3 ld = b.q.inv_rotate(wdir);
+        float bd = -INFINITY;
+        uint32_t bf = 0xFFFFFFFFu, boff = 0;
+        uint32_t off = s->ifirst;
+        for (uint32_t fi = 0; fi < s->fnum; ++fi) {
+            uint32_t n = T.face_sizes[s->ffirst + fi];
+            Vec3 a = hv(T, s->vfirst + T.face_idx[off]), bb = hv(T, s->vfirst + T.face_idx[off + 1]),
+                 c = hv(T, s->vfirst + T.face_idx[off + 2]);
+            Vec3 fn = (bb - a).cross(c - a).normalized_or(Vec3(0.0f, 1.0f, 0.0f));
+            float d = fn.dot(ld);
+            if (d > bd) { bd = d; bf = fi; boff = off; }
+            off += n;
+        }
+        if (bf == 0xFFFFFFFFu) return false;
+        uint32_t n = T.face_sizes[s->ffirst + bf];
+        if (n > kMaxFaceVerts) n = kMaxFaceVerts;
+        for (uint32_t i = 0; i < n; ++i) out[i] = xform(b.q, b.t, hv(T, s->vfirst + T.face_idx[boff + i]));
+        cnt = n;
+        Vec3 a = hv(T, s->vfirst + T.face_idx[boff]), bb = hv(T, s->vfirst + T.face_idx[boff + 1]),
+             c = hv(T, s->vfirst + T.face_idx[boff + 2]);
+        nworld = b.q.rotate((bb - a).cross(c - a).normalized_or(Vec3(0.0f, 1.0f, 0.0f)));
+        return true;
+    }
+    return false;
+}
+
+struct ClipPoly {
+    Vec3 v[kMaxFaceVerts * 2];
+    uint32_t n;
+    __device__ void add(const Vec3& p) {
+        if (n < kMaxFaceVerts * 2) v[n++] = p;
+    }
+};
+
+__device__ inline void clip_plane(const ClipPoly& in, const Vec3& pn, float pd, ClipPoly& out) {
+    out.n = 0;
+    if (in.n == 0) return;
+    for (uint32_t i = 0; i < in.n; ++i) {
+        Vec3 cur = in.v[i], nxt = in.v[(i + 1) % in.n];
+        float dc = pn.dot(cur) - pd, dn = pn.dot(nxt) - pd;
+        if (dc <= 0.0f) out.add(cur);
+        if ((dc <= 0.0f) != (dn <= 0.0f)) {
+            float t = rdiv(dc, dc - dn);
+            out.add(lerp(cur, nxt, t));
+        }
+    }
+}
+
+__device__ inline bool is_poly(const ShapeDev* s) { return s->type == kBox || s->type == kHull; }
+
+// Writes at most kMaxFaceVerts*2 candidate points before reduction; keeps the reference's
+// (i*(n-1)/3) reduction of more than four points.
+__device__ inline uint32_t collide_polyhedral(const ShapeTables& T, const Body& A, const Body& B, float max_sep,
+                                              Manifold& m, const Vec3& normal) {
+    Vec3 fa[kMaxFaceVerts], fb[kMaxFaceVerts], na, nb;
+    uint32_t ca = 0, cb = 0;
+    bool ha = shape_face(T, A, -normal, fa, ca, na);
+    bool hb = shape_face(T, B, normal, fb, cb, nb);
+    if (!ha || !hb) return 0;
+    float ala = na.dot(-normal), alb = nb.dot(normal);
+    const bool ref_a = ala >= alb;
+    const Vec3* rv = ref_a ? fa : fb;
+    const Vec3* iv = ref_a ? fb : fa;
+    const uint32_t rc = ref_a ? ca : cb, ic = ref_a ? cb : ca;
+    Vec3 rn = ref_a ? na : nb;
+    float rd = rn.dot(rv[0]);
+    ClipPoly poly, tmp;
+    poly.n = 0;
+    for (uint32_t i = 0; i < ic; ++i) poly.add(iv[i]);
+    Vec3 cen;
+    for (uint32_t i = 0; i < rc; ++i) cen = cen + rv[i];
+    cen = cen / (float)rc;
+    for (uint32_t i = 0; i < rc; ++i) {
+        Vec3 v0 = rv[i], v1 = rv[(i + 1) % rc];
+        Vec3 sn = (v1 - v0).cross(rn);
+        float len = sn.len();
+        if (len < 1.0e-9f) continue;
+        sn = sn / len;
+        if (sn.dot(v0 - cen) < 0.0f) sn = -sn;
+        float sd = sn.dot(v0);
+        clip_plane(poly, sn, sd, tmp);
+        poly = tmp;
+        if (poly.n == 0) break;
+    }
+    // Keep-list of up to 8 candidates (kMaxManifoldPoints), then reduce to 4.
+    ContactPt cand[8];
+    uint32_t nc = 0;
+    for (uint32_t i = 0; i < poly.n && nc < 8; ++i) {
+        Vec3 p = poly.v[i];
+        float sep = rn.dot(p) - rd;
+        if (sep > max_sep) continue;
+        Vec3 proj = p - rn * sep;
+        cand[nc].pA = ref_a ? proj : p;
+        cand[nc].pB = ref_a ? p : proj;
+        cand[nc].n = normal;
+        cand[nc].sep = sep;
+        cand[nc].feature = i;
+        ++nc;
+    }
+    if (nc > 4) {
+        for (uint32_t i = 0; i < 4; ++i) m.pts[i] = cand[i * (nc - 1) / 3];
+        nc = 4;
+    } else {
+        for (uint32_t i = 0; i < nc; ++i) m.pts[i] = cand[i];
+    }
+    m.n = nc;
+    return nc;
+}
+
+__device__ __forceinline__ void add_point(Manifold& m, const Vec3& pA, const Vec3& pB, const Vec3& n, float sep) {
+    if (m.n < kMaxManifold) {
+        ContactPt& c = m.pts[m.n++];
+        c.pA = pA; c.pB = pB; c.n = n; c.sep = sep; c.feature = 0;
+    }
+}
+
+__device__ __forceinline__ void swap_manifold(Manifold& m) {
+    for (uint32_t i = 0; i < m.n; ++i) {
+        Vec3 t = m.pts[i].pA;
+        m.pts[i].pA = m.pts[i].pB;
+        m.pts[i].pB = t;
+        m.pts[i].n = -m.pts[i].n;
+    }
+}
+
+__device__ inline uint32_t collide_generic(const ShapeTables& T, const Body& A, const Body& B, float max_sep, float tol,
+                                           Manifold& m, EpaScratch& S, uint32_t* err) {
+    SupportMap map{&T, A, B};
+    GjkOut g;
+    gjk(map, tol, 32, g);
+    const bool poly = is_poly(A.s) && is_poly(B.s);
+    if (!g.intersect) {
+        if (g.distance > max_sep) return 0;
+        if (poly && g.normal.len2() > 0.0f) {
+            if (collide_polyhedral(T, A, B, max_sep, m, g.normal) > 0) return m.n;
+        }
+        add_point(m, g.pA, g.pB, g.normal, g.distance);
+        return m.n;
+    }
+    EpaOut e;
+    if (poly) {
+        epa(map, g, tol, 64, S, e, err);
+        if (e.valid) {
+            if (collide_polyhedral(T, A, B, max_sep, m, e.normal) > 0) return m.n;
+            add_point(m, e.pA, e.pB, e.normal, -e.depth);
+            return m.n;
+        }
+    }
+    epa(map, g, tol, 64, S, e, err);
+    if (e.valid) {
+        add_point(m, e.pA, e.pB, e.normal, -e.depth);
+        return m.n;
+    }
+    add_point(m, g.pA, g.pB, g.normal.len2() > 0.0f ? g.normal : Vec3(0.0f, 1.0f, 0.0f), 0.0f);
+    return m.n;
+}
+
+__device__ inline uint32_t collide_sphere_convex(const ShapeTables& T, const Body& S_, const Body& B, float max_sep,
+                                                 float tol, Manifold& m, EpaScratch& S, uint32_t* err) {
+    ShapeDev point{};
+    point.type = kSphere;
+    point.p[0] = 1.0e-4f;
+    Body P{&point, S_.q, S_.t};
+    SupportMap map{&T, P, B};
+    GjkOut g;
+    gjk(map, tol, 32, g);
+    const float radius = S_.s->p[0];
+    const Vec3 center = S_.t;
+    if (g.intersect) {
+        EpaOut e;
+        epa(map, g, tol, 64, S, e, err);
+        if (e.valid) {
+            Vec3 n = -e.normal;
+            add_point(m, center + n * radius, e.pB, n, -(e.depth + radius));
+            return m.n;
+        }
+        return 0;
+    }
+    float dist = g.distance;
+    float sep = dist - radius;
+    if (sep > max_sep) return 0;
+    Vec3 n = (dist > kEps) ? (center - g.pB) / dist : Vec3(0.0f, 1.0f, 0.0f);
+    add_point(m, center - n * radius, g.pB, n, sep);
+    return m.n;
+}
+
+__device__ inline uint32_t collide_sphere_sphere(const Body& A, const Body& B, float max_sep, Manifold& m) {
+    Vec3 d = A.t - B.t;
+    float dist = d.len();
+    float sep = dist - (A.s->p[0] + B.s->p[0]);
+    if (sep > max_sep) return 0;
+    Vec3 n = dist > kEps ? d / dist : Vec3(0.0f, 1.0f, 0.0f);
+    add_point(m, A.t - n * A.s->p[0], B.t + n * B.s->p[0], n, sep);
+    return m.n;
+}
+
+__device__ inline uint32_t collide_plane_convex(const ShapeTables& T, const Body& P, const Body& B, float max_sep,
+                                                Manifold& m) {
+    Vec3 pn = P.q.rotate(Vec3(P.s->p[0], P.s->p[1], P.s->p[2]));
+    float pd = P.s->p[3] + pn.dot(P.t);
+    if (is_poly(B.s)) {
+        ContactPt cand[8];
+        uint32_t count = 0;
+        const uint32_t nverts = B.s->type == kBox ? 8u : (B.s->vnum < kMaxFaceVerts ? B.s->vnum : kMaxFaceVerts);
+        for (uint32_t i = 0; i < nverts && count < 8; ++i) {
+            Vec3 v;
+            if (B.s->type == kBox) {
+                Vec3 he(B.s->p[0], B.s->p[1], B.s->p[2]);
+                v = xform(B.q, B.t, Vec3((i & 1) ? he.x : -he.x, (i & 2) ? he.y : -he.y, (i & 4) ? he.z : -he.z));
+            } else {
+                v = xform(B.q, B.t, hv(T, B.s->vfirst + i));
+            }
+            float d = pn.dot(v) - pd;
+            if (d > max_sep) continue;
+            cand[count].n = pn;
+            cand[count].pA = v;
+            cand[count].pB = v - pn * d;
+            cand[count].sep = d;
+            cand[count].feature = 0;
+            ++count;
+        }
+        if (count > 4) {
+            for (uint32_t i = 0; i < 4; ++i) m.pts[i] = cand[i * (count - 1) / 3];
+            count = 4;
+        } else {
+            for (uint32_t i = 0; i < count; ++i) m.pts[i] = cand[i];
+        }
+        m.n = count;
+        return count;
+    }
+    Vec3 ld = B.q.inv_rotate(-pn);
+    Vec3 deep = xform(B.q, B.t, support_local(T, B.s, ld));
+    float d = pn.dot(deep) - pd;
+    if (d > max_sep) return 0;
+    add_point(m, deep, deep - pn * d, pn, d);
+    return m.n;
+}
+
+// NarrowPhase::Collide dispatch (CollideShape.cpp:480-592) for the device shape set.
+__device__ inline uint32_t collide(const ShapeTables& T, const Body& A, const Body& B, float max_sep, float tol,
+                                   Manifold& m, EpaScratch& S, uint32_t* err) {
+    m.n = 0;
+    const uint32_t ta = A.s->type, tb = B.s->type;
+    if (ta == kPlane) {
+        uint32_t n = collide_plane_convex(T, A, B, max_sep, m);
+        if (n > 0) swap_manifold(m);
+        return n;
+    }
+    if (tb == kPlane) return collide_plane_convex(T, B, A, max_sep, m);
+    if (ta == kSphere && tb == kSphere) return collide_sphere_sphere(A, B, max_sep, m);
+    if (ta == kSphere) return collide_sphere_convex(T, A, B, max_sep, tol, m, S, err);
+    if (tb == kSphere) {
+        uint32_t n = collide_sphere_convex(T, B, A, max_sep, tol, m, S, err);
+        if (n > 0) swap_manifold(m);
+        return n;
+    }
+    return collide_generic(T, A, B, max_sep, tol, m, S, err);
+}
+
+}  // namespace kzg

@@ -1,0 +1,996 @@
+// kzg_step.cu - the per-step contact pipeline on the GPU (PhysicsWorld::StepFixed,
+// reference src/World/PhysicsWorld.cpp:245-329), kernel by kernel:
+//
+//   broad phase      k_aabb, cell sort, k_find_pairs, pair-key sort   (canonical MakePairKey order)
+//   narrow phase     k_narrow: one thread per pair                    (Collide, :350-400)
+//   constraints      k_con_flags, scan, k_build_constraints           (BuildContactConstraints, :454-535)
+//   velocities       k_integrate_vel                                  (IntegrateVelocities, :757-783)
+//   prepare          k_prepare: one thread per contact point row      (ContactSolver::PrepareConstraint)
+//   islands          union-find k_uf_*, stable sort by island         (BuildIslands, :587-664)
+//   schedule         k_schedule: one thread per island builds the reference's greedy 4-wide
+//                    batches (:680-717) and the dependency levels of the warm-start, velocity
+//                    and bias sweeps
+//   solve            k_solve: one CTA per island sweeps level by level (SolveIsland, :666-743)
+//   cache store      k_cache_store                                    (:568-581)
+//   positions        k_integrate_pos: positions, pseudo velocities, world inertia, force clear
+//
+// Floating point follows the reference op for op (kzg_math.cuh), so with the same pair order the
+// result is bit-identical to the reference; levels only reorder work between bodies that share
+// no dynamic body, which cannot change any value.
+#include <cub/cub.cuh>
+
+#include "kzg_ctx.h"
+#include "kzg_internal.h"
+
+namespace kzg {
+
+// ---------------------------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ Vec3 V3(float4 a) { return Vec3(a.x, a.y, a.z); }
+__device__ __forceinline__ float4 F4(const Vec3& v, float w) { return make_float4(v.x, v.y, v.z, w); }
+__device__ __forceinline__ Quat Q4(float4 a) { return Quat(a.x, a.y, a.z, a.w); }
+__device__ __forceinline__ float4 F4q(const Quat& q) { return make_float4(q.x, q.y, q.z, q.w); }
+__device__ __forceinline__ Mat3 M3(const float4* c) { return Mat3{V3(c[0]), V3(c[1]), V3(c[2])}; }
+__device__ __forceinline__ unsigned long long pair_key(uint32_t pa, uint32_t pb) {
+    if (pa > pb) { uint32_t t = pa; pa = pb; pb = t; }
+    return ((unsigned long long)pa << 32) | (unsigned long long)pb;
+}
+__device__ __forceinline__ uint32_t hash_key(unsigned long long k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return (uint32_t)k;
+}
+
+constexpr uint32_t kInvalid = 0xFFFFFFFFu;
+constexpr int kThreads = 256;
+inline unsigned blocks_for(uint32_t n, int t = kThreads) { return (unsigned)((n + t - 1) / t); }
+
+// ---------------------------------------------------------------------------------------------
+// broad phase
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t cell_coord(float c, float inv_cell) {
+    float f = floorf(c * inv_cell);
+    f = fminf(fmaxf(f, -32000.0f), 32000.0f);
+    return (uint32_t)((int)f + 32768);
+}
+__device__ __forceinline__ unsigned long long cell_key(uint32_t world, uint32_t ix, uint32_t iy, uint32_t iz) {
+    return ((unsigned long long)(world & 0xFFFFu) << 48) | ((unsigned long long)ix << 32) |
+           ((unsigned long long)iy << 16) | (unsigned long long)iz;
+}
+
+// Tight world AABB of every body (Shape::GetWorldBounds = local bounds transformed, Math.cpp:176)
+// and its grid cell key; bodies that bypass the grid get key ~0.
+__global__ void k_aabb(DeviceBodies b, const ShapeDev* __restrict__ shapes, uint32_t n, float inv_cell,
+                       const uint8_t* __restrict__ is_large, unsigned long long* keys, uint32_t* vals) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ShapeDev& s = shapes[b.shape[i]];
+    AABB local{Vec3(s.lmn[0], s.lmn[1], s.lmn[2]), Vec3(s.lmx[0], s.lmx[1], s.lmx[2])};
+    AABB w = aabb_transformed(local, Q4(b.rot[i]), V3(b.pos[i]));
+    b.aabb_mn[i] = F4(w.mn, 0.0f);
+    b.aabb_mx[i] = F4(w.mx, 0.0f);
+    unsigned long long key = ~0ull;
+    if (!is_large[i]) {
+        Vec3 c = (w.mn + w.mx) * 0.5f;
+        key = cell_key(b.world[i], cell_coord(c.x, inv_cell), cell_coord(c.y, inv_cell), cell_coord(c.z, inv_cell));
+    }
+    keys[i] = key;
+    vals[i] = i;
+}
+
+__device__ __forceinline__ bool pair_ok(const DeviceBodies& b, uint32_t i, uint32_t j) {
+    if ((b.layer[i] & b.mask[j]) == 0u || (b.layer[j] & b.mask[i]) == 0u) return false;
+    AABB A{V3(b.aabb_mn[i]), V3(b.aabb_mx[i])}, B{V3(b.aabb_mn[j]), V3(b.aabb_mx[j])};
+    return aabb_overlaps(A, B);
+}
+
+__device__ __forceinline__ void emit_pair(unsigned long long* out, Counters* cnt, uint32_t cap, uint32_t pi, uint32_t pj) {
+    uint32_t slot = atomicAdd(&cnt->npairs, 1u);
+    if (slot < cap) out[slot] = pair_key(pi, pj);
+    else atomicOr(&cnt->error, KZG_DEVERR_PAIRS);
+}
+
+// Every overlapping pair exactly once (BroadPhase::UpdatePairs semantics: layer filter both ways,
+// tight AABB overlap with <=).  Grid bodies query the 27 neighbouring cells for partners with a
+// larger packed id; large bodies (planes) are tested against every body of their world.
+__global__ void k_find_pairs(DeviceBodies b, uint32_t n, const unsigned long long* __restrict__ skeys,
+                             const uint32_t* __restrict__ svals, uint32_t nsmall, float inv_cell,
+                             const uint8_t* __restrict__ is_large, const uint32_t* __restrict__ large_list,
+                             const uint32_t* __restrict__ large_off, uint32_t nworld_large, unsigned long long* out,
+                             Counters* cnt, uint32_t cap) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t pi = b.packed[i];
+    const uint32_t wi = b.world[i];
+    // large bodies of this world
+    if (wi < nworld_large) {
+        for (uint32_t k = large_off[wi]; k < large_off[wi + 1]; ++k) {
+            uint32_t j = large_list[k];
+            if (j == i) continue;
+            if (is_large[i] && b.packed[j] <= pi) continue;  // large-large: owned by the lower id
+            if (pair_ok(b, i, j)) emit_pair(out, cnt, cap, pi, b.packed[j]);
+        }
+    }
+    if (is_large[i]) return;
+    Vec3 c = (V3(b.aabb_mn[i]) + V3(b.aabb_mx[i])) * 0.5f;
+    int ix = (int)cell_coord(c.x, inv_cell), iy = (int)cell_coord(c.y, inv_cell), iz = (int)cell_coord(c.z, inv_cell);
+    for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dz = -1; dz <= 1; ++dz) {
+                unsigned long long key = cell_key(wi, (uint32_t)(ix + dx), (uint32_t)(iy + dy), (uint32_t)(iz + dz));
+                // lower_bound
+                uint32_t lo = 0, hi = nsmall;
+                while (lo < hi) {
+                    uint32_t mid = (lo + hi) >> 1;
+                    if (skeys[mid] < key) lo = mid + 1; else hi = mid;
+                }
+                for (uint32_t s = lo; s < nsmall && skeys[s] == key; ++s) {
+                    uint32_t j = svals[s];
+                    if (b.packed[j] <= pi) continue;
+                    if (pair_ok(b, i, j)) emit_pair(out, cnt, cap, pi, b.packed[j]);
+                }
+            }
+}
+
+__global__ void k_unpack_pairs(const unsigned long long* __restrict__ keys, const Counters* cnt, uint2* pairs) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cnt->npairs) return;
+    unsigned long long k = keys[i];
+    pairs[i] = make_uint2((uint32_t)(k >> 32) & 0x00FFFFFFu, (uint32_t)k & 0x00FFFFFFu);
+}
+
+// Caller-supplied pairs (packed BodyIDs, broad-phase order) -> slots; stale ids become invalid.
+__global__ void k_pairs_from_packed(const uint32_t* __restrict__ packed_pairs, uint32_t np, DeviceBodies b, uint32_t nb,
+                                    uint2* pairs) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    uint32_t pa = packed_pairs[2 * i], pb = packed_pairs[2 * i + 1];
+    uint32_t sa = pa & 0x00FFFFFFu, sb = pb & 0x00FFFFFFu;
+    bool ok = sa < nb && sb < nb && b.packed[sa] == pa && b.packed[sb] == pb;
+    pairs[i] = ok ? make_uint2(sa, sb) : make_uint2(kInvalid, kInvalid);
+}
+
+// ---------------------------------------------------------------------------------------------
+// narrow phase (PhysicsWorld::Collide, :366-393)
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_narrow(ShapeTables T, DeviceBodies b, const uint2* __restrict__ pairs,
+                                                const Counters* cnt, uint32_t* m_count, float4* m_data,
+                                                unsigned long long* m_key, uint32_t* err) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cnt->npairs) return;
+    uint2 pr = pairs[i];
+    m_count[i] = 0;
+    m_key[i] = 0;
+    if (pr.x == kInvalid) return;
+    const uint32_t A = pr.x, B = pr.y;
+    if (b.motion[A] != KZG_MOTION_DYNAMIC && b.motion[B] != KZG_MOTION_DYNAMIC) return;
+    const uint32_t pa = b.packed[A], pb = b.packed[B];
+    const bool swapped = pa > pb;
+    const uint32_t f = swapped ? B : A, s = swapped ? A : B;
+    Body BA{&T.shapes[b.shape[f]], Q4(b.rot[f]), V3(b.pos[f])};
+    Body BB{&T.shapes[b.shape[s]], Q4(b.rot[s]), V3(b.pos[s])};
+    Manifold m;
+    EpaScratch S;
+    collide(T, BA, BB, 0.02f, 1.0e-4f, m, S, err);
+    if (swapped) swap_manifold(m);
+    m_key[i] = pair_key(pa, pb);
+    m_count[i] = m.n;
+    float4* o = m_data + 12ull * i;
+    for (uint32_t k = 0; k < m.n; ++k) {
+        o[3 * k + 0] = F4(m.pts[k].pA, m.pts[k].sep);
+        o[3 * k + 1] = F4(m.pts[k].pB, __uint_as_float(m.pts[k].feature));
+        o[3 * k + 2] = F4(m.pts[k].n, 0.0f);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// constraints + warm start from the cache (BuildContactConstraints, :454-535)
+// ---------------------------------------------------------------------------------------------
+__global__ void k_con_flags(const uint32_t* __restrict__ m_count, const unsigned long long* __restrict__ m_key,
+                            const Counters* cnt, uint32_t* flag) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cnt->npairs) return;
+    flag[i] = (m_count[i] != 0u && m_key[i] != 0ull) ? 1u : 0u;
+}
+
+__device__ inline int cache_find(const unsigned long long* __restrict__ keys, uint32_t cap, unsigned long long key) {
+    uint32_t mask = cap - 1u;
+    uint32_t slot = hash_key(key) & mask;
+    for (uint32_t p = 0; p < cap; ++p) {
+        unsigned long long k = keys[slot];
+        if (k == key) return (int)slot;
+        if (k == 0ull) return -1;
+        slot = (slot + 1u) & mask;
+    }
+    return -1;
+}
+
+__global__ void k_build_constraints(const uint2* __restrict__ pairs, const uint32_t* __restrict__ flag,
+                                    const uint32_t* __restrict__ cidx, const uint32_t* __restrict__ m_count,
+                                    const float4* __restrict__ m_data, const unsigned long long* __restrict__ m_key,
+                                    DeviceBodies b, Counters* cnt, uint32_t* con_pair, uint32_t* con_a, uint32_t* con_b,
+                                    uint32_t* con_np, uint32_t* con_bits, float2* con_fr,
+                                    unsigned long long* con_key, DeviceRows r, const unsigned long long* __restrict__ c_key,
+                                    const uint32_t* __restrict__ c_np, const float4* __restrict__ c_pos,
+                                    const float4* __restrict__ c_imp, uint32_t c_cap, int warm) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t np = cnt->npairs;
+    if (i >= np) return;
+    if (i == np - 1) cnt->ncons = cidx[i] + flag[i];
+    if (!flag[i]) return;
+    uint32_t c = cidx[i];
+    uint32_t A = pairs[i].x, B = pairs[i].y;
+    if (b.packed[A] > b.packed[B]) { uint32_t t = A; A = B; B = t; }
+    con_pair[c] = i;
+    con_a[c] = A;
+    con_b[c] = B;
+    uint32_t n = m_count[i];
+    con_np[c] = n;
+    unsigned long long key = m_key[i];
+    con_key[c] = key;
+    const bool sensor = ((b.flags[A] | b.flags[B]) & KZG_BODY_SENSOR) != 0u;
+    const float fr = rsqrt_ieee(b.prm1[A].y * b.prm1[B].y);
+    const float rs = rmax(b.prm1[A].z, b.prm1[B].z);
+    con_fr[c] = make_float2(fr, rs);
+    con_bits[c] = (sensor ? 1u : 0u) | (b.motion[A] == KZG_MOTION_DYNAMIC ? 2u : 0u) |
+                  (b.motion[B] == KZG_MOTION_DYNAMIC ? 4u : 0u);
+    int slot = warm ? cache_find(c_key, c_cap, key) : -1;
+    const float4* md = m_data + 12ull * i;
+    for (uint32_t p = 0; p < n; ++p) {
+        uint32_t row = 4u * c + p;
+        float4 pA = md[3 * p], pB = md[3 * p + 1], nn = md[3 * p + 2];
+        r.pA[row] = pA;
+        r.pB[row] = pB;
+        r.n[row] = make_float4(nn.x, nn.y, nn.z, rs);
+        r.t1[row] = make_float4(0.0f, 0.0f, 0.0f, fr);
+        float ni = 0.0f, t1 = 0.0f, t2 = 0.0f;
+        if (slot >= 0) {
+            float best = 0.10f * 0.10f;
+            uint32_t bi = kInvalid;
+            uint32_t cn = c_np[slot];
+            Vec3 pa = V3(pA);
+            for (uint32_t k = 0; k < cn; ++k) {
+                float d = (V3(c_pos[4u * slot + k]) - pa).len2();
+                if (d < best) { best = d; bi = k; }
+            }
+            if (bi != kInvalid) {
+                float4 im = c_imp[4u * slot + bi];
+                ni = im.x; t1 = im.y; t2 = im.z;
+            }
+        }
+        r.imp[row] = make_float4(ni, t1, t2, 0.0f);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// IntegrateVelocities (:757-783)
+// ---------------------------------------------------------------------------------------------
+__global__ void k_integrate_vel(DeviceBodies b, uint32_t n, float3 g, float dt) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || b.motion[i] != KZG_MOTION_DYNAMIC) return;
+    float4 p0 = b.prm0[i], p1 = b.prm1[i];
+    float im = b.inv_mass[i];
+    Vec3 lv = V3(b.lv[i]), av = V3(b.av[i]);
+    Vec3 acc = Vec3(g.x, g.y, g.z) * p0.z + V3(b.force[i]) * im;
+    lv = lv + acc * dt;
+    av = av + (M3(&b.iiw[3 * i]) * V3(b.torque[i])) * dt;
+    lv = lv * rdiv(1.0f, 1.0f + p0.x * dt);
+    av = av * rdiv(1.0f, 1.0f + p0.y * dt);
+    lv = clamp_length(lv, p0.w);
+    av = clamp_length(av, p1.x);
+    if (!lv.finite() || !av.finite()) { lv = Vec3(); av = Vec3(); }
+    b.lv[i] = F4(lv, 0.0f);
+    b.av[i] = F4(av, 0.0f);
+}
+
+// ---------------------------------------------------------------------------------------------
+// PrepareConstraint (ContactSolver.cpp:56-112), one thread per point row
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ float eff_mass(float imA, float imB, const Mat3& IA, const Mat3& IB, const Vec3& rA,
+                                          const Vec3& rB, const Vec3& d) {
+    Vec3 ra = rA.cross(d), rb = rB.cross(d);
+    float k = imA + imB;
+    k += ra.dot(IA * ra);
+    k += rb.dot(IB * rb);
+    return k > kEps ? rdiv(1.0f, k) : 0.0f;
+}
+
+struct PrepParams {
+    float dt, baumgarte, slop, rest_thresh, max_bias;
+};
+
+__global__ void k_prepare(DeviceBodies b, const Counters* cnt, const uint32_t* __restrict__ con_a,
+                          const uint32_t* __restrict__ con_b, const uint32_t* __restrict__ con_np, DeviceRows r,
+                          PrepParams pp) {
+    uint32_t row = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t c = row >> 2, p = row & 3u;
+    if (c >= cnt->ncons || p >= con_np[c]) return;
+    const uint32_t A = con_a[c], B = con_b[c];
+    const Vec3 posA = V3(b.pos[A]), posB = V3(b.pos[B]);
+    const Quat qA = Q4(b.rot[A]), qB = Q4(b.rot[B]);
+    float4 pA4 = r.pA[row], pB4 = r.pB[row], n4 = r.n[row], t14 = r.t1[row], imp = r.imp[row];
+    const Vec3 pA = V3(pA4), pB = V3(pB4);
+    const float sep = pA4.w, rest = n4.w, fric = t14.w;
+    Vec3 rA = pA - posA, rB = pB - posB;
+    Vec3 laA = qA.inv_rotate(rA), laB = qB.inv_rotate(rB);
+    Vec3 n = V3(n4).normalized_or(Vec3(0.0f, 1.0f, 0.0f));
+    Vec3 t1 = n.perp_normalized();
+    Vec3 t2 = n.cross(t1);
+    const float imA = b.inv_mass[A], imB = b.inv_mass[B];
+    const Mat3 IA = M3(&b.iiw[3 * A]), IB = M3(&b.iiw[3 * B]);
+    float nm = eff_mass(imA, imB, IA, IB, rA, rB, n);
+    float tm1 = eff_mass(imA, imB, IA, IB, rA, rB, t1);
+    float tm2 = eff_mass(imA, imB, IA, IB, rA, rB, t2);
+    Vec3 vA = V3(b.lv[A]) + V3(b.av[A]).cross(pA - posA);
+    Vec3 vB = V3(b.lv[B]) + V3(b.av[B]).cross(pB - posB);
+    float nvel = (vA - vB).dot(n);
+    float rbias = 0.0f;
+    if (nvel < -pp.rest_thresh) rbias = -rest * nvel;
+    float pbias = 0.0f;
+    if (sep < -pp.slop) {
+        pbias = rdiv(pp.baumgarte, pp.dt) * (-sep - pp.slop);
+        pbias = rmin(pbias, pp.max_bias);
+    }
+    float mf = fric * imp.x;
+    float ti1 = rclamp(imp.y, -mf, mf), ti2 = rclamp(imp.z, -mf, mf);
+    float ni = rmax(imp.x, 0.0f);
+    r.n[row] = F4(n, rest);
+    r.t1[row] = F4(t1, fric);
+    r.t2[row] = F4(t2, 0.0f);
+    r.rA[row] = F4(rA, 0.0f);
+    r.rB[row] = F4(rB, 0.0f);
+    r.laA[row] = F4(laA, 0.0f);
+    r.laB[row] = F4(laB, 0.0f);
+    r.rAr[row] = F4(qA.rotate(laA), 0.0f);
+    r.rBr[row] = F4(qB.rotate(laB), 0.0f);
+    r.mass[row] = make_float4(nm, tm1, tm2, 0.0f);
+    r.imp[row] = make_float4(ni, ti1, ti2, 0.0f);
+    r.bias[row] = make_float4(rbias, pbias, nvel, 0.0f);
+}
+
+// ---------------------------------------------------------------------------------------------
+// islands (BuildIslands, :587-664): union-find over dynamic-dynamic contacts
+// ---------------------------------------------------------------------------------------------
+__global__ void k_uf_init(uint32_t* uf, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) uf[i] = i;
+}
+__device__ __forceinline__ uint32_t uf_find(uint32_t* uf, uint32_t x) {
+    for (;;) {
+        uint32_t p = __ldcg(&uf[x]);
+        if (p == x) return x;
+        uint32_t gp = __ldcg(&uf[p]);
+        if (gp != p) atomicCAS(&uf[x], p, gp);  // path halving
+        x = p;
+    }
+}
+__global__ void k_uf_union(const Counters* cnt, const uint32_t* __restrict__ con_a, const uint32_t* __restrict__ con_b,
+                           const uint32_t* __restrict__ con_bits, uint32_t* uf) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cnt->ncons || (con_bits[c] & 6u) != 6u) return;
+    uint32_t a = con_a[c], bb = con_b[c];
+    for (;;) {
+        a = uf_find(uf, a);
+        bb = uf_find(uf, bb);
+        if (a == bb) return;
+        if (a > bb) { uint32_t t = a; a = bb; bb = t; }
+        uint32_t old = atomicCAS(&uf[bb], bb, a);  // hook the larger root under the smaller
+        if (old == bb) return;
+        bb = old;
+    }
+}
+__global__ void k_island_keys(const Counters* cnt, const uint32_t* __restrict__ con_a, const uint32_t* __restrict__ con_b,
+                              const uint32_t* __restrict__ con_bits, uint32_t* uf, uint32_t* key, uint32_t* val) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cnt->ncons) return;
+    uint32_t d = (con_bits[c] & 2u) ? con_a[c] : con_b[c];  // islandOf(A), else islandOf(B)
+    key[c] = uf_find(uf, d);
+    val[c] = c;
+}
+__global__ void k_island_heads(const Counters* cnt, const uint32_t* __restrict__ skey, uint32_t* head) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= cnt->ncons) return;
+    head[s] = (s == 0 || skey[s] != skey[s - 1]) ? 1u : 0u;
+}
+__global__ void k_island_starts(Counters* cnt, const uint32_t* __restrict__ head, const uint32_t* __restrict__ hscan,
+                                uint32_t* start) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t n = cnt->ncons;
+    if (s >= n) return;
+    if (head[s]) start[hscan[s]] = s;
+    if (s == n - 1) {
+        uint32_t ni = hscan[s] + head[s];
+        start[ni] = n;
+        cnt->nislands = ni;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// schedule: one thread per island.  Reproduces the reference's greedy first-fit batching of
+// contact points (at most 4 per batch, no body - static ones included - twice in a batch,
+// sensors skipped; PhysicsWorld.cpp:680-717) and converts the three sequential sweeps into
+// dependency levels over dynamic bodies:
+//   warm start : every point in island constraint order          (:673)
+//   velocity   : batch order                                      (:718-722)
+//   bias       : points with positionBias > 0, constraint order    (:736-742)
+// A point's level is 1 + the level of the previous point of the same sweep on either of its
+// dynamic bodies, so each body sees exactly the reference's update sequence.
+// ---------------------------------------------------------------------------------------------
+struct SchedBufs {
+    const uint32_t *isl_start, *isl_con, *con_a, *con_b, *con_np, *con_bits;
+    const float4* bias;
+    const float* inv_mass;
+    uint32_t *batch_cnt, *batch_body, *batch_mem, *last, *lvl_tmp, *ids_tmp, *lvl_count;
+    uint32_t *wl_list, *vl_list, *bl_list, *wl_off, *vl_off, *bl_off, *meta;
+};
+
+__device__ void sched_sort(uint32_t base, uint32_t loff, uint32_t npts, uint32_t nlev, const uint32_t* pts_level,
+                           const uint32_t* pts_id, uint32_t* count, uint32_t* list, uint32_t* off) {
+    // counting sort of npts points by level (levels 1..nlev) into list[base..], offsets off[loff..]
+    for (uint32_t l = 0; l <= nlev; ++l) count[loff + l] = 0;
+    for (uint32_t k = 0; k < npts; ++k) count[loff + pts_level[base + k] - 1]++;
+    uint32_t run = 0;
+    for (uint32_t l = 0; l < nlev; ++l) {
+        uint32_t c = count[loff + l];
+        off[loff + l] = run;
+        count[loff + l] = run;
+        run += c;
+    }
+    off[loff + nlev] = run;
+    for (uint32_t k = 0; k < npts; ++k) list[base + count[loff + pts_level[base + k] - 1]++] = pts_id[base + k];
+}
+
+__global__ void k_schedule(SchedBufs S, Counters* cnt) {
+    uint32_t isl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (isl >= cnt->nislands) return;
+    const uint32_t s0 = S.isl_start[isl], s1 = S.isl_start[isl + 1];
+    const uint32_t base = 4u * s0;      // point region of this island
+    const uint32_t loff = base + isl;   // level-offset region (one extra entry per island)
+    uint32_t* lvl = S.lvl_tmp;          // per point region: level of each listed point
+    uint32_t* ids = S.ids_tmp;          // per point region: row id of each listed point
+
+    // ---- greedy first-fit batching (point order = constraint order, then point index)
+    uint32_t nbt = 0, first_open = 0;
+    for (uint32_t s = s0; s < s1; ++s) {
+        uint32_t c = S.isl_con[s];
+        if (S.con_bits[c] & 1u) continue;  // sensor
+        const uint32_t a = S.con_a[c], bb = S.con_b[c];
+        for (uint32_t p = 0; p < S.con_np[c]; ++p) {
+            uint32_t pt = 4u * c + p;
+            bool placed = false;
+            for (uint32_t bi = first_open; bi < nbt; ++bi) {
+                uint32_t cntb = S.batch_cnt[base + bi];
+                if (cntb >= 4u) continue;
+                const uint32_t* bodies = &S.batch_body[8u * (base + bi)];
+                bool conflict = false;
+                for (uint32_t k = 0; k < cntb; ++k) {
+                    uint32_t x = bodies[2 * k], y = bodies[2 * k + 1];
+                    if (x == a || x == bb || y == a || y == bb) { conflict = true; break; }
+                }
+                if (conflict) continue;
+                S.batch_body[8u * (base + bi) + 2 * cntb] = a;
+                S.batch_body[8u * (base + bi) + 2 * cntb + 1] = bb;
+                S.batch_mem[4u * (base + bi) + cntb] = pt;
+                S.batch_cnt[base + bi] = cntb + 1;
+                if (cntb + 1 == 4u && bi == first_open)
+                    while (first_open < nbt && S.batch_cnt[base + first_open] >= 4u) ++first_open;
+                placed = true;
+                break;
+            }
+            if (!placed) {
+                S.batch_cnt[base + nbt] = 1;
+                S.batch_body[8u * (base + nbt)] = a;
+                S.batch_body[8u * (base + nbt) + 1] = bb;
+                S.batch_mem[4u * (base + nbt)] = pt;
+                ++nbt;
+            }
+        }
+    }
+    // ---- velocity levels in batch order
+    uint32_t nv = 0, nvpts = 0;
+    for (uint32_t bi = 0; bi < nbt; ++bi) {
+        uint32_t cntb = S.batch_cnt[base + bi];
+        for (uint32_t k = 0; k < cntb; ++k) {
+            uint32_t pt = S.batch_mem[4u * (base + bi) + k];
+            uint32_t c = pt >> 2;
+            uint32_t bits = S.con_bits[c];
+            uint32_t l = 0;
+            if (bits & 2u) l = max(l, S.last[S.con_a[c]]);
+            if (bits & 4u) l = max(l, S.last[S.con_b[c]]);
+            ++l;
+            if (bits & 2u) S.last[S.con_a[c]] = l;
+            if (bits & 4u) S.last[S.con_b[c]] = l;
+            nv = max(nv, l);
+            lvl[base + nvpts] = l;
+            ids[base + nvpts] = pt;
+            ++nvpts;
+        }
+    }
+    for (uint32_t s = s0; s < s1; ++s) {
+        uint32_t c = S.isl_con[s];
+        S.last[S.con_a[c]] = 0;
+        S.last[S.con_b[c]] = 0;
+    }
+    sched_sort(base, loff, nvpts, nv, lvl, ids, S.lvl_count, S.vl_list, S.vl_off);
+
+    // ---- warm-start levels: all points, constraint order
+    uint32_t nw = 0, nwpts = 0;
+    for (uint32_t s = s0; s < s1; ++s) {
+        uint32_t c = S.isl_con[s];
+        uint32_t bits = S.con_bits[c];
+        for (uint32_t p = 0; p < S.con_np[c]; ++p) {
+            uint32_t l = 0;
+            if (bits & 2u) l = max(l, S.last[S.con_a[c]]);
+            if (bits & 4u) l = max(l, S.last[S.con_b[c]]);
+            ++l;
+            if (bits & 2u) S.last[S.con_a[c]] = l;
+            if (bits & 4u) S.last[S.con_b[c]] = l;
+            nw = max(nw, l);
+            lvl[base + nwpts] = l;
+            ids[base + nwpts] = 4u * c + p;
+            ++nwpts;
+        }
+    }
+    for (uint32_t s = s0; s < s1; ++s) {
+        uint32_t c = S.isl_con[s];
+        S.last[S.con_a[c]] = 0;
+        S.last[S.con_b[c]] = 0;
+    }
+    sched_sort(base, loff, nwpts, nw, lvl, ids, S.lvl_count, S.wl_list, S.wl_off);
+
+    // ---- bias levels: points with positionBias > 0 of constraints with a massive body
+    uint32_t nbl = 0, nbpts = 0;
+    for (uint32_t s = s0; s < s1; ++s) {
+        uint32_t c = S.isl_con[s];
+        const uint32_t a = S.con_a[c], bb = S.con_b[c];
+        if (S.inv_mass[a] <= 0.0f && S.inv_mass[bb] <= 0.0f) continue;
+        uint32_t bits = S.con_bits[c];
+        for (uint32_t p = 0; p < S.con_np[c]; ++p) {
+            if (S.bias[4u * c + p].y <= 0.0f) continue;
+            uint32_t l = 0;
+            if (bits & 2u) l = max(l, S.last[a]);
+            if (bits & 4u) l = max(l, S.last[bb]);
+            ++l;
+            if (bits & 2u) S.last[a] = l;
+            if (bits & 4u) S.last[bb] = l;
+            nbl = max(nbl, l);
+            lvl[base + nbpts] = l;
+            ids[base + nbpts] = 4u * c + p;
+            ++nbpts;
+        }
+    }
+    for (uint32_t s = s0; s < s1; ++s) {
+        uint32_t c = S.isl_con[s];
+        S.last[S.con_a[c]] = 0;
+        S.last[S.con_b[c]] = 0;
+    }
+    sched_sort(base, loff, nbpts, nbl, lvl, ids, S.lvl_count, S.bl_list, S.bl_off);
+
+    S.meta[4 * isl + 0] = nw;
+    S.meta[4 * isl + 1] = nv;
+    S.meta[4 * isl + 2] = nbl;
+    S.meta[4 * isl + 3] = nbt;
+    atomicAdd(&cnt->batches, nbt);
+    atomicMax(&cnt->max_vlev, nv);
+    atomicMax(&cnt->max_blev, nbl);
+}
+
+// ---------------------------------------------------------------------------------------------
+// solve: one CTA per island, level by level
+// ---------------------------------------------------------------------------------------------
+struct SolveBufs {
+    const uint32_t *isl_start, *con_a, *con_b, *con_bits, *meta;
+    const uint32_t *wl_list, *vl_list, *bl_list, *wl_off, *vl_off, *bl_off;
+    DeviceRows r;
+    DeviceBodies b;
+    uint32_t vel_iters, pos_iters;
+    float ws_factor;
+    int vel_bias;
+};
+
+// WarmStart for one point (ContactSolver.cpp:117-132 + ApplyImpulsePair :32-43).
+__device__ __forceinline__ void warm_point(const SolveBufs& S, uint32_t row) {
+    uint32_t c = row >> 2;
+    uint32_t bits = S.con_bits[c];
+    const uint32_t A = S.con_a[c], B = S.con_b[c];
+    float4 im = S.r.imp[row];
+    Vec3 n = V3(S.r.n[row]), t1 = V3(S.r.t1[row]), t2 = V3(S.r.t2[row]);
+    Vec3 imp = ((n * im.x + t1 * im.y) + t2 * im.z) * S.ws_factor;
+    if (bits & 2u) {
+        Vec3 rA = V3(S.r.rA[row]);
+        S.b.lv[A] = F4(V3(S.b.lv[A]) + imp * S.b.inv_mass[A], 0.0f);
+        S.b.av[A] = F4(V3(S.b.av[A]) + M3(&S.b.iiw[3 * A]) * rA.cross(imp), 0.0f);
+    }
+    if (bits & 4u) {
+        Vec3 rB = V3(S.r.rB[row]);
+        S.b.lv[B] = F4(V3(S.b.lv[B]) - imp * S.b.inv_mass[B], 0.0f);
+        S.b.av[B] = F4(V3(S.b.av[B]) - M3(&S.b.iiw[3 * B]) * rB.cross(imp), 0.0f);
+    }
+}
+
+// One lane of SolveVelocityBatchSIMD (ContactSolverSIMD.cpp:93-256): friction t1, t2 (relative
+// velocity recomputed before each axis), then normal; only _mm_{add,sub,mul,min,max}_ps semantics.
+__device__ __forceinline__ void velocity_point(const SolveBufs& S, uint32_t row) {
+    uint32_t c = row >> 2;
+    uint32_t bits = S.con_bits[c];
+    const uint32_t A = S.con_a[c], B = S.con_b[c];
+    const Vec3 rA = V3(S.r.rAr[row]), rB = V3(S.r.rBr[row]);
+    Vec3 vA = V3(S.b.lv[A]), wA = V3(S.b.av[A]), vB = V3(S.b.lv[B]), wB = V3(S.b.av[B]);
+    const float invA = S.b.inv_mass[A], invB = S.b.inv_mass[B];
+    const Mat3 IA = M3(&S.b.iiw[3 * A]), IB = M3(&S.b.iiw[3 * B]);
+    const float4 n4 = S.r.n[row], t14 = S.r.t1[row], t24 = S.r.t2[row], m4 = S.r.mass[row];
+    float4 im = S.r.imp[row];
+    const float4 bias = S.r.bias[row];
+    const float nb = bias.x + (S.vel_bias ? bias.y : 0.0f);
+    const float fric = t14.w;
+    float nacc = im.x, t1acc = im.y, t2acc = im.z;
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+        const Vec3 dir = t == 0 ? V3(t14) : (t == 1 ? V3(t24) : V3(n4));
+        Vec3 wa = wA.cross(rA), wb = wB.cross(rB);
+        Vec3 rel((vA.x + wa.x) - (vB.x + wb.x), (vA.y + wa.y) - (vB.y + wb.y), (vA.z + wa.z) - (vB.z + wb.z));
+        float vd = rel.dot(dir);
+        float dl;
+        if (t < 2) {
+            const float mass = t == 0 ? m4.y : m4.z;
+            const float acc = t == 0 ? t1acc : t2acc;
+            float lambda = (0.0f - mass) * vd;
+            float maxf = fric * nacc;
+            float na = acc + lambda;
+            float lo = 0.0f - maxf;
+            na = na > lo ? na : lo;
+            na = na < maxf ? na : maxf;
+            dl = na - acc;
+            if (t == 0) t1acc = na; else t2acc = na;
+        } else {
+            float lambda = (0.0f - m4.x) * (vd - nb);
+            float na = nacc + lambda;
+            na = na > 0.0f ? na : 0.0f;
+            dl = na - nacc;
+            nacc = na;
+        }
+        Vec3 imp(dir.x * dl, dir.y * dl, dir.z * dl);
+        vA = Vec3(vA.x + imp.x * invA, vA.y + imp.y * invA, vA.z + imp.z * invA);
+        wA = wA + IA * rA.cross(imp);
+        vB = Vec3(vB.x - imp.x * invB, vB.y - imp.y * invB, vB.z - imp.z * invB);
+        wB = wB - IB * rB.cross(imp);
+    }
+    if (bits & 2u) { S.b.lv[A] = F4(vA, 0.0f); S.b.av[A] = F4(wA, 0.0f); }
+    if (bits & 4u) { S.b.lv[B] = F4(vB, 0.0f); S.b.av[B] = F4(wB, 0.0f); }
+    S.r.imp[row] = make_float4(nacc, t1acc, t2acc, im.w);
+}
+
+// SolveBiasConstraint for one point (ContactSolver.cpp:265-289).
+__device__ __forceinline__ void bias_point(const SolveBufs& S, uint32_t row) {
+    uint32_t c = row >> 2;
+    uint32_t bits = S.con_bits[c];
+    const uint32_t A = S.con_a[c], B = S.con_b[c];
+    const Vec3 rA = V3(S.r.rAr[row]), rB = V3(S.r.rBr[row]);
+    const Vec3 n = V3(S.r.n[row]);
+    const float nm = S.r.mass[row].x, pbias = S.r.bias[row].y;
+    float4 im = S.r.imp[row];
+    Vec3 vr = (V3(S.b.plv[A]) + V3(S.b.pav[A]).cross(rA)) - (V3(S.b.plv[B]) + V3(S.b.pav[B]).cross(rB));
+    float lambda = -nm * (vr.dot(n) - pbias);
+    float ni = rmax(im.w + lambda, 0.0f);
+    lambda = ni - im.w;
+    im.w = ni;
+    S.r.imp[row] = im;
+    Vec3 imp = n * lambda;
+    if (bits & 2u) {
+        S.b.plv[A] = F4(V3(S.b.plv[A]) + imp * S.b.inv_mass[A], 0.0f);
+        S.b.pav[A] = F4(V3(S.b.pav[A]) + M3(&S.b.iiw[3 * A]) * rA.cross(imp), 0.0f);
+    }
+    if (bits & 4u) {
+        S.b.plv[B] = F4(V3(S.b.plv[B]) - imp * S.b.inv_mass[B], 0.0f);
+        S.b.pav[B] = F4(V3(S.b.pav[B]) - M3(&S.b.iiw[3 * B]) * rB.cross(imp), 0.0f);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_solve(SolveBufs S, const Counters* cnt) {
+    const uint32_t nisl = cnt->nislands;
+    for (uint32_t isl = blockIdx.x; isl < nisl; isl += gridDim.x) {
+        const uint32_t base = 4u * S.isl_start[isl];
+        const uint32_t loff = base + isl;
+        const uint32_t nw = S.meta[4 * isl], nv = S.meta[4 * isl + 1], nbl = S.meta[4 * isl + 2];
+        for (uint32_t l = 0; l < nw; ++l) {
+            const uint32_t e = S.wl_off[loff + l + 1];
+            for (uint32_t k = S.wl_off[loff + l] + threadIdx.x; k < e; k += blockDim.x) warm_point(S, S.wl_list[base + k]);
+            __syncthreads();
+        }
+        for (uint32_t it = 0; it < S.vel_iters; ++it)
+            for (uint32_t l = 0; l < nv; ++l) {
+                const uint32_t e = S.vl_off[loff + l + 1];
+                for (uint32_t k = S.vl_off[loff + l] + threadIdx.x; k < e; k += blockDim.x)
+                    velocity_point(S, S.vl_list[base + k]);
+                __syncthreads();
+            }
+        if (!S.vel_bias)
+            for (uint32_t it = 0; it < S.pos_iters; ++it)
+                for (uint32_t l = 0; l < nbl; ++l) {
+                    const uint32_t e = S.bl_off[loff + l + 1];
+                    for (uint32_t k = S.bl_off[loff + l] + threadIdx.x; k < e; k += blockDim.x)
+                        bias_point(S, S.bl_list[base + k]);
+                    __syncthreads();
+                }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// cache store (:568-581) and position integration (:276-290, 785-802, 854-861)
+// ---------------------------------------------------------------------------------------------
+__global__ void k_cache_store(Counters* cnt, const unsigned long long* __restrict__ con_key,
+                              const uint32_t* __restrict__ con_np, DeviceRows r, unsigned long long* c_key,
+                              uint32_t* c_np, float4* c_pos, float4* c_imp, uint32_t cap) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cnt->ncons) return;
+    unsigned long long key = con_key[c];
+    uint32_t mask = cap - 1u;
+    uint32_t slot = hash_key(key) & mask;
+    uint32_t probes = 0;
+    for (;;) {
+        unsigned long long prev = atomicCAS(&c_key[slot], 0ull, key);
+        if (prev == 0ull) { atomicAdd(&cnt->cache_entries, 1u); break; }
+        if (prev == key) break;
+        slot = (slot + 1u) & mask;
+        if (++probes >= cap) { atomicOr(&cnt->error, KZG_DEVERR_CACHE); return; }
+    }
+    uint32_t n = con_np[c];
+    c_np[slot] = n;
+    for (uint32_t p = 0; p < n; ++p) {
+        float4 pa = r.pA[4u * c + p];
+        float4 im = r.imp[4u * c + p];
+        c_pos[4u * slot + p] = make_float4(pa.x, pa.y, pa.z, 0.0f);
+        c_imp[4u * slot + p] = make_float4(im.x, im.y, im.z, 0.0f);
+    }
+}
+
+__global__ void k_integrate_pos(DeviceBodies b, uint32_t n, float dt, int vel_bias) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t mt = b.motion[i];
+    if (mt != KZG_MOTION_STATIC) {
+        Vec3 p = V3(b.pos[i]);
+        Quat q = Q4(b.rot[i]);
+        Vec3 lv = V3(b.lv[i]), av = V3(b.av[i]);
+        p = p + lv * dt;
+        if (av.len2() > 0.0f) q = integrate_rotation(q, av, dt);
+        if (!vel_bias) {
+            Vec3 pl = V3(b.plv[i]), pa = V3(b.pav[i]);
+            if (pl.len2() > 0.0f) p = p + pl * dt;
+            if (pa.len2() > 0.0f) q = integrate_rotation(q, pa, dt);
+            b.plv[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            b.pav[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        b.pos[i] = F4(p, 0.0f);
+        b.rot[i] = F4q(q);
+        if (mt == KZG_MOTION_DYNAMIC) {
+            Mat3 R = q.to_mat3();
+            Mat3 W = (R * M3(&b.iil[3 * i])) * R.transposed();
+            b.iiw[3 * i] = F4(W.c0, 0.0f);
+            b.iiw[3 * i + 1] = F4(W.c1, 0.0f);
+            b.iiw[3 * i + 2] = F4(W.c2, 0.0f);
+        }
+    }
+    b.force[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    b.torque[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// ComputeStateHash words (PhysicsWorld.cpp:1152-1172); the FNV-1a fold runs on the host.
+__global__ void k_hash_words(DeviceBodies b, uint32_t n, unsigned long long* out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = b.pos[i], q = b.rot[i], l = b.lv[i], a = b.av[i];
+    float v[13] = {p.x, p.y, p.z, q.x, q.y, q.z, q.w, l.x, l.y, l.z, a.x, a.y, a.z};
+    out[14ull * i] = b.packed[i];
+    for (int k = 0; k < 13; ++k) out[14ull * i + 1 + k] = (unsigned long long)(long long)(v[k] * 100000.0f);
+}
+
+// ---------------------------------------------------------------------------------------------
+// host orchestration
+// ---------------------------------------------------------------------------------------------
+#define KZG_CK(x)                                                        \
+    do {                                                                 \
+        cudaError_t e_ = (x);                                            \
+        if (e_ != cudaSuccess) {                                         \
+            ctx.err = std::string(#x) + ": " + cudaGetErrorString(e_);   \
+            return KZG_ERR_CUDA;                                         \
+        }                                                                \
+    } while (0)
+
+static kzg_status fetch_counters(Ctx& ctx) {
+    KZG_CK(cudaMemcpyAsync(ctx.hcnt, ctx.dcnt, sizeof(Counters), cudaMemcpyDeviceToHost, ctx.stream));
+    KZG_CK(cudaStreamSynchronize(ctx.stream));
+    return KZG_OK;
+}
+
+size_t cub_temp_bytes(uint32_t max_items) {
+    size_t a = 0, b = 0, c = 0, d = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, a, (unsigned long long*)nullptr, (unsigned long long*)nullptr,
+                                    (uint32_t*)nullptr, (uint32_t*)nullptr, (int)max_items);
+    cub::DeviceRadixSort::SortKeys(nullptr, b, (unsigned long long*)nullptr, (unsigned long long*)nullptr,
+                                   (int)max_items);
+    cub::DeviceScan::ExclusiveSum(nullptr, c, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)max_items);
+    cub::DeviceRadixSort::SortPairs(nullptr, d, (uint32_t*)nullptr, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                    (uint32_t*)nullptr, (int)max_items);
+    return std::max(std::max(a, b), std::max(c, d));
+}
+
+static int bits_for(uint32_t v) {
+    int b = 1;
+    while (b < 32 && (1ull << b) <= v) ++b;
+    return b;
+}
+
+// Runs one step after the pair list is in ctx.pairs and hcnt->npairs is valid on the device.
+static kzg_status step_after_pairs(Ctx& ctx, float dt) {
+    cudaStream_t st = ctx.stream;
+    const uint32_t nb = ctx.nbodies;
+    const uint32_t np = ctx.hcnt->npairs;
+    ShapeTables T{ctx.shapes, ctx.hull_verts, ctx.face_sizes, ctx.face_idx};
+    KZG_CK(cudaEventRecord(ctx.ev[1], st));
+    if (np > 0) {
+        k_narrow<<<blocks_for(np, 128), 128, 0, st>>>(T, ctx.b, ctx.pairs, ctx.dcnt, ctx.m_count, ctx.m_data,
+                                                      ctx.m_key, &ctx.dcnt->error);
+        k_con_flags<<<blocks_for(np), kThreads, 0, st>>>(ctx.m_count, ctx.m_key, ctx.dcnt, ctx.con_flag);
+        size_t tb = ctx.cub_tmp_bytes;
+        KZG_CK(cub::DeviceScan::ExclusiveSum(ctx.cub_tmp, tb, ctx.con_flag, ctx.con_index, (int)np, st));
+    }
+    KZG_CK(cudaEventRecord(ctx.ev[2], st));
+    if (np > 0)
+        k_build_constraints<<<blocks_for(np), kThreads, 0, st>>>(
+            ctx.pairs, ctx.con_flag, ctx.con_index, ctx.m_count, ctx.m_data, ctx.m_key, ctx.b, ctx.dcnt,
+            ctx.con_pair, ctx.con_a, ctx.con_b, ctx.con_np, ctx.con_bits, ctx.con_fr, ctx.con_key, ctx.r, ctx.c_key,
+            ctx.c_np, ctx.c_pos, ctx.c_imp, ctx.cfg.max_cache_entries, ctx.ws.warm_start);
+    k_integrate_vel<<<blocks_for(nb), kThreads, 0, st>>>(
+        ctx.b, nb, make_float3(ctx.ws.gravity[0], ctx.ws.gravity[1], ctx.ws.gravity[2]), dt);
+    kzg_status s = fetch_counters(ctx);
+    if (s != KZG_OK) return s;
+    const uint32_t nc = ctx.hcnt->ncons;
+    KZG_CK(cudaEventRecord(ctx.ev[3], st));
+    if (nc > 0) {
+        PrepParams pp{dt, ctx.ss.baumgarte, ctx.ss.penetration_slop, ctx.ss.restitution_threshold,
+                      ctx.ss.max_bias_velocity};
+        k_prepare<<<blocks_for(4 * nc), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_np, ctx.r, pp);
+        k_uf_init<<<blocks_for(nb), kThreads, 0, st>>>(ctx.uf, nb);
+        k_uf_union<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf);
+        k_island_keys<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf,
+                                                           ctx.isl_key, ctx.isl_con_in);
+        size_t tb = ctx.cub_tmp_bytes;
+        KZG_CK(cub::DeviceRadixSort::SortPairs(ctx.cub_tmp, tb, ctx.isl_key, ctx.isl_key_sorted, ctx.isl_con_in,
+                                               ctx.isl_con, (int)nc, 0, bits_for(nb), st));
+        k_island_heads<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_key_sorted, ctx.isl_head);
+        tb = ctx.cub_tmp_bytes;
+        KZG_CK(cub::DeviceScan::ExclusiveSum(ctx.cub_tmp, tb, ctx.isl_head, ctx.isl_pts, (int)nc, st));
+        k_island_starts<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_head, ctx.isl_pts, ctx.isl_start);
+        s = fetch_counters(ctx);
+        if (s != KZG_OK) return s;
+        const uint32_t ni = ctx.hcnt->nislands;
+        SchedBufs SB{ctx.isl_start, ctx.isl_con, ctx.con_a, ctx.con_b, ctx.con_np, ctx.con_bits, ctx.r.bias,
+                     ctx.b.inv_mass, ctx.batch_cnt, ctx.batch_body, ctx.batch_mem, ctx.last_lvl, ctx.lvl_tmp,
+                     ctx.ids_tmp, ctx.lvl_count, ctx.wl_list, ctx.vl_list,
+                     ctx.bl_list, ctx.wl_off, ctx.vl_off, ctx.bl_off, ctx.isl_meta};
+        k_schedule<<<blocks_for(ni, 64), 64, 0, st>>>(SB, ctx.dcnt);
+        KZG_CK(cudaEventRecord(ctx.ev[4], st));
+        SolveBufs SV{ctx.isl_start, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.isl_meta, ctx.wl_list, ctx.vl_list,
+                     ctx.bl_list, ctx.wl_off, ctx.vl_off, ctx.bl_off, ctx.r, ctx.b, ctx.ss.velocity_iterations,
+                     ctx.ss.position_iterations, ctx.ss.warm_start_factor, ctx.ss.use_velocity_bias};
+        unsigned grid = ni < 65535u ? ni : 65535u;
+        if (grid > 0) k_solve<<<grid, 128, 0, st>>>(SV, ctx.dcnt);
+        k_cache_store<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.con_key, ctx.con_np, ctx.r, ctx.c_key,
+                                                           ctx.c_np, ctx.c_pos, ctx.c_imp, ctx.cfg.max_cache_entries);
+    } else {
+        KZG_CK(cudaEventRecord(ctx.ev[4], st));
+    }
+    KZG_CK(cudaEventRecord(ctx.ev[5], st));
+    k_integrate_pos<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, dt, ctx.ss.use_velocity_bias);
+    KZG_CK(cudaEventRecord(ctx.ev[6], st));
+    KZG_CK(cudaGetLastError());
+    s = fetch_counters(ctx);
+    if (s != KZG_OK) return s;
+    return KZG_OK;
+}
+
+static void reset_counters_async(Ctx& ctx) {
+    // npairs, ncons, nislands, batches, max levels and error restart each step; cache_entries persists
+    cudaMemsetAsync(ctx.dcnt, 0, offsetof(Counters, cache_entries), ctx.stream);
+}
+
+static kzg_status finish_stats(Ctx& ctx) {
+    Counters& h = *ctx.hcnt;
+    kzg_stats& s = ctx.stats;
+    s.num_bodies = ctx.nbodies;
+    s.num_broadphase_pairs = h.npairs;
+    s.num_contact_constraints = h.ncons;
+    s.num_islands = h.nislands;
+    s.num_batches = h.batches;
+    s.max_velocity_levels = h.max_vlev;
+    s.max_bias_levels = h.max_blev;
+    s.cache_entries = h.cache_entries;
+    s.device_error = h.error;
+    cudaEventElapsedTime(&s.broadphase_ms, ctx.ev[0], ctx.ev[1]);
+    cudaEventElapsedTime(&s.narrowphase_ms, ctx.ev[1], ctx.ev[2]);
+    cudaEventElapsedTime(&s.constraints_ms, ctx.ev[2], ctx.ev[3]);
+    cudaEventElapsedTime(&s.solve_ms, ctx.ev[3], ctx.ev[5]);
+    cudaEventElapsedTime(&s.integrate_ms, ctx.ev[5], ctx.ev[6]);
+    cudaEventElapsedTime(&s.step_ms, ctx.ev[0], ctx.ev[6]);
+    if (h.error) {
+        ctx.err = "device error word " + std::to_string(h.error) + " (see KZG_DEVERR_*)";
+        return (h.error & (KZG_DEVERR_PAIRS | KZG_DEVERR_CACHE)) ? KZG_ERR_CAPACITY : KZG_ERR_DEVICE;
+    }
+    return KZG_OK;
+}
+
+kzg_status step_canonical(Ctx& ctx, float dt) {
+    cudaStream_t st = ctx.stream;
+    const uint32_t nb = ctx.nbodies;
+    ++ctx.frame;
+    reset_counters_async(ctx);
+    KZG_CK(cudaEventRecord(ctx.ev[0], st));
+    k_aabb<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, ctx.shapes, nb, 1.0f / ctx.cell_size, ctx.is_large,
+                                                ctx.cell_keys, ctx.cell_vals);
+    size_t tb = ctx.cub_tmp_bytes;
+    KZG_CK(cub::DeviceRadixSort::SortPairs(ctx.cub_tmp, tb, ctx.cell_keys, ctx.cell_keys_sorted, ctx.cell_vals,
+                                           ctx.cell_vals_sorted, (int)nb, 0, 64, st));
+    const uint32_t nsmall = nb - ctx.nlarge;
+    k_find_pairs<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, ctx.cell_keys_sorted, ctx.cell_vals_sorted, nsmall,
+                                                      1.0f / ctx.cell_size, ctx.is_large, ctx.large_list,
+                                                      ctx.large_off, ctx.nworlds, ctx.pair_keys, ctx.dcnt,
+                                                      ctx.cfg.max_pairs);
+    kzg_status s = fetch_counters(ctx);
+    if (s != KZG_OK) return s;
+    if (ctx.hcnt->error & KZG_DEVERR_PAIRS) return finish_stats(ctx);
+    const uint32_t np = ctx.hcnt->npairs;
+    if (np > 0) {
+        tb = ctx.cub_tmp_bytes;
+        KZG_CK(cub::DeviceRadixSort::SortKeys(ctx.cub_tmp, tb, ctx.pair_keys, ctx.pair_keys_sorted, (int)np, 0, 64, st));
+        k_unpack_pairs<<<blocks_for(np), kThreads, 0, st>>>(ctx.pair_keys_sorted, ctx.dcnt, ctx.pairs);
+    }
+    s = step_after_pairs(ctx, dt);
+    if (s != KZG_OK) return s;
+    return finish_stats(ctx);
+}
+
+kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t np, float dt) {
+    cudaStream_t st = ctx.stream;
+    if (np > ctx.cfg.max_pairs) {
+        ctx.err = "pair count exceeds kzg_config.max_pairs";
+        return KZG_ERR_CAPACITY;
+    }
+    ++ctx.frame;
+    reset_counters_async(ctx);
+    KZG_CK(cudaEventRecord(ctx.ev[0], st));
+    if (np > 0) {
+        KZG_CK(cudaMemcpyAsync(ctx.pair_keys, host_pairs, sizeof(uint32_t) * 2 * np, cudaMemcpyHostToDevice, st));
+        k_pairs_from_packed<<<blocks_for(np), kThreads, 0, st>>>((const uint32_t*)ctx.pair_keys, np, ctx.b,
+                                                                 ctx.nbodies, ctx.pairs);
+    }
+    KZG_CK(cudaMemcpyAsync(&ctx.dcnt->npairs, &np, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    ctx.hcnt->npairs = np;
+    kzg_status s = step_after_pairs(ctx, dt);
+    if (s != KZG_OK) return s;
+    return finish_stats(ctx);
+}
+
+kzg_status hash_state(Ctx& ctx, uint64_t* out) {
+    const uint32_t nb = ctx.nbodies;
+    std::vector<unsigned long long> w(14ull * nb);
+    if (nb) {
+        k_hash_words<<<blocks_for(nb), kThreads, 0, ctx.stream>>>(ctx.b, nb, ctx.hash_words);
+        KZG_CK(cudaMemcpyAsync(w.data(), ctx.hash_words, sizeof(unsigned long long) * w.size(), cudaMemcpyDeviceToHost,
+                               ctx.stream));
+        KZG_CK(cudaStreamSynchronize(ctx.stream));
+    }
+    uint64_t h = 1469598103934665603ull;
+    for (unsigned long long v : w) {
+        h ^= v;
+        h *= 1099511628211ull;
+    }
+    *out = h;
+    return KZG_OK;
+}
+
+}  // namespace kzg

@@ -1,0 +1,88 @@
+"""Generate the golden fixtures in tests/golden/ from the reference engine itself.
+
+Runs only where the reference sources exist (this script builds oracle/_ref/ref_trace from them
+with oracle/Makefile.ref).  For every fixture scene it records what the unmodified reference
+computed: the ComputeStateHash value after every step, the full body state at checkpoint steps,
+the broad-phase pair list and contact constraints of the first steps, WorldStats counters, the
+resolved mass properties and every hull as built by ConvexHullShape::Create.
+
+    python tests/golden/gen_golden.py [--ref /root/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from kizuriphysics3d_gb300 import scenes  # noqa: E402
+from oracle import trace as T  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def fixture_scenes():
+    """name -> (scene, steps, detail steps, checkpoint steps)."""
+    out = {}
+    out["pyramid20"] = (scenes.pyramid(20), 600, 2, [0, 1, 2, 9, 59, 119, 299, 599])
+    out["pile200"] = (scenes.pile(200, seed=1234, extent=3.0, y_range=(2.0, 12.0)), 600, 2, [0, 1, 59, 299, 599])
+    out["stacks2x2x20"] = (scenes.stacks(2, 2, 20), 300, 2, [0, 1, 59, 299])
+    out["pile64_nows"] = (_nows(scenes.pile(64, seed=77, extent=1.5, y_range=(1.0, 5.0))), 240, 2, [0, 59, 239])
+    out["pyramid4_tests"] = (_reference_test_pyramid(), 240, 2, [0, 239])
+    return out
+
+
+def _nows(sc):
+    sc.flags |= scenes.WORLD_FLAG_NO_WARM_START
+    sc.name += "_nows"
+    return sc
+
+
+def _reference_test_pyramid():
+    """World_PyramidRest (tests/TestWorld.cpp:103-128) with the reference test's materials and the
+    reference default solver settings (16 velocity / 6 position iterations)."""
+    sc = scenes.pyramid(4, friction=0.6, vel_iters=16, pos_iters=6)
+    sc.bodies[0].friction = 0.8  # AddGround uses friction 0.8 (TestWorld.cpp:16)
+    sc.name = "pyramid4_tests"
+    return sc
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    subprocess.run(["make", "-s", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"), f"REF={args.ref}", "-j8"],
+                   check=True)
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_trace")
+    with tempfile.TemporaryDirectory() as td:
+        for name, (sc, steps, detail, ckpt) in fixture_scenes().items():
+            sp = os.path.join(td, name + ".kzsc")
+            tp = os.path.join(td, name + ".kztr")
+            sc.save(sp)
+            subprocess.run([exe, sp, tp, str(steps), str(detail)], check=True)
+            tr = T.read_trace(tp)
+            fx = dict(hashes=tr.hashes, stats=tr.stats, packed=tr.packed, inv_mass=tr.inv_mass,
+                      inv_inertia_local=tr.inv_inertia_local, inv_inertia_world=tr.inv_inertia_world,
+                      state0=tr.state0, ckpt_steps=np.array(ckpt, np.int32),
+                      ckpt_states=np.stack([tr.states[s] for s in ckpt]))
+            for si, hull in tr.hulls.items():
+                fx[f"hull{si}_verts"] = hull.verts
+                fx[f"hull{si}_sizes"] = hull.sizes
+                fx[f"hull{si}_idx"] = hull.idx
+            for d, det in enumerate(tr.detail):
+                fx[f"d{d}_pairs"] = det.pairs
+                fx[f"d{d}_con_hdr"] = det.con_hdr
+                fx[f"d{d}_con_fr"] = det.con_fr
+                fx[f"d{d}_con_pts"] = det.con_pts
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **fx)
+            print(f"{name}: {steps} steps, final hash {int(tr.hashes[-1]):016x}")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,129 @@
+"""GPU parity: the CUDA pipeline (through the C-ABI of libkzg.so) against the oracle and the
+reference's golden fixtures.  The bar is bit-exact: identical ComputeStateHash after every step,
+identical float bits of every body state, contact point and impulse.
+
+Mode A feeds the GPU the reference's own broad-phase pair order (produced by the oracle's
+restatement of the reference's dynamic AABB tree, itself pinned to the reference); mode B is the
+production path with the GPU broad phase (canonical MakePairKey order) checked against the oracle
+running the same pair order.
+"""
+import numpy as np
+import pytest
+
+from conftest import bits, golden_resolved, load_golden, oracle_blob
+from tests.golden.gen_golden import fixture_scenes
+
+FIXTURES = fixture_scenes()
+pytestmark = pytest.mark.gpu
+
+
+def _pair_worlds(name, mode, oracle_lib, **kw):
+    from kizuriphysics3d_gb300 import World
+    sc = FIXTURES[name][0]
+    g = load_golden(name)
+    res = golden_resolved(sc, g)
+    ow = oracle_lib.OracleWorld(sc.to_bytes(), oracle_blob(sc, res), mode, threads=kw.pop("threads", 1))
+    gw = World(sc, resolved=res, **kw)
+    return sc, g, ow, gw
+
+
+@pytest.mark.parametrize("name", sorted(FIXTURES))
+def test_mode_a_bit_exact_with_reference(name, oracle_lib, kzg_lib):
+    sc, g, ow, gw = _pair_worlds(name, oracle_lib.PAIRS_TREE, oracle_lib)
+    steps, detail = FIXTURES[name][1], FIXTURES[name][2]
+    with gw:
+        im, iw = gw.mass()
+        assert np.array_equal(bits(iw), bits(g["inv_inertia_world"]))
+        for s in range(steps):
+            ow.step(np.float32(sc.dt))
+            gw.step_with_pairs(ow.pairs())
+            st = gw.state()
+            if not np.array_equal(bits(st), bits(ow.state())):
+                bad = np.argwhere(bits(st) != bits(ow.state()))
+                pytest.fail(f"{name}: GPU state differs from the oracle at step {s}, first entries {bad[:4].tolist()}")
+            assert gw.compute_state_hash() == int(g["hashes"][s]), f"{name}: hash differs from the reference at {s}"
+            if s < detail:
+                hdr, pts, fr = gw.contact_constraints()
+                assert np.array_equal(hdr, g[f"d{s}_con_hdr"])
+                assert np.array_equal(bits(fr), bits(g[f"d{s}_con_fr"]))
+                assert np.array_equal(bits(pts), bits(g[f"d{s}_con_pts"]))
+        assert gw.get_stats()["device_error"] == 0
+
+
+@pytest.mark.parametrize("name,steps", [("pile200", 300), ("stacks2x2x20", 200), ("pyramid20", 200)])
+def test_mode_b_bit_exact_with_oracle(name, steps, oracle_lib, kzg_lib):
+    sc, g, ow, gw = _pair_worlds(name, oracle_lib.PAIRS_CANONICAL, oracle_lib)
+    with gw:
+        for s in range(steps):
+            ow.step(np.float32(sc.dt))
+            gw.step_fixed()
+            assert np.array_equal(gw.broadphase_pairs(), ow.pairs()), f"pair list differs at step {s}"
+            assert np.array_equal(bits(gw.state()), bits(ow.state())), f"state differs at step {s}"
+        hdr, pts, fr = gw.contact_constraints()
+        ohdr, opts, ofr = ow.constraints()
+        assert np.array_equal(hdr, ohdr) and np.array_equal(bits(pts), bits(opts))
+
+
+def test_mode_b_larger_pile(oracle_lib, kzg_lib):
+    from kizuriphysics3d_gb300 import World, resolve, scenes
+    sc = scenes.pile(1500, seed=99, extent=6.0, y_range=(1.0, 20.0))
+    res = resolve(sc)
+    ow = oracle_lib.OracleWorld(sc.to_bytes(), oracle_blob(sc, res), oracle_lib.PAIRS_CANONICAL, threads=8)
+    with World(sc, resolved=res) as gw:
+        for s in range(150):
+            ow.step(np.float32(sc.dt))
+            gw.step_fixed()
+        assert np.array_equal(bits(gw.state()), bits(ow.state()))
+        assert gw.compute_state_hash() == ow.hash()
+
+
+def test_hash_identical_run_to_run(kzg_lib):
+    from kizuriphysics3d_gb300 import World, resolve, scenes
+    sc = scenes.pile(800, seed=5, extent=4.0, y_range=(1.0, 12.0))
+    res = resolve(sc)
+    hashes = []
+    for _ in range(2):
+        with World(sc, resolved=res) as w:
+            w.step_fixed(n=120)
+            hashes.append(w.compute_state_hash())
+    assert hashes[0] == hashes[1]
+
+
+def test_full_size_box_field_properties(kzg_lib):
+    """400 stacks x 500 unit boxes (the large-box-field workload) at full size: exact pair count,
+    no device error, nothing tunnels through the plane, run-to-run identical state."""
+    from kizuriphysics3d_gb300 import World, resolve, scenes
+    sc = scenes.stacks(20, 20, 500)
+    res = resolve(sc)
+    hashes = []
+    for _ in range(2):
+        with World(sc, resolved=res, max_pairs=4 * len(sc.bodies)) as w:
+            w.step_fixed()
+            st = w.get_stats()
+            assert st["num_broadphase_pairs"] == 400 * 499 + 400
+            w.step_fixed(n=4)
+            st = w.get_stats()
+            assert st["device_error"] == 0
+            assert st["num_islands"] == 400
+            s = w.state()
+            assert float(s[1:, 1].min()) > 0.4
+            hashes.append(w.compute_state_hash())
+    assert hashes[0] == hashes[1]
+
+
+def test_pair_capacity_overflow_is_reported(kzg_lib):
+    from kizuriphysics3d_gb300 import World, capi, scenes
+    sc = scenes.pyramid(8)
+    with World(sc, max_pairs=8) as w:
+        with pytest.raises(capi.KzgError) as e:
+            w.step_fixed()
+        assert e.value.status == -3
+
+
+def test_stale_pair_ids_are_skipped(kzg_lib):
+    from kizuriphysics3d_gb300 import World, scenes
+    sc = scenes.pyramid(3)
+    with World(sc) as w:
+        w.step_with_pairs(np.array([[0, 1], [0xFF000001, 2], [999, 3]], np.uint32))
+        hdr, _, _ = w.contact_constraints()
+        assert all(h[0] < len(sc.bodies) and h[1] < len(sc.bodies) for h in hdr)
