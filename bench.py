@@ -1,0 +1,366 @@
+#!/usr/bin/env python
+"""Benchmark of the per-step contact pipeline (PhysicsWorld::StepFixed) on GB300.
+
+Default workload: the random convex pile - 20,000 bodies (sphere / box / capsule / 16-point hull,
+seed 1234), 10 velocity + 2 position iterations, dt 1/60 - timed in its settled, contact-rich
+phase: the run starts from the pile's state after 600 steps (a committed snapshot, or simulated
+untimed when absent).  A "step" is one full StepFixed: broad phase, narrow phase, manifold cache,
+constraint build, islands, the reference's batch schedule, solve and integration.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+Prints one JSON line (rank 0).  value = dynamic body-steps/s from CUDA events on the library's
+stream with inputs resident in HBM; e2e = the same metric through the C-ABI with host buffers
+(forces uploaded, transforms read back every step).  L2 (129 MB) is flushed between timed steps
+by writing a 256 MB buffer.  --impl reference times the reference algorithm on the host cores:
+the oracle port (oracle/, a C restatement of the reference pinned bit-exact to it), all threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "body-steps/s on 1 GB300 at residual 1e-4, learned vs plain warm start vs CPU"
+SNAP_DIR = os.path.join(ROOT, "kizuriphysics3d_gb300", "data")
+
+
+# ---------------------------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------------------------
+def make_workload(name: str):
+    from kizuriphysics3d_gb300 import scenes
+    if name == "pile20000":
+        return scenes.pile(20000, seed=1234), 600, {
+            "workload": "random convex pile, 20000 bodies (sphere/box/capsule/16-point hull), seed 1234, "
+                        "positions U[-20,20]x[2,100]x[-20,20], 10 velocity + 2 position iterations, dt 1/60",
+            "bodies": 20000}
+    if name == "stacks":
+        return scenes.stacks(20, 20, 500), 0, {
+            "workload": "large box field, 400 stacks x 500 unit boxes, jitter seed 7, 8 velocity + 2 position "
+                        "iterations, dt 1/60", "bodies": 200000}
+    if name == "pyramid20":
+        return scenes.pyramid(20), 0, {
+            "workload": "20-row pyramid, 210 unit boxes, 10 velocity + 2 position iterations, dt 1/60", "bodies": 210}
+    raise SystemExit(f"unknown workload {name}")
+
+
+def snapshot_path(name: str, preroll: int) -> str:
+    return os.path.join(SNAP_DIR, f"{name}_step{preroll}.npz")
+
+
+def load_snapshot(name: str, preroll: int):
+    p = snapshot_path(name, preroll)
+    if preroll and os.path.exists(p):
+        with np.load(p) as z:
+            return z["state"]
+    return None
+
+
+def scene_with_state(sc, state):
+    """The same scene whose bodies start at the given state (pos, rot, linear, angular)."""
+    import copy
+    s2 = copy.copy(sc)
+    s2.bodies = [copy.copy(b) for b in sc.bodies]
+    for b, st in zip(s2.bodies, state):
+        b.pos, b.rot, b.vel, b.ang = tuple(st[0:3]), tuple(st[3:7]), tuple(st[7:10]), tuple(st[10:13])
+    return s2
+
+
+# ---------------------------------------------------------------------------------------------
+# algorithmic bytes (the roofline model)
+# ---------------------------------------------------------------------------------------------
+SHAPE_BYTES = {0: 4, 1: 12, 2: 8, 4: 192, 8: 16}
+
+
+def narrow_bytes(sc, pairs: np.ndarray, points: int) -> float:
+    """Per pair: ids 8 + two pose gathers 56 + manifold header 16 + both shape records; 40 B per
+    contact point written."""
+    st = np.array([sc.shapes[b.shape].type for b in sc.bodies])
+    sb = np.vectorize(SHAPE_BYTES.get)(st)
+    return float(pairs.shape[0] * 80 + sb[pairs[:, 0]].sum() + sb[pairs[:, 1]].sum() + 40 * points)
+
+
+def solve_bytes(points: int, dyn_bodies: int) -> float:
+    """Rows read once (92 B) and impulses written (16 B) per point; per dynamic body velocity read +
+    write (48 B), inverse mass and world inertia read (40 B)."""
+    return float(points * (92 + 16) + dyn_bodies * 88)
+
+
+def step_bytes(n_dyn: int, pair_bytes: float, points: int, constraints: int) -> float:
+    """Whole-step compulsory traffic: 236 B per dynamic body + pair bytes + 312 B per point +
+    32 B per constraint."""
+    return 236.0 * n_dyn + pair_bytes + 312.0 * points + 32.0 * constraints
+
+
+# ---------------------------------------------------------------------------------------------
+# clocks sampler
+# ---------------------------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join("/tmp", f"kzg_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU legs (oracle port of the reference algorithm)
+# ---------------------------------------------------------------------------------------------
+def cpu_leg(sc, res, state, steps_max: int, budget_s: float, threads: int):
+    from oracle import pykzo, trace
+    s2 = scene_with_state(sc, state) if state is not None else sc
+    hulls = {i: trace.Hull(h.verts, h.sizes, h.idx, 0.0) for i, h in res.hulls.items()}
+    w = pykzo.OracleWorld(s2.to_bytes(), trace.resolved_blob(s2, hulls, res.inv_mass, res.inv_inertia_local),
+                          pykzo.PAIRS_TREE, threads=threads)
+    done, t0 = 0, time.perf_counter()
+    while done < steps_max:
+        w.step(np.float32(sc.dt))
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    w.close()
+    return done, dt
+
+
+# ---------------------------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="pile20000")
+    ap.add_argument("--preroll", type=int, default=None)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--save-snapshot", default=None, help="write the post-preroll state to this .npz path")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    sc, preroll_default, cfg = make_workload(args.workload)
+    preroll = preroll_default if args.preroll is None else args.preroll
+    n_dyn = sc.num_dynamic
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        run_reference(args, sc, cfg, preroll, n_dyn)
+        return
+
+    import torch
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    torch.cuda.set_device(local_rank)
+
+    from kizuriphysics3d_gb300 import World, resolve
+    res = resolve(sc)
+    snap = load_snapshot(args.workload, preroll)
+    start_scene = scene_with_state(sc, snap) if snap is not None else sc
+    max_pairs = max(8 * len(sc.bodies), 4096)
+    w = World(start_scene, resolved=res, device=local_rank, max_pairs=max_pairs)
+    t_setup = time.perf_counter()
+    if snap is None and preroll:
+        done = 0
+        while done < preroll:
+            k = min(100, preroll - done)
+            w.step_fixed(n=k)
+            done += k
+            st = w.get_stats()
+            print(f"preroll {done}/{preroll}: {time.perf_counter() - t_setup:.1f} s, pairs {st['num_broadphase_pairs']}, "
+                  f"points {st['num_contact_points']}, islands {st['num_islands']}, step {st['step_ms']:.2f} ms "
+                  f"(schedule {st['schedule_ms']:.2f}, solve {st['solve_ms']:.2f}), levels "
+                  f"{st['max_velocity_levels']}/{st['max_bias_levels']}", file=sys.stderr, flush=True)
+        if args.save_snapshot and rank == 0:
+            np.savez_compressed(args.save_snapshot, state=w.state())
+    preroll_s = time.perf_counter() - t_setup
+
+    for _ in range(args.warmup):
+        w.step_fixed()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
+
+    keys = ("broadphase_ms", "narrowphase_ms", "constraints_ms", "schedule_ms", "solve_ms", "integrate_ms", "step_ms")
+    acc = {k: 0.0 for k in keys}
+    launches = 0
+    last = None
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    with Clocks(local_rank) as clocks:
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            torch.cuda.synchronize()
+            w.step_fixed()
+            st = w.get_stats()
+            for k in keys:
+                acc[k] += st[k]
+            launches += st["kernel_launches"]
+            last = st
+        torch.cuda.synchronize()
+    clk = clocks.summary()
+    total_ms = acc["step_ms"]
+    if dist:
+        t = torch.tensor([total_ms], device=f"cuda:{local_rank}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world_size * n_dyn * args.steps / (total_ms / 1e3)
+
+    # e2e through the C-ABI with host buffers
+    ft = np.zeros((w.n, 6), np.float32)
+    tr = np.zeros((w.n, 7), np.float32)
+    e2e_s = 0.0
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        w.upload_forces(ft)
+        w.step_fixed()
+        w.transforms(tr)
+        e2e_s += time.perf_counter() - t0
+    e2e_value = world_size * n_dyn * args.steps / e2e_s
+
+    # roofline of the dominant kernel, from the last step's counts and the timed averages
+    pairs = w.broadphase_pairs()
+    points = last["num_contact_points"]
+    nb = narrow_bytes(sc, pairs, points)
+    cand = {
+        "k_narrow": (acc["narrowphase_ms"] / args.steps, nb),
+        "k_solve": (acc["solve_ms"] / args.steps, solve_bytes(points, n_dyn)),
+    }
+    kname = max(cand, key=lambda k: cand[k][0])
+    kms, kbytes = cand[kname]
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = kbytes / (kms / 1e3) / 1e9 if kms > 0 else 0.0
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        traffic = json.load(open(tfile)).get(args.workload, {}).get(kname)
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0 and world_size == 1:
+        state0 = snap if snap is not None else None
+        threads = os.cpu_count() or 1
+        n_steps, secs = cpu_leg(sc, res, state0, 10 ** 6, args.cpu_budget, threads)
+        cpu = {"value": n_dyn * n_steps / secs, "unit": "body-steps/s", "cores": threads, "kind": "port",
+               "sample": f"{n_steps} steps of the same workload from the same starting state (cold manifold "
+                         f"cache), reference pair order, {secs:.1f} s"}
+
+    ms_per_step = total_ms / args.steps
+    out = {
+        "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+        "config": dict(cfg, window=f"steps {preroll}+ of the run" if preroll else "from the initial scene",
+                       start_state="committed snapshot" if snap is not None else "simulated untimed",
+                       solver="fixed iterations, the reference's 4-wide batch order (bit-exact)",
+                       pair_order="canonical (GPU broad phase)", l2="flushed between timed steps (256 MB write)",
+                       parallelism="replicas" if world_size > 1 else "single GPU",
+                       contacts=points, pairs=int(pairs.shape[0]), islands=last["num_islands"],
+                       max_velocity_levels=last["max_velocity_levels"], max_bias_levels=last["max_bias_levels"]),
+        "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": int(ft.nbytes),
+                "d2h_bytes_per_step": int(tr.nbytes)},
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": kbytes,
+                     "avg_launch_ms": kms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+        "cpu_baseline": cpu,
+        "gpu_launches": launches,
+        "clocks": clk,
+        "stage_ms": {k: v / args.steps for k, v in acc.items()},
+        "model_gbs_step": step_bytes(n_dyn, nb - 40 * points, points, last["num_contact_constraints"]) /
+                          (ms_per_step / 1e3) / 1e9,
+        "preroll_s": preroll_s,
+    }
+    w.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_reference(args, sc, cfg, preroll, n_dyn):
+    snap = load_snapshot(args.workload, preroll)
+    if preroll and snap is None:
+        print(json.dumps({"impl": "reference", "unavailable": "starting-state snapshot for this workload is not "
+                                                              "committed; the CPU cannot simulate the untimed "
+                                                              "pre-roll within minutes"}))
+        return
+    from kizuriphysics3d_gb300 import resolve
+    res = resolve(sc)
+    threads = os.cpu_count() or 1
+    budget = max(30.0, min(240.0, 8.0 * (args.steps + args.warmup)))
+    n_steps, secs = cpu_leg(sc, res, snap, args.steps, budget, threads)
+    value = n_dyn * n_steps / secs
+    out = {"metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": 0, "steps": n_steps,
+           "warmup": 1, "ms_per_step": 1e3 * secs / max(n_steps, 1), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)", "impl": "reference",
+           "config": dict(cfg, window=f"steps {preroll}+ of the run" if preroll else "from the initial scene",
+                          pair_order="reference dynamic AABB tree"),
+           "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port",
+                            "sample": f"{n_steps} of {args.steps} requested steps within a {budget:.0f} s budget"},
+           "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

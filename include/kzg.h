@@ -135,7 +135,11 @@ typedef struct {
     uint32_t max_bias_levels;
     uint32_t cache_entries;
     uint32_t device_error;  /* bit mask of KZG_DEVERR_* raised by kernels */
-    float broadphase_ms, narrowphase_ms, constraints_ms, solve_ms, integrate_ms, step_ms;
+    uint32_t kernel_launches; /* kernels launched by the last step (own kernels + CUB passes) */
+    /* CUDA-event times of the last step on the context stream: broad phase; narrow-phase kernel;
+     * constraint build + velocity integration; prepare + islands + batch schedule; solver kernel;
+     * cache store + position integration; whole step. */
+    float broadphase_ms, narrowphase_ms, constraints_ms, schedule_ms, solve_ms, integrate_ms, step_ms;
 } kzg_stats;
 
 #define KZG_DEVERR_PAIRS 1u     /* pair buffer overflow */

@@ -53,9 +53,9 @@ class KzgBodySoa(ctypes.Structure):
 class KzgStats(ctypes.Structure):
     _fields_ = [(n, u32) for n in ("num_bodies", "num_broadphase_pairs", "num_contact_constraints",
                                    "num_contact_points", "num_islands", "num_batches", "max_velocity_levels",
-                                   "max_bias_levels", "cache_entries", "device_error")] + \
-               [(n, f32) for n in ("broadphase_ms", "narrowphase_ms", "constraints_ms", "solve_ms", "integrate_ms",
-                                   "step_ms")]
+                                   "max_bias_levels", "cache_entries", "device_error", "kernel_launches")] + \
+               [(n, f32) for n in ("broadphase_ms", "narrowphase_ms", "constraints_ms", "schedule_ms", "solve_ms",
+                                   "integrate_ms", "step_ms")]
 
 
 EXPORTS = ["kzg_create", "kzg_destroy", "kzg_last_error", "kzg_set_stream", "kzg_synchronize",

@@ -98,6 +98,21 @@ kzg_status alloc_all(Ctx* ctx) {
     CK(dalloc(&ctx->vl_off, R + P + 1));
     CK(dalloc(&ctx->bl_off, R + P + 1));
     CK(dalloc(&ctx->isl_meta, 4 * P));
+    CK(dalloc(&ctx->onx, R + 2 * P + 2));
+    CK(dalloc(&ctx->hnx0, R + 2 * P + 2));
+    CK(dalloc(&ctx->hnx1, R + 2 * P + 2));
+    CK(dalloc(&ctx->body_stamp, B));
+    CK(cudaMemset(ctx->body_stamp, 0, sizeof(uint32_t) * B));
+    CK(dalloc(&ctx->body_loc, B));
+    CK(dalloc(&ctx->body_cnt, B));
+    CK(cudaMemset(ctx->body_cnt, 0, sizeof(uint32_t) * B));
+    CK(dalloc(&ctx->isl_bodies, 2 * P));
+    CK(dalloc(&ctx->last_local, 2 * P));
+    CK(dalloc(&ctx->con_la, P));
+    CK(dalloc(&ctx->con_lb, P));
+    CK(dalloc(&ctx->isl_small, P));
+    CK(dalloc(&ctx->isl_large, P));
+    CK(configure_kernels());
     CK(dalloc(&ctx->c_key, H));
     CK(cudaMemset(ctx->c_key, 0, sizeof(unsigned long long) * H));
     CK(dalloc(&ctx->c_np, H));
@@ -128,6 +143,8 @@ void free_all(Ctx* ctx) {
                     ctx->last_lvl, ctx->batch_cnt, ctx->batch_body, ctx->batch_mem, ctx->lvl_tmp, ctx->ids_tmp,
                     ctx->wl_list, ctx->vl_list, ctx->bl_list, ctx->wl_off, ctx->vl_off, ctx->bl_off, ctx->isl_meta,
                     ctx->c_key, ctx->c_np, ctx->c_pos, ctx->c_imp, ctx->dcnt, ctx->cub_tmp, ctx->hash_words,
+                    ctx->onx, ctx->hnx0, ctx->hnx1, ctx->body_stamp, ctx->body_loc, ctx->body_cnt,
+                    ctx->isl_bodies, ctx->last_local, ctx->con_la, ctx->con_lb, ctx->isl_small, ctx->isl_large,
                     ctx->shapes, ctx->hull_verts, ctx->face_sizes, ctx->face_idx};
     for (void* p : ptrs)
         if (p) cudaFree(p);

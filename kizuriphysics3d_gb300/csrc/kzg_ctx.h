@@ -50,6 +50,9 @@ struct Counters {  // device-side counters, copied back after each stage that si
     uint32_t max_vlev;
     uint32_t max_blev;
     uint32_t error;
+    uint32_t npoints;
+    uint32_t nsmall;
+    uint32_t nlarge;
     uint32_t cache_entries;
 };
 
@@ -119,7 +122,12 @@ struct Ctx {
     uint32_t* ids_tmp = nullptr;      // per point row id of the sweep being sorted
     uint32_t *wl_list = nullptr, *vl_list = nullptr, *bl_list = nullptr;   // per island point lists by level
     uint32_t *wl_off = nullptr, *vl_off = nullptr, *bl_off = nullptr;      // level offsets
-    uint32_t* isl_meta = nullptr;     // per island: nw, nv, nb levels, level offset base
+    uint32_t* isl_meta = nullptr;     // per island: warm / velocity / bias level counts, dynamic bodies
+    uint32_t *onx = nullptr, *hnx0 = nullptr, *hnx1 = nullptr;  // batch skip structures
+    uint32_t *body_stamp = nullptr, *body_loc = nullptr, *body_cnt = nullptr;  // per body scratch
+    uint32_t *isl_bodies = nullptr, *last_local = nullptr;     // per island body lists
+    uint32_t *con_la = nullptr, *con_lb = nullptr;             // per constraint local body indices
+    uint32_t *isl_small = nullptr, *isl_large = nullptr;       // islands by solve kernel
 
     // cache
     unsigned long long* c_key = nullptr;
@@ -136,6 +144,7 @@ struct Ctx {
     cudaEvent_t ev[8] = {};
     kzg_stats stats{};
     uint32_t frame = 0;
+    uint32_t launches = 0;
 };
 
 }  // namespace kzg

@@ -4,6 +4,8 @@
 #include <cstddef>
 #include <cstdint>
 
+#include <cuda_runtime.h>
+
 #include "../../include/kzg.h"
 
 namespace kzg {
@@ -11,6 +13,7 @@ namespace kzg {
 struct Ctx;
 
 size_t cub_temp_bytes(uint32_t max_items);
+cudaError_t configure_kernels();  // per-device kernel attributes (large dynamic shared memory)
 kzg_status step_canonical(Ctx& ctx, float dt);
 kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t num_pairs, float dt);
 kzg_status hash_state(Ctx& ctx, uint64_t* out);

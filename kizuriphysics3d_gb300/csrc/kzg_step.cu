@@ -230,6 +230,7 @@ __global__ void k_build_constraints(const uint2* __restrict__ pairs, const uint3
     con_b[c] = B;
     uint32_t n = m_count[i];
     con_np[c] = n;
+    atomicAdd(&cnt->npoints, n);
     unsigned long long key = m_key[i];
     con_key[c] = key;
     const bool sensor = ((b.flags[A] | b.flags[B]) & KZG_BODY_SENSOR) != 0u;
@@ -409,315 +410,11 @@ __global__ void k_island_starts(Counters* cnt, const uint32_t* __restrict__ head
     }
 }
 
-// ---------------------------------------------------------------------------------------------
-// schedule: one thread per island.  Reproduces the reference's greedy first-fit batching of
-// contact points (at most 4 per batch, no body - static ones included - twice in a batch,
-// sensors skipped; PhysicsWorld.cpp:680-717) and converts the three sequential sweeps into
-// dependency levels over dynamic bodies:
-//   warm start : every point in island constraint order          (:673)
-//   velocity   : batch order                                      (:718-722)
-//   bias       : points with positionBias > 0, constraint order    (:736-742)
-// A point's level is 1 + the level of the previous point of the same sweep on either of its
-// dynamic bodies, so each body sees exactly the reference's update sequence.
-// ---------------------------------------------------------------------------------------------
-struct SchedBufs {
-    const uint32_t *isl_start, *isl_con, *con_a, *con_b, *con_np, *con_bits;
-    const float4* bias;
-    const float* inv_mass;
-    uint32_t *batch_cnt, *batch_body, *batch_mem, *last, *lvl_tmp, *ids_tmp, *lvl_count;
-    uint32_t *wl_list, *vl_list, *bl_list, *wl_off, *vl_off, *bl_off, *meta;
-};
+}  // namespace kzg
 
-__device__ void sched_sort(uint32_t base, uint32_t loff, uint32_t npts, uint32_t nlev, const uint32_t* pts_level,
-                           const uint32_t* pts_id, uint32_t* count, uint32_t* list, uint32_t* off) {
-    // counting sort of npts points by level (levels 1..nlev) into list[base..], offsets off[loff..]
-    for (uint32_t l = 0; l <= nlev; ++l) count[loff + l] = 0;
-    for (uint32_t k = 0; k < npts; ++k) count[loff + pts_level[base + k] - 1]++;
-    uint32_t run = 0;
-    for (uint32_t l = 0; l < nlev; ++l) {
-        uint32_t c = count[loff + l];
-        off[loff + l] = run;
-        count[loff + l] = run;
-        run += c;
-    }
-    off[loff + nlev] = run;
-    for (uint32_t k = 0; k < npts; ++k) list[base + count[loff + pts_level[base + k] - 1]++] = pts_id[base + k];
-}
+#include "kzg_solver.cuh"
 
-__global__ void k_schedule(SchedBufs S, Counters* cnt) {
-    uint32_t isl = blockIdx.x * blockDim.x + threadIdx.x;
-    if (isl >= cnt->nislands) return;
-    const uint32_t s0 = S.isl_start[isl], s1 = S.isl_start[isl + 1];
-    const uint32_t base = 4u * s0;      // point region of this island
-    const uint32_t loff = base + isl;   // level-offset region (one extra entry per island)
-    uint32_t* lvl = S.lvl_tmp;          // per point region: level of each listed point
-    uint32_t* ids = S.ids_tmp;          // per point region: row id of each listed point
-
-    // ---- greedy first-fit batching (point order = constraint order, then point index)
-    uint32_t nbt = 0, first_open = 0;
-    for (uint32_t s = s0; s < s1; ++s) {
-        uint32_t c = S.isl_con[s];
-        if (S.con_bits[c] & 1u) continue;  // sensor
-        const uint32_t a = S.con_a[c], bb = S.con_b[c];
-        for (uint32_t p = 0; p < S.con_np[c]; ++p) {
-            uint32_t pt = 4u * c + p;
-            bool placed = false;
-            for (uint32_t bi = first_open; bi < nbt; ++bi) {
-                uint32_t cntb = S.batch_cnt[base + bi];
-                if (cntb >= 4u) continue;
-                const uint32_t* bodies = &S.batch_body[8u * (base + bi)];
-                bool conflict = false;
-                for (uint32_t k = 0; k < cntb; ++k) {
-                    uint32_t x = bodies[2 * k], y = bodies[2 * k + 1];
-                    if (x == a || x == bb || y == a || y == bb) { conflict = true; break; }
-                }
-                if (conflict) continue;
-                S.batch_body[8u * (base + bi) + 2 * cntb] = a;
-                S.batch_body[8u * (base + bi) + 2 * cntb + 1] = bb;
-                S.batch_mem[4u * (base + bi) + cntb] = pt;
-                S.batch_cnt[base + bi] = cntb + 1;
-                if (cntb + 1 == 4u && bi == first_open)
-                    while (first_open < nbt && S.batch_cnt[base + first_open] >= 4u) ++first_open;
-                placed = true;
-                break;
-            }
-            if (!placed) {
-                S.batch_cnt[base + nbt] = 1;
-                S.batch_body[8u * (base + nbt)] = a;
-                S.batch_body[8u * (base + nbt) + 1] = bb;
-                S.batch_mem[4u * (base + nbt)] = pt;
-                ++nbt;
-            }
-        }
-    }
-    // ---- velocity levels in batch order
-    uint32_t nv = 0, nvpts = 0;
-    for (uint32_t bi = 0; bi < nbt; ++bi) {
-        uint32_t cntb = S.batch_cnt[base + bi];
-        for (uint32_t k = 0; k < cntb; ++k) {
-            uint32_t pt = S.batch_mem[4u * (base + bi) + k];
-            uint32_t c = pt >> 2;
-            uint32_t bits = S.con_bits[c];
-            uint32_t l = 0;
-            if (bits & 2u) l = max(l, S.last[S.con_a[c]]);
-            if (bits & 4u) l = max(l, S.last[S.con_b[c]]);
-            ++l;
-            if (bits & 2u) S.last[S.con_a[c]] = l;
-            if (bits & 4u) S.last[S.con_b[c]] = l;
-            nv = max(nv, l);
-            lvl[base + nvpts] = l;
-            ids[base + nvpts] = pt;
-            ++nvpts;
-        }
-    }
-    for (uint32_t s = s0; s < s1; ++s) {
-        uint32_t c = S.isl_con[s];
-        S.last[S.con_a[c]] = 0;
-        S.last[S.con_b[c]] = 0;
-    }
-    sched_sort(base, loff, nvpts, nv, lvl, ids, S.lvl_count, S.vl_list, S.vl_off);
-
-    // ---- warm-start levels: all points, constraint order
-    uint32_t nw = 0, nwpts = 0;
-    for (uint32_t s = s0; s < s1; ++s) {
-        uint32_t c = S.isl_con[s];
-        uint32_t bits = S.con_bits[c];
-        for (uint32_t p = 0; p < S.con_np[c]; ++p) {
-            uint32_t l = 0;
-            if (bits & 2u) l = max(l, S.last[S.con_a[c]]);
-            if (bits & 4u) l = max(l, S.last[S.con_b[c]]);
-            ++l;
-            if (bits & 2u) S.last[S.con_a[c]] = l;
-            if (bits & 4u) S.last[S.con_b[c]] = l;
-            nw = max(nw, l);
-            lvl[base + nwpts] = l;
-            ids[base + nwpts] = 4u * c + p;
-            ++nwpts;
-        }
-    }
-    for (uint32_t s = s0; s < s1; ++s) {
-        uint32_t c = S.isl_con[s];
-        S.last[S.con_a[c]] = 0;
-        S.last[S.con_b[c]] = 0;
-    }
-    sched_sort(base, loff, nwpts, nw, lvl, ids, S.lvl_count, S.wl_list, S.wl_off);
-
-    // ---- bias levels: points with positionBias > 0 of constraints with a massive body
-    uint32_t nbl = 0, nbpts = 0;
-    for (uint32_t s = s0; s < s1; ++s) {
-        uint32_t c = S.isl_con[s];
-        const uint32_t a = S.con_a[c], bb = S.con_b[c];
-        if (S.inv_mass[a] <= 0.0f && S.inv_mass[bb] <= 0.0f) continue;
-        uint32_t bits = S.con_bits[c];
-        for (uint32_t p = 0; p < S.con_np[c]; ++p) {
-            if (S.bias[4u * c + p].y <= 0.0f) continue;
-            uint32_t l = 0;
-            if (bits & 2u) l = max(l, S.last[a]);
-            if (bits & 4u) l = max(l, S.last[bb]);
-            ++l;
-            if (bits & 2u) S.last[a] = l;
-            if (bits & 4u) S.last[bb] = l;
-            nbl = max(nbl, l);
-            lvl[base + nbpts] = l;
-            ids[base + nbpts] = 4u * c + p;
-            ++nbpts;
-        }
-    }
-    for (uint32_t s = s0; s < s1; ++s) {
-        uint32_t c = S.isl_con[s];
-        S.last[S.con_a[c]] = 0;
-        S.last[S.con_b[c]] = 0;
-    }
-    sched_sort(base, loff, nbpts, nbl, lvl, ids, S.lvl_count, S.bl_list, S.bl_off);
-
-    S.meta[4 * isl + 0] = nw;
-    S.meta[4 * isl + 1] = nv;
-    S.meta[4 * isl + 2] = nbl;
-    S.meta[4 * isl + 3] = nbt;
-    atomicAdd(&cnt->batches, nbt);
-    atomicMax(&cnt->max_vlev, nv);
-    atomicMax(&cnt->max_blev, nbl);
-}
-
-// ---------------------------------------------------------------------------------------------
-// solve: one CTA per island, level by level
-// ---------------------------------------------------------------------------------------------
-struct SolveBufs {
-    const uint32_t *isl_start, *con_a, *con_b, *con_bits, *meta;
-    const uint32_t *wl_list, *vl_list, *bl_list, *wl_off, *vl_off, *bl_off;
-    DeviceRows r;
-    DeviceBodies b;
-    uint32_t vel_iters, pos_iters;
-    float ws_factor;
-    int vel_bias;
-};
-
-// WarmStart for one point (ContactSolver.cpp:117-132 + ApplyImpulsePair :32-43).
-__device__ __forceinline__ void warm_point(const SolveBufs& S, uint32_t row) {
-    uint32_t c = row >> 2;
-    uint32_t bits = S.con_bits[c];
-    const uint32_t A = S.con_a[c], B = S.con_b[c];
-    float4 im = S.r.imp[row];
-    Vec3 n = V3(S.r.n[row]), t1 = V3(S.r.t1[row]), t2 = V3(S.r.t2[row]);
-    Vec3 imp = ((n * im.x + t1 * im.y) + t2 * im.z) * S.ws_factor;
-    if (bits & 2u) {
-        Vec3 rA = V3(S.r.rA[row]);
-        S.b.lv[A] = F4(V3(S.b.lv[A]) + imp * S.b.inv_mass[A], 0.0f);
-        S.b.av[A] = F4(V3(S.b.av[A]) + M3(&S.b.iiw[3 * A]) * rA.cross(imp), 0.0f);
-    }
-    if (bits & 4u) {
-        Vec3 rB = V3(S.r.rB[row]);
-        S.b.lv[B] = F4(V3(S.b.lv[B]) - imp * S.b.inv_mass[B], 0.0f);
-        S.b.av[B] = F4(V3(S.b.av[B]) - M3(&S.b.iiw[3 * B]) * rB.cross(imp), 0.0f);
-    }
-}
-
-// One lane of SolveVelocityBatchSIMD (ContactSolverSIMD.cpp:93-256): friction t1, t2 (relative
-// velocity recomputed before each axis), then normal; only _mm_{add,sub,mul,min,max}_ps semantics.
-__device__ __forceinline__ void velocity_point(const SolveBufs& S, uint32_t row) {
-    uint32_t c = row >> 2;
-    uint32_t bits = S.con_bits[c];
-    const uint32_t A = S.con_a[c], B = S.con_b[c];
-    const Vec3 rA = V3(S.r.rAr[row]), rB = V3(S.r.rBr[row]);
-    Vec3 vA = V3(S.b.lv[A]), wA = V3(S.b.av[A]), vB = V3(S.b.lv[B]), wB = V3(S.b.av[B]);
-    const float invA = S.b.inv_mass[A], invB = S.b.inv_mass[B];
-    const Mat3 IA = M3(&S.b.iiw[3 * A]), IB = M3(&S.b.iiw[3 * B]);
-    const float4 n4 = S.r.n[row], t14 = S.r.t1[row], t24 = S.r.t2[row], m4 = S.r.mass[row];
-    float4 im = S.r.imp[row];
-    const float4 bias = S.r.bias[row];
-    const float nb = bias.x + (S.vel_bias ? bias.y : 0.0f);
-    const float fric = t14.w;
-    float nacc = im.x, t1acc = im.y, t2acc = im.z;
-#pragma unroll
-    for (int t = 0; t < 3; ++t) {
-        const Vec3 dir = t == 0 ? V3(t14) : (t == 1 ? V3(t24) : V3(n4));
-        Vec3 wa = wA.cross(rA), wb = wB.cross(rB);
-        Vec3 rel((vA.x + wa.x) - (vB.x + wb.x), (vA.y + wa.y) - (vB.y + wb.y), (vA.z + wa.z) - (vB.z + wb.z));
-        float vd = rel.dot(dir);
-        float dl;
-        if (t < 2) {
-            const float mass = t == 0 ? m4.y : m4.z;
-            const float acc = t == 0 ? t1acc : t2acc;
-            float lambda = (0.0f - mass) * vd;
-            float maxf = fric * nacc;
-            float na = acc + lambda;
-            float lo = 0.0f - maxf;
-            na = na > lo ? na : lo;
-            na = na < maxf ? na : maxf;
-            dl = na - acc;
-            if (t == 0) t1acc = na; else t2acc = na;
-        } else {
-            float lambda = (0.0f - m4.x) * (vd - nb);
-            float na = nacc + lambda;
-            na = na > 0.0f ? na : 0.0f;
-            dl = na - nacc;
-            nacc = na;
-        }
-        Vec3 imp(dir.x * dl, dir.y * dl, dir.z * dl);
-        vA = Vec3(vA.x + imp.x * invA, vA.y + imp.y * invA, vA.z + imp.z * invA);
-        wA = wA + IA * rA.cross(imp);
-        vB = Vec3(vB.x - imp.x * invB, vB.y - imp.y * invB, vB.z - imp.z * invB);
-        wB = wB - IB * rB.cross(imp);
-    }
-    if (bits & 2u) { S.b.lv[A] = F4(vA, 0.0f); S.b.av[A] = F4(wA, 0.0f); }
-    if (bits & 4u) { S.b.lv[B] = F4(vB, 0.0f); S.b.av[B] = F4(wB, 0.0f); }
-    S.r.imp[row] = make_float4(nacc, t1acc, t2acc, im.w);
-}
-
-// SolveBiasConstraint for one point (ContactSolver.cpp:265-289).
-__device__ __forceinline__ void bias_point(const SolveBufs& S, uint32_t row) {
-    uint32_t c = row >> 2;
-    uint32_t bits = S.con_bits[c];
-    const uint32_t A = S.con_a[c], B = S.con_b[c];
-    const Vec3 rA = V3(S.r.rAr[row]), rB = V3(S.r.rBr[row]);
-    const Vec3 n = V3(S.r.n[row]);
-    const float nm = S.r.mass[row].x, pbias = S.r.bias[row].y;
-    float4 im = S.r.imp[row];
-    Vec3 vr = (V3(S.b.plv[A]) + V3(S.b.pav[A]).cross(rA)) - (V3(S.b.plv[B]) + V3(S.b.pav[B]).cross(rB));
-    float lambda = -nm * (vr.dot(n) - pbias);
-    float ni = rmax(im.w + lambda, 0.0f);
-    lambda = ni - im.w;
-    im.w = ni;
-    S.r.imp[row] = im;
-    Vec3 imp = n * lambda;
-    if (bits & 2u) {
-        S.b.plv[A] = F4(V3(S.b.plv[A]) + imp * S.b.inv_mass[A], 0.0f);
-        S.b.pav[A] = F4(V3(S.b.pav[A]) + M3(&S.b.iiw[3 * A]) * rA.cross(imp), 0.0f);
-    }
-    if (bits & 4u) {
-        S.b.plv[B] = F4(V3(S.b.plv[B]) - imp * S.b.inv_mass[B], 0.0f);
-        S.b.pav[B] = F4(V3(S.b.pav[B]) - M3(&S.b.iiw[3 * B]) * rB.cross(imp), 0.0f);
-    }
-}
-
-__global__ void __launch_bounds__(128) k_solve(SolveBufs S, const Counters* cnt) {
-    const uint32_t nisl = cnt->nislands;
-    for (uint32_t isl = blockIdx.x; isl < nisl; isl += gridDim.x) {
-        const uint32_t base = 4u * S.isl_start[isl];
-        const uint32_t loff = base + isl;
-        const uint32_t nw = S.meta[4 * isl], nv = S.meta[4 * isl + 1], nbl = S.meta[4 * isl + 2];
-        for (uint32_t l = 0; l < nw; ++l) {
-            const uint32_t e = S.wl_off[loff + l + 1];
-            for (uint32_t k = S.wl_off[loff + l] + threadIdx.x; k < e; k += blockDim.x) warm_point(S, S.wl_list[base + k]);
-            __syncthreads();
-        }
-        for (uint32_t it = 0; it < S.vel_iters; ++it)
-            for (uint32_t l = 0; l < nv; ++l) {
-                const uint32_t e = S.vl_off[loff + l + 1];
-                for (uint32_t k = S.vl_off[loff + l] + threadIdx.x; k < e; k += blockDim.x)
-                    velocity_point(S, S.vl_list[base + k]);
-                __syncthreads();
-            }
-        if (!S.vel_bias)
-            for (uint32_t it = 0; it < S.pos_iters; ++it)
-                for (uint32_t l = 0; l < nbl; ++l) {
-                    const uint32_t e = S.bl_off[loff + l + 1];
-                    for (uint32_t k = S.bl_off[loff + l] + threadIdx.x; k < e; k += blockDim.x)
-                        bias_point(S, S.bl_list[base + k]);
-                    __syncthreads();
-                }
-    }
-}
+namespace kzg {
 
 // ---------------------------------------------------------------------------------------------
 // cache store (:568-581) and position integration (:276-290, 785-802, 854-861)
@@ -819,6 +516,11 @@ size_t cub_temp_bytes(uint32_t max_items) {
     return std::max(std::max(a, b), std::max(c, d));
 }
 
+cudaError_t configure_kernels() {
+    return cudaFuncSetAttribute(k_solve_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(2 * kCtaBodiesMax * sizeof(float4)));
+}
+
 static int bits_for(uint32_t v) {
     int b = 1;
     while (b < 32 && (1ull << b) <= v) ++b;
@@ -835,11 +537,15 @@ static kzg_status step_after_pairs(Ctx& ctx, float dt) {
     if (np > 0) {
         k_narrow<<<blocks_for(np, 128), 128, 0, st>>>(T, ctx.b, ctx.pairs, ctx.dcnt, ctx.m_count, ctx.m_data,
                                                       ctx.m_key, &ctx.dcnt->error);
+        ++ctx.launches;
+    }
+    KZG_CK(cudaEventRecord(ctx.ev[2], st));
+    if (np > 0) {
         k_con_flags<<<blocks_for(np), kThreads, 0, st>>>(ctx.m_count, ctx.m_key, ctx.dcnt, ctx.con_flag);
         size_t tb = ctx.cub_tmp_bytes;
         KZG_CK(cub::DeviceScan::ExclusiveSum(ctx.cub_tmp, tb, ctx.con_flag, ctx.con_index, (int)np, st));
+        ctx.launches += 3;
     }
-    KZG_CK(cudaEventRecord(ctx.ev[2], st));
     if (np > 0)
         k_build_constraints<<<blocks_for(np), kThreads, 0, st>>>(
             ctx.pairs, ctx.con_flag, ctx.con_index, ctx.m_count, ctx.m_data, ctx.m_key, ctx.b, ctx.dcnt,
@@ -847,6 +553,7 @@ static kzg_status step_after_pairs(Ctx& ctx, float dt) {
             ctx.c_np, ctx.c_pos, ctx.c_imp, ctx.cfg.max_cache_entries, ctx.ws.warm_start);
     k_integrate_vel<<<blocks_for(nb), kThreads, 0, st>>>(
         ctx.b, nb, make_float3(ctx.ws.gravity[0], ctx.ws.gravity[1], ctx.ws.gravity[2]), dt);
+    ctx.launches += np > 0 ? 2 : 1;
     kzg_status s = fetch_counters(ctx);
     if (s != KZG_OK) return s;
     const uint32_t nc = ctx.hcnt->ncons;
@@ -870,23 +577,34 @@ static kzg_status step_after_pairs(Ctx& ctx, float dt) {
         if (s != KZG_OK) return s;
         const uint32_t ni = ctx.hcnt->nislands;
         SchedBufs SB{ctx.isl_start, ctx.isl_con, ctx.con_a, ctx.con_b, ctx.con_np, ctx.con_bits, ctx.r.bias,
-                     ctx.b.inv_mass, ctx.batch_cnt, ctx.batch_body, ctx.batch_mem, ctx.last_lvl, ctx.lvl_tmp,
-                     ctx.ids_tmp, ctx.lvl_count, ctx.wl_list, ctx.vl_list,
-                     ctx.bl_list, ctx.wl_off, ctx.vl_off, ctx.bl_off, ctx.isl_meta};
-        k_schedule<<<blocks_for(ni, 64), 64, 0, st>>>(SB, ctx.dcnt);
+                     ctx.b.inv_mass, ctx.frame, ctx.batch_cnt, ctx.batch_body, ctx.batch_mem, ctx.onx, ctx.hnx0,
+                     ctx.hnx1, ctx.body_stamp, ctx.body_loc, ctx.body_cnt, ctx.isl_bodies, ctx.last_local,
+                     ctx.con_la, ctx.con_lb, ctx.lvl_tmp, ctx.ids_tmp, ctx.lvl_count, ctx.wl_list, ctx.vl_list,
+                     ctx.bl_list, ctx.wl_off, ctx.vl_off, ctx.bl_off, ctx.isl_meta, ctx.isl_small, ctx.isl_large};
+        k_schedule<<<blocks_for(ni, 32), 32, 0, st>>>(SB, ctx.dcnt);
+        ctx.launches += 16;  // prepare, union-find (3), island sort (4 CUB passes), heads, scan (2), starts, schedule
         KZG_CK(cudaEventRecord(ctx.ev[4], st));
-        SolveBufs SV{ctx.isl_start, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.isl_meta, ctx.wl_list, ctx.vl_list,
-                     ctx.bl_list, ctx.wl_off, ctx.vl_off, ctx.bl_off, ctx.r, ctx.b, ctx.ss.velocity_iterations,
+        SolveBufs SV{ctx.isl_start, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.con_la, ctx.con_lb, ctx.isl_meta,
+                     ctx.isl_bodies, ctx.wl_list, ctx.vl_list, ctx.bl_list, ctx.wl_off, ctx.vl_off, ctx.bl_off,
+                     ctx.isl_small, ctx.isl_large, ctx.r, ctx.b, ctx.ss.velocity_iterations,
                      ctx.ss.position_iterations, ctx.ss.warm_start_factor, ctx.ss.use_velocity_bias};
-        unsigned grid = ni < 65535u ? ni : 65535u;
-        if (grid > 0) k_solve<<<grid, 128, 0, st>>>(SV, ctx.dcnt);
+        if (ni > 0) {
+            const unsigned gw = std::min<unsigned>(blocks_for(ni, kWarpsPerBlock), 152u * 16u);
+            k_solve_warp<<<gw, kWarpsPerBlock * 32, kWarpsPerBlock * 2 * kWarpBodies * sizeof(float4), st>>>(SV, ctx.dcnt);
+            const unsigned gc = std::min<unsigned>(ni, 152u * 2u);
+            k_solve_cta<<<gc, kCtaThreads, 2 * kCtaBodiesMax * sizeof(float4), st>>>(SV, ctx.dcnt, kCtaBodiesMax);
+            ctx.launches += 2;
+        }
+        KZG_CK(cudaEventRecord(ctx.ev[5], st));
+        ++ctx.launches;
         k_cache_store<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.con_key, ctx.con_np, ctx.r, ctx.c_key,
                                                            ctx.c_np, ctx.c_pos, ctx.c_imp, ctx.cfg.max_cache_entries);
     } else {
         KZG_CK(cudaEventRecord(ctx.ev[4], st));
+        KZG_CK(cudaEventRecord(ctx.ev[5], st));
     }
-    KZG_CK(cudaEventRecord(ctx.ev[5], st));
     k_integrate_pos<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, dt, ctx.ss.use_velocity_bias);
+    ++ctx.launches;
     KZG_CK(cudaEventRecord(ctx.ev[6], st));
     KZG_CK(cudaGetLastError());
     s = fetch_counters(ctx);
@@ -905,16 +623,19 @@ static kzg_status finish_stats(Ctx& ctx) {
     s.num_bodies = ctx.nbodies;
     s.num_broadphase_pairs = h.npairs;
     s.num_contact_constraints = h.ncons;
+    s.num_contact_points = h.npoints;
     s.num_islands = h.nislands;
     s.num_batches = h.batches;
     s.max_velocity_levels = h.max_vlev;
     s.max_bias_levels = h.max_blev;
     s.cache_entries = h.cache_entries;
     s.device_error = h.error;
+    s.kernel_launches = ctx.launches;
     cudaEventElapsedTime(&s.broadphase_ms, ctx.ev[0], ctx.ev[1]);
     cudaEventElapsedTime(&s.narrowphase_ms, ctx.ev[1], ctx.ev[2]);
     cudaEventElapsedTime(&s.constraints_ms, ctx.ev[2], ctx.ev[3]);
-    cudaEventElapsedTime(&s.solve_ms, ctx.ev[3], ctx.ev[5]);
+    cudaEventElapsedTime(&s.schedule_ms, ctx.ev[3], ctx.ev[4]);
+    cudaEventElapsedTime(&s.solve_ms, ctx.ev[4], ctx.ev[5]);
     cudaEventElapsedTime(&s.integrate_ms, ctx.ev[5], ctx.ev[6]);
     cudaEventElapsedTime(&s.step_ms, ctx.ev[0], ctx.ev[6]);
     if (h.error) {
@@ -928,8 +649,10 @@ kzg_status step_canonical(Ctx& ctx, float dt) {
     cudaStream_t st = ctx.stream;
     const uint32_t nb = ctx.nbodies;
     ++ctx.frame;
+    ctx.launches = 0;
     reset_counters_async(ctx);
     KZG_CK(cudaEventRecord(ctx.ev[0], st));
+    ctx.launches += 8;  // aabb, cell sort (4 CUB passes), find pairs, key sort + unpack counted below
     k_aabb<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, ctx.shapes, nb, 1.0f / ctx.cell_size, ctx.is_large,
                                                 ctx.cell_keys, ctx.cell_vals);
     size_t tb = ctx.cub_tmp_bytes;
@@ -948,6 +671,7 @@ kzg_status step_canonical(Ctx& ctx, float dt) {
         tb = ctx.cub_tmp_bytes;
         KZG_CK(cub::DeviceRadixSort::SortKeys(ctx.cub_tmp, tb, ctx.pair_keys, ctx.pair_keys_sorted, (int)np, 0, 64, st));
         k_unpack_pairs<<<blocks_for(np), kThreads, 0, st>>>(ctx.pair_keys_sorted, ctx.dcnt, ctx.pairs);
+        ctx.launches += 5;
     }
     s = step_after_pairs(ctx, dt);
     if (s != KZG_OK) return s;
@@ -961,6 +685,7 @@ kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t np, floa
         return KZG_ERR_CAPACITY;
     }
     ++ctx.frame;
+    ctx.launches = np > 0 ? 1 : 0;
     reset_counters_async(ctx);
     KZG_CK(cudaEventRecord(ctx.ev[0], st));
     if (np > 0) {
