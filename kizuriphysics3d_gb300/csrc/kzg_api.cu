@@ -59,6 +59,7 @@ kzg_status alloc_all(Ctx* ctx) {
     CK(dalloc(&ctx->m_count, P));
     CK(dalloc(&ctx->m_data, 12 * P));
     CK(dalloc(&ctx->m_key, P));
+    CK(dalloc(&ctx->epa_list, P));
     CK(dalloc(&ctx->con_flag, P));
     CK(dalloc(&ctx->con_index, P));
     CK(dalloc(&ctx->con_pair, P));
@@ -84,11 +85,10 @@ kzg_status alloc_all(Ctx* ctx) {
     CK(dalloc(&ctx->isl_start, P + 1));
     CK(dalloc(&ctx->isl_pts, P));
     CK(dalloc(&ctx->lvl_count, R + P + 1));
-    CK(dalloc(&ctx->last_lvl, B));
-    CK(cudaMemset(ctx->last_lvl, 0, sizeof(uint32_t) * B));
-    CK(dalloc(&ctx->batch_cnt, R));
-    CK(dalloc(&ctx->batch_body, 8 * R));
-    CK(dalloc(&ctx->batch_mem, 4 * R));
+    CK(dalloc(&ctx->brec, 4 * (R + P + 1)));
+    CK(dalloc(&ctx->last_g, 3 * 2 * P));
+    CK(dalloc(&ctx->first_w, P));
+    CK(dalloc(&ctx->first_b, P));
     CK(dalloc(&ctx->lvl_tmp, R));
     CK(dalloc(&ctx->ids_tmp, R));
     CK(dalloc(&ctx->wl_list, R));
@@ -98,16 +98,10 @@ kzg_status alloc_all(Ctx* ctx) {
     CK(dalloc(&ctx->vl_off, R + P + 1));
     CK(dalloc(&ctx->bl_off, R + P + 1));
     CK(dalloc(&ctx->isl_meta, 4 * P));
-    CK(dalloc(&ctx->onx, R + 2 * P + 2));
-    CK(dalloc(&ctx->hnx0, R + 2 * P + 2));
-    CK(dalloc(&ctx->hnx1, R + 2 * P + 2));
     CK(dalloc(&ctx->body_stamp, B));
     CK(cudaMemset(ctx->body_stamp, 0, sizeof(uint32_t) * B));
     CK(dalloc(&ctx->body_loc, B));
-    CK(dalloc(&ctx->body_cnt, B));
-    CK(cudaMemset(ctx->body_cnt, 0, sizeof(uint32_t) * B));
     CK(dalloc(&ctx->isl_bodies, 2 * P));
-    CK(dalloc(&ctx->last_local, 2 * P));
     CK(dalloc(&ctx->con_la, P));
     CK(dalloc(&ctx->con_lb, P));
     CK(dalloc(&ctx->isl_small, P));
@@ -135,16 +129,16 @@ void free_all(Ctx* ctx) {
                     b.iiw, b.iil, b.inv_mass, b.shape, b.motion, b.flags, b.layer, b.mask, b.world, b.packed,
                     ctx->is_large, ctx->large_list, ctx->large_off, ctx->cell_keys, ctx->cell_keys_sorted,
                     ctx->cell_vals, ctx->cell_vals_sorted, ctx->pair_keys, ctx->pair_keys_sorted, ctx->pairs,
-                    ctx->m_count, ctx->m_data, ctx->m_key, ctx->con_flag, ctx->con_index, ctx->con_pair, ctx->con_a,
+                    ctx->m_count, ctx->m_data, ctx->m_key, ctx->epa_list, ctx->con_flag, ctx->con_index, ctx->con_pair, ctx->con_a,
                     ctx->con_b, ctx->con_np, ctx->con_bits, ctx->con_fr, ctx->con_key, ctx->r.pA, ctx->r.pB, ctx->r.n,
                     ctx->r.t1, ctx->r.t2, ctx->r.rA, ctx->r.rB, ctx->r.rAr, ctx->r.rBr, ctx->r.laA, ctx->r.laB,
                     ctx->r.mass, ctx->r.imp, ctx->r.bias, ctx->uf, ctx->isl_key, ctx->isl_key_sorted,
                     ctx->isl_con_in, ctx->isl_con, ctx->isl_head, ctx->isl_start, ctx->isl_pts, ctx->lvl_count,
-                    ctx->last_lvl, ctx->batch_cnt, ctx->batch_body, ctx->batch_mem, ctx->lvl_tmp, ctx->ids_tmp,
+                    ctx->brec, ctx->last_g, ctx->first_w, ctx->first_b, ctx->lvl_tmp, ctx->ids_tmp,
                     ctx->wl_list, ctx->vl_list, ctx->bl_list, ctx->wl_off, ctx->vl_off, ctx->bl_off, ctx->isl_meta,
                     ctx->c_key, ctx->c_np, ctx->c_pos, ctx->c_imp, ctx->dcnt, ctx->cub_tmp, ctx->hash_words,
-                    ctx->onx, ctx->hnx0, ctx->hnx1, ctx->body_stamp, ctx->body_loc, ctx->body_cnt,
-                    ctx->isl_bodies, ctx->last_local, ctx->con_la, ctx->con_lb, ctx->isl_small, ctx->isl_large,
+                    ctx->body_stamp, ctx->body_loc, ctx->isl_bodies, ctx->con_la, ctx->con_lb, ctx->isl_small,
+                    ctx->isl_large,
                     ctx->shapes, ctx->hull_verts, ctx->face_sizes, ctx->face_idx};
     for (void* p : ptrs)
         if (p) cudaFree(p);

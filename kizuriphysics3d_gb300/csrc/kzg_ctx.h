@@ -53,6 +53,7 @@ struct Counters {  // device-side counters, copied back after each stage that si
     uint32_t npoints;
     uint32_t nsmall;
     uint32_t nlarge;
+    uint32_t nepa;
     uint32_t cache_entries;
 };
 
@@ -95,6 +96,7 @@ struct Ctx {
     uint32_t* m_count = nullptr;
     float4* m_data = nullptr;  // 12 float4 per pair
     unsigned long long* m_key = nullptr;
+    uint32_t* epa_list = nullptr;  // pairs whose narrow phase needs EPA (warp pass)
 
     // constraints
     uint32_t* con_flag = nullptr;    // per pair: 1 if it makes a constraint
@@ -114,18 +116,16 @@ struct Ctx {
     uint32_t* isl_start = nullptr;    // nislands + 1
     uint32_t* isl_pts = nullptr;      // first point slot of each island in the level lists
     uint32_t* lvl_count = nullptr;    // per island level counters (4*ncons + nislands + 1)
-    uint32_t* last_lvl = nullptr;     // per body: level of its last update in the current sweep
-    uint32_t* batch_cnt = nullptr;    // per batch member count (batches <= points)
-    uint32_t* batch_body = nullptr;   // 8 body slots per batch
-    uint32_t* batch_mem = nullptr;    // 4 point rows per batch
-    uint32_t* lvl_tmp = nullptr;      // per point level of the sweep being sorted
-    uint32_t* ids_tmp = nullptr;      // per point row id of the sweep being sorted
+    uint4* brec = nullptr;            // batch records, 64 B each (4*ncons + nislands + 1)
+    uint32_t* last_g = nullptr;       // level tables that do not fit shared memory (3 x 2*ncons)
+    uint32_t *first_w = nullptr, *first_b = nullptr;  // per sorted constraint: first warm / bias level
+    uint32_t* lvl_tmp = nullptr;      // per point: velocity level (batch order)
+    uint32_t* ids_tmp = nullptr;      // per point: velocity item row (batch order)
     uint32_t *wl_list = nullptr, *vl_list = nullptr, *bl_list = nullptr;   // per island point lists by level
     uint32_t *wl_off = nullptr, *vl_off = nullptr, *bl_off = nullptr;      // level offsets
     uint32_t* isl_meta = nullptr;     // per island: warm / velocity / bias level counts, dynamic bodies
-    uint32_t *onx = nullptr, *hnx0 = nullptr, *hnx1 = nullptr;  // batch skip structures
-    uint32_t *body_stamp = nullptr, *body_loc = nullptr, *body_cnt = nullptr;  // per body scratch
-    uint32_t *isl_bodies = nullptr, *last_local = nullptr;     // per island body lists
+    uint32_t *body_stamp = nullptr, *body_loc = nullptr;       // per body scratch
+    uint32_t* isl_bodies = nullptr;                             // per island dynamic bodies
     uint32_t *con_la = nullptr, *con_lb = nullptr;             // per constraint local body indices
     uint32_t *isl_small = nullptr, *isl_large = nullptr;       // islands by solve kernel
 

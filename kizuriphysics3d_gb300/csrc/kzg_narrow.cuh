@@ -396,94 +396,243 @@ __device__ inline void epa_finish(const EpaFace& f, const SP* vs, EpaOut& r) {
     r.pB = (vs[f.a].pB * u + vs[f.b].pB * v) + vs[f.c].pB * w;
 }
 
-// Scratch for one EPA run (thread-local memory).
-struct EpaScratch {
-    SP verts[kEpaVerts];
-    EpaFace faces[kEpaFaces];
+// Polytope of one EPA run, in shared memory, owned by one warp.
+struct EpaWarpSmem {
+    float vp[kEpaVerts][3], va[kEpaVerts][3], vb[kEpaVerts][3];  // SupportPoint p, pointA, pointB
+    float fnx[kEpaFaces], fny[kEpaFaces], fnz[kEpaFaces], fd[kEpaFaces];
+    uint8_t fa[kEpaFaces], fb[kEpaFaces], fc[kEpaFaces], dead[kEpaFaces];
     uint16_t vis[kEpaFaces];
     uint8_t hu[kEpaHorizon], hv[kEpaHorizon];
 };
 
-__device__ inline void epa(const SupportMap& map, const GjkOut& g, float tol, uint32_t max_iter, EpaScratch& S,
-                           EpaOut& r, uint32_t* err) {
+__device__ __forceinline__ Vec3 sm_vp(const EpaWarpSmem& S, uint32_t i) { return Vec3(S.vp[i][0], S.vp[i][1], S.vp[i][2]); }
+
+// BuildFace (EPA.cpp:16-31) on vertices held in shared memory.
+__device__ __forceinline__ bool epa_build_face_sm(uint32_t& fa, uint32_t& fb, uint32_t& fc, Vec3& n_out, float& d_out,
+                                                  const EpaWarpSmem& S) {
+    Vec3 A = sm_vp(S, fa), B = sm_vp(S, fb), C = sm_vp(S, fc);
+    Vec3 n = (B - A).cross(C - A);
+    float len = n.len();
+    if (len < 1.0e-12f) return false;
+    n = n / len;
+    float d = n.dot(A);
+    if (d < 0.0f) {
+        n = -n;
+        d = -d;
+        uint32_t t = fb; fb = fc; fc = t;
+    }
+    n_out = n;
+    d_out = d;
+    return true;
+}
+
+__device__ __forceinline__ void sm_put_face(EpaWarpSmem& S, uint32_t k, uint32_t a, uint32_t b, uint32_t c, const Vec3& n,
+                                            float d) {
+    S.fa[k] = (uint8_t)a; S.fb[k] = (uint8_t)b; S.fc[k] = (uint8_t)c;
+    S.fnx[k] = n.x; S.fny[k] = n.y; S.fnz[k] = n.z; S.fd[k] = d;
+}
+
+// FinishFace (EPA.cpp:163-172) for face k of the shared polytope.
+__device__ inline void epa_finish_sm(const EpaWarpSmem& S, uint32_t k, EpaOut& r) {
+    const Vec3 n(S.fnx[k], S.fny[k], S.fnz[k]);
+    const float dist = S.fd[k];
+    const uint32_t ia = S.fa[k], ib = S.fb[k], ic = S.fc[k];
+    Vec3 proj = n * dist;
+    Vec3 a = sm_vp(S, ia), b = sm_vp(S, ib), c = sm_vp(S, ic);
+    Vec3 v0 = b - a, v1 = c - a, v2 = proj - a;
+    float d00 = v0.dot(v0), d01 = v0.dot(v1), d11 = v1.dot(v1);
+    float d20 = v2.dot(v0), d21 = v2.dot(v1);
+    float denom = d00 * d11 - d01 * d01;
+    float u, v, w;
+    if (rabs(denom) < 1.0e-18f) { u = 1.0f; v = 0.0f; w = 0.0f; }
+    else {
+        v = rdiv(d11 * d20 - d01 * d21, denom);
+        w = rdiv(d00 * d21 - d01 * d20, denom);
+        u = 1.0f - v - w;
+    }
+    r.valid = true;
+    r.depth = dist;
+    r.normal = -n;
+    const Vec3 Aa(S.va[ia][0], S.va[ia][1], S.va[ia][2]), Ba(S.va[ib][0], S.va[ib][1], S.va[ib][2]),
+        Ca(S.va[ic][0], S.va[ic][1], S.va[ic][2]);
+    const Vec3 Ab(S.vb[ia][0], S.vb[ia][1], S.vb[ia][2]), Bb(S.vb[ib][0], S.vb[ib][1], S.vb[ib][2]),
+        Cb(S.vb[ic][0], S.vb[ic][1], S.vb[ic][2]);
+    r.pA = (Aa * u + Ba * v) + Ca * w;
+    r.pB = (Ab * u + Bb * v) + Cb * w;
+}
+
+// First face with the smallest distance (EPA.cpp:212-219), reduced over the warp.
+__device__ __forceinline__ uint32_t epa_best_face(const EpaWarpSmem& S, uint32_t nf, uint32_t lane) {
+    float bd = INFINITY;
+    uint32_t bf = 0xFFFFFFFFu;
+    for (uint32_t i = lane; i < nf; i += 32)
+        if (S.fd[i] < bd) { bd = S.fd[i]; bf = i; }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float od = __shfl_xor_sync(0xffffffffu, bd, o);
+        const uint32_t of = __shfl_xor_sync(0xffffffffu, bf, o);
+        if (of != 0xFFFFFFFFu && (bf == 0xFFFFFFFFu || od < bd || (od == bd && of < bf))) { bd = od; bf = of; }
+    }
+    return bf;
+}
+
+// EPA::Compute (EPA.cpp:176-296) by one warp.  Every per-face float operation runs on one lane in
+// the reference's order; selections use the reference's tie rules and ordered ballot compaction
+// keeps the visible list, horizon edges and face array in the reference's order.
+__device__ inline void epa_warp(const SupportMap& map, const GjkOut& g, float tol, uint32_t max_iter, EpaWarpSmem& S,
+                         EpaOut& r, uint32_t lane, uint32_t* err) {
+    const unsigned full = 0xffffffffu;
+    const unsigned lt = (1u << lane) - 1u;
     r.valid = false;
     r.depth = 0.0f;
     r.normal = Vec3(0.0f, 1.0f, 0.0f);
     r.pA = r.pB = Vec3();
     SP tet[4];
-    if (!epa_initial_tetra(map, g, tet)) return;
-    uint32_t nv = 0;
-    for (int i = 0; i < 4; ++i) S.verts[nv++] = tet[i];
+    if (!epa_initial_tetra(map, g, tet)) return;  // identical on every lane
+    if (lane < 4) {
+        const SP& t = tet[lane];
+        S.vp[lane][0] = t.p.x; S.vp[lane][1] = t.p.y; S.vp[lane][2] = t.p.z;
+        S.va[lane][0] = t.pA.x; S.va[lane][1] = t.pA.y; S.va[lane][2] = t.pA.z;
+        S.vb[lane][0] = t.pB.x; S.vb[lane][1] = t.pB.y; S.vb[lane][2] = t.pB.z;
+    }
+    __syncwarp();
     uint32_t nf = 0;
     const uint8_t T4[4][3] = {{0, 1, 2}, {0, 2, 3}, {0, 3, 1}, {1, 3, 2}};
     for (int i = 0; i < 4; ++i) {
-        EpaFace f{T4[i][0], T4[i][1], T4[i][2], Vec3(0.0f, 1.0f, 0.0f), 0.0f, 1u};
-        if (epa_build_face(f, S.verts)) S.faces[nf++] = f;
+        uint32_t fa = T4[i][0], fb = T4[i][1], fc = T4[i][2];
+        Vec3 n;
+        float d;
+        if (epa_build_face_sm(fa, fb, fc, n, d, S)) {
+            if (lane == 0) sm_put_face(S, nf, fa, fb, fc, n, d);
+            ++nf;
+        }
     }
+    __syncwarp();
     if (nf < 4) return;
     const float eps = tol;
+    uint32_t nv = 4;
     for (uint32_t it = 0; it < max_iter; ++it) {
-        float bd = INFINITY;
-        uint32_t bf = 0xFFFFFFFFu;
-        for (uint32_t i = 0; i < nf; ++i)
-            if (S.faces[i].alive && S.faces[i].dist < bd) { bd = S.faces[i].dist; bf = i; }
+        const uint32_t bf = epa_best_face(S, nf, lane);
         if (bf == 0xFFFFFFFFu) break;
-        EpaFace face = S.faces[bf];
-        SP w = map(face.n);
-        float d = w.p.dot(face.n);
-        if (d - face.dist < eps || nv >= 256) {
-            epa_finish(face, S.verts, r);
+        const Vec3 fn(S.fnx[bf], S.fny[bf], S.fnz[bf]);
+        const float fdist = S.fd[bf];
+        const SP w = map(fn);
+        const float d = w.p.dot(fn);
+        if (d - fdist < eps || nv >= 256) {
+            epa_finish_sm(S, bf, r);
             return;
         }
         if (nv >= kEpaVerts) {  // unreachable with max_iter <= 64
-            atomicOr(err, 4u);
-            epa_finish(face, S.verts, r);
+            if (lane == 0) atomicOr(err, 4u);
+            epa_finish_sm(S, bf, r);
             return;
         }
-        uint32_t ni = nv;
-        S.verts[nv++] = w;
+        const uint32_t ni = nv;
+        __syncwarp();
+        if (lane == 0) {
+            S.vp[ni][0] = w.p.x; S.vp[ni][1] = w.p.y; S.vp[ni][2] = w.p.z;
+            S.va[ni][0] = w.pA.x; S.va[ni][1] = w.pA.y; S.va[ni][2] = w.pA.z;
+            S.vb[ni][0] = w.pB.x; S.vb[ni][1] = w.pB.y; S.vb[ni][2] = w.pB.z;
+        }
+        ++nv;
+        // faces visible from w, in index order
         uint32_t nvis = 0;
-        for (uint32_t i = 0; i < nf; ++i)
-            if (S.faces[i].alive && S.faces[i].n.dot(w.p) - S.faces[i].dist > eps) {
-                S.faces[i].alive = 0;
-                S.vis[nvis++] = (uint16_t)i;
+        for (uint32_t base = 0; base < nf; base += 32) {
+            const uint32_t i = base + lane;
+            bool v = false;
+            if (i < nf) {
+                const Vec3 n(S.fnx[i], S.fny[i], S.fnz[i]);
+                v = n.dot(w.p) - S.fd[i] > eps;
+                S.dead[i] = v ? 1 : 0;
             }
+            const unsigned m = __ballot_sync(full, v);
+            if (v) S.vis[nvis + __popc(m & lt)] = (uint16_t)i;
+            nvis += __popc(m);
+        }
+        __syncwarp();
+        // horizon: edges of visible faces without a reverse edge in another visible face
         uint32_t nh = 0;
-        for (uint32_t vi = 0; vi < nvis; ++vi) {
-            const EpaFace& fi = S.faces[S.vis[vi]];
-            uint32_t ev[3][2] = {{fi.a, fi.b}, {fi.b, fi.c}, {fi.c, fi.a}};
-            for (int e = 0; e < 3; ++e) {
+        const uint32_t items = 3 * nvis;
+        for (uint32_t base = 0; base < items; base += 32) {
+            const uint32_t item = base + lane;
+            bool keep = false;
+            uint32_t eu = 0, ev = 0;
+            if (item < items) {
+                const uint32_t vi = item / 3, e = item % 3, fi = S.vis[vi];
+                const uint32_t A = S.fa[fi], B = S.fb[fi], C = S.fc[fi];
+                eu = e == 0 ? A : (e == 1 ? B : C);
+                ev = e == 0 ? B : (e == 1 ? C : A);
                 bool shared = false;
                 for (uint32_t vj = 0; vj < nvis && !shared; ++vj) {
                     if (vj == vi) continue;
-                    const EpaFace& fj = S.faces[S.vis[vj]];
-                    if ((fj.a == ev[e][1] && fj.b == ev[e][0]) || (fj.b == ev[e][1] && fj.c == ev[e][0]) ||
-                        (fj.c == ev[e][1] && fj.a == ev[e][0]))
-                        shared = true;
+                    const uint32_t fj = S.vis[vj];
+                    const uint32_t a2 = S.fa[fj], b2 = S.fb[fj], c2 = S.fc[fj];
+                    shared = (a2 == ev && b2 == eu) || (b2 == ev && c2 == eu) || (c2 == ev && a2 == eu);
                 }
-                if (!shared && nh < kEpaHorizon) {
-                    S.hu[nh] = (uint8_t)ev[e][0];
-                    S.hv[nh] = (uint8_t)ev[e][1];
-                    ++nh;
-                }
+                keep = !shared;
             }
+            const unsigned m = __ballot_sync(full, keep);
+            const uint32_t pos = nh + __popc(m & lt);
+            if (keep && pos < kEpaHorizon) { S.hu[pos] = (uint8_t)eu; S.hv[pos] = (uint8_t)ev; }
+            nh = min(kEpaHorizon, nh + (uint32_t)__popc(m));
         }
+        __syncwarp();
+        // drop the visible faces, keeping order
         uint32_t wi = 0;
-        for (uint32_t i = 0; i < nf; ++i)
-            if (S.faces[i].alive) S.faces[wi++] = S.faces[i];
+        for (uint32_t base = 0; base < nf; base += 32) {
+            const uint32_t i = base + lane;
+            const bool alive = i < nf && !S.dead[i];
+            uint32_t a = 0, b = 0, c = 0;
+            float nx = 0.0f, ny = 0.0f, nz = 0.0f, dd = 0.0f;
+            if (alive) { a = S.fa[i]; b = S.fb[i]; c = S.fc[i]; nx = S.fnx[i]; ny = S.fny[i]; nz = S.fnz[i]; dd = S.fd[i]; }
+            const unsigned m = __ballot_sync(full, alive);
+            __syncwarp();
+            if (alive) sm_put_face(S, wi + __popc(m & lt), a, b, c, Vec3(nx, ny, nz), dd);
+            wi += __popc(m);
+            __syncwarp();
+        }
         nf = wi;
-        for (uint32_t i = 0; i < nh; ++i) {
-            if (nf >= kEpaFaces) break;
-            EpaFace f{S.hv[i], S.hu[i], ni, Vec3(0.0f, 1.0f, 0.0f), 0.0f, 1u};
-            if (epa_build_face(f, S.verts)) S.faces[nf++] = f;
+        // new faces (horizon.v, horizon.u, new vertex) in horizon order, up to the face capacity
+        for (uint32_t base = 0; base < nh; base += 32) {
+            const uint32_t k = base + lane;
+            bool okf = false;
+            uint32_t fa = 0, fb = 0, fc = ni;
+            Vec3 n;
+            float dd = 0.0f;
+            if (k < nh) {
+                fa = S.hv[k];
+                fb = S.hu[k];
+                okf = epa_build_face_sm(fa, fb, fc, n, dd, S);
+            }
+            const unsigned m = __ballot_sync(full, okf);
+            const uint32_t pos = nf + __popc(m & lt);
+            if (okf && pos < kEpaFaces) sm_put_face(S, pos, fa, fb, fc, n, dd);
+            nf = min(kEpaFaces, nf + (uint32_t)__popc(m));
+            __syncwarp();
         }
     }
-    float bd = INFINITY;
-    uint32_t bf = 0xFFFFFFFFu;
-    for (uint32_t i = 0; i < nf; ++i)
-        if (S.faces[i].alive && S.faces[i].dist < bd) { bd = S.faces[i].dist; bf = i; }
-    if (bf != 0xFFFFFFFFu) epa_finish(S.faces[bf], S.verts, r);
+    const uint32_t bf = epa_best_face(S, nf, lane);
+    if (bf != 0xFFFFFFFFu) epa_finish_sm(S, bf, r);
 }
+
+// How the pair routines obtain EPA results: the thread-per-pair pass defers pairs that need EPA
+// to a worklist; the warp-per-pair pass runs them cooperatively.
+struct EpaDefer {
+    bool deferred = false;
+    __device__ void operator()(const SupportMap&, const GjkOut&, float, uint32_t, EpaOut& e) {
+        deferred = true;
+        e.valid = false;
+    }
+};
+struct EpaCoop {
+    EpaWarpSmem* S;
+    uint32_t lane;
+    uint32_t* err;
+    bool deferred = false;
+    __device__ void operator()(const SupportMap& m, const GjkOut& g, float tol, uint32_t it, EpaOut& e) {
+        epa_warp(m, g, tol, it, *S, e, lane, err);
+    }
+};
 
 // ---------------------------------------------------------------------------------------------
 // Face clipping (CollideShape.cpp:30-228)
@@ -639,8 +788,9 @@ __device__ __forceinline__ void swap_manifold(Manifold& m) {
     }
 }
 
+template <typename Epa>
 __device__ inline uint32_t collide_generic(const ShapeTables& T, const Body& A, const Body& B, float max_sep, float tol,
-                                           Manifold& m, EpaScratch& S, uint32_t* err) {
+                                           Manifold& m, Epa& epa) {
     SupportMap map{&T, A, B};
     GjkOut g;
     gjk(map, tol, 32, g);
@@ -655,14 +805,16 @@ __device__ inline uint32_t collide_generic(const ShapeTables& T, const Body& A, 
     }
     EpaOut e;
     if (poly) {
-        epa(map, g, tol, 64, S, e, err);
+        epa(map, g, tol, 64, e);
+        if (epa.deferred) return 0;
         if (e.valid) {
             if (collide_polyhedral(T, A, B, max_sep, m, e.normal) > 0) return m.n;
             add_point(m, e.pA, e.pB, e.normal, -e.depth);
             return m.n;
         }
     }
-    epa(map, g, tol, 64, S, e, err);
+    epa(map, g, tol, 64, e);
+    if (epa.deferred) return 0;
     if (e.valid) {
         add_point(m, e.pA, e.pB, e.normal, -e.depth);
         return m.n;
@@ -671,8 +823,9 @@ __device__ inline uint32_t collide_generic(const ShapeTables& T, const Body& A, 
     return m.n;
 }
 
+template <typename Epa>
 __device__ inline uint32_t collide_sphere_convex(const ShapeTables& T, const Body& S_, const Body& B, float max_sep,
-                                                 float tol, Manifold& m, EpaScratch& S, uint32_t* err) {
+                                                 float tol, Manifold& m, Epa& epa) {
     ShapeDev point{};
     point.type = kSphere;
     point.p[0] = 1.0e-4f;
@@ -684,7 +837,8 @@ __device__ inline uint32_t collide_sphere_convex(const ShapeTables& T, const Bod
     const Vec3 center = S_.t;
     if (g.intersect) {
         EpaOut e;
-        epa(map, g, tol, 64, S, e, err);
+        epa(map, g, tol, 64, e);
+        if (epa.deferred) return 0;
         if (e.valid) {
             Vec3 n = -e.normal;
             add_point(m, center + n * radius, e.pB, n, -(e.depth + radius));
@@ -752,9 +906,11 @@ __device__ inline uint32_t collide_plane_convex(const ShapeTables& T, const Body
     return m.n;
 }
 
-// NarrowPhase::Collide dispatch (CollideShape.cpp:480-592) for the device shape set.
+// NarrowPhase::Collide dispatch (CollideShape.cpp:480-592) for the device shape set.  With
+// EpaDefer the result is incomplete when epa.deferred is set afterwards.
+template <typename Epa>
 __device__ inline uint32_t collide(const ShapeTables& T, const Body& A, const Body& B, float max_sep, float tol,
-                                   Manifold& m, EpaScratch& S, uint32_t* err) {
+                                   Manifold& m, Epa& epa) {
     m.n = 0;
     const uint32_t ta = A.s->type, tb = B.s->type;
     if (ta == kPlane) {
@@ -764,13 +920,13 @@ __device__ inline uint32_t collide(const ShapeTables& T, const Body& A, const Bo
     }
     if (tb == kPlane) return collide_plane_convex(T, B, A, max_sep, m);
     if (ta == kSphere && tb == kSphere) return collide_sphere_sphere(A, B, max_sep, m);
-    if (ta == kSphere) return collide_sphere_convex(T, A, B, max_sep, tol, m, S, err);
+    if (ta == kSphere) return collide_sphere_convex(T, A, B, max_sep, tol, m, epa);
     if (tb == kSphere) {
-        uint32_t n = collide_sphere_convex(T, B, A, max_sep, tol, m, S, err);
+        uint32_t n = collide_sphere_convex(T, B, A, max_sep, tol, m, epa);
         if (n > 0) swap_manifold(m);
         return n;
     }
-    return collide_generic(T, A, B, max_sep, tol, m, S, err);
+    return collide_generic(T, A, B, max_sep, tol, m, epa);
 }
 
 }  // namespace kzg

@@ -1,0 +1,382 @@
+// kzg_schedule.cuh - per-island solve schedule (included by kzg_solver.cuh).
+//
+// For every island this builds, bit-compatible with the reference:
+//   * the greedy first-fit batches of contact points (at most 4 per batch, no body - static ones
+//     included - twice in a batch, sensors skipped; PhysicsWorld.cpp:680-717);
+//   * the dependency levels of the three sequential sweeps of SolveIsland (:666-743):
+//       warm start : every point in island constraint order
+//       velocity   : batch order
+//       bias       : points with positionBias > 0, island constraint order, constraints with a
+//                    massive body only (ContactSolver.cpp:263-267)
+//     A point's level is one more than the last level of the same sweep on either of its dynamic
+//     bodies; all points of one level touch distinct dynamic bodies and commute exactly.
+//
+// Only the first-fit itself is sequential.  It runs on one lane with union-find "next usable batch"
+// skip structures stored in 64-byte batch records, so each point costs O(its bodies' degree) instead
+// of the reference's O(batches): one structure skips full batches, and one per hub body (the
+// island's planes) also skips batches already holding that hub.  Local body indices, hub detection,
+// the level sweeps (32-item warp windows resolved with shuffles) and the level sorts run in
+// parallel.  Small islands take one warp, large ones one CTA.
+#pragma once
+
+namespace kzg {
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr uint32_t kWarpBodies = 384;      // island velocities staged per warp (warp-per-island solve)
+constexpr uint32_t kWarpsPerBlock = 4;
+constexpr uint32_t kCtaThreads = 256;
+constexpr uint32_t kCtaBodiesMax = 6400;   // island velocities staged per CTA (2 x 16 B x 6400 = 200 KB)
+constexpr uint32_t kSchedSmallCons = 128;  // islands with at most this many constraints: warp schedule
+constexpr uint32_t kSchedWarpBodies = 2 * kSchedSmallCons;
+constexpr uint32_t kSchedCtaBodies = 16384;  // per-sweep level table in shared memory (3 x 64 KB)
+
+struct SchedBufs {
+    const uint32_t *isl_start, *isl_con, *con_a, *con_b, *con_np, *con_bits;
+    const float4* bias;
+    const float* inv_mass;
+    const uint8_t* is_large;   // planes and other grid-bypassing bodies: hub candidates
+    uint32_t frame;
+    uint4* brec;               // batch records (64 B): {nx, hub0 nx, hub1 nx, count}, 8 bodies, 4 rows
+    uint32_t *body_stamp, *body_loc;
+    uint32_t *isl_bodies;      // per island dynamic bodies, region 2*s0
+    uint32_t *last_g;          // level tables when they do not fit shared memory: 3 x (2P)
+    uint32_t last_stride;
+    uint32_t *con_la, *con_lb; // per constraint local index of A / B (kNone if not dynamic)
+    uint32_t *first_w, *first_b;  // per sorted constraint position: first warm / bias level
+    uint32_t *vitems, *vlev;   // per point region: velocity items in batch order and their level
+    uint32_t *lvl_count;
+    uint32_t *wl_list, *vl_list, *bl_list, *wl_off, *vl_off, *bl_off, *meta;
+    uint32_t *small_list, *large_list;
+};
+
+struct SchedShared {  // per island scratch living in shared memory
+    uint32_t nloc, hub0, hub1, nbt, nv, nw, nb, total;
+};
+
+__device__ __forceinline__ uint32_t* rec(const SchedBufs& S, uint32_t r) { return reinterpret_cast<uint32_t*>(S.brec + 4ull * r); }
+
+// smallest usable batch >= i along skip structure `f` (path halving; links only point forward)
+__device__ __forceinline__ uint32_t nx_find(const SchedBufs& S, uint32_t rb, uint32_t f, uint32_t i) {
+    for (;;) {
+        uint32_t p = rec(S, rb + i)[f];
+        if (p == i) return i;
+        uint32_t gp = rec(S, rb + p)[f];
+        rec(S, rb + i)[f] = gp;
+        i = gp;
+    }
+}
+
+__device__ __forceinline__ bool rec_has(const uint32_t* r, uint32_t x) {
+    const uint32_t n = 2 * r[3];
+    for (uint32_t k = 0; k < n; ++k)
+        if (r[4 + k] == x) return true;
+    return false;
+}
+
+// Exclusive scan of v over a group of `nthreads` threads (tid < nthreads); returns the prefix and
+// writes the group total to *total.  tmp: at least 33 words of shared memory.
+template <typename Sync>
+__device__ uint32_t group_scan(uint32_t v, uint32_t tid, uint32_t nthreads, uint32_t* tmp, uint32_t* total, Sync sync) {
+    const uint32_t lane = tid & 31u, warp = tid >> 5, nwarps = (nthreads + 31) >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) tmp[warp] = x;
+    sync();
+    if (tid == 0) {
+        uint32_t run = 0;
+        for (uint32_t w = 0; w < nwarps; ++w) { uint32_t t = tmp[w]; tmp[w] = run; run += t; }
+        tmp[32] = run;
+    }
+    sync();
+    const uint32_t r = tmp[warp] + x - v;
+    *total = tmp[32];
+    sync();
+    return r;
+}
+
+// One 32-item window of a sequential level sweep, resolved by one warp.  Item i has dynamic body
+// slots (la, lb) in the level table `last` (kNone if absent) and occupies `len` consecutive levels;
+// returns its first level and advances `last` exactly as a sequential pass would.
+__device__ __forceinline__ uint32_t level_window(uint32_t* last, bool valid, uint32_t la, uint32_t lb, uint32_t len,
+                                                 uint32_t lane) {
+    const unsigned full = 0xffffffffu;
+    if (!valid) { la = kNone; lb = kNone; len = 0; }
+    uint32_t base = 0;
+    if (la != kNone) base = last[la];
+    if (lb != kNone) base = max(base, last[lb]);
+    bool supA = false, supB = false;
+    for (uint32_t j = 0; j < 32; ++j) {
+        const uint32_t aj = __shfl_sync(full, la, j), bj = __shfl_sync(full, lb, j);
+        const uint32_t ej = __shfl_sync(full, base, j) + __shfl_sync(full, len, j);
+        const bool hitA = la != kNone && (la == aj || la == bj);
+        const bool hitB = lb != kNone && (lb == aj || lb == bj);
+        if (lane > j && (hitA || hitB) && ej > base) base = ej;
+        if (j > lane) { supA |= hitA; supB |= hitB; }
+    }
+    const uint32_t end = base + len;
+    __syncwarp();
+    if (la != kNone && !supA) last[la] = end;
+    if (lb != kNone && !supB) last[lb] = end;
+    __syncwarp();
+    return base + 1;
+}
+
+// Counting sort of one sweep's points by level into list/off (order inside a level is free).
+template <typename Sync, typename Emit>
+__device__ void level_sort(const SchedBufs& S, uint32_t loff, uint32_t base, uint32_t nlev, uint32_t tid,
+                           uint32_t nthreads, uint32_t* tmp, uint32_t* list, uint32_t* off, Emit emit, Sync sync) {
+    uint32_t* cnt = S.lvl_count + loff;
+    for (uint32_t l = tid; l <= nlev; l += nthreads) cnt[l] = 0;
+    sync();
+    emit([&](uint32_t lvl, uint32_t) { atomicAdd(&cnt[lvl - 1], 1u); });
+    sync();
+    // exclusive scan of cnt[0..nlev) in chunks owned by each thread
+    const uint32_t chunk = (nlev + nthreads - 1) / nthreads;
+    const uint32_t lo = min(nlev, tid * chunk), hi = min(nlev, lo + chunk);
+    uint32_t part = 0;
+    for (uint32_t l = lo; l < hi; ++l) part += cnt[l];
+    uint32_t total;
+    uint32_t run = group_scan(part, tid, nthreads, tmp, &total, sync);
+    for (uint32_t l = lo; l < hi; ++l) {
+        const uint32_t c = cnt[l];
+        off[loff + l] = run;
+        cnt[l] = run;
+        run += c;
+    }
+    if (tid == 0) off[loff + nlev] = total;
+    sync();
+    emit([&](uint32_t lvl, uint32_t row) { list[base + atomicAdd(&cnt[lvl - 1], 1u)] = row; });
+    sync();
+}
+
+template <typename Sync>
+__device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl, uint32_t tid, uint32_t nthreads,
+                                SchedShared* sh, uint32_t* tmp, uint32_t* last_sm, uint32_t last_cap, Sync sync) {
+    const uint32_t s0 = S.isl_start[isl], s1 = S.isl_start[isl + 1];
+    const uint32_t base = 4u * s0;     // point region
+    const uint32_t loff = base + isl;  // level-offset region
+    const uint32_t rb = base + isl;    // batch-record region (npts + 1 records)
+    const uint32_t boff = 2u * s0;     // body region
+    const uint32_t lane = tid & 31u, warp = tid >> 5;
+
+    // ---- A: local indices of the island's dynamic bodies, hub candidates (large bodies)
+    if (tid == 0) { sh->nloc = 0; sh->hub0 = kNone; sh->hub1 = kNone; }
+    sync();
+    for (uint32_t s = s0 + tid; s < s1; s += nthreads) {
+        const uint32_t c = S.isl_con[s], bits = S.con_bits[c];
+        const uint32_t xs[2] = {S.con_a[c], S.con_b[c]};
+        for (int q = 0; q < 2; ++q) {
+            const uint32_t x = xs[q];
+            if (bits & (2u << q)) {
+                if (atomicExch(&S.body_stamp[x], S.frame) != S.frame) {
+                    const uint32_t l = atomicAdd(&sh->nloc, 1u);
+                    S.body_loc[x] = l;
+                    S.isl_bodies[boff + l] = x;
+                }
+            } else if (S.is_large[x] && !(bits & 1u)) {
+                atomicMin(&sh->hub0, x);
+            }
+        }
+    }
+    sync();
+    for (uint32_t s = s0 + tid; s < s1; s += nthreads) {
+        const uint32_t c = S.isl_con[s], bits = S.con_bits[c];
+        S.con_la[c] = (bits & 2u) ? S.body_loc[S.con_a[c]] : kNone;
+        S.con_lb[c] = (bits & 4u) ? S.body_loc[S.con_b[c]] : kNone;
+        const uint32_t xs[2] = {S.con_a[c], S.con_b[c]};
+        for (int q = 0; q < 2; ++q)
+            if (!(bits & (2u << q)) && S.is_large[xs[q]] && !(bits & 1u) && xs[q] != sh->hub0) atomicMin(&sh->hub1, xs[q]);
+    }
+    sync();
+
+    // ---- B: first-fit batching on one lane
+    if (tid == 0) {
+        const uint32_t hub0 = sh->hub0, hub1 = sh->hub1;
+        uint32_t* r0 = rec(S, rb);
+        r0[0] = 0; r0[1] = 0; r0[2] = 0;
+        uint32_t nbt = 0;
+        for (uint32_t s = s0; s < s1; ++s) {
+            const uint32_t c = S.isl_con[s];
+            if (S.con_bits[c] & 1u) continue;  // sensors are never batched (:690)
+            const uint32_t a = S.con_a[c], b = S.con_b[c], np = S.con_np[c];
+            const int ha = a == hub0 ? 0 : (a == hub1 ? 1 : -1);
+            const int hb = b == hub0 ? 0 : (b == hub1 ? 1 : -1);
+            const uint32_t f = ha >= 0 ? 1u + ha : (hb >= 0 ? 1u + hb : 0u);
+            const uint32_t other = ha >= 0 ? b : a;
+            uint32_t from = 0;
+            for (uint32_t p = 0; p < np; ++p) {
+                uint32_t j = nx_find(S, rb, f, from);
+                if (f != 0) {
+                    while (j < nbt && rec_has(rec(S, rb + j), other)) j = nx_find(S, rb, f, j + 1);
+                } else {
+                    while (j < nbt) {
+                        const uint32_t* r = rec(S, rb + j);
+                        if (!rec_has(r, a) && !rec_has(r, b)) break;
+                        j = nx_find(S, rb, 0, j + 1);
+                    }
+                }
+                uint32_t* r = rec(S, rb + j);
+                if (j == nbt) {  // open a new batch; the record past it becomes the sentinel
+                    r[3] = 0;
+                    ++nbt;
+                    uint32_t* t = rec(S, rb + nbt);
+                    t[0] = nbt; t[1] = nbt; t[2] = nbt;
+                }
+                const uint32_t k = r[3];
+                r[4 + 2 * k] = a;
+                r[5 + 2 * k] = b;
+                r[12 + k] = 4u * c + p;
+                r[3] = k + 1;
+                if (k + 1 == 4u) { r[0] = j + 1; r[1] = j + 1; r[2] = j + 1; }
+                if (ha == 0 || hb == 0) r[1] = j + 1;
+                if (ha == 1 || hb == 1) r[2] = j + 1;
+                from = j + 1;
+            }
+        }
+        sh->nbt = nbt;
+    }
+    sync();
+
+    // ---- C: velocity items in batch order
+    const uint32_t nbt = sh->nbt;
+    {
+        const uint32_t chunk = (nbt + nthreads - 1) / nthreads;
+        const uint32_t lo = min(nbt, tid * chunk), hi = min(nbt, lo + chunk);
+        uint32_t part = 0;
+        for (uint32_t j = lo; j < hi; ++j) part += rec(S, rb + j)[3];
+        uint32_t total;
+        uint32_t pos = group_scan(part, tid, nthreads, tmp, &total, sync);
+        for (uint32_t j = lo; j < hi; ++j) {
+            const uint32_t* r = rec(S, rb + j);
+            for (uint32_t k = 0; k < r[3]; ++k) S.vitems[base + pos++] = r[12 + k];
+        }
+        if (tid == 0) sh->total = total;
+    }
+    sync();
+
+    // ---- D: the three level sweeps, one warp each (or one after another on a single warp)
+    const uint32_t nloc = sh->nloc;
+    const uint32_t nvit = sh->total;
+    const bool in_shared = nloc <= last_cap;
+    const uint32_t nwarps = (nthreads + 31) >> 5;
+    for (uint32_t sweep = 0; sweep < 3; ++sweep) {
+        const uint32_t owner = nwarps >= 3 ? sweep : 0;
+        if (warp != owner) continue;
+        uint32_t* last = in_shared ? last_sm + (nwarps >= 3 ? sweep * last_cap : 0)
+                                   : S.last_g + sweep * S.last_stride + boff;
+        for (uint32_t k = lane; k < nloc; k += 32) last[k] = 0;
+        __syncwarp();
+        uint32_t top = 0;
+        if (sweep == 0) {  // velocity: batch order, one level per point
+            for (uint32_t w0 = 0; w0 < nvit; w0 += 32) {
+                const uint32_t i = w0 + lane;
+                const bool v = i < nvit;
+                const uint32_t row = v ? S.vitems[base + i] : 0u, c = row >> 2;
+                const uint32_t lvl = level_window(last, v, v ? S.con_la[c] : kNone, v ? S.con_lb[c] : kNone, 1u, lane);
+                if (v) { S.vlev[base + i] = lvl; top = max(top, lvl); }
+            }
+        } else {  // warm (all points) / bias (positionBias > 0): constraint order, consecutive levels
+            for (uint32_t w0 = s0; w0 < s1; w0 += 32) {
+                const uint32_t s = w0 + lane;
+                bool v = s < s1;
+                uint32_t c = v ? S.isl_con[s] : 0u, len = 0;
+                if (v) {
+                    const uint32_t np = S.con_np[c];
+                    if (sweep == 1) {
+                        len = np;
+                    } else if (!(S.inv_mass[S.con_a[c]] <= 0.0f && S.inv_mass[S.con_b[c]] <= 0.0f)) {
+                        for (uint32_t p = 0; p < np; ++p) len += S.bias[4u * c + p].y > 0.0f ? 1u : 0u;
+                    }
+                    v = len > 0;
+                }
+                const uint32_t lvl = level_window(last, v, v ? S.con_la[c] : kNone, v ? S.con_lb[c] : kNone, len, lane);
+                if (s < s1) (sweep == 1 ? S.first_w : S.first_b)[s] = v ? lvl : 0u;
+                if (v) top = max(top, lvl + len - 1);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) top = max(top, __shfl_xor_sync(0xffffffffu, top, o));
+        if (lane == 0) (sweep == 0 ? sh->nv : (sweep == 1 ? sh->nw : sh->nb)) = top;
+        __syncwarp();
+    }
+    sync();
+
+    // ---- E: sort each sweep's points by level
+    const uint32_t nv = sh->nv, nw = sh->nw, nb = sh->nb;
+    level_sort(S, loff, base, nv, tid, nthreads, tmp, S.vl_list, S.vl_off,
+               [&](auto put) {
+                   for (uint32_t i = tid; i < nvit; i += nthreads) put(S.vlev[base + i], S.vitems[base + i]);
+               },
+               sync);
+    level_sort(S, loff, base, nw, tid, nthreads, tmp, S.wl_list, S.wl_off,
+               [&](auto put) {
+                   for (uint32_t s = s0 + tid; s < s1; s += nthreads) {
+                       const uint32_t c = S.isl_con[s], f = S.first_w[s];
+                       for (uint32_t p = 0; p < S.con_np[c]; ++p) put(f + p, 4u * c + p);
+                   }
+               },
+               sync);
+    level_sort(S, loff, base, nb, tid, nthreads, tmp, S.bl_list, S.bl_off,
+               [&](auto put) {
+                   for (uint32_t s = s0 + tid; s < s1; s += nthreads) {
+                       const uint32_t f = S.first_b[s];
+                       if (f == 0) continue;
+                       const uint32_t c = S.isl_con[s];
+                       uint32_t k = 0;
+                       for (uint32_t p = 0; p < S.con_np[c]; ++p)
+                           if (S.bias[4u * c + p].y > 0.0f) put(f + k++, 4u * c + p);
+                   }
+               },
+               sync);
+
+    if (tid == 0) {
+        S.meta[4 * isl + 0] = nw;
+        S.meta[4 * isl + 1] = nv;
+        S.meta[4 * isl + 2] = nb;
+        S.meta[4 * isl + 3] = nloc;
+        if (nloc <= kWarpBodies) S.small_list[atomicAdd(&cnt->nsmall, 1u)] = isl;
+        else S.large_list[atomicAdd(&cnt->nlarge, 1u)] = isl;
+        atomicAdd(&cnt->batches, nbt);
+        atomicMax(&cnt->max_vlev, nv);
+        atomicMax(&cnt->max_blev, nb);
+    }
+    sync();
+}
+
+struct SchedWarpSync {
+    __device__ __forceinline__ void operator()() const { __syncwarp(); }
+};
+struct SchedCtaSync {
+    __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+
+// Islands with at most kSchedSmallCons constraints: one warp each.
+__global__ void __launch_bounds__(128) k_schedule_warp(SchedBufs S, Counters* cnt) {
+    __shared__ SchedShared sh[4];
+    __shared__ uint32_t tmp[4][33];
+    __shared__ uint32_t last[4][kSchedWarpBodies];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t n = cnt->nislands;
+    for (uint32_t isl = blockIdx.x * 4 + warp; isl < n; isl += gridDim.x * 4) {
+        if (S.isl_start[isl + 1] - S.isl_start[isl] > kSchedSmallCons) continue;
+        schedule_island(S, cnt, isl, lane, 32u, &sh[warp], tmp[warp], last[warp], kSchedWarpBodies, SchedWarpSync{});
+    }
+}
+
+// Larger islands: one CTA each.
+__global__ void __launch_bounds__(256) k_schedule_cta(SchedBufs S, Counters* cnt) {
+    extern __shared__ uint32_t last_sm[];
+    __shared__ SchedShared sh;
+    __shared__ uint32_t tmp[33];
+    const uint32_t n = cnt->nislands;
+    for (uint32_t isl = blockIdx.x; isl < n; isl += gridDim.x) {
+        if (S.isl_start[isl + 1] - S.isl_start[isl] <= kSchedSmallCons) continue;
+        schedule_island(S, cnt, isl, threadIdx.x, blockDim.x, &sh, tmp, last_sm, kSchedCtaBodies, SchedCtaSync{});
+    }
+}
+
+}  // namespace kzg

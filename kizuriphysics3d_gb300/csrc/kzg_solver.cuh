@@ -11,240 +11,9 @@
 // the level-synchronous solve applies every body's updates in the reference's order, bit for bit.
 #pragma once
 
+#include "kzg_schedule.cuh"
+
 namespace kzg {
-
-constexpr uint32_t kNone = 0xFFFFFFFFu;
-constexpr uint32_t kHubMin = 24;        // points on one body in one island that make it a hub
-constexpr uint32_t kWarpBodies = 384;   // island velocities staged per warp (warp-per-island solve)
-constexpr uint32_t kWarpsPerBlock = 4;
-constexpr uint32_t kCtaThreads = 256;
-constexpr uint32_t kCtaBodiesMax = 6400;  // island velocities staged per CTA (2 x 16 B x 6400 = 200 KB)
-
-struct SchedBufs {
-    const uint32_t *isl_start, *isl_con, *con_a, *con_b, *con_np, *con_bits;
-    const float4* bias;
-    const float* inv_mass;
-    uint32_t frame;
-    uint32_t *bcnt, *bbody, *bmem;      // batch count, 8 bodies, 4 point rows per batch
-    uint32_t *onx, *hnx0, *hnx1;        // skip structures (next usable batch), region base + 2*isl
-    uint32_t *body_stamp, *body_loc, *body_cnt;
-    uint32_t *isl_bodies, *last_local;  // per island dynamic bodies / level scratch, region 2*s0
-    uint32_t *con_la, *con_lb;          // per constraint: local index of A / B (kNone if not dynamic)
-    uint32_t *lvl_tmp, *ids_tmp, *lvl_count;
-    uint32_t *wl_list, *vl_list, *bl_list, *wl_off, *vl_off, *bl_off, *meta;
-    uint32_t *small_list, *large_list;
-};
-
-// smallest usable batch index >= i (path halving; every link points forward)
-__device__ __forceinline__ uint32_t nx_find(uint32_t* nx, uint32_t i) {
-    for (;;) {
-        uint32_t p = nx[i];
-        if (p == i) return i;
-        uint32_t gp = nx[p];
-        nx[i] = gp;
-        i = gp;
-    }
-}
-
-__device__ __forceinline__ bool batch_has(const uint32_t* bbody, uint32_t cntb, uint32_t x) {
-    for (uint32_t k = 0; k < 2 * cntb; ++k)
-        if (bbody[k] == x) return true;
-    return false;
-}
-
-__device__ void sched_sort(uint32_t base, uint32_t loff, uint32_t npts, uint32_t nlev, const uint32_t* pts_level,
-                           const uint32_t* pts_id, uint32_t* count, uint32_t* list, uint32_t* off) {
-    // counting sort of npts points by level (levels 1..nlev) into list[base..], offsets off[loff..]
-    for (uint32_t l = 0; l <= nlev; ++l) count[loff + l] = 0;
-    for (uint32_t k = 0; k < npts; ++k) count[loff + pts_level[base + k] - 1]++;
-    uint32_t run = 0;
-    for (uint32_t l = 0; l < nlev; ++l) {
-        uint32_t c = count[loff + l];
-        off[loff + l] = run;
-        count[loff + l] = run;
-        run += c;
-    }
-    off[loff + nlev] = run;
-    for (uint32_t k = 0; k < npts; ++k) list[base + count[loff + pts_level[base + k] - 1]++] = pts_id[base + k];
-}
-
-__global__ void k_schedule(SchedBufs S, Counters* cnt) {
-    uint32_t isl = blockIdx.x * blockDim.x + threadIdx.x;
-    if (isl >= cnt->nislands) return;
-    const uint32_t s0 = S.isl_start[isl], s1 = S.isl_start[isl + 1];
-    const uint32_t base = 4u * s0;      // point region of this island
-    const uint32_t loff = base + isl;   // level-offset region (one extra entry per island)
-    const uint32_t xoff = base + 2u * isl;  // skip-structure region (two extra entries)
-    const uint32_t boff = 2u * s0;      // body region
-    uint32_t* lvl = S.lvl_tmp;
-    uint32_t* ids = S.ids_tmp;
-
-    // ---- local indices of the island's dynamic bodies; points per body (hub detection)
-    uint32_t nloc = 0;
-    for (uint32_t s = s0; s < s1; ++s) {
-        const uint32_t c = S.isl_con[s];
-        const uint32_t bits = S.con_bits[c], a = S.con_a[c], b = S.con_b[c], np = S.con_np[c];
-        uint32_t la = kNone, lb = kNone;
-        if (bits & 2u) {
-            if (S.body_stamp[a] != S.frame) {
-                S.body_stamp[a] = S.frame;
-                S.body_loc[a] = nloc;
-                S.isl_bodies[boff + nloc++] = a;
-            }
-            la = S.body_loc[a];
-        }
-        if (bits & 4u) {
-            if (S.body_stamp[b] != S.frame) {
-                S.body_stamp[b] = S.frame;
-                S.body_loc[b] = nloc;
-                S.isl_bodies[boff + nloc++] = b;
-            }
-            lb = S.body_loc[b];
-        }
-        S.con_la[c] = la;
-        S.con_lb[c] = lb;
-        if (!(bits & 1u)) {
-            S.body_cnt[a] += np;
-            S.body_cnt[b] += np;
-        }
-    }
-    uint32_t hub0 = kNone, hub1 = kNone, c0 = kHubMin - 1, c1 = kHubMin - 1;
-    for (uint32_t s = s0; s < s1; ++s) {
-        const uint32_t c = S.isl_con[s];
-        const uint32_t xs[2] = {S.con_a[c], S.con_b[c]};
-        for (int q = 0; q < 2; ++q) {
-            const uint32_t x = xs[q];
-            const uint32_t k = S.body_cnt[x];
-            if (x == hub0 || x == hub1 || k <= c1) continue;
-            if (k > c0) { hub1 = hub0; c1 = c0; hub0 = x; c0 = k; }
-            else { hub1 = x; c1 = k; }
-        }
-    }
-    for (uint32_t s = s0; s < s1; ++s) {
-        const uint32_t c = S.isl_con[s];
-        S.body_cnt[S.con_a[c]] = 0;
-        S.body_cnt[S.con_b[c]] = 0;
-    }
-
-    // ---- greedy first-fit batching (constraint order, then point index).  onx finds the first
-    // batch that is not full; hnxK the first that is not full and does not hold hub K.
-    uint32_t* onx = S.onx + xoff;
-    uint32_t* hx0 = S.hnx0 + xoff;
-    uint32_t* hx1 = S.hnx1 + xoff;
-    onx[0] = 0; hx0[0] = 0; hx1[0] = 0;
-    uint32_t nbt = 0;
-    for (uint32_t s = s0; s < s1; ++s) {
-        const uint32_t c = S.isl_con[s];
-        if (S.con_bits[c] & 1u) continue;  // sensors are never batched (:690)
-        const uint32_t a = S.con_a[c], b = S.con_b[c];
-        const int ha = a == hub0 ? 0 : (a == hub1 ? 1 : -1);
-        const int hb = b == hub0 ? 0 : (b == hub1 ? 1 : -1);
-        for (uint32_t p = 0; p < S.con_np[c]; ++p) {
-            uint32_t j;
-            if (ha >= 0 || hb >= 0) {
-                const int h = ha >= 0 ? ha : hb;
-                const uint32_t other = ha >= 0 ? b : a;
-                uint32_t* hx = h == 0 ? hx0 : hx1;
-                j = nx_find(hx, 0);
-                while (j < nbt && batch_has(&S.bbody[8u * (base + j)], S.bcnt[base + j], other)) j = nx_find(hx, j + 1);
-            } else {
-                j = nx_find(onx, 0);
-                while (j < nbt && (batch_has(&S.bbody[8u * (base + j)], S.bcnt[base + j], a) ||
-                                   batch_has(&S.bbody[8u * (base + j)], S.bcnt[base + j], b)))
-                    j = nx_find(onx, j + 1);
-            }
-            if (j == nbt) {  // new batch
-                S.bcnt[base + j] = 0;
-                ++nbt;
-                onx[nbt] = nbt; hx0[nbt] = nbt; hx1[nbt] = nbt;
-            }
-            const uint32_t k = S.bcnt[base + j];
-            S.bbody[8u * (base + j) + 2 * k] = a;
-            S.bbody[8u * (base + j) + 2 * k + 1] = b;
-            S.bmem[4u * (base + j) + k] = 4u * c + p;
-            S.bcnt[base + j] = k + 1;
-            if (k + 1 == 4u) { onx[j] = j + 1; hx0[j] = j + 1; hx1[j] = j + 1; }
-            if (ha == 0 || hb == 0) hx0[j] = j + 1;
-            if (ha == 1 || hb == 1) hx1[j] = j + 1;
-        }
-    }
-
-    uint32_t* last = S.last_local + boff;
-    // ---- velocity levels in batch order
-    for (uint32_t k = 0; k < nloc; ++k) last[k] = 0;
-    uint32_t nv = 0, nvpts = 0;
-    for (uint32_t bi = 0; bi < nbt; ++bi) {
-        const uint32_t cntb = S.bcnt[base + bi];
-        for (uint32_t k = 0; k < cntb; ++k) {
-            const uint32_t pt = S.bmem[4u * (base + bi) + k];
-            const uint32_t c = pt >> 2, la = S.con_la[c], lb = S.con_lb[c];
-            uint32_t l = 0;
-            if (la != kNone) l = max(l, last[la]);
-            if (lb != kNone) l = max(l, last[lb]);
-            ++l;
-            if (la != kNone) last[la] = l;
-            if (lb != kNone) last[lb] = l;
-            nv = max(nv, l);
-            lvl[base + nvpts] = l;
-            ids[base + nvpts] = pt;
-            ++nvpts;
-        }
-    }
-    sched_sort(base, loff, nvpts, nv, lvl, ids, S.lvl_count, S.vl_list, S.vl_off);
-
-    // ---- warm-start levels: every point, constraint order
-    for (uint32_t k = 0; k < nloc; ++k) last[k] = 0;
-    uint32_t nw = 0, nwpts = 0;
-    for (uint32_t s = s0; s < s1; ++s) {
-        const uint32_t c = S.isl_con[s], la = S.con_la[c], lb = S.con_lb[c];
-        for (uint32_t p = 0; p < S.con_np[c]; ++p) {
-            uint32_t l = 0;
-            if (la != kNone) l = max(l, last[la]);
-            if (lb != kNone) l = max(l, last[lb]);
-            ++l;
-            if (la != kNone) last[la] = l;
-            if (lb != kNone) last[lb] = l;
-            nw = max(nw, l);
-            lvl[base + nwpts] = l;
-            ids[base + nwpts] = 4u * c + p;
-            ++nwpts;
-        }
-    }
-    sched_sort(base, loff, nwpts, nw, lvl, ids, S.lvl_count, S.wl_list, S.wl_off);
-
-    // ---- bias levels: points with positionBias > 0 of constraints with a massive body
-    for (uint32_t k = 0; k < nloc; ++k) last[k] = 0;
-    uint32_t nbl = 0, nbpts = 0;
-    for (uint32_t s = s0; s < s1; ++s) {
-        const uint32_t c = S.isl_con[s];
-        if (S.inv_mass[S.con_a[c]] <= 0.0f && S.inv_mass[S.con_b[c]] <= 0.0f) continue;
-        const uint32_t la = S.con_la[c], lb = S.con_lb[c];
-        for (uint32_t p = 0; p < S.con_np[c]; ++p) {
-            if (S.bias[4u * c + p].y <= 0.0f) continue;
-            uint32_t l = 0;
-            if (la != kNone) l = max(l, last[la]);
-            if (lb != kNone) l = max(l, last[lb]);
-            ++l;
-            if (la != kNone) last[la] = l;
-            if (lb != kNone) last[lb] = l;
-            nbl = max(nbl, l);
-            lvl[base + nbpts] = l;
-            ids[base + nbpts] = 4u * c + p;
-            ++nbpts;
-        }
-    }
-    sched_sort(base, loff, nbpts, nbl, lvl, ids, S.lvl_count, S.bl_list, S.bl_off);
-
-    S.meta[4 * isl + 0] = nw;
-    S.meta[4 * isl + 1] = nv;
-    S.meta[4 * isl + 2] = nbl;
-    S.meta[4 * isl + 3] = nloc;
-    if (nloc <= kWarpBodies) S.small_list[atomicAdd(&cnt->nsmall, 1u)] = isl;
-    else S.large_list[atomicAdd(&cnt->nlarge, 1u)] = isl;
-    atomicAdd(&cnt->batches, nbt);
-    atomicMax(&cnt->max_vlev, nv);
-    atomicMax(&cnt->max_blev, nbl);
-}
 
 // ---------------------------------------------------------------------------------------------
 // solve

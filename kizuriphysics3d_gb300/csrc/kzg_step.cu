@@ -157,9 +157,22 @@ __global__ void k_pairs_from_packed(const uint32_t* __restrict__ packed_pairs, u
 // ---------------------------------------------------------------------------------------------
 // narrow phase (PhysicsWorld::Collide, :366-393)
 // ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void store_manifold(const Manifold& m, uint32_t i, unsigned long long key, uint32_t* m_count,
+                                               float4* m_data, unsigned long long* m_key) {
+    m_key[i] = key;
+    m_count[i] = m.n;
+    float4* o = m_data + 12ull * i;
+    for (uint32_t k = 0; k < m.n; ++k) {
+        o[3 * k + 0] = F4(m.pts[k].pA, m.pts[k].sep);
+        o[3 * k + 1] = F4(m.pts[k].pB, __uint_as_float(m.pts[k].feature));
+        o[3 * k + 2] = F4(m.pts[k].n, 0.0f);
+    }
+}
+
+// One thread per pair.  Pairs whose routine needs EPA are deferred to the warp pass below.
 __global__ void __launch_bounds__(128) k_narrow(ShapeTables T, DeviceBodies b, const uint2* __restrict__ pairs,
-                                                const Counters* cnt, uint32_t* m_count, float4* m_data,
-                                                unsigned long long* m_key, uint32_t* err) {
+                                                Counters* cnt, uint32_t* m_count, float4* m_data,
+                                                unsigned long long* m_key, uint32_t* epa_list) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cnt->npairs) return;
     uint2 pr = pairs[i];
@@ -174,16 +187,40 @@ __global__ void __launch_bounds__(128) k_narrow(ShapeTables T, DeviceBodies b, c
     Body BA{&T.shapes[b.shape[f]], Q4(b.rot[f]), V3(b.pos[f])};
     Body BB{&T.shapes[b.shape[s]], Q4(b.rot[s]), V3(b.pos[s])};
     Manifold m;
-    EpaScratch S;
-    collide(T, BA, BB, 0.02f, 1.0e-4f, m, S, err);
+    EpaDefer ed;
+    collide(T, BA, BB, 0.02f, 1.0e-4f, m, ed);
+    if (ed.deferred) {
+        epa_list[atomicAdd(&cnt->nepa, 1u)] = i;
+        return;
+    }
     if (swapped) swap_manifold(m);
-    m_key[i] = pair_key(pa, pb);
-    m_count[i] = m.n;
-    float4* o = m_data + 12ull * i;
-    for (uint32_t k = 0; k < m.n; ++k) {
-        o[3 * k + 0] = F4(m.pts[k].pA, m.pts[k].sep);
-        o[3 * k + 1] = F4(m.pts[k].pB, __uint_as_float(m.pts[k].feature));
-        o[3 * k + 2] = F4(m.pts[k].n, 0.0f);
+    store_manifold(m, i, pair_key(pa, pb), m_count, m_data, m_key);
+}
+
+// One warp per deferred pair: the same routine with the warp-cooperative EPA.
+constexpr uint32_t kEpaWarps = 4;
+__global__ void __launch_bounds__(kEpaWarps * 32) k_narrow_epa(ShapeTables T, DeviceBodies b, const uint2* __restrict__ pairs,
+                                                               const Counters* cnt, const uint32_t* __restrict__ epa_list,
+                                                               uint32_t* m_count, float4* m_data, unsigned long long* m_key,
+                                                               uint32_t* err) {
+    extern __shared__ EpaWarpSmem epa_smem[];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t n = cnt->nepa;
+    for (uint32_t idx = blockIdx.x * kEpaWarps + warp; idx < n; idx += gridDim.x * kEpaWarps) {
+        const uint32_t i = epa_list[idx];
+        const uint2 pr = pairs[i];
+        const uint32_t A = pr.x, B = pr.y;
+        const uint32_t pa = b.packed[A], pb = b.packed[B];
+        const bool swapped = pa > pb;
+        const uint32_t f = swapped ? B : A, s = swapped ? A : B;
+        Body BA{&T.shapes[b.shape[f]], Q4(b.rot[f]), V3(b.pos[f])};
+        Body BB{&T.shapes[b.shape[s]], Q4(b.rot[s]), V3(b.pos[s])};
+        Manifold m;
+        EpaCoop ec{&epa_smem[warp], lane, err};
+        collide(T, BA, BB, 0.02f, 1.0e-4f, m, ec);
+        if (swapped) swap_manifold(m);
+        if (lane == 0) store_manifold(m, i, pair_key(pa, pb), m_count, m_data, m_key);
+        __syncwarp();
     }
 }
 
@@ -517,8 +554,14 @@ size_t cub_temp_bytes(uint32_t max_items) {
 }
 
 cudaError_t configure_kernels() {
-    return cudaFuncSetAttribute(k_solve_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(2 * kCtaBodiesMax * sizeof(float4)));
+    cudaError_t e = cudaFuncSetAttribute(k_solve_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(2 * kCtaBodiesMax * sizeof(float4)));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_narrow_epa, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(kEpaWarps * sizeof(EpaWarpSmem)));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_schedule_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(3 * kSchedCtaBodies * sizeof(uint32_t)));
 }
 
 static int bits_for(uint32_t v) {
@@ -536,8 +579,11 @@ static kzg_status step_after_pairs(Ctx& ctx, float dt) {
     KZG_CK(cudaEventRecord(ctx.ev[1], st));
     if (np > 0) {
         k_narrow<<<blocks_for(np, 128), 128, 0, st>>>(T, ctx.b, ctx.pairs, ctx.dcnt, ctx.m_count, ctx.m_data,
-                                                      ctx.m_key, &ctx.dcnt->error);
-        ++ctx.launches;
+                                                      ctx.m_key, ctx.epa_list);
+        const unsigned ge = std::min<unsigned>(blocks_for(np, kEpaWarps), 152u * 8u);
+        k_narrow_epa<<<ge, kEpaWarps * 32, kEpaWarps * sizeof(EpaWarpSmem), st>>>(
+            T, ctx.b, ctx.pairs, ctx.dcnt, ctx.epa_list, ctx.m_count, ctx.m_data, ctx.m_key, &ctx.dcnt->error);
+        ctx.launches += 2;
     }
     KZG_CK(cudaEventRecord(ctx.ev[2], st));
     if (np > 0) {
@@ -577,12 +623,13 @@ static kzg_status step_after_pairs(Ctx& ctx, float dt) {
         if (s != KZG_OK) return s;
         const uint32_t ni = ctx.hcnt->nislands;
         SchedBufs SB{ctx.isl_start, ctx.isl_con, ctx.con_a, ctx.con_b, ctx.con_np, ctx.con_bits, ctx.r.bias,
-                     ctx.b.inv_mass, ctx.frame, ctx.batch_cnt, ctx.batch_body, ctx.batch_mem, ctx.onx, ctx.hnx0,
-                     ctx.hnx1, ctx.body_stamp, ctx.body_loc, ctx.body_cnt, ctx.isl_bodies, ctx.last_local,
-                     ctx.con_la, ctx.con_lb, ctx.lvl_tmp, ctx.ids_tmp, ctx.lvl_count, ctx.wl_list, ctx.vl_list,
-                     ctx.bl_list, ctx.wl_off, ctx.vl_off, ctx.bl_off, ctx.isl_meta, ctx.isl_small, ctx.isl_large};
-        k_schedule<<<blocks_for(ni, 32), 32, 0, st>>>(SB, ctx.dcnt);
-        ctx.launches += 16;  // prepare, union-find (3), island sort (4 CUB passes), heads, scan (2), starts, schedule
+                     ctx.b.inv_mass, ctx.is_large, ctx.frame, ctx.brec, ctx.body_stamp, ctx.body_loc, ctx.isl_bodies,
+                     ctx.last_g, 2u * ctx.cfg.max_pairs, ctx.con_la, ctx.con_lb, ctx.first_w, ctx.first_b,
+                     ctx.ids_tmp, ctx.lvl_tmp, ctx.lvl_count, ctx.wl_list, ctx.vl_list, ctx.bl_list, ctx.wl_off,
+                     ctx.vl_off, ctx.bl_off, ctx.isl_meta, ctx.isl_small, ctx.isl_large};
+        k_schedule_warp<<<std::min<unsigned>(blocks_for(ni, 4), 152u * 16u), 128, 0, st>>>(SB, ctx.dcnt);
+        k_schedule_cta<<<std::min<unsigned>(ni, 152u * 2u), 256, 3 * kSchedCtaBodies * sizeof(uint32_t), st>>>(SB, ctx.dcnt);
+        ctx.launches += 17;  // prepare, union-find (3), island sort (4 CUB passes), heads, scan (2), starts, schedule (2)
         KZG_CK(cudaEventRecord(ctx.ev[4], st));
         SolveBufs SV{ctx.isl_start, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.con_la, ctx.con_lb, ctx.isl_meta,
                      ctx.isl_bodies, ctx.wl_list, ctx.vl_list, ctx.bl_list, ctx.wl_off, ctx.vl_off, ctx.bl_off,

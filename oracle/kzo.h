@@ -54,8 +54,8 @@ uint32_t kzo_num_constraints(const kzo_world* w);
  * nImp t1Imp t2Imp restitutionBias positionBias biasImpulse normalVelocity */
 void kzo_get_constraints(const kzo_world* w, uint32_t* hdr, float* pts, float* fric_rest);
 /* pairs, constraints, points, islands, batches, max velocity levels, max bias levels,
- * largest island points, sum of velocity levels over islands */
-void kzo_get_stats(const kzo_world* w, uint32_t* out9);
+ * largest island points, sum of velocity levels over islands, most batches open at once */
+void kzo_get_stats(const kzo_world* w, uint32_t* out10);
 void kzo_get_mass(const kzo_world* w, float* inv_mass, float* inv_inertia_world /*9 per body*/);
 
 /* Narrow phase between two bodies at their current poses (A = first argument). Returns the

@@ -104,7 +104,7 @@ struct kzo_world {
     uint32_t* isl_con;
     int* island_index;
     /* stats */
-    uint32_t st_points, st_batches, st_max_vl, st_max_bl, st_max_isl_pts, st_sum_vl;
+    uint32_t st_points, st_batches, st_max_vl, st_max_bl, st_max_isl_pts, st_sum_vl, st_max_open;
 };
 
 /* ----------------------------------------------------------------------------- */
@@ -641,7 +641,7 @@ static void solve_island(kzo_world* w, uint32_t isl, uint32_t* out_batches, uint
     uint32_t npts = 0;
     for (uint32_t i = 0; i < nc; ++i) npts += w->cons[list[i]].npts;
     batch_t* bt = (batch_t*)xrealloc(NULL, sizeof(batch_t) * (npts ? npts : 1));
-    uint32_t nbt = 0;
+    uint32_t nbt = 0, nopen = 0, max_open = 0;
     for (uint32_t i = 0; i < nc; ++i) {
         con_t* c = &w->cons[list[i]];
         if (c->sensor) continue;
@@ -659,6 +659,7 @@ static void solve_island(kzo_world* w, uint32_t isl, uint32_t* out_batches, uint
                 b->a[b->count] = c->a;
                 b->b[b->count] = c->b;
                 ++b->count;
+                if (b->count == 4) --nopen;
                 placed = 1;
             }
             if (!placed) {
@@ -668,9 +669,12 @@ static void solve_island(kzo_world* w, uint32_t isl, uint32_t* out_batches, uint
                 b->ref[0].pt = p;
                 b->a[0] = c->a;
                 b->b[0] = c->b;
+                ++nopen;
             }
+            if (nopen > max_open) max_open = nopen;
         }
     }
+    if (w->sched_stats && max_open > w->st_max_open) w->st_max_open = max_open;  /* racy max: statistics only */
     for (uint32_t it = 0; it < w->vel_iters; ++it)
         for (uint32_t bi = 0; bi < nbt; ++bi)
             for (uint32_t k = 0; k < bt[bi].count; ++k) {
@@ -914,7 +918,7 @@ int kzo_step(kzo_world* w, float dt) {
     /* 5. solve */
     for (uint32_t ci = 0; ci < w->ncons; ++ci) prepare(w, &w->cons[ci], dt);
     build_islands(w);
-    w->st_batches = w->st_max_vl = w->st_max_bl = w->st_max_isl_pts = w->st_sum_vl = 0;
+    w->st_batches = w->st_max_vl = w->st_max_bl = w->st_max_isl_pts = w->st_sum_vl = w->st_max_open = 0;
     int ni = (int)w->nislands;
     uint32_t* ib = (uint32_t*)calloc((size_t)(ni ? ni : 1) * 4, sizeof(uint32_t));
 #ifdef _OPENMP
@@ -1176,6 +1180,7 @@ void kzo_get_constraints(const kzo_world* w, uint32_t* hdr, float* pts, float* f
 void kzo_get_stats(const kzo_world* w, uint32_t* o) {
     o[0] = w->npairs; o[1] = w->ncons; o[2] = w->st_points; o[3] = w->nislands;
     o[4] = w->st_batches; o[5] = w->st_max_vl; o[6] = w->st_max_bl; o[7] = w->st_max_isl_pts; o[8] = w->st_sum_vl;
+    o[9] = w->st_max_open;
 }
 
 void kzo_get_mass(const kzo_world* w, float* im, float* iw) {

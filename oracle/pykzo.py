@@ -136,10 +136,10 @@ class OracleWorld:
         return hdr, pts, fr
 
     def stats(self) -> dict:
-        o = np.zeros(9, np.uint32)
+        o = np.zeros(10, np.uint32)
         lib().kzo_get_stats(self._w, _ptr(o))
         keys = ["pairs", "constraints", "points", "islands", "batches", "max_vel_levels",
-                "max_bias_levels", "max_island_points", "sum_vel_levels"]
+                "max_bias_levels", "max_island_points", "sum_vel_levels", "max_open_batches"]
         return dict(zip(keys, (int(x) for x in o)))
 
     def mass(self):
