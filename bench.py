@@ -214,7 +214,7 @@ def main():
     res = resolve(sc)
     snap = load_snapshot(args.workload, preroll)
     start_scene = scene_with_state(sc, snap) if snap is not None else sc
-    max_pairs = max(8 * len(sc.bodies), 4096)
+    max_pairs = max(48 * len(sc.bodies), 4096)  # a settled pile holds ~12 broad-phase pairs per body
     w = World(start_scene, resolved=res, device=local_rank, max_pairs=max_pairs)
     t_setup = time.perf_counter()
     if snap is None and preroll:
