@@ -11,12 +11,15 @@
 //     A point's level is one more than the last level of the same sweep on either of its dynamic
 //     bodies; all points of one level touch distinct dynamic bodies and commute exactly.
 //
-// Only the first-fit itself is sequential.  It runs on one lane with union-find "next usable batch"
-// skip structures stored in 64-byte batch records, so each point costs O(its bodies' degree) instead
-// of the reference's O(batches): one structure skips full batches, and one per hub body (the
-// island's planes) also skips batches already holding that hub.  Local body indices, hub detection,
-// the level sweeps (32-item warp windows resolved with shuffles) and the level sorts run in
-// parallel.  Small islands take one warp, large ones one CTA.
+// Only the first-fit itself is sequential.  In a CTA island one warp runs it over a shared-memory
+// table of the open batches (first_fit_warp: 32 candidates per ballot against 16-bit body
+// codes).  Small islands, and islands whose open batches outgrow that table, run it on one lane
+// with union-find "next usable batch" skip structures stored in 64-byte batch records, so each
+// point costs O(its bodies' degree) instead of the reference's O(batches): one structure skips
+// full batches, and one per hub body (the island's planes) also skips batches already holding
+// that hub.  Local body indices, hub detection, the level sweeps (32-item warp windows resolved
+// with shuffles) and the level sorts run in parallel.  Small islands take one warp, large ones
+// one CTA.
 #pragma once
 
 namespace kzg {
@@ -50,7 +53,7 @@ struct SchedBufs {
 };
 
 struct SchedShared {  // per island scratch living in shared memory
-    uint32_t nloc, hub0, hub1, nbt, nv, nw, nb, total;
+    uint32_t nloc, hub0, hub1, nbt, nv, nw, nb, total, ff_ok;
 };
 
 __device__ __forceinline__ uint32_t* rec(const SchedBufs& S, uint32_t r) { return reinterpret_cast<uint32_t*>(S.brec + 4ull * r); }
@@ -153,9 +156,259 @@ __device__ void level_sort(const SchedBufs& S, uint32_t loff, uint32_t base, uin
     sync();
 }
 
+// ---------------------------------------------------------------------------------------------
+// Warp first-fit over a shared-memory table of the open batches (CTA islands).
+//
+// Only batches with fewer than 4 points can take a point, so the table holds just those ("slots",
+// in batch order) with the island-local codes of their non-hub bodies (at most 6, 16 bits each),
+// plus, per hub, the list of open batches that do not hold that hub.  A point without a hub scans
+// the slots from the first open one; a point with a hub scans that hub's list.  Each step tests
+// 32 consecutive candidates with one ballot, and the first candidate without a shared body is the
+// reference's first fit; if none is left the point opens a new batch.  Full batches are dropped by
+// compacting the table when it fills.  If the open batches alone outgrow it (or the island has too
+// many bodies for 16-bit codes), the caller falls back to the one-lane skip-structure version.
+//
+// Body codes: a dynamic body's local index; any other non-hub body (a static or kinematic body
+// that is not one of the island's two hubs) gets nloc + its index in a 256-entry hash table.
+constexpr uint32_t kFfSlots = 8192;
+constexpr uint32_t kFfCodes = 256;
+constexpr uint32_t kFfBytes = kFfSlots * (12 + 4 + 2 + 2 + 2 + 1) + kFfCodes * 4;
+constexpr uint32_t kFfH0 = 8u, kFfH1 = 16u;
+constexpr uint32_t kFfDead = 0xFFFFu;
+constexpr uint32_t kFfMaxLocal = 0xFFFFu - kFfCodes - 1u;
+
+struct FfTable {
+    uint32_t* bod[3];   // per slot: 6 body codes, two per word (0xFFFF = empty)
+    uint32_t* bid;      // per slot: batch index
+    uint16_t* list[2];  // per hub: slots of the open batches without that hub, batch order
+    uint16_t* remap;    // compaction: old slot -> new slot
+    uint8_t* cnt;       // per slot: points (bits 0-2) | kFfH0 | kFfH1 | codes (bits 5-7)
+    uint32_t* keys;     // code table: body index per entry (kNone = empty)
+};
+
+__device__ __forceinline__ FfTable ff_table_of(void* smem_v) {
+    uint8_t* smem = static_cast<uint8_t*>(smem_v);
+    FfTable T;
+    for (int w = 0; w < 3; ++w) T.bod[w] = reinterpret_cast<uint32_t*>(smem + 4u * w * kFfSlots);
+    T.bid = reinterpret_cast<uint32_t*>(smem + 12u * kFfSlots);
+    T.list[0] = reinterpret_cast<uint16_t*>(smem + 16u * kFfSlots);
+    T.list[1] = reinterpret_cast<uint16_t*>(smem + 18u * kFfSlots);
+    T.remap = reinterpret_cast<uint16_t*>(smem + 20u * kFfSlots);
+    T.cnt = smem + 22u * kFfSlots;
+    T.keys = reinterpret_cast<uint32_t*>(smem + 23u * kFfSlots);
+    return T;
+}
+
+__device__ __forceinline__ uint32_t ff_hash(uint32_t x) { return (x * 0x9E3779B1u) >> 24; }
+
+// Insert a body into the code table; false when the table is full.
+__device__ __forceinline__ bool ff_insert(const FfTable& T, uint32_t x) {
+    uint32_t h = ff_hash(x);
+    for (uint32_t probe = 0; probe < kFfCodes; ++probe, h = (h + 1) & (kFfCodes - 1)) {
+        const uint32_t prev = atomicCAS(&T.keys[h], kNone, x);
+        if (prev == kNone || prev == x) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ uint32_t ff_code(const FfTable& T, uint32_t x, uint32_t loc, uint32_t nloc) {
+    if (loc != kNone) return loc;
+    uint32_t h = ff_hash(x);
+    for (uint32_t probe = 0; probe < kFfCodes; ++probe, h = (h + 1) & (kFfCodes - 1))
+        if (T.keys[h] == x) return nloc + h;
+    return kFfDead;  // not reached: every non-hub body of a batched constraint was inserted
+}
+
+__device__ __forceinline__ bool ff_holds(uint32_t w, uint32_t x) { return (w & 0xFFFFu) == x || (w >> 16) == x; }
+
+// Drop full batches from the slots and the hub lists (whole warp).
+__device__ void ff_compact(const FfTable& T, uint32_t& ns, uint32_t* nl, uint32_t lane) {
+    const unsigned full = 0xffffffffu, lt = (1u << lane) - 1u;
+    uint32_t out = 0;
+    for (uint32_t base = 0; base < ns; base += 32) {
+        const uint32_t i = base + lane;
+        bool live = false;
+        uint32_t bid = 0, cn = 0, w0 = 0, w1 = 0, w2 = 0;
+        if (i < ns) {
+            cn = T.cnt[i];
+            live = (cn & 7u) < 4u;
+            bid = T.bid[i];
+            w0 = T.bod[0][i];
+            w1 = T.bod[1][i];
+            w2 = T.bod[2][i];
+        }
+        const unsigned m = __ballot_sync(full, live);
+        const uint32_t idx = out + __popc(m & lt);
+        __syncwarp();
+        if (i < ns) T.remap[i] = live ? (uint16_t)idx : (uint16_t)kFfDead;
+        if (live) {
+            T.cnt[idx] = (uint8_t)cn;
+            T.bid[idx] = bid;
+            T.bod[0][idx] = w0;
+            T.bod[1][idx] = w1;
+            T.bod[2][idx] = w2;
+        }
+        out += __popc(m);
+        __syncwarp();
+    }
+    ns = out;
+    for (int f = 0; f < 2; ++f) {
+        uint16_t* L = T.list[f];
+        const uint32_t flag = f ? kFfH1 : kFfH0;
+        uint32_t o = 0;
+        for (uint32_t base = 0; base < nl[f]; base += 32) {
+            const uint32_t i = base + lane;
+            uint32_t s2 = kFfDead;
+            bool live = false;
+            if (i < nl[f]) {
+                s2 = T.remap[L[i]];
+                live = s2 != kFfDead && !(T.cnt[s2] & flag);
+            }
+            const unsigned m = __ballot_sync(full, live);
+            const uint32_t idx = o + __popc(m & lt);
+            __syncwarp();
+            if (live) L[idx] = (uint16_t)s2;
+            o += __popc(m);
+            __syncwarp();
+        }
+        nl[f] = o;
+    }
+    __syncwarp();
+}
+
+// Append body codes to a slot's code words (one lane).
+__device__ __forceinline__ uint32_t ff_add_code(const FfTable& T, uint32_t slot, uint32_t nc, uint32_t code) {
+    const uint32_t w = nc >> 1, sh = 16u * (nc & 1u);
+    T.bod[w][slot] = (T.bod[w][slot] & ~(0xFFFFu << sh)) | (code << sh);
+    return nc + 1;
+}
+
+// First-fit batches of one island's points (whole warp).  Returns the number of batches, or kNone
+// when the open batches do not fit the table.
+__device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1, uint32_t rb, uint32_t hub0,
+                                   uint32_t hub1, uint32_t nloc, uint8_t* smem, uint32_t lane) {
+    const unsigned full = 0xffffffffu;
+    const FfTable T = ff_table_of(smem);
+    uint32_t ns = 0, nbt = 0, nl[2] = {0, 0};
+    uint32_t head = 0, hhead[2] = {0, 0};
+    for (uint32_t w0 = s0; w0 < s1; w0 += 32) {
+        uint32_t mc = 0, mbits = 1u, ma = 0, mb = 0, mnp = 0, mca = kFfDead, mcb = kFfDead;
+        if (w0 + lane < s1) {
+            mc = S.isl_con[w0 + lane];
+            mbits = S.con_bits[mc];
+            ma = S.con_a[mc];
+            mb = S.con_b[mc];
+            mnp = S.con_np[mc];
+            if (!(mbits & 1u)) {
+                if (ma != hub0 && ma != hub1) mca = ff_code(T, ma, S.con_la[mc], nloc);
+                if (mb != hub0 && mb != hub1) mcb = ff_code(T, mb, S.con_lb[mc], nloc);
+            }
+        }
+        const uint32_t m = min(32u, s1 - w0);
+        for (uint32_t k = 0; k < m; ++k) {
+            const uint32_t c = __shfl_sync(full, mc, k), bits = __shfl_sync(full, mbits, k);
+            if (bits & 1u) continue;  // sensors are never batched (:690)
+            const uint32_t a = __shfl_sync(full, ma, k), b = __shfl_sync(full, mb, k), np = __shfl_sync(full, mnp, k);
+            const uint32_t ca = __shfl_sync(full, mca, k), cb = __shfl_sync(full, mcb, k);
+            const int ha = a == hub0 ? 0 : (a == hub1 ? 1 : -1);
+            const int hb = b == hub0 ? 0 : (b == hub1 ? 1 : -1);
+            const int hub = ha >= 0 ? ha : hb;
+            // codes tested against a candidate: both bodies, or the non-hub body twice
+            const uint32_t x0 = hub < 0 ? ca : (ha >= 0 ? cb : ca);
+            const uint32_t x1 = hub < 0 ? cb : x0;
+            const uint32_t hflag = hub == 0 ? kFfH0 : (hub == 1 ? kFfH1 : 0u);
+            uint32_t pos = hub < 0 ? head : hhead[hub];
+            for (uint32_t p = 0; p < np; ++p) {
+                // ---- search: first open candidate holding neither body
+                const uint16_t* L = hub < 0 ? nullptr : T.list[hub];
+                const uint32_t nL = hub < 0 ? ns : nl[hub];
+                int slot = -1;
+                uint32_t lidx = 0;
+                for (;;) {
+                    const uint32_t i = pos + lane;
+                    bool live = false, ok = false;
+                    uint32_t s = 0;
+                    if (i < nL) {
+                        s = hub < 0 ? i : L[i];
+                        const uint32_t cn = T.cnt[s];
+                        live = (cn & 7u) < 4u && !(cn & hflag);
+                        if (live) {
+                            const uint32_t w0c = T.bod[0][s], w1c = T.bod[1][s], w2c = T.bod[2][s];
+                            ok = !(ff_holds(w0c, x0) || ff_holds(w1c, x0) || ff_holds(w2c, x0) ||
+                                   ff_holds(w0c, x1) || ff_holds(w1c, x1) || ff_holds(w2c, x1));
+                        }
+                    }
+                    const unsigned livem = __ballot_sync(full, live);
+                    const unsigned okm = __ballot_sync(full, ok);
+                    uint32_t& hd = hub < 0 ? head : hhead[hub];
+                    if (pos == hd) {  // skip a dead prefix for good
+                        if (livem) hd += __ffs(livem) - 1;
+                        else if (pos + 32 <= nL) hd += 32;
+                    }
+                    if (okm) {
+                        const uint32_t found = __ffs(okm) - 1;
+                        slot = (int)__shfl_sync(full, s, found);
+                        lidx = pos + found;
+                        break;
+                    }
+                    if (pos + 32 >= nL) break;
+                    pos += 32;
+                }
+                // ---- place
+                const uint32_t row = 4u * c + p;
+                if (slot >= 0) {
+                    const uint32_t j = T.bid[slot];
+                    __syncwarp();
+                    if (lane == 0) {
+                        const uint32_t cn = T.cnt[slot], kk = cn & 7u;
+                        uint32_t nc = cn >> 5;
+                        if (kk + 1 < 4u) {  // a full batch's codes are never read again
+                            nc = ff_add_code(T, slot, nc, x0);
+                            if (hub < 0) nc = ff_add_code(T, slot, nc, x1);
+                        }
+                        T.cnt[slot] = (uint8_t)((kk + 1) | (cn & (kFfH0 | kFfH1)) | hflag | (nc << 5));
+                        uint32_t* r = rec(S, rb + j);
+                        r[12 + kk] = row;
+                        r[3] = kk + 1;
+                    }
+                    pos = (hub < 0 ? (uint32_t)slot : lidx) + 1;
+                } else {
+                    if (ns == kFfSlots) {
+                        ff_compact(T, ns, nl, lane);
+                        head = 0;
+                        hhead[0] = 0;
+                        hhead[1] = 0;
+                        if (ns > kFfSlots - 1024u) return kNone;
+                    }
+                    const uint32_t sl = ns++, j = nbt++;
+                    __syncwarp();
+                    if (lane == 0) {
+                        T.bid[sl] = j;
+                        T.bod[0][sl] = hub < 0 ? (x0 | (x1 << 16)) : (x0 | 0xFFFF0000u);
+                        T.bod[1][sl] = 0xFFFFFFFFu;
+                        T.bod[2][sl] = 0xFFFFFFFFu;
+                        T.cnt[sl] = (uint8_t)(1u | hflag | ((hub < 0 ? 2u : 1u) << 5));
+                        uint32_t* r = rec(S, rb + j);
+                        r[3] = 1;
+                        r[12] = row;
+                        if (hub != 0) T.list[0][nl[0]] = (uint16_t)sl;
+                        if (hub != 1) T.list[1][nl[1]] = (uint16_t)sl;
+                    }
+                    if (hub != 0) ++nl[0];
+                    if (hub != 1) ++nl[1];
+                    pos = hub < 0 ? ns : nl[hub];
+                }
+                __syncwarp();
+            }
+        }
+    }
+    return nbt;
+}
+
 template <typename Sync>
 __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl, uint32_t tid, uint32_t nthreads,
-                                SchedShared* sh, uint32_t* tmp, uint32_t* last_sm, uint32_t last_cap, Sync sync) {
+                                SchedShared* sh, uint32_t* tmp, uint32_t* last_sm, uint32_t last_cap, bool ff_table,
+                                Sync sync) {
     const uint32_t s0 = S.isl_start[isl], s1 = S.isl_start[isl + 1];
     const uint32_t base = 4u * s0;     // point region
     const uint32_t loff = base + isl;  // level-offset region
@@ -164,7 +417,10 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
     const uint32_t lane = tid & 31u, warp = tid >> 5;
 
     // ---- A: local indices of the island's dynamic bodies, hub candidates (large bodies)
-    if (tid == 0) { sh->nloc = 0; sh->hub0 = kNone; sh->hub1 = kNone; }
+    if (tid == 0) { sh->nloc = 0; sh->hub0 = kNone; sh->hub1 = kNone; sh->ff_ok = ff_table ? 1u : 0u; }
+    const FfTable T = ff_table_of(last_sm);
+    if (ff_table)
+        for (uint32_t k = tid; k < kFfCodes; k += nthreads) T.keys[k] = kNone;
     sync();
     for (uint32_t s = s0 + tid; s < s1; s += nthreads) {
         const uint32_t c = S.isl_con[s], bits = S.con_bits[c];
@@ -192,9 +448,32 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
             if (!(bits & (2u << q)) && S.is_large[xs[q]] && !(bits & 1u) && xs[q] != sh->hub0) atomicMin(&sh->hub1, xs[q]);
     }
     sync();
+    if (ff_table) {  // codes of the non-dynamic, non-hub bodies of batched constraints
+        const uint32_t hub0 = sh->hub0, hub1 = sh->hub1;
+        bool ok = true;
+        for (uint32_t s = s0 + tid; s < s1; s += nthreads) {
+            const uint32_t c = S.isl_con[s], bits = S.con_bits[c];
+            if (bits & 1u) continue;
+            const uint32_t xs[2] = {S.con_a[c], S.con_b[c]};
+            for (int q = 0; q < 2; ++q)
+                if (!(bits & (2u << q)) && xs[q] != hub0 && xs[q] != hub1) ok = ok && ff_insert(T, xs[q]);
+        }
+        if (!ok) sh->ff_ok = 0u;
+        sync();
+    }
 
-    // ---- B: first-fit batching on one lane
-    if (tid == 0) {
+    // ---- B: first-fit batching: one warp over the shared-memory table, else one lane
+    bool batched = false;
+    if (ff_table && sh->ff_ok && sh->nloc <= kFfMaxLocal) {
+        if (warp == 0) {
+            const uint32_t r = first_fit_warp(S, s0, s1, rb, sh->hub0, sh->hub1, sh->nloc, reinterpret_cast<uint8_t*>(last_sm), lane);
+            if (lane == 0) sh->nbt = r;
+        }
+        sync();
+        batched = sh->nbt != kNone;
+        sync();
+    }
+    if (!batched && tid == 0) {
         const uint32_t hub0 = sh->hub0, hub1 = sh->hub1;
         uint32_t* r0 = rec(S, rb);
         r0[0] = 0; r0[1] = 0; r0[2] = 0;
@@ -363,11 +642,13 @@ __global__ void __launch_bounds__(128) k_schedule_warp(SchedBufs S, Counters* cn
     const uint32_t n = cnt->nislands;
     for (uint32_t isl = blockIdx.x * 4 + warp; isl < n; isl += gridDim.x * 4) {
         if (S.isl_start[isl + 1] - S.isl_start[isl] > kSchedSmallCons) continue;
-        schedule_island(S, cnt, isl, lane, 32u, &sh[warp], tmp[warp], last[warp], kSchedWarpBodies, SchedWarpSync{});
+        schedule_island(S, cnt, isl, lane, 32u, &sh[warp], tmp[warp], last[warp], kSchedWarpBodies, false,
+                        SchedWarpSync{});
     }
 }
 
 // Larger islands: one CTA each.
+static_assert(kFfBytes <= 3 * kSchedCtaBodies * sizeof(uint32_t), "first-fit table must fit the level tables' shared memory");
 __global__ void __launch_bounds__(256) k_schedule_cta(SchedBufs S, Counters* cnt) {
     extern __shared__ uint32_t last_sm[];
     __shared__ SchedShared sh;
@@ -375,7 +656,7 @@ __global__ void __launch_bounds__(256) k_schedule_cta(SchedBufs S, Counters* cnt
     const uint32_t n = cnt->nislands;
     for (uint32_t isl = blockIdx.x; isl < n; isl += gridDim.x) {
         if (S.isl_start[isl + 1] - S.isl_start[isl] <= kSchedSmallCons) continue;
-        schedule_island(S, cnt, isl, threadIdx.x, blockDim.x, &sh, tmp, last_sm, kSchedCtaBodies, SchedCtaSync{});
+        schedule_island(S, cnt, isl, threadIdx.x, blockDim.x, &sh, tmp, last_sm, kSchedCtaBodies, true, SchedCtaSync{});
     }
 }
 

@@ -228,21 +228,30 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_solve_warp(SolveBufs S,
         solve_island_shared(S, S.small_list[idx], sv, sw, lane, 32u, WarpSync{});
 }
 
-// Large islands: one CTA each; velocities in shared memory when they fit, else in place.
+// Large islands whose velocities fit shared memory: one CTA each.
 __global__ void __launch_bounds__(kCtaThreads) k_solve_cta(SolveBufs S, const Counters* cnt, uint32_t smem_bodies) {
     extern __shared__ float4 smem[];
     const uint32_t n = cnt->nlarge;
     for (uint32_t idx = blockIdx.x; idx < n; idx += gridDim.x) {
         const uint32_t isl = S.large_list[idx];
-        if (S.meta[4 * isl + 3] <= smem_bodies) {
-            solve_island_shared(S, isl, smem, smem + smem_bodies, threadIdx.x, blockDim.x, CtaSync{});
-        } else {
-            const VelView V{S.b.lv, S.b.av, S.b.lv, S.b.av, false};
-            const VelView P{S.b.plv, S.b.pav, S.b.lv, S.b.av, false};
-            solve_velocity(S, isl, V, threadIdx.x, blockDim.x, CtaSync{});
-            solve_bias(S, isl, P, threadIdx.x, blockDim.x, CtaSync{});
-            __syncthreads();
-        }
+        if (S.meta[4 * isl + 3] > smem_bodies) continue;
+        solve_island_shared(S, isl, smem, smem + smem_bodies, threadIdx.x, blockDim.x, CtaSync{});
+    }
+}
+
+// Islands too large for shared memory: one 1024-thread CTA each, velocities updated in place
+// (L2-resident).  A level of a settled pile holds ~1,000 points, one per thread.
+constexpr uint32_t kBigThreads = 1024;
+__global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, const Counters* cnt, uint32_t smem_bodies) {
+    const uint32_t n = cnt->nlarge;
+    for (uint32_t idx = blockIdx.x; idx < n; idx += gridDim.x) {
+        const uint32_t isl = S.large_list[idx];
+        if (S.meta[4 * isl + 3] <= smem_bodies) continue;
+        const VelView V{S.b.lv, S.b.av, S.b.lv, S.b.av, false};
+        const VelView P{S.b.plv, S.b.pav, S.b.lv, S.b.av, false};
+        solve_velocity(S, isl, V, threadIdx.x, blockDim.x, CtaSync{});
+        solve_bias(S, isl, P, threadIdx.x, blockDim.x, CtaSync{});
+        __syncthreads();
     }
 }
 

@@ -2,15 +2,17 @@
 // reference src/World/PhysicsWorld.cpp:245-329), kernel by kernel:
 //
 //   broad phase      k_aabb, cell sort, k_find_pairs, pair-key sort   (canonical MakePairKey order)
-//   narrow phase     k_narrow: one thread per pair                    (Collide, :350-400)
+//   narrow phase     k_narrow: one thread per pair; pairs that need EPA go to k_narrow_epa,
+//                    one warp per pair                               (Collide, :350-400)
 //   constraints      k_con_flags, scan, k_build_constraints           (BuildContactConstraints, :454-535)
 //   velocities       k_integrate_vel                                  (IntegrateVelocities, :757-783)
 //   prepare          k_prepare: one thread per contact point row      (ContactSolver::PrepareConstraint)
 //   islands          union-find k_uf_*, stable sort by island         (BuildIslands, :587-664)
-//   schedule         k_schedule: one thread per island builds the reference's greedy 4-wide
-//                    batches (:680-717) and the dependency levels of the warm-start, velocity
-//                    and bias sweeps
-//   solve            k_solve: one CTA per island sweeps level by level (SolveIsland, :666-743)
+//   schedule         k_schedule_warp / k_schedule_cta: one warp per small island, one CTA per
+//                    large one, build the reference's greedy 4-wide batches (:680-717) and the
+//                    dependency levels of the warm-start, velocity and bias sweeps
+//   solve            k_solve_warp / k_solve_cta / k_solve_big: one warp, CTA or 1024-thread CTA
+//                    per island sweeps level by level (SolveIsland, :666-743)
 //   cache store      k_cache_store                                    (:568-581)
 //   positions        k_integrate_pos: positions, pseudo velocities, world inertia, force clear
 //
@@ -640,7 +642,8 @@ static kzg_status step_after_pairs(Ctx& ctx, float dt) {
             k_solve_warp<<<gw, kWarpsPerBlock * 32, kWarpsPerBlock * 2 * kWarpBodies * sizeof(float4), st>>>(SV, ctx.dcnt);
             const unsigned gc = std::min<unsigned>(ni, 152u * 2u);
             k_solve_cta<<<gc, kCtaThreads, 2 * kCtaBodiesMax * sizeof(float4), st>>>(SV, ctx.dcnt, kCtaBodiesMax);
-            ctx.launches += 2;
+            k_solve_big<<<std::min<unsigned>(ni, 152u), kBigThreads, 0, st>>>(SV, ctx.dcnt, kCtaBodiesMax);
+            ctx.launches += 3;
         }
         KZG_CK(cudaEventRecord(ctx.ev[5], st));
         ++ctx.launches;

@@ -77,6 +77,32 @@ def test_mode_b_larger_pile(oracle_lib, kzg_lib):
         assert gw.compute_state_hash() == ow.hash()
 
 
+def test_mode_b_settled_full_pile(oracle_lib, kzg_lib):
+    """The 20,000-body random convex pile at its settled state (the bench snapshot): one giant
+    island of ~100k contact points, so the schedule's open-batch table compacts and the solve runs
+    the in-place big-island kernel.  Two steps, bit-exact against the oracle."""
+    import os
+    from kizuriphysics3d_gb300 import World, resolve, scenes
+    snap = os.path.join(os.path.dirname(__file__), "..", "kizuriphysics3d_gb300", "data", "pile20000_step600.npz")
+    sc = scenes.pile(20000, seed=1234)
+    with np.load(snap) as z:
+        state = z["state"]
+    for b, st in zip(sc.bodies, state):
+        b.pos, b.rot, b.vel, b.ang = tuple(st[0:3]), tuple(st[3:7]), tuple(st[7:10]), tuple(st[10:13])
+    res = resolve(sc)
+    ow = oracle_lib.OracleWorld(sc.to_bytes(), oracle_blob(sc, res), oracle_lib.PAIRS_CANONICAL,
+                                threads=os.cpu_count() or 1)
+    with World(sc, resolved=res, max_pairs=48 * len(sc.bodies)) as gw:
+        for s in range(2):
+            ow.step(np.float32(sc.dt))
+            gw.step_fixed()
+            assert gw.compute_state_hash() == ow.hash(), f"step {s}"
+        st = gw.get_stats()
+        assert st["device_error"] == 0
+        assert st["num_contact_points"] > 80000
+        assert np.array_equal(bits(gw.state()), bits(ow.state()))
+
+
 def test_hash_identical_run_to_run(kzg_lib):
     from kizuriphysics3d_gb300 import World, resolve, scenes
     sc = scenes.pile(800, seed=5, extent=4.0, y_range=(1.0, 12.0))
