@@ -197,6 +197,22 @@ kzg_status kzg_num_constraints(kzg_ctx* ctx, uint32_t* n);
  * (the fields of ContactPointConstraint, reference ContactSolver.h:13-43). */
 kzg_status kzg_download_constraints(kzg_ctx* ctx, uint32_t* hdr, float* fr, float* pts, uint32_t capacity);
 
+/* ComputeStateHash (PhysicsWorld.cpp:1145-1175) of body state in the caller's own device buffers,
+ * allocating nothing on the host or the device.  No counterpart in the reference: it exists for
+ * callers that must not allocate in their frame loop (lockstep games that compare state hashes
+ * every tick, hosts whose device memory budget is fixed after start-up).
+ *   state      device pointer, n x 13 floats per body in kzg_download_state's layout
+ *   packed_ids device pointer, n BodyID::Packed values (slot order)
+ *   stream     cudaStream_t to run on (NULL: the legacy default stream); the call synchronises it
+ *   error      optional; receives a static message on failure
+ * n above KZG_NOALLOC_HASH_MAX_BODIES returns KZG_ERR_CAPACITY.  The work runs in one fixed
+ * 1.75 MiB device scratch array shared by all calls on a device: the first call on a device sets it
+ * up (symbol lookup, module load) and should come before any stream capture, and calls that
+ * overlap on one device race on the scratch - serialise them. */
+#define KZG_NOALLOC_HASH_MAX_BODIES 16384
+kzg_status kzg_state_hash_noalloc(const float* state, const uint32_t* packed_ids, uint32_t n, void* stream,
+                                  uint64_t* out, const char** error);
+
 /* ---- host-side setup helpers (no device needed) ---------------------------------------------- */
 /* ConvexHullShape::Create (reference src/Geometry/Shapes.cpp:331-471): builds the hull of a point
  * cloud keeping the reference's vertex order.  Returns KZG_ERR_INVALID for degenerate clouds.
