@@ -32,6 +32,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "body-steps/s on 1 GB300 at residual 1e-4, learned vs plain warm start vs CPU"
+RESIDUAL_TOL = 1e-4   # relative impulse change of a velocity iteration, sum|dImpulse| / sum|impulse|
+RESIDUAL_CAP = 64
 SNAP_DIR = os.path.join(ROOT, "kizuriphysics3d_gb300", "data")
 
 
@@ -97,6 +99,12 @@ def solve_bytes(points: int, dyn_bodies: int) -> float:
     return float(points * (92 + 16) + dyn_bodies * 88)
 
 
+def schedule_bytes(points: int, constraints: int) -> float:
+    """Constraint ids read (16 B per constraint), batch records written and read back (32 B per point),
+    three level lists written and read (24 B per point)."""
+    return float(16 * constraints + 56 * points)
+
+
 def step_bytes(n_dyn: int, pair_bytes: float, points: int, constraints: int) -> float:
     """Whole-step compulsory traffic: 236 B per dynamic body + pair bytes + 312 B per point +
     32 B per constraint."""
@@ -117,6 +125,8 @@ class Clocks:
         self.path = os.path.join("/tmp", f"kzg_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
+        if self.gpu < 0:  # not sampled
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -158,12 +168,14 @@ class Clocks:
 # ---------------------------------------------------------------------------------------------
 # CPU legs (oracle port of the reference algorithm)
 # ---------------------------------------------------------------------------------------------
-def cpu_leg(sc, res, state, steps_max: int, budget_s: float, threads: int):
+def cpu_leg(sc, res, state, steps_max: int, budget_s: float, threads: int, residual: bool = True):
     from oracle import pykzo, trace
     s2 = scene_with_state(sc, state) if state is not None else sc
     hulls = {i: trace.Hull(h.verts, h.sizes, h.idx, 0.0) for i, h in res.hulls.items()}
     w = pykzo.OracleWorld(s2.to_bytes(), trace.resolved_blob(s2, hulls, res.inv_mass, res.inv_inertia_local),
                           pykzo.PAIRS_TREE, threads=threads)
+    if residual:
+        w.set_residual(RESIDUAL_TOL, RESIDUAL_CAP)
     done, t0 = 0, time.perf_counter()
     while done < steps_max:
         w.step(np.float32(sc.dt))
@@ -211,6 +223,7 @@ def main():
     torch.cuda.set_device(local_rank)
 
     from kizuriphysics3d_gb300 import World, resolve
+    from kizuriphysics3d_gb300.learned import MODEL_PATH, WarmStartModel
     res = resolve(sc)
     snap = load_snapshot(args.workload, preroll)
     start_scene = scene_with_state(sc, snap) if snap is not None else sc
@@ -232,35 +245,63 @@ def main():
             np.savez_compressed(args.save_snapshot, state=w.state())
     preroll_s = time.perf_counter() - t_setup
 
-    for _ in range(args.warmup):
-        w.step_fixed()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
 
-    keys = ("broadphase_ms", "narrowphase_ms", "constraints_ms", "schedule_ms", "solve_ms", "integrate_ms", "step_ms")
-    acc = {k: 0.0 for k in keys}
-    launches = 0
-    last = None
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    with Clocks(local_rank) as clocks:
-        for i in range(args.steps):
-            flush.fill_(float(i))
-            torch.cuda.synchronize()
-            w.step_fixed()
-            st = w.get_stats()
-            for k in keys:
-                acc[k] += st[k]
-            launches += st["kernel_launches"]
-            last = st
+    def fresh_world(mode: str):
+        """A world at the starting state, solving with the fixed iteration count ("fixed"), or
+        residual-terminated with the plain ("plain") or learned ("learned") warm start."""
+        wx = World(start_scene, resolved=res, device=local_rank, max_pairs=max_pairs)
+        if mode != "fixed":
+            wx.set_residual(RESIDUAL_TOL, RESIDUAL_CAP)
+        if mode == "learned":
+            WarmStartModel.load(MODEL_PATH).apply(wx)
+        return wx
+
+    def timed(wx, steps: int, sample_clocks: bool):
+        keys = ("broadphase_ms", "narrowphase_ms", "constraints_ms", "schedule_ms", "solve_ms", "integrate_ms",
+                "step_ms")
+        acc = {k: 0.0 for k in keys}
+        tot = {"launches": 0, "point_iterations": 0, "max_iterations": 0, "final_residual": 0.0}
+        last = None
         torch.cuda.synchronize()
-    clk = clocks.summary()
-    total_ms = acc["step_ms"]
-    if dist:
-        t = torch.tensor([total_ms], device=f"cuda:{local_rank}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        if dist:
+            dist.barrier()
+        with Clocks(local_rank if sample_clocks else -1) as clocks:
+            for i in range(steps):
+                flush.fill_(float(i))
+                torch.cuda.synchronize()
+                wx.step_fixed()
+                st = wx.get_stats()
+                for k in keys:
+                    acc[k] += st[k]
+                tot["launches"] += st["kernel_launches"]
+                tot["point_iterations"] += st["point_velocity_iterations"]
+                tot["max_iterations"] = max(tot["max_iterations"], st["max_velocity_iterations_used"])
+                tot["final_residual"] += st["final_residual"] / steps
+                last = st
+            torch.cuda.synchronize()
+        total_ms = acc["step_ms"]
+        if dist:
+            t = torch.tensor([total_ms], device=f"cuda:{local_rank}", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total_ms = float(t.item())
+        return acc, tot, last, total_ms, (clocks.summary() if sample_clocks else None)
+
+    def solver_summary(tot, last, steps):
+        pts = max(1, last["num_contact_points"])
+        return {"velocity_iterations_per_point": tot["point_iterations"] / steps / pts,
+                "max_island_iterations": tot["max_iterations"], "mean_final_residual": tot["final_residual"]}
+
+    # ---- plain warm start, residual-terminated: the headline
+    if snap is None and preroll:
+        start_scene = scene_with_state(sc, w.state())
+    w.close()
+    w = fresh_world("plain")
+    for _ in range(args.warmup):
+        w.step_fixed()
+    acc, tot, last, total_ms, clk = timed(w, args.steps, True)
     value = world_size * n_dyn * args.steps / (total_ms / 1e3)
+    launches = tot["launches"]
 
     # e2e through the C-ABI with host buffers
     ft = np.zeros((w.n, 6), np.float32)
@@ -275,14 +316,33 @@ def main():
         w.transforms(tr)
         e2e_s += time.perf_counter() - t0
     e2e_value = world_size * n_dyn * args.steps / e2e_s
+    pairs = w.broadphase_pairs()
+    w.close()
+
+    # ---- learned warm start (same tolerance) and the fixed iteration count
+    legs = {}
+    for mode in ("learned", "fixed"):
+        if mode == "learned" and not os.path.exists(MODEL_PATH):
+            legs[mode] = {"unavailable": "no trained model file"}
+            continue
+        wx = fresh_world(mode)
+        for _ in range(args.warmup):
+            wx.step_fixed()
+        acc_m, tot_m, last_m, ms_m, _ = timed(wx, args.steps, False)
+        wx.close()
+        legs[mode] = {"value": world_size * n_dyn * args.steps / (ms_m / 1e3), "unit": "body-steps/s",
+                      "ms_per_step": ms_m / args.steps, "solver": solver_summary(tot_m, last_m, args.steps),
+                      "stage_ms": {k: v / args.steps for k, v in acc_m.items()}}
+    legs["plain"] = {"solver": solver_summary(tot, last, args.steps)}
 
     # roofline of the dominant kernel, from the last step's counts and the timed averages
-    pairs = w.broadphase_pairs()
     points = last["num_contact_points"]
     nb = narrow_bytes(sc, pairs, points)
     cand = {
-        "k_narrow": (acc["narrowphase_ms"] / args.steps, nb),
-        "k_solve": (acc["solve_ms"] / args.steps, solve_bytes(points, n_dyn)),
+        "k_narrow + k_narrow_epa": (acc["narrowphase_ms"] / args.steps, nb),
+        "k_schedule_cta + k_schedule_warp": (acc["schedule_ms"] / args.steps,
+                                             schedule_bytes(points, last["num_contact_constraints"])),
+        "k_solve_big + k_solve_cta + k_solve_warp": (acc["solve_ms"] / args.steps, solve_bytes(points, n_dyn)),
     }
     kname = max(cand, key=lambda k: cand[k][0])
     kms, kbytes = cand[kname]
@@ -299,12 +359,12 @@ def main():
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0 and world_size == 1:
-        state0 = snap if snap is not None else None
         threads = os.cpu_count() or 1
-        n_steps, secs = cpu_leg(sc, res, state0, 10 ** 6, args.cpu_budget, threads)
+        n_steps, secs = cpu_leg(sc, res, snap, 10 ** 6, args.cpu_budget, threads, residual=True)
         cpu = {"value": n_dyn * n_steps / secs, "unit": "body-steps/s", "cores": threads, "kind": "port",
                "sample": f"{n_steps} steps of the same workload from the same starting state (cold manifold "
-                         f"cache), reference pair order, {secs:.1f} s"}
+                         f"cache), reference pair order, residual {RESIDUAL_TOL:g} / cap {RESIDUAL_CAP}, "
+                         f"{secs:.1f} s"}
 
     ms_per_step = total_ms / args.steps
     out = {
@@ -313,7 +373,8 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
         "config": dict(cfg, window=f"steps {preroll}+ of the run" if preroll else "from the initial scene",
                        start_state="committed snapshot" if snap is not None else "simulated untimed",
-                       solver="fixed iterations, the reference's 4-wide batch order (bit-exact)",
+                       solver=f"plain warm start, velocity iterations until the relative impulse change is "
+                              f"<= {RESIDUAL_TOL:g} (cap {RESIDUAL_CAP}); the reference's 4-wide batch order",
                        pair_order="canonical (GPU broad phase)", l2="flushed between timed steps (256 MB write)",
                        parallelism="replicas" if world_size > 1 else "single GPU",
                        contacts=points, pairs=int(pairs.shape[0]), islands=last["num_islands"],
@@ -326,12 +387,14 @@ def main():
         "cpu_baseline": cpu,
         "gpu_launches": launches,
         "clocks": clk,
+        "learned": legs["learned"],
+        "fixed_iterations": legs["fixed"],
+        "plain_solver": legs["plain"]["solver"],
         "stage_ms": {k: v / args.steps for k, v in acc.items()},
         "model_gbs_step": step_bytes(n_dyn, nb - 40 * points, points, last["num_contact_constraints"]) /
                           (ms_per_step / 1e3) / 1e9,
         "preroll_s": preroll_s,
     }
-    w.close()
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist:
@@ -349,13 +412,15 @@ def run_reference(args, sc, cfg, preroll, n_dyn):
     res = resolve(sc)
     threads = os.cpu_count() or 1
     budget = max(30.0, min(240.0, 8.0 * (args.steps + args.warmup)))
-    n_steps, secs = cpu_leg(sc, res, snap, args.steps, budget, threads)
+    n_steps, secs = cpu_leg(sc, res, snap, args.steps, budget, threads, residual=True)
     value = n_dyn * n_steps / secs
     out = {"metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": 0, "steps": n_steps,
            "warmup": 1, "ms_per_step": 1e3 * secs / max(n_steps, 1), "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)", "impl": "reference",
            "config": dict(cfg, window=f"steps {preroll}+ of the run" if preroll else "from the initial scene",
-                          pair_order="reference dynamic AABB tree"),
+                          pair_order="reference dynamic AABB tree",
+                          solver=f"velocity iterations until the relative impulse change is <= {RESIDUAL_TOL:g} "
+                                 f"(cap {RESIDUAL_CAP}); the reference's first-fit 4-wide batches"),
            "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port",
                             "sample": f"{n_steps} of {args.steps} requested steps within a {budget:.0f} s budget"},
            "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -75,6 +75,13 @@ typedef struct {
     float warm_start_factor;
     int use_velocity_bias;
     int schedule; /* KZG_SCHEDULE_* */
+    /* Residual-terminated velocity iterations (not in the reference, which always runs
+     * velocity_iterations): with residual_tolerance > 0 an island stops iterating once the largest
+     * velocity change |dImpulse| / effectiveMass that any of its rows applied in an iteration is
+     * <= residual_tolerance (m/s), after at most max_velocity_iterations iterations.  0 keeps the
+     * reference's fixed count. */
+    float residual_tolerance;
+    uint32_t max_velocity_iterations;
 } kzg_solver_settings;
 
 /* Mirrors the WorldSettings fields the step reads (reference PhysicsWorld.h:20-43). */
@@ -136,10 +143,13 @@ typedef struct {
     uint32_t cache_entries;
     uint32_t device_error;  /* bit mask of KZG_DEVERR_* raised by kernels */
     uint32_t kernel_launches; /* kernels launched by the last step (own kernels + CUB passes) */
+    uint32_t max_velocity_iterations_used;  /* most velocity iterations any island ran */
+    uint32_t point_velocity_iterations;     /* sum over islands of batched points x iterations */
     /* CUDA-event times of the last step on the context stream: broad phase; narrow-phase kernel;
      * constraint build + velocity integration; prepare + islands + batch schedule; solver kernel;
      * cache store + position integration; whole step. */
     float broadphase_ms, narrowphase_ms, constraints_ms, schedule_ms, solve_ms, integrate_ms, step_ms;
+    float final_residual; /* largest residual of any island's last velocity iteration (m/s) */
 } kzg_stats;
 
 #define KZG_DEVERR_PAIRS 1u     /* pair buffer overflow */
@@ -212,6 +222,33 @@ kzg_status kzg_download_constraints(kzg_ctx* ctx, uint32_t* hdr, float* fr, floa
 #define KZG_NOALLOC_HASH_MAX_BODIES 16384
 kzg_status kzg_state_hash_noalloc(const float* state, const uint32_t* packed_ids, uint32_t n, void* stream,
                                   uint64_t* out, const char** error);
+
+/* ---- learned warm start ------------------------------------------------------------------------
+ * No counterpart in the reference, which warm-starts a contact point that misses the manifold
+ * cache with zero impulses (PhysicsWorld.cpp:518-529).  With a model set and enabled, such points
+ * start from the prediction of an MLP (24 features -> 64 -> 64 -> 3, ReLU; BF16 weights and
+ * activations, FP32 accumulation on the tensor cores).  Parameters: KZG_MLP_PARAMS floats,
+ * row-major W1[64][24], b1[64], W2[64][64], b2[64], W3[3][64], b3[3]; features are standardised
+ * with the given mean / std.  An output o maps to impulse / effective mass 0.05 sinh(o) (|o|
+ * limited to 6) for the normal and the two tangent rows.  Training runs on the GPU too: log
+ * samples (features + converged impulse / effective mass) while stepping, load them as a dataset
+ * with the targets mapped through asinh(y / 0.05), take Adam steps. */
+#define KZG_MLP_FEATURES 24
+#define KZG_MLP_PARAMS 5955
+#define KZG_MLP_LOG_FLOATS 30 /* per sample: 24 features, 3 targets, 3 target masks */
+kzg_status kzg_mlp_set_params(kzg_ctx* ctx, const float* theta, const float* mean, const float* std);
+kzg_status kzg_mlp_get_params(kzg_ctx* ctx, float* theta, float* mean, float* std);
+kzg_status kzg_mlp_enable(kzg_ctx* ctx, int enabled);
+/* Log every cache-missing contact point of the following steps (features before the solve,
+ * impulse / effective mass after it) into a device buffer of `capacity` samples; 0 stops. */
+kzg_status kzg_mlp_log_begin(kzg_ctx* ctx, uint32_t capacity);
+kzg_status kzg_mlp_log_fetch(kzg_ctx* ctx, float* out, uint32_t capacity, uint32_t* count);
+kzg_status kzg_mlp_set_dataset(kzg_ctx* ctx, const float* samples, uint32_t n); /* log layout */
+/* Mean-squared error over the valid targets of samples [first, first + count): its gradient
+ * (no update), or one Adam step (beta 0.9 / 0.999). */
+kzg_status kzg_mlp_gradient(kzg_ctx* ctx, uint32_t first, uint32_t count, float* grad, float* loss);
+kzg_status kzg_mlp_train_step(kzg_ctx* ctx, uint32_t first, uint32_t count, float lr, float* loss);
+kzg_status kzg_mlp_predict(kzg_ctx* ctx, uint32_t first, uint32_t count, float* out); /* 3 per sample */
 
 /* ---- host-side setup helpers (no device needed) ---------------------------------------------- */
 /* ConvexHullShape::Create (reference src/Geometry/Shapes.cpp:331-471): builds the hull of a point

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libkzg.so")
-SOURCES = ["kzg_step.cu", "kzg_api.cu", "kzg_hull.cpp", "kzg_noalloc.cu"]
+SOURCES = ["kzg_step.cu", "kzg_api.cu", "kzg_hull.cpp", "kzg_noalloc.cu", "kzg_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
               "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", "-I", os.path.join(HERE, "..", "include")]

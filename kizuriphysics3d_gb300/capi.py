@@ -15,6 +15,9 @@ from . import build as _build
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 KZG_OK = 0
+MLP_FEATURES = 24
+MLP_PARAMS = 5955
+MLP_LOG_FLOATS = 30
 ERRORS = {-1: "KZG_ERR_INVALID", -2: "KZG_ERR_CUDA", -3: "KZG_ERR_CAPACITY", -4: "KZG_ERR_UNSUPPORTED",
           -5: "KZG_ERR_DEVICE"}
 
@@ -29,7 +32,8 @@ class KzgConfig(ctypes.Structure):
 class KzgSolverSettings(ctypes.Structure):
     _fields_ = [("velocity_iterations", u32), ("position_iterations", u32), ("baumgarte", f32),
                 ("penetration_slop", f32), ("restitution_threshold", f32), ("max_bias_velocity", f32),
-                ("warm_start_factor", f32), ("use_velocity_bias", ctypes.c_int), ("schedule", ctypes.c_int)]
+                ("warm_start_factor", f32), ("use_velocity_bias", ctypes.c_int), ("schedule", ctypes.c_int),
+                ("residual_tolerance", f32), ("max_velocity_iterations", u32)]
 
 
 class KzgWorldSettings(ctypes.Structure):
@@ -53,9 +57,10 @@ class KzgBodySoa(ctypes.Structure):
 class KzgStats(ctypes.Structure):
     _fields_ = [(n, u32) for n in ("num_bodies", "num_broadphase_pairs", "num_contact_constraints",
                                    "num_contact_points", "num_islands", "num_batches", "max_velocity_levels",
-                                   "max_bias_levels", "cache_entries", "device_error", "kernel_launches")] + \
+                                   "max_bias_levels", "cache_entries", "device_error", "kernel_launches",
+                                   "max_velocity_iterations_used", "point_velocity_iterations")] + \
                [(n, f32) for n in ("broadphase_ms", "narrowphase_ms", "constraints_ms", "schedule_ms", "solve_ms",
-                                   "integrate_ms", "step_ms")]
+                                   "integrate_ms", "step_ms", "final_residual")]
 
 
 EXPORTS = ["kzg_create", "kzg_destroy", "kzg_last_error", "kzg_set_stream", "kzg_synchronize",
@@ -113,6 +118,16 @@ def load(build_if_missing: bool = True):
     L.kzg_download_constraints.argtypes = [vp, vp, vp, vp, u32]
     L.kzg_hull_build.argtypes = [vp, u32, u32, vp, P(u32), vp, P(u32), vp, P(u32), u32]
     L.kzg_mass_properties.argtypes = [P(KzgShapeDesc), vp, vp, vp, u32, f32, f32, P(f32), vp]
+    L.kzg_state_hash_noalloc.argtypes = [vp, vp, u32, vp, P(ctypes.c_uint64), P(ctypes.c_char_p)]
+    L.kzg_mlp_set_params.argtypes = [vp, vp, vp, vp]
+    L.kzg_mlp_get_params.argtypes = [vp, vp, vp, vp]
+    L.kzg_mlp_enable.argtypes = [vp, ctypes.c_int]
+    L.kzg_mlp_log_begin.argtypes = [vp, u32]
+    L.kzg_mlp_log_fetch.argtypes = [vp, vp, u32, P(u32)]
+    L.kzg_mlp_set_dataset.argtypes = [vp, vp, u32]
+    L.kzg_mlp_gradient.argtypes = [vp, u32, u32, vp, P(f32)]
+    L.kzg_mlp_train_step.argtypes = [vp, u32, u32, f32, P(f32)]
+    L.kzg_mlp_predict.argtypes = [vp, u32, u32, vp]
     _lib = L
     return L
 

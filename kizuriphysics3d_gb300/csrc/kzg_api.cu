@@ -106,6 +106,8 @@ kzg_status alloc_all(Ctx* ctx) {
     CK(dalloc(&ctx->con_lb, P));
     CK(dalloc(&ctx->isl_small, P));
     CK(dalloc(&ctx->isl_large, P));
+    CK(dalloc(&ctx->miss_rows, R));
+    CK(dalloc(&ctx->miss_prior, R));
     CK(configure_kernels());
     CK(dalloc(&ctx->c_key, H));
     CK(cudaMemset(ctx->c_key, 0, sizeof(unsigned long long) * H));
@@ -138,7 +140,7 @@ void free_all(Ctx* ctx) {
                     ctx->wl_list, ctx->vl_list, ctx->bl_list, ctx->wl_off, ctx->vl_off, ctx->bl_off, ctx->isl_meta,
                     ctx->c_key, ctx->c_np, ctx->c_pos, ctx->c_imp, ctx->dcnt, ctx->cub_tmp, ctx->hash_words,
                     ctx->body_stamp, ctx->body_loc, ctx->isl_bodies, ctx->con_la, ctx->con_lb, ctx->isl_small,
-                    ctx->isl_large,
+                    ctx->isl_large, ctx->miss_rows, ctx->miss_prior,
                     ctx->shapes, ctx->hull_verts, ctx->face_sizes, ctx->face_idx};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -146,6 +148,7 @@ void free_all(Ctx* ctx) {
     for (cudaEvent_t e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    mlp_free(*ctx);
 }
 
 struct HostShape {
@@ -238,6 +241,8 @@ void kzg_default_settings(kzg_world_settings* ws, kzg_solver_settings* ss) {
         ss->warm_start_factor = 1.0f;
         ss->use_velocity_bias = 0;
         ss->schedule = KZG_SCHEDULE_REFERENCE;
+        ss->residual_tolerance = 0.0f;
+        ss->max_velocity_iterations = 64;
     }
 }
 
@@ -327,6 +332,10 @@ kzg_status kzg_set_solver_settings(kzg_ctx* k, const kzg_solver_settings* s) {
     if (check(k) || !s) return KZG_ERR_INVALID;
     if (s->schedule != KZG_SCHEDULE_REFERENCE) {
         k->c.err = "unknown solver schedule";
+        return KZG_ERR_INVALID;
+    }
+    if (!(s->residual_tolerance >= 0.0f) || (s->residual_tolerance > 0.0f && s->max_velocity_iterations == 0)) {
+        k->c.err = "residual_tolerance must be >= 0, with max_velocity_iterations >= 1 when it is > 0";
         return KZG_ERR_INVALID;
     }
     k->c.ss = *s;
@@ -664,6 +673,56 @@ kzg_status kzg_download_constraints(kzg_ctx* k, uint32_t* hdr, float* fr, float*
         }
     }
     return KZG_OK;
+}
+
+kzg_status kzg_mlp_set_params(kzg_ctx* k, const float* theta, const float* mean, const float* stdv) {
+    if (check(k) || !theta || !mean || !stdv) return KZG_ERR_INVALID;
+    return mlp_set_params(k->c, theta, mean, stdv);
+}
+
+kzg_status kzg_mlp_get_params(kzg_ctx* k, float* theta, float* mean, float* stdv) {
+    if (check(k) || !theta) return KZG_ERR_INVALID;
+    return mlp_get_params(k->c, theta, mean, stdv);
+}
+
+kzg_status kzg_mlp_enable(kzg_ctx* k, int enabled) {
+    if (check(k)) return KZG_ERR_INVALID;
+    if (enabled && !k->c.mlp.have) {
+        k->c.err = "kzg_mlp_enable: set the model parameters first";
+        return KZG_ERR_INVALID;
+    }
+    k->c.mlp.enabled = enabled != 0;
+    return KZG_OK;
+}
+
+kzg_status kzg_mlp_log_begin(kzg_ctx* k, uint32_t capacity) {
+    if (check(k)) return KZG_ERR_INVALID;
+    return mlp_log_begin(k->c, capacity);
+}
+
+kzg_status kzg_mlp_log_fetch(kzg_ctx* k, float* out, uint32_t capacity, uint32_t* count) {
+    if (check(k) || !count) return KZG_ERR_INVALID;
+    return mlp_log_fetch(k->c, out, capacity, count);
+}
+
+kzg_status kzg_mlp_set_dataset(kzg_ctx* k, const float* samples, uint32_t n) {
+    if (check(k) || (n && !samples)) return KZG_ERR_INVALID;
+    return mlp_set_dataset(k->c, samples, n);
+}
+
+kzg_status kzg_mlp_gradient(kzg_ctx* k, uint32_t first, uint32_t count, float* grad, float* loss) {
+    if (check(k) || !grad) return KZG_ERR_INVALID;
+    return mlp_gradient(k->c, first, count, grad, loss);
+}
+
+kzg_status kzg_mlp_train_step(kzg_ctx* k, uint32_t first, uint32_t count, float lr, float* loss) {
+    if (check(k) || !(lr > 0.0f)) return KZG_ERR_INVALID;
+    return mlp_train_step(k->c, first, count, lr, loss);
+}
+
+kzg_status kzg_mlp_predict(kzg_ctx* k, uint32_t first, uint32_t count, float* out) {
+    if (check(k) || (count && !out)) return KZG_ERR_INVALID;
+    return mlp_predict(k->c, first, count, out);
 }
 
 kzg_status kzg_hull_build(const float* pts, uint32_t n, uint32_t max_points, float* ov, uint32_t* onv, uint8_t* osz,

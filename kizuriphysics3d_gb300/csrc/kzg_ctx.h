@@ -54,7 +54,32 @@ struct Counters {  // device-side counters, copied back after each stage that si
     uint32_t nsmall;
     uint32_t nlarge;
     uint32_t nepa;
+    uint32_t max_iters;  // most velocity iterations of an island
+    uint32_t pt_iters;   // sum of batched points x iterations
+    uint32_t res_bits;   // largest final residual (float bits, >= 0)
+    uint32_t nmiss;      // contact points without a cached warm start (learned warm start / logging)
     uint32_t cache_entries;
+};
+
+// Learned warm start (kzg_mlp.cu): model, optimiser state, training log and dataset.
+struct MlpState {
+    bool have = false, enabled = false, logging = false;
+    float* theta = nullptr;  // KZG_MLP_PARAMS fp32 parameters
+    float *adam_m = nullptr, *adam_v = nullptr;
+    uint32_t adam_t = 0;
+    float* grad = nullptr;  // KZG_MLP_PARAMS + loss
+    float* norm = nullptr;  // feature mean[24], 1/std[24]
+    std::vector<float> std;
+    uint32_t* log_n = nullptr;
+    float* log = nullptr;  // KZG_MLP_LOG_FLOATS per sample
+    uint32_t log_cap = 0;
+    float* ds = nullptr;  // training samples, same layout as the log
+    uint32_t ds_n = 0;
+    std::vector<double> ds_valid_prefix;
+    float* part = nullptr;  // per-CTA partial gradients
+    uint32_t part_blocks = 0;
+    float* out = nullptr;
+    uint32_t out_cap = 0;
 };
 
 struct Ctx {
@@ -128,6 +153,9 @@ struct Ctx {
     uint32_t* isl_bodies = nullptr;                             // per island dynamic bodies
     uint32_t *con_la = nullptr, *con_lb = nullptr;             // per constraint local body indices
     uint32_t *isl_small = nullptr, *isl_large = nullptr;       // islands by solve kernel
+    uint32_t* miss_rows = nullptr;                              // rows without a cached warm start
+    float4* miss_prior = nullptr;  // per miss: nearest cached point of the pair (impulses, distance; -1: none)
+    MlpState mlp;
 
     // cache
     unsigned long long* c_key = nullptr;

@@ -18,6 +18,20 @@ kzg_status step_canonical(Ctx& ctx, float dt);
 kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t num_pairs, float dt);
 kzg_status hash_state(Ctx& ctx, uint64_t* out);
 
+// learned warm start (kzg_mlp.cu)
+cudaError_t mlp_configure_kernels();
+void mlp_free(Ctx& ctx);
+kzg_status mlp_set_params(Ctx& ctx, const float* theta, const float* mean, const float* stdv);
+kzg_status mlp_get_params(Ctx& ctx, float* theta, float* mean, float* stdv);
+kzg_status mlp_log_begin(Ctx& ctx, uint32_t capacity);
+kzg_status mlp_log_fetch(Ctx& ctx, float* out, uint32_t cap, uint32_t* n);
+kzg_status mlp_set_dataset(Ctx& ctx, const float* samples, uint32_t n);
+kzg_status mlp_gradient(Ctx& ctx, uint32_t first, uint32_t count, float* grad, float* loss);
+kzg_status mlp_train_step(Ctx& ctx, uint32_t first, uint32_t count, float lr, float* loss);
+kzg_status mlp_predict(Ctx& ctx, uint32_t first, uint32_t count, float* out);
+uint32_t mlp_after_prepare(Ctx& ctx, float dt);  // kernels launched
+uint32_t mlp_after_solve(Ctx& ctx, float dt);
+
 // host setup (kzg_hull.cpp)
 int hull_build(const float* pts, uint32_t n, uint32_t max_points, float* out_v, uint32_t* out_nv, uint8_t* out_sizes,
                uint32_t* out_nf, uint32_t* out_idx, uint32_t* out_ni, uint32_t cap_faces);

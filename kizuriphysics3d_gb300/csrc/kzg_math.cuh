@@ -178,4 +178,11 @@ KZG_HD AABB aabb_transformed(const AABB& b, const Quat& q, const Vec3& t) {
     return AABB{nc - ne, nc + ne};
 }
 
+// float4 storage <-> math types (device buffers keep vectors as float4)
+__device__ __forceinline__ Vec3 V3(float4 a) { return Vec3(a.x, a.y, a.z); }
+__device__ __forceinline__ float4 F4(const Vec3& v, float w) { return make_float4(v.x, v.y, v.z, w); }
+__device__ __forceinline__ Quat Q4(float4 a) { return Quat(a.x, a.y, a.z, a.w); }
+__device__ __forceinline__ float4 F4q(const Quat& q) { return make_float4(q.x, q.y, q.z, q.w); }
+__device__ __forceinline__ Mat3 M3(const float4* c) { return Mat3{V3(c[0]), V3(c[1]), V3(c[2])}; }
+
 }  // namespace kzg

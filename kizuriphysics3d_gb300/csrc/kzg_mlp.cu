@@ -1,0 +1,733 @@
+// kzg_mlp.cu - learned warm start for contact points that miss the manifold cache.
+//
+// The reference warm-starts a new contact point with the impulses of the nearest cached point
+// within 0.1 m, else with zero (BuildContactConstraints, PhysicsWorld.cpp:518-529).  With a model
+// loaded and enabled, the zero is replaced by the prediction of a small MLP: 24 features of the
+// prepared contact row -> 64 -> 64 -> 3 (ReLU), BF16 weights and activations, FP32 accumulation on
+// the tensor cores (mma.sync m16n8k16 bf16).  The network predicts the impulses divided by the row
+// effective masses (a velocity, m/s; learned through asinh, see kTargetScale); the impulse is the
+// prediction times the effective mass, clamped into the friction cone.  The solver then runs unchanged, so the solution still converges
+// to the same tolerance - the prediction only changes where it starts.
+//
+// The same translation unit holds the training path (all on the GPU): logging of features and
+// converged impulses during a step, and one Adam step = forward + backward over a batch of logged
+// samples (one CTA per 128 samples, per-CTA partial gradients summed in a fixed order, so training
+// is deterministic).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "kzg_ctx.h"
+#include "kzg_internal.h"
+
+namespace kzg {
+
+namespace {
+
+constexpr int kF = KZG_MLP_FEATURES;  // 24
+constexpr int kH = 64;
+constexpr int kO = 3;
+constexpr int kP = KZG_MLP_PARAMS;  // 5955
+constexpr int kOffW1 = 0, kOffB1 = kH * kF, kOffW2 = kOffB1 + kH, kOffB2 = kOffW2 + kH * kH, kOffW3 = kOffB2 + kH,
+              kOffB3 = kOffW3 + kO * kH;
+static_assert(kOffB3 + kO == kP, "parameter layout");
+constexpr int kTile = 128;  // samples per CTA (4 warps x 32 rows)
+constexpr int kMlpThreads = 128;
+constexpr int kLogFloats = KZG_MLP_LOG_FLOATS;  // 24 features + 3 targets + 3 masks
+
+// shared-memory strides (bf16 elements), padded by 8 to spread banks
+constexpr int SX = 40, SH = 72, ST = 136, SY = 24;
+
+typedef __nv_bfloat16 bf16;
+
+__device__ __forceinline__ uint32_t ld2(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+// D(16x8) += A(16x16, row-major) * B(16x8); A rows at a (lda), B stored as 8 rows of K (ldb).
+__device__ __forceinline__ void mma_16x8x16(float c[4], const bf16* a, int lda, const bf16* b, int ldb, int lane) {
+    const int g = lane >> 2, t = lane & 3;
+    const uint32_t a0 = ld2(a + g * lda + 2 * t), a1 = ld2(a + (g + 8) * lda + 2 * t);
+    const uint32_t a2 = ld2(a + g * lda + 2 * t + 8), a3 = ld2(a + (g + 8) * lda + 2 * t + 8);
+    const uint32_t b0 = ld2(b + g * ldb + 2 * t), b1 = ld2(b + g * ldb + 2 * t + 8);
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// C tile (16 x 8*NT) = A (16 x K) * B^T where B is stored as rows of K; K a multiple of 16.
+template <int NT>
+__device__ __forceinline__ void warp_gemm(float (&c)[NT][4], const bf16* a, int lda, const bf16* b, int ldb, int K,
+                                          int lane) {
+#pragma unroll
+    for (int n = 0; n < NT; ++n) c[n][0] = c[n][1] = c[n][2] = c[n][3] = 0.0f;
+    for (int k = 0; k < K; k += 16)
+#pragma unroll
+        for (int n = 0; n < NT; ++n) mma_16x8x16(c[n], a + k, lda, b + n * 8 * ldb + k, ldb, lane);
+}
+
+struct MlpSmemFwd {
+    bf16 X[kTile * SX];
+    bf16 H1[kTile * SH];
+    bf16 H2[kTile * SH];
+    bf16 W1[kH * SX];
+    bf16 W2[kH * SH];
+    bf16 W3[8 * SH];
+    float b1[kH], b2[kH], b3[8];
+    float Y[kTile * 4];
+};
+
+// Stage the bf16 weights (W1 padded to K = 32, W3 padded to 8 rows) and biases.
+__device__ void stage_weights(const float* __restrict__ th, bf16* W1, bf16* W2, bf16* W3, float* b1, float* b2,
+                              float* b3, int tid) {
+    for (int i = tid; i < kH * 32; i += kMlpThreads) {
+        const int r = i >> 5, k = i & 31;
+        W1[r * SX + k] = __float2bfloat16_rn(k < kF ? th[kOffW1 + r * kF + k] : 0.0f);
+    }
+    for (int i = tid; i < kH * kH; i += kMlpThreads) W2[(i >> 6) * SH + (i & 63)] = __float2bfloat16_rn(th[kOffW2 + i]);
+    for (int i = tid; i < 8 * kH; i += kMlpThreads) {
+        const int r = i >> 6, k = i & 63;
+        W3[r * SH + k] = __float2bfloat16_rn(r < kO ? th[kOffW3 + r * kH + k] : 0.0f);
+    }
+    for (int i = tid; i < kH; i += kMlpThreads) {
+        b1[i] = th[kOffB1 + i];
+        b2[i] = th[kOffB2 + i];
+    }
+    if (tid < 8) b3[tid] = tid < kO ? th[kOffB3 + tid] : 0.0f;
+}
+
+// Forward pass of the warp's 32 rows: X -> H1 -> H2 -> Y (fp32, 3 of 4 columns used).
+// Optional transposed copies (feature-major) of H1/H2 for the weight gradients.
+__device__ void forward_rows(bf16* X, bf16* H1, bf16* H2, const bf16* W1, const bf16* W2, const bf16* W3,
+                             const float* b1, const float* b2, const float* b3, float* Y, bf16* H1t, bf16* H2t,
+                             int warp, int lane) {
+    const int g = lane >> 2, t = lane & 3;
+    for (int layer = 0; layer < 2; ++layer) {
+        const bf16* A = layer == 0 ? X : H1;
+        const int lda = layer == 0 ? SX : SH, K = layer == 0 ? 32 : kH;
+        const bf16* W = layer == 0 ? W1 : W2;
+        const int ldw = layer == 0 ? SX : SH;
+        const float* bias = layer == 0 ? b1 : b2;
+        bf16* Hout = layer == 0 ? H1 : H2;
+        bf16* Ht = layer == 0 ? H1t : H2t;
+        for (int mt = 0; mt < 2; ++mt) {
+            const int r0 = warp * 32 + mt * 16;
+            float c[8][4];
+            warp_gemm<8>(c, A + r0 * lda, lda, W, ldw, K, lane);
+#pragma unroll
+            for (int n = 0; n < 8; ++n)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int row = r0 + g + (q >> 1) * 8, col = n * 8 + 2 * t + (q & 1);
+                    const bf16 h = __float2bfloat16_rn(fmaxf(c[n][q] + bias[col], 0.0f));
+                    Hout[row * SH + col] = h;
+                    if (Ht) Ht[col * ST + row] = h;
+                }
+        }
+        __syncwarp();
+    }
+    for (int mt = 0; mt < 2; ++mt) {
+        const int r0 = warp * 32 + mt * 16;
+        float c[1][4];
+        warp_gemm<1>(c, H2 + r0 * SH, SH, W3, SH, kH, lane);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int row = r0 + g + (q >> 1) * 8, col = 2 * t + (q & 1);
+            if (col < 4) Y[row * 4 + col] = c[0][q] + b3[col];
+        }
+    }
+    __syncwarp();
+}
+
+// ---- features ------------------------------------------------------------------------------
+// 24 features of a prepared contact row that missed the cache, in the contact frame (n, t1, t2):
+//   0 normal velocity  1-2 tangential velocities  3 penetration depth
+//   4-6 rA . (n, t1, t2)   7-9 rB . (n, t1, t2)
+//   10-11 log inverse masses   12-13 log n.I^-1 n (A, B)
+//   14-16 impulses of the pair's nearest cached point / effective masses (0 without one)
+//   17 distance to that point (-1 without one)
+//   18-20 log effective masses (n, t1, t2)   21 friction   22 restitution bias   23 dt (g . n)
+// Mass-like quantities enter as log(x + 1e-6) so that bodies of any size share one scale.
+__device__ void row_features(const DeviceBodies& b, const DeviceRows& r, uint32_t A, uint32_t B, uint32_t row,
+                             float4 prior, float3 g, float dt, float* f) {
+    const Vec3 n = V3(r.n[row]), t1 = V3(r.t1[row]), t2 = V3(r.t2[row]);
+    const Vec3 rA = V3(r.rAr[row]), rB = V3(r.rBr[row]);
+    const Vec3 rel = (V3(b.lv[A]) + V3(b.av[A]).cross(rA)) - (V3(b.lv[B]) + V3(b.av[B]).cross(rB));
+    const float4 m = r.mass[row], bias = r.bias[row];
+    const Mat3 IA = M3(&b.iiw[3 * A]), IB = M3(&b.iiw[3 * B]);
+    const float eps = 1e-6f;
+    f[0] = bias.z;
+    f[1] = rel.dot(t1);
+    f[2] = rel.dot(t2);
+    f[3] = -r.pA[row].w;
+    f[4] = rA.dot(n); f[5] = rA.dot(t1); f[6] = rA.dot(t2);
+    f[7] = rB.dot(n); f[8] = rB.dot(t1); f[9] = rB.dot(t2);
+    f[10] = logf(b.inv_mass[A] + eps);
+    f[11] = logf(b.inv_mass[B] + eps);
+    f[12] = logf(n.dot(IA * n) + eps);
+    f[13] = logf(n.dot(IB * n) + eps);
+    f[14] = m.x > 0.0f ? prior.x / m.x : 0.0f;
+    f[15] = m.y > 0.0f ? prior.y / m.y : 0.0f;
+    f[16] = m.z > 0.0f ? prior.z / m.z : 0.0f;
+    f[17] = prior.w;
+    f[18] = logf(m.x + eps);
+    f[19] = logf(m.y + eps);
+    f[20] = logf(m.z + eps);
+    f[21] = r.t1[row].w;
+    f[22] = bias.x;
+    f[23] = dt * ((g.x * n.x + g.y * n.y) + g.z * n.z);
+}
+
+// Targets are impulse / effective mass y (m/s), learned as asinh(y / kTargetScale) so that the
+// heavy tail of deep-stack contacts does not swamp the loss; predictions map back with sinh,
+// limited to |y| <= kTargetScale * sinh(kOutLimit).
+constexpr float kTargetScale = 0.05f;
+constexpr float kOutLimit = 6.0f;
+
+struct StepView {
+    DeviceBodies b;
+    DeviceRows r;
+    const uint32_t *con_a, *con_b, *miss_rows;
+    const float4* miss_prior;
+    const Counters* cnt;
+    float3 g;
+    float dt;
+};
+
+// ---- inference: warm start of the cache misses --------------------------------------------
+__global__ void __launch_bounds__(kMlpThreads) k_mlp_infer(StepView v, const float* __restrict__ theta,
+                                                        const float* __restrict__ norm) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    MlpSmemFwd& S = *reinterpret_cast<MlpSmemFwd*>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    stage_weights(theta, S.W1, S.W2, S.W3, S.b1, S.b2, S.b3, tid);
+    const uint32_t nmiss = v.cnt->nmiss;
+    for (uint32_t base = blockIdx.x * kTile; base < nmiss; base += gridDim.x * kTile) {
+        const uint32_t k = base + tid;
+        uint32_t row = 0;
+        if (k < nmiss) {
+            row = v.miss_rows[k];
+            const uint32_t c = row >> 2;
+            float f[kF];
+            row_features(v.b, v.r, v.con_a[c], v.con_b[c], row, v.miss_prior[k], v.g, v.dt, f);
+            for (int i = 0; i < kF; ++i) S.X[tid * SX + i] = __float2bfloat16_rn((f[i] - norm[i]) * norm[kF + i]);
+        } else {
+            for (int i = 0; i < kF; ++i) S.X[tid * SX + i] = __float2bfloat16_rn(0.0f);
+        }
+        for (int i = kF; i < 32; ++i) S.X[tid * SX + i] = __float2bfloat16_rn(0.0f);
+        __syncthreads();
+        forward_rows(S.X, S.H1, S.H2, S.W1, S.W2, S.W3, S.b1, S.b2, S.b3, S.Y, nullptr, nullptr, warp, lane);
+        __syncthreads();
+        if (k < nmiss) {
+            const float4 m = v.r.mass[row];
+            const float fric = v.r.t1[row].w;
+            float y[3];
+            for (int q = 0; q < 3; ++q) y[q] = kTargetScale * sinhf(fminf(fmaxf(S.Y[tid * 4 + q], -kOutLimit), kOutLimit));
+            const float ni = fmaxf(y[0] * m.x, 0.0f);
+            const float mf = fric * ni;
+            const float t1 = fminf(fmaxf(y[1] * m.y, -mf), mf);
+            const float t2 = fminf(fmaxf(y[2] * m.z, -mf), mf);
+            const float4 im = v.r.imp[row];
+            v.r.imp[row] = make_float4(ni, t1, t2, im.w);
+        }
+        __syncthreads();
+    }
+}
+
+// ---- logging: features before the solve, converged impulses after it ----------------------
+__global__ void k_mlp_log_features(StepView v, float* log, const uint32_t* log_n, uint32_t cap) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= v.cnt->nmiss) return;
+    const uint32_t slot = *log_n + k;
+    if (slot >= cap) return;
+    const uint32_t row = v.miss_rows[k], c = row >> 2;
+    float f[kF];
+    row_features(v.b, v.r, v.con_a[c], v.con_b[c], row, v.miss_prior[k], v.g, v.dt, f);
+    float* o = log + (size_t)slot * kLogFloats;
+    for (int i = 0; i < kF; ++i) o[i] = f[i];
+}
+
+__global__ void k_mlp_log_targets(StepView v, float* log, const uint32_t* log_n, uint32_t cap) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= v.cnt->nmiss) return;
+    const uint32_t slot = *log_n + k;
+    if (slot >= cap) return;
+    const uint32_t row = v.miss_rows[k];
+    const float4 m = v.r.mass[row], im = v.r.imp[row];
+    float* o = log + (size_t)slot * kLogFloats + kF;
+    const float ms[3] = {m.x, m.y, m.z}, ls[3] = {im.x, im.y, im.z};
+    for (int q = 0; q < 3; ++q) {
+        const bool ok = ms[q] > 0.0f;
+        o[q] = ok ? ls[q] / ms[q] : 0.0f;
+        o[3 + q] = ok ? 1.0f : 0.0f;
+    }
+}
+
+__global__ void k_mlp_log_advance(const Counters* cnt, uint32_t* log_n, uint32_t cap) {
+    *log_n = min(cap, *log_n + cnt->nmiss);
+}
+
+// ---- training ------------------------------------------------------------------------------
+struct MlpSmemTrain {
+    MlpSmemFwd f;
+    bf16 Xt[32 * ST];
+    bf16 H1t[kH * ST];
+    bf16 H2t[kH * ST];
+    bf16 dZ2[kTile * SH];
+    bf16 dZ2t[kH * ST];
+    bf16 dZ1t[kH * ST];
+    bf16 dY[kTile * SY];
+    bf16 dYt[16 * ST];
+    bf16 W2T[kH * SH];
+    bf16 W3T[kH * SY];
+    float bred[4][kH + kH + 8];
+    float lred[4];
+};
+
+// Column sums over the warp's 16-row tile fragments, in a fixed order (xor tree over the 8 row
+// groups); returns the sum for columns 2t and 2t+1 of n-tile n in lanes with g == 0.
+__device__ __forceinline__ float2 frag_colsum(const float c[4]) {
+    float s0 = c[0] + c[2], s1 = c[1] + c[3];
+#pragma unroll
+    for (int o = 4; o < 32; o <<= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    return make_float2(s0, s1);
+}
+
+// One CTA: forward + backward of up to 128 samples; writes its partial gradient (kP floats) and
+// partial loss.  Loss = sum over valid outputs of (y - target)^2 * inv_nvalid.
+__global__ void __launch_bounds__(kMlpThreads) k_mlp_train(const float* __restrict__ theta, const float* __restrict__ norm,
+                                                        const float* __restrict__ ds, uint32_t first, uint32_t count,
+                                                        float inv_nvalid, float* __restrict__ part,
+                                                        float* __restrict__ part_loss) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    MlpSmemTrain& S = *reinterpret_cast<MlpSmemTrain*>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    stage_weights(theta, S.f.W1, S.f.W2, S.f.W3, S.f.b1, S.f.b2, S.f.b3, tid);
+    for (int i = tid; i < kH * kH; i += kMlpThreads) {  // W2T[i][j] = W2[j][i]
+        const int j = i >> 6, ii = i & 63;
+        S.W2T[ii * SH + j] = __float2bfloat16_rn(theta[kOffW2 + i]);
+    }
+    for (int i = tid; i < kH * 16; i += kMlpThreads) {  // W3T[h][o] = W3[o][h], o padded to 16
+        const int h = i >> 4, o = i & 15;
+        S.W3T[h * SY + o] = __float2bfloat16_rn(o < kO ? theta[kOffW3 + o * kH + h] : 0.0f);
+    }
+    const uint32_t s = blockIdx.x * kTile + tid;
+    const bool valid = s < count;
+    const float* rec = ds + (size_t)(first + (valid ? s : 0)) * kLogFloats;
+    float tgt[3] = {0, 0, 0}, msk[3] = {0, 0, 0};
+    for (int i = 0; i < 32; ++i) {
+        const float x = (valid && i < kF) ? (rec[i] - norm[i]) * norm[kF + i] : 0.0f;
+        const bf16 xb = __float2bfloat16_rn(x);
+        S.f.X[tid * SX + i] = xb;
+        S.Xt[i * ST + tid] = xb;
+    }
+    if (valid)
+        for (int q = 0; q < 3; ++q) {
+            tgt[q] = rec[kF + q];
+            msk[q] = rec[kF + 3 + q];
+        }
+    __syncthreads();
+    forward_rows(S.f.X, S.f.H1, S.f.H2, S.f.W1, S.f.W2, S.f.W3, S.f.b1, S.f.b2, S.f.b3, S.f.Y, S.H1t, S.H2t, warp,
+                 lane);
+    __syncthreads();
+    // loss and dY (fp32 -> bf16 for the GEMMs; fp32 for the bias gradient)
+    float loss = 0.0f, dy[3];
+    for (int q = 0; q < 3; ++q) {
+        const float e = S.f.Y[tid * 4 + q] - tgt[q];
+        loss += msk[q] * e * e;
+        dy[q] = msk[q] * 2.0f * e * inv_nvalid;
+    }
+    for (int o = 0; o < 16; ++o) {
+        const bf16 v = __float2bfloat16_rn(o < 3 ? dy[o] : 0.0f);
+        S.dY[tid * SY + o] = v;
+        S.dYt[o * ST + tid] = v;
+    }
+    {  // fixed-order block sums: loss, db3
+        float l = loss * inv_nvalid, d0 = dy[0], d1 = dy[1], d2 = dy[2];
+        for (int o = 16; o > 0; o >>= 1) {
+            l += __shfl_xor_sync(0xffffffffu, l, o);
+            d0 += __shfl_xor_sync(0xffffffffu, d0, o);
+            d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+            d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+        }
+        if (lane == 0) {
+            S.lred[warp] = l;
+            S.bred[warp][2 * kH + 0] = d0;
+            S.bred[warp][2 * kH + 1] = d1;
+            S.bred[warp][2 * kH + 2] = d2;
+        }
+    }
+    __syncthreads();
+    float* P = part + (size_t)blockIdx.x * kP;
+    // dW3 (3 x 64) = dY^T H2: M = 16 (3 used), N = 64 -> warp w takes n-tiles 2w, 2w+1
+    {
+        float c[2][4];
+        warp_gemm<2>(c, S.dYt, ST, S.H2t + (warp * 16) * ST, ST, kTile, lane);
+        for (int n = 0; n < 2; ++n)
+            for (int q = 0; q < 4; ++q) {
+                const int o = g + (q >> 1) * 8, h = warp * 16 + n * 8 + 2 * t + (q & 1);
+                if (o < kO) P[kOffW3 + o * kH + h] = c[n][q];
+            }
+    }
+    // dH2 = dY W3 -> dZ2 = dH2 * (H2 > 0), own rows
+    for (int mt = 0; mt < 2; ++mt) {
+        const int r0 = warp * 32 + mt * 16;
+        float c[8][4];
+        warp_gemm<8>(c, S.dY + r0 * SY, SY, S.W3T, SY, 16, lane);
+        for (int n = 0; n < 8; ++n)
+            for (int q = 0; q < 4; ++q) {
+                const int row = r0 + g + (q >> 1) * 8, col = n * 8 + 2 * t + (q & 1);
+                const bool on = __bfloat162float(S.f.H2[row * SH + col]) > 0.0f;
+                c[n][q] = on ? c[n][q] : 0.0f;
+                const bf16 v = __float2bfloat16_rn(c[n][q]);
+                S.dZ2[row * SH + col] = v;
+                S.dZ2t[col * ST + row] = v;
+            }
+        for (int n = 0; n < 8; ++n) {  // db2 partial of this 16-row tile
+            const float2 cs = frag_colsum(c[n]);
+            if (g == 0) {
+                if (mt == 0) {
+                    S.bred[warp][kH + n * 8 + 2 * t] = cs.x;
+                    S.bred[warp][kH + n * 8 + 2 * t + 1] = cs.y;
+                } else {
+                    S.bred[warp][kH + n * 8 + 2 * t] += cs.x;
+                    S.bred[warp][kH + n * 8 + 2 * t + 1] += cs.y;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // dW2 (64 x 64) = dZ2^T H1: 4 m-tiles x 8 n-tiles, warp w takes m-tile w
+    {
+        float c[8][4];
+        warp_gemm<8>(c, S.dZ2t + (warp * 16) * ST, ST, S.H1t, ST, kTile, lane);
+        for (int n = 0; n < 8; ++n)
+            for (int q = 0; q < 4; ++q) {
+                const int j = warp * 16 + g + (q >> 1) * 8, i = n * 8 + 2 * t + (q & 1);
+                P[kOffW2 + j * kH + i] = c[n][q];
+            }
+    }
+    // dH1 = dZ2 W2 -> dZ1 = dH1 * (H1 > 0), own rows (transposed copy only)
+    for (int mt = 0; mt < 2; ++mt) {
+        const int r0 = warp * 32 + mt * 16;
+        float c[8][4];
+        warp_gemm<8>(c, S.dZ2 + r0 * SH, SH, S.W2T, SH, kH, lane);
+        for (int n = 0; n < 8; ++n)
+            for (int q = 0; q < 4; ++q) {
+                const int row = r0 + g + (q >> 1) * 8, col = n * 8 + 2 * t + (q & 1);
+                const bool on = __bfloat162float(S.f.H1[row * SH + col]) > 0.0f;
+                c[n][q] = on ? c[n][q] : 0.0f;
+                S.dZ1t[col * ST + row] = __float2bfloat16_rn(c[n][q]);
+            }
+        for (int n = 0; n < 8; ++n) {
+            const float2 cs = frag_colsum(c[n]);
+            if (g == 0) {
+                if (mt == 0) {
+                    S.bred[warp][n * 8 + 2 * t] = cs.x;
+                    S.bred[warp][n * 8 + 2 * t + 1] = cs.y;
+                } else {
+                    S.bred[warp][n * 8 + 2 * t] += cs.x;
+                    S.bred[warp][n * 8 + 2 * t + 1] += cs.y;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // dW1 (64 x 24) = dZ1^T X: 4 m-tiles x 4 n-tiles (32 columns, 24 kept), warp w takes m-tile w
+    {
+        float c[4][4];
+        warp_gemm<4>(c, S.dZ1t + (warp * 16) * ST, ST, S.Xt, ST, kTile, lane);
+        for (int n = 0; n < 4; ++n)
+            for (int q = 0; q < 4; ++q) {
+                const int i = warp * 16 + g + (q >> 1) * 8, f = n * 8 + 2 * t + (q & 1);
+                if (f < kF) P[kOffW1 + i * kF + f] = c[n][q];
+            }
+    }
+    // bias gradients and loss: sum the four warps in order
+    for (int i = tid; i < kH + kH + kO; i += kMlpThreads) {
+        const float v = ((S.bred[0][i] + S.bred[1][i]) + S.bred[2][i]) + S.bred[3][i];
+        if (i < kH) P[kOffB1 + i] = v;
+        else if (i < 2 * kH) P[kOffB2 + (i - kH)] = v;
+        else P[kOffB3 + (i - 2 * kH)] = v;
+    }
+    if (tid == 0) part_loss[blockIdx.x] = ((S.lred[0] + S.lred[1]) + S.lred[2]) + S.lred[3];
+}
+
+// grad[i] = sum over CTAs of part[cta][i], in CTA order.
+__global__ void k_mlp_reduce(const float* __restrict__ part, const float* __restrict__ part_loss, uint32_t nblk,
+                             float* __restrict__ grad, float* __restrict__ loss) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < (uint32_t)kP) {
+        float s = 0.0f;
+        for (uint32_t bidx = 0; bidx < nblk; ++bidx) s += part[(size_t)bidx * kP + i];
+        grad[i] = s;
+    }
+    if (i == 0) {
+        float s = 0.0f;
+        for (uint32_t bidx = 0; bidx < nblk; ++bidx) s += part_loss[bidx];
+        *loss = s;
+    }
+}
+
+__global__ void k_mlp_adam(float* __restrict__ theta, float* __restrict__ m, float* __restrict__ v,
+                           const float* __restrict__ grad, float lr, float bc1, float bc2) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint32_t)kP) return;
+    const float gi = grad[i];
+    const float mi = 0.9f * m[i] + 0.1f * gi, vi = 0.999f * v[i] + 0.001f * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    theta[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + 1e-8f);
+}
+
+// Forward only over dataset samples (predictions for tests).
+__global__ void __launch_bounds__(kMlpThreads) k_mlp_predict(const float* __restrict__ theta, const float* __restrict__ norm,
+                                                          const float* __restrict__ ds, uint32_t first, uint32_t count,
+                                                          float* __restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    MlpSmemFwd& S = *reinterpret_cast<MlpSmemFwd*>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    stage_weights(theta, S.W1, S.W2, S.W3, S.b1, S.b2, S.b3, tid);
+    const uint32_t s = blockIdx.x * kTile + tid;
+    const bool valid = s < count;
+    const float* rec = ds + (size_t)(first + (valid ? s : 0)) * kLogFloats;
+    for (int i = 0; i < 32; ++i)
+        S.X[tid * SX + i] = __float2bfloat16_rn((valid && i < kF) ? (rec[i] - norm[i]) * norm[kF + i] : 0.0f);
+    __syncthreads();
+    forward_rows(S.X, S.H1, S.H2, S.W1, S.W2, S.W3, S.b1, S.b2, S.b3, S.Y, nullptr, nullptr, warp, lane);
+    __syncthreads();
+    if (valid)
+        for (int q = 0; q < kO; ++q) out[(size_t)s * kO + q] = S.Y[tid * 4 + q];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------------------------
+#define MLP_CK(x)                                                      \
+    do {                                                               \
+        cudaError_t e_ = (x);                                          \
+        if (e_ != cudaSuccess) {                                       \
+            ctx.err = std::string(#x) + ": " + cudaGetErrorString(e_); \
+            return KZG_ERR_CUDA;                                       \
+        }                                                              \
+    } while (0)
+
+cudaError_t mlp_configure_kernels() {
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(MlpSmemTrain));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmemFwd));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_mlp_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmemFwd));
+}
+
+static kzg_status mlp_alloc(Ctx& ctx) {
+    MlpState& M = ctx.mlp;
+    if (M.theta) return KZG_OK;
+    MLP_CK(cudaMalloc(&M.theta, sizeof(float) * kP));
+    MLP_CK(cudaMalloc(&M.adam_m, sizeof(float) * kP));
+    MLP_CK(cudaMalloc(&M.adam_v, sizeof(float) * kP));
+    MLP_CK(cudaMalloc(&M.grad, sizeof(float) * (kP + 1)));
+    MLP_CK(cudaMalloc(&M.norm, sizeof(float) * 2 * kF));
+    MLP_CK(cudaMalloc(&M.log_n, sizeof(uint32_t)));
+    MLP_CK(cudaMemset(M.adam_m, 0, sizeof(float) * kP));
+    MLP_CK(cudaMemset(M.adam_v, 0, sizeof(float) * kP));
+    MLP_CK(cudaMemset(M.log_n, 0, sizeof(uint32_t)));
+    return KZG_OK;
+}
+
+void mlp_free(Ctx& ctx) {
+    MlpState& M = ctx.mlp;
+    for (void* p : {(void*)M.theta, (void*)M.adam_m, (void*)M.adam_v, (void*)M.grad, (void*)M.norm, (void*)M.log_n,
+                    (void*)M.log, (void*)M.ds, (void*)M.part, (void*)M.out})
+        if (p) cudaFree(p);
+    M = MlpState{};
+}
+
+kzg_status mlp_set_params(Ctx& ctx, const float* theta, const float* mean, const float* stdv) {
+    kzg_status s = mlp_alloc(ctx);
+    if (s != KZG_OK) return s;
+    std::vector<float> norm(2 * kF);
+    for (int i = 0; i < kF; ++i) {
+        if (!(stdv[i] > 0.0f)) {
+            ctx.err = "feature standard deviations must be > 0";
+            return KZG_ERR_INVALID;
+        }
+        norm[i] = mean[i];
+        norm[kF + i] = 1.0f / stdv[i];
+    }
+    MLP_CK(cudaMemcpy(ctx.mlp.theta, theta, sizeof(float) * kP, cudaMemcpyHostToDevice));
+    MLP_CK(cudaMemcpy(ctx.mlp.norm, norm.data(), sizeof(float) * 2 * kF, cudaMemcpyHostToDevice));
+    MLP_CK(cudaMemset(ctx.mlp.adam_m, 0, sizeof(float) * kP));
+    MLP_CK(cudaMemset(ctx.mlp.adam_v, 0, sizeof(float) * kP));
+    ctx.mlp.adam_t = 0;
+    ctx.mlp.std.assign(stdv, stdv + kF);
+    ctx.mlp.have = true;
+    return KZG_OK;
+}
+
+kzg_status mlp_get_params(Ctx& ctx, float* theta, float* mean, float* stdv) {
+    if (!ctx.mlp.have) {
+        ctx.err = "no model parameters set";
+        return KZG_ERR_INVALID;
+    }
+    std::vector<float> norm(2 * kF);
+    MLP_CK(cudaMemcpy(theta, ctx.mlp.theta, sizeof(float) * kP, cudaMemcpyDeviceToHost));
+    MLP_CK(cudaMemcpy(norm.data(), ctx.mlp.norm, sizeof(float) * 2 * kF, cudaMemcpyDeviceToHost));
+    if (mean) std::memcpy(mean, norm.data(), sizeof(float) * kF);
+    if (stdv) std::memcpy(stdv, ctx.mlp.std.data(), sizeof(float) * kF);
+    return KZG_OK;
+}
+
+kzg_status mlp_log_begin(Ctx& ctx, uint32_t capacity) {
+    kzg_status s = mlp_alloc(ctx);
+    if (s != KZG_OK) return s;
+    MlpState& M = ctx.mlp;
+    if (M.log) cudaFree(M.log);
+    M.log = nullptr;
+    if (capacity) MLP_CK(cudaMalloc(&M.log, sizeof(float) * kLogFloats * (size_t)capacity));
+    MLP_CK(cudaMemset(M.log_n, 0, sizeof(uint32_t)));
+    M.log_cap = capacity;
+    M.logging = capacity > 0;
+    return KZG_OK;
+}
+
+kzg_status mlp_log_fetch(Ctx& ctx, float* out, uint32_t cap, uint32_t* n) {
+    MlpState& M = ctx.mlp;
+    uint32_t h = 0;
+    if (M.log_n) MLP_CK(cudaMemcpy(&h, M.log_n, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    *n = h;
+    if (out && h) MLP_CK(cudaMemcpy(out, M.log, sizeof(float) * kLogFloats * std::min(h, cap), cudaMemcpyDeviceToHost));
+    return KZG_OK;
+}
+
+kzg_status mlp_set_dataset(Ctx& ctx, const float* samples, uint32_t n) {
+    kzg_status s = mlp_alloc(ctx);
+    if (s != KZG_OK) return s;
+    MlpState& M = ctx.mlp;
+    if (M.ds) cudaFree(M.ds);
+    M.ds = nullptr;
+    M.ds_n = n;
+    M.ds_valid_prefix.assign(n + 1, 0.0);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* m = samples + (size_t)i * kLogFloats + kF + 3;
+        M.ds_valid_prefix[i + 1] = M.ds_valid_prefix[i] + (double)(m[0] + m[1] + m[2]);
+    }
+    if (n) {
+        MLP_CK(cudaMalloc(&M.ds, sizeof(float) * kLogFloats * (size_t)n));
+        MLP_CK(cudaMemcpy(M.ds, samples, sizeof(float) * kLogFloats * (size_t)n, cudaMemcpyHostToDevice));
+    }
+    return KZG_OK;
+}
+
+static kzg_status mlp_batch_grad(Ctx& ctx, uint32_t first, uint32_t count, float* loss_out) {
+    MlpState& M = ctx.mlp;
+    if (!M.have || !M.ds || count == 0 || first > M.ds_n || count > M.ds_n - first) {
+        ctx.err = "mlp: parameters and a dataset covering [first, first + count) are required";
+        return KZG_ERR_INVALID;
+    }
+    const uint32_t nblk = (count + kTile - 1) / kTile;
+    if (nblk > M.part_blocks) {
+        if (M.part) cudaFree(M.part);
+        M.part = nullptr;
+        MLP_CK(cudaMalloc(&M.part, sizeof(float) * ((size_t)nblk * kP + nblk)));
+        M.part_blocks = nblk;
+    }
+    const double nvalid = M.ds_valid_prefix[first + count] - M.ds_valid_prefix[first];
+    const float inv = nvalid > 0.0 ? (float)(1.0 / nvalid) : 0.0f;
+    float* part_loss = M.part + (size_t)nblk * kP;
+    k_mlp_train<<<nblk, kMlpThreads, sizeof(MlpSmemTrain), ctx.stream>>>(M.theta, M.norm, M.ds, first, count, inv, M.part,
+                                                                     part_loss);
+    k_mlp_reduce<<<(kP + 255) / 256, 256, 0, ctx.stream>>>(M.part, part_loss, nblk, M.grad, M.grad + kP);
+    MLP_CK(cudaGetLastError());
+    if (loss_out) {
+        MLP_CK(cudaMemcpyAsync(loss_out, M.grad + kP, sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
+        MLP_CK(cudaStreamSynchronize(ctx.stream));
+    }
+    return KZG_OK;
+}
+
+kzg_status mlp_gradient(Ctx& ctx, uint32_t first, uint32_t count, float* grad, float* loss) {
+    kzg_status s = mlp_batch_grad(ctx, first, count, loss);
+    if (s != KZG_OK) return s;
+    MLP_CK(cudaMemcpyAsync(grad, ctx.mlp.grad, sizeof(float) * kP, cudaMemcpyDeviceToHost, ctx.stream));
+    MLP_CK(cudaStreamSynchronize(ctx.stream));
+    return KZG_OK;
+}
+
+kzg_status mlp_train_step(Ctx& ctx, uint32_t first, uint32_t count, float lr, float* loss) {
+    kzg_status s = mlp_batch_grad(ctx, first, count, nullptr);
+    if (s != KZG_OK) return s;
+    MlpState& M = ctx.mlp;
+    ++M.adam_t;
+    const float bc1 = 1.0f - std::pow(0.9f, (float)M.adam_t), bc2 = 1.0f - std::pow(0.999f, (float)M.adam_t);
+    k_mlp_adam<<<(kP + 255) / 256, 256, 0, ctx.stream>>>(M.theta, M.adam_m, M.adam_v, M.grad, lr, bc1, bc2);
+    MLP_CK(cudaGetLastError());
+    if (loss) {
+        MLP_CK(cudaMemcpyAsync(loss, M.grad + kP, sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
+        MLP_CK(cudaStreamSynchronize(ctx.stream));
+    }
+    return KZG_OK;
+}
+
+kzg_status mlp_predict(Ctx& ctx, uint32_t first, uint32_t count, float* out) {
+    MlpState& M = ctx.mlp;
+    if (!M.have || !M.ds || first > M.ds_n || count > M.ds_n - first) {
+        ctx.err = "mlp: parameters and a dataset covering [first, first + count) are required";
+        return KZG_ERR_INVALID;
+    }
+    if (count == 0) return KZG_OK;
+    if (count > M.out_cap) {
+        if (M.out) cudaFree(M.out);
+        M.out = nullptr;
+        MLP_CK(cudaMalloc(&M.out, sizeof(float) * kO * (size_t)count));
+        M.out_cap = count;
+    }
+    const uint32_t nblk = (count + kTile - 1) / kTile;
+    k_mlp_predict<<<nblk, kMlpThreads, sizeof(MlpSmemFwd), ctx.stream>>>(M.theta, M.norm, M.ds, first, count, M.out);
+    MLP_CK(cudaGetLastError());
+    MLP_CK(cudaMemcpyAsync(out, M.out, sizeof(float) * kO * (size_t)count, cudaMemcpyDeviceToHost, ctx.stream));
+    MLP_CK(cudaStreamSynchronize(ctx.stream));
+    return KZG_OK;
+}
+
+// In-step hooks (kzg_step.cu).  launches: kernels issued.
+static StepView step_view(Ctx& ctx, float dt) {
+    return StepView{ctx.b, ctx.r, ctx.con_a, ctx.con_b, ctx.miss_rows, ctx.miss_prior, ctx.dcnt,
+                    make_float3(ctx.ws.gravity[0], ctx.ws.gravity[1], ctx.ws.gravity[2]), dt};
+}
+
+uint32_t mlp_after_prepare(Ctx& ctx, float dt) {
+    MlpState& M = ctx.mlp;
+    uint32_t n = 0;
+    const uint32_t rows = 4u * ctx.hcnt->ncons;
+    if (M.logging) {
+        k_mlp_log_features<<<(rows + 255) / 256, 256, 0, ctx.stream>>>(step_view(ctx, dt), M.log, M.log_n, M.log_cap);
+        ++n;
+    }
+    if (M.enabled && M.have) {
+        const unsigned grid = std::max(1u, std::min((rows + kTile - 1) / kTile, 152u * 4u));
+        k_mlp_infer<<<grid, kMlpThreads, sizeof(MlpSmemFwd), ctx.stream>>>(step_view(ctx, dt), M.theta, M.norm);
+        ++n;
+    }
+    return n;
+}
+
+uint32_t mlp_after_solve(Ctx& ctx, float dt) {
+    MlpState& M = ctx.mlp;
+    if (!M.logging) return 0;
+    const uint32_t rows = 4u * ctx.hcnt->ncons;
+    k_mlp_log_targets<<<(rows + 255) / 256, 256, 0, ctx.stream>>>(step_view(ctx, dt), M.log, M.log_n, M.log_cap);
+    k_mlp_log_advance<<<1, 1, 0, ctx.stream>>>(ctx.dcnt, M.log_n, M.log_cap);
+    return 2;
+}
+
+}  // namespace kzg

@@ -178,21 +178,23 @@ constexpr uint32_t kFfDead = 0xFFFFu;
 constexpr uint32_t kFfMaxLocal = 0xFFFFu - kFfCodes - 1u;
 
 struct FfTable {
-    uint32_t* bod[3];   // per slot: 6 body codes, two per word (0xFFFF = empty)
-    uint32_t* bid;      // per slot: batch index
-    uint16_t* list[2];  // per hub: slots of the open batches without that hub, batch order
-    uint16_t* remap;    // compaction: old slot -> new slot
-    uint8_t* cnt;       // per slot: points (bits 0-2) | kFfH0 | kFfH1 | codes (bits 5-7)
-    uint32_t* keys;     // code table: body index per entry (kNone = empty)
+    uint32_t *bod0, *bod1, *bod2;  // per slot: 6 body codes, two per word (0xFFFF = empty)
+    uint32_t* bid;                 // per slot: batch index
+    uint16_t *list0, *list1;       // per hub: slots of the open batches without that hub, batch order
+    uint16_t* remap;               // compaction: old slot -> new slot
+    uint8_t* cnt;                  // per slot: points (bits 0-2) | kFfH0 | kFfH1 | codes (bits 5-7)
+    uint32_t* keys;                // code table: body index per entry (kNone = empty)
 };
 
 __device__ __forceinline__ FfTable ff_table_of(void* smem_v) {
     uint8_t* smem = static_cast<uint8_t*>(smem_v);
     FfTable T;
-    for (int w = 0; w < 3; ++w) T.bod[w] = reinterpret_cast<uint32_t*>(smem + 4u * w * kFfSlots);
+    T.bod0 = reinterpret_cast<uint32_t*>(smem);
+    T.bod1 = reinterpret_cast<uint32_t*>(smem + 4u * kFfSlots);
+    T.bod2 = reinterpret_cast<uint32_t*>(smem + 8u * kFfSlots);
     T.bid = reinterpret_cast<uint32_t*>(smem + 12u * kFfSlots);
-    T.list[0] = reinterpret_cast<uint16_t*>(smem + 16u * kFfSlots);
-    T.list[1] = reinterpret_cast<uint16_t*>(smem + 18u * kFfSlots);
+    T.list0 = reinterpret_cast<uint16_t*>(smem + 16u * kFfSlots);
+    T.list1 = reinterpret_cast<uint16_t*>(smem + 18u * kFfSlots);
     T.remap = reinterpret_cast<uint16_t*>(smem + 20u * kFfSlots);
     T.cnt = smem + 22u * kFfSlots;
     T.keys = reinterpret_cast<uint32_t*>(smem + 23u * kFfSlots);
@@ -222,7 +224,7 @@ __device__ __forceinline__ uint32_t ff_code(const FfTable& T, uint32_t x, uint32
 __device__ __forceinline__ bool ff_holds(uint32_t w, uint32_t x) { return (w & 0xFFFFu) == x || (w >> 16) == x; }
 
 // Drop full batches from the slots and the hub lists (whole warp).
-__device__ void ff_compact(const FfTable& T, uint32_t& ns, uint32_t* nl, uint32_t lane) {
+__device__ void ff_compact(const FfTable& T, uint32_t& ns, uint32_t& nl0, uint32_t& nl1, uint32_t lane) {
     const unsigned full = 0xffffffffu, lt = (1u << lane) - 1u;
     uint32_t out = 0;
     for (uint32_t base = 0; base < ns; base += 32) {
@@ -233,9 +235,9 @@ __device__ void ff_compact(const FfTable& T, uint32_t& ns, uint32_t* nl, uint32_
             cn = T.cnt[i];
             live = (cn & 7u) < 4u;
             bid = T.bid[i];
-            w0 = T.bod[0][i];
-            w1 = T.bod[1][i];
-            w2 = T.bod[2][i];
+            w0 = T.bod0[i];
+            w1 = T.bod1[i];
+            w2 = T.bod2[i];
         }
         const unsigned m = __ballot_sync(full, live);
         const uint32_t idx = out + __popc(m & lt);
@@ -244,23 +246,24 @@ __device__ void ff_compact(const FfTable& T, uint32_t& ns, uint32_t* nl, uint32_
         if (live) {
             T.cnt[idx] = (uint8_t)cn;
             T.bid[idx] = bid;
-            T.bod[0][idx] = w0;
-            T.bod[1][idx] = w1;
-            T.bod[2][idx] = w2;
+            T.bod0[idx] = w0;
+            T.bod1[idx] = w1;
+            T.bod2[idx] = w2;
         }
         out += __popc(m);
         __syncwarp();
     }
     ns = out;
     for (int f = 0; f < 2; ++f) {
-        uint16_t* L = T.list[f];
+        uint16_t* L = f ? T.list1 : T.list0;
         const uint32_t flag = f ? kFfH1 : kFfH0;
+        const uint32_t n = f ? nl1 : nl0;
         uint32_t o = 0;
-        for (uint32_t base = 0; base < nl[f]; base += 32) {
+        for (uint32_t base = 0; base < n; base += 32) {
             const uint32_t i = base + lane;
             uint32_t s2 = kFfDead;
             bool live = false;
-            if (i < nl[f]) {
+            if (i < n) {
                 s2 = T.remap[L[i]];
                 live = s2 != kFfDead && !(T.cnt[s2] & flag);
             }
@@ -271,135 +274,149 @@ __device__ void ff_compact(const FfTable& T, uint32_t& ns, uint32_t* nl, uint32_
             o += __popc(m);
             __syncwarp();
         }
-        nl[f] = o;
+        if (f) nl1 = o; else nl0 = o;
     }
     __syncwarp();
 }
 
-// Append body codes to a slot's code words (one lane).
+// Append a body code to a slot's code words (one lane).
 __device__ __forceinline__ uint32_t ff_add_code(const FfTable& T, uint32_t slot, uint32_t nc, uint32_t code) {
-    const uint32_t w = nc >> 1, sh = 16u * (nc & 1u);
-    T.bod[w][slot] = (T.bod[w][slot] & ~(0xFFFFu << sh)) | (code << sh);
+    uint32_t* w = nc < 2u ? T.bod0 : (nc < 4u ? T.bod1 : T.bod2);
+    const uint32_t sh = 16u * (nc & 1u);
+    w[slot] = (w[slot] & ~(0xFFFFu << sh)) | (code << sh);
     return nc + 1;
 }
 
 // First-fit batches of one island's points (whole warp).  Returns the number of batches, or kNone
 // when the open batches do not fit the table.
+//
+// All points of a constraint share its two bodies, so point p's first fit (searched after point
+// p-1's batch, PhysicsWorld.cpp:688-706) is the p-th open candidate, in batch order, that holds
+// neither body: one scan serves the whole constraint, and the points are placed by the lanes that
+// found their candidates.  Constraint fields are fetched two 32-constraint windows ahead.
 __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1, uint32_t rb, uint32_t hub0,
                                    uint32_t hub1, uint32_t nloc, uint8_t* smem, uint32_t lane) {
-    const unsigned full = 0xffffffffu;
+    const unsigned full = 0xffffffffu, lt = (1u << lane) - 1u;
     const FfTable T = ff_table_of(smem);
-    uint32_t ns = 0, nbt = 0, nl[2] = {0, 0};
-    uint32_t head = 0, hhead[2] = {0, 0};
+    uint32_t ns = 0, nbt = 0, nl0 = 0, nl1 = 0, head = 0, head0 = 0, head1 = 0;
+    // pipeline: id of the constraint two windows ahead, fields of the next window
+    auto load_id = [&](uint32_t w0) -> uint32_t { return w0 + lane < s1 ? S.isl_con[w0 + lane] : kNone; };
+    uint32_t nx_c = load_id(s0), nx_bits = 1u, nx_a = 0, nx_b = 0, nx_np = 0, nx_la = kNone, nx_lb = kNone;
+    if (nx_c != kNone) {
+        nx_bits = S.con_bits[nx_c]; nx_a = S.con_a[nx_c]; nx_b = S.con_b[nx_c]; nx_np = S.con_np[nx_c];
+        nx_la = S.con_la[nx_c]; nx_lb = S.con_lb[nx_c];
+    }
+    uint32_t id2 = load_id(s0 + 32);
     for (uint32_t w0 = s0; w0 < s1; w0 += 32) {
-        uint32_t mc = 0, mbits = 1u, ma = 0, mb = 0, mnp = 0, mca = kFfDead, mcb = kFfDead;
-        if (w0 + lane < s1) {
-            mc = S.isl_con[w0 + lane];
-            mbits = S.con_bits[mc];
-            ma = S.con_a[mc];
-            mb = S.con_b[mc];
-            mnp = S.con_np[mc];
-            if (!(mbits & 1u)) {
-                if (ma != hub0 && ma != hub1) mca = ff_code(T, ma, S.con_la[mc], nloc);
-                if (mb != hub0 && mb != hub1) mcb = ff_code(T, mb, S.con_lb[mc], nloc);
+        const uint32_t mc = nx_c, mbits = nx_bits, ma = nx_a, mb = nx_b, mnp = nx_np, mla = nx_la, mlb = nx_lb;
+        nx_c = id2;  // fields of the next window start loading now
+        nx_bits = 1u; nx_np = 0; nx_la = kNone; nx_lb = kNone;
+        if (nx_c != kNone) {
+            nx_bits = S.con_bits[nx_c]; nx_a = S.con_a[nx_c]; nx_b = S.con_b[nx_c]; nx_np = S.con_np[nx_c];
+            nx_la = S.con_la[nx_c]; nx_lb = S.con_lb[nx_c];
+        }
+        id2 = load_id(w0 + 64);
+        // decode this lane's constraint: body codes and hub
+        uint32_t dx = 0, meta = 0;  // meta: np | hub + 1 << 4 | sensor << 6
+        if (mc != kNone) {
+            const int ha = ma == hub0 ? 0 : (ma == hub1 ? 1 : -1);
+            const int hb = mb == hub0 ? 0 : (mb == hub1 ? 1 : -1);
+            const int hub = ha >= 0 ? ha : hb;
+            const bool sensor = (mbits & 1u) != 0u;
+            uint32_t x0 = kFfDead, x1 = kFfDead;
+            if (!sensor) {
+                const uint32_t ca = ha >= 0 ? kFfDead : ff_code(T, ma, mla, nloc);
+                const uint32_t cb = hb >= 0 ? kFfDead : ff_code(T, mb, mlb, nloc);
+                x0 = hub < 0 ? ca : (ha >= 0 ? cb : ca);
+                x1 = hub < 0 ? cb : x0;
             }
+            dx = x0 | (x1 << 16);
+            meta = mnp | ((uint32_t)(hub + 1) << 4) | (sensor ? 64u : 0u);
+        } else {
+            meta = 64u;
         }
         const uint32_t m = min(32u, s1 - w0);
         for (uint32_t k = 0; k < m; ++k) {
-            const uint32_t c = __shfl_sync(full, mc, k), bits = __shfl_sync(full, mbits, k);
-            if (bits & 1u) continue;  // sensors are never batched (:690)
-            const uint32_t a = __shfl_sync(full, ma, k), b = __shfl_sync(full, mb, k), np = __shfl_sync(full, mnp, k);
-            const uint32_t ca = __shfl_sync(full, mca, k), cb = __shfl_sync(full, mcb, k);
-            const int ha = a == hub0 ? 0 : (a == hub1 ? 1 : -1);
-            const int hb = b == hub0 ? 0 : (b == hub1 ? 1 : -1);
-            const int hub = ha >= 0 ? ha : hb;
-            // codes tested against a candidate: both bodies, or the non-hub body twice
-            const uint32_t x0 = hub < 0 ? ca : (ha >= 0 ? cb : ca);
-            const uint32_t x1 = hub < 0 ? cb : x0;
+            const uint32_t md = __shfl_sync(full, meta, k);
+            if (md & 64u) continue;  // sensors are never batched (:690)
+            const uint32_t c = __shfl_sync(full, mc, k), xx = __shfl_sync(full, dx, k);
+            const uint32_t np = md & 15u, x0 = xx & 0xFFFFu, x1 = xx >> 16;
+            const int hub = (int)((md >> 4) & 3u) - 1;
             const uint32_t hflag = hub == 0 ? kFfH0 : (hub == 1 ? kFfH1 : 0u);
-            uint32_t pos = hub < 0 ? head : hhead[hub];
-            for (uint32_t p = 0; p < np; ++p) {
-                // ---- search: first open candidate holding neither body
-                const uint16_t* L = hub < 0 ? nullptr : T.list[hub];
-                const uint32_t nL = hub < 0 ? ns : nl[hub];
-                int slot = -1;
-                uint32_t lidx = 0;
-                for (;;) {
-                    const uint32_t i = pos + lane;
-                    bool live = false, ok = false;
-                    uint32_t s = 0;
-                    if (i < nL) {
-                        s = hub < 0 ? i : L[i];
-                        const uint32_t cn = T.cnt[s];
-                        live = (cn & 7u) < 4u && !(cn & hflag);
-                        if (live) {
-                            const uint32_t w0c = T.bod[0][s], w1c = T.bod[1][s], w2c = T.bod[2][s];
-                            ok = !(ff_holds(w0c, x0) || ff_holds(w1c, x0) || ff_holds(w2c, x0) ||
-                                   ff_holds(w0c, x1) || ff_holds(w1c, x1) || ff_holds(w2c, x1));
-                        }
+            const uint16_t* L = hub == 0 ? T.list0 : T.list1;
+            const uint32_t nL = hub < 0 ? ns : (hub == 0 ? nl0 : nl1);
+            uint32_t pos = hub < 0 ? head : (hub == 0 ? head0 : head1);
+            uint32_t placed = 0;
+            // ---- scan: the first np open candidates holding neither body take the points
+            while (placed < np && pos < nL) {
+                const uint32_t i = pos + lane;
+                bool live = false, ok = false;
+                uint32_t s = 0, cn = 0;
+                if (i < nL) {
+                    s = hub < 0 ? i : L[i];
+                    cn = T.cnt[s];
+                    live = (cn & 7u) < 4u && !(cn & hflag);
+                    if (live) {
+                        const uint32_t w0c = T.bod0[s], w1c = T.bod1[s], w2c = T.bod2[s];
+                        ok = !(ff_holds(w0c, x0) || ff_holds(w1c, x0) || ff_holds(w2c, x0) ||
+                               ff_holds(w0c, x1) || ff_holds(w1c, x1) || ff_holds(w2c, x1));
                     }
-                    const unsigned livem = __ballot_sync(full, live);
-                    const unsigned okm = __ballot_sync(full, ok);
-                    uint32_t& hd = hub < 0 ? head : hhead[hub];
-                    if (pos == hd) {  // skip a dead prefix for good
-                        if (livem) hd += __ffs(livem) - 1;
-                        else if (pos + 32 <= nL) hd += 32;
-                    }
-                    if (okm) {
-                        const uint32_t found = __ffs(okm) - 1;
-                        slot = (int)__shfl_sync(full, s, found);
-                        lidx = pos + found;
-                        break;
-                    }
-                    if (pos + 32 >= nL) break;
-                    pos += 32;
                 }
-                // ---- place
-                const uint32_t row = 4u * c + p;
-                if (slot >= 0) {
-                    const uint32_t j = T.bid[slot];
-                    __syncwarp();
-                    if (lane == 0) {
-                        const uint32_t cn = T.cnt[slot], kk = cn & 7u;
+                const unsigned livem = __ballot_sync(full, live);
+                const unsigned okm = __ballot_sync(full, ok);
+                const uint32_t hd = hub < 0 ? head : (hub == 0 ? head0 : head1);
+                if (pos == hd) {  // skip a dead prefix for good
+                    const uint32_t adv = livem ? (uint32_t)(__ffs(livem) - 1) : (pos + 32 <= nL ? 32u : 0u);
+                    if (hub < 0) head += adv; else if (hub == 0) head0 += adv; else head1 += adv;
+                }
+                const uint32_t take = min((uint32_t)__popc(okm), np - placed);
+                if (ok) {
+                    const uint32_t rank = __popc(okm & lt);
+                    if (rank < take) {  // place point placed + rank into this candidate
+                        const uint32_t kk = cn & 7u;
                         uint32_t nc = cn >> 5;
                         if (kk + 1 < 4u) {  // a full batch's codes are never read again
-                            nc = ff_add_code(T, slot, nc, x0);
-                            if (hub < 0) nc = ff_add_code(T, slot, nc, x1);
+                            nc = ff_add_code(T, s, nc, x0);
+                            if (hub < 0) nc = ff_add_code(T, s, nc, x1);
                         }
-                        T.cnt[slot] = (uint8_t)((kk + 1) | (cn & (kFfH0 | kFfH1)) | hflag | (nc << 5));
-                        uint32_t* r = rec(S, rb + j);
-                        r[12 + kk] = row;
+                        T.cnt[s] = (uint8_t)((kk + 1) | (cn & (kFfH0 | kFfH1)) | hflag | (nc << 5));
+                        uint32_t* r = rec(S, rb + T.bid[s]);
+                        r[12 + kk] = 4u * c + placed + rank;
                         r[3] = kk + 1;
                     }
-                    pos = (hub < 0 ? (uint32_t)slot : lidx) + 1;
-                } else {
-                    if (ns == kFfSlots) {
-                        ff_compact(T, ns, nl, lane);
-                        head = 0;
-                        hhead[0] = 0;
-                        hhead[1] = 0;
-                        if (ns > kFfSlots - 1024u) return kNone;
-                    }
-                    const uint32_t sl = ns++, j = nbt++;
-                    __syncwarp();
-                    if (lane == 0) {
-                        T.bid[sl] = j;
-                        T.bod[0][sl] = hub < 0 ? (x0 | (x1 << 16)) : (x0 | 0xFFFF0000u);
-                        T.bod[1][sl] = 0xFFFFFFFFu;
-                        T.bod[2][sl] = 0xFFFFFFFFu;
-                        T.cnt[sl] = (uint8_t)(1u | hflag | ((hub < 0 ? 2u : 1u) << 5));
-                        uint32_t* r = rec(S, rb + j);
-                        r[3] = 1;
-                        r[12] = row;
-                        if (hub != 0) T.list[0][nl[0]] = (uint16_t)sl;
-                        if (hub != 1) T.list[1][nl[1]] = (uint16_t)sl;
-                    }
-                    if (hub != 0) ++nl[0];
-                    if (hub != 1) ++nl[1];
-                    pos = hub < 0 ? ns : nl[hub];
                 }
-                __syncwarp();
+                placed += take;
+                pos += 32;
             }
+            // ---- the remaining points open new batches
+            const uint32_t rem = np - placed;
+            if (rem) {
+                if (ns + rem > kFfSlots) {
+                    ff_compact(T, ns, nl0, nl1, lane);
+                    head = 0;
+                    head0 = 0;
+                    head1 = 0;
+                    if (ns + rem > kFfSlots - 1024u) return kNone;
+                }
+                if (lane < rem) {
+                    const uint32_t sl = ns + lane, j = nbt + lane;
+                    T.bid[sl] = j;
+                    T.bod0[sl] = hub < 0 ? (x0 | (x1 << 16)) : (x0 | 0xFFFF0000u);
+                    T.bod1[sl] = 0xFFFFFFFFu;
+                    T.bod2[sl] = 0xFFFFFFFFu;
+                    T.cnt[sl] = (uint8_t)(1u | hflag | ((hub < 0 ? 2u : 1u) << 5));
+                    uint32_t* r = rec(S, rb + j);
+                    r[3] = 1;
+                    r[12] = 4u * c + placed + lane;
+                    if (hub != 0) T.list0[nl0 + lane] = (uint16_t)sl;
+                    if (hub != 1) T.list1[nl1 + lane] = (uint16_t)sl;
+                }
+                ns += rem;
+                nbt += rem;
+                if (hub != 0) nl0 += rem;
+                if (hub != 1) nl1 += rem;
+            }
+            __syncwarp();
         }
     }
     return nbt;

@@ -27,6 +27,8 @@ struct SolveBufs {
     uint32_t vel_iters, pos_iters;
     float ws_factor;
     int vel_bias;
+    float res_tol;     // > 0: residual-terminated velocity iterations
+    uint32_t res_cap;  // their cap
 };
 
 // Velocity storage of one island: staged in shared memory (local index) or read/written in place
@@ -72,7 +74,9 @@ __device__ __forceinline__ void warm_point(const SolveBufs& S, const VelView& V,
 
 // One lane of SolveVelocityBatchSIMD (ContactSolverSIMD.cpp:93-256): friction t1, t2 (relative
 // velocity recomputed before each axis), then normal; _mm_{add,sub,mul,min,max}_ps semantics.
-__device__ __forceinline__ void velocity_point(const SolveBufs& S, const VelView& V, uint32_t row) {
+// Returns the point's share of the island residual: (sum over its rows of |dImpulse|,
+// (|n| + |t1|) + |t2| of its accumulated impulses).
+__device__ __forceinline__ float2 velocity_point(const SolveBufs& S, const VelView& V, uint32_t row) {
     const uint32_t c = row >> 2;
     const uint32_t A = S.con_a[c], B = S.con_b[c], la = S.con_la[c], lb = S.con_lb[c];
     const Vec3 rA = V3(S.r.rAr[row]), rB = V3(S.r.rBr[row]);
@@ -85,6 +89,7 @@ __device__ __forceinline__ void velocity_point(const SolveBufs& S, const VelView
     const float nb = bias.x + (S.vel_bias ? bias.y : 0.0f);
     const float fric = t14.w;
     float nacc = im.x, t1acc = im.y, t2acc = im.z;
+    float dsum = 0.0f;
 #pragma unroll
     for (int t = 0; t < 3; ++t) {
         const Vec3 dir = t == 0 ? V3(t14) : (t == 1 ? V3(t24) : V3(n4));
@@ -110,6 +115,7 @@ __device__ __forceinline__ void velocity_point(const SolveBufs& S, const VelView
             dl = na - nacc;
             nacc = na;
         }
+        dsum += fabsf(dl);
         const Vec3 imp(dir.x * dl, dir.y * dl, dir.z * dl);
         vA = Vec3(vA.x + imp.x * invA, vA.y + imp.y * invA, vA.z + imp.z * invA);
         wA = wA + IA * rA.cross(imp);
@@ -119,6 +125,13 @@ __device__ __forceinline__ void velocity_point(const SolveBufs& S, const VelView
     if (la != kNone) V.put(la, A, vA, wA);
     if (lb != kNone) V.put(lb, B, vB, wB);
     S.r.imp[row] = make_float4(nacc, t1acc, t2acc, im.w);
+    return make_float2(dsum, (fabsf(nacc) + fabsf(t1acc)) + fabsf(t2acc));
+}
+
+// Fixed-point (2^-20 N s) magnitude for the residual sums: integer sums are exact and independent
+// of the order of the additions, so the stopping iteration does not depend on the thread count.
+__device__ __forceinline__ unsigned long long res_fixed(float x) {
+    return (unsigned long long)(fminf(x, 1e12f) * 1048576.0f);
 }
 
 // SolveBiasConstraint for one point (ContactSolver.cpp:265-289); V holds pseudo velocities.
@@ -144,24 +157,49 @@ __device__ __forceinline__ void bias_point(const SolveBufs& S, const VelView& V,
     if (lb != kNone) V.put(lb, B, pvB - imp * S.b.inv_mass[B], pwB - M3(&S.b.iiw[3 * B]) * rB.cross(imp));
 }
 
-// Warm start + velocity sweeps, then the bias sweeps, of one island; sync() separates levels.
+// Warm start + velocity sweeps of one island; sync() separates levels.  Velocity iterations run
+// the fixed count, or - with a residual tolerance - until the island's residual, the relative
+// impulse change sum|dImpulse| / sum|impulse| of an iteration (reduced by sync.sum2), is within
+// it, at most res_cap times.
 template <typename Sync>
 __device__ __forceinline__ void solve_velocity(const SolveBufs& S, uint32_t isl, const VelView& V, uint32_t tid,
-                                               uint32_t nthreads, Sync sync) {
+                                               uint32_t nthreads, Sync sync, Counters* cnt) {
     const uint32_t base = 4u * S.isl_start[isl];
     const uint32_t loff = base + isl;
     const uint32_t nw = S.meta[4 * isl], nv = S.meta[4 * isl + 1];
+    sync.reset(tid);
     for (uint32_t l = 0; l < nw; ++l) {
         const uint32_t e = S.wl_off[loff + l + 1];
         for (uint32_t k = S.wl_off[loff + l] + tid; k < e; k += nthreads) warm_point(S, V, S.wl_list[base + k]);
         sync();
     }
-    for (uint32_t it = 0; it < S.vel_iters; ++it)
+    const bool residual = S.res_tol > 0.0f;
+    const uint32_t iters = residual ? S.res_cap : S.vel_iters;
+    uint32_t used = 0;
+    float res = 0.0f;
+    for (uint32_t it = 0; it < iters; ++it) {
+        unsigned long long sd = 0, sl = 0;
         for (uint32_t l = 0; l < nv; ++l) {
             const uint32_t e = S.vl_off[loff + l + 1];
-            for (uint32_t k = S.vl_off[loff + l] + tid; k < e; k += nthreads) velocity_point(S, V, S.vl_list[base + k]);
+            for (uint32_t k = S.vl_off[loff + l] + tid; k < e; k += nthreads) {
+                const float2 q = velocity_point(S, V, S.vl_list[base + k]);
+                sd += res_fixed(q.x);
+                sl += res_fixed(q.y);
+            }
             sync();
         }
+        used = it + 1;
+        if (residual || used == iters) {
+            sync.sum2(sd, sl, it);
+            res = sl ? (float)((double)sd / (double)sl) : (sd ? 1.0f : 0.0f);
+            if (residual && (double)sd <= (double)S.res_tol * (double)sl) break;
+        }
+    }
+    if (tid == 0) {
+        atomicMax(&cnt->max_iters, used);
+        atomicAdd(&cnt->pt_iters, S.vl_off[loff + nv] * used);
+        atomicMax(&cnt->res_bits, __float_as_uint(res));
+    }
 }
 
 template <typename Sync>
@@ -179,11 +217,47 @@ __device__ __forceinline__ void solve_bias(const SolveBufs& S, uint32_t isl, con
         }
 }
 
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 struct WarpSync {
     __device__ __forceinline__ void operator()() const { __syncwarp(); }
+    __device__ __forceinline__ void reset(uint32_t) const {}
+    // group-wide sums of the two residual accumulators (every lane gets them)
+    __device__ __forceinline__ void sum2(unsigned long long& a, unsigned long long& b, uint32_t) const {
+        a = warp_sum(a);
+        b = warp_sum(b);
+    }
 };
+// Residual sums go through three rotating pairs of shared words: iteration it accumulates into
+// red[it % 3] and clears red[(it + 1) % 3], which was last read two barriers earlier.
 struct CtaSync {
+    unsigned long long* red;  // 3 x 2 words
     __device__ __forceinline__ void operator()() const { __syncthreads(); }
+    __device__ __forceinline__ void reset(uint32_t tid) const {
+        if (tid < 6) red[tid] = 0ull;
+        __syncthreads();
+    }
+    __device__ __forceinline__ void sum2(unsigned long long& a, unsigned long long& b, uint32_t it) const {
+        a = warp_sum(a);
+        b = warp_sum(b);
+        unsigned long long* r = red + 2 * (it % 3);
+        if ((threadIdx.x & 31u) == 0) {
+            atomicAdd(&r[0], a);
+            atomicAdd(&r[1], b);
+        }
+        if (threadIdx.x == 0) {
+            unsigned long long* nx = red + 2 * ((it + 1) % 3);
+            nx[0] = 0ull;
+            nx[1] = 0ull;
+        }
+        __syncthreads();
+        a = r[0];
+        b = r[1];
+    }
 };
 
 // Stage an island's velocities in shared memory, run the warm-start and velocity sweeps, write
@@ -191,7 +265,7 @@ struct CtaSync {
 // start of every step, PhysicsWorld.cpp:286-287) and the bias sweeps.
 template <typename Sync>
 __device__ __forceinline__ void solve_island_shared(const SolveBufs& S, uint32_t isl, float4* sv, float4* sw,
-                                                    uint32_t tid, uint32_t nthreads, Sync sync) {
+                                                    uint32_t tid, uint32_t nthreads, Sync sync, Counters* cnt) {
     const uint32_t nloc = S.meta[4 * isl + 3];
     const uint32_t* bodies = S.isl_bodies + 2u * S.isl_start[isl];
     for (uint32_t k = tid; k < nloc; k += nthreads) {
@@ -200,7 +274,7 @@ __device__ __forceinline__ void solve_island_shared(const SolveBufs& S, uint32_t
     }
     sync();
     const VelView V{sv, sw, S.b.lv, S.b.av, true};
-    solve_velocity(S, isl, V, tid, nthreads, sync);
+    solve_velocity(S, isl, V, tid, nthreads, sync, cnt);
     for (uint32_t k = tid; k < nloc; k += nthreads) {
         S.b.lv[bodies[k]] = sv[k];
         S.b.av[bodies[k]] = sw[k];
@@ -218,39 +292,41 @@ __device__ __forceinline__ void solve_island_shared(const SolveBufs& S, uint32_t
 }
 
 // Small islands: one warp each.
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_solve_warp(SolveBufs S, const Counters* cnt) {
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_solve_warp(SolveBufs S, Counters* cnt) {
     extern __shared__ float4 smem[];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     float4* sv = smem + warp * 2u * kWarpBodies;
     float4* sw = sv + kWarpBodies;
     const uint32_t n = cnt->nsmall;
     for (uint32_t idx = blockIdx.x * kWarpsPerBlock + warp; idx < n; idx += gridDim.x * kWarpsPerBlock)
-        solve_island_shared(S, S.small_list[idx], sv, sw, lane, 32u, WarpSync{});
+        solve_island_shared(S, S.small_list[idx], sv, sw, lane, 32u, WarpSync{}, cnt);
 }
 
 // Large islands whose velocities fit shared memory: one CTA each.
-__global__ void __launch_bounds__(kCtaThreads) k_solve_cta(SolveBufs S, const Counters* cnt, uint32_t smem_bodies) {
+__global__ void __launch_bounds__(kCtaThreads) k_solve_cta(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
     extern __shared__ float4 smem[];
+    __shared__ unsigned long long red[6];
     const uint32_t n = cnt->nlarge;
     for (uint32_t idx = blockIdx.x; idx < n; idx += gridDim.x) {
         const uint32_t isl = S.large_list[idx];
         if (S.meta[4 * isl + 3] > smem_bodies) continue;
-        solve_island_shared(S, isl, smem, smem + smem_bodies, threadIdx.x, blockDim.x, CtaSync{});
+        solve_island_shared(S, isl, smem, smem + smem_bodies, threadIdx.x, blockDim.x, CtaSync{red}, cnt);
     }
 }
 
 // Islands too large for shared memory: one 1024-thread CTA each, velocities updated in place
 // (L2-resident).  A level of a settled pile holds ~1,000 points, one per thread.
 constexpr uint32_t kBigThreads = 1024;
-__global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, const Counters* cnt, uint32_t smem_bodies) {
+__global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
+    __shared__ unsigned long long red[6];
     const uint32_t n = cnt->nlarge;
     for (uint32_t idx = blockIdx.x; idx < n; idx += gridDim.x) {
         const uint32_t isl = S.large_list[idx];
         if (S.meta[4 * isl + 3] <= smem_bodies) continue;
         const VelView V{S.b.lv, S.b.av, S.b.lv, S.b.av, false};
         const VelView P{S.b.plv, S.b.pav, S.b.lv, S.b.av, false};
-        solve_velocity(S, isl, V, threadIdx.x, blockDim.x, CtaSync{});
-        solve_bias(S, isl, P, threadIdx.x, blockDim.x, CtaSync{});
+        solve_velocity(S, isl, V, threadIdx.x, blockDim.x, CtaSync{red}, cnt);
+        solve_bias(S, isl, P, threadIdx.x, blockDim.x, CtaSync{red});
         __syncthreads();
     }
 }

@@ -20,6 +20,7 @@
 // result is bit-identical to the reference; levels only reorder work between bodies that share
 // no dynamic body, which cannot change any value.
 #include <cub/cub.cuh>
+#include <cstring>
 
 #include "kzg_ctx.h"
 #include "kzg_internal.h"
@@ -29,11 +30,6 @@ namespace kzg {
 // ---------------------------------------------------------------------------------------------
 // small helpers
 // ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ Vec3 V3(float4 a) { return Vec3(a.x, a.y, a.z); }
-__device__ __forceinline__ float4 F4(const Vec3& v, float w) { return make_float4(v.x, v.y, v.z, w); }
-__device__ __forceinline__ Quat Q4(float4 a) { return Quat(a.x, a.y, a.z, a.w); }
-__device__ __forceinline__ float4 F4q(const Quat& q) { return make_float4(q.x, q.y, q.z, q.w); }
-__device__ __forceinline__ Mat3 M3(const float4* c) { return Mat3{V3(c[0]), V3(c[1]), V3(c[2])}; }
 __device__ __forceinline__ unsigned long long pair_key(uint32_t pa, uint32_t pb) {
     if (pa > pb) { uint32_t t = pa; pa = pb; pb = t; }
     return ((unsigned long long)pa << 32) | (unsigned long long)pb;
@@ -255,7 +251,8 @@ __global__ void k_build_constraints(const uint2* __restrict__ pairs, const uint3
                                     uint32_t* con_np, uint32_t* con_bits, float2* con_fr,
                                     unsigned long long* con_key, DeviceRows r, const unsigned long long* __restrict__ c_key,
                                     const uint32_t* __restrict__ c_np, const float4* __restrict__ c_pos,
-                                    const float4* __restrict__ c_imp, uint32_t c_cap, int warm) {
+                                    const float4* __restrict__ c_imp, uint32_t c_cap, int warm, uint32_t* miss_rows,
+                                    float4* miss_prior) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t np = cnt->npairs;
     if (i >= np) return;
@@ -300,7 +297,28 @@ __global__ void k_build_constraints(const uint2* __restrict__ pairs, const uint3
             if (bi != kInvalid) {
                 float4 im = c_imp[4u * slot + bi];
                 ni = im.x; t1 = im.y; t2 = im.z;
+            } else if (miss_rows) {
+                // cache miss: remember the pair's nearest cached point at any distance (a feature
+                // of the learned warm start), then the reference's zero start stands
+                uint32_t nk = kInvalid;
+                float nd = 0.0f;
+                for (uint32_t k = 0; k < cn; ++k) {
+                    float d = (V3(c_pos[4u * slot + k]) - pa).len2();
+                    if (nk == kInvalid || d < nd) { nd = d; nk = k; }
+                }
+                const uint32_t m = atomicAdd(&cnt->nmiss, 1u);
+                miss_rows[m] = row;
+                float4 pr = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+                if (nk != kInvalid) {
+                    const float4 im = c_imp[4u * slot + nk];
+                    pr = make_float4(im.x, im.y, im.z, sqrtf(nd));
+                }
+                miss_prior[m] = pr;
             }
+        } else if (warm && miss_rows) {
+            const uint32_t m = atomicAdd(&cnt->nmiss, 1u);
+            miss_rows[m] = row;
+            miss_prior[m] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
         }
         r.imp[row] = make_float4(ni, t1, t2, 0.0f);
     }
@@ -562,8 +580,10 @@ cudaError_t configure_kernels() {
     e = cudaFuncSetAttribute(k_narrow_epa, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(kEpaWarps * sizeof(EpaWarpSmem)));
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_schedule_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(3 * kSchedCtaBodies * sizeof(uint32_t)));
+    e = cudaFuncSetAttribute(k_schedule_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(3 * kSchedCtaBodies * sizeof(uint32_t)));
+    if (e != cudaSuccess) return e;
+    return mlp_configure_kernels();
 }
 
 static int bits_for(uint32_t v) {
@@ -598,7 +618,8 @@ static kzg_status step_after_pairs(Ctx& ctx, float dt) {
         k_build_constraints<<<blocks_for(np), kThreads, 0, st>>>(
             ctx.pairs, ctx.con_flag, ctx.con_index, ctx.m_count, ctx.m_data, ctx.m_key, ctx.b, ctx.dcnt,
             ctx.con_pair, ctx.con_a, ctx.con_b, ctx.con_np, ctx.con_bits, ctx.con_fr, ctx.con_key, ctx.r, ctx.c_key,
-            ctx.c_np, ctx.c_pos, ctx.c_imp, ctx.cfg.max_cache_entries, ctx.ws.warm_start);
+            ctx.c_np, ctx.c_pos, ctx.c_imp, ctx.cfg.max_cache_entries, ctx.ws.warm_start,
+            (ctx.mlp.logging || (ctx.mlp.enabled && ctx.mlp.have)) ? ctx.miss_rows : nullptr, ctx.miss_prior);
     k_integrate_vel<<<blocks_for(nb), kThreads, 0, st>>>(
         ctx.b, nb, make_float3(ctx.ws.gravity[0], ctx.ws.gravity[1], ctx.ws.gravity[2]), dt);
     ctx.launches += np > 0 ? 2 : 1;
@@ -610,6 +631,7 @@ static kzg_status step_after_pairs(Ctx& ctx, float dt) {
         PrepParams pp{dt, ctx.ss.baumgarte, ctx.ss.penetration_slop, ctx.ss.restitution_threshold,
                       ctx.ss.max_bias_velocity};
         k_prepare<<<blocks_for(4 * nc), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_np, ctx.r, pp);
+        ctx.launches += mlp_after_prepare(ctx, dt);
         k_uf_init<<<blocks_for(nb), kThreads, 0, st>>>(ctx.uf, nb);
         k_uf_union<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf);
         k_island_keys<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf,
@@ -636,7 +658,8 @@ static kzg_status step_after_pairs(Ctx& ctx, float dt) {
         SolveBufs SV{ctx.isl_start, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.con_la, ctx.con_lb, ctx.isl_meta,
                      ctx.isl_bodies, ctx.wl_list, ctx.vl_list, ctx.bl_list, ctx.wl_off, ctx.vl_off, ctx.bl_off,
                      ctx.isl_small, ctx.isl_large, ctx.r, ctx.b, ctx.ss.velocity_iterations,
-                     ctx.ss.position_iterations, ctx.ss.warm_start_factor, ctx.ss.use_velocity_bias};
+                     ctx.ss.position_iterations, ctx.ss.warm_start_factor, ctx.ss.use_velocity_bias,
+                     ctx.ss.residual_tolerance, ctx.ss.max_velocity_iterations};
         if (ni > 0) {
             const unsigned gw = std::min<unsigned>(blocks_for(ni, kWarpsPerBlock), 152u * 16u);
             k_solve_warp<<<gw, kWarpsPerBlock * 32, kWarpsPerBlock * 2 * kWarpBodies * sizeof(float4), st>>>(SV, ctx.dcnt);
@@ -645,6 +668,7 @@ static kzg_status step_after_pairs(Ctx& ctx, float dt) {
             k_solve_big<<<std::min<unsigned>(ni, 152u), kBigThreads, 0, st>>>(SV, ctx.dcnt, kCtaBodiesMax);
             ctx.launches += 3;
         }
+        ctx.launches += mlp_after_solve(ctx, dt);
         KZG_CK(cudaEventRecord(ctx.ev[5], st));
         ++ctx.launches;
         k_cache_store<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.con_key, ctx.con_np, ctx.r, ctx.c_key,
@@ -681,6 +705,9 @@ static kzg_status finish_stats(Ctx& ctx) {
     s.cache_entries = h.cache_entries;
     s.device_error = h.error;
     s.kernel_launches = ctx.launches;
+    s.max_velocity_iterations_used = h.max_iters;
+    s.point_velocity_iterations = h.pt_iters;
+    memcpy(&s.final_residual, &h.res_bits, sizeof(float));
     cudaEventElapsedTime(&s.broadphase_ms, ctx.ev[0], ctx.ev[1]);
     cudaEventElapsedTime(&s.narrowphase_ms, ctx.ev[1], ctx.ev[2]);
     cudaEventElapsedTime(&s.constraints_ms, ctx.ev[2], ctx.ev[3]);

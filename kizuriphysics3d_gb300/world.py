@@ -136,6 +136,7 @@ class World:
         ss.use_velocity_bias = int(bool(scene.flags & WORLD_FLAG_VELOCITY_BIAS))
         self._check(L.kzg_set_world_settings(h, ctypes.byref(ws)))
         self._check(L.kzg_set_solver_settings(h, ctypes.byref(ss)))
+        self._ss = ss
         self._check(L.kzg_upload_shapes(h, descs, len(scene.shapes), capi.ptr(V), V.shape[0], capi.ptr(S), S.shape[0],
                                         capi.ptr(I), I.shape[0]))
         bodies = scene.bodies
@@ -169,6 +170,19 @@ class World:
         first = ctypes.c_uint32()
         self._check(L.kzg_add_bodies(h, n, ctypes.byref(soa), ctypes.byref(first)))
         self.dt = float(np.float32(scene.dt))
+
+    # -- settings ----------------------------------------------------------------------------
+    def set_solver(self, **fields):
+        """Change SolverSettings fields (kzg_solver_settings names) for the following steps."""
+        for k, v in fields.items():
+            if not hasattr(self._ss, k):
+                raise AttributeError(f"kzg_solver_settings has no field {k}")
+            setattr(self._ss, k, v)
+        self._check(capi.load().kzg_set_solver_settings(self._h, ctypes.byref(self._ss)))
+
+    def set_residual(self, tolerance: float, max_iterations: int = 64):
+        """Residual-terminated velocity iterations (tolerance in m/s; 0 = the fixed count)."""
+        self.set_solver(residual_tolerance=float(tolerance), max_velocity_iterations=int(max_iterations))
 
     # -- lifetime ----------------------------------------------------------------------------
     def close(self):
@@ -259,6 +273,57 @@ class World:
         if n.value:
             self._check(L.kzg_download_constraints(self._h, capi.ptr(hdr), capi.ptr(fr), capi.ptr(pts), n.value))
         return hdr, pts, fr
+
+    # -- learned warm start ------------------------------------------------------------------
+    def mlp_set_params(self, theta: np.ndarray, mean: np.ndarray, std: np.ndarray):
+        th = np.ascontiguousarray(theta, np.float32).reshape(-1)
+        if th.size != capi.MLP_PARAMS:
+            raise ValueError(f"expected {capi.MLP_PARAMS} parameters, got {th.size}")
+        mu = np.ascontiguousarray(mean, np.float32).reshape(-1)
+        sd = np.ascontiguousarray(std, np.float32).reshape(-1)
+        self._check(capi.load().kzg_mlp_set_params(self._h, capi.ptr(th), capi.ptr(mu), capi.ptr(sd)))
+
+    def mlp_get_params(self):
+        th = np.zeros(capi.MLP_PARAMS, np.float32)
+        mu = np.zeros(capi.MLP_FEATURES, np.float32)
+        sd = np.zeros(capi.MLP_FEATURES, np.float32)
+        self._check(capi.load().kzg_mlp_get_params(self._h, capi.ptr(th), capi.ptr(mu), capi.ptr(sd)))
+        return th, mu, sd
+
+    def mlp_enable(self, on: bool = True):
+        self._check(capi.load().kzg_mlp_enable(self._h, int(bool(on))))
+
+    def mlp_log_begin(self, capacity: int):
+        self._check(capi.load().kzg_mlp_log_begin(self._h, int(capacity)))
+
+    def mlp_log_fetch(self) -> np.ndarray:
+        L = capi.load()
+        n = ctypes.c_uint32()
+        self._check(L.kzg_mlp_log_fetch(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros((n.value, capi.MLP_LOG_FLOATS), np.float32)
+        if n.value:
+            self._check(L.kzg_mlp_log_fetch(self._h, capi.ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    def mlp_set_dataset(self, samples: np.ndarray):
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, capi.MLP_LOG_FLOATS)
+        self._check(capi.load().kzg_mlp_set_dataset(self._h, capi.ptr(s), s.shape[0]))
+
+    def mlp_gradient(self, first: int, count: int):
+        g = np.zeros(capi.MLP_PARAMS, np.float32)
+        loss = ctypes.c_float()
+        self._check(capi.load().kzg_mlp_gradient(self._h, first, count, capi.ptr(g), ctypes.byref(loss)))
+        return g, loss.value
+
+    def mlp_train_step(self, first: int, count: int, lr: float) -> float:
+        loss = ctypes.c_float()
+        self._check(capi.load().kzg_mlp_train_step(self._h, first, count, np.float32(lr), ctypes.byref(loss)))
+        return loss.value
+
+    def mlp_predict(self, first: int, count: int) -> np.ndarray:
+        out = np.zeros((count, 3), np.float32)
+        self._check(capi.load().kzg_mlp_predict(self._h, first, count, capi.ptr(out)))
+        return out
 
     # reference-style aliases
     StepFixed = step_fixed

@@ -38,6 +38,11 @@ void kzo_set_threads(kzo_world* w, int threads);
 void kzo_set_pair_mode(kzo_world* w, int mode);
 int kzo_set_external_pairs(kzo_world* w, const uint32_t* packed_pairs, uint32_t n);
 void kzo_set_schedule_stats(kzo_world* w, int enabled);
+/* Residual-terminated velocity iterations (not in the reference, which always runs the fixed
+ * count): tol > 0 stops an island's iterations once the relative impulse change of an iteration,
+ * sum|dImpulse| / sum|impulse| over its batched points (2^-20 N s fixed-point sums), is <= tol,
+ * after at most cap iterations; tol = 0 restores the fixed count. */
+void kzo_set_residual(kzo_world* w, float tol, uint32_t cap);
 
 int kzo_step(kzo_world* w, float dt);
 
@@ -54,8 +59,10 @@ uint32_t kzo_num_constraints(const kzo_world* w);
  * nImp t1Imp t2Imp restitutionBias positionBias biasImpulse normalVelocity */
 void kzo_get_constraints(const kzo_world* w, uint32_t* hdr, float* pts, float* fric_rest);
 /* pairs, constraints, points, islands, batches, max velocity levels, max bias levels,
- * largest island points, sum of velocity levels over islands, most batches open at once */
-void kzo_get_stats(const kzo_world* w, uint32_t* out10);
+ * largest island points, sum of velocity levels over islands, most batches open at once,
+ * most velocity iterations of an island, sum over islands of batched points x iterations,
+ * largest final residual (float bits) */
+void kzo_get_stats(const kzo_world* w, uint32_t* out13);
 void kzo_get_mass(const kzo_world* w, float* inv_mass, float* inv_inertia_world /*9 per body*/);
 
 /* Narrow phase between two bodies at their current poses (A = first argument). Returns the

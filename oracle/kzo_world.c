@@ -66,6 +66,8 @@ struct kzo_world {
     float fixed_dt, baumgarte, slop, rest_thresh, max_bias, ws_factor;
     uint32_t vel_iters, pos_iters;
     int vel_bias, no_ws, threads, pair_mode, sched_stats;
+    float res_tol;     /* > 0: velocity iterations stop once the island's residual is <= res_tol */
+    uint32_t res_cap;  /* iteration cap when res_tol > 0 */
     /* shapes */
     int nshapes;
     kzo_shape* shapes;
@@ -105,6 +107,8 @@ struct kzo_world {
     int* island_index;
     /* stats */
     uint32_t st_points, st_batches, st_max_vl, st_max_bl, st_max_isl_pts, st_sum_vl, st_max_open;
+    uint32_t st_max_iters, st_pt_iters;
+    float st_final_res;
 };
 
 /* ----------------------------------------------------------------------------- */
@@ -554,8 +558,15 @@ static void warm_start(kzo_world* w, con_t* c) {
     }
 }
 
-/* One lane of SolveVelocityBatchSIMD (ContactSolverSIMD.cpp:93-256). */
-static void solve_lane(kzo_world* w, con_t* c, cpc_t* p) {
+/* Fixed-point (2^-20 N s) magnitude used by the residual sums: integer sums do not depend on the
+ * order of the additions, so every implementation stops after the same iteration. */
+static uint64_t res_fixed(float x) { return (uint64_t)(fminf(x, 1e12f) * 1048576.0f); }
+
+/* One lane of SolveVelocityBatchSIMD (ContactSolverSIMD.cpp:93-256).  Adds the lane's share of the
+ * island residual: |dImpulse| summed over its three rows (t1, t2, n) to *sd and its accumulated
+ * |impulse| (|n| + |t1|) + |t2| to *sl.  The reference has no residual (fixed iteration counts);
+ * this one decides when a residual-terminated solve stops. */
+static void solve_lane(kzo_world* w, con_t* c, cpc_t* p, uint64_t* sd, uint64_t* sl) {
     int A = c->a, B = c->b;
     v3 rA = qrotate(w->rot[A], p->laA);
     v3 rB = qrotate(w->rot[B], p->laB);
@@ -565,6 +576,7 @@ static void solve_lane(kzo_world* w, con_t* c, cpc_t* p) {
     const m3* IB = &w->iiw[B];
     const float nb = p->rbias + (w->vel_bias ? p->pbias : 0.0f);
     float nacc = p->ni, t1acc = p->ti1, t2acc = p->ti2;
+    float dsum = 0.0f;
     for (int t = 0; t < 3; ++t) {
         v3 dir = t == 0 ? p->t1 : (t == 1 ? p->t2 : p->n);
         v3 wa = vcross(wA, rA), wb = vcross(wB, rB);
@@ -589,6 +601,7 @@ static void solve_lane(kzo_world* w, con_t* c, cpc_t* p) {
             dl = na - nacc;
             nacc = na;
         }
+        dsum += fabsf(dl);
         v3 imp = V(dir.x * dl, dir.y * dl, dir.z * dl);
         vA = V(vA.x + imp.x * invA, vA.y + imp.y * invA, vA.z + imp.z * invA);
         v3 cA = vcross(rA, imp);
@@ -602,6 +615,8 @@ static void solve_lane(kzo_world* w, con_t* c, cpc_t* p) {
     p->ni = nacc;
     p->ti1 = t1acc;
     p->ti2 = t2acc;
+    *sd += res_fixed(dsum);
+    *sl += res_fixed((fabsf(nacc) + fabsf(t1acc)) + fabsf(t2acc));
 }
 
 /* SolveBiasConstraint, ContactSolver.cpp:257-290 */
@@ -632,7 +647,7 @@ static void solve_bias(kzo_world* w, con_t* c) {
 
 /* SolveIsland, PhysicsWorld.cpp:666-743 (SIMD path, no joints). */
 static void solve_island(kzo_world* w, uint32_t isl, uint32_t* out_batches, uint32_t* out_vl, uint32_t* out_bl,
-                         uint32_t* out_pts) {
+                         uint32_t* out_pts, uint32_t* out_iters, uint32_t* out_pt_iters, float* out_res) {
     const uint32_t* list = w->isl_con + w->isl_off[isl];
     uint32_t nc = w->isl_off[isl + 1] - w->isl_off[isl];
     if (nc == 0) return;
@@ -675,12 +690,28 @@ static void solve_island(kzo_world* w, uint32_t isl, uint32_t* out_batches, uint
         }
     }
     if (w->sched_stats && max_open > w->st_max_open) w->st_max_open = max_open;  /* racy max: statistics only */
-    for (uint32_t it = 0; it < w->vel_iters; ++it)
+    /* velocity iterations: the fixed count (the reference), or until the island residual - the
+     * relative change sum|dImpulse| / sum|impulse| of the iteration - is <= res_tol, at most
+     * res_cap iterations */
+    const uint32_t iters = w->res_tol > 0.0f ? w->res_cap : w->vel_iters;
+    uint32_t used = 0;
+    float res = 0.0f;
+    for (uint32_t it = 0; it < iters; ++it) {
+        uint64_t sd = 0, sl = 0;
         for (uint32_t bi = 0; bi < nbt; ++bi)
             for (uint32_t k = 0; k < bt[bi].count; ++k) {
                 con_t* c = &w->cons[bt[bi].ref[k].con];
-                solve_lane(w, c, &c->p[bt[bi].ref[k].pt]);
+                solve_lane(w, c, &c->p[bt[bi].ref[k].pt], &sd, &sl);
             }
+        used = it + 1;
+        res = sl ? (float)((double)sd / (double)sl) : (sd ? 1.0f : 0.0f);
+        if (w->res_tol > 0.0f && (double)sd <= (double)w->res_tol * (double)sl) break;
+    }
+    uint32_t nbp = 0;
+    for (uint32_t bi = 0; bi < nbt; ++bi) nbp += bt[bi].count;
+    *out_iters = used;
+    *out_pt_iters = nbp * used;
+    *out_res = res;
     if (!w->vel_bias)
         for (uint32_t it = 0; it < w->pos_iters; ++it)
             for (uint32_t i = 0; i < nc; ++i) solve_bias(w, &w->cons[list[i]]);
@@ -920,18 +951,27 @@ int kzo_step(kzo_world* w, float dt) {
     build_islands(w);
     w->st_batches = w->st_max_vl = w->st_max_bl = w->st_max_isl_pts = w->st_sum_vl = w->st_max_open = 0;
     int ni = (int)w->nislands;
-    uint32_t* ib = (uint32_t*)calloc((size_t)(ni ? ni : 1) * 4, sizeof(uint32_t));
+    uint32_t* ib = (uint32_t*)calloc((size_t)(ni ? ni : 1) * 6, sizeof(uint32_t));
+    float* ires = (float*)calloc((size_t)(ni ? ni : 1), sizeof(float));
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 1) num_threads(w->threads) if (w->threads > 1 && ni > 1)
 #endif
-    for (int i = 0; i < ni; ++i) solve_island(w, (uint32_t)i, &ib[4 * i], &ib[4 * i + 1], &ib[4 * i + 2], &ib[4 * i + 3]);
+    for (int i = 0; i < ni; ++i)
+        solve_island(w, (uint32_t)i, &ib[6 * i], &ib[6 * i + 1], &ib[6 * i + 2], &ib[6 * i + 3], &ib[6 * i + 4],
+                     &ib[6 * i + 5], &ires[i]);
+    w->st_max_iters = w->st_pt_iters = 0;
+    w->st_final_res = 0.0f;
     for (int i = 0; i < ni; ++i) {
-        w->st_batches += ib[4 * i];
-        if (ib[4 * i + 1] > w->st_max_vl) w->st_max_vl = ib[4 * i + 1];
-        if (ib[4 * i + 2] > w->st_max_bl) w->st_max_bl = ib[4 * i + 2];
-        if (ib[4 * i + 3] > w->st_max_isl_pts) w->st_max_isl_pts = ib[4 * i + 3];
-        w->st_sum_vl += ib[4 * i + 1];
+        w->st_batches += ib[6 * i];
+        if (ib[6 * i + 1] > w->st_max_vl) w->st_max_vl = ib[6 * i + 1];
+        if (ib[6 * i + 2] > w->st_max_bl) w->st_max_bl = ib[6 * i + 2];
+        if (ib[6 * i + 3] > w->st_max_isl_pts) w->st_max_isl_pts = ib[6 * i + 3];
+        w->st_sum_vl += ib[6 * i + 1];
+        if (ib[6 * i + 4] > w->st_max_iters) w->st_max_iters = ib[6 * i + 4];
+        w->st_pt_iters += ib[6 * i + 5];
+        w->st_final_res = fmaxf(w->st_final_res, ires[i]);
     }
+    free(ires);
     free(ib);
     for (uint32_t ci = 0; ci < w->ncons; ++ci) {
         con_t* c = &w->cons[ci];
@@ -1106,6 +1146,10 @@ void kzo_destroy(kzo_world* w) {
 void kzo_set_threads(kzo_world* w, int t) { w->threads = t > 0 ? t : 1; }
 void kzo_set_pair_mode(kzo_world* w, int m) { w->pair_mode = m; }
 void kzo_set_schedule_stats(kzo_world* w, int e) { w->sched_stats = e; }
+void kzo_set_residual(kzo_world* w, float tol, uint32_t cap) {
+    w->res_tol = tol;
+    w->res_cap = cap ? cap : 1u;
+}
 int kzo_set_external_pairs(kzo_world* w, const uint32_t* p, uint32_t n) {
     w->ext_pairs = (uint32_t*)xrealloc(w->ext_pairs, sizeof(uint32_t) * 2 * (n ? n : 1));
     memcpy(w->ext_pairs, p, sizeof(uint32_t) * 2 * n);
@@ -1181,6 +1225,8 @@ void kzo_get_stats(const kzo_world* w, uint32_t* o) {
     o[0] = w->npairs; o[1] = w->ncons; o[2] = w->st_points; o[3] = w->nislands;
     o[4] = w->st_batches; o[5] = w->st_max_vl; o[6] = w->st_max_bl; o[7] = w->st_max_isl_pts; o[8] = w->st_sum_vl;
     o[9] = w->st_max_open;
+    o[10] = w->st_max_iters; o[11] = w->st_pt_iters;
+    memcpy(&o[12], &w->st_final_res, sizeof(float));
 }
 
 void kzo_get_mass(const kzo_world* w, float* im, float* iw) {

@@ -42,6 +42,7 @@ def lib():
         L.kzo_set_threads.argtypes = [vp, ctypes.c_int]
         L.kzo_set_pair_mode.argtypes = [vp, ctypes.c_int]
         L.kzo_set_schedule_stats.argtypes = [vp, ctypes.c_int]
+        L.kzo_set_residual.argtypes = [vp, f32, u32]
         L.kzo_set_external_pairs.argtypes = [vp, vp, u32]
         L.kzo_step.argtypes = [vp, f32]
         L.kzo_num_bodies.restype = u32
@@ -100,6 +101,9 @@ class OracleWorld:
     def set_schedule_stats(self, on: bool):
         lib().kzo_set_schedule_stats(self._w, int(on))
 
+    def set_residual(self, tol: float, cap: int = 64):
+        lib().kzo_set_residual(self._w, np.float32(tol), cap)
+
     def set_external_pairs(self, pairs: np.ndarray):
         p = np.ascontiguousarray(pairs, np.uint32)
         lib().kzo_set_external_pairs(self._w, _ptr(p), p.shape[0])
@@ -136,11 +140,14 @@ class OracleWorld:
         return hdr, pts, fr
 
     def stats(self) -> dict:
-        o = np.zeros(10, np.uint32)
+        o = np.zeros(13, np.uint32)
         lib().kzo_get_stats(self._w, _ptr(o))
         keys = ["pairs", "constraints", "points", "islands", "batches", "max_vel_levels",
-                "max_bias_levels", "max_island_points", "sum_vel_levels", "max_open_batches"]
-        return dict(zip(keys, (int(x) for x in o)))
+                "max_bias_levels", "max_island_points", "sum_vel_levels", "max_open_batches",
+                "max_velocity_iterations", "point_velocity_iterations"]
+        d = dict(zip(keys, (int(x) for x in o[:12])))
+        d["final_residual"] = float(o[12:13].view(np.float32)[0])
+        return d
 
     def mass(self):
         im = np.zeros(self.n, np.float32)

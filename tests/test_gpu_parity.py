@@ -103,6 +103,28 @@ def test_mode_b_settled_full_pile(oracle_lib, kzg_lib):
         assert np.array_equal(bits(gw.state()), bits(ow.state()))
 
 
+@pytest.mark.parametrize("name,steps", [("pile200", 120), ("pyramid20", 60)])
+def test_residual_terminated_bit_exact_with_oracle(name, steps, oracle_lib, kzg_lib):
+    """Residual-terminated velocity iterations (r <= 1e-4 m/s, cap 64): same iteration counts,
+    same final residual and same state bits as the oracle running the same rule."""
+    sc, g, ow, gw = _pair_worlds(name, oracle_lib.PAIRS_CANONICAL, oracle_lib)
+    ow.set_residual(1e-4, 64)
+    with gw:
+        gw.set_residual(1e-4, 64)
+        seen_iters = set()
+        for s in range(steps):
+            ow.step(np.float32(sc.dt))
+            gw.step_fixed()
+            o, st = ow.stats(), gw.get_stats()
+            assert st["max_velocity_iterations_used"] == o["max_velocity_iterations"], f"step {s}"
+            assert st["point_velocity_iterations"] == o["point_velocity_iterations"], f"step {s}"
+            assert np.float32(st["final_residual"]).view(np.uint32) == np.float32(o["final_residual"]).view(np.uint32)
+            assert gw.compute_state_hash() == ow.hash(), f"step {s}"
+            seen_iters.add(st["max_velocity_iterations_used"])
+        assert np.array_equal(bits(gw.state()), bits(ow.state()))
+        assert len(seen_iters) > 1  # the stopping rule actually varied the iteration count
+
+
 def test_hash_identical_run_to_run(kzg_lib):
     from kizuriphysics3d_gb300 import World, resolve, scenes
     sc = scenes.pile(800, seed=5, extent=4.0, y_range=(1.0, 12.0))
