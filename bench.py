@@ -54,6 +54,14 @@ def make_workload(name: str):
     if name == "pyramid20":
         return scenes.pyramid(20), 0, {
             "workload": "20-row pyramid, 210 unit boxes, 10 velocity + 2 position iterations, dt 1/60", "bodies": 210}
+    if name == "worlds4096":
+        sc, ids = scenes.merge_worlds(scenes.world_batch(4096, seed=4242))
+        sc.world_ids = ids
+        return sc, 0, {
+            "workload": "4096 independent worlds (seed 4242), bodies per world log-uniform in [8, 512]: even worlds "
+                        "pyramids, odd worlds convex piles with xz extent scaled by sqrt(N/20000), each with its own "
+                        "plane; 10 velocity + 2 position iterations, dt 1/60; one context, steps replayed from a "
+                        "captured CUDA graph, launch shapes autotuned", "bodies": len(sc.bodies), "worlds": 4096}
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -227,8 +235,11 @@ def main():
     res = resolve(sc)
     snap = load_snapshot(args.workload, preroll)
     start_scene = scene_with_state(sc, snap) if snap is not None else sc
-    max_pairs = max(48 * len(sc.bodies), 4096)  # a settled pile holds ~12 broad-phase pairs per body
-    w = World(start_scene, resolved=res, device=local_rank, max_pairs=max_pairs)
+    world_ids = getattr(sc, "world_ids", None)
+    batched = world_ids is not None
+    # a settled pile holds ~12 broad-phase pairs per body
+    max_pairs = max((16 if batched else 48) * len(sc.bodies), 4096)
+    w = World(start_scene, resolved=res, world_ids=world_ids, device=local_rank, max_pairs=max_pairs)
     t_setup = time.perf_counter()
     if snap is None and preroll:
         done = 0
@@ -247,14 +258,19 @@ def main():
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
 
+    tuned = {}
+
     def fresh_world(mode: str):
         """A world at the starting state, solving with the fixed iteration count ("fixed"), or
         residual-terminated with the plain ("plain") or learned ("learned") warm start."""
-        wx = World(start_scene, resolved=res, device=local_rank, max_pairs=max_pairs)
+        wx = World(start_scene, resolved=res, world_ids=world_ids, device=local_rank, max_pairs=max_pairs)
         if mode != "fixed":
             wx.set_residual(RESIDUAL_TOL, RESIDUAL_CAP)
         if mode == "learned":
             WarmStartModel.load(MODEL_PATH).apply(wx)
+        if batched:  # many small islands: graph replay and autotuned launch shapes (the autotune
+            wx.set_graph(True)  # steps count as warm-up)
+            tuned["choice"] = wx.autotune(steps_per_candidate=2)
         return wx
 
     def timed(wx, steps: int, sample_clocks: bool):
@@ -295,6 +311,7 @@ def main():
     # ---- plain warm start, residual-terminated: the headline
     if snap is None and preroll:
         start_scene = scene_with_state(sc, w.state())
+        start_scene.world_ids = world_ids
     w.close()
     w = fresh_world("plain")
     for _ in range(args.warmup):
@@ -391,6 +408,7 @@ def main():
         "fixed_iterations": legs["fixed"],
         "plain_solver": legs["plain"]["solver"],
         "stage_ms": {k: v / args.steps for k, v in acc.items()},
+        "tuning": tuned.get("choice"),
         "model_gbs_step": step_bytes(n_dyn, nb - 40 * points, points, last["num_contact_constraints"]) /
                           (ms_per_step / 1e3) / 1e9,
         "preroll_s": preroll_s,

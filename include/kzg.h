@@ -183,6 +183,26 @@ kzg_status kzg_step(kzg_ctx* ctx, float dt, uint32_t nsteps);
 /* One step using the caller's broad-phase pairs, in order (2 packed BodyIDs per pair, host
  * memory).  With the reference's own pair list this reproduces the reference bit for bit. */
 kzg_status kzg_step_with_pairs(kzg_ctx* ctx, const uint32_t* packed_pairs, uint32_t num_pairs, float dt);
+/* Step kzg_step through a CUDA graph: one step is captured once (again after dt or any setting
+ * changes) and kzg_step's nsteps steps are launched back to back with one synchronisation at the
+ * end; stats then describe the last step, except that the stage times are 0 and step_ms is the
+ * mean over the replayed steps.  No counterpart in the reference. */
+kzg_status kzg_set_graph(kzg_ctx* ctx, int enabled);
+
+/* Launch shapes of the island work, all bit-identical in result: islands with at most
+ * small_island_constraints constraints (<= 128) get one warp for their schedule, islands with at
+ * most warp_island_bodies dynamic bodies (<= 384) one warp for their solve, larger ones a CTA.
+ * kzg_autotune steps the world steps_per_candidate steps with each of a small set of choices,
+ * keeps the fastest (by CUDA-event step time) and returns it; the world advances by all those
+ * steps, exactly as plain stepping would.  No counterpart in the reference. */
+typedef struct {
+    uint32_t small_island_constraints;
+    uint32_t warp_island_bodies;
+    float step_ms; /* out: mean step time of this choice during kzg_autotune */
+} kzg_tuning;
+kzg_status kzg_set_tuning(kzg_ctx* ctx, const kzg_tuning* t);
+kzg_status kzg_get_tuning(kzg_ctx* ctx, kzg_tuning* t);
+kzg_status kzg_autotune(kzg_ctx* ctx, float dt, uint32_t steps_per_candidate, kzg_tuning* best);
 
 /* ---- state access (Body getters/setters, Body.h:146-178) ------------------------------------ */
 /* 13 floats per body in slot order: position xyz, rotation xyzw, linear xyz, angular xyz. */

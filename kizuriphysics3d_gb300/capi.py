@@ -54,6 +54,10 @@ class KzgBodySoa(ctypes.Structure):
                                    "collision_mask", "world_id")]
 
 
+class KzgTuning(ctypes.Structure):
+    _fields_ = [("small_island_constraints", u32), ("warp_island_bodies", u32), ("step_ms", f32)]
+
+
 class KzgStats(ctypes.Structure):
     _fields_ = [(n, u32) for n in ("num_bodies", "num_broadphase_pairs", "num_contact_constraints",
                                    "num_contact_points", "num_islands", "num_batches", "max_velocity_levels",
@@ -119,6 +123,10 @@ def load(build_if_missing: bool = True):
     L.kzg_hull_build.argtypes = [vp, u32, u32, vp, P(u32), vp, P(u32), vp, P(u32), u32]
     L.kzg_mass_properties.argtypes = [P(KzgShapeDesc), vp, vp, vp, u32, f32, f32, P(f32), vp]
     L.kzg_state_hash_noalloc.argtypes = [vp, vp, u32, vp, P(ctypes.c_uint64), P(ctypes.c_char_p)]
+    L.kzg_set_graph.argtypes = [vp, ctypes.c_int]
+    L.kzg_set_tuning.argtypes = [vp, P(KzgTuning)]
+    L.kzg_get_tuning.argtypes = [vp, P(KzgTuning)]
+    L.kzg_autotune.argtypes = [vp, f32, u32, P(KzgTuning)]
     L.kzg_mlp_set_params.argtypes = [vp, vp, vp, vp]
     L.kzg_mlp_get_params.argtypes = [vp, vp, vp, vp]
     L.kzg_mlp_enable.argtypes = [vp, ctypes.c_int]

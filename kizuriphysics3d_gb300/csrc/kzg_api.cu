@@ -147,6 +147,7 @@ void free_all(Ctx* ctx) {
     if (ctx->hcnt) cudaFreeHost(ctx->hcnt);
     for (cudaEvent_t e : ctx->ev)
         if (e) cudaEventDestroy(e);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     mlp_free(*ctx);
 }
@@ -178,6 +179,7 @@ kzg_status finalize_bodies(kzg_ctx* k) {
     Ctx* ctx = &k->c;
     HostSide& h = k->h;
     if (!h.dirty) return KZG_OK;
+    ctx->graph_dirty = true;
     const uint32_t n = ctx->nbodies;
     std::vector<float> rad;
     for (uint32_t i = 0; i < n; ++i) {
@@ -299,6 +301,7 @@ kzg_status kzg_destroy(kzg_ctx* k) {
 const char* kzg_last_error(const kzg_ctx* k) { return k ? k->c.err.c_str() : g_create_error.c_str(); }
 
 kzg_status kzg_set_stream(kzg_ctx* k, void* stream) {
+    if (k) k->c.graph_dirty = true;
     if (check(k)) return KZG_ERR_INVALID;
     Ctx* ctx = &k->c;
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -319,6 +322,7 @@ kzg_status kzg_synchronize(kzg_ctx* k) {
 }
 
 kzg_status kzg_set_world_settings(kzg_ctx* k, const kzg_world_settings* s) {
+    if (k) k->c.graph_dirty = true;
     if (check(k) || !s) return KZG_ERR_INVALID;
     if (s->allow_sleeping) {
         k->c.err = "sleeping (WorldSettings::allowSleeping) is outside the accelerated path";
@@ -329,6 +333,7 @@ kzg_status kzg_set_world_settings(kzg_ctx* k, const kzg_world_settings* s) {
 }
 
 kzg_status kzg_set_solver_settings(kzg_ctx* k, const kzg_solver_settings* s) {
+    if (k) k->c.graph_dirty = true;
     if (check(k) || !s) return KZG_ERR_INVALID;
     if (s->schedule != KZG_SCHEDULE_REFERENCE) {
         k->c.err = "unknown solver schedule";
@@ -489,10 +494,68 @@ kzg_status kzg_step(kzg_ctx* k, float dt, uint32_t nsteps) {
     CK(cudaSetDevice(ctx->device));
     kzg_status s = finalize_bodies(k);
     if (s != KZG_OK) return s;
-    for (uint32_t i = 0; i < nsteps; ++i) {
-        s = step_canonical(*ctx, dt);
-        if (s != KZG_OK) return s;
+    if (nsteps == 0) return KZG_OK;
+    return step_canonical(*ctx, dt, nsteps);
+}
+
+kzg_status kzg_set_tuning(kzg_ctx* k, const kzg_tuning* t) {
+    if (check(k) || !t) return KZG_ERR_INVALID;
+    if (t->small_island_constraints == 0 || t->small_island_constraints > 128 || t->warp_island_bodies == 0 ||
+        t->warp_island_bodies > 384) {
+        k->c.err = "kzg_tuning: small_island_constraints in [1, 128], warp_island_bodies in [1, 384]";
+        return KZG_ERR_INVALID;
     }
+    k->c.tune = *t;
+    k->c.graph_dirty = true;
+    return KZG_OK;
+}
+
+kzg_status kzg_get_tuning(kzg_ctx* k, kzg_tuning* t) {
+    if (check(k) || !t) return KZG_ERR_INVALID;
+    *t = k->c.tune;
+    return KZG_OK;
+}
+
+kzg_status kzg_autotune(kzg_ctx* k, float dt, uint32_t steps_per_candidate, kzg_tuning* best) {
+    if (check(k) || !(dt > 0.0f) || steps_per_candidate == 0) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    CK(cudaSetDevice(ctx->device));
+    kzg_status s = finalize_bodies(k);
+    if (s != KZG_OK) return s;
+    const uint32_t small[3] = {32u, 64u, 128u}, warp[3] = {128u, 256u, 384u};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    kzg_tuning win{128u, 384u, 1e30f};
+    for (uint32_t a = 0; a < 3 && s == KZG_OK; ++a)
+        for (uint32_t b = 0; b < 3 && s == KZG_OK; ++b) {
+            kzg_tuning t{small[a], warp[b], 0.0f};
+            ctx->tune = t;
+            ctx->graph_dirty = true;
+            s = step_canonical(*ctx, dt, 1);  // first step of a choice: graph capture, not timed
+            if (s != KZG_OK) break;
+            cudaEventRecord(e0, ctx->stream);
+            s = step_canonical(*ctx, dt, steps_per_candidate);
+            cudaEventRecord(e1, ctx->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            t.step_ms = ms / (float)steps_per_candidate;
+            if (t.step_ms < win.step_ms) win = t;
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != KZG_OK) return s;
+    ctx->tune = win;
+    ctx->graph_dirty = true;
+    if (best) *best = win;
+    return KZG_OK;
+}
+
+kzg_status kzg_set_graph(kzg_ctx* k, int enabled) {
+    if (check(k)) return KZG_ERR_INVALID;
+    k->c.use_graph = enabled != 0;
+    k->c.graph_dirty = true;
     return KZG_OK;
 }
 
@@ -676,6 +739,7 @@ kzg_status kzg_download_constraints(kzg_ctx* k, uint32_t* hdr, float* fr, float*
 }
 
 kzg_status kzg_mlp_set_params(kzg_ctx* k, const float* theta, const float* mean, const float* stdv) {
+    if (k) k->c.graph_dirty = true;
     if (check(k) || !theta || !mean || !stdv) return KZG_ERR_INVALID;
     return mlp_set_params(k->c, theta, mean, stdv);
 }
@@ -686,6 +750,7 @@ kzg_status kzg_mlp_get_params(kzg_ctx* k, float* theta, float* mean, float* stdv
 }
 
 kzg_status kzg_mlp_enable(kzg_ctx* k, int enabled) {
+    if (k) k->c.graph_dirty = true;
     if (check(k)) return KZG_ERR_INVALID;
     if (enabled && !k->c.mlp.have) {
         k->c.err = "kzg_mlp_enable: set the model parameters first";
@@ -696,6 +761,7 @@ kzg_status kzg_mlp_enable(kzg_ctx* k, int enabled) {
 }
 
 kzg_status kzg_mlp_log_begin(kzg_ctx* k, uint32_t capacity) {
+    if (k) k->c.graph_dirty = true;
     if (check(k)) return KZG_ERR_INVALID;
     return mlp_log_begin(k->c, capacity);
 }

@@ -58,7 +58,8 @@ struct Counters {  // device-side counters, copied back after each stage that si
     uint32_t pt_iters;   // sum of batched points x iterations
     uint32_t res_bits;   // largest final residual (float bits, >= 0)
     uint32_t nmiss;      // contact points without a cached warm start (learned warm start / logging)
-    uint32_t cache_entries;
+    uint32_t cache_entries;  // persists across steps
+    uint32_t frame;          // step counter, advanced on the device by k_begin_step
 };
 
 // Learned warm start (kzg_mlp.cu): model, optimiser state, training log and dataset.
@@ -173,6 +174,15 @@ struct Ctx {
     kzg_stats stats{};
     uint32_t frame = 0;
     uint32_t launches = 0;
+
+    // launch-shape choices (kzg_set_tuning / kzg_autotune); every choice gives identical results
+    kzg_tuning tune{128u, 384u, 0.0f};
+
+    // CUDA graph of one canonical step (kzg_set_graph); recaptured when dt or the configuration changes
+    bool use_graph = false, graph_dirty = true, capturing = false;
+    float graph_dt = 0.0f;
+    cudaGraphExec_t graph_exec = nullptr;
+    uint32_t graph_launches = 0;
 };
 
 }  // namespace kzg

@@ -708,7 +708,7 @@ static StepView step_view(Ctx& ctx, float dt) {
 uint32_t mlp_after_prepare(Ctx& ctx, float dt) {
     MlpState& M = ctx.mlp;
     uint32_t n = 0;
-    const uint32_t rows = 4u * ctx.hcnt->ncons;
+    const uint32_t rows = 4u * ctx.cfg.max_pairs;  // grids by capacity: kernels stop at the device count
     if (M.logging) {
         k_mlp_log_features<<<(rows + 255) / 256, 256, 0, ctx.stream>>>(step_view(ctx, dt), M.log, M.log_n, M.log_cap);
         ++n;
@@ -724,7 +724,7 @@ uint32_t mlp_after_prepare(Ctx& ctx, float dt) {
 uint32_t mlp_after_solve(Ctx& ctx, float dt) {
     MlpState& M = ctx.mlp;
     if (!M.logging) return 0;
-    const uint32_t rows = 4u * ctx.hcnt->ncons;
+    const uint32_t rows = 4u * ctx.cfg.max_pairs;
     k_mlp_log_targets<<<(rows + 255) / 256, 256, 0, ctx.stream>>>(step_view(ctx, dt), M.log, M.log_n, M.log_cap);
     k_mlp_log_advance<<<1, 1, 0, ctx.stream>>>(ctx.dcnt, M.log_n, M.log_cap);
     return 2;

@@ -38,7 +38,6 @@ struct SchedBufs {
     const float4* bias;
     const float* inv_mass;
     const uint8_t* is_large;   // planes and other grid-bypassing bodies: hub candidates
-    uint32_t frame;
     uint4* brec;               // batch records (64 B): {nx, hub0 nx, hub1 nx, count}, 8 bodies, 4 rows
     uint32_t *body_stamp, *body_loc;
     uint32_t *isl_bodies;      // per island dynamic bodies, region 2*s0
@@ -50,6 +49,8 @@ struct SchedBufs {
     uint32_t *lvl_count;
     uint32_t *wl_list, *vl_list, *bl_list, *wl_off, *vl_off, *bl_off, *meta;
     uint32_t *small_list, *large_list;
+    uint32_t small_cons;   // islands with at most this many constraints: warp schedule (<= kSchedSmallCons)
+    uint32_t warp_bodies;  // islands with at most this many dynamic bodies: warp solve (<= kWarpBodies)
 };
 
 struct SchedShared {  // per island scratch living in shared memory
@@ -299,6 +300,44 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
     const unsigned full = 0xffffffffu, lt = (1u << lane) - 1u;
     const FfTable T = ff_table_of(smem);
     uint32_t ns = 0, nbt = 0, nl0 = 0, nl1 = 0, head = 0, head0 = 0, head1 = 0;
+    // The 32 open slots from `head`, held in registers (one per lane) while consecutive constraints
+    // without a hub are placed into them; written back before any other access to the table.
+    bool win = false, wdirty = false;
+    uint32_t wcnt = 4u, ww0 = 0, ww1 = 0, ww2 = 0, wbid = 0;
+    auto win_flush = [&]() {
+        if (win && wdirty && head + lane < ns) {
+            T.cnt[head + lane] = (uint8_t)wcnt;
+            T.bod0[head + lane] = ww0;
+            T.bod1[head + lane] = ww1;
+            T.bod2[head + lane] = ww2;
+        }
+        win = false;
+        wdirty = false;
+        __syncwarp();
+    };
+    auto win_load = [&]() {  // skip the dead prefix for good, then hold the next 32 slots
+        for (;;) {
+            const uint32_t i = head + lane;
+            wcnt = 4u;
+            if (i < ns) {
+                wcnt = T.cnt[i];
+                ww0 = T.bod0[i];
+                ww1 = T.bod1[i];
+                ww2 = T.bod2[i];
+                wbid = T.bid[i];
+            }
+            const unsigned livem = __ballot_sync(full, (wcnt & 7u) < 4u);
+            if (livem & 1u) break;
+            if (!livem) {
+                if (head + 32 >= ns) break;
+                head += 32;
+            } else {
+                head += __ffs(livem) - 1;
+            }
+        }
+        win = true;
+        wdirty = false;
+    };
     // pipeline: id of the constraint two windows ahead, fields of the next window
     auto load_id = [&](uint32_t w0) -> uint32_t { return w0 + lane < s1 ? S.isl_con[w0 + lane] : kNone; };
     uint32_t nx_c = load_id(s0), nx_bits = 1u, nx_a = 0, nx_b = 0, nx_np = 0, nx_la = kNone, nx_lb = kNone;
@@ -342,6 +381,35 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
             const uint32_t c = __shfl_sync(full, mc, k), xx = __shfl_sync(full, dx, k);
             const uint32_t np = md & 15u, x0 = xx & 0xFFFFu, x1 = xx >> 16;
             const int hub = (int)((md >> 4) & 3u) - 1;
+            if (hub < 0) {  // ---- fast path: the first np slots of the held window that fit
+                if (!win) win_load();
+                const bool fits = (wcnt & 7u) < 4u && !(ff_holds(ww0, x0) || ff_holds(ww1, x0) || ff_holds(ww2, x0) ||
+                                                       ff_holds(ww0, x1) || ff_holds(ww1, x1) || ff_holds(ww2, x1));
+                const unsigned okm = __ballot_sync(full, fits);
+                if ((uint32_t)__popc(okm) >= np) {
+                    const uint32_t rank = __popc(okm & lt);
+                    if (fits && rank < np) {
+                        const uint32_t kk = wcnt & 7u;
+                        uint32_t nc = wcnt >> 5;
+                        if (kk + 1 < 4u) {  // a full batch's codes are never read again
+                            const uint32_t add[2] = {x0, x1};
+                            for (int q = 0; q < 2; ++q, ++nc) {
+                                const uint32_t sh = 16u * (nc & 1u), msk = ~(0xFFFFu << sh), v = add[q] << sh;
+                                if (nc < 2u) ww0 = (ww0 & msk) | v;
+                                else if (nc < 4u) ww1 = (ww1 & msk) | v;
+                                else ww2 = (ww2 & msk) | v;
+                            }
+                        }
+                        wcnt = (kk + 1) | (wcnt & (kFfH0 | kFfH1)) | (nc << 5);
+                        wdirty = true;
+                        uint32_t* r = rec(S, rb + wbid);
+                        r[12 + kk] = 4u * c + rank;
+                        r[3] = kk + 1;
+                    }
+                    continue;
+                }
+            }
+            win_flush();  // the table is read and written directly below
             const uint32_t hflag = hub == 0 ? kFfH0 : (hub == 1 ? kFfH1 : 0u);
             const uint16_t* L = hub == 0 ? T.list0 : T.list1;
             const uint32_t nL = hub < 0 ? ns : (hub == 0 ? nl0 : nl1);
@@ -419,6 +487,7 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
             __syncwarp();
         }
     }
+    win_flush();
     return nbt;
 }
 
@@ -445,7 +514,7 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
         for (int q = 0; q < 2; ++q) {
             const uint32_t x = xs[q];
             if (bits & (2u << q)) {
-                if (atomicExch(&S.body_stamp[x], S.frame) != S.frame) {
+                if (atomicExch(&S.body_stamp[x], cnt->frame) != cnt->frame) {
                     const uint32_t l = atomicAdd(&sh->nloc, 1u);
                     S.body_loc[x] = l;
                     S.isl_bodies[boff + l] = x;
@@ -634,7 +703,7 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
         S.meta[4 * isl + 1] = nv;
         S.meta[4 * isl + 2] = nb;
         S.meta[4 * isl + 3] = nloc;
-        if (nloc <= kWarpBodies) S.small_list[atomicAdd(&cnt->nsmall, 1u)] = isl;
+        if (nloc <= S.warp_bodies) S.small_list[atomicAdd(&cnt->nsmall, 1u)] = isl;
         else S.large_list[atomicAdd(&cnt->nlarge, 1u)] = isl;
         atomicAdd(&cnt->batches, nbt);
         atomicMax(&cnt->max_vlev, nv);
@@ -658,7 +727,7 @@ __global__ void __launch_bounds__(128) k_schedule_warp(SchedBufs S, Counters* cn
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t n = cnt->nislands;
     for (uint32_t isl = blockIdx.x * 4 + warp; isl < n; isl += gridDim.x * 4) {
-        if (S.isl_start[isl + 1] - S.isl_start[isl] > kSchedSmallCons) continue;
+        if (S.isl_start[isl + 1] - S.isl_start[isl] > S.small_cons) continue;
         schedule_island(S, cnt, isl, lane, 32u, &sh[warp], tmp[warp], last[warp], kSchedWarpBodies, false,
                         SchedWarpSync{});
     }
@@ -672,7 +741,7 @@ __global__ void __launch_bounds__(256) k_schedule_cta(SchedBufs S, Counters* cnt
     __shared__ uint32_t tmp[33];
     const uint32_t n = cnt->nislands;
     for (uint32_t isl = blockIdx.x; isl < n; isl += gridDim.x) {
-        if (S.isl_start[isl + 1] - S.isl_start[isl] <= kSchedSmallCons) continue;
+        if (S.isl_start[isl + 1] - S.isl_start[isl] <= S.small_cons) continue;
         schedule_island(S, cnt, isl, threadIdx.x, blockDim.x, &sh, tmp, last_sm, kSchedCtaBodies, true, SchedCtaSync{});
     }
 }

@@ -11,7 +11,11 @@
 // the level-synchronous solve applies every body's updates in the reference's order, bit for bit.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "kzg_schedule.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace kzg {
 
@@ -29,6 +33,8 @@ struct SolveBufs {
     int vel_bias;
     float res_tol;     // > 0: residual-terminated velocity iterations
     uint32_t res_cap;  // their cap
+    uint4* vrec;       // big islands: per velocity item {row, A, B, dynamic A | dynamic B << 1} (reuses
+                       // the batch-record buffer, free once the schedule is built)
 };
 
 // Velocity storage of one island: staged in shared memory (local index) or read/written in place
@@ -53,10 +59,47 @@ struct VelView {
         v[k] = F4(l, 0.0f);
         w[k] = F4(a, 0.0f);
     }
+    // pseudo velocities: zero for bodies that are not dynamic
+    __device__ __forceinline__ Vec3 plin(uint32_t loc, uint32_t body) const {
+        return loc == kNone ? Vec3() : V3(v[shared ? loc : body]);
+    }
+    __device__ __forceinline__ Vec3 pang(uint32_t loc, uint32_t body) const {
+        return loc == kNone ? Vec3() : V3(w[shared ? loc : body]);
+    }
+};
+
+// Velocity storage of a giant island spread over the shared memory of a thread-block cluster:
+// local body l lives in CTA l % kClusterCtas, slot l / kClusterCtas, read and written through
+// distributed shared memory.
+constexpr uint32_t kClusterCtas = 8;
+struct ClusterView {
+    float4* v;  // this CTA's arrays; the same offsets in every CTA of the cluster
+    float4* w;
+    const float4* glv;
+    const float4* gav;
+    __device__ __forceinline__ float4* rv(uint32_t loc) const {
+        return cg::this_cluster().map_shared_rank(v, loc % kClusterCtas) + loc / kClusterCtas;
+    }
+    __device__ __forceinline__ float4* rw(uint32_t loc) const {
+        return cg::this_cluster().map_shared_rank(w, loc % kClusterCtas) + loc / kClusterCtas;
+    }
+    __device__ __forceinline__ Vec3 lin(uint32_t loc, uint32_t body) const {
+        return loc == kNone ? V3(__ldg(&glv[body])) : V3(*rv(loc));
+    }
+    __device__ __forceinline__ Vec3 ang(uint32_t loc, uint32_t body) const {
+        return loc == kNone ? V3(__ldg(&gav[body])) : V3(*rw(loc));
+    }
+    __device__ __forceinline__ void put(uint32_t loc, uint32_t, const Vec3& l, const Vec3& a) const {
+        *rv(loc) = F4(l, 0.0f);
+        *rw(loc) = F4(a, 0.0f);
+    }
+    __device__ __forceinline__ Vec3 plin(uint32_t loc, uint32_t) const { return loc == kNone ? Vec3() : V3(*rv(loc)); }
+    __device__ __forceinline__ Vec3 pang(uint32_t loc, uint32_t) const { return loc == kNone ? Vec3() : V3(*rw(loc)); }
 };
 
 // WarmStart for one point (ContactSolver.cpp:117-132 + ApplyImpulsePair :32-43).
-__device__ __forceinline__ void warm_point(const SolveBufs& S, const VelView& V, uint32_t row) {
+template <typename View>
+__device__ __forceinline__ void warm_point(const SolveBufs& S, const View& V, uint32_t row) {
     const uint32_t c = row >> 2;
     const uint32_t A = S.con_a[c], B = S.con_b[c], la = S.con_la[c], lb = S.con_lb[c];
     const float4 im = S.r.imp[row];
@@ -76,9 +119,9 @@ __device__ __forceinline__ void warm_point(const SolveBufs& S, const VelView& V,
 // velocity recomputed before each axis), then normal; _mm_{add,sub,mul,min,max}_ps semantics.
 // Returns the point's share of the island residual: (sum over its rows of |dImpulse|,
 // (|n| + |t1|) + |t2| of its accumulated impulses).
-__device__ __forceinline__ float2 velocity_point(const SolveBufs& S, const VelView& V, uint32_t row) {
-    const uint32_t c = row >> 2;
-    const uint32_t A = S.con_a[c], B = S.con_b[c], la = S.con_la[c], lb = S.con_lb[c];
+template <typename View>
+__device__ __forceinline__ float2 velocity_point_ab(const SolveBufs& S, const View& V, uint32_t row, uint32_t A,
+                                                   uint32_t B, uint32_t la, uint32_t lb) {
     const Vec3 rA = V3(S.r.rAr[row]), rB = V3(S.r.rBr[row]);
     const float4 n4 = S.r.n[row], t14 = S.r.t1[row], t24 = S.r.t2[row], m4 = S.r.mass[row];
     const float4 im = S.r.imp[row];
@@ -128,6 +171,12 @@ __device__ __forceinline__ float2 velocity_point(const SolveBufs& S, const VelVi
     return make_float2(dsum, (fabsf(nacc) + fabsf(t1acc)) + fabsf(t2acc));
 }
 
+template <typename View>
+__device__ __forceinline__ float2 velocity_point(const SolveBufs& S, const View& V, uint32_t row) {
+    const uint32_t c = row >> 2;
+    return velocity_point_ab(S, V, row, S.con_a[c], S.con_b[c], S.con_la[c], S.con_lb[c]);
+}
+
 // Fixed-point (2^-20 N s) magnitude for the residual sums: integer sums are exact and independent
 // of the order of the additions, so the stopping iteration does not depend on the thread count.
 __device__ __forceinline__ unsigned long long res_fixed(float x) {
@@ -135,17 +184,16 @@ __device__ __forceinline__ unsigned long long res_fixed(float x) {
 }
 
 // SolveBiasConstraint for one point (ContactSolver.cpp:265-289); V holds pseudo velocities.
-__device__ __forceinline__ void bias_point(const SolveBufs& S, const VelView& V, uint32_t row) {
+template <typename View>
+__device__ __forceinline__ void bias_point(const SolveBufs& S, const View& V, uint32_t row) {
     const uint32_t c = row >> 2;
     const uint32_t A = S.con_a[c], B = S.con_b[c], la = S.con_la[c], lb = S.con_lb[c];
     const Vec3 rA = V3(S.r.rAr[row]), rB = V3(S.r.rBr[row]);
     const Vec3 n = V3(S.r.n[row]);
     const float nm = S.r.mass[row].x, pbias = S.r.bias[row].y;
     float4 im = S.r.imp[row];
-    const Vec3 pvA = la != kNone ? V3(V.v[V.shared ? la : A]) : Vec3();
-    const Vec3 pwA = la != kNone ? V3(V.w[V.shared ? la : A]) : Vec3();
-    const Vec3 pvB = lb != kNone ? V3(V.v[V.shared ? lb : B]) : Vec3();
-    const Vec3 pwB = lb != kNone ? V3(V.w[V.shared ? lb : B]) : Vec3();
+    const Vec3 pvA = V.plin(la, A), pwA = V.pang(la, A);
+    const Vec3 pvB = V.plin(lb, B), pwB = V.pang(lb, B);
     const Vec3 vr = (pvA + pwA.cross(rA)) - (pvB + pwB.cross(rB));
     float lambda = -nm * (vr.dot(n) - pbias);
     const float ni = rmax(im.w + lambda, 0.0f);
@@ -161,8 +209,8 @@ __device__ __forceinline__ void bias_point(const SolveBufs& S, const VelView& V,
 // the fixed count, or - with a residual tolerance - until the island's residual, the relative
 // impulse change sum|dImpulse| / sum|impulse| of an iteration (reduced by sync.sum2), is within
 // it, at most res_cap times.
-template <typename Sync>
-__device__ __forceinline__ void solve_velocity(const SolveBufs& S, uint32_t isl, const VelView& V, uint32_t tid,
+template <typename Sync, typename View>
+__device__ __forceinline__ void solve_velocity(const SolveBufs& S, uint32_t isl, const View& V, uint32_t tid,
                                                uint32_t nthreads, Sync sync, Counters* cnt) {
     const uint32_t base = 4u * S.isl_start[isl];
     const uint32_t loff = base + isl;
@@ -202,8 +250,8 @@ __device__ __forceinline__ void solve_velocity(const SolveBufs& S, uint32_t isl,
     }
 }
 
-template <typename Sync>
-__device__ __forceinline__ void solve_bias(const SolveBufs& S, uint32_t isl, const VelView& P, uint32_t tid,
+template <typename Sync, typename View>
+__device__ __forceinline__ void solve_bias(const SolveBufs& S, uint32_t isl, const View& P, uint32_t tid,
                                            uint32_t nthreads, Sync sync) {
     if (S.vel_bias) return;
     const uint32_t base = 4u * S.isl_start[isl];
@@ -316,18 +364,179 @@ __global__ void __launch_bounds__(kCtaThreads) k_solve_cta(SolveBufs S, Counters
 
 // Islands too large for shared memory: one 1024-thread CTA each, velocities updated in place
 // (L2-resident).  A level of a settled pile holds ~1,000 points, one per thread.
-constexpr uint32_t kBigThreads = 1024;
-__global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
+constexpr uint32_t kBigThreads = 768;
+constexpr uint32_t kBigOffs = 8192;  // velocity level offsets staged in shared memory
+
+// Warm start + velocity sweeps of a big island.  Each velocity item is one 16-byte record
+// {row, A, B, dynamic flags}, and every thread loads its record of the next level before it solves
+// the current one, so after a barrier only the row and body loads stand between it and its math.
+__device__ void solve_velocity_big(const SolveBufs& S, uint32_t isl, uint32_t* soff, unsigned long long* red,
+                                   Counters* cnt) {
+    const uint32_t tid = threadIdx.x, nthreads = blockDim.x;
+    const uint32_t base = 4u * S.isl_start[isl], loff = base + isl;
+    const uint32_t nw = S.meta[4 * isl], nv = S.meta[4 * isl + 1];
+    const VelView V{S.b.lv, S.b.av, S.b.lv, S.b.av, false};
+    const CtaSync sync{red};
+    const uint32_t total = S.vl_off[loff + nv];
+    for (uint32_t k = tid; k < total; k += nthreads) {
+        const uint32_t row = S.vl_list[base + k], c = row >> 2;
+        S.vrec[base + k] = make_uint4(row, S.con_a[c], S.con_b[c],
+                                      (S.con_la[c] != kNone ? 1u : 0u) | (S.con_lb[c] != kNone ? 2u : 0u));
+    }
+    const bool staged = nv <= kBigOffs;
+    if (staged)
+        for (uint32_t l = tid; l <= nv; l += nthreads) soff[l] = S.vl_off[loff + l];
+    sync.reset(tid);
+    for (uint32_t l = 0; l < nw; ++l) {
+        const uint32_t e = S.wl_off[loff + l + 1];
+        for (uint32_t k = S.wl_off[loff + l] + tid; k < e; k += nthreads) warm_point(S, V, S.wl_list[base + k]);
+        sync();
+    }
+    auto off = [&](uint32_t l) -> uint32_t { return staged ? soff[l] : S.vl_off[loff + l]; };
+    auto item = [&](const uint4& r) -> float2 {
+        return velocity_point_ab(S, V, r.x, r.y, r.z, (r.w & 1u) ? 0u : kNone, (r.w & 2u) ? 0u : kNone);
+    };
+    const bool residual = S.res_tol > 0.0f;
+    const uint32_t iters = residual ? S.res_cap : S.vel_iters;
+    uint32_t used = 0;
+    float res = 0.0f;
+    uint4 cur = make_uint4(kNone, 0u, 0u, 0u);
+    if (iters && nv && off(0) + tid < off(1)) cur = S.vrec[base + off(0) + tid];
+    for (uint32_t it = 0; it < iters; ++it) {
+        unsigned long long sd = 0, sl = 0;
+        for (uint32_t l = 0; l < nv; ++l) {
+            const uint32_t lo = off(l), hi = off(l + 1);
+            const uint32_t ln = l + 1 < nv ? l + 1 : 0u;  // after the last level: the next iteration's first
+            const uint32_t nlo = off(ln), nhi = off(ln + 1);
+            uint4 nxt = make_uint4(kNone, 0u, 0u, 0u);
+            if (nlo + tid < nhi) nxt = S.vrec[base + nlo + tid];
+            if (cur.x != kNone) {
+                const float2 q = item(cur);
+                sd += res_fixed(q.x);
+                sl += res_fixed(q.y);
+            }
+            for (uint32_t k = lo + tid + nthreads; k < hi; k += nthreads) {
+                const float2 q = item(S.vrec[base + k]);
+                sd += res_fixed(q.x);
+                sl += res_fixed(q.y);
+            }
+            sync();
+            cur = nxt;
+        }
+        used = it + 1;
+        if (residual || used == iters) {
+            sync.sum2(sd, sl, it);
+            res = sl ? (float)((double)sd / (double)sl) : (sd ? 1.0f : 0.0f);
+            if (residual && (double)sd <= (double)S.res_tol * (double)sl) break;
+        }
+    }
+    if (tid == 0) {
+        atomicMax(&cnt->max_iters, used);
+        atomicAdd(&cnt->pt_iters, total * used);
+        atomicMax(&cnt->res_bits, __float_as_uint(res));
+    }
+}
+
+// cluster_max: islands up to this many bodies are solved by k_solve_cluster (0: none).
+__global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, Counters* cnt, uint32_t smem_bodies,
+                                                              uint32_t cluster_max) {
     __shared__ unsigned long long red[6];
+    __shared__ uint32_t soff[kBigOffs + 1];
     const uint32_t n = cnt->nlarge;
     for (uint32_t idx = blockIdx.x; idx < n; idx += gridDim.x) {
         const uint32_t isl = S.large_list[idx];
-        if (S.meta[4 * isl + 3] <= smem_bodies) continue;
-        const VelView V{S.b.lv, S.b.av, S.b.lv, S.b.av, false};
+        if (S.meta[4 * isl + 3] <= smem_bodies || S.meta[4 * isl + 3] <= cluster_max) continue;
         const VelView P{S.b.plv, S.b.pav, S.b.lv, S.b.av, false};
-        solve_velocity(S, isl, V, threadIdx.x, blockDim.x, CtaSync{red}, cnt);
+        solve_velocity_big(S, isl, soff, red, cnt);
         solve_bias(S, isl, P, threadIdx.x, blockDim.x, CtaSync{red});
         __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Giant islands on a thread-block cluster
+// ---------------------------------------------------------------------------------------------
+// A settled pile is one island of ~20k bodies whose dependency levels hold ~1,000 points each.
+// One CTA is bound by its own L2 bandwidth and latency on every level; here kClusterCtas CTAs on
+// as many SMs share each level, the island's velocities live in their distributed shared memory
+// (ClusterView) and a hardware cluster barrier separates the levels.
+constexpr uint32_t kClusterThreads = 512;
+constexpr uint32_t kClusterSlots = 6144;  // bodies per CTA: 2 x 16 B x 6144 = 192 KB
+
+// Level barrier and residual sums over the whole cluster: every CTA sums its warps into its own
+// rotating words (as CtaSync does), and after the barrier every thread adds the kClusterCtas partial
+// sums it reads through distributed shared memory.
+struct ClusterSync {
+    unsigned long long* red;  // 3 x 2 words per CTA
+    __device__ __forceinline__ void operator()() const { cg::this_cluster().sync(); }
+    __device__ __forceinline__ void reset(uint32_t) const {
+        if (threadIdx.x < 6) red[threadIdx.x] = 0ull;
+        cg::this_cluster().sync();
+    }
+    __device__ __forceinline__ void sum2(unsigned long long& a, unsigned long long& b, uint32_t it) const {
+        cg::cluster_group cl = cg::this_cluster();
+        a = warp_sum(a);
+        b = warp_sum(b);
+        unsigned long long* r = red + 2 * (it % 3);
+        if ((threadIdx.x & 31u) == 0) {
+            atomicAdd(&r[0], a);
+            atomicAdd(&r[1], b);
+        }
+        if (threadIdx.x == 0) {
+            unsigned long long* nx = red + 2 * ((it + 1) % 3);
+            nx[0] = 0ull;
+            nx[1] = 0ull;
+        }
+        cl.sync();
+        a = 0ull;
+        b = 0ull;
+        for (uint32_t k = 0; k < kClusterCtas; ++k) {
+            const unsigned long long* rk = cl.map_shared_rank(r, k);
+            a += rk[0];
+            b += rk[1];
+        }
+    }
+};
+
+// Islands with more than smem_bodies and at most kClusterCtas * kClusterSlots dynamic bodies.
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads, 1)
+    k_solve_cluster(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
+    extern __shared__ float4 smem[];
+    __shared__ unsigned long long red[6];
+    cg::cluster_group cl = cg::this_cluster();
+    float4* sv = smem;
+    float4* sw = smem + kClusterSlots;
+    const uint32_t rank = cl.block_rank(), tid = threadIdx.x;
+    const uint32_t gtid = rank * blockDim.x + tid, gthreads = kClusterCtas * blockDim.x;
+    const uint32_t ncl = gridDim.x / kClusterCtas, cid = blockIdx.x / kClusterCtas;
+    const uint32_t n = cnt->nlarge;
+    const ClusterView V{sv, sw, S.b.lv, S.b.av};
+    const ClusterSync sync{red};
+    for (uint32_t idx = cid; idx < n; idx += ncl) {  // the same islands in every CTA of a cluster
+        const uint32_t isl = S.large_list[idx];
+        const uint32_t nloc = S.meta[4 * isl + 3];
+        if (nloc <= smem_bodies || nloc > kClusterCtas * kClusterSlots) continue;
+        const uint32_t* bodies = S.isl_bodies + 2u * S.isl_start[isl];
+        for (uint32_t l = rank + kClusterCtas * tid; l < nloc; l += gthreads) {
+            sv[l / kClusterCtas] = S.b.lv[bodies[l]];
+            sw[l / kClusterCtas] = S.b.av[bodies[l]];
+        }
+        cl.sync();
+        solve_velocity(S, isl, V, gtid, gthreads, sync, cnt);
+        for (uint32_t l = rank + kClusterCtas * tid; l < nloc; l += gthreads) {
+            S.b.lv[bodies[l]] = sv[l / kClusterCtas];
+            S.b.av[bodies[l]] = sw[l / kClusterCtas];
+            sv[l / kClusterCtas] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // pseudo velocities start at zero
+            sw[l / kClusterCtas] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        cl.sync();
+        solve_bias(S, isl, V, gtid, gthreads, sync);
+        if (!S.vel_bias)
+            for (uint32_t l = rank + kClusterCtas * tid; l < nloc; l += gthreads) {
+                S.b.plv[bodies[l]] = sv[l / kClusterCtas];
+                S.b.pav[bodies[l]] = sw[l / kClusterCtas];
+            }
+        cl.sync();
     }
 }
 

@@ -134,6 +134,26 @@ __global__ void k_find_pairs(DeviceBodies b, uint32_t n, const unsigned long lon
             }
 }
 
+// Per-step counters to zero, the step counter advanced (the first kernel of every step).
+__global__ void k_begin_step(Counters* cnt) {
+    const uint32_t nz = (uint32_t)(offsetof(Counters, cache_entries) / sizeof(uint32_t));
+    uint32_t* w = reinterpret_cast<uint32_t*>(cnt);
+    for (uint32_t i = threadIdx.x; i < nz; i += blockDim.x) w[i] = 0u;
+    if (threadIdx.x == 0) ++cnt->frame;
+}
+
+// A pair count past the capacity (flagged KZG_DEVERR_PAIRS by emit_pair) is clamped, so the rest of
+// the step runs on the pairs that were stored and the overflow is reported after the step.
+__global__ void k_clamp_pairs(Counters* cnt, uint32_t cap) {
+    if (cnt->npairs > cap) cnt->npairs = cap;
+}
+
+// Pair keys past the pair count (up to cap) sort last.
+__global__ void k_pad_keys(unsigned long long* keys, const Counters* cnt, uint32_t cap) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cnt->npairs && i < cap) keys[i] = ~0ull;
+}
+
 __global__ void k_unpack_pairs(const unsigned long long* __restrict__ keys, const Counters* cnt, uint2* pairs) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cnt->npairs) return;
@@ -441,10 +461,19 @@ __global__ void k_uf_union(const Counters* cnt, const uint32_t* __restrict__ con
         bb = old;
     }
 }
+// Island of every constraint; slots past the constraint count (up to cap) get a key above every
+// body index so that a capacity-sized sort leaves them at the end.
 __global__ void k_island_keys(const Counters* cnt, const uint32_t* __restrict__ con_a, const uint32_t* __restrict__ con_b,
-                              const uint32_t* __restrict__ con_bits, uint32_t* uf, uint32_t* key, uint32_t* val) {
+                              const uint32_t* __restrict__ con_bits, uint32_t* uf, uint32_t* key, uint32_t* val,
+                              uint32_t cap, uint32_t pad) {
     uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= cnt->ncons) return;
+    if (c >= cnt->ncons) {
+        if (c < cap) {
+            key[c] = pad;
+            val[c] = c;
+        }
+        return;
+    }
     uint32_t d = (con_bits[c] & 2u) ? con_a[c] : con_b[c];  // islandOf(A), else islandOf(B)
     key[c] = uf_find(uf, d);
     val[c] = c;
@@ -573,6 +602,9 @@ size_t cub_temp_bytes(uint32_t max_items) {
     return std::max(std::max(a, b), std::max(c, d));
 }
 
+// Whether this device can hold one k_solve_cluster cluster (checked once in configure_kernels).
+static bool g_cluster_ok = false;
+
 cudaError_t configure_kernels() {
     cudaError_t e = cudaFuncSetAttribute(k_solve_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(2 * kCtaBodiesMax * sizeof(float4)));
@@ -583,6 +615,27 @@ cudaError_t configure_kernels() {
     e = cudaFuncSetAttribute(k_schedule_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(3 * kSchedCtaBodies * sizeof(uint32_t)));
     if (e != cudaSuccess) return e;
+    // the cluster solve needs kClusterCtas co-resident CTAs with 192 KB of shared memory each
+    e = cudaFuncSetAttribute(k_solve_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(2 * kClusterSlots * sizeof(float4)));
+    if (e != cudaSuccess) return e;
+    {
+        cudaLaunchConfig_t lc = {};
+        lc.gridDim = dim3(kClusterCtas * 16u);
+        lc.blockDim = dim3(kClusterThreads);
+        lc.dynamicSmemBytes = 2 * kClusterSlots * sizeof(float4);
+        cudaLaunchAttribute at;
+        at.id = cudaLaunchAttributeClusterDimension;
+        at.val.clusterDim.x = kClusterCtas;
+        at.val.clusterDim.y = 1;
+        at.val.clusterDim.z = 1;
+        lc.attrs = &at;
+        lc.numAttrs = 1;
+        int nclusters = 0;
+        g_cluster_ok = cudaOccupancyMaxActiveClusters(&nclusters, (void*)k_solve_cluster, &lc) == cudaSuccess &&
+                       nclusters > 0;
+        cudaGetLastError();
+    }
     return mlp_configure_kernels();
 }
 
@@ -592,106 +645,92 @@ static int bits_for(uint32_t v) {
     return b;
 }
 
-// Runs one step after the pair list is in ctx.pairs and hcnt->npairs is valid on the device.
-static kzg_status step_after_pairs(Ctx& ctx, float dt) {
+// Stage boundary event (not inside a graph capture: events recorded by graph nodes cannot be
+// timed, so a replayed graph is timed as a whole).
+static cudaError_t mark(Ctx& ctx, int i) {
+    return ctx.capturing ? cudaSuccess : cudaEventRecord(ctx.ev[i], ctx.stream);
+}
+
+// Issues one step after the pair list is in ctx.pairs and the pair count is on the device.
+// No host synchronisation: every count lives on the device, grids and sorts are sized by the
+// context's capacities and kernels stop at the device counts, so the sequence can be captured in
+// a CUDA graph.
+static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     cudaStream_t st = ctx.stream;
     const uint32_t nb = ctx.nbodies;
-    const uint32_t np = ctx.hcnt->npairs;
+    const uint32_t P = ctx.cfg.max_pairs, R = 4u * P;
     ShapeTables T{ctx.shapes, ctx.hull_verts, ctx.face_sizes, ctx.face_idx};
-    KZG_CK(cudaEventRecord(ctx.ev[1], st));
-    if (np > 0) {
-        k_narrow<<<blocks_for(np, 128), 128, 0, st>>>(T, ctx.b, ctx.pairs, ctx.dcnt, ctx.m_count, ctx.m_data,
-                                                      ctx.m_key, ctx.epa_list);
-        const unsigned ge = std::min<unsigned>(blocks_for(np, kEpaWarps), 152u * 8u);
-        k_narrow_epa<<<ge, kEpaWarps * 32, kEpaWarps * sizeof(EpaWarpSmem), st>>>(
-            T, ctx.b, ctx.pairs, ctx.dcnt, ctx.epa_list, ctx.m_count, ctx.m_data, ctx.m_key, &ctx.dcnt->error);
-        ctx.launches += 2;
-    }
-    KZG_CK(cudaEventRecord(ctx.ev[2], st));
-    if (np > 0) {
-        k_con_flags<<<blocks_for(np), kThreads, 0, st>>>(ctx.m_count, ctx.m_key, ctx.dcnt, ctx.con_flag);
-        size_t tb = ctx.cub_tmp_bytes;
-        KZG_CK(cub::DeviceScan::ExclusiveSum(ctx.cub_tmp, tb, ctx.con_flag, ctx.con_index, (int)np, st));
-        ctx.launches += 3;
-    }
-    if (np > 0)
-        k_build_constraints<<<blocks_for(np), kThreads, 0, st>>>(
-            ctx.pairs, ctx.con_flag, ctx.con_index, ctx.m_count, ctx.m_data, ctx.m_key, ctx.b, ctx.dcnt,
-            ctx.con_pair, ctx.con_a, ctx.con_b, ctx.con_np, ctx.con_bits, ctx.con_fr, ctx.con_key, ctx.r, ctx.c_key,
-            ctx.c_np, ctx.c_pos, ctx.c_imp, ctx.cfg.max_cache_entries, ctx.ws.warm_start,
-            (ctx.mlp.logging || (ctx.mlp.enabled && ctx.mlp.have)) ? ctx.miss_rows : nullptr, ctx.miss_prior);
+    KZG_CK(mark(ctx, 1));
+    k_narrow<<<blocks_for(P, 128), 128, 0, st>>>(T, ctx.b, ctx.pairs, ctx.dcnt, ctx.m_count, ctx.m_data, ctx.m_key,
+                                                 ctx.epa_list);
+    k_narrow_epa<<<152u * 8u, kEpaWarps * 32, kEpaWarps * sizeof(EpaWarpSmem), st>>>(
+        T, ctx.b, ctx.pairs, ctx.dcnt, ctx.epa_list, ctx.m_count, ctx.m_data, ctx.m_key, &ctx.dcnt->error);
+    KZG_CK(mark(ctx, 2));
+    k_con_flags<<<blocks_for(P), kThreads, 0, st>>>(ctx.m_count, ctx.m_key, ctx.dcnt, ctx.con_flag);
+    size_t tb = ctx.cub_tmp_bytes;
+    KZG_CK(cub::DeviceScan::ExclusiveSum(ctx.cub_tmp, tb, ctx.con_flag, ctx.con_index, (int)P, st));
+    k_build_constraints<<<blocks_for(P), kThreads, 0, st>>>(
+        ctx.pairs, ctx.con_flag, ctx.con_index, ctx.m_count, ctx.m_data, ctx.m_key, ctx.b, ctx.dcnt, ctx.con_pair,
+        ctx.con_a, ctx.con_b, ctx.con_np, ctx.con_bits, ctx.con_fr, ctx.con_key, ctx.r, ctx.c_key, ctx.c_np, ctx.c_pos,
+        ctx.c_imp, ctx.cfg.max_cache_entries, ctx.ws.warm_start,
+        (ctx.mlp.logging || (ctx.mlp.enabled && ctx.mlp.have)) ? ctx.miss_rows : nullptr, ctx.miss_prior);
     k_integrate_vel<<<blocks_for(nb), kThreads, 0, st>>>(
         ctx.b, nb, make_float3(ctx.ws.gravity[0], ctx.ws.gravity[1], ctx.ws.gravity[2]), dt);
-    ctx.launches += np > 0 ? 2 : 1;
-    kzg_status s = fetch_counters(ctx);
-    if (s != KZG_OK) return s;
-    const uint32_t nc = ctx.hcnt->ncons;
-    KZG_CK(cudaEventRecord(ctx.ev[3], st));
-    if (nc > 0) {
-        PrepParams pp{dt, ctx.ss.baumgarte, ctx.ss.penetration_slop, ctx.ss.restitution_threshold,
-                      ctx.ss.max_bias_velocity};
-        k_prepare<<<blocks_for(4 * nc), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_np, ctx.r, pp);
-        ctx.launches += mlp_after_prepare(ctx, dt);
-        k_uf_init<<<blocks_for(nb), kThreads, 0, st>>>(ctx.uf, nb);
-        k_uf_union<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf);
-        k_island_keys<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf,
-                                                           ctx.isl_key, ctx.isl_con_in);
-        size_t tb = ctx.cub_tmp_bytes;
-        KZG_CK(cub::DeviceRadixSort::SortPairs(ctx.cub_tmp, tb, ctx.isl_key, ctx.isl_key_sorted, ctx.isl_con_in,
-                                               ctx.isl_con, (int)nc, 0, bits_for(nb), st));
-        k_island_heads<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_key_sorted, ctx.isl_head);
-        tb = ctx.cub_tmp_bytes;
-        KZG_CK(cub::DeviceScan::ExclusiveSum(ctx.cub_tmp, tb, ctx.isl_head, ctx.isl_pts, (int)nc, st));
-        k_island_starts<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_head, ctx.isl_pts, ctx.isl_start);
-        s = fetch_counters(ctx);
-        if (s != KZG_OK) return s;
-        const uint32_t ni = ctx.hcnt->nislands;
-        SchedBufs SB{ctx.isl_start, ctx.isl_con, ctx.con_a, ctx.con_b, ctx.con_np, ctx.con_bits, ctx.r.bias,
-                     ctx.b.inv_mass, ctx.is_large, ctx.frame, ctx.brec, ctx.body_stamp, ctx.body_loc, ctx.isl_bodies,
-                     ctx.last_g, 2u * ctx.cfg.max_pairs, ctx.con_la, ctx.con_lb, ctx.first_w, ctx.first_b,
-                     ctx.ids_tmp, ctx.lvl_tmp, ctx.lvl_count, ctx.wl_list, ctx.vl_list, ctx.bl_list, ctx.wl_off,
-                     ctx.vl_off, ctx.bl_off, ctx.isl_meta, ctx.isl_small, ctx.isl_large};
-        k_schedule_warp<<<std::min<unsigned>(blocks_for(ni, 4), 152u * 16u), 128, 0, st>>>(SB, ctx.dcnt);
-        k_schedule_cta<<<std::min<unsigned>(ni, 152u * 2u), 256, 3 * kSchedCtaBodies * sizeof(uint32_t), st>>>(SB, ctx.dcnt);
-        ctx.launches += 17;  // prepare, union-find (3), island sort (4 CUB passes), heads, scan (2), starts, schedule (2)
-        KZG_CK(cudaEventRecord(ctx.ev[4], st));
-        SolveBufs SV{ctx.isl_start, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.con_la, ctx.con_lb, ctx.isl_meta,
-                     ctx.isl_bodies, ctx.wl_list, ctx.vl_list, ctx.bl_list, ctx.wl_off, ctx.vl_off, ctx.bl_off,
-                     ctx.isl_small, ctx.isl_large, ctx.r, ctx.b, ctx.ss.velocity_iterations,
-                     ctx.ss.position_iterations, ctx.ss.warm_start_factor, ctx.ss.use_velocity_bias,
-                     ctx.ss.residual_tolerance, ctx.ss.max_velocity_iterations};
-        if (ni > 0) {
-            const unsigned gw = std::min<unsigned>(blocks_for(ni, kWarpsPerBlock), 152u * 16u);
-            k_solve_warp<<<gw, kWarpsPerBlock * 32, kWarpsPerBlock * 2 * kWarpBodies * sizeof(float4), st>>>(SV, ctx.dcnt);
-            const unsigned gc = std::min<unsigned>(ni, 152u * 2u);
-            k_solve_cta<<<gc, kCtaThreads, 2 * kCtaBodiesMax * sizeof(float4), st>>>(SV, ctx.dcnt, kCtaBodiesMax);
-            k_solve_big<<<std::min<unsigned>(ni, 152u), kBigThreads, 0, st>>>(SV, ctx.dcnt, kCtaBodiesMax);
-            ctx.launches += 3;
-        }
-        ctx.launches += mlp_after_solve(ctx, dt);
-        KZG_CK(cudaEventRecord(ctx.ev[5], st));
+    ctx.launches += 7;  // narrow (2), flags, scan (2), build, integrate
+    KZG_CK(mark(ctx, 3));
+    PrepParams pp{dt, ctx.ss.baumgarte, ctx.ss.penetration_slop, ctx.ss.restitution_threshold, ctx.ss.max_bias_velocity};
+    k_prepare<<<blocks_for(R), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_np, ctx.r, pp);
+    ctx.launches += mlp_after_prepare(ctx, dt);
+    k_uf_init<<<blocks_for(nb), kThreads, 0, st>>>(ctx.uf, nb);
+    k_uf_union<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf);
+    const int kbits = bits_for(nb);
+    k_island_keys<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf,
+                                                      ctx.isl_key, ctx.isl_con_in, P, (1u << kbits) - 1u);
+    tb = ctx.cub_tmp_bytes;
+    KZG_CK(cub::DeviceRadixSort::SortPairs(ctx.cub_tmp, tb, ctx.isl_key, ctx.isl_key_sorted, ctx.isl_con_in,
+                                           ctx.isl_con, (int)P, 0, kbits, st));
+    k_island_heads<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_key_sorted, ctx.isl_head);
+    tb = ctx.cub_tmp_bytes;
+    KZG_CK(cub::DeviceScan::ExclusiveSum(ctx.cub_tmp, tb, ctx.isl_head, ctx.isl_pts, (int)P, st));
+    k_island_starts<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_head, ctx.isl_pts, ctx.isl_start);
+    SchedBufs SB{ctx.isl_start, ctx.isl_con, ctx.con_a, ctx.con_b, ctx.con_np, ctx.con_bits, ctx.r.bias,
+                 ctx.b.inv_mass, ctx.is_large, ctx.brec, ctx.body_stamp, ctx.body_loc, ctx.isl_bodies,
+                 ctx.last_g, 2u * ctx.cfg.max_pairs, ctx.con_la, ctx.con_lb, ctx.first_w, ctx.first_b,
+                 ctx.ids_tmp, ctx.lvl_tmp, ctx.lvl_count, ctx.wl_list, ctx.vl_list, ctx.bl_list, ctx.wl_off,
+                 ctx.vl_off, ctx.bl_off, ctx.isl_meta, ctx.isl_small, ctx.isl_large,
+                 std::min(ctx.tune.small_island_constraints, kSchedSmallCons),
+                 std::min(ctx.tune.warp_island_bodies, kWarpBodies)};
+    k_schedule_warp<<<152u * 16u, 128, 0, st>>>(SB, ctx.dcnt);
+    k_schedule_cta<<<152u * 2u, 256, 3 * kSchedCtaBodies * sizeof(uint32_t), st>>>(SB, ctx.dcnt);
+    ctx.launches += 17;  // prepare, union-find (3), island sort (4 CUB passes), heads, scan (2), starts, schedule (2)
+    KZG_CK(mark(ctx, 4));
+    SolveBufs SV{ctx.isl_start, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.con_la, ctx.con_lb, ctx.isl_meta,
+                 ctx.isl_bodies, ctx.wl_list, ctx.vl_list, ctx.bl_list, ctx.wl_off, ctx.vl_off, ctx.bl_off,
+                 ctx.isl_small, ctx.isl_large, ctx.r, ctx.b, ctx.ss.velocity_iterations,
+                 ctx.ss.position_iterations, ctx.ss.warm_start_factor, ctx.ss.use_velocity_bias,
+                 ctx.ss.residual_tolerance, ctx.ss.max_velocity_iterations, ctx.brec};
+    k_solve_warp<<<152u * 16u, kWarpsPerBlock * 32, kWarpsPerBlock * 2 * kWarpBodies * sizeof(float4), st>>>(SV, ctx.dcnt);
+    k_solve_cta<<<152u * 2u, kCtaThreads, 2 * kCtaBodiesMax * sizeof(float4), st>>>(SV, ctx.dcnt, kCtaBodiesMax);
+    if (g_cluster_ok) {
+        k_solve_cluster<<<kClusterCtas * 16u, kClusterThreads, 2 * kClusterSlots * sizeof(float4), st>>>(
+            SV, ctx.dcnt, kCtaBodiesMax);
         ++ctx.launches;
-        k_cache_store<<<blocks_for(nc), kThreads, 0, st>>>(ctx.dcnt, ctx.con_key, ctx.con_np, ctx.r, ctx.c_key,
-                                                           ctx.c_np, ctx.c_pos, ctx.c_imp, ctx.cfg.max_cache_entries);
-    } else {
-        KZG_CK(cudaEventRecord(ctx.ev[4], st));
-        KZG_CK(cudaEventRecord(ctx.ev[5], st));
     }
+    k_solve_big<<<152u, kBigThreads, 0, st>>>(SV, ctx.dcnt, kCtaBodiesMax,
+                                              g_cluster_ok ? kClusterCtas * kClusterSlots : 0u);
+    ctx.launches += 3;
+    ctx.launches += mlp_after_solve(ctx, dt);
+    KZG_CK(mark(ctx, 5));
+    k_cache_store<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_key, ctx.con_np, ctx.r, ctx.c_key, ctx.c_np,
+                                                      ctx.c_pos, ctx.c_imp, ctx.cfg.max_cache_entries);
     k_integrate_pos<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, dt, ctx.ss.use_velocity_bias);
-    ++ctx.launches;
-    KZG_CK(cudaEventRecord(ctx.ev[6], st));
+    ctx.launches += 2;
+    KZG_CK(mark(ctx, 6));
     KZG_CK(cudaGetLastError());
-    s = fetch_counters(ctx);
-    if (s != KZG_OK) return s;
     return KZG_OK;
 }
 
-static void reset_counters_async(Ctx& ctx) {
-    // npairs, ncons, nislands, batches, max levels and error restart each step; cache_entries persists
-    cudaMemsetAsync(ctx.dcnt, 0, offsetof(Counters, cache_entries), ctx.stream);
-}
-
-static kzg_status finish_stats(Ctx& ctx) {
+static kzg_status finish_stats(Ctx& ctx, uint32_t graph_steps = 0) {
     Counters& h = *ctx.hcnt;
     kzg_stats& s = ctx.stats;
     s.num_bodies = ctx.nbodies;
@@ -708,13 +747,20 @@ static kzg_status finish_stats(Ctx& ctx) {
     s.max_velocity_iterations_used = h.max_iters;
     s.point_velocity_iterations = h.pt_iters;
     memcpy(&s.final_residual, &h.res_bits, sizeof(float));
-    cudaEventElapsedTime(&s.broadphase_ms, ctx.ev[0], ctx.ev[1]);
-    cudaEventElapsedTime(&s.narrowphase_ms, ctx.ev[1], ctx.ev[2]);
-    cudaEventElapsedTime(&s.constraints_ms, ctx.ev[2], ctx.ev[3]);
-    cudaEventElapsedTime(&s.schedule_ms, ctx.ev[3], ctx.ev[4]);
-    cudaEventElapsedTime(&s.solve_ms, ctx.ev[4], ctx.ev[5]);
-    cudaEventElapsedTime(&s.integrate_ms, ctx.ev[5], ctx.ev[6]);
-    cudaEventElapsedTime(&s.step_ms, ctx.ev[0], ctx.ev[6]);
+    if (graph_steps) {  // replayed graph: its mean step time, no stage split
+        float ms = 0.0f;
+        KZG_CK(cudaEventElapsedTime(&ms, ctx.ev[0], ctx.ev[6]));
+        s.broadphase_ms = s.narrowphase_ms = s.constraints_ms = s.schedule_ms = s.solve_ms = s.integrate_ms = 0.0f;
+        s.step_ms = ms / (float)graph_steps;
+    } else {
+        KZG_CK(cudaEventElapsedTime(&s.broadphase_ms, ctx.ev[0], ctx.ev[1]));
+        KZG_CK(cudaEventElapsedTime(&s.narrowphase_ms, ctx.ev[1], ctx.ev[2]));
+        KZG_CK(cudaEventElapsedTime(&s.constraints_ms, ctx.ev[2], ctx.ev[3]));
+        KZG_CK(cudaEventElapsedTime(&s.schedule_ms, ctx.ev[3], ctx.ev[4]));
+        KZG_CK(cudaEventElapsedTime(&s.solve_ms, ctx.ev[4], ctx.ev[5]));
+        KZG_CK(cudaEventElapsedTime(&s.integrate_ms, ctx.ev[5], ctx.ev[6]));
+        KZG_CK(cudaEventElapsedTime(&s.step_ms, ctx.ev[0], ctx.ev[6]));
+    }
     if (h.error) {
         ctx.err = "device error word " + std::to_string(h.error) + " (see KZG_DEVERR_*)";
         return (h.error & (KZG_DEVERR_PAIRS | KZG_DEVERR_CACHE)) ? KZG_ERR_CAPACITY : KZG_ERR_DEVICE;
@@ -722,14 +768,14 @@ static kzg_status finish_stats(Ctx& ctx) {
     return KZG_OK;
 }
 
-kzg_status step_canonical(Ctx& ctx, float dt) {
+// One canonical step (GPU broad phase), issued without host synchronisation.
+static kzg_status record_canonical(Ctx& ctx, float dt) {
     cudaStream_t st = ctx.stream;
-    const uint32_t nb = ctx.nbodies;
-    ++ctx.frame;
+    KZG_CK(cudaPeekAtLastError());
+    const uint32_t nb = ctx.nbodies, P = ctx.cfg.max_pairs;
     ctx.launches = 0;
-    reset_counters_async(ctx);
-    KZG_CK(cudaEventRecord(ctx.ev[0], st));
-    ctx.launches += 8;  // aabb, cell sort (4 CUB passes), find pairs, key sort + unpack counted below
+    k_begin_step<<<1, 32, 0, st>>>(ctx.dcnt);
+    KZG_CK(mark(ctx, 0));
     k_aabb<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, ctx.shapes, nb, 1.0f / ctx.cell_size, ctx.is_large,
                                                 ctx.cell_keys, ctx.cell_vals);
     size_t tb = ctx.cub_tmp_bytes;
@@ -738,21 +784,65 @@ kzg_status step_canonical(Ctx& ctx, float dt) {
     const uint32_t nsmall = nb - ctx.nlarge;
     k_find_pairs<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, ctx.cell_keys_sorted, ctx.cell_vals_sorted, nsmall,
                                                       1.0f / ctx.cell_size, ctx.is_large, ctx.large_list,
-                                                      ctx.large_off, ctx.nworlds, ctx.pair_keys, ctx.dcnt,
-                                                      ctx.cfg.max_pairs);
-    kzg_status s = fetch_counters(ctx);
-    if (s != KZG_OK) return s;
-    if (ctx.hcnt->error & KZG_DEVERR_PAIRS) return finish_stats(ctx);
-    const uint32_t np = ctx.hcnt->npairs;
-    if (np > 0) {
-        tb = ctx.cub_tmp_bytes;
-        KZG_CK(cub::DeviceRadixSort::SortKeys(ctx.cub_tmp, tb, ctx.pair_keys, ctx.pair_keys_sorted, (int)np, 0, 64, st));
-        k_unpack_pairs<<<blocks_for(np), kThreads, 0, st>>>(ctx.pair_keys_sorted, ctx.dcnt, ctx.pairs);
-        ctx.launches += 5;
+                                                      ctx.large_off, ctx.nworlds, ctx.pair_keys, ctx.dcnt, P);
+    k_clamp_pairs<<<1, 1, 0, st>>>(ctx.dcnt, P);
+    k_pad_keys<<<blocks_for(P), kThreads, 0, st>>>(ctx.pair_keys, ctx.dcnt, P);
+    tb = ctx.cub_tmp_bytes;
+    KZG_CK(cub::DeviceRadixSort::SortKeys(ctx.cub_tmp, tb, ctx.pair_keys, ctx.pair_keys_sorted, (int)P, 0, 64, st));
+    k_unpack_pairs<<<blocks_for(P), kThreads, 0, st>>>(ctx.pair_keys_sorted, ctx.dcnt, ctx.pairs);
+    ctx.launches += 16;  // begin, aabb, cell sort (4 CUB passes), find pairs, clamp, pad, key sort (4+), unpack
+    return record_after_pairs(ctx, dt);
+}
+
+// Capture one canonical step into a CUDA graph (once per dt and configuration).
+static kzg_status ensure_graph(Ctx& ctx, float dt) {
+    if (ctx.graph_exec && !ctx.graph_dirty && ctx.graph_dt == dt) return KZG_OK;
+    KZG_CK(cudaGetLastError());
+    if (ctx.graph_exec) cudaGraphExecDestroy(ctx.graph_exec);
+    ctx.graph_exec = nullptr;
+    cudaGraph_t g = nullptr;
+    KZG_CK(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));
+    ctx.capturing = true;
+    kzg_status s = record_canonical(ctx, dt);
+    ctx.capturing = false;
+    cudaError_t e = cudaStreamEndCapture(ctx.stream, &g);
+    if (s != KZG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return s;
     }
-    s = step_after_pairs(ctx, dt);
-    if (s != KZG_OK) return s;
-    return finish_stats(ctx);
+    KZG_CK(e);
+    e = cudaGraphInstantiate(&ctx.graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    KZG_CK(e);
+    ctx.graph_dt = dt;
+    ctx.graph_dirty = false;
+    ctx.graph_launches = ctx.launches;
+    return KZG_OK;
+}
+
+kzg_status step_canonical(Ctx& ctx, float dt, uint32_t nsteps) {
+    if (ctx.use_graph) {
+        kzg_status s = ensure_graph(ctx, dt);
+        if (s != KZG_OK) return s;
+        KZG_CK(cudaEventRecord(ctx.ev[0], ctx.stream));
+        for (uint32_t i = 0; i < nsteps; ++i) KZG_CK(cudaGraphLaunch(ctx.graph_exec, ctx.stream));
+        KZG_CK(cudaEventRecord(ctx.ev[6], ctx.stream));
+        ctx.frame += nsteps;
+        ctx.launches = ctx.graph_launches;
+        s = fetch_counters(ctx);
+        if (s != KZG_OK) return s;
+        return finish_stats(ctx, nsteps);
+    }
+    for (uint32_t i = 0; i < nsteps; ++i) {
+        ++ctx.frame;
+        kzg_status s = record_canonical(ctx, dt);
+        if (s != KZG_OK) return s;
+        s = fetch_counters(ctx);
+        if (s != KZG_OK) return s;
+        s = finish_stats(ctx);
+        if (s != KZG_OK) return s;
+    }
+    return KZG_OK;
 }
 
 kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t np, float dt) {
@@ -762,8 +852,8 @@ kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t np, floa
         return KZG_ERR_CAPACITY;
     }
     ++ctx.frame;
-    ctx.launches = np > 0 ? 1 : 0;
-    reset_counters_async(ctx);
+    ctx.launches = np > 0 ? 2 : 1;
+    k_begin_step<<<1, 32, 0, st>>>(ctx.dcnt);
     KZG_CK(cudaEventRecord(ctx.ev[0], st));
     if (np > 0) {
         KZG_CK(cudaMemcpyAsync(ctx.pair_keys, host_pairs, sizeof(uint32_t) * 2 * np, cudaMemcpyHostToDevice, st));
@@ -771,8 +861,9 @@ kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t np, floa
                                                                  ctx.nbodies, ctx.pairs);
     }
     KZG_CK(cudaMemcpyAsync(&ctx.dcnt->npairs, &np, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    ctx.hcnt->npairs = np;
-    kzg_status s = step_after_pairs(ctx, dt);
+    kzg_status s = record_after_pairs(ctx, dt);
+    if (s != KZG_OK) return s;
+    s = fetch_counters(ctx);
     if (s != KZG_OK) return s;
     return finish_stats(ctx);
 }

@@ -309,3 +309,28 @@ def world_batch(num_worlds: int = 4096, seed: int = 4242, lo: int = 8, hi: int =
         sc.name = f"world{w}"
         worlds.append(sc)
     return worlds
+
+
+def merge_worlds(worlds: List[Scene]):
+    """Independent worlds as one scene plus a world id per body: shape tables are concatenated
+    (bodies re-indexed), world and solver settings are taken from the first world (all must agree).
+    Bodies of different worlds never interact (the broad phase keys its cells and its plane lists by
+    world)."""
+    if not worlds:
+        raise ValueError("no worlds")
+    first = worlds[0]
+    keys = ("gravity", "dt", "velocity_iterations", "position_iterations", "flags", "baumgarte",
+            "penetration_slop", "restitution_threshold", "max_bias_velocity", "warm_start_factor")
+    out = Scene(name=f"{len(worlds)} worlds", **{k: getattr(first, k) for k in keys})
+    ids = []
+    for w, sc in enumerate(worlds):
+        if any(getattr(sc, k) != getattr(first, k) for k in keys):
+            raise ValueError(f"world {w} has different settings")
+        base = len(out.shapes)
+        out.shapes.extend(sc.shapes)
+        for b in sc.bodies:
+            nb = Body(**{f: getattr(b, f) for f in b.__dataclass_fields__})
+            nb.shape = b.shape + base
+            out.bodies.append(nb)
+            ids.append(w)
+    return out, np.asarray(ids, np.uint32)

@@ -180,6 +180,26 @@ class World:
             setattr(self._ss, k, v)
         self._check(capi.load().kzg_set_solver_settings(self._h, ctypes.byref(self._ss)))
 
+    def set_graph(self, enabled: bool = True):
+        """Step through a captured CUDA graph (step_fixed(n) then launches n steps back to back)."""
+        self._check(capi.load().kzg_set_graph(self._h, int(bool(enabled))))
+
+    def set_tuning(self, small_island_constraints: int, warp_island_bodies: int):
+        t = capi.KzgTuning(small_island_constraints, warp_island_bodies, 0.0)
+        self._check(capi.load().kzg_set_tuning(self._h, ctypes.byref(t)))
+
+    def get_tuning(self) -> dict:
+        t = capi.KzgTuning()
+        self._check(capi.load().kzg_get_tuning(self._h, ctypes.byref(t)))
+        return {n: getattr(t, n) for n, _ in capi.KzgTuning._fields_}
+
+    def autotune(self, steps_per_candidate: int = 3, dt: Optional[float] = None) -> dict:
+        """Pick the fastest launch shapes on the live world (advances it 10 x steps_per_candidate steps)."""
+        t = capi.KzgTuning()
+        self._check(capi.load().kzg_autotune(self._h, np.float32(self.dt if dt is None else dt),
+                                             int(steps_per_candidate), ctypes.byref(t)))
+        return {n: getattr(t, n) for n, _ in capi.KzgTuning._fields_}
+
     def set_residual(self, tolerance: float, max_iterations: int = 64):
         """Residual-terminated velocity iterations (tolerance in m/s; 0 = the fixed count)."""
         self.set_solver(residual_tolerance=float(tolerance), max_velocity_iterations=int(max_iterations))

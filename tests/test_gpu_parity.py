@@ -125,6 +125,27 @@ def test_residual_terminated_bit_exact_with_oracle(name, steps, oracle_lib, kzg_
         assert len(seen_iters) > 1  # the stopping rule actually varied the iteration count
 
 
+def test_graph_stepping_matches_direct_stepping(kzg_lib):
+    """kzg_set_graph: steps replayed from one captured CUDA graph give the same bits as steps issued
+    one by one, including after a settings change forces a new capture."""
+    from kizuriphysics3d_gb300 import World, resolve, scenes
+    sc = scenes.pile(600, seed=8, extent=4.0, y_range=(1.0, 12.0))
+    res = resolve(sc)
+    with World(sc, resolved=res) as a, World(sc, resolved=res) as b:
+        b.set_graph(True)
+        for chunk in (1, 7, 20, 20):
+            a.step_fixed(n=chunk)
+            b.step_fixed(n=chunk)
+            assert a.compute_state_hash() == b.compute_state_hash()
+        a.set_residual(1e-4, 64)
+        b.set_residual(1e-4, 64)
+        a.step_fixed(n=15)
+        b.step_fixed(n=15)
+        assert a.compute_state_hash() == b.compute_state_hash()
+        assert np.array_equal(bits(a.state()), bits(b.state()))
+        assert b.get_stats()["max_velocity_iterations_used"] == a.get_stats()["max_velocity_iterations_used"]
+
+
 def test_hash_identical_run_to_run(kzg_lib):
     from kizuriphysics3d_gb300 import World, resolve, scenes
     sc = scenes.pile(800, seed=5, extent=4.0, y_range=(1.0, 12.0))

@@ -74,3 +74,23 @@ def test_scene_roundtrip():
     assert scenes.Scene.from_bytes(b).to_bytes() == b
     assert scenes.pyramid(20).num_dynamic == 210
     assert len(scenes.stacks(3, 2, 7).bodies) == 1 + 3 * 2 * 7
+
+
+def test_merge_worlds_remaps_shapes_and_tags_bodies():
+    from kizuriphysics3d_gb300 import scenes
+    ws = [scenes.pyramid(3), scenes.pile(12, seed=3, extent=2.0), scenes.pyramid(2)]
+    merged, ids = scenes.merge_worlds(ws)
+    assert len(merged.bodies) == sum(len(w.bodies) for w in ws) == ids.shape[0]
+    assert len(merged.shapes) == sum(len(w.shapes) for w in ws)
+    off_s, off_b = 0, 0
+    for k, w in enumerate(ws):
+        for j, b in enumerate(w.bodies):
+            mb = merged.bodies[off_b + j]
+            assert ids[off_b + j] == k
+            assert merged.shapes[mb.shape] is w.shapes[b.shape]
+            assert mb.pos == b.pos and mb.motion == b.motion
+        off_s += len(w.shapes)
+        off_b += len(w.bodies)
+    worlds = scenes.world_batch(16, seed=4242)
+    sizes = [len(w.bodies) - 1 for w in worlds]  # minus the plane
+    assert all(s >= 1 for s in sizes)
