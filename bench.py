@@ -47,6 +47,10 @@ def make_workload(name: str):
             "workload": "random convex pile, 20000 bodies (sphere/box/capsule/16-point hull), seed 1234, "
                         "positions U[-20,20]x[2,100]x[-20,20], 10 velocity + 2 position iterations, dt 1/60",
             "bodies": 20000}
+    if name == "pile4000":  # a smaller pile of the same generator (profiling case)
+        return scenes.pile(4000, seed=1234, extent=20.0 * (4000 / 20000) ** 0.5, y_range=(2.0, 40.0)), 0, {
+            "workload": "random convex pile, 4000 bodies, seed 1234, extent scaled by sqrt(4000/20000), "
+                        "y in [2, 40], 10 velocity + 2 position iterations, dt 1/60", "bodies": 4000}
     if name == "stacks":
         return scenes.stacks(20, 20, 500), 0, {
             "workload": "large box field, 400 stacks x 500 unit boxes, jitter seed 7, 8 velocity + 2 position "
@@ -359,7 +363,7 @@ def main():
         "k_narrow + k_narrow_epa": (acc["narrowphase_ms"] / args.steps, nb),
         "k_schedule_cta + k_schedule_warp": (acc["schedule_ms"] / args.steps,
                                              schedule_bytes(points, last["num_contact_constraints"])),
-        "k_solve_big + k_solve_cta + k_solve_warp": (acc["solve_ms"] / args.steps, solve_bytes(points, n_dyn)),
+        "k_solve_cluster + k_solve_big + k_solve_cta + k_solve_warp": (acc["solve_ms"] / args.steps, solve_bytes(points, n_dyn)),
     }
     kname = max(cand, key=lambda k: cand[k][0])
     kms, kbytes = cand[kname]

@@ -243,6 +243,15 @@ kzg_status kzg_download_constraints(kzg_ctx* ctx, uint32_t* hdr, float* fr, floa
 kzg_status kzg_state_hash_noalloc(const float* state, const uint32_t* packed_ids, uint32_t n, void* stream,
                                   uint64_t* out, const char** error);
 
+/* ---- device snapshots (no counterpart in the reference) ---------------------------------------
+ * Body state (positions, rotations, velocities, pseudo velocities, force accumulators, world
+ * inverse inertia) and the occupied entries of the manifold cache, so that a context built from the
+ * same bodies resumes bit-exactly where the snapshot was taken.  The reference's KZP1 files
+ * (kizuriphysics3d_gb300/kzp1.py) carry bodies only: warm starting restarts from zero. */
+kzg_status kzg_snapshot_size(kzg_ctx* ctx, size_t* bytes);
+kzg_status kzg_snapshot_save(kzg_ctx* ctx, void* out, size_t capacity);
+kzg_status kzg_snapshot_load(kzg_ctx* ctx, const void* in, size_t size);
+
 /* ---- learned warm start ------------------------------------------------------------------------
  * No counterpart in the reference, which warm-starts a contact point that misses the manifold
  * cache with zero impulses (PhysicsWorld.cpp:518-529).  With a model set and enabled, such points
@@ -259,12 +268,18 @@ kzg_status kzg_state_hash_noalloc(const float* state, const uint32_t* packed_ids
 kzg_status kzg_mlp_set_params(kzg_ctx* ctx, const float* theta, const float* mean, const float* std);
 kzg_status kzg_mlp_get_params(kzg_ctx* ctx, float* theta, float* mean, float* std);
 kzg_status kzg_mlp_enable(kzg_ctx* ctx, int enabled);
+/* Fractions in [0, 1] of the predicted normal and tangent impulses used as the warm start
+ * (default 1, 1). */
+kzg_status kzg_mlp_set_blend(kzg_ctx* ctx, float normal, float tangent);
 /* Log every cache-missing contact point of the following steps (features before the solve,
  * impulse / effective mass after it) into a device buffer of `capacity` samples; 0 stops. */
 kzg_status kzg_mlp_log_begin(kzg_ctx* ctx, uint32_t capacity);
 kzg_status kzg_mlp_log_fetch(kzg_ctx* ctx, float* out, uint32_t capacity, uint32_t* count);
 kzg_status kzg_mlp_set_dataset(kzg_ctx* ctx, const float* samples, uint32_t n); /* log layout */
-/* Mean-squared error over the valid targets of samples [first, first + count): its gradient
+/* Training loss: 0 (default) the squared error, tau in (0, 1) the pinball loss of quantile tau
+ * (fits the tau-quantile of the target: below-median quantiles give conservative warm starts). */
+kzg_status kzg_mlp_set_quantile(kzg_ctx* ctx, float tau);
+/* Loss averaged over the valid targets of samples [first, first + count): its gradient
  * (no update), or one Adam step (beta 0.9 / 0.999). */
 kzg_status kzg_mlp_gradient(kzg_ctx* ctx, uint32_t first, uint32_t count, float* grad, float* loss);
 kzg_status kzg_mlp_train_step(kzg_ctx* ctx, uint32_t first, uint32_t count, float lr, float* loss);

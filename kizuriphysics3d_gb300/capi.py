@@ -124,12 +124,17 @@ def load(build_if_missing: bool = True):
     L.kzg_mass_properties.argtypes = [P(KzgShapeDesc), vp, vp, vp, u32, f32, f32, P(f32), vp]
     L.kzg_state_hash_noalloc.argtypes = [vp, vp, u32, vp, P(ctypes.c_uint64), P(ctypes.c_char_p)]
     L.kzg_set_graph.argtypes = [vp, ctypes.c_int]
+    L.kzg_snapshot_size.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
+    L.kzg_snapshot_save.argtypes = [vp, vp, ctypes.c_size_t]
+    L.kzg_snapshot_load.argtypes = [vp, vp, ctypes.c_size_t]
     L.kzg_set_tuning.argtypes = [vp, P(KzgTuning)]
     L.kzg_get_tuning.argtypes = [vp, P(KzgTuning)]
     L.kzg_autotune.argtypes = [vp, f32, u32, P(KzgTuning)]
     L.kzg_mlp_set_params.argtypes = [vp, vp, vp, vp]
     L.kzg_mlp_get_params.argtypes = [vp, vp, vp, vp]
     L.kzg_mlp_enable.argtypes = [vp, ctypes.c_int]
+    L.kzg_mlp_set_blend.argtypes = [vp, f32, f32]
+    L.kzg_mlp_set_quantile.argtypes = [vp, f32]
     L.kzg_mlp_log_begin.argtypes = [vp, u32]
     L.kzg_mlp_log_fetch.argtypes = [vp, vp, u32, P(u32)]
     L.kzg_mlp_set_dataset.argtypes = [vp, vp, u32]

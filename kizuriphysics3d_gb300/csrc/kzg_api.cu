@@ -738,6 +738,130 @@ kzg_status kzg_download_constraints(kzg_ctx* k, uint32_t* hdr, float* fr, float*
     return KZG_OK;
 }
 
+// ---- device snapshots: body state and the manifold cache, for exact resume ------------------
+namespace {
+constexpr uint32_t kSnapMagic = 0x53475A4Bu;  // 'KZGS'
+constexpr uint32_t kSnapVersion = 1;
+struct SnapHeader {
+    uint32_t magic, version, nbodies, cache_cap, cache_entries, cache_used, reserved[2];
+};
+constexpr int kSnapBodyArrays = 8;  // pos, rot, lv, av, plv, pav, force, torque (+ 3 iiw columns)
+constexpr size_t kSnapBodyBytes = sizeof(float4) * (kSnapBodyArrays + 3);
+constexpr size_t kSnapCacheBytes = sizeof(uint32_t) + sizeof(unsigned long long) + sizeof(uint32_t) + 8 * sizeof(float4);
+
+float4** snap_body_arrays(DeviceBodies& b, float4** out) {
+    float4* a[kSnapBodyArrays] = {b.pos, b.rot, b.lv, b.av, b.plv, b.pav, b.force, b.torque};
+    for (int i = 0; i < kSnapBodyArrays; ++i) out[i] = a[i];
+    return out;
+}
+}  // namespace
+
+kzg_status kzg_snapshot_size(kzg_ctx* k, size_t* bytes) {
+    if (check(k) || !bytes) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const size_t H = ctx->cfg.max_cache_entries;
+    std::vector<unsigned long long> keys(H);
+    CK(cudaMemcpy(keys.data(), ctx->c_key, sizeof(unsigned long long) * H, cudaMemcpyDeviceToHost));
+    size_t used = 0;
+    for (unsigned long long key : keys) used += key != 0ull;
+    *bytes = sizeof(SnapHeader) + kSnapBodyBytes * ctx->nbodies + kSnapCacheBytes * used;
+    return KZG_OK;
+}
+
+kzg_status kzg_snapshot_save(kzg_ctx* k, void* out, size_t capacity) {
+    if (check(k) || !out) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const size_t H = ctx->cfg.max_cache_entries, nb = ctx->nbodies;
+    std::vector<unsigned long long> keys(H);
+    std::vector<uint32_t> np(H);
+    std::vector<float4> pos(4 * H), imp(4 * H);
+    CK(cudaMemcpy(keys.data(), ctx->c_key, sizeof(unsigned long long) * H, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(np.data(), ctx->c_np, sizeof(uint32_t) * H, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(pos.data(), ctx->c_pos, sizeof(float4) * 4 * H, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(imp.data(), ctx->c_imp, sizeof(float4) * 4 * H, cudaMemcpyDeviceToHost));
+    size_t used = 0;
+    for (unsigned long long key : keys) used += key != 0ull;
+    const size_t need = sizeof(SnapHeader) + kSnapBodyBytes * nb + kSnapCacheBytes * used;
+    if (capacity < need) {
+        ctx->err = "kzg_snapshot_save: buffer smaller than kzg_snapshot_size";
+        return KZG_ERR_CAPACITY;
+    }
+    uint8_t* p = static_cast<uint8_t*>(out);
+    SnapHeader h{kSnapMagic, kSnapVersion, (uint32_t)nb, (uint32_t)H, ctx->hcnt->cache_entries, (uint32_t)used, {0, 0}};
+    CK(cudaMemcpy(&h.cache_entries, &ctx->dcnt->cache_entries, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    std::memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    float4* arrs[kSnapBodyArrays];
+    snap_body_arrays(ctx->b, arrs);
+    for (int a = 0; a < kSnapBodyArrays; ++a) {
+        CK(cudaMemcpy(p, arrs[a], sizeof(float4) * nb, cudaMemcpyDeviceToHost));
+        p += sizeof(float4) * nb;
+    }
+    CK(cudaMemcpy(p, ctx->b.iiw, sizeof(float4) * 3 * nb, cudaMemcpyDeviceToHost));
+    p += sizeof(float4) * 3 * nb;
+    for (size_t slot = 0; slot < H; ++slot) {  // occupied slots of the open-addressing table
+        if (!keys[slot]) continue;
+        const uint32_t s32 = (uint32_t)slot;
+        std::memcpy(p, &s32, 4); p += 4;
+        std::memcpy(p, &keys[slot], 8); p += 8;
+        std::memcpy(p, &np[slot], 4); p += 4;
+        std::memcpy(p, &pos[4 * slot], 4 * sizeof(float4)); p += 4 * sizeof(float4);
+        std::memcpy(p, &imp[4 * slot], 4 * sizeof(float4)); p += 4 * sizeof(float4);
+    }
+    return KZG_OK;
+}
+
+kzg_status kzg_snapshot_load(kzg_ctx* k, const void* in, size_t size) {
+    if (check(k) || !in || size < sizeof(SnapHeader)) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    CK(cudaSetDevice(ctx->device));
+    kzg_status st = finalize_bodies(k);
+    if (st != KZG_OK) return st;
+    SnapHeader h;
+    std::memcpy(&h, in, sizeof(h));
+    const size_t H = ctx->cfg.max_cache_entries, nb = ctx->nbodies;
+    if (h.magic != kSnapMagic || h.version != kSnapVersion || h.nbodies != nb || h.cache_cap != H ||
+        size != sizeof(SnapHeader) + kSnapBodyBytes * nb + kSnapCacheBytes * (size_t)h.cache_used) {
+        ctx->err = "kzg_snapshot_load: snapshot does not match this context (bodies, cache capacity or size)";
+        return KZG_ERR_INVALID;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    const uint8_t* p = static_cast<const uint8_t*>(in) + sizeof(h);
+    float4* arrs[kSnapBodyArrays];
+    snap_body_arrays(ctx->b, arrs);
+    for (int a = 0; a < kSnapBodyArrays; ++a) {
+        CK(cudaMemcpy(arrs[a], p, sizeof(float4) * nb, cudaMemcpyHostToDevice));
+        p += sizeof(float4) * nb;
+    }
+    CK(cudaMemcpy(ctx->b.iiw, p, sizeof(float4) * 3 * nb, cudaMemcpyHostToDevice));
+    p += sizeof(float4) * 3 * nb;
+    std::vector<unsigned long long> keys(H, 0ull);
+    std::vector<uint32_t> np(H, 0u);
+    std::vector<float4> pos(4 * H, make_float4(0.0f, 0.0f, 0.0f, 0.0f)), imp(4 * H, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    for (uint32_t e = 0; e < h.cache_used; ++e) {
+        uint32_t slot;
+        std::memcpy(&slot, p, 4); p += 4;
+        if (slot >= H) {
+            ctx->err = "kzg_snapshot_load: cache slot out of range";
+            return KZG_ERR_INVALID;
+        }
+        std::memcpy(&keys[slot], p, 8); p += 8;
+        std::memcpy(&np[slot], p, 4); p += 4;
+        std::memcpy(&pos[4 * slot], p, 4 * sizeof(float4)); p += 4 * sizeof(float4);
+        std::memcpy(&imp[4 * slot], p, 4 * sizeof(float4)); p += 4 * sizeof(float4);
+    }
+    CK(cudaMemcpy(ctx->c_key, keys.data(), sizeof(unsigned long long) * H, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->c_np, np.data(), sizeof(uint32_t) * H, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->c_pos, pos.data(), sizeof(float4) * 4 * H, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->c_imp, imp.data(), sizeof(float4) * 4 * H, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(&ctx->dcnt->cache_entries, &h.cache_entries, sizeof(uint32_t), cudaMemcpyHostToDevice));
+    return KZG_OK;
+}
+
 kzg_status kzg_mlp_set_params(kzg_ctx* k, const float* theta, const float* mean, const float* stdv) {
     if (k) k->c.graph_dirty = true;
     if (check(k) || !theta || !mean || !stdv) return KZG_ERR_INVALID;
@@ -757,6 +881,21 @@ kzg_status kzg_mlp_enable(kzg_ctx* k, int enabled) {
         return KZG_ERR_INVALID;
     }
     k->c.mlp.enabled = enabled != 0;
+    return KZG_OK;
+}
+
+kzg_status kzg_mlp_set_blend(kzg_ctx* k, float normal, float tangent) {
+    if (k) k->c.graph_dirty = true;
+    if (check(k) || !(normal >= 0.0f && normal <= 1.0f) || !(tangent >= 0.0f && tangent <= 1.0f))
+        return KZG_ERR_INVALID;
+    k->c.mlp.blend_n = normal;
+    k->c.mlp.blend_t = tangent;
+    return KZG_OK;
+}
+
+kzg_status kzg_mlp_set_quantile(kzg_ctx* k, float tau) {
+    if (check(k) || !(tau >= 0.0f && tau < 1.0f)) return KZG_ERR_INVALID;
+    k->c.mlp.tau = tau;
     return KZG_OK;
 }
 

@@ -65,6 +65,8 @@ struct Counters {  // device-side counters, copied back after each stage that si
 // Learned warm start (kzg_mlp.cu): model, optimiser state, training log and dataset.
 struct MlpState {
     bool have = false, enabled = false, logging = false;
+    float blend_n = 1.0f, blend_t = 1.0f;  // fractions of the normal / tangent predictions used
+    float tau = 0.0f;                      // training loss: 0 squared error, else pinball of this quantile
     float* theta = nullptr;  // KZG_MLP_PARAMS fp32 parameters
     float *adam_m = nullptr, *adam_v = nullptr;
     uint32_t adam_t = 0;
@@ -155,7 +157,7 @@ struct Ctx {
     uint32_t *con_la = nullptr, *con_lb = nullptr;             // per constraint local body indices
     uint32_t *isl_small = nullptr, *isl_large = nullptr;       // islands by solve kernel
     uint32_t* miss_rows = nullptr;                              // rows without a cached warm start
-    float4* miss_prior = nullptr;  // per miss: nearest cached point of the pair (impulses, distance; -1: none)
+    float4* miss_prior = nullptr;  // per miss: nearest cached point's impulses, pair's cached normal impulse per point
     MlpState mlp;
 
     // cache

@@ -148,7 +148,7 @@ __device__ void forward_rows(bf16* X, bf16* H1, bf16* H2, const bf16* W1, const 
 //   4-6 rA . (n, t1, t2)   7-9 rB . (n, t1, t2)
 //   10-11 log inverse masses   12-13 log n.I^-1 n (A, B)
 //   14-16 impulses of the pair's nearest cached point / effective masses (0 without one)
-//   17 distance to that point (-1 without one)
+//   17 the pair's cached normal impulse per current point / normal effective mass (0 without)
 //   18-20 log effective masses (n, t1, t2)   21 friction   22 restitution bias   23 dt (g . n)
 // Mass-like quantities enter as log(x + 1e-6) so that bodies of any size share one scale.
 __device__ void row_features(const DeviceBodies& b, const DeviceRows& r, uint32_t A, uint32_t B, uint32_t row,
@@ -172,7 +172,7 @@ __device__ void row_features(const DeviceBodies& b, const DeviceRows& r, uint32_
     f[14] = m.x > 0.0f ? prior.x / m.x : 0.0f;
     f[15] = m.y > 0.0f ? prior.y / m.y : 0.0f;
     f[16] = m.z > 0.0f ? prior.z / m.z : 0.0f;
-    f[17] = prior.w;
+    f[17] = m.x > 0.0f ? prior.w / m.x : 0.0f;
     f[18] = logf(m.x + eps);
     f[19] = logf(m.y + eps);
     f[20] = logf(m.z + eps);
@@ -199,7 +199,7 @@ struct StepView {
 
 // ---- inference: warm start of the cache misses --------------------------------------------
 __global__ void __launch_bounds__(kMlpThreads) k_mlp_infer(StepView v, const float* __restrict__ theta,
-                                                        const float* __restrict__ norm) {
+                                                        const float* __restrict__ norm, float blend_n, float blend_t) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     MlpSmemFwd& S = *reinterpret_cast<MlpSmemFwd*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -225,7 +225,9 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_infer(StepView v, const flo
             const float4 m = v.r.mass[row];
             const float fric = v.r.t1[row].w;
             float y[3];
-            for (int q = 0; q < 3; ++q) y[q] = kTargetScale * sinhf(fminf(fmaxf(S.Y[tid * 4 + q], -kOutLimit), kOutLimit));
+            for (int q = 0; q < 3; ++q)
+                y[q] = (q == 0 ? blend_n : blend_t) * kTargetScale *
+                       sinhf(fminf(fmaxf(S.Y[tid * 4 + q], -kOutLimit), kOutLimit));
             const float ni = fmaxf(y[0] * m.x, 0.0f);
             const float mf = fric * ni;
             const float t1 = fminf(fmaxf(y[1] * m.y, -mf), mf);
@@ -300,10 +302,12 @@ __device__ __forceinline__ float2 frag_colsum(const float c[4]) {
 }
 
 // One CTA: forward + backward of up to 128 samples; writes its partial gradient (kP floats) and
-// partial loss.  Loss = sum over valid outputs of (y - target)^2 * inv_nvalid.
+// partial loss.  Loss over the valid outputs, times inv_nvalid: (y - target)^2 (tau = 0), or the
+// pinball loss of quantile tau, tau (target - y) above the prediction and (1 - tau) (y - target)
+// below it, which fits the tau-quantile of the target instead of its mean.
 __global__ void __launch_bounds__(kMlpThreads) k_mlp_train(const float* __restrict__ theta, const float* __restrict__ norm,
                                                         const float* __restrict__ ds, uint32_t first, uint32_t count,
-                                                        float inv_nvalid, float* __restrict__ part,
+                                                        float inv_nvalid, float tau, float* __restrict__ part,
                                                         float* __restrict__ part_loss) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     MlpSmemTrain& S = *reinterpret_cast<MlpSmemTrain*>(smem_raw);
@@ -340,8 +344,13 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_train(const float* __restri
     float loss = 0.0f, dy[3];
     for (int q = 0; q < 3; ++q) {
         const float e = S.f.Y[tid * 4 + q] - tgt[q];
-        loss += msk[q] * e * e;
-        dy[q] = msk[q] * 2.0f * e * inv_nvalid;
+        if (tau > 0.0f) {
+            loss += msk[q] * (e > 0.0f ? (1.0f - tau) * e : -tau * e);
+            dy[q] = msk[q] * (e > 0.0f ? (1.0f - tau) : -tau) * inv_nvalid;
+        } else {
+            loss += msk[q] * e * e;
+            dy[q] = msk[q] * 2.0f * e * inv_nvalid;
+        }
     }
     for (int o = 0; o < 16; ++o) {
         const bf16 v = __float2bfloat16_rn(o < 3 ? dy[o] : 0.0f);
@@ -644,8 +653,8 @@ static kzg_status mlp_batch_grad(Ctx& ctx, uint32_t first, uint32_t count, float
     const double nvalid = M.ds_valid_prefix[first + count] - M.ds_valid_prefix[first];
     const float inv = nvalid > 0.0 ? (float)(1.0 / nvalid) : 0.0f;
     float* part_loss = M.part + (size_t)nblk * kP;
-    k_mlp_train<<<nblk, kMlpThreads, sizeof(MlpSmemTrain), ctx.stream>>>(M.theta, M.norm, M.ds, first, count, inv, M.part,
-                                                                     part_loss);
+    k_mlp_train<<<nblk, kMlpThreads, sizeof(MlpSmemTrain), ctx.stream>>>(M.theta, M.norm, M.ds, first, count, inv,
+                                                                        M.tau, M.part, part_loss);
     k_mlp_reduce<<<(kP + 255) / 256, 256, 0, ctx.stream>>>(M.part, part_loss, nblk, M.grad, M.grad + kP);
     MLP_CK(cudaGetLastError());
     if (loss_out) {
@@ -715,7 +724,8 @@ uint32_t mlp_after_prepare(Ctx& ctx, float dt) {
     }
     if (M.enabled && M.have) {
         const unsigned grid = std::max(1u, std::min((rows + kTile - 1) / kTile, 152u * 4u));
-        k_mlp_infer<<<grid, kMlpThreads, sizeof(MlpSmemFwd), ctx.stream>>>(step_view(ctx, dt), M.theta, M.norm);
+        k_mlp_infer<<<grid, kMlpThreads, sizeof(MlpSmemFwd), ctx.stream>>>(step_view(ctx, dt), M.theta, M.norm,
+                                                                          M.blend_n, M.blend_t);
         ++n;
     }
     return n;

@@ -315,6 +315,30 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
         wdirty = false;
         __syncwarp();
     };
+    auto win_fits = [&](uint32_t x0, uint32_t x1) -> bool {  // this lane's slot takes a point of (x0, x1)
+        const uint32_t p0 = x0 | (x0 << 16), p1 = x1 | (x1 << 16);  // SIMD 16-bit compares
+        const uint32_t hit = (__vcmpeq2(ww0, p0) | __vcmpeq2(ww1, p0) | __vcmpeq2(ww2, p0)) |
+                             (__vcmpeq2(ww0, p1) | __vcmpeq2(ww1, p1) | __vcmpeq2(ww2, p1));
+        return (wcnt & 7u) < 4u && hit == 0u;
+    };
+    auto win_place = [&](uint32_t x0, uint32_t x1, uint32_t row) {  // one point into this lane's slot
+        const uint32_t kk = wcnt & 7u;
+        uint32_t nc = wcnt >> 5;
+        if (kk + 1 < 4u) {  // a full batch's codes are never read again
+            const uint32_t add[2] = {x0, x1};
+            for (int q = 0; q < 2; ++q, ++nc) {
+                const uint32_t sh = 16u * (nc & 1u), msk = ~(0xFFFFu << sh), v = add[q] << sh;
+                if (nc < 2u) ww0 = (ww0 & msk) | v;
+                else if (nc < 4u) ww1 = (ww1 & msk) | v;
+                else ww2 = (ww2 & msk) | v;
+            }
+        }
+        wcnt = (kk + 1) | (wcnt & (kFfH0 | kFfH1)) | (nc << 5);
+        wdirty = true;
+        uint32_t* r = rec(S, rb + wbid);
+        r[12 + kk] = row;
+        r[3] = kk + 1;
+    };
     auto win_load = [&]() {  // skip the dead prefix for good, then hold the next 32 slots
         for (;;) {
             const uint32_t i = head + lane;
@@ -383,28 +407,36 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
             const int hub = (int)((md >> 4) & 3u) - 1;
             if (hub < 0) {  // ---- fast path: the first np slots of the held window that fit
                 if (!win) win_load();
-                const bool fits = (wcnt & 7u) < 4u && !(ff_holds(ww0, x0) || ff_holds(ww1, x0) || ff_holds(ww2, x0) ||
-                                                       ff_holds(ww0, x1) || ff_holds(ww1, x1) || ff_holds(ww2, x1));
-                const unsigned okm = __ballot_sync(full, fits);
+                const unsigned okm = __ballot_sync(full, win_fits(x0, x1));
                 if ((uint32_t)__popc(okm) >= np) {
                     const uint32_t rank = __popc(okm & lt);
-                    if (fits && rank < np) {
-                        const uint32_t kk = wcnt & 7u;
-                        uint32_t nc = wcnt >> 5;
-                        if (kk + 1 < 4u) {  // a full batch's codes are never read again
-                            const uint32_t add[2] = {x0, x1};
-                            for (int q = 0; q < 2; ++q, ++nc) {
-                                const uint32_t sh = 16u * (nc & 1u), msk = ~(0xFFFFu << sh), v = add[q] << sh;
-                                if (nc < 2u) ww0 = (ww0 & msk) | v;
-                                else if (nc < 4u) ww1 = (ww1 & msk) | v;
-                                else ww2 = (ww2 & msk) | v;
-                            }
+                    const bool sel = ((okm >> lane) & 1u) && rank < np;
+                    // The next constraint rides along when it has no hub either: its fits are taken on
+                    // the same window state, minus the slots this one fills up and, if they share a
+                    // body, the slots this one takes.
+                    bool pair = false;
+                    uint32_t cB = 0, x0B = 0, x1B = 0, npB = 0;
+                    unsigned okB = 0;
+                    if (k + 1 < m) {
+                        const uint32_t mdB = __shfl_sync(full, meta, k + 1);
+                        const uint32_t cBs = __shfl_sync(full, mc, k + 1), xxB = __shfl_sync(full, dx, k + 1);
+                        if (!(mdB & 64u) && ((mdB >> 4) & 3u) == 0u) {
+                            cB = cBs;
+                            npB = mdB & 15u;
+                            x0B = xxB & 0xFFFFu;
+                            x1B = xxB >> 16;
+                            const bool share = x0 == x0B || x0 == x1B || x1 == x0B || x1 == x1B;
+                            const unsigned selm = __ballot_sync(full, sel);
+                            const unsigned fullm = __ballot_sync(full, sel && (wcnt & 7u) + 1u == 4u);
+                            okB = __ballot_sync(full, win_fits(x0B, x1B)) & ~fullm & (share ? ~selm : ~0u);
+                            pair = (uint32_t)__popc(okB) >= npB;
                         }
-                        wcnt = (kk + 1) | (wcnt & (kFfH0 | kFfH1)) | (nc << 5);
-                        wdirty = true;
-                        uint32_t* r = rec(S, rb + wbid);
-                        r[12 + kk] = 4u * c + rank;
-                        r[3] = kk + 1;
+                    }
+                    if (sel) win_place(x0, x1, 4u * c + rank);
+                    if (pair) {
+                        const uint32_t rankB = __popc(okB & lt);
+                        if (((okB >> lane) & 1u) && rankB < npB) win_place(x0B, x1B, 4u * cB + rankB);
+                        ++k;
                     }
                     continue;
                 }

@@ -119,18 +119,41 @@ __device__ __forceinline__ void warm_point(const SolveBufs& S, const View& V, ui
 // velocity recomputed before each axis), then normal; _mm_{add,sub,mul,min,max}_ps semantics.
 // Returns the point's share of the island residual: (sum over its rows of |dImpulse|,
 // (|n| + |t1|) + |t2| of its accumulated impulses).
-template <typename View>
-__device__ __forceinline__ float2 velocity_point_ab(const SolveBufs& S, const View& V, uint32_t row, uint32_t A,
-                                                   uint32_t B, uint32_t la, uint32_t lb) {
-    const Vec3 rA = V3(S.r.rAr[row]), rB = V3(S.r.rBr[row]);
-    const float4 n4 = S.r.n[row], t14 = S.r.t1[row], t24 = S.r.t2[row], m4 = S.r.mass[row];
-    const float4 im = S.r.imp[row];
+// Everything one velocity point reads besides the body velocities (loaded ahead of time by the
+// prefetching sweep).
+struct VelItem {
+    uint32_t row, A, B, la, lb;
+    float4 rA, rB, n, t1, t2, m, im;  // t1.w = friction
+    float nb, invA, invB;
+    Mat3 IA, IB;
+};
+
+__device__ __forceinline__ void load_vel_item(const SolveBufs& S, uint32_t row, uint32_t A, uint32_t B, uint32_t la,
+                                              uint32_t lb, VelItem& it) {
+    it.row = row; it.A = A; it.B = B; it.la = la; it.lb = lb;
+    it.rA = S.r.rAr[row];
+    it.rB = S.r.rBr[row];
+    it.n = S.r.n[row];
+    it.t1 = S.r.t1[row];
+    it.t2 = S.r.t2[row];
+    it.m = S.r.mass[row];
+    it.im = S.r.imp[row];
     const float4 bias = S.r.bias[row];
-    const float invA = S.b.inv_mass[A], invB = S.b.inv_mass[B];
-    const Mat3 IA = M3(&S.b.iiw[3 * A]), IB = M3(&S.b.iiw[3 * B]);
+    it.nb = bias.x + (S.vel_bias ? bias.y : 0.0f);
+    it.invA = S.b.inv_mass[A];
+    it.invB = S.b.inv_mass[B];
+    it.IA = M3(&S.b.iiw[3 * A]);
+    it.IB = M3(&S.b.iiw[3 * B]);
+}
+
+// One lane of SolveVelocityBatchSIMD on a loaded item.
+template <typename View>
+__device__ __forceinline__ float2 velocity_item(const SolveBufs& S, const View& V, const VelItem& it) {
+    const Vec3 rA = V3(it.rA), rB = V3(it.rB);
+    const float4 n4 = it.n, t14 = it.t1, t24 = it.t2, m4 = it.m, im = it.im;
+    const float invA = it.invA, invB = it.invB, nb = it.nb, fric = t14.w;
+    const uint32_t A = it.A, B = it.B, la = it.la, lb = it.lb;
     Vec3 vA = V.lin(la, A), wA = V.ang(la, A), vB = V.lin(lb, B), wB = V.ang(lb, B);
-    const float nb = bias.x + (S.vel_bias ? bias.y : 0.0f);
-    const float fric = t14.w;
     float nacc = im.x, t1acc = im.y, t2acc = im.z;
     float dsum = 0.0f;
 #pragma unroll
@@ -161,14 +184,22 @@ __device__ __forceinline__ float2 velocity_point_ab(const SolveBufs& S, const Vi
         dsum += fabsf(dl);
         const Vec3 imp(dir.x * dl, dir.y * dl, dir.z * dl);
         vA = Vec3(vA.x + imp.x * invA, vA.y + imp.y * invA, vA.z + imp.z * invA);
-        wA = wA + IA * rA.cross(imp);
+        wA = wA + it.IA * rA.cross(imp);
         vB = Vec3(vB.x - imp.x * invB, vB.y - imp.y * invB, vB.z - imp.z * invB);
-        wB = wB - IB * rB.cross(imp);
+        wB = wB - it.IB * rB.cross(imp);
     }
     if (la != kNone) V.put(la, A, vA, wA);
     if (lb != kNone) V.put(lb, B, vB, wB);
-    S.r.imp[row] = make_float4(nacc, t1acc, t2acc, im.w);
+    S.r.imp[it.row] = make_float4(nacc, t1acc, t2acc, im.w);
     return make_float2(dsum, (fabsf(nacc) + fabsf(t1acc)) + fabsf(t2acc));
+}
+
+template <typename View>
+__device__ __forceinline__ float2 velocity_point_ab(const SolveBufs& S, const View& V, uint32_t row, uint32_t A,
+                                                   uint32_t B, uint32_t la, uint32_t lb) {
+    VelItem it;
+    load_vel_item(S, row, A, B, la, lb, it);
+    return velocity_item(S, V, it);
 }
 
 template <typename View>
@@ -460,7 +491,7 @@ __global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, Count
 // One CTA is bound by its own L2 bandwidth and latency on every level; here kClusterCtas CTAs on
 // as many SMs share each level, the island's velocities live in their distributed shared memory
 // (ClusterView) and a hardware cluster barrier separates the levels.
-constexpr uint32_t kClusterThreads = 512;
+constexpr uint32_t kClusterThreads = 256;
 constexpr uint32_t kClusterSlots = 6144;  // bodies per CTA: 2 x 16 B x 6144 = 192 KB
 
 // Level barrier and residual sums over the whole cluster: every CTA sums its warps into its own
@@ -498,6 +529,88 @@ struct ClusterSync {
     }
 };
 
+// Warm start + velocity sweeps of a cluster island, prefetching: before it solves its point of a
+// level, every thread loads its point of the next level (row data, masses, inertias: nothing that
+// the current level writes), so after each barrier only the velocity loads stand between it and
+// its math.  Items are 16-byte records {row, A, B, local A | local B << 16} built up front.
+template <typename Sync, typename View>
+__device__ void solve_velocity_pf(const SolveBufs& S, uint32_t isl, const View& V, uint32_t gtid, uint32_t gthreads,
+                                  Sync sync, Counters* cnt) {
+    const uint32_t base = 4u * S.isl_start[isl], loff = base + isl;
+    const uint32_t nw = S.meta[4 * isl], nv = S.meta[4 * isl + 1];
+    const uint32_t total = S.vl_off[loff + nv];
+    for (uint32_t k = gtid; k < total; k += gthreads) {
+        const uint32_t row = S.vl_list[base + k], c = row >> 2;
+        const uint32_t la = S.con_la[c], lb = S.con_lb[c];
+        S.vrec[base + k] = make_uint4(row, S.con_a[c], S.con_b[c],
+                                      (la == kNone ? 0xFFFFu : la) | ((lb == kNone ? 0xFFFFu : lb) << 16));
+    }
+    sync.reset(gtid);
+    for (uint32_t l = 0; l < nw; ++l) {
+        const uint32_t e = S.wl_off[loff + l + 1];
+        for (uint32_t k = S.wl_off[loff + l] + gtid; k < e; k += gthreads) warm_point(S, V, S.wl_list[base + k]);
+        sync();
+    }
+    auto rec_at = [&](uint32_t l) -> uint4 {
+        const uint32_t lo = S.vl_off[loff + l];
+        return lo + gtid < S.vl_off[loff + l + 1] ? S.vrec[base + lo + gtid] : make_uint4(kNone, 0u, 0u, 0u);
+    };
+    auto unpack = [&](const uint4& r, VelItem& it) {
+        const uint32_t la = r.w & 0xFFFFu, lb = r.w >> 16;
+        load_vel_item(S, r.x, r.y, r.z, la == 0xFFFFu ? kNone : la, lb == 0xFFFFu ? kNone : lb, it);
+    };
+    const bool residual = S.res_tol > 0.0f;
+    const uint32_t iters = residual ? S.res_cap : S.vel_iters;
+    uint32_t used = 0;
+    float res = 0.0f;
+    VelItem cur;
+    bool has_cur = false;
+    uint4 rnext = make_uint4(kNone, 0u, 0u, 0u);
+    if (iters && nv) {
+        const uint4 r0 = rec_at(0);
+        has_cur = r0.x != kNone;
+        if (has_cur) unpack(r0, cur);
+        rnext = rec_at(1 % nv);
+    }
+    for (uint32_t it = 0; it < iters; ++it) {
+        unsigned long long sd = 0, sl = 0;
+        for (uint32_t l = 0; l < nv; ++l) {
+            VelItem nxt;
+            const bool has_nxt = rnext.x != kNone;
+            if (has_nxt) unpack(rnext, nxt);                // the next level's point (wraps to level 0)
+            const uint4 rnn = rec_at(l + 2 < nv ? l + 2 : l + 2 - nv);
+            if (has_cur) {
+                const float2 q = velocity_item(S, V, cur);
+                sd += res_fixed(q.x);
+                sl += res_fixed(q.y);
+            }
+            const uint32_t hi = S.vl_off[loff + l + 1];
+            for (uint32_t k = S.vl_off[loff + l] + gtid + gthreads; k < hi; k += gthreads) {  // wide levels
+                VelItem x;
+                unpack(S.vrec[base + k], x);
+                const float2 q = velocity_item(S, V, x);
+                sd += res_fixed(q.x);
+                sl += res_fixed(q.y);
+            }
+            sync();
+            cur = nxt;
+            has_cur = has_nxt;
+            rnext = rnn;
+        }
+        used = it + 1;
+        if (residual || used == iters) {
+            sync.sum2(sd, sl, it);
+            res = sl ? (float)((double)sd / (double)sl) : (sd ? 1.0f : 0.0f);
+            if (residual && (double)sd <= (double)S.res_tol * (double)sl) break;
+        }
+    }
+    if (gtid == 0) {
+        atomicMax(&cnt->max_iters, used);
+        atomicAdd(&cnt->pt_iters, total * used);
+        atomicMax(&cnt->res_bits, __float_as_uint(res));
+    }
+}
+
 // Islands with more than smem_bodies and at most kClusterCtas * kClusterSlots dynamic bodies.
 __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads, 1)
     k_solve_cluster(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
@@ -522,7 +635,10 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
             sw[l / kClusterCtas] = S.b.av[bodies[l]];
         }
         cl.sync();
-        solve_velocity(S, isl, V, gtid, gthreads, sync, cnt);
+        if (S.meta[4 * isl + 1] >= 2)  // prefetching needs two distinct levels
+            solve_velocity_pf(S, isl, V, gtid, gthreads, sync, cnt);
+        else
+            solve_velocity(S, isl, V, gtid, gthreads, sync, cnt);
         for (uint32_t l = rank + kClusterCtas * tid; l < nloc; l += gthreads) {
             S.b.lv[bodies[l]] = sv[l / kClusterCtas];
             S.b.av[bodies[l]] = sw[l / kClusterCtas];

@@ -318,27 +318,29 @@ __global__ void k_build_constraints(const uint2* __restrict__ pairs, const uint3
                 float4 im = c_imp[4u * slot + bi];
                 ni = im.x; t1 = im.y; t2 = im.z;
             } else if (miss_rows) {
-                // cache miss: remember the pair's nearest cached point at any distance (a feature
-                // of the learned warm start), then the reference's zero start stands
+                // cache miss: remember the pair's nearest cached point at any distance and the
+                // pair's cached normal impulse per current point (features of the learned warm
+                // start), then the reference's zero start stands
                 uint32_t nk = kInvalid;
-                float nd = 0.0f;
+                float nd = 0.0f, sum_n = 0.0f;
                 for (uint32_t k = 0; k < cn; ++k) {
                     float d = (V3(c_pos[4u * slot + k]) - pa).len2();
                     if (nk == kInvalid || d < nd) { nd = d; nk = k; }
+                    sum_n += c_imp[4u * slot + k].x;
                 }
                 const uint32_t m = atomicAdd(&cnt->nmiss, 1u);
                 miss_rows[m] = row;
-                float4 pr = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+                float4 pr = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 if (nk != kInvalid) {
                     const float4 im = c_imp[4u * slot + nk];
-                    pr = make_float4(im.x, im.y, im.z, sqrtf(nd));
+                    pr = make_float4(im.x, im.y, im.z, sum_n / (float)n);
                 }
                 miss_prior[m] = pr;
             }
         } else if (warm && miss_rows) {
             const uint32_t m = atomicAdd(&cnt->nmiss, 1u);
             miss_rows[m] = row;
-            miss_prior[m] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+            miss_prior[m] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
         r.imp[row] = make_float4(ni, t1, t2, 0.0f);
     }

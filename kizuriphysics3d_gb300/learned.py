@@ -45,6 +45,8 @@ class WarmStartModel:
     theta: np.ndarray  # MLP_PARAMS float32
     mean: np.ndarray   # 24
     std: np.ndarray    # 24
+    blend: float = 1.0          # fraction of the normal prediction used (chosen on held-out scenes)
+    blend_tangent: float = 0.0  # fraction of the tangent predictions used
 
     @staticmethod
     def init(mean: np.ndarray, std: np.ndarray, seed: int = 0) -> "WarmStartModel":
@@ -57,17 +59,20 @@ class WarmStartModel:
         return WarmStartModel(theta.astype(np.float32), np.asarray(mean, np.float32), np.asarray(std, np.float32))
 
     def save(self, path: str, meta: Optional[dict] = None):
-        np.savez(path, theta=self.theta, mean=self.mean, std=self.std,
-                 meta=json.dumps(meta or {}))
+        np.savez(path, theta=self.theta, mean=self.mean, std=self.std, blend=np.float32(self.blend),
+                 blend_tangent=np.float32(self.blend_tangent), meta=json.dumps(meta or {}))
 
     @staticmethod
     def load(path: str = MODEL_PATH) -> "WarmStartModel":
         with np.load(path) as z:
+            blend = float(z["blend"]) if "blend" in z.files else 1.0
+            bt = float(z["blend_tangent"]) if "blend_tangent" in z.files else 0.0
             return WarmStartModel(z["theta"].astype(np.float32), z["mean"].astype(np.float32),
-                                  z["std"].astype(np.float32))
+                                  z["std"].astype(np.float32), blend, bt)
 
     def apply(self, world: World, enable: bool = True):
         world.mlp_set_params(self.theta, self.mean, self.std)
+        world.mlp_set_blend(self.blend, self.blend_tangent)
         world.mlp_enable(enable)
 
 
@@ -90,8 +95,9 @@ def collect(scene: scenes.Scene, steps: int, skip: int = 0, iterations: int = 64
 
 
 def train(samples: np.ndarray, model: WarmStartModel, epochs: int = 20, batch: int = 4096, lr: float = 1e-3,
-          seed: int = 0, world: Optional[World] = None, log=None) -> List[float]:
-    """Adam on the mean-squared error of the valid targets, on the GPU.  Returns the epoch losses."""
+          seed: int = 0, world: Optional[World] = None, log=None, quantile: float = 0.0) -> List[float]:
+    """Adam on the valid targets, on the GPU: squared error, or with 0 < quantile < 1 the pinball
+    loss of that quantile.  Returns the epoch losses."""
     own = world is None
     if own:
         world = World(scenes.pyramid(1))
@@ -99,6 +105,7 @@ def train(samples: np.ndarray, model: WarmStartModel, epochs: int = 20, batch: i
         rng = np.random.default_rng(seed)
         order = rng.permutation(samples.shape[0])
         world.mlp_set_params(model.theta, model.mean, model.std)
+        world.mlp_set_quantile(quantile)
         world.mlp_set_dataset(to_network_targets(samples[order]))
         n = samples.shape[0]
         losses = []
@@ -143,32 +150,34 @@ def evaluate(scene: scenes.Scene, model: Optional[WarmStartModel], steps: int, s
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--out", default=MODEL_PATH)
-    ap.add_argument("--pile-steps", type=int, default=240)
-    ap.add_argument("--pile-skip", type=int, default=120)
-    ap.add_argument("--field-steps", type=int, default=6)
-    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--per-source", type=int, default=60000, help="samples kept from each source")
+    ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--lr", type=float, default=1e-3)
-    ap.add_argument("--save-samples", default=None, help="also write the collected samples (.npz)")
+    ap.add_argument("--save-samples", default=None, help="also write the training samples (.npz)")
     args = ap.parse_args()
     t0 = time.time()
     log = lambda m: print(f"[{time.time() - t0:7.1f} s] {m}", flush=True)
+    rng = np.random.default_rng(0)
+    keep = lambda a: a[np.sort(rng.permutation(a.shape[0])[:args.per_source])]
     pile = scenes.pile(20000, seed=1234)
-    s1 = collect(pile, args.pile_steps, args.pile_skip, max_pairs=48 * 20001)
-    log(f"random convex pile (seed 1234): {s1.shape[0]} samples")
-    field = scenes.stacks(20, 20, 500)
-    s2 = collect(field, args.field_steps, 0, max_pairs=4 * 200_401)
-    keep = np.random.default_rng(7).permutation(s2.shape[0])[:s1.shape[0]]  # as many as the pile gave
-    s2 = s2[np.sort(keep)]
-    log(f"large box field (seed 7): {s2.shape[0]} samples")
-    samples = np.concatenate([s1, s2])
-    if args.save_samples:  # a 100k subsample of each source, for inspection
-        sub = lambda a: a[np.sort(np.random.default_rng(0).permutation(a.shape[0])[:100000])]
-        np.savez_compressed(args.save_samples, pile=sub(s1), field=sub(s2))
+    falling = keep(collect(pile, 200, 150, max_pairs=48 * 20001))
+    snap = os.path.join(HERE, "data", "pile20000_step600.npz")
+    with np.load(snap) as z:
+        state = z["state"]
+    settled_scene = scenes.pile(20000, seed=1234)
+    for b, st in zip(settled_scene.bodies, state):
+        b.pos, b.rot, b.vel, b.ang = tuple(st[0:3]), tuple(st[3:7]), tuple(st[7:10]), tuple(st[10:13])
+    settled = keep(collect(settled_scene, 40, 5, max_pairs=48 * 20001))
+    field = keep(collect(scenes.stacks(20, 20, 500), 4, 0, max_pairs=4 * 200_401))
+    log(f"samples: pile falling {falling.shape[0]}, pile settled {settled.shape[0]}, box field {field.shape[0]}")
+    samples = np.concatenate([falling, settled, field])
+    if args.save_samples:
+        np.savez_compressed(args.save_samples, pile=falling, settled=settled, field=field)
     mean, std = feature_stats(samples)
     model = WarmStartModel.init(mean, std, seed=0)
-    losses = train(samples, model, epochs=args.epochs, lr=args.lr, log=log)
-    model.save(args.out, {"samples": int(samples.shape[0]), "losses": losses, "pile_steps": args.pile_steps,
-                          "pile_skip": args.pile_skip, "field_steps": args.field_steps, "epochs": args.epochs})
+    losses = train(samples, model, epochs=args.epochs, batch=2048, lr=args.lr, log=log)
+    model.blend, model.blend_tangent = 1.0, 0.0  # normal impulse only: tangent predictions hurt
+    model.save(args.out, {"samples": int(samples.shape[0]), "losses": losses, "epochs": args.epochs})
     log(f"saved {args.out}")
 
 

@@ -180,6 +180,19 @@ class World:
             setattr(self._ss, k, v)
         self._check(capi.load().kzg_set_solver_settings(self._h, ctypes.byref(self._ss)))
 
+    def snapshot(self) -> bytes:
+        """Device state and manifold cache (kzg_snapshot_save): restore() resumes bit-exactly."""
+        L = capi.load()
+        n = ctypes.c_size_t()
+        self._check(L.kzg_snapshot_size(self._h, ctypes.byref(n)))
+        buf = np.zeros(n.value, np.uint8)
+        self._check(L.kzg_snapshot_save(self._h, capi.ptr(buf), n.value))
+        return buf.tobytes()
+
+    def restore(self, snap: bytes):
+        buf = np.frombuffer(snap, np.uint8).copy()
+        self._check(capi.load().kzg_snapshot_load(self._h, capi.ptr(buf), buf.size))
+
     def set_graph(self, enabled: bool = True):
         """Step through a captured CUDA graph (step_fixed(n) then launches n steps back to back)."""
         self._check(capi.load().kzg_set_graph(self._h, int(bool(enabled))))
@@ -312,6 +325,12 @@ class World:
 
     def mlp_enable(self, on: bool = True):
         self._check(capi.load().kzg_mlp_enable(self._h, int(bool(on))))
+
+    def mlp_set_blend(self, normal: float, tangent: float):
+        self._check(capi.load().kzg_mlp_set_blend(self._h, np.float32(normal), np.float32(tangent)))
+
+    def mlp_set_quantile(self, tau: float):
+        self._check(capi.load().kzg_mlp_set_quantile(self._h, np.float32(tau)))
 
     def mlp_log_begin(self, capacity: int):
         self._check(capi.load().kzg_mlp_log_begin(self._h, int(capacity)))

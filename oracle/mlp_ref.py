@@ -58,8 +58,9 @@ def forward(theta, mean, std, x_raw, bf=True):
     return {"X": X, "H1": H1, "H2": H2, "Y": Y}
 
 
-def loss_and_grad(theta, mean, std, samples, bf=True):
-    """Mean-squared error over the valid targets and its gradient w.r.t. theta."""
+def loss_and_grad(theta, mean, std, samples, bf=True, tau=0.0):
+    """Loss over the valid targets (squared error, or with tau > 0 the pinball loss of quantile
+    tau) and its gradient w.r.t. theta."""
     s = np.asarray(samples, np.float64)
     x_raw, tgt, msk = s[:, :F], s[:, F:F + O], s[:, F + O:F + 2 * O]
     r = bf16 if bf else (lambda a: np.asarray(a, np.float64))
@@ -69,8 +70,12 @@ def loss_and_grad(theta, mean, std, samples, bf=True):
     nvalid = msk.sum()
     inv = 1.0 / nvalid if nvalid > 0 else 0.0
     e = Y - tgt
-    loss = float((msk * e * e).sum() * inv)
-    dy = msk * 2.0 * e * inv
+    if tau > 0.0:
+        loss = float((msk * np.where(e > 0, (1.0 - tau) * e, -tau * e)).sum() * inv)
+        dy = msk * np.where(e > 0, 1.0 - tau, -tau) * inv
+    else:
+        loss = float((msk * e * e).sum() * inv)
+        dy = msk * 2.0 * e * inv
     dYb = r(dy)
     dW3 = dYb.T @ H2
     db3 = dy.sum(0)

@@ -146,6 +146,38 @@ def test_graph_stepping_matches_direct_stepping(kzg_lib):
         assert b.get_stats()["max_velocity_iterations_used"] == a.get_stats()["max_velocity_iterations_used"]
 
 
+def test_snapshot_resumes_bit_exactly(kzg_lib):
+    """kzg_snapshot_save / load: a second context restored from a snapshot continues bit-exactly;
+    restoring the body state alone (cold manifold cache) does not, which is what the cache part of
+    the snapshot is for."""
+    from kizuriphysics3d_gb300 import World, resolve, scenes
+    sc = scenes.pile(500, seed=12, extent=4.0, y_range=(1.0, 10.0))
+    res = resolve(sc)
+    with World(sc, resolved=res) as a, World(sc, resolved=res) as b, World(sc, resolved=res) as c:
+        a.step_fixed(n=60)
+        snap, state60 = a.snapshot(), a.state()
+        a.step_fixed(n=40)
+        b.restore(snap)
+        b.step_fixed(n=40)
+        assert b.compute_state_hash() == a.compute_state_hash()
+        assert np.array_equal(bits(b.state()), bits(a.state()))
+        c.set_state(state60)
+        c.step_fixed(n=40)
+        assert c.compute_state_hash() != a.compute_state_hash()
+
+
+def test_kzp1_world_steps_like_the_scene(kzg_lib):
+    """A world loaded from KZP1 bytes of a box scene (no hulls to rebuild) steps to the same state
+    as the scene it was written from."""
+    from kizuriphysics3d_gb300 import World, kzp1, scenes
+    sc = scenes.pyramid(6)
+    back = kzp1.from_kzp1(kzp1.to_kzp1(sc), template=sc)
+    with World(sc) as a, World(back) as b:
+        a.step_fixed(n=50)
+        b.step_fixed(n=50)
+        assert a.compute_state_hash() == b.compute_state_hash()
+
+
 def test_hash_identical_run_to_run(kzg_lib):
     from kizuriphysics3d_gb300 import World, resolve, scenes
     sc = scenes.pile(800, seed=5, extent=4.0, y_range=(1.0, 12.0))

@@ -94,3 +94,39 @@ def test_merge_worlds_remaps_shapes_and_tags_bodies():
     worlds = scenes.world_batch(16, seed=4242)
     sizes = [len(w.bodies) - 1 for w in worlds]  # minus the plane
     assert all(s >= 1 for s in sizes)
+
+
+def test_kzp1_round_trip():
+    """KZP1 (the reference's world file, Serializer.cpp): write, read back, write again - identical
+    bytes; every BodySettings field and shape parameter survives; hulls are stored as vertices."""
+    import struct
+    from kizuriphysics3d_gb300 import kzp1, scenes
+    sc = scenes.pile(24, seed=5, extent=2.0)
+    sc.bodies[3].friction = 0.25
+    sc.bodies[4].flags = scenes.BODY_FLAG_SENSOR
+    sc.bodies[5].mass_override = 7.5
+    data = kzp1.to_kzp1(sc)
+    assert struct.unpack_from("<III", data) == (0x31505A4B, 1, len(sc.bodies))
+    back = kzp1.from_kzp1(data, template=sc)
+    assert len(back.bodies) == len(sc.bodies)
+    for a, b in zip(sc.bodies, back.bodies):
+        assert np.allclose(a.pos, b.pos) and np.allclose(a.rot, b.rot)
+        for f in ("motion", "layer", "mask", "flags"):
+            assert getattr(a, f) == getattr(b, f), f
+        for f in ("friction", "restitution", "linear_damping", "angular_damping", "gravity_factor",
+                  "max_linear_velocity", "max_angular_velocity", "density", "mass_override"):
+            assert np.float32(getattr(a, f)) == np.float32(getattr(b, f)), f
+        sa, sb = sc.shapes[a.shape], back.shapes[b.shape]
+        assert sa.type == sb.type
+        if sa.type != scenes.SHAPE_HULL:
+            assert np.allclose(sa.params, sb.params)
+    # a hull is rebuilt from its stored vertices on load (as the reference does): same vertex set
+    again = kzp1.from_kzp1(kzp1.to_kzp1(back), template=sc)
+    for a, b in zip(back.bodies, again.bodies):
+        sa, sb = back.shapes[a.shape], again.shapes[b.shape]
+        if sa.type == scenes.SHAPE_HULL:
+            assert np.array_equal(np.unique(sa.points, axis=0), np.unique(sb.points, axis=0))
+    pyr = scenes.pyramid(4)
+    assert kzp1.to_kzp1(kzp1.from_kzp1(kzp1.to_kzp1(pyr), template=pyr)) == kzp1.to_kzp1(pyr)
+    with pytest.raises(ValueError):
+        kzp1.from_kzp1(data[:-3])
