@@ -145,6 +145,8 @@ struct Ctx {
     uint32_t* isl_pts = nullptr;      // first point slot of each island in the level lists
     uint32_t* lvl_count = nullptr;    // per island level counters (4*ncons + nislands + 1)
     uint4* brec = nullptr;            // batch records, 64 B each (4*ncons + nislands + 1)
+    float4* pk = nullptr;             // packed velocity items of cluster islands (kPackArrays x pk_cap per cluster)
+    uint32_t pk_cap = 0;
     uint32_t* last_g = nullptr;       // level tables that do not fit shared memory (3 x 2*ncons)
     uint32_t *first_w = nullptr, *first_b = nullptr;  // per sorted constraint: first warm / bias level
     uint32_t* lvl_tmp = nullptr;      // per point: velocity level (batch order)

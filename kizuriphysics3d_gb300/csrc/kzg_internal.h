@@ -14,6 +14,9 @@ struct Ctx;
 
 size_t cub_temp_bytes(uint32_t max_items);
 cudaError_t configure_kernels();  // per-device kernel attributes (large dynamic shared memory)
+// Packed-item scratch of the cluster solve for `points` point rows: entries per cluster island
+// (cap) and float4 elements to allocate.
+size_t pack_elements(uint32_t points, uint32_t* cap);
 kzg_status step_canonical(Ctx& ctx, float dt, uint32_t nsteps);
 kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t num_pairs, float dt);
 kzg_status hash_state(Ctx& ctx, uint64_t* out);

@@ -130,10 +130,12 @@ __device__ __forceinline__ uint32_t level_window(uint32_t* last, bool valid, uin
 }
 
 // Counting sort of one sweep's points by level into list/off (order inside a level is free).
+// The level counters live in shared memory (scnt, scap words) when they fit.
 template <typename Sync, typename Emit>
 __device__ void level_sort(const SchedBufs& S, uint32_t loff, uint32_t base, uint32_t nlev, uint32_t tid,
-                           uint32_t nthreads, uint32_t* tmp, uint32_t* list, uint32_t* off, Emit emit, Sync sync) {
-    uint32_t* cnt = S.lvl_count + loff;
+                           uint32_t nthreads, uint32_t* tmp, uint32_t* list, uint32_t* off, Emit emit, Sync sync,
+                           uint32_t* scnt = nullptr, uint32_t scap = 0) {
+    uint32_t* cnt = (scnt && nlev < scap) ? scnt : S.lvl_count + loff;
     for (uint32_t l = tid; l <= nlev; l += nthreads) cnt[l] = 0;
     sync();
     emit([&](uint32_t lvl, uint32_t) { atomicAdd(&cnt[lvl - 1], 1u); });
@@ -704,11 +706,12 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
 
     // ---- E: sort each sweep's points by level
     const uint32_t nv = sh->nv, nw = sh->nw, nb = sh->nb;
+    const uint32_t scap = nthreads >= 64 ? 3u * last_cap : 0u;  // CTA: the level tables' shared memory is free now
     level_sort(S, loff, base, nv, tid, nthreads, tmp, S.vl_list, S.vl_off,
                [&](auto put) {
                    for (uint32_t i = tid; i < nvit; i += nthreads) put(S.vlev[base + i], S.vitems[base + i]);
                },
-               sync);
+               sync, last_sm, scap);
     level_sort(S, loff, base, nw, tid, nthreads, tmp, S.wl_list, S.wl_off,
                [&](auto put) {
                    for (uint32_t s = s0 + tid; s < s1; s += nthreads) {
@@ -716,7 +719,7 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
                        for (uint32_t p = 0; p < S.con_np[c]; ++p) put(f + p, 4u * c + p);
                    }
                },
-               sync);
+               sync, last_sm, scap);
     level_sort(S, loff, base, nb, tid, nthreads, tmp, S.bl_list, S.bl_off,
                [&](auto put) {
                    for (uint32_t s = s0 + tid; s < s1; s += nthreads) {
@@ -728,7 +731,7 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
                            if (S.bias[4u * c + p].y > 0.0f) put(f + k++, 4u * c + p);
                    }
                },
-               sync);
+               sync, last_sm, scap);
 
     if (tid == 0) {
         S.meta[4 * isl + 0] = nw;

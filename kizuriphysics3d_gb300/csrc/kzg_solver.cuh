@@ -35,6 +35,8 @@ struct SolveBufs {
     uint32_t res_cap;  // their cap
     uint4* vrec;       // big islands: per velocity item {row, A, B, dynamic A | dynamic B << 1} (reuses
                        // the batch-record buffer, free once the schedule is built)
+    float4* pk;        // cluster islands: packed velocity items, kPackArrays x pk_cap per cluster
+    uint32_t pk_cap;   // points per cluster island (0: no cluster solve)
 };
 
 // Velocity storage of one island: staged in shared memory (local index) or read/written in place
@@ -71,7 +73,7 @@ struct VelView {
 // Velocity storage of a giant island spread over the shared memory of a thread-block cluster:
 // local body l lives in CTA l % kClusterCtas, slot l / kClusterCtas, read and written through
 // distributed shared memory.
-constexpr uint32_t kClusterCtas = 8;
+constexpr uint32_t kClusterCtas = 16;
 struct ClusterView {
     float4* v;  // this CTA's arrays; the same offsets in every CTA of the cluster
     float4* w;
@@ -146,14 +148,14 @@ __device__ __forceinline__ void load_vel_item(const SolveBufs& S, uint32_t row, 
     it.IB = M3(&S.b.iiw[3 * B]);
 }
 
-// One lane of SolveVelocityBatchSIMD on a loaded item.
-template <typename View>
-__device__ __forceinline__ float2 velocity_item(const SolveBufs& S, const View& V, const VelItem& it) {
-    const Vec3 rA = V3(it.rA), rB = V3(it.rB);
-    const float4 n4 = it.n, t14 = it.t1, t24 = it.t2, m4 = it.m, im = it.im;
-    const float invA = it.invA, invB = it.invB, nb = it.nb, fric = t14.w;
-    const uint32_t A = it.A, B = it.B, la = it.la, lb = it.lb;
-    Vec3 vA = V.lin(la, A), wA = V.ang(la, A), vB = V.lin(lb, B), wB = V.ang(lb, B);
+// The three rows of one lane of SolveVelocityBatchSIMD on loaded data: updates the body
+// velocities and the accumulated impulses im (normal, t1, t2) in place and returns the point's
+// residual shares.
+__device__ __forceinline__ float2 velocity_rows(const Vec3& rA, const Vec3& rB, const float4& n4, const float4& t14,
+                                                const float4& t24, const float4& m4, float invA, float invB, float nb,
+                                                const Mat3& IA, const Mat3& IB, Vec3& vA, Vec3& wA, Vec3& vB,
+                                                Vec3& wB, float4& im) {
+    const float fric = t14.w;
     float nacc = im.x, t1acc = im.y, t2acc = im.z;
     float dsum = 0.0f;
 #pragma unroll
@@ -184,14 +186,26 @@ __device__ __forceinline__ float2 velocity_item(const SolveBufs& S, const View& 
         dsum += fabsf(dl);
         const Vec3 imp(dir.x * dl, dir.y * dl, dir.z * dl);
         vA = Vec3(vA.x + imp.x * invA, vA.y + imp.y * invA, vA.z + imp.z * invA);
-        wA = wA + it.IA * rA.cross(imp);
+        wA = wA + IA * rA.cross(imp);
         vB = Vec3(vB.x - imp.x * invB, vB.y - imp.y * invB, vB.z - imp.z * invB);
-        wB = wB - it.IB * rB.cross(imp);
+        wB = wB - IB * rB.cross(imp);
     }
+    im = make_float4(nacc, t1acc, t2acc, im.w);
+    return make_float2(dsum, (fabsf(nacc) + fabsf(t1acc)) + fabsf(t2acc));
+}
+
+// One lane of SolveVelocityBatchSIMD on a loaded item.
+template <typename View>
+__device__ __forceinline__ float2 velocity_item(const SolveBufs& S, const View& V, const VelItem& it) {
+    const uint32_t A = it.A, B = it.B, la = it.la, lb = it.lb;
+    Vec3 vA = V.lin(la, A), wA = V.ang(la, A), vB = V.lin(lb, B), wB = V.ang(lb, B);
+    float4 im = it.im;
+    const float2 q = velocity_rows(V3(it.rA), V3(it.rB), it.n, it.t1, it.t2, it.m, it.invA, it.invB, it.nb, it.IA,
+                                   it.IB, vA, wA, vB, wB, im);
     if (la != kNone) V.put(la, A, vA, wA);
     if (lb != kNone) V.put(lb, B, vB, wB);
-    S.r.imp[it.row] = make_float4(nacc, t1acc, t2acc, im.w);
-    return make_float2(dsum, (fabsf(nacc) + fabsf(t1acc)) + fabsf(t2acc));
+    S.r.imp[it.row] = im;
+    return q;
 }
 
 template <typename View>
@@ -468,15 +482,16 @@ __device__ void solve_velocity_big(const SolveBufs& S, uint32_t isl, uint32_t* s
     }
 }
 
-// cluster_max: islands up to this many bodies are solved by k_solve_cluster (0: none).
-__global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, Counters* cnt, uint32_t smem_bodies,
-                                                              uint32_t cluster_max) {
+__device__ __forceinline__ bool cluster_island(const SolveBufs& S, uint32_t isl, uint32_t smem_bodies);
+
+// Large islands that neither one CTA's shared memory nor (when S.pk_cap > 0) a cluster takes.
+__global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
     __shared__ unsigned long long red[6];
     __shared__ uint32_t soff[kBigOffs + 1];
     const uint32_t n = cnt->nlarge;
     for (uint32_t idx = blockIdx.x; idx < n; idx += gridDim.x) {
         const uint32_t isl = S.large_list[idx];
-        if (S.meta[4 * isl + 3] <= smem_bodies || S.meta[4 * isl + 3] <= cluster_max) continue;
+        if (S.meta[4 * isl + 3] <= smem_bodies || (S.pk_cap && cluster_island(S, isl, smem_bodies))) continue;
         const VelView P{S.b.plv, S.b.pav, S.b.lv, S.b.av, false};
         solve_velocity_big(S, isl, soff, red, cnt);
         solve_bias(S, isl, P, threadIdx.x, blockDim.x, CtaSync{red});
@@ -529,73 +544,145 @@ struct ClusterSync {
     }
 };
 
-// Warm start + velocity sweeps of a cluster island, prefetching: before it solves its point of a
-// level, every thread loads its point of the next level (row data, masses, inertias: nothing that
-// the current level writes), so after each barrier only the velocity loads stand between it and
-// its math.  Items are 16-byte records {row, A, B, local A | local B << 16} built up front.
-template <typename Sync, typename View>
-__device__ void solve_velocity_pf(const SolveBufs& S, uint32_t isl, const View& V, uint32_t gtid, uint32_t gthreads,
-                                  Sync sync, Counters* cnt) {
+// Packed velocity items of a cluster island, in the island's velocity-level order: kPackArrays
+// float4 arrays of pk_cap entries per cluster (structure of arrays).  The points a warp solves in
+// one level are consecutive, so every field is one coalesced 16-byte load with no index to chase,
+// and a point is packed, read and updated by the one thread that solves it.
+//   0 rA, inverse mass A     1 rB, inverse mass B      2 normal, velocity bias   3 t1, friction
+//   4 t2, local A            5 masses, local B         6-10 inverse inertias of A and B (9 + 9
+//   floats), 10.z = row      11 accumulated impulses   12, 13 linear and angular velocity of the
+//   body that is not dynamic (constant during the solve; zero when both are dynamic)
+constexpr uint32_t kPackArrays = 14;
+constexpr uint32_t kPackCapMax = 1u << 19;
+constexpr uint32_t kClusterGrid = 2;     // clusters launched; more giant islands queue on them
+constexpr uint32_t kClusterOffs = 4096;  // velocity levels staged in shared memory
+
+struct PackItem {
+    float4 q[kPackArrays];
+};
+
+__device__ __forceinline__ void pack_item(const SolveBufs& S, float4* pk, uint32_t cap, uint32_t k, uint32_t row) {
+    const uint32_t c = row >> 2;
+    const uint32_t A = S.con_a[c], B = S.con_b[c], la = S.con_la[c], lb = S.con_lb[c];
+    const float4 rA = S.r.rAr[row], rB = S.r.rBr[row], bias = S.r.bias[row];
+    const float4 n = S.r.n[row], t2 = S.r.t2[row], m = S.r.mass[row];
+    const Mat3 IA = M3(&S.b.iiw[3 * A]), IB = M3(&S.b.iiw[3 * B]);
+    const uint32_t st = la == kNone ? A : (lb == kNone ? B : kNone);
+    pk[0 * cap + k] = make_float4(rA.x, rA.y, rA.z, S.b.inv_mass[A]);
+    pk[1 * cap + k] = make_float4(rB.x, rB.y, rB.z, S.b.inv_mass[B]);
+    pk[2 * cap + k] = make_float4(n.x, n.y, n.z, bias.x + (S.vel_bias ? bias.y : 0.0f));
+    pk[3 * cap + k] = S.r.t1[row];
+    pk[4 * cap + k] = make_float4(t2.x, t2.y, t2.z, __uint_as_float(la));
+    pk[5 * cap + k] = make_float4(m.x, m.y, m.z, __uint_as_float(lb));
+    pk[6 * cap + k] = make_float4(IA.c0.x, IA.c0.y, IA.c0.z, IA.c1.x);
+    pk[7 * cap + k] = make_float4(IA.c1.y, IA.c1.z, IA.c2.x, IA.c2.y);
+    pk[8 * cap + k] = make_float4(IA.c2.z, IB.c0.x, IB.c0.y, IB.c0.z);
+    pk[9 * cap + k] = make_float4(IB.c1.x, IB.c1.y, IB.c1.z, IB.c2.x);
+    pk[10 * cap + k] = make_float4(IB.c2.y, IB.c2.z, __uint_as_float(row), 0.0f);
+    pk[11 * cap + k] = S.r.imp[row];
+    pk[12 * cap + k] = st == kNone ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : S.b.lv[st];
+    pk[13 * cap + k] = st == kNone ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : S.b.av[st];
+}
+
+__device__ __forceinline__ void load_pack(const float4* pk, uint32_t cap, uint32_t k, PackItem& it) {
+#pragma unroll
+    for (uint32_t j = 0; j < kPackArrays; ++j) it.q[j] = pk[j * cap + k];
+}
+
+// Velocity loads of a packed item: the dynamic bodies' from distributed shared memory, the other
+// body's from the item.
+struct PackVel {
+    Vec3 vA, wA, vB, wB;
+};
+__device__ __forceinline__ PackVel pack_velocities(const ClusterView& V, const PackItem& it) {
+    const uint32_t la = __float_as_uint(it.q[4].w), lb = __float_as_uint(it.q[5].w);
+    PackVel p;
+    p.vA = la != kNone ? V3(*V.rv(la)) : V3(it.q[12]);
+    p.wA = la != kNone ? V3(*V.rw(la)) : V3(it.q[13]);
+    p.vB = lb != kNone ? V3(*V.rv(lb)) : V3(it.q[12]);
+    p.wB = lb != kNone ? V3(*V.rw(lb)) : V3(it.q[13]);
+    return p;
+}
+
+// Solves a packed item whose velocities are loaded; stores the velocities and the impulses.
+__device__ __forceinline__ float2 pack_solve(const ClusterView& V, float4* pk, uint32_t cap, uint32_t k,
+                                             const PackItem& it, PackVel& p) {
+    const float4* q = it.q;
+    const Mat3 IA{V3(q[6]), Vec3(q[6].w, q[7].x, q[7].y), Vec3(q[7].z, q[7].w, q[8].x)};
+    const Mat3 IB{Vec3(q[8].y, q[8].z, q[8].w), V3(q[9]), Vec3(q[9].w, q[10].x, q[10].y)};
+    float4 im = q[11];
+    const float2 r = velocity_rows(V3(q[0]), V3(q[1]), q[2], q[3], q[4], q[5], q[0].w, q[1].w, q[2].w, IA, IB, p.vA,
+                                   p.wA, p.vB, p.wB, im);
+    const uint32_t la = __float_as_uint(q[4].w), lb = __float_as_uint(q[5].w);
+    if (la != kNone) {
+        *V.rv(la) = F4(p.vA, 0.0f);
+        *V.rw(la) = F4(p.wA, 0.0f);
+    }
+    if (lb != kNone) {
+        *V.rv(lb) = F4(p.vB, 0.0f);
+        *V.rw(lb) = F4(p.wB, 0.0f);
+    }
+    pk[11 * cap + k] = im;
+    return r;
+}
+
+// Warm start + velocity sweeps of a cluster island on packed items.  Every thread packs the points
+// it will solve (level l: items soff[l] + gtid, + gthreads, ...), and before it solves its point of
+// a level it loads its packed point of the next one - nothing the current level writes - so after
+// each barrier only the distributed-shared-memory velocity loads stand between it and its math.
+// Needs at least two velocity levels (the prefetched point must differ from the current one).
+template <typename Sync>
+__device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const ClusterView& V, float4* pk,
+                                      uint32_t* soff, uint32_t gtid, uint32_t gthreads, Sync sync, Counters* cnt) {
+    const uint32_t cap = S.pk_cap;
     const uint32_t base = 4u * S.isl_start[isl], loff = base + isl;
     const uint32_t nw = S.meta[4 * isl], nv = S.meta[4 * isl + 1];
-    const uint32_t total = S.vl_off[loff + nv];
-    for (uint32_t k = gtid; k < total; k += gthreads) {
-        const uint32_t row = S.vl_list[base + k], c = row >> 2;
-        const uint32_t la = S.con_la[c], lb = S.con_lb[c];
-        S.vrec[base + k] = make_uint4(row, S.con_a[c], S.con_b[c],
-                                      (la == kNone ? 0xFFFFu : la) | ((lb == kNone ? 0xFFFFu : lb) << 16));
-    }
+    for (uint32_t l = threadIdx.x; l <= nv; l += blockDim.x) soff[l] = S.vl_off[loff + l];
+    __syncthreads();
+    const uint32_t total = soff[nv];
+    for (uint32_t l = 0; l < nv; ++l)
+        for (uint32_t k = soff[l] + gtid; k < soff[l + 1]; k += gthreads) pack_item(S, pk, cap, k, S.vl_list[base + k]);
     sync.reset(gtid);
     for (uint32_t l = 0; l < nw; ++l) {
         const uint32_t e = S.wl_off[loff + l + 1];
         for (uint32_t k = S.wl_off[loff + l] + gtid; k < e; k += gthreads) warm_point(S, V, S.wl_list[base + k]);
         sync();
     }
-    auto rec_at = [&](uint32_t l) -> uint4 {
-        const uint32_t lo = S.vl_off[loff + l];
-        return lo + gtid < S.vl_off[loff + l + 1] ? S.vrec[base + lo + gtid] : make_uint4(kNone, 0u, 0u, 0u);
-    };
-    auto unpack = [&](const uint4& r, VelItem& it) {
-        const uint32_t la = r.w & 0xFFFFu, lb = r.w >> 16;
-        load_vel_item(S, r.x, r.y, r.z, la == 0xFFFFu ? kNone : la, lb == 0xFFFFu ? kNone : lb, it);
-    };
     const bool residual = S.res_tol > 0.0f;
     const uint32_t iters = residual ? S.res_cap : S.vel_iters;
     uint32_t used = 0;
     float res = 0.0f;
-    VelItem cur;
-    bool has_cur = false;
-    uint4 rnext = make_uint4(kNone, 0u, 0u, 0u);
-    if (iters && nv) {
-        const uint4 r0 = rec_at(0);
-        has_cur = r0.x != kNone;
-        if (has_cur) unpack(r0, cur);
-        rnext = rec_at(1 % nv);
-    }
+    PackItem cur;
+    uint32_t kc = soff[0] + gtid;
+    bool has_cur = iters && kc < soff[1];
+    if (has_cur) load_pack(pk, cap, kc, cur);
     for (uint32_t it = 0; it < iters; ++it) {
         unsigned long long sd = 0, sl = 0;
         for (uint32_t l = 0; l < nv; ++l) {
-            VelItem nxt;
-            const bool has_nxt = rnext.x != kNone;
-            if (has_nxt) unpack(rnext, nxt);                // the next level's point (wraps to level 0)
-            const uint4 rnn = rec_at(l + 2 < nv ? l + 2 : l + 2 - nv);
+            const uint32_t ln = l + 1 < nv ? l + 1 : 0u;  // after the last level: the next iteration's first
+            const uint32_t kn = soff[ln] + gtid;
+            const bool has_nxt = kn < soff[ln + 1];
+            PackVel pv;
+            if (has_cur) pv = pack_velocities(V, cur);  // issued first: the level's critical path
+            PackItem nxt;
+            if (has_nxt) load_pack(pk, cap, kn, nxt);
             if (has_cur) {
-                const float2 q = velocity_item(S, V, cur);
+                const float2 q = pack_solve(V, pk, cap, kc, cur, pv);
                 sd += res_fixed(q.x);
                 sl += res_fixed(q.y);
             }
-            const uint32_t hi = S.vl_off[loff + l + 1];
-            for (uint32_t k = S.vl_off[loff + l] + gtid + gthreads; k < hi; k += gthreads) {  // wide levels
-                VelItem x;
-                unpack(S.vrec[base + k], x);
-                const float2 q = velocity_item(S, V, x);
+            for (uint32_t k = soff[l] + gtid + gthreads; k < soff[l + 1]; k += gthreads) {  // wide levels
+                PackItem x;
+                load_pack(pk, cap, k, x);
+                PackVel px = pack_velocities(V, x);
+                const float2 q = pack_solve(V, pk, cap, k, x, px);
                 sd += res_fixed(q.x);
                 sl += res_fixed(q.y);
             }
             sync();
             cur = nxt;
+            kc = kn;
             has_cur = has_nxt;
-            rnext = rnn;
         }
         used = it + 1;
         if (residual || used == iters) {
@@ -604,6 +691,9 @@ __device__ void solve_velocity_pf(const SolveBufs& S, uint32_t isl, const View& 
             if (residual && (double)sd <= (double)S.res_tol * (double)sl) break;
         }
     }
+    for (uint32_t l = 0; l < nv; ++l)  // the accumulated impulses back to their rows
+        for (uint32_t k = soff[l] + gtid; k < soff[l + 1]; k += gthreads)
+            S.r.imp[__float_as_uint(pk[10 * cap + k].z)] = pk[11 * cap + k];
     if (gtid == 0) {
         atomicMax(&cnt->max_iters, used);
         atomicAdd(&cnt->pt_iters, total * used);
@@ -611,11 +701,21 @@ __device__ void solve_velocity_pf(const SolveBufs& S, uint32_t isl, const View& 
     }
 }
 
+// Whether k_solve_cluster solves a large island (k_solve_big takes the rest of those that do not fit
+// one CTA's shared memory).
+__device__ __forceinline__ bool cluster_island(const SolveBufs& S, uint32_t isl, uint32_t smem_bodies) {
+    const uint32_t nloc = S.meta[4 * isl + 3], nv = S.meta[4 * isl + 1];
+    if (nloc <= smem_bodies || nloc > kClusterCtas * kClusterSlots || nv > kClusterOffs) return false;
+    const uint32_t base = 4u * S.isl_start[isl];
+    return S.vl_off[base + isl + nv] <= S.pk_cap;
+}
+
 // Islands with more than smem_bodies and at most kClusterCtas * kClusterSlots dynamic bodies.
 __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads, 1)
     k_solve_cluster(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
     extern __shared__ float4 smem[];
     __shared__ unsigned long long red[6];
+    __shared__ uint32_t soff[kClusterOffs + 1];
     cg::cluster_group cl = cg::this_cluster();
     float4* sv = smem;
     float4* sw = smem + kClusterSlots;
@@ -627,8 +727,8 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
     const ClusterSync sync{red};
     for (uint32_t idx = cid; idx < n; idx += ncl) {  // the same islands in every CTA of a cluster
         const uint32_t isl = S.large_list[idx];
+        if (!cluster_island(S, isl, smem_bodies)) continue;
         const uint32_t nloc = S.meta[4 * isl + 3];
-        if (nloc <= smem_bodies || nloc > kClusterCtas * kClusterSlots) continue;
         const uint32_t* bodies = S.isl_bodies + 2u * S.isl_start[isl];
         for (uint32_t l = rank + kClusterCtas * tid; l < nloc; l += gthreads) {
             sv[l / kClusterCtas] = S.b.lv[bodies[l]];
@@ -636,7 +736,8 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
         }
         cl.sync();
         if (S.meta[4 * isl + 1] >= 2)  // prefetching needs two distinct levels
-            solve_velocity_pf(S, isl, V, gtid, gthreads, sync, cnt);
+            solve_velocity_packed(S, isl, V, S.pk + (size_t)cid * kPackArrays * S.pk_cap, soff, gtid, gthreads, sync,
+                                  cnt);
         else
             solve_velocity(S, isl, V, gtid, gthreads, sync, cnt);
         for (uint32_t l = rank + kClusterCtas * tid; l < nloc; l += gthreads) {

@@ -604,6 +604,11 @@ size_t cub_temp_bytes(uint32_t max_items) {
     return std::max(std::max(a, b), std::max(c, d));
 }
 
+size_t pack_elements(uint32_t points, uint32_t* cap) {
+    *cap = std::min(points, kPackCapMax);
+    return (size_t)kClusterGrid * kPackArrays * *cap;
+}
+
 // Whether this device can hold one k_solve_cluster cluster (checked once in configure_kernels).
 static bool g_cluster_ok = false;
 
@@ -621,9 +626,13 @@ cudaError_t configure_kernels() {
     e = cudaFuncSetAttribute(k_solve_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(2 * kClusterSlots * sizeof(float4)));
     if (e != cudaSuccess) return e;
+    if (kClusterCtas > 8) {
+        e = cudaFuncSetAttribute(k_solve_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return e;
+    }
     {
         cudaLaunchConfig_t lc = {};
-        lc.gridDim = dim3(kClusterCtas * 16u);
+        lc.gridDim = dim3(kClusterCtas * kClusterGrid);
         lc.blockDim = dim3(kClusterThreads);
         lc.dynamicSmemBytes = 2 * kClusterSlots * sizeof(float4);
         cudaLaunchAttribute at;
@@ -710,16 +719,16 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
                  ctx.isl_bodies, ctx.wl_list, ctx.vl_list, ctx.bl_list, ctx.wl_off, ctx.vl_off, ctx.bl_off,
                  ctx.isl_small, ctx.isl_large, ctx.r, ctx.b, ctx.ss.velocity_iterations,
                  ctx.ss.position_iterations, ctx.ss.warm_start_factor, ctx.ss.use_velocity_bias,
-                 ctx.ss.residual_tolerance, ctx.ss.max_velocity_iterations, ctx.brec};
+                 ctx.ss.residual_tolerance, ctx.ss.max_velocity_iterations, ctx.brec, ctx.pk,
+                 g_cluster_ok ? ctx.pk_cap : 0u};
     k_solve_warp<<<152u * 16u, kWarpsPerBlock * 32, kWarpsPerBlock * 2 * kWarpBodies * sizeof(float4), st>>>(SV, ctx.dcnt);
     k_solve_cta<<<152u * 2u, kCtaThreads, 2 * kCtaBodiesMax * sizeof(float4), st>>>(SV, ctx.dcnt, kCtaBodiesMax);
     if (g_cluster_ok) {
-        k_solve_cluster<<<kClusterCtas * 16u, kClusterThreads, 2 * kClusterSlots * sizeof(float4), st>>>(
+        k_solve_cluster<<<kClusterCtas * kClusterGrid, kClusterThreads, 2 * kClusterSlots * sizeof(float4), st>>>(
             SV, ctx.dcnt, kCtaBodiesMax);
         ++ctx.launches;
     }
-    k_solve_big<<<152u, kBigThreads, 0, st>>>(SV, ctx.dcnt, kCtaBodiesMax,
-                                              g_cluster_ok ? kClusterCtas * kClusterSlots : 0u);
+    k_solve_big<<<152u, kBigThreads, 0, st>>>(SV, ctx.dcnt, kCtaBodiesMax);
     ctx.launches += 3;
     ctx.launches += mlp_after_solve(ctx, dt);
     KZG_CK(mark(ctx, 5));
