@@ -302,65 +302,81 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
     const unsigned full = 0xffffffffu, lt = (1u << lane) - 1u;
     const FfTable T = ff_table_of(smem);
     uint32_t ns = 0, nbt = 0, nl0 = 0, nl1 = 0, head = 0, head0 = 0, head1 = 0;
-    // The 32 open slots from `head`, held in registers (one per lane) while consecutive constraints
-    // without a hub are placed into them; written back before any other access to the table.
+    // The slots head .. head + 31, held in registers (one per lane) while constraints are placed
+    // into them; lanes past the table's last slot stand for the batches that would be opened next
+    // (in batch order, after every existing one).  Written back - opened batches appended to the
+    // table and to the hub lists - before any other access to the table.
     bool win = false, wdirty = false;
-    uint32_t wcnt = 4u, ww0 = 0, ww1 = 0, ww2 = 0, wbid = 0;
+    uint32_t wcnt = 4u, ww0 = 0, ww1 = 0, ww2 = 0, wbid = 0, wns = 0;
     auto win_flush = [&]() {
-        if (win && wdirty && head + lane < ns) {
-            T.cnt[head + lane] = (uint8_t)wcnt;
-            T.bod0[head + lane] = ww0;
-            T.bod1[head + lane] = ww1;
-            T.bod2[head + lane] = ww2;
+        if (win && wdirty) {
+            const uint32_t i = head + lane;
+            const bool made = i >= wns && i < ns;  // opened while the window was held
+            if (i < ns) {
+                T.cnt[i] = (uint8_t)wcnt;
+                T.bod0[i] = ww0;
+                T.bod1[i] = ww1;
+                T.bod2[i] = ww2;
+                if (made) T.bid[i] = wbid;
+            }
+            const unsigned m0 = __ballot_sync(full, made && !(wcnt & kFfH0));
+            const unsigned m1 = __ballot_sync(full, made && !(wcnt & kFfH1));
+            if ((m0 >> lane) & 1u) T.list0[nl0 + __popc(m0 & lt)] = (uint16_t)i;
+            if ((m1 >> lane) & 1u) T.list1[nl1 + __popc(m1 & lt)] = (uint16_t)i;
+            nl0 += __popc(m0);
+            nl1 += __popc(m1);
         }
         win = false;
         wdirty = false;
         __syncwarp();
     };
-    auto win_fits = [&](uint32_t x0, uint32_t x1) -> bool {  // this lane's slot takes a point of (x0, x1)
+    // this lane's slot takes a point of (x0, x1) (x1 == x0 for a hub constraint, hflag its hub)
+    auto win_fits = [&](uint32_t x0, uint32_t x1, uint32_t hflag) -> bool {
         const uint32_t p0 = x0 | (x0 << 16), p1 = x1 | (x1 << 16);  // SIMD 16-bit compares
         const uint32_t hit = (__vcmpeq2(ww0, p0) | __vcmpeq2(ww1, p0) | __vcmpeq2(ww2, p0)) |
                              (__vcmpeq2(ww0, p1) | __vcmpeq2(ww1, p1) | __vcmpeq2(ww2, p1));
-        return (wcnt & 7u) < 4u && hit == 0u;
+        return (wcnt & 7u) < 4u && !(wcnt & hflag) && hit == 0u;
     };
-    auto win_place = [&](uint32_t x0, uint32_t x1, uint32_t row) {  // one point into this lane's slot
+    auto win_place = [&](uint32_t x0, uint32_t x1, uint32_t hflag, uint32_t row) {  // one point, this lane
         const uint32_t kk = wcnt & 7u;
         uint32_t nc = wcnt >> 5;
+        auto add = [&](uint32_t x) {
+            const uint32_t sh = 16u * (nc & 1u), msk = ~(0xFFFFu << sh), v = x << sh;
+            if (nc < 2u) ww0 = (ww0 & msk) | v;
+            else if (nc < 4u) ww1 = (ww1 & msk) | v;
+            else ww2 = (ww2 & msk) | v;
+            ++nc;
+        };
         if (kk + 1 < 4u) {  // a full batch's codes are never read again
-            const uint32_t add[2] = {x0, x1};
-            for (int q = 0; q < 2; ++q, ++nc) {
-                const uint32_t sh = 16u * (nc & 1u), msk = ~(0xFFFFu << sh), v = add[q] << sh;
-                if (nc < 2u) ww0 = (ww0 & msk) | v;
-                else if (nc < 4u) ww1 = (ww1 & msk) | v;
-                else ww2 = (ww2 & msk) | v;
-            }
+            add(x0);
+            if (!hflag) add(x1);
         }
-        wcnt = (kk + 1) | (wcnt & (kFfH0 | kFfH1)) | (nc << 5);
-        wdirty = true;
+        wcnt = (kk + 1) | (wcnt & (kFfH0 | kFfH1)) | hflag | (nc << 5);
         uint32_t* r = rec(S, rb + wbid);
         r[12 + kk] = row;
         r[3] = kk + 1;
     };
-    auto win_load = [&]() {  // skip the dead prefix for good, then hold the next 32 slots
+    auto win_load = [&]() {  // skip the full prefix for good, then hold the next 32 slots
         for (;;) {
             const uint32_t i = head + lane;
-            wcnt = 4u;
+            wcnt = i < kFfSlots ? 0u : 4u;  // past the last slot: a batch to open (none past the table)
+            ww0 = 0xFFFFFFFFu;
+            ww1 = 0xFFFFFFFFu;
+            ww2 = 0xFFFFFFFFu;
+            bool live = true;
             if (i < ns) {
                 wcnt = T.cnt[i];
                 ww0 = T.bod0[i];
                 ww1 = T.bod1[i];
                 ww2 = T.bod2[i];
                 wbid = T.bid[i];
+                live = (wcnt & 7u) < 4u;
             }
-            const unsigned livem = __ballot_sync(full, (wcnt & 7u) < 4u);
+            const unsigned livem = __ballot_sync(full, live);
             if (livem & 1u) break;
-            if (!livem) {
-                if (head + 32 >= ns) break;
-                head += 32;
-            } else {
-                head += __ffs(livem) - 1;
-            }
+            head += livem ? (uint32_t)(__ffs(livem) - 1) : 32u;
         }
+        wns = ns;
         win = true;
         wdirty = false;
     };
@@ -407,44 +423,37 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
             const uint32_t c = __shfl_sync(full, mc, k), xx = __shfl_sync(full, dx, k);
             const uint32_t np = md & 15u, x0 = xx & 0xFFFFu, x1 = xx >> 16;
             const int hub = (int)((md >> 4) & 3u) - 1;
-            if (hub < 0) {  // ---- fast path: the first np slots of the held window that fit
+            const uint32_t hflag = hub == 0 ? kFfH0 : (hub == 1 ? kFfH1 : 0u);
+            // ---- fast path: the first np lanes of the held window that take a point (sliding the
+            // window once past its full batches if it has to)
+            bool done = false;
+            for (int attempt = 0; attempt < 2; ++attempt) {
                 if (!win) win_load();
-                const unsigned okm = __ballot_sync(full, win_fits(x0, x1));
+                const bool ok = win_fits(x0, x1, hflag);
+                const unsigned okm = __ballot_sync(full, ok);
                 if ((uint32_t)__popc(okm) >= np) {
                     const uint32_t rank = __popc(okm & lt);
-                    const bool sel = ((okm >> lane) & 1u) && rank < np;
-                    // The next constraint rides along when it has no hub either: its fits are taken on
-                    // the same window state, minus the slots this one fills up and, if they share a
-                    // body, the slots this one takes.
-                    bool pair = false;
-                    uint32_t cB = 0, x0B = 0, x1B = 0, npB = 0;
-                    unsigned okB = 0;
-                    if (k + 1 < m) {
-                        const uint32_t mdB = __shfl_sync(full, meta, k + 1);
-                        const uint32_t cBs = __shfl_sync(full, mc, k + 1), xxB = __shfl_sync(full, dx, k + 1);
-                        if (!(mdB & 64u) && ((mdB >> 4) & 3u) == 0u) {
-                            cB = cBs;
-                            npB = mdB & 15u;
-                            x0B = xxB & 0xFFFFu;
-                            x1B = xxB >> 16;
-                            const bool share = x0 == x0B || x0 == x1B || x1 == x0B || x1 == x1B;
-                            const unsigned selm = __ballot_sync(full, sel);
-                            const unsigned fullm = __ballot_sync(full, sel && (wcnt & 7u) + 1u == 4u);
-                            okB = __ballot_sync(full, win_fits(x0B, x1B)) & ~fullm & (share ? ~selm : ~0u);
-                            pair = (uint32_t)__popc(okB) >= npB;
-                        }
+                    const bool sel = ok && rank < np;
+                    const uint32_t vfirst = ns - head;  // first lane that opens a batch
+                    const unsigned newm = __ballot_sync(full, sel && lane >= vfirst);
+                    if (sel) {
+                        if (lane >= vfirst) wbid = nbt + (lane - vfirst);
+                        win_place(x0, x1, hflag, 4u * c + rank);
                     }
-                    if (sel) win_place(x0, x1, 4u * c + rank);
-                    if (pair) {
-                        const uint32_t rankB = __popc(okB & lt);
-                        if (((okB >> lane) & 1u) && rankB < npB) win_place(x0B, x1B, 4u * cB + rankB);
-                        ++k;
-                    }
+                    ns += __popc(newm);
+                    nbt += __popc(newm);
+                    wdirty = true;
+                    done = true;
+                    break;
+                }
+                if (attempt == 0 && (__shfl_sync(full, wcnt, 0) & 7u) >= 4u) {
+                    win_flush();  // full batches at the front: slide and try again
                     continue;
                 }
+                break;
             }
+            if (done) continue;
             win_flush();  // the table is read and written directly below
-            const uint32_t hflag = hub == 0 ? kFfH0 : (hub == 1 ? kFfH1 : 0u);
             const uint16_t* L = hub == 0 ? T.list0 : T.list1;
             const uint32_t nL = hub < 0 ? ns : (hub == 0 ? nl0 : nl1);
             uint32_t pos = hub < 0 ? head : (hub == 0 ? head0 : head1);
@@ -525,6 +534,54 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
     return nbt;
 }
 
+// One level sweep of an island on one warp, with the level table `last` (nloc words, any memory):
+// 0 velocity (batch order, one level per point; local bodies staged per item in vl_list / bl_list),
+// 1 warm start (all points) and 2 bias (points with positionBias > 0) in constraint order, the
+// points of a constraint on consecutive levels.  Writes the levels and the sweep's level count.
+__device__ void level_sweep(const SchedBufs& S, SchedShared* sh, uint32_t sweep, uint32_t* last, uint32_t s0,
+                            uint32_t s1, uint32_t base, uint32_t lane) {
+    const uint32_t nloc = sh->nloc;
+    for (uint32_t k = lane; k < nloc; k += 32) last[k] = 0;
+    __syncwarp();
+    uint32_t top = 0;
+    if (sweep == 0) {
+        const uint32_t nvit = sh->total;
+        uint32_t nla = kNone, nlb = kNone;  // the next window's bodies, loaded a window ahead
+        if (lane < nvit) { nla = S.vl_list[base + lane]; nlb = S.bl_list[base + lane]; }
+        for (uint32_t w0 = 0; w0 < nvit; w0 += 32) {
+            const uint32_t i = w0 + lane, la = nla, lb = nlb;
+            const bool v = i < nvit;
+            nla = kNone;
+            nlb = kNone;
+            if (i + 32 < nvit) { nla = S.vl_list[base + i + 32]; nlb = S.bl_list[base + i + 32]; }
+            const uint32_t lvl = level_window(last, v, la, lb, 1u, lane);
+            if (v) { S.vlev[base + i] = lvl; top = max(top, lvl); }
+        }
+    } else {
+        for (uint32_t w0 = s0; w0 < s1; w0 += 32) {
+            const uint32_t s = w0 + lane;
+            bool v = s < s1;
+            uint32_t c = v ? S.isl_con[s] : 0u, len = 0;
+            if (v) {
+                const uint32_t np = S.con_np[c];
+                if (sweep == 1) {
+                    len = np;
+                } else if (!(S.inv_mass[S.con_a[c]] <= 0.0f && S.inv_mass[S.con_b[c]] <= 0.0f)) {
+                    for (uint32_t p = 0; p < np; ++p) len += S.bias[4u * c + p].y > 0.0f ? 1u : 0u;
+                }
+                v = len > 0;
+            }
+            const uint32_t lvl = level_window(last, v, v ? S.con_la[c] : kNone, v ? S.con_lb[c] : kNone, len, lane);
+            if (s < s1) (sweep == 1 ? S.first_w : S.first_b)[s] = v ? lvl : 0u;
+            if (v) top = max(top, lvl + len - 1);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) top = max(top, __shfl_xor_sync(0xffffffffu, top, o));
+    if (lane == 0) (sweep == 0 ? sh->nv : (sweep == 1 ? sh->nw : sh->nb)) = top;
+    __syncwarp();
+}
+
 template <typename Sync>
 __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl, uint32_t tid, uint32_t nthreads,
                                 SchedShared* sh, uint32_t* tmp, uint32_t* last_sm, uint32_t last_cap, bool ff_table,
@@ -582,17 +639,20 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
         sync();
     }
 
-    // ---- B: first-fit batching: one warp over the shared-memory table, else one lane
-    bool batched = false;
-    if (ff_table && sh->ff_ok && sh->nloc <= kFfMaxLocal) {
-        if (warp == 0) {
-            const uint32_t r = first_fit_warp(S, s0, s1, rb, sh->hub0, sh->hub1, sh->nloc, reinterpret_cast<uint8_t*>(last_sm), lane);
-            if (lane == 0) sh->nbt = r;
-        }
-        sync();
-        batched = sh->nbt != kNone;
-        sync();
+    // ---- B: first-fit batching: one warp over the shared-memory table, else one lane.  When the
+    // island's level tables do not fit shared memory anyway, warps 1 and 2 meanwhile run the warm
+    // and bias level sweeps, which do not depend on the batches.
+    const uint32_t nwarps = (nthreads + 31) >> 5;
+    const bool early = nwarps >= 3 && sh->nloc > last_cap;
+    const bool table_ff = ff_table && sh->ff_ok && sh->nloc <= kFfMaxLocal;
+    if (table_ff && warp == 0) {
+        const uint32_t r = first_fit_warp(S, s0, s1, rb, sh->hub0, sh->hub1, sh->nloc, reinterpret_cast<uint8_t*>(last_sm), lane);
+        if (lane == 0) sh->nbt = r;
     }
+    if (early && (warp == 1 || warp == 2)) level_sweep(S, sh, warp, S.last_g + warp * S.last_stride + boff, s0, s1, base, lane);
+    sync();
+    const bool batched = table_ff && sh->nbt != kNone;
+    sync();
     if (!batched && tid == 0) {
         const uint32_t hub0 = sh->hub0, hub1 = sh->hub1;
         uint32_t* r0 = rec(S, rb);
@@ -649,86 +709,97 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
         for (uint32_t j = lo; j < hi; ++j) part += rec(S, rb + j)[3];
         uint32_t total;
         uint32_t pos = group_scan(part, tid, nthreads, tmp, &total, sync);
-        for (uint32_t j = lo; j < hi; ++j) {
+        for (uint32_t j = lo; j < hi; ++j) {  // rows, and their local bodies for the velocity sweep
             const uint32_t* r = rec(S, rb + j);
-            for (uint32_t k = 0; k < r[3]; ++k) S.vitems[base + pos++] = r[12 + k];
+            for (uint32_t k = 0; k < r[3]; ++k, ++pos) {
+                const uint32_t row = r[12 + k];
+                S.vitems[base + pos] = row;
+                S.vl_list[base + pos] = S.con_la[row >> 2];
+                S.bl_list[base + pos] = S.con_lb[row >> 2];
+            }
         }
         if (tid == 0) sh->total = total;
     }
     sync();
 
-    // ---- D: the three level sweeps, one warp each (or one after another on a single warp)
+    // ---- D: the level sweeps left, one warp each (or one after another on a single warp); the
+    // velocity sweep alone gets all of the shared memory when the others ran during B
     const uint32_t nloc = sh->nloc;
     const uint32_t nvit = sh->total;
-    const bool in_shared = nloc <= last_cap;
-    const uint32_t nwarps = (nthreads + 31) >> 5;
     for (uint32_t sweep = 0; sweep < 3; ++sweep) {
+        if (early && sweep != 0) continue;
         const uint32_t owner = nwarps >= 3 ? sweep : 0;
         if (warp != owner) continue;
-        uint32_t* last = in_shared ? last_sm + (nwarps >= 3 ? sweep * last_cap : 0)
-                                   : S.last_g + sweep * S.last_stride + boff;
-        for (uint32_t k = lane; k < nloc; k += 32) last[k] = 0;
-        __syncwarp();
-        uint32_t top = 0;
-        if (sweep == 0) {  // velocity: batch order, one level per point
-            for (uint32_t w0 = 0; w0 < nvit; w0 += 32) {
-                const uint32_t i = w0 + lane;
-                const bool v = i < nvit;
-                const uint32_t row = v ? S.vitems[base + i] : 0u, c = row >> 2;
-                const uint32_t lvl = level_window(last, v, v ? S.con_la[c] : kNone, v ? S.con_lb[c] : kNone, 1u, lane);
-                if (v) { S.vlev[base + i] = lvl; top = max(top, lvl); }
-            }
-        } else {  // warm (all points) / bias (positionBias > 0): constraint order, consecutive levels
-            for (uint32_t w0 = s0; w0 < s1; w0 += 32) {
-                const uint32_t s = w0 + lane;
-                bool v = s < s1;
-                uint32_t c = v ? S.isl_con[s] : 0u, len = 0;
-                if (v) {
-                    const uint32_t np = S.con_np[c];
-                    if (sweep == 1) {
-                        len = np;
-                    } else if (!(S.inv_mass[S.con_a[c]] <= 0.0f && S.inv_mass[S.con_b[c]] <= 0.0f)) {
-                        for (uint32_t p = 0; p < np; ++p) len += S.bias[4u * c + p].y > 0.0f ? 1u : 0u;
-                    }
-                    v = len > 0;
-                }
-                const uint32_t lvl = level_window(last, v, v ? S.con_la[c] : kNone, v ? S.con_lb[c] : kNone, len, lane);
-                if (s < s1) (sweep == 1 ? S.first_w : S.first_b)[s] = v ? lvl : 0u;
-                if (v) top = max(top, lvl + len - 1);
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) top = max(top, __shfl_xor_sync(0xffffffffu, top, o));
-        if (lane == 0) (sweep == 0 ? sh->nv : (sweep == 1 ? sh->nw : sh->nb)) = top;
-        __syncwarp();
+        uint32_t* last = (early ? nloc <= 3u * last_cap : nloc <= last_cap)
+                             ? last_sm + (nwarps >= 3 && !early ? sweep * last_cap : 0)
+                             : S.last_g + sweep * S.last_stride + boff;
+        level_sweep(S, sh, sweep, last, s0, s1, base, lane);
     }
     sync();
 
     // ---- E: sort each sweep's points by level
     const uint32_t nv = sh->nv, nw = sh->nw, nb = sh->nb;
     const uint32_t scap = nthreads >= 64 ? 3u * last_cap : 0u;  // CTA: the level tables' shared memory is free now
+    // The emitters walk kU items per thread at once so that their loads overlap.
+    constexpr uint32_t kU = 8;
     level_sort(S, loff, base, nv, tid, nthreads, tmp, S.vl_list, S.vl_off,
                [&](auto put) {
-                   for (uint32_t i = tid; i < nvit; i += nthreads) put(S.vlev[base + i], S.vitems[base + i]);
+                   for (uint32_t i0 = tid; i0 < nvit; i0 += kU * nthreads) {
+                       uint32_t lv[kU], rw[kU];
+#pragma unroll
+                       for (uint32_t j = 0; j < kU; ++j) {
+                           const uint32_t i = i0 + j * nthreads;
+                           lv[j] = i < nvit ? S.vlev[base + i] : 0u;
+                           rw[j] = i < nvit ? S.vitems[base + i] : 0u;
+                       }
+#pragma unroll
+                       for (uint32_t j = 0; j < kU; ++j)
+                           if (lv[j]) put(lv[j], rw[j]);
+                   }
                },
                sync, last_sm, scap);
     level_sort(S, loff, base, nw, tid, nthreads, tmp, S.wl_list, S.wl_off,
                [&](auto put) {
-                   for (uint32_t s = s0 + tid; s < s1; s += nthreads) {
-                       const uint32_t c = S.isl_con[s], f = S.first_w[s];
-                       for (uint32_t p = 0; p < S.con_np[c]; ++p) put(f + p, 4u * c + p);
+                   for (uint32_t t0 = s0 + tid; t0 < s1; t0 += kU * nthreads) {
+                       uint32_t cc[kU], ff[kU], nn[kU];
+#pragma unroll
+                       for (uint32_t j = 0; j < kU; ++j) {
+                           const uint32_t t = t0 + j * nthreads;
+                           cc[j] = t < s1 ? S.isl_con[t] : 0u;
+                           ff[j] = t < s1 ? S.first_w[t] : 0u;
+                       }
+#pragma unroll
+                       for (uint32_t j = 0; j < kU; ++j) nn[j] = t0 + j * nthreads < s1 ? S.con_np[cc[j]] : 0u;
+#pragma unroll
+                       for (uint32_t j = 0; j < kU; ++j)
+                           for (uint32_t p = 0; p < nn[j]; ++p) put(ff[j] + p, 4u * cc[j] + p);
                    }
                },
                sync, last_sm, scap);
     level_sort(S, loff, base, nb, tid, nthreads, tmp, S.bl_list, S.bl_off,
                [&](auto put) {
-                   for (uint32_t s = s0 + tid; s < s1; s += nthreads) {
-                       const uint32_t f = S.first_b[s];
-                       if (f == 0) continue;
-                       const uint32_t c = S.isl_con[s];
-                       uint32_t k = 0;
-                       for (uint32_t p = 0; p < S.con_np[c]; ++p)
-                           if (S.bias[4u * c + p].y > 0.0f) put(f + k++, 4u * c + p);
+                   for (uint32_t t0 = s0 + tid; t0 < s1; t0 += kU * nthreads) {
+                       uint32_t cc[kU], ff[kU], nn[kU];
+#pragma unroll
+                       for (uint32_t j = 0; j < kU; ++j) {
+                           const uint32_t t = t0 + j * nthreads;
+                           ff[j] = t < s1 ? S.first_b[t] : 0u;
+                           cc[j] = ff[j] ? S.isl_con[t] : 0u;
+                       }
+#pragma unroll
+                       for (uint32_t j = 0; j < kU; ++j) nn[j] = ff[j] ? S.con_np[cc[j]] : 0u;
+                       float by[kU][4];
+#pragma unroll
+                       for (uint32_t j = 0; j < kU; ++j)
+#pragma unroll
+                           for (uint32_t p = 0; p < 4; ++p) by[j][p] = p < nn[j] ? S.bias[4u * cc[j] + p].y : 0.0f;
+#pragma unroll
+                       for (uint32_t j = 0; j < kU; ++j) {
+                           uint32_t k = 0;
+#pragma unroll
+                           for (uint32_t p = 0; p < 4; ++p)
+                               if (p < nn[j] && by[j][p] > 0.0f) put(ff[j] + k++, 4u * cc[j] + p);
+                       }
                    }
                },
                sync, last_sm, scap);
@@ -755,7 +826,7 @@ struct SchedCtaSync {
 };
 
 // Islands with at most kSchedSmallCons constraints: one warp each.
-__global__ void __launch_bounds__(128) k_schedule_warp(SchedBufs S, Counters* cnt) {
+__global__ void __launch_bounds__(128, 8) k_schedule_warp(SchedBufs S, Counters* cnt) {
     __shared__ SchedShared sh[4];
     __shared__ uint32_t tmp[4][33];
     __shared__ uint32_t last[4][kSchedWarpBodies];
@@ -770,7 +841,7 @@ __global__ void __launch_bounds__(128) k_schedule_warp(SchedBufs S, Counters* cn
 
 // Larger islands: one CTA each.
 static_assert(kFfBytes <= 3 * kSchedCtaBodies * sizeof(uint32_t), "first-fit table must fit the level tables' shared memory");
-__global__ void __launch_bounds__(256) k_schedule_cta(SchedBufs S, Counters* cnt) {
+__global__ void __launch_bounds__(256, 1) k_schedule_cta(SchedBufs S, Counters* cnt) {
     extern __shared__ uint32_t last_sm[];
     __shared__ SchedShared sh;
     __shared__ uint32_t tmp[33];
