@@ -181,11 +181,11 @@ constexpr uint32_t kFfDead = 0xFFFFu;
 constexpr uint32_t kFfMaxLocal = 0xFFFFu - kFfCodes - 1u;
 
 struct FfTable {
-    uint32_t *bod0, *bod1, *bod2;  // per slot: 6 body codes, two per word (0xFFFF = empty)
+    uint32_t *bod0, *bod1, *bod2;  // per slot: up to 6 body codes, two per word (ff_shift_codes)
     uint32_t* bid;                 // per slot: batch index
     uint16_t *list0, *list1;       // per hub: slots of the open batches without that hub, batch order
     uint16_t* remap;               // compaction: old slot -> new slot
-    uint8_t* cnt;                  // per slot: points (bits 0-2) | kFfH0 | kFfH1 | codes (bits 5-7)
+    uint8_t* cnt;                  // per slot: points (bits 0-2) | kFfH0 | kFfH1
     uint32_t* keys;                // code table: body index per entry (kNone = empty)
 };
 
@@ -282,12 +282,21 @@ __device__ void ff_compact(const FfTable& T, uint32_t& ns, uint32_t& nl0, uint32
     __syncwarp();
 }
 
-// Append a body code to a slot's code words (one lane).
-__device__ __forceinline__ uint32_t ff_add_code(const FfTable& T, uint32_t slot, uint32_t nc, uint32_t code) {
-    uint32_t* w = nc < 2u ? T.bod0 : (nc < 4u ? T.bod1 : T.bod2);
-    const uint32_t sh = 16u * (nc & 1u);
-    w[slot] = (w[slot] & ~(0xFFFFu << sh)) | (code << sh);
-    return nc + 1;
+// A slot's body codes form a 96-bit shift register over its three code words (newest in the low
+// half of word 0, empty halves 0xFFFF): a point adds its non-hub codes by shifting them in.  At most
+// six codes are ever added (three points of two bodies; a batch's fourth point fills it and its
+// codes are never read again), so nothing valid is shifted out.
+__device__ __forceinline__ void ff_shift_codes(uint32_t& w0, uint32_t& w1, uint32_t& w2, uint32_t x0, uint32_t x1,
+                                               bool hub) {
+    if (hub) {
+        w2 = __funnelshift_l(w1, w2, 16);
+        w1 = __funnelshift_l(w0, w1, 16);
+        w0 = (w0 << 16) | x0;
+    } else {
+        w2 = w1;
+        w1 = w0;
+        w0 = x0 | (x1 << 16);
+    }
 }
 
 // First-fit batches of one island's points (whole warp).  Returns the number of batches, or kNone
@@ -339,19 +348,8 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
     };
     auto win_place = [&](uint32_t x0, uint32_t x1, uint32_t hflag, uint32_t row) {  // one point, this lane
         const uint32_t kk = wcnt & 7u;
-        uint32_t nc = wcnt >> 5;
-        auto add = [&](uint32_t x) {
-            const uint32_t sh = 16u * (nc & 1u), msk = ~(0xFFFFu << sh), v = x << sh;
-            if (nc < 2u) ww0 = (ww0 & msk) | v;
-            else if (nc < 4u) ww1 = (ww1 & msk) | v;
-            else ww2 = (ww2 & msk) | v;
-            ++nc;
-        };
-        if (kk + 1 < 4u) {  // a full batch's codes are never read again
-            add(x0);
-            if (!hflag) add(x1);
-        }
-        wcnt = (kk + 1) | (wcnt & (kFfH0 | kFfH1)) | hflag | (nc << 5);
+        if (kk + 1 < 4u) ff_shift_codes(ww0, ww1, ww2, x0, x1, hflag != 0u);  // a full batch's codes are never read again
+        wcnt = (kk + 1) | (wcnt & (kFfH0 | kFfH1)) | hflag;
         uint32_t* r = rec(S, rb + wbid);
         r[12 + kk] = row;
         r[3] = kk + 1;
@@ -436,12 +434,49 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
                     const bool sel = ok && rank < np;
                     const uint32_t vfirst = ns - head;  // first lane that opens a batch
                     const unsigned newm = __ballot_sync(full, sel && lane >= vfirst);
+                    const uint32_t nnew = __popc(newm);
+                    // The next constraint rides along when the window serves it too: its fits are taken
+                    // on the same window state, minus the lanes this one fills up and, if they share a
+                    // body or a hub, the lanes this one takes.
+                    bool pair = false;
+                    uint32_t cB = 0, x0B = 0, x1B = 0, npB = 0, hfB = 0;
+                    unsigned okB = 0;
+                    if (k + 1 < m) {
+                        const uint32_t mdB = __shfl_sync(full, meta, k + 1);
+                        const uint32_t cBs = __shfl_sync(full, mc, k + 1), xxB = __shfl_sync(full, dx, k + 1);
+                        if (!(mdB & 64u)) {
+                            cB = cBs;
+                            npB = mdB & 15u;
+                            x0B = xxB & 0xFFFFu;
+                            x1B = xxB >> 16;
+                            const uint32_t hB = (mdB >> 4) & 3u;
+                            hfB = hB == 1u ? kFfH0 : (hB == 2u ? kFfH1 : 0u);
+                            const bool share = x0 == x0B || x0 == x1B || x1 == x0B || x1 == x1B || (hfB & hflag);
+                            const unsigned selm = __ballot_sync(full, sel);
+                            const unsigned fullm = __ballot_sync(full, sel && (wcnt & 7u) + 1u == 4u);
+                            okB = __ballot_sync(full, win_fits(x0B, x1B, hfB)) & ~fullm & (share ? ~selm : ~0u);
+                            pair = (uint32_t)__popc(okB) >= npB;
+                        }
+                    }
                     if (sel) {
                         if (lane >= vfirst) wbid = nbt + (lane - vfirst);
                         win_place(x0, x1, hflag, 4u * c + rank);
                     }
-                    ns += __popc(newm);
-                    nbt += __popc(newm);
+                    ns += nnew;
+                    nbt += nnew;
+                    if (pair) {
+                        const uint32_t rankB = __popc(okB & lt);
+                        const bool selB = ((okB >> lane) & 1u) && rankB < npB;
+                        const uint32_t vB = ns - head;
+                        const unsigned newB = __ballot_sync(full, selB && lane >= vB);
+                        if (selB) {
+                            if (lane >= vB) wbid = nbt + (lane - vB);
+                            win_place(x0B, x1B, hfB, 4u * cB + rankB);
+                        }
+                        ns += __popc(newB);
+                        nbt += __popc(newB);
+                        ++k;
+                    }
                     wdirty = true;
                     done = true;
                     break;
@@ -485,12 +520,14 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
                     const uint32_t rank = __popc(okm & lt);
                     if (rank < take) {  // place point placed + rank into this candidate
                         const uint32_t kk = cn & 7u;
-                        uint32_t nc = cn >> 5;
                         if (kk + 1 < 4u) {  // a full batch's codes are never read again
-                            nc = ff_add_code(T, s, nc, x0);
-                            if (hub < 0) nc = ff_add_code(T, s, nc, x1);
+                            uint32_t c0 = T.bod0[s], c1 = T.bod1[s], c2 = T.bod2[s];
+                            ff_shift_codes(c0, c1, c2, x0, x1, hub >= 0);
+                            T.bod0[s] = c0;
+                            T.bod1[s] = c1;
+                            T.bod2[s] = c2;
                         }
-                        T.cnt[s] = (uint8_t)((kk + 1) | (cn & (kFfH0 | kFfH1)) | hflag | (nc << 5));
+                        T.cnt[s] = (uint8_t)((kk + 1) | (cn & (kFfH0 | kFfH1)) | hflag);
                         uint32_t* r = rec(S, rb + T.bid[s]);
                         r[12 + kk] = 4u * c + placed + rank;
                         r[3] = kk + 1;
@@ -515,7 +552,7 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
                     T.bod0[sl] = hub < 0 ? (x0 | (x1 << 16)) : (x0 | 0xFFFF0000u);
                     T.bod1[sl] = 0xFFFFFFFFu;
                     T.bod2[sl] = 0xFFFFFFFFu;
-                    T.cnt[sl] = (uint8_t)(1u | hflag | ((hub < 0 ? 2u : 1u) << 5));
+                    T.cnt[sl] = (uint8_t)(1u | hflag);
                     uint32_t* r = rec(S, rb + j);
                     r[3] = 1;
                     r[12] = 4u * c + placed + lane;
