@@ -79,11 +79,14 @@ struct ClusterView {
     float4* w;
     const float4* glv;
     const float4* gav;
+    uint32_t rank;  // this CTA's rank: its own bodies are read and written without the cluster mapping
     __device__ __forceinline__ float4* rv(uint32_t loc) const {
-        return cg::this_cluster().map_shared_rank(v, loc % kClusterCtas) + loc / kClusterCtas;
+        const uint32_t r = loc % kClusterCtas;
+        return (r == rank ? v : cg::this_cluster().map_shared_rank(v, r)) + loc / kClusterCtas;
     }
     __device__ __forceinline__ float4* rw(uint32_t loc) const {
-        return cg::this_cluster().map_shared_rank(w, loc % kClusterCtas) + loc / kClusterCtas;
+        const uint32_t r = loc % kClusterCtas;
+        return (r == rank ? w : cg::this_cluster().map_shared_rank(w, r)) + loc / kClusterCtas;
     }
     __device__ __forceinline__ Vec3 lin(uint32_t loc, uint32_t body) const {
         return loc == kNone ? V3(__ldg(&glv[body])) : V3(*rv(loc));
@@ -544,10 +547,11 @@ struct ClusterSync {
     }
 };
 
-// Packed velocity items of a cluster island, in the island's velocity-level order: kPackArrays
-// float4 arrays of pk_cap entries per cluster (structure of arrays).  The points a warp solves in
-// one level are consecutive, so every field is one coalesced 16-byte load with no index to chase,
-// and a point is packed, read and updated by the one thread that solves it.
+// Packed velocity items of a cluster island: kPackArrays float4 arrays of pk_cap entries per cluster
+// (structure of arrays).  Every point belongs to the CTA that holds its first dynamic body (so that
+// body's velocity is local shared memory); each CTA's points form one region, in velocity-level
+// order.  The points a warp solves in one level are consecutive, so every field is one coalesced
+// 16-byte load with no index to chase.
 //   0 rA, inverse mass A     1 rB, inverse mass B      2 normal, velocity bias   3 t1, friction
 //   4 t2, local A            5 masses, local B         6-10 inverse inertias of A and B (9 + 9
 //   floats), 10.z = row      11 accumulated impulses   12, 13 linear and angular velocity of the
@@ -584,9 +588,16 @@ __device__ __forceinline__ void pack_item(const SolveBufs& S, float4* pk, uint32
     pk[13 * cap + k] = st == kNone ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : S.b.av[st];
 }
 
+// Loads bypass L1: other CTAs of the cluster packed the items.
 __device__ __forceinline__ void load_pack(const float4* pk, uint32_t cap, uint32_t k, PackItem& it) {
 #pragma unroll
-    for (uint32_t j = 0; j < kPackArrays; ++j) it.q[j] = pk[j * cap + k];
+    for (uint32_t j = 0; j < kPackArrays; ++j) it.q[j] = __ldcg(&pk[j * cap + k]);
+}
+
+// The CTA of the cluster that holds a point's first dynamic body.
+__device__ __forceinline__ uint32_t point_owner(const SolveBufs& S, uint32_t row) {
+    const uint32_t c = row >> 2, la = S.con_la[c];
+    return (la != kNone ? la : S.con_lb[c]) % kClusterCtas;
 }
 
 // Velocity loads of a packed item: the dynamic bodies' from distributed shared memory, the other
@@ -626,23 +637,65 @@ __device__ __forceinline__ float2 pack_solve(const ClusterView& V, float4* pk, u
     return r;
 }
 
-// Warm start + velocity sweeps of a cluster island on packed items.  Every thread packs the points
-// it will solve (level l: items soff[l] + gtid, + gthreads, ...), and before it solves its point of
-// a level it loads its packed point of the next one - nothing the current level writes - so after
-// each barrier only the distributed-shared-memory velocity loads stand between it and its math.
-// Needs at least two velocity levels (the prefetched point must differ from the current one).
+// Warm start + velocity sweeps of a cluster island on packed items.  The points are first
+// partitioned: each level's points go to the CTAs holding their first dynamic bodies (counted into
+// every CTA's level table soff, scanned there, then packed at region start + level offset + rank).
+// Before a thread solves its point of a level it loads its packed point of the next one - nothing
+// the current level writes - so after each barrier only the velocity loads stand between it and its
+// math.  Needs at least two velocity levels (the prefetched point must differ from the current one).
 template <typename Sync>
 __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const ClusterView& V, float4* pk,
-                                      uint32_t* soff, uint32_t gtid, uint32_t gthreads, Sync sync, Counters* cnt) {
-    const uint32_t cap = S.pk_cap;
+                                      uint32_t* soff, uint32_t* rall, uint32_t* tmp, uint32_t rank, uint32_t gtid,
+                                      uint32_t gthreads, Sync sync, Counters* cnt) {
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t cap = S.pk_cap, tid = threadIdx.x, nthr = blockDim.x;
     const uint32_t base = 4u * S.isl_start[isl], loff = base + isl;
     const uint32_t nw = S.meta[4 * isl], nv = S.meta[4 * isl + 1];
-    for (uint32_t l = threadIdx.x; l <= nv; l += blockDim.x) soff[l] = S.vl_off[loff + l];
+    const uint32_t total = S.vl_off[loff + nv];
+    // ---- partition: counts per (level, owner); a point's rank inside its group goes to vrec.x
+    for (uint32_t l = tid; l <= nv; l += nthr) soff[l] = 0;
+    cl.sync();
+    for (uint32_t l = 0; l < nv; ++l) {
+        const uint32_t hi = S.vl_off[loff + l + 1];
+        for (uint32_t k = S.vl_off[loff + l] + gtid; k < hi; k += gthreads) {
+            const uint32_t o = point_owner(S, S.vl_list[base + k]);
+            S.vrec[base + k].x = atomicAdd(cl.map_shared_rank(soff, o) + l, 1u);
+        }
+    }
+    cl.sync();
+    {  // exclusive scan of this CTA's level counts; soff[nv] = its points
+        const uint32_t chunk = (nv + nthr - 1) / nthr;
+        const uint32_t lo = min(nv, tid * chunk), hi = min(nv, lo + chunk);
+        uint32_t part = 0;
+        for (uint32_t l = lo; l < hi; ++l) part += soff[l];
+        uint32_t run = group_scan(part, tid, nthr, tmp, &soff[nv + 1], CtaSync{nullptr});
+        for (uint32_t l = lo; l < hi; ++l) {
+            const uint32_t c = soff[l];
+            soff[l] = run;
+            run += c;
+        }
+        __syncthreads();
+        if (tid == 0) soff[nv] = soff[nv + 1];
+    }
+    cl.sync();
+    if (tid < kClusterCtas) rall[tid] = cl.map_shared_rank(soff, tid)[nv];
     __syncthreads();
-    const uint32_t total = soff[nv];
-    for (uint32_t l = 0; l < nv; ++l)
-        for (uint32_t k = soff[l] + gtid; k < soff[l + 1]; k += gthreads) pack_item(S, pk, cap, k, S.vl_list[base + k]);
-    sync.reset(gtid);
+    if (tid == 0)
+        for (uint32_t r = 0, run = 0; r < kClusterCtas; ++r) {
+            const uint32_t c = rall[r];
+            rall[r] = run;
+            run += c;
+        }
+    __syncthreads();
+    for (uint32_t l = 0; l < nv; ++l) {
+        const uint32_t hi = S.vl_off[loff + l + 1];
+        for (uint32_t k = S.vl_off[loff + l] + gtid; k < hi; k += gthreads) {
+            const uint32_t row = S.vl_list[base + k], o = point_owner(S, row);
+            pack_item(S, pk, cap, rall[o] + cl.map_shared_rank(soff, o)[l] + S.vrec[base + k].x, row);
+        }
+    }
+    const uint32_t R = rall[rank];
+    sync.reset(gtid);  // a cluster barrier: every packed point is visible
     for (uint32_t l = 0; l < nw; ++l) {
         const uint32_t e = S.wl_off[loff + l + 1];
         for (uint32_t k = S.wl_off[loff + l] + gtid; k < e; k += gthreads) warm_point(S, V, S.wl_list[base + k]);
@@ -653,15 +706,15 @@ __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const Cl
     uint32_t used = 0;
     float res = 0.0f;
     PackItem cur;
-    uint32_t kc = soff[0] + gtid;
-    bool has_cur = iters && kc < soff[1];
+    uint32_t kc = R + soff[0] + tid;
+    bool has_cur = iters && kc < R + soff[1];
     if (has_cur) load_pack(pk, cap, kc, cur);
     for (uint32_t it = 0; it < iters; ++it) {
         unsigned long long sd = 0, sl = 0;
         for (uint32_t l = 0; l < nv; ++l) {
             const uint32_t ln = l + 1 < nv ? l + 1 : 0u;  // after the last level: the next iteration's first
-            const uint32_t kn = soff[ln] + gtid;
-            const bool has_nxt = kn < soff[ln + 1];
+            const uint32_t kn = R + soff[ln] + tid;
+            const bool has_nxt = kn < R + soff[ln + 1];
             PackVel pv;
             if (has_cur) pv = pack_velocities(V, cur);  // issued first: the level's critical path
             PackItem nxt;
@@ -671,7 +724,7 @@ __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const Cl
                 sd += res_fixed(q.x);
                 sl += res_fixed(q.y);
             }
-            for (uint32_t k = soff[l] + gtid + gthreads; k < soff[l + 1]; k += gthreads) {  // wide levels
+            for (uint32_t k = R + soff[l] + tid + nthr; k < R + soff[l + 1]; k += nthr) {  // wide levels
                 PackItem x;
                 load_pack(pk, cap, k, x);
                 PackVel px = pack_velocities(V, x);
@@ -691,9 +744,8 @@ __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const Cl
             if (residual && (double)sd <= (double)S.res_tol * (double)sl) break;
         }
     }
-    for (uint32_t l = 0; l < nv; ++l)  // the accumulated impulses back to their rows
-        for (uint32_t k = soff[l] + gtid; k < soff[l + 1]; k += gthreads)
-            S.r.imp[__float_as_uint(pk[10 * cap + k].z)] = pk[11 * cap + k];
+    for (uint32_t k = R + tid; k < R + soff[nv]; k += nthr)  // the accumulated impulses back to their rows
+        S.r.imp[__float_as_uint(pk[10 * cap + k].z)] = pk[11 * cap + k];
     if (gtid == 0) {
         atomicMax(&cnt->max_iters, used);
         atomicAdd(&cnt->pt_iters, total * used);
@@ -715,7 +767,8 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
     k_solve_cluster(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
     extern __shared__ float4 smem[];
     __shared__ unsigned long long red[6];
-    __shared__ uint32_t soff[kClusterOffs + 1];
+    __shared__ uint32_t soff[kClusterOffs + 2];
+    __shared__ uint32_t rall[kClusterCtas], tmp[33];
     cg::cluster_group cl = cg::this_cluster();
     float4* sv = smem;
     float4* sw = smem + kClusterSlots;
@@ -723,7 +776,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
     const uint32_t gtid = rank * blockDim.x + tid, gthreads = kClusterCtas * blockDim.x;
     const uint32_t ncl = gridDim.x / kClusterCtas, cid = blockIdx.x / kClusterCtas;
     const uint32_t n = cnt->nlarge;
-    const ClusterView V{sv, sw, S.b.lv, S.b.av};
+    const ClusterView V{sv, sw, S.b.lv, S.b.av, rank};
     const ClusterSync sync{red};
     for (uint32_t idx = cid; idx < n; idx += ncl) {  // the same islands in every CTA of a cluster
         const uint32_t isl = S.large_list[idx];
@@ -736,8 +789,8 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
         }
         cl.sync();
         if (S.meta[4 * isl + 1] >= 2)  // prefetching needs two distinct levels
-            solve_velocity_packed(S, isl, V, S.pk + (size_t)cid * kPackArrays * S.pk_cap, soff, gtid, gthreads, sync,
-                                  cnt);
+            solve_velocity_packed(S, isl, V, S.pk + (size_t)cid * kPackArrays * S.pk_cap, soff, rall, tmp, rank, gtid,
+                                  gthreads, sync, cnt);
         else
             solve_velocity(S, isl, V, gtid, gthreads, sync, cnt);
         for (uint32_t l = rank + kClusterCtas * tid; l < nloc; l += gthreads) {
