@@ -87,6 +87,7 @@ kzg_status alloc_all(Ctx* ctx) {
     CK(dalloc(&ctx->lvl_count, R + P + 1));
     CK(dalloc(&ctx->brec, 4 * (R + P + 1)));
     CK(dalloc(&ctx->pk, pack_elements((uint32_t)std::min<size_t>(R, 0xFFFFFFFFu), &ctx->pk_cap)));
+    CK(dalloc(&ctx->cl_ids, cluster_id_words((uint32_t)P)));
     CK(dalloc(&ctx->last_g, 3 * 2 * P));
     CK(dalloc(&ctx->first_w, P));
     CK(dalloc(&ctx->first_b, P));
@@ -137,7 +138,7 @@ void free_all(Ctx* ctx) {
                     ctx->r.t1, ctx->r.t2, ctx->r.rA, ctx->r.rB, ctx->r.rAr, ctx->r.rBr, ctx->r.laA, ctx->r.laB,
                     ctx->r.mass, ctx->r.imp, ctx->r.bias, ctx->uf, ctx->isl_key, ctx->isl_key_sorted,
                     ctx->isl_con_in, ctx->isl_con, ctx->isl_head, ctx->isl_start, ctx->isl_pts, ctx->lvl_count,
-                    ctx->brec, ctx->pk, ctx->last_g, ctx->first_w, ctx->first_b, ctx->lvl_tmp, ctx->ids_tmp,
+                    ctx->brec, ctx->pk, ctx->cl_ids, ctx->last_g, ctx->first_w, ctx->first_b, ctx->lvl_tmp, ctx->ids_tmp,
                     ctx->wl_list, ctx->vl_list, ctx->bl_list, ctx->wl_off, ctx->vl_off, ctx->bl_off, ctx->isl_meta,
                     ctx->c_key, ctx->c_np, ctx->c_pos, ctx->c_imp, ctx->dcnt, ctx->cub_tmp, ctx->hash_words,
                     ctx->body_stamp, ctx->body_loc, ctx->isl_bodies, ctx->con_la, ctx->con_lb, ctx->isl_small,

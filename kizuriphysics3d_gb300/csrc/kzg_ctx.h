@@ -147,6 +147,7 @@ struct Ctx {
     uint4* brec = nullptr;            // batch records, 64 B each (4*ncons + nislands + 1)
     float4* pk = nullptr;             // packed velocity items of cluster islands (kPackArrays x pk_cap per cluster)
     uint32_t pk_cap = 0;
+    uint32_t* cl_ids = nullptr;       // local-id scratch of cluster islands (cluster_id_words)
     uint32_t* last_g = nullptr;       // level tables that do not fit shared memory (3 x 2*ncons)
     uint32_t *first_w = nullptr, *first_b = nullptr;  // per sorted constraint: first warm / bias level
     uint32_t* lvl_tmp = nullptr;      // per point: velocity level (batch order)

@@ -17,6 +17,7 @@ cudaError_t configure_kernels();  // per-device kernel attributes (large dynamic
 // Packed-item scratch of the cluster solve for `points` point rows: entries per cluster island
 // (cap) and float4 elements to allocate.
 size_t pack_elements(uint32_t points, uint32_t* cap);
+size_t cluster_id_words(uint32_t max_cons);  // local-id scratch of the cluster solve
 kzg_status step_canonical(Ctx& ctx, float dt, uint32_t nsteps);
 kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t num_pairs, float dt);
 kzg_status hash_state(Ctx& ctx, uint64_t* out);

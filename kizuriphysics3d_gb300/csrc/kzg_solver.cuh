@@ -37,6 +37,11 @@ struct SolveBufs {
                        // the batch-record buffer, free once the schedule is built)
     float4* pk;        // cluster islands: packed velocity items, kPackArrays x pk_cap per cluster
     uint32_t pk_cap;   // points per cluster island (0: no cluster solve)
+    const uint32_t* isl_con;  // constraints of each island (sorted)
+    uint32_t max_cons;        // constraint capacity
+    uint32_t* cl_ids;  // cluster islands: per cluster 2 x kClusterBodies words (new local id of each
+                       // local body; body of each new id), then the permuted local ids of A and B
+                       // per constraint (2 x max_pairs)
 };
 
 // Velocity storage of one island: staged in shared memory (local index) or read/written in place
@@ -106,7 +111,7 @@ struct ClusterView {
 template <typename View>
 __device__ __forceinline__ void warm_point(const SolveBufs& S, const View& V, uint32_t row) {
     const uint32_t c = row >> 2;
-    const uint32_t A = S.con_a[c], B = S.con_b[c], la = S.con_la[c], lb = S.con_lb[c];
+    const uint32_t A = S.con_a[c], B = S.con_b[c], la = __ldcg(&S.con_la[c]), lb = __ldcg(&S.con_lb[c]);
     const float4 im = S.r.imp[row];
     const Vec3 n = V3(S.r.n[row]), t1 = V3(S.r.t1[row]), t2 = V3(S.r.t2[row]);
     const Vec3 imp = ((n * im.x + t1 * im.y) + t2 * im.z) * S.ws_factor;
@@ -222,7 +227,7 @@ __device__ __forceinline__ float2 velocity_point_ab(const SolveBufs& S, const Vi
 template <typename View>
 __device__ __forceinline__ float2 velocity_point(const SolveBufs& S, const View& V, uint32_t row) {
     const uint32_t c = row >> 2;
-    return velocity_point_ab(S, V, row, S.con_a[c], S.con_b[c], S.con_la[c], S.con_lb[c]);
+    return velocity_point_ab(S, V, row, S.con_a[c], S.con_b[c], __ldcg(&S.con_la[c]), __ldcg(&S.con_lb[c]));
 }
 
 // Fixed-point (2^-20 N s) magnitude for the residual sums: integer sums are exact and independent
@@ -235,7 +240,7 @@ __device__ __forceinline__ unsigned long long res_fixed(float x) {
 template <typename View>
 __device__ __forceinline__ void bias_point(const SolveBufs& S, const View& V, uint32_t row) {
     const uint32_t c = row >> 2;
-    const uint32_t A = S.con_a[c], B = S.con_b[c], la = S.con_la[c], lb = S.con_lb[c];
+    const uint32_t A = S.con_a[c], B = S.con_b[c], la = __ldcg(&S.con_la[c]), lb = __ldcg(&S.con_lb[c]);
     const Vec3 rA = V3(S.r.rAr[row]), rB = V3(S.r.rBr[row]);
     const Vec3 n = V3(S.r.n[row]);
     const float nm = S.r.mass[row].x, pbias = S.r.bias[row].y;
@@ -511,6 +516,7 @@ __global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, Count
 // (ClusterView) and a hardware cluster barrier separates the levels.
 constexpr uint32_t kClusterThreads = 256;
 constexpr uint32_t kClusterSlots = 6144;  // bodies per CTA: 2 x 16 B x 6144 = 192 KB
+constexpr uint32_t kClusterBodies = kClusterCtas * kClusterSlots;
 
 // Level barrier and residual sums over the whole cluster: every CTA sums its warps into its own
 // rotating words (as CtaSync does), and after the barrier every thread adds the kClusterCtas partial
@@ -567,7 +573,7 @@ struct PackItem {
 
 __device__ __forceinline__ void pack_item(const SolveBufs& S, float4* pk, uint32_t cap, uint32_t k, uint32_t row) {
     const uint32_t c = row >> 2;
-    const uint32_t A = S.con_a[c], B = S.con_b[c], la = S.con_la[c], lb = S.con_lb[c];
+    const uint32_t A = S.con_a[c], B = S.con_b[c], la = __ldcg(&S.con_la[c]), lb = __ldcg(&S.con_lb[c]);
     const float4 rA = S.r.rAr[row], rB = S.r.rBr[row], bias = S.r.bias[row];
     const float4 n = S.r.n[row], t2 = S.r.t2[row], m = S.r.mass[row];
     const Mat3 IA = M3(&S.b.iiw[3 * A]), IB = M3(&S.b.iiw[3 * B]);
@@ -596,8 +602,8 @@ __device__ __forceinline__ void load_pack(const float4* pk, uint32_t cap, uint32
 
 // The CTA of the cluster that holds a point's first dynamic body.
 __device__ __forceinline__ uint32_t point_owner(const SolveBufs& S, uint32_t row) {
-    const uint32_t c = row >> 2, la = S.con_la[c];
-    return (la != kNone ? la : S.con_lb[c]) % kClusterCtas;
+    const uint32_t c = row >> 2, la = __ldcg(&S.con_la[c]);
+    return (la != kNone ? la : __ldcg(&S.con_lb[c])) % kClusterCtas;
 }
 
 // Velocity loads of a packed item: the dynamic bodies' from distributed shared memory, the other
@@ -762,13 +768,114 @@ __device__ __forceinline__ bool cluster_island(const SolveBufs& S, uint32_t isl,
     return S.vl_off[base + isl + nv] <= S.pk_cap;
 }
 
+// Spatial ownership of a cluster island's bodies: CTA t holds the bodies whose x-z position falls in
+// tile t of a 4 x 4 grid over the island's extent - contacts join near bodies, so most points find
+// both velocities in one CTA's shared memory.  New local ids are slot * kClusterCtas + tile (the
+// ClusterView mapping); if a tile overflows its kClusterSlots slots the island keeps its ids.
+// Writes the new ids of the island's constraints (SC.con_la / SC.con_lb) and its bodies by new id;
+// returns how many bodies this CTA holds.  Every read of what it writes goes through L2.
+static_assert(kClusterCtas == 16, "cluster_layout tiles the island 4 x 4");
+__device__ uint32_t cluster_layout(const SolveBufs& S, const SolveBufs& SC, uint32_t isl, uint32_t* ids,
+                                   uint32_t* sc, float* sbb, uint32_t rank, uint32_t gtid, uint32_t gthreads) {
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const uint32_t nloc = S.meta[4 * isl + 3], s0 = S.isl_start[isl], s1 = S.isl_start[isl + 1];
+    const uint32_t* bodies = S.isl_bodies + 2u * s0;
+    uint32_t* newid = ids;                     // by old local id
+    uint32_t* body_of = ids + kClusterBodies;  // by new local id
+    // island extent in x and z: warp partials in sbb[4 * warp ..], the CTA's in sbb[0..3]
+    float mnx = 3.0e38f, mxx = -3.0e38f, mnz = 3.0e38f, mxz = -3.0e38f;
+    for (uint32_t l = gtid; l < nloc; l += gthreads) {
+        const float4 p = S.b.pos[bodies[l]];
+        mnx = fminf(mnx, p.x);
+        mxx = fmaxf(mxx, p.x);
+        mnz = fminf(mnz, p.z);
+        mxz = fmaxf(mxz, p.z);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mnz = fminf(mnz, __shfl_xor_sync(0xffffffffu, mnz, o));
+        mxz = fmaxf(mxz, __shfl_xor_sync(0xffffffffu, mxz, o));
+    }
+    if (lane == 0) {
+        sbb[4 + 4 * warp + 0] = mnx;
+        sbb[4 + 4 * warp + 1] = mxx;
+        sbb[4 + 4 * warp + 2] = mnz;
+        sbb[4 + 4 * warp + 3] = mxz;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (uint32_t w = 1; w < nwarps; ++w) {
+            mnx = fminf(mnx, sbb[4 + 4 * w + 0]);
+            mxx = fmaxf(mxx, sbb[4 + 4 * w + 1]);
+            mnz = fminf(mnz, sbb[4 + 4 * w + 2]);
+            mxz = fmaxf(mxz, sbb[4 + 4 * w + 3]);
+        }
+        sbb[0] = mnx;
+        sbb[1] = mxx;
+        sbb[2] = mnz;
+        sbb[3] = mxz;
+        sc[0] = 0;  // bodies this CTA holds
+    }
+    cl.sync();
+    if (tid == 0) {
+        for (uint32_t r = 0; r < kClusterCtas; ++r) {
+            const float* o = cl.map_shared_rank(sbb, r);
+            mnx = fminf(mnx, o[0]);
+            mxx = fmaxf(mxx, o[1]);
+            mnz = fminf(mnz, o[2]);
+            mxz = fmaxf(mxz, o[3]);
+        }
+        sbb[36] = mnx;
+        sbb[37] = 4.0f / fmaxf(mxx - mnx, 1.0e-6f);
+        sbb[38] = mnz;
+        sbb[39] = 4.0f / fmaxf(mxz - mnz, 1.0e-6f);
+    }
+    __syncthreads();
+    const float x0 = sbb[36], sx = sbb[37], z0 = sbb[38], sz = sbb[39];
+    for (uint32_t l = gtid; l < nloc; l += gthreads) {
+        const float4 p = S.b.pos[bodies[l]];
+        const uint32_t ix = min(3u, (uint32_t)fmaxf(0.0f, (p.x - x0) * sx));
+        const uint32_t iz = min(3u, (uint32_t)fmaxf(0.0f, (p.z - z0) * sz));
+        const uint32_t t = ix * 4u + iz;
+        const uint32_t slot = atomicAdd(cl.map_shared_rank(sc, t), 1u);
+        newid[l] = slot * kClusterCtas + t;
+    }
+    cl.sync();
+    if (tid == 0) {  // a full tile: keep the plain ids
+        uint32_t over = 0;
+        for (uint32_t r = 0; r < kClusterCtas; ++r) over |= cl.map_shared_rank(sc, r)[0] > kClusterSlots ? 1u : 0u;
+        sc[1] = over;
+    }
+    __syncthreads();
+    const bool plain = sc[1] != 0u;
+    for (uint32_t l = gtid; l < nloc; l += gthreads) {  // the same thread wrote newid[l]
+        const uint32_t n = plain ? l : newid[l];
+        if (plain) newid[l] = l;
+        body_of[n] = bodies[l];
+    }
+    cl.sync();
+    uint32_t* la = const_cast<uint32_t*>(SC.con_la);
+    uint32_t* lb = const_cast<uint32_t*>(SC.con_lb);
+    for (uint32_t k = s0 + gtid; k < s1; k += gthreads) {
+        const uint32_t c = S.isl_con[k], a = S.con_la[c], b = S.con_lb[c];
+        la[c] = a == kNone ? kNone : __ldcg(&newid[a]);
+        lb[c] = b == kNone ? kNone : __ldcg(&newid[b]);
+    }
+    cl.sync();
+    return plain ? (nloc + kClusterCtas - 1 - rank) / kClusterCtas : sc[0];
+}
+
 // Islands with more than smem_bodies and at most kClusterCtas * kClusterSlots dynamic bodies.
 __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads, 1)
     k_solve_cluster(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
     extern __shared__ float4 smem[];
     __shared__ unsigned long long red[6];
     __shared__ uint32_t soff[kClusterOffs + 2];
-    __shared__ uint32_t rall[kClusterCtas], tmp[33];
+    __shared__ uint32_t rall[kClusterCtas], tmp[33], sc[2];
+    __shared__ float sbb[40];
     cg::cluster_group cl = cg::this_cluster();
     float4* sv = smem;
     float4* sw = smem + kClusterSlots;
@@ -778,33 +885,40 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
     const uint32_t n = cnt->nlarge;
     const ClusterView V{sv, sw, S.b.lv, S.b.av, rank};
     const ClusterSync sync{red};
+    SolveBufs SC = S;  // the island's constraints with permuted local ids
+    SC.con_la = S.cl_ids + 2u * kClusterGrid * kClusterBodies;
+    SC.con_lb = SC.con_la + S.max_cons;
+    uint32_t* ids = S.cl_ids + 2u * kClusterBodies * cid;
+    const uint32_t* body_of = ids + kClusterBodies;
     for (uint32_t idx = cid; idx < n; idx += ncl) {  // the same islands in every CTA of a cluster
         const uint32_t isl = S.large_list[idx];
         if (!cluster_island(S, isl, smem_bodies)) continue;
-        const uint32_t nloc = S.meta[4 * isl + 3];
-        const uint32_t* bodies = S.isl_bodies + 2u * S.isl_start[isl];
-        for (uint32_t l = rank + kClusterCtas * tid; l < nloc; l += gthreads) {
-            sv[l / kClusterCtas] = S.b.lv[bodies[l]];
-            sw[l / kClusterCtas] = S.b.av[bodies[l]];
+        const uint32_t nown = cluster_layout(S, SC, isl, ids, sc, sbb, rank, gtid, gthreads);
+        for (uint32_t k = tid; k < nown; k += blockDim.x) {
+            const uint32_t b = __ldcg(&body_of[k * kClusterCtas + rank]);
+            sv[k] = S.b.lv[b];
+            sw[k] = S.b.av[b];
         }
         cl.sync();
         if (S.meta[4 * isl + 1] >= 2)  // prefetching needs two distinct levels
-            solve_velocity_packed(S, isl, V, S.pk + (size_t)cid * kPackArrays * S.pk_cap, soff, rall, tmp, rank, gtid,
+            solve_velocity_packed(SC, isl, V, S.pk + (size_t)cid * kPackArrays * S.pk_cap, soff, rall, tmp, rank, gtid,
                                   gthreads, sync, cnt);
         else
-            solve_velocity(S, isl, V, gtid, gthreads, sync, cnt);
-        for (uint32_t l = rank + kClusterCtas * tid; l < nloc; l += gthreads) {
-            S.b.lv[bodies[l]] = sv[l / kClusterCtas];
-            S.b.av[bodies[l]] = sw[l / kClusterCtas];
-            sv[l / kClusterCtas] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // pseudo velocities start at zero
-            sw[l / kClusterCtas] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            solve_velocity(SC, isl, V, gtid, gthreads, sync, cnt);
+        for (uint32_t k = tid; k < nown; k += blockDim.x) {
+            const uint32_t b = __ldcg(&body_of[k * kClusterCtas + rank]);
+            S.b.lv[b] = sv[k];
+            S.b.av[b] = sw[k];
+            sv[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // pseudo velocities start at zero
+            sw[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
         cl.sync();
-        solve_bias(S, isl, V, gtid, gthreads, sync);
+        solve_bias(SC, isl, V, gtid, gthreads, sync);
         if (!S.vel_bias)
-            for (uint32_t l = rank + kClusterCtas * tid; l < nloc; l += gthreads) {
-                S.b.plv[bodies[l]] = sv[l / kClusterCtas];
-                S.b.pav[bodies[l]] = sw[l / kClusterCtas];
+            for (uint32_t k = tid; k < nown; k += blockDim.x) {
+                const uint32_t b = __ldcg(&body_of[k * kClusterCtas + rank]);
+                S.b.plv[b] = sv[k];
+                S.b.pav[b] = sw[k];
             }
         cl.sync();
     }

@@ -609,6 +609,8 @@ size_t pack_elements(uint32_t points, uint32_t* cap) {
     return (size_t)kClusterGrid * kPackArrays * *cap;
 }
 
+size_t cluster_id_words(uint32_t max_cons) { return 2ull * kClusterGrid * kClusterBodies + 2ull * max_cons; }
+
 // Whether this device can hold one k_solve_cluster cluster (checked once in configure_kernels).
 static bool g_cluster_ok = false;
 
@@ -720,7 +722,7 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
                  ctx.isl_small, ctx.isl_large, ctx.r, ctx.b, ctx.ss.velocity_iterations,
                  ctx.ss.position_iterations, ctx.ss.warm_start_factor, ctx.ss.use_velocity_bias,
                  ctx.ss.residual_tolerance, ctx.ss.max_velocity_iterations, ctx.brec, ctx.pk,
-                 g_cluster_ok ? ctx.pk_cap : 0u};
+                 g_cluster_ok ? ctx.pk_cap : 0u, ctx.isl_con, ctx.cfg.max_pairs, ctx.cl_ids};
     k_solve_warp<<<152u * 16u, kWarpsPerBlock * 32, kWarpsPerBlock * 2 * kWarpBodies * sizeof(float4), st>>>(SV, ctx.dcnt);
     k_solve_cta<<<152u * 2u, kCtaThreads, 2 * kCtaBodiesMax * sizeof(float4), st>>>(SV, ctx.dcnt, kCtaBodiesMax);
     if (g_cluster_ok) {
