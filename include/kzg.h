@@ -156,6 +156,7 @@ typedef struct {
 #define KZG_DEVERR_CACHE 2u     /* cache table full */
 #define KZG_DEVERR_EPA 4u       /* EPA polytope exceeded its face capacity */
 #define KZG_DEVERR_MANIFOLD 8u  /* a manifold produced more than 4 points */
+#define KZG_DEVERR_WAIT 16u     /* a bounded wait between the warps of a kernel gave up (step abandoned) */
 
 /* ---- lifecycle (PhysicsWorld ctor/dtor, PhysicsWorld.cpp:64-78) ----------------------------- */
 kzg_status kzg_create(const kzg_config* cfg, kzg_ctx** out);

@@ -55,6 +55,9 @@ struct SchedBufs {
 
 struct SchedShared {  // per island scratch living in shared memory
     uint32_t nloc, hub0, hub1, nbt, nv, nw, nb, total, ff_ok;
+    uint32_t ff_final;   // streamed first fit: batches below this are full and their records written
+    uint32_t ff_done;    // 0 running, 1 done (nbt set), 2 gave up
+    uint32_t stream_ok;  // the velocity level sweep ran behind the first fit
 };
 
 __device__ __forceinline__ uint32_t* rec(const SchedBufs& S, uint32_t r) { return reinterpret_cast<uint32_t*>(S.brec + 4ull * r); }
@@ -307,7 +310,8 @@ __device__ __forceinline__ void ff_shift_codes(uint32_t& w0, uint32_t& w1, uint3
 // neither body: one scan serves the whole constraint, and the points are placed by the lanes that
 // found their candidates.  Constraint fields are fetched two 32-constraint windows ahead.
 __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1, uint32_t rb, uint32_t hub0,
-                                   uint32_t hub1, uint32_t nloc, uint8_t* smem, uint32_t lane) {
+                                   uint32_t hub1, uint32_t nloc, uint8_t* smem, uint32_t lane,
+                                   volatile uint32_t* pub = nullptr) {
     const unsigned full = 0xffffffffu, lt = (1u << lane) - 1u;
     const FfTable T = ff_table_of(smem);
     uint32_t ns = 0, nbt = 0, nl0 = 0, nl1 = 0, head = 0, head0 = 0, head1 = 0;
@@ -377,6 +381,12 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
         wns = ns;
         win = true;
         wdirty = false;
+        if (pub) {  // every batch before the first open one is full, its records written
+            const uint32_t fb = __shfl_sync(full, head < ns ? wbid : nbt, 0);
+            __syncwarp();
+            __threadfence_block();
+            if (lane == 0) *pub = fb;
+        }
     };
     // pipeline: id of the constraint two windows ahead, fields of the next window
     auto load_id = [&](uint32_t w0) -> uint32_t { return w0 + lane < s1 ? S.isl_con[w0 + lane] : kNone; };
@@ -619,6 +629,84 @@ __device__ void level_sweep(const SchedBufs& S, SchedShared* sh, uint32_t sweep,
     __syncwarp();
 }
 
+// The velocity level sweep run on its own warp behind the first fit (streamed first fit): batches
+// below sh->ff_final are full and final, so their points sit at 4 * batch + slot in batch order and
+// can be levelled while the first fit goes on; once it is done the rest (batches not full) follow.
+// Returns false - the caller then runs the sweep itself - if the first fit gave up.  The wait is
+// bounded: past kStreamSpins polls it raises KZG_DEVERR_WAIT and gives up.
+constexpr uint32_t kStreamSpins = 1u << 26;
+__device__ bool velocity_stream(const SchedBufs& S, Counters* cnt, SchedShared* sh, uint32_t* last, uint32_t rb,
+                                uint32_t base, uint32_t lane) {
+    const unsigned full = 0xffffffffu;
+    const uint32_t nloc = sh->nloc;
+    for (uint32_t k = lane; k < nloc; k += 32) last[k] = 0;
+    __syncwarp();
+    volatile uint32_t* vfin = &sh->ff_final;
+    volatile uint32_t* vdone = &sh->ff_done;
+    uint32_t b = 0, top = 0, spins = 0;
+    for (;;) {
+        uint32_t fin = 0, done = 0;
+        for (;;) {  // until 8 more batches are final, or the first fit is over
+            if (lane == 0) {
+                done = *vdone;
+                fin = *vfin;
+            }
+            done = __shfl_sync(full, done, 0);
+            fin = __shfl_sync(full, fin, 0);
+            if (done || fin >= b + 8) break;
+            if (++spins > kStreamSpins) {
+                if (lane == 0) atomicOr(&cnt->error, KZG_DEVERR_WAIT);
+                return false;
+            }
+            __nanosleep(128);
+        }
+        __threadfence_block();
+        if (done == 2u) return false;
+        if (fin < b + 8) break;  // done: the rest below
+        const uint32_t row = rec(S, rb + b + (lane >> 2))[12 + (lane & 3u)];
+        const uint32_t c = row >> 2;
+        const uint32_t lvl = level_window(last, true, S.con_la[c], S.con_lb[c], 1u, lane);
+        S.vitems[base + 4 * b + lane] = row;
+        S.vlev[base + 4 * b + lane] = lvl;
+        top = max(top, lvl);
+        b += 8;
+    }
+    const uint32_t nbt = sh->nbt;  // the batches from b on, in batch order
+    uint32_t pos = 4 * b;
+    for (uint32_t j0 = b; j0 < nbt; j0 += 32) {
+        const uint32_t j = j0 + lane;
+        const uint32_t* r = rec(S, rb + j);
+        const uint32_t cj = j < nbt ? r[3] : 0u;
+        uint32_t x = cj;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(full, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        for (uint32_t k = 0; k < cj; ++k) S.vitems[base + pos + x - cj + k] = r[12 + k];
+        pos += __shfl_sync(full, x, 31);
+    }
+    __syncwarp();
+    for (uint32_t w0 = 4 * b; w0 < pos; w0 += 32) {
+        const uint32_t i = w0 + lane;
+        const bool v = i < pos;
+        const uint32_t row = v ? S.vitems[base + i] : 0u, c = row >> 2;
+        const uint32_t lvl = level_window(last, v, v ? S.con_la[c] : kNone, v ? S.con_lb[c] : kNone, 1u, lane);
+        if (v) {
+            S.vlev[base + i] = lvl;
+            top = max(top, lvl);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) top = max(top, __shfl_xor_sync(full, top, o));
+    if (lane == 0) {
+        sh->nv = top;
+        sh->total = pos;
+    }
+    __syncwarp();
+    return true;
+}
+
 template <typename Sync>
 __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl, uint32_t tid, uint32_t nthreads,
                                 SchedShared* sh, uint32_t* tmp, uint32_t* last_sm, uint32_t last_cap, bool ff_table,
@@ -679,16 +767,36 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
     // ---- B: first-fit batching: one warp over the shared-memory table, else one lane.  When the
     // island's level tables do not fit shared memory anyway, warps 1 and 2 meanwhile run the warm
     // and bias level sweeps, which do not depend on the batches.
+    // Warp 3 then runs the velocity level sweep right behind the first fit (velocity_stream).
     const uint32_t nwarps = (nthreads + 31) >> 5;
     const bool early = nwarps >= 3 && sh->nloc > last_cap;
     const bool table_ff = ff_table && sh->ff_ok && sh->nloc <= kFfMaxLocal;
+    const bool stream = early && table_ff && nwarps >= 4;
+    if (tid == 0) {
+        sh->ff_final = 0;
+        sh->ff_done = 0;
+        sh->stream_ok = 0;
+    }
+    sync();
     if (table_ff && warp == 0) {
-        const uint32_t r = first_fit_warp(S, s0, s1, rb, sh->hub0, sh->hub1, sh->nloc, reinterpret_cast<uint8_t*>(last_sm), lane);
-        if (lane == 0) sh->nbt = r;
+        const uint32_t r = first_fit_warp(S, s0, s1, rb, sh->hub0, sh->hub1, sh->nloc, reinterpret_cast<uint8_t*>(last_sm),
+                                          lane, stream ? &sh->ff_final : nullptr);
+        __syncwarp();
+        __threadfence_block();
+        if (lane == 0) {
+            sh->nbt = r;
+            __threadfence_block();
+            *(volatile uint32_t*)&sh->ff_done = r == kNone ? 2u : 1u;
+        }
     }
     if (early && (warp == 1 || warp == 2)) level_sweep(S, sh, warp, S.last_g + warp * S.last_stride + boff, s0, s1, base, lane);
+    if (stream && warp == 3) {
+        const bool ok = velocity_stream(S, cnt, sh, S.last_g + boff, rb, base, lane);
+        if (lane == 0) sh->stream_ok = ok ? 1u : 0u;
+    }
     sync();
     const bool batched = table_ff && sh->nbt != kNone;
+    const bool streamed = batched && sh->stream_ok != 0u;
     sync();
     if (!batched && tid == 0) {
         const uint32_t hub0 = sh->hub0, hub1 = sh->hub1;
@@ -737,9 +845,9 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
     }
     sync();
 
-    // ---- C: velocity items in batch order
+    // ---- C: velocity items in batch order (the streamed sweep wrote them)
     const uint32_t nbt = sh->nbt;
-    {
+    if (!streamed) {
         const uint32_t chunk = (nbt + nthreads - 1) / nthreads;
         const uint32_t lo = min(nbt, tid * chunk), hi = min(nbt, lo + chunk);
         uint32_t part = 0;
@@ -765,6 +873,7 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
     const uint32_t nvit = sh->total;
     for (uint32_t sweep = 0; sweep < 3; ++sweep) {
         if (early && sweep != 0) continue;
+        if (streamed && sweep == 0) continue;
         const uint32_t owner = nwarps >= 3 ? sweep : 0;
         if (warp != owner) continue;
         uint32_t* last = (early ? nloc <= 3u * last_cap : nloc <= last_cap)
