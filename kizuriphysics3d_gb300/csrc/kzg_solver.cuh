@@ -571,30 +571,35 @@ struct PackItem {
     float4 q[kPackArrays];
 };
 
-__device__ __forceinline__ void pack_item(const SolveBufs& S, float4* pk, uint32_t cap, uint32_t k, uint32_t row) {
+// The fields of a point's packed item, gathered from its row and bodies.
+__device__ __forceinline__ void gather_item(const SolveBufs& S, uint32_t row, PackItem& it) {
     const uint32_t c = row >> 2;
     const uint32_t A = S.con_a[c], B = S.con_b[c], la = __ldcg(&S.con_la[c]), lb = __ldcg(&S.con_lb[c]);
     const float4 rA = S.r.rAr[row], rB = S.r.rBr[row], bias = S.r.bias[row];
     const float4 n = S.r.n[row], t2 = S.r.t2[row], m = S.r.mass[row];
     const Mat3 IA = M3(&S.b.iiw[3 * A]), IB = M3(&S.b.iiw[3 * B]);
     const uint32_t st = la == kNone ? A : (lb == kNone ? B : kNone);
-    pk[0 * cap + k] = make_float4(rA.x, rA.y, rA.z, S.b.inv_mass[A]);
-    pk[1 * cap + k] = make_float4(rB.x, rB.y, rB.z, S.b.inv_mass[B]);
-    pk[2 * cap + k] = make_float4(n.x, n.y, n.z, bias.x + (S.vel_bias ? bias.y : 0.0f));
-    pk[3 * cap + k] = S.r.t1[row];
-    pk[4 * cap + k] = make_float4(t2.x, t2.y, t2.z, __uint_as_float(la));
-    pk[5 * cap + k] = make_float4(m.x, m.y, m.z, __uint_as_float(lb));
-    pk[6 * cap + k] = make_float4(IA.c0.x, IA.c0.y, IA.c0.z, IA.c1.x);
-    pk[7 * cap + k] = make_float4(IA.c1.y, IA.c1.z, IA.c2.x, IA.c2.y);
-    pk[8 * cap + k] = make_float4(IA.c2.z, IB.c0.x, IB.c0.y, IB.c0.z);
-    pk[9 * cap + k] = make_float4(IB.c1.x, IB.c1.y, IB.c1.z, IB.c2.x);
-    pk[10 * cap + k] = make_float4(IB.c2.y, IB.c2.z, __uint_as_float(row), 0.0f);
-    pk[11 * cap + k] = S.r.imp[row];
-    pk[12 * cap + k] = st == kNone ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : S.b.lv[st];
-    pk[13 * cap + k] = st == kNone ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : S.b.av[st];
+    it.q[0] = make_float4(rA.x, rA.y, rA.z, S.b.inv_mass[A]);
+    it.q[1] = make_float4(rB.x, rB.y, rB.z, S.b.inv_mass[B]);
+    it.q[2] = make_float4(n.x, n.y, n.z, bias.x + (S.vel_bias ? bias.y : 0.0f));
+    it.q[3] = S.r.t1[row];
+    it.q[4] = make_float4(t2.x, t2.y, t2.z, __uint_as_float(la));
+    it.q[5] = make_float4(m.x, m.y, m.z, __uint_as_float(lb));
+    it.q[6] = make_float4(IA.c0.x, IA.c0.y, IA.c0.z, IA.c1.x);
+    it.q[7] = make_float4(IA.c1.y, IA.c1.z, IA.c2.x, IA.c2.y);
+    it.q[8] = make_float4(IA.c2.z, IB.c0.x, IB.c0.y, IB.c0.z);
+    it.q[9] = make_float4(IB.c1.x, IB.c1.y, IB.c1.z, IB.c2.x);
+    it.q[10] = make_float4(IB.c2.y, IB.c2.z, __uint_as_float(row), 0.0f);
+    it.q[11] = S.r.imp[row];
+    it.q[12] = st == kNone ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : S.b.lv[st];
+    it.q[13] = st == kNone ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : S.b.av[st];
 }
 
-// Loads bypass L1: other CTAs of the cluster packed the items.
+__device__ __forceinline__ void store_pack(float4* pk, uint32_t cap, uint32_t k, const PackItem& it) {
+#pragma unroll
+    for (uint32_t j = 0; j < kPackArrays; ++j) pk[j * cap + k] = it.q[j];
+}
+
 __device__ __forceinline__ void load_pack(const float4* pk, uint32_t cap, uint32_t k, PackItem& it) {
 #pragma unroll
     for (uint32_t j = 0; j < kPackArrays; ++j) it.q[j] = __ldcg(&pk[j * cap + k]);
@@ -643,6 +648,105 @@ __device__ __forceinline__ float2 pack_solve(const ClusterView& V, float4* pk, u
     return r;
 }
 
+// Warm-start and bias points of a cluster island, loaded ahead: each thread loads its point of the
+// next level while it applies the current one (nothing a level writes is read by these loads but
+// the velocities, which are not part of them).
+struct WarmItem {
+    uint32_t A, B, la, lb;
+    float4 im, n, t1, t2, rA, rB;
+    float iA, iB;
+    Mat3 IA, IB;
+};
+__device__ __forceinline__ void load_warm(const SolveBufs& S, uint32_t row, WarmItem& w) {
+    const uint32_t c = row >> 2;
+    w.A = S.con_a[c];
+    w.B = S.con_b[c];
+    w.la = __ldcg(&S.con_la[c]);
+    w.lb = __ldcg(&S.con_lb[c]);
+    w.im = S.r.imp[row];
+    w.n = S.r.n[row];
+    w.t1 = S.r.t1[row];
+    w.t2 = S.r.t2[row];
+    w.rA = S.r.rA[row];
+    w.rB = S.r.rB[row];
+    w.iA = S.b.inv_mass[w.A];
+    w.iB = S.b.inv_mass[w.B];
+    w.IA = M3(&S.b.iiw[3 * w.A]);
+    w.IB = M3(&S.b.iiw[3 * w.B]);
+}
+// WarmStart for one loaded point (the arithmetic of warm_point).
+template <typename View>
+__device__ __forceinline__ void apply_warm(const SolveBufs& S, const View& V, const WarmItem& w) {
+    const Vec3 imp = ((V3(w.n) * w.im.x + V3(w.t1) * w.im.y) + V3(w.t2) * w.im.z) * S.ws_factor;
+    if (w.la != kNone) V.put(w.la, w.A, V.lin(w.la, w.A) + imp * w.iA, V.ang(w.la, w.A) + w.IA * V3(w.rA).cross(imp));
+    if (w.lb != kNone) V.put(w.lb, w.B, V.lin(w.lb, w.B) - imp * w.iB, V.ang(w.lb, w.B) - w.IB * V3(w.rB).cross(imp));
+}
+
+// Bias points load only their indices ahead (registers are short); their row and body data are
+// independent loads issued together at the level.
+struct BiasIdx {
+    uint32_t row, A, B, la, lb;
+};
+__device__ __forceinline__ void load_bias_idx(const SolveBufs& S, uint32_t row, BiasIdx& b) {
+    const uint32_t c = row >> 2;
+    b.row = row;
+    b.A = S.con_a[c];
+    b.B = S.con_b[c];
+    b.la = __ldcg(&S.con_la[c]);
+    b.lb = __ldcg(&S.con_lb[c]);
+}
+// SolveBiasConstraint for one point (the arithmetic of bias_point).
+template <typename View>
+__device__ __forceinline__ void apply_bias(const SolveBufs& S, const View& V, const BiasIdx& b) {
+    const uint32_t row = b.row, A = b.A, B = b.B, la = b.la, lb = b.lb;
+    const Vec3 rA = V3(S.r.rAr[row]), rB = V3(S.r.rBr[row]);
+    const Vec3 n = V3(S.r.n[row]);
+    const float nm = S.r.mass[row].x, pbias = S.r.bias[row].y;
+    float4 im = S.r.imp[row];
+    const float iA = S.b.inv_mass[A], iB = S.b.inv_mass[B];
+    const Mat3 IA = M3(&S.b.iiw[3 * A]), IB = M3(&S.b.iiw[3 * B]);
+    const Vec3 pvA = V.plin(la, A), pwA = V.pang(la, A);
+    const Vec3 pvB = V.plin(lb, B), pwB = V.pang(lb, B);
+    const Vec3 vr = (pvA + pwA.cross(rA)) - (pvB + pwB.cross(rB));
+    float lambda = -nm * (vr.dot(n) - pbias);
+    const float ni = rmax(im.w + lambda, 0.0f);
+    lambda = ni - im.w;
+    im.w = ni;
+    S.r.imp[row] = im;
+    const Vec3 imp = n * lambda;
+    if (la != kNone) V.put(la, A, pvA + imp * iA, pwA + IA * rA.cross(imp));
+    if (lb != kNone) V.put(lb, B, pvB - imp * iB, pwB - IB * rB.cross(imp));
+}
+
+// One pass over a sweep's levels (list/off at the island's regions), each thread taking the points
+// gtid, gtid + gthreads, ... of a level, its first point of the next level loaded ahead.
+template <typename Item, typename Sync, typename Load, typename Apply>
+__device__ __forceinline__ void sweep_prefetched(const uint32_t* list, const uint32_t* off, uint32_t base,
+                                                 uint32_t loff, uint32_t nl, uint32_t gtid, uint32_t gthreads,
+                                                 Sync sync, Load load, Apply apply) {
+    Item cur, nxt;
+    bool has_cur = nl && off[loff] + gtid < off[loff + 1];
+    if (has_cur) load(list[base + off[loff] + gtid], cur);
+    for (uint32_t l = 0; l < nl; ++l) {
+        const uint32_t lo = off[loff + l], hi = off[loff + l + 1];
+        bool has_nxt = false;
+        if (l + 1 < nl) {
+            const uint32_t kn = hi + gtid;
+            has_nxt = kn < off[loff + l + 2];
+            if (has_nxt) load(list[base + kn], nxt);
+        }
+        if (has_cur) apply(cur);
+        for (uint32_t k = lo + gtid + gthreads; k < hi; k += gthreads) {  // wide levels
+            Item x;
+            load(list[base + k], x);
+            apply(x);
+        }
+        sync();
+        cur = nxt;
+        has_cur = has_nxt;
+    }
+}
+
 // Warm start + velocity sweeps of a cluster island on packed items.  The points are first
 // partitioned: each level's points go to the CTAs holding their first dynamic bodies (counted into
 // every CTA's level table soff, scanned there, then packed at region start + level offset + rank).
@@ -651,22 +755,44 @@ __device__ __forceinline__ float2 pack_solve(const ClusterView& V, float4* pk, u
 // math.  Needs at least two velocity levels (the prefetched point must differ from the current one).
 template <typename Sync>
 __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const ClusterView& V, float4* pk,
-                                      uint32_t* soff, uint32_t* rall, uint32_t* tmp, uint32_t rank, uint32_t gtid,
-                                      uint32_t gthreads, Sync sync, Counters* cnt) {
+                                      uint32_t* soff, uint32_t* lofs, uint32_t* rall, uint32_t* tmp, uint32_t rank,
+                                      uint32_t gtid, uint32_t gthreads, Sync sync, Counters* cnt) {
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t cap = S.pk_cap, tid = threadIdx.x, nthr = blockDim.x;
     const uint32_t base = 4u * S.isl_start[isl], loff = base + isl;
     const uint32_t nw = S.meta[4 * isl], nv = S.meta[4 * isl + 1];
     const uint32_t total = S.vl_off[loff + nv];
-    // ---- partition: counts per (level, owner); a point's rank inside its group goes to vrec.x
-    for (uint32_t l = tid; l <= nv; l += nthr) soff[l] = 0;
+    // ---- partition: counts per (level, owner); a point's rank inside its group goes to vrec.x.
+    // Both passes walk the island's points flat, kB per thread at once so that their loads overlap;
+    // a point's level comes from the level offsets staged in lofs.
+    for (uint32_t l = tid; l <= nv; l += nthr) {
+        soff[l] = 0;
+        lofs[l] = S.vl_off[loff + l];
+    }
     cl.sync();
-    for (uint32_t l = 0; l < nv; ++l) {
-        const uint32_t hi = S.vl_off[loff + l + 1];
-        for (uint32_t k = S.vl_off[loff + l] + gtid; k < hi; k += gthreads) {
-            const uint32_t o = point_owner(S, S.vl_list[base + k]);
-            S.vrec[base + k].x = atomicAdd(cl.map_shared_rank(soff, o) + l, 1u);
+    auto level_of = [&](uint32_t k) -> uint32_t {  // the level l with lofs[l] <= k < lofs[l + 1]
+        uint32_t lo = 0, hi = nv;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (lofs[mid] <= k) lo = mid; else hi = mid;
         }
+        return lo;
+    };
+    constexpr uint32_t kB = 4;
+    for (uint32_t k0 = gtid; k0 < total; k0 += kB * gthreads) {
+        uint32_t rw[kB], lv[kB], ow[kB];
+#pragma unroll
+        for (uint32_t j = 0; j < kB; ++j) {
+            const uint32_t k = k0 + j * gthreads;
+            rw[j] = k < total ? S.vl_list[base + k] : 0u;
+            lv[j] = k < total ? level_of(k) : 0u;
+        }
+#pragma unroll
+        for (uint32_t j = 0; j < kB; ++j) ow[j] = k0 + j * gthreads < total ? point_owner(S, rw[j]) : 0u;
+#pragma unroll
+        for (uint32_t j = 0; j < kB; ++j)
+            if (k0 + j * gthreads < total)
+                S.vrec[base + k0 + j * gthreads].x = atomicAdd(cl.map_shared_rank(soff, ow[j]) + lv[j], 1u);
     }
     cl.sync();
     {  // exclusive scan of this CTA's level counts; soff[nv] = its points
@@ -693,20 +819,18 @@ __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const Cl
             run += c;
         }
     __syncthreads();
-    for (uint32_t l = 0; l < nv; ++l) {
-        const uint32_t hi = S.vl_off[loff + l + 1];
-        for (uint32_t k = S.vl_off[loff + l] + gtid; k < hi; k += gthreads) {
-            const uint32_t row = S.vl_list[base + k], o = point_owner(S, row);
-            pack_item(S, pk, cap, rall[o] + cl.map_shared_rank(soff, o)[l] + S.vrec[base + k].x, row);
-        }
+    for (uint32_t k = gtid; k < total; k += gthreads) {
+        const uint32_t row = S.vl_list[base + k], o = point_owner(S, row);
+        const uint32_t pos = rall[o] + cl.map_shared_rank(soff, o)[level_of(k)] + S.vrec[base + k].x;
+        PackItem x;
+        gather_item(S, row, x);
+        store_pack(pk, cap, pos, x);
     }
     const uint32_t R = rall[rank];
     sync.reset(gtid);  // a cluster barrier: every packed point is visible
-    for (uint32_t l = 0; l < nw; ++l) {
-        const uint32_t e = S.wl_off[loff + l + 1];
-        for (uint32_t k = S.wl_off[loff + l] + gtid; k < e; k += gthreads) warm_point(S, V, S.wl_list[base + k]);
-        sync();
-    }
+    sweep_prefetched<WarmItem>(S.wl_list, S.wl_off, base, loff, nw, gtid, gthreads, sync,
+                               [&](uint32_t row, WarmItem& w) { load_warm(S, row, w); },
+                               [&](const WarmItem& w) { apply_warm(S, V, w); });
     const bool residual = S.res_tol > 0.0f;
     const uint32_t iters = residual ? S.res_cap : S.vel_iters;
     uint32_t used = 0;
@@ -873,7 +997,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
     k_solve_cluster(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
     extern __shared__ float4 smem[];
     __shared__ unsigned long long red[6];
-    __shared__ uint32_t soff[kClusterOffs + 2];
+    __shared__ uint32_t soff[kClusterOffs + 2], lofs[kClusterOffs + 1];
     __shared__ uint32_t rall[kClusterCtas], tmp[33], sc[2];
     __shared__ float sbb[40];
     cg::cluster_group cl = cg::this_cluster();
@@ -901,8 +1025,8 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
         }
         cl.sync();
         if (S.meta[4 * isl + 1] >= 2)  // prefetching needs two distinct levels
-            solve_velocity_packed(SC, isl, V, S.pk + (size_t)cid * kPackArrays * S.pk_cap, soff, rall, tmp, rank, gtid,
-                                  gthreads, sync, cnt);
+            solve_velocity_packed(SC, isl, V, S.pk + (size_t)cid * kPackArrays * S.pk_cap, soff, lofs, rall, tmp, rank,
+                                  gtid, gthreads, sync, cnt);
         else
             solve_velocity(SC, isl, V, gtid, gthreads, sync, cnt);
         for (uint32_t k = tid; k < nown; k += blockDim.x) {
@@ -913,7 +1037,13 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
             sw[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
         cl.sync();
-        solve_bias(SC, isl, V, gtid, gthreads, sync);
+        if (!S.vel_bias) {
+            const uint32_t base = 4u * S.isl_start[isl], loff = base + isl, nbl = S.meta[4 * isl + 2];
+            for (uint32_t it = 0; it < S.pos_iters; ++it)
+                sweep_prefetched<BiasIdx>(S.bl_list, S.bl_off, base, loff, nbl, gtid, gthreads, sync,
+                                          [&](uint32_t row, BiasIdx& b) { load_bias_idx(SC, row, b); },
+                                          [&](const BiasIdx& b) { apply_bias(SC, V, b); });
+        }
         if (!S.vel_bias)
             for (uint32_t k = tid; k < nown; k += blockDim.x) {
                 const uint32_t b = __ldcg(&body_of[k * kClusterCtas + rank]);
