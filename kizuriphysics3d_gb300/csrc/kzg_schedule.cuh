@@ -724,30 +724,68 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
     if (ff_table)
         for (uint32_t k = tid; k < kFfCodes; k += nthreads) T.keys[k] = kNone;
     sync();
-    for (uint32_t s = s0 + tid; s < s1; s += nthreads) {
-        const uint32_t c = S.isl_con[s], bits = S.con_bits[c];
-        const uint32_t xs[2] = {S.con_a[c], S.con_b[c]};
-        for (int q = 0; q < 2; ++q) {
-            const uint32_t x = xs[q];
-            if (bits & (2u << q)) {
-                if (atomicExch(&S.body_stamp[x], cnt->frame) != cnt->frame) {
-                    const uint32_t l = atomicAdd(&sh->nloc, 1u);
-                    S.body_loc[x] = l;
-                    S.isl_bodies[boff + l] = x;
+    // (the constraint loops take kA constraints per thread at once so that their loads overlap)
+    constexpr uint32_t kA = 4;
+    const uint32_t frame = cnt->frame;
+    for (uint32_t t0 = s0 + tid; t0 < s1; t0 += kA * nthreads) {
+        uint32_t cc[kA], bb[kA], xa[kA], xb[kA], ea[kA], eb[kA];
+#pragma unroll
+        for (uint32_t j = 0; j < kA; ++j) cc[j] = t0 + j * nthreads < s1 ? S.isl_con[t0 + j * nthreads] : kNone;
+#pragma unroll
+        for (uint32_t j = 0; j < kA; ++j) {
+            bb[j] = cc[j] != kNone ? S.con_bits[cc[j]] : 0u;
+            xa[j] = cc[j] != kNone ? S.con_a[cc[j]] : 0u;
+            xb[j] = cc[j] != kNone ? S.con_b[cc[j]] : 0u;
+        }
+#pragma unroll
+        for (uint32_t j = 0; j < kA; ++j) {  // first touch of a dynamic body this frame: a local index
+            ea[j] = (bb[j] & 2u) ? atomicExch(&S.body_stamp[xa[j]], frame) : frame;
+            eb[j] = (bb[j] & 4u) ? atomicExch(&S.body_stamp[xb[j]], frame) : frame;
+        }
+#pragma unroll
+        for (uint32_t j = 0; j < kA; ++j) {
+            if (cc[j] == kNone) continue;
+            const uint32_t xs[2] = {xa[j], xb[j]}, es[2] = {ea[j], eb[j]};
+            for (int q = 0; q < 2; ++q) {
+                const uint32_t x = xs[q];
+                if (bb[j] & (2u << q)) {
+                    if (es[q] != frame) {
+                        const uint32_t l = atomicAdd(&sh->nloc, 1u);
+                        S.body_loc[x] = l;
+                        S.isl_bodies[boff + l] = x;
+                    }
+                } else if (S.is_large[x] && !(bb[j] & 1u)) {
+                    atomicMin(&sh->hub0, x);
                 }
-            } else if (S.is_large[x] && !(bits & 1u)) {
-                atomicMin(&sh->hub0, x);
             }
         }
     }
     sync();
-    for (uint32_t s = s0 + tid; s < s1; s += nthreads) {
-        const uint32_t c = S.isl_con[s], bits = S.con_bits[c];
-        S.con_la[c] = (bits & 2u) ? S.body_loc[S.con_a[c]] : kNone;
-        S.con_lb[c] = (bits & 4u) ? S.body_loc[S.con_b[c]] : kNone;
-        const uint32_t xs[2] = {S.con_a[c], S.con_b[c]};
-        for (int q = 0; q < 2; ++q)
-            if (!(bits & (2u << q)) && S.is_large[xs[q]] && !(bits & 1u) && xs[q] != sh->hub0) atomicMin(&sh->hub1, xs[q]);
+    for (uint32_t t0 = s0 + tid; t0 < s1; t0 += kA * nthreads) {
+        uint32_t cc[kA], bb[kA], xa[kA], xb[kA], la[kA], lb[kA];
+#pragma unroll
+        for (uint32_t j = 0; j < kA; ++j) cc[j] = t0 + j * nthreads < s1 ? S.isl_con[t0 + j * nthreads] : kNone;
+#pragma unroll
+        for (uint32_t j = 0; j < kA; ++j) {
+            bb[j] = cc[j] != kNone ? S.con_bits[cc[j]] : 0u;
+            xa[j] = cc[j] != kNone ? S.con_a[cc[j]] : 0u;
+            xb[j] = cc[j] != kNone ? S.con_b[cc[j]] : 0u;
+        }
+#pragma unroll
+        for (uint32_t j = 0; j < kA; ++j) {
+            la[j] = (bb[j] & 2u) ? S.body_loc[xa[j]] : kNone;
+            lb[j] = (bb[j] & 4u) ? S.body_loc[xb[j]] : kNone;
+        }
+#pragma unroll
+        for (uint32_t j = 0; j < kA; ++j) {
+            if (cc[j] == kNone) continue;
+            S.con_la[cc[j]] = la[j];
+            S.con_lb[cc[j]] = lb[j];
+            const uint32_t xs[2] = {xa[j], xb[j]};
+            for (int q = 0; q < 2; ++q)
+                if (!(bb[j] & (2u << q)) && S.is_large[xs[q]] && !(bb[j] & 1u) && xs[q] != sh->hub0)
+                    atomicMin(&sh->hub1, xs[q]);
+        }
     }
     sync();
     if (ff_table) {  // codes of the non-dynamic, non-hub bodies of batched constraints
