@@ -54,6 +54,7 @@ struct Counters {  // device-side counters, copied back after each stage that si
     uint32_t nsmall;
     uint32_t nlarge;
     uint32_t nepa;
+    uint32_t epa_next;   // next deferred pair for the EPA warps
     uint32_t max_iters;  // most velocity iterations of an island
     uint32_t pt_iters;   // sum of batched points x iterations
     uint32_t res_bits;   // largest final residual (float bits, >= 0)

@@ -251,7 +251,7 @@ __device__ inline void gjk(const SupportMap& map, float tol, uint32_t max_iter, 
 // EPA (EPA.cpp:16-296).  Polytope capacities are the reference's (256 vertices are never
 // reached: 4 + 64 iterations; 512 faces; 256 horizon edges).
 // ---------------------------------------------------------------------------------------------
-constexpr uint32_t kEpaVerts = 72;
+constexpr uint32_t kEpaVerts = 68;  // the initial tetrahedron + one vertex per iteration (64)
 constexpr uint32_t kEpaFaces = 512;
 constexpr uint32_t kEpaHorizon = 256;
 
@@ -400,7 +400,9 @@ __device__ inline void epa_finish(const EpaFace& f, const SP* vs, EpaOut& r) {
 struct EpaWarpSmem {
     float vp[kEpaVerts][3], va[kEpaVerts][3], vb[kEpaVerts][3];  // SupportPoint p, pointA, pointB
     float fnx[kEpaFaces], fny[kEpaFaces], fnz[kEpaFaces], fd[kEpaFaces];
-    uint8_t fa[kEpaFaces], fb[kEpaFaces], fc[kEpaFaces], dead[kEpaFaces];
+    uint8_t fa[kEpaFaces], fb[kEpaFaces], fc[kEpaFaces];
+    uint32_t dead[kEpaFaces / 32];  // visible faces of the current iteration, one bit each
+    uint32_t ebits[(kEpaVerts * kEpaVerts + 31) / 32];  // directed edges (u, v) of the visible faces
     uint16_t vis[kEpaFaces];
     uint8_t hu[kEpaHorizon], hv[kEpaHorizon];
 };
@@ -543,33 +545,40 @@ __device__ inline void epa_warp(const SupportMap& map, const GjkOut& g, float to
             if (i < nf) {
                 const Vec3 n(S.fnx[i], S.fny[i], S.fnz[i]);
                 v = n.dot(w.p) - S.fd[i] > eps;
-                S.dead[i] = v ? 1 : 0;
             }
             const unsigned m = __ballot_sync(full, v);
+            if (lane == 0) S.dead[base >> 5] = m;
             if (v) S.vis[nvis + __popc(m & lt)] = (uint16_t)i;
             nvis += __popc(m);
         }
         __syncwarp();
-        // horizon: edges of visible faces without a reverse edge in another visible face
+        // horizon: edges of visible faces without a reverse edge in another visible face.  The
+        // visible faces' directed edges go into a bit table first (a face never holds both (u, v)
+        // and (v, u): its three vertices differ), so each edge's test is one lookup.
         uint32_t nh = 0;
         const uint32_t items = 3 * nvis;
+        constexpr uint32_t kEdgeWords = (kEpaVerts * kEpaVerts + 31) / 32;
+        for (uint32_t k = lane; k < kEdgeWords; k += 32) S.ebits[k] = 0u;
+        __syncwarp();
+        for (uint32_t item = lane; item < items; item += 32) {
+            const uint32_t fi = S.vis[item / 3], e = item % 3;
+            const uint32_t A = S.fa[fi], B = S.fb[fi], C = S.fc[fi];
+            const uint32_t u = e == 0 ? A : (e == 1 ? B : C), v = e == 0 ? B : (e == 1 ? C : A);
+            const uint32_t key = u * kEpaVerts + v;
+            atomicOr(&S.ebits[key >> 5], 1u << (key & 31u));
+        }
+        __syncwarp();
         for (uint32_t base = 0; base < items; base += 32) {
             const uint32_t item = base + lane;
             bool keep = false;
             uint32_t eu = 0, ev = 0;
             if (item < items) {
-                const uint32_t vi = item / 3, e = item % 3, fi = S.vis[vi];
+                const uint32_t fi = S.vis[item / 3], e = item % 3;
                 const uint32_t A = S.fa[fi], B = S.fb[fi], C = S.fc[fi];
                 eu = e == 0 ? A : (e == 1 ? B : C);
                 ev = e == 0 ? B : (e == 1 ? C : A);
-                bool shared = false;
-                for (uint32_t vj = 0; vj < nvis && !shared; ++vj) {
-                    if (vj == vi) continue;
-                    const uint32_t fj = S.vis[vj];
-                    const uint32_t a2 = S.fa[fj], b2 = S.fb[fj], c2 = S.fc[fj];
-                    shared = (a2 == ev && b2 == eu) || (b2 == ev && c2 == eu) || (c2 == ev && a2 == eu);
-                }
-                keep = !shared;
+                const uint32_t rkey = ev * kEpaVerts + eu;
+                keep = !((S.ebits[rkey >> 5] >> (rkey & 31u)) & 1u);
             }
             const unsigned m = __ballot_sync(full, keep);
             const uint32_t pos = nh + __popc(m & lt);
@@ -581,7 +590,7 @@ __device__ inline void epa_warp(const SupportMap& map, const GjkOut& g, float to
         uint32_t wi = 0;
         for (uint32_t base = 0; base < nf; base += 32) {
             const uint32_t i = base + lane;
-            const bool alive = i < nf && !S.dead[i];
+            const bool alive = i < nf && !((S.dead[i >> 5] >> (i & 31u)) & 1u);
             uint32_t a = 0, b = 0, c = 0;
             float nx = 0.0f, ny = 0.0f, nz = 0.0f, dd = 0.0f;
             if (alive) { a = S.fa[i]; b = S.fb[i]; c = S.fc[i]; nx = S.fnx[i]; ny = S.fny[i]; nz = S.fnz[i]; dd = S.fd[i]; }

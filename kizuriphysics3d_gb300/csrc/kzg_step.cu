@@ -218,13 +218,18 @@ __global__ void __launch_bounds__(128) k_narrow(ShapeTables T, DeviceBodies b, c
 // One warp per deferred pair: the same routine with the warp-cooperative EPA.
 constexpr uint32_t kEpaWarps = 4;
 __global__ void __launch_bounds__(kEpaWarps * 32) k_narrow_epa(ShapeTables T, DeviceBodies b, const uint2* __restrict__ pairs,
-                                                               const Counters* cnt, const uint32_t* __restrict__ epa_list,
+                                                               Counters* cnt, const uint32_t* __restrict__ epa_list,
                                                                uint32_t* m_count, float4* m_data, unsigned long long* m_key,
                                                                uint32_t* err) {
     extern __shared__ EpaWarpSmem epa_smem[];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t n = cnt->nepa;
-    for (uint32_t idx = blockIdx.x * kEpaWarps + warp; idx < n; idx += gridDim.x * kEpaWarps) {
+    // pairs are taken from a shared counter: their EPA costs vary by orders of magnitude
+    for (;;) {
+        uint32_t idx = 0;
+        if (lane == 0) idx = atomicAdd(&cnt->epa_next, 1u);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx >= n) break;
         const uint32_t i = epa_list[idx];
         const uint2 pr = pairs[i];
         const uint32_t A = pr.x, B = pr.y;
@@ -620,6 +625,8 @@ cudaError_t configure_kernels() {
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_narrow_epa, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(kEpaWarps * sizeof(EpaWarpSmem)));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_narrow_epa, cudaFuncAttributePreferredSharedMemoryCarveout, 100);  // 4 CTAs per SM
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_schedule_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(3 * kSchedCtaBodies * sizeof(uint32_t)));
