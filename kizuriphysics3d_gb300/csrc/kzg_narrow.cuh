@@ -628,6 +628,7 @@ __device__ inline void epa_warp(const SupportMap& map, const GjkOut& g, float to
 // to a worklist; the warp-per-pair pass runs them cooperatively.
 struct EpaDefer {
     bool deferred = false;
+    __device__ bool solo() const { return true; }
     __device__ void operator()(const SupportMap&, const GjkOut&, float, uint32_t, EpaOut& e) {
         deferred = true;
         e.valid = false;
@@ -638,6 +639,7 @@ struct EpaCoop {
     uint32_t lane;
     uint32_t* err;
     bool deferred = false;
+    __device__ bool solo() const { return lane == 0; }  // the lane that stores the manifold
     __device__ void operator()(const SupportMap& m, const GjkOut& g, float tol, uint32_t it, EpaOut& e) {
         epa_warp(m, g, tol, it, *S, e, lane, err);
     }
@@ -817,6 +819,7 @@ __device__ inline uint32_t collide_generic(const ShapeTables& T, const Body& A, 
         epa(map, g, tol, 64, e);
         if (epa.deferred) return 0;
         if (e.valid) {
+            if (!epa.solo()) return 0;  // a cooperative EPA: one lane finishes the manifold
             if (collide_polyhedral(T, A, B, max_sep, m, e.normal) > 0) return m.n;
             add_point(m, e.pA, e.pB, e.normal, -e.depth);
             return m.n;

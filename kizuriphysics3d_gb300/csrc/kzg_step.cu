@@ -116,22 +116,23 @@ __global__ void k_find_pairs(DeviceBodies b, uint32_t n, const unsigned long lon
     if (is_large[i]) return;
     Vec3 c = (V3(b.aabb_mn[i]) + V3(b.aabb_mx[i])) * 0.5f;
     int ix = (int)cell_coord(c.x, inv_cell), iy = (int)cell_coord(c.y, inv_cell), iz = (int)cell_coord(c.z, inv_cell);
+    // The three cells along z of a column are consecutive keys (cell coordinates stay far from the
+    // 16-bit field's ends), so each of the 9 columns is one lower_bound and a forward scan.
     for (int dx = -1; dx <= 1; ++dx)
-        for (int dy = -1; dy <= 1; ++dy)
-            for (int dz = -1; dz <= 1; ++dz) {
-                unsigned long long key = cell_key(wi, (uint32_t)(ix + dx), (uint32_t)(iy + dy), (uint32_t)(iz + dz));
-                // lower_bound
-                uint32_t lo = 0, hi = nsmall;
-                while (lo < hi) {
-                    uint32_t mid = (lo + hi) >> 1;
-                    if (skeys[mid] < key) lo = mid + 1; else hi = mid;
-                }
-                for (uint32_t s = lo; s < nsmall && skeys[s] == key; ++s) {
-                    uint32_t j = svals[s];
-                    if (b.packed[j] <= pi) continue;
-                    if (pair_ok(b, i, j)) emit_pair(out, cnt, cap, pi, b.packed[j]);
-                }
+        for (int dy = -1; dy <= 1; ++dy) {
+            const unsigned long long key = cell_key(wi, (uint32_t)(ix + dx), (uint32_t)(iy + dy), (uint32_t)(iz - 1));
+            const unsigned long long key_hi = key + 2;
+            uint32_t lo = 0, hi = nsmall;  // lower_bound
+            while (lo < hi) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (skeys[mid] < key) lo = mid + 1; else hi = mid;
             }
+            for (uint32_t s = lo; s < nsmall && skeys[s] <= key_hi; ++s) {
+                uint32_t j = svals[s];
+                if (b.packed[j] <= pi) continue;
+                if (pair_ok(b, i, j)) emit_pair(out, cnt, cap, pi, b.packed[j]);
+            }
+        }
 }
 
 // Per-step counters to zero, the step counter advanced (the first kernel of every step).
