@@ -200,7 +200,7 @@ struct GjkOut {
     SP simplex[4];
 };
 
-__device__ inline void gjk(const SupportMap& map, float tol, uint32_t max_iter, GjkOut& r) {
+static __device__ __noinline__ void gjk(const SupportMap& map, float tol, uint32_t max_iter, GjkOut& r) {
     r.intersect = false;
     r.distance = 0.0f;
     r.pA = r.pB = r.normal = Vec3();
@@ -481,7 +481,7 @@ __device__ __forceinline__ uint32_t epa_best_face(const EpaWarpSmem& S, uint32_t
 // EPA::Compute (EPA.cpp:176-296) by one warp.  Every per-face float operation runs on one lane in
 // the reference's order; selections use the reference's tie rules and ordered ballot compaction
 // keeps the visible list, horizon edges and face array in the reference's order.
-__device__ inline void epa_warp(const SupportMap& map, const GjkOut& g, float tol, uint32_t max_iter, EpaWarpSmem& S,
+static __device__ __noinline__ void epa_warp(const SupportMap& map, const GjkOut& g, float tol, uint32_t max_iter, EpaWarpSmem& S,
                          EpaOut& r, uint32_t lane, uint32_t* err) {
     const unsigned full = 0xffffffffu;
     const unsigned lt = (1u << lane) - 1u;
@@ -726,7 +726,7 @@ __device__ inline bool is_poly(const ShapeDev* s) { return s->type == kBox || s-
 
 // Writes at most kMaxFaceVerts*2 candidate points before reduction; keeps the reference's
 // (i*(n-1)/3) reduction of more than four points.
-__device__ inline uint32_t collide_polyhedral(const ShapeTables& T, const Body& A, const Body& B, float max_sep,
+static __device__ __noinline__ uint32_t collide_polyhedral(const ShapeTables& T, const Body& A, const Body& B, float max_sep,
                                               Manifold& m, const Vec3& normal) {
     Vec3 fa[kMaxFaceVerts], fb[kMaxFaceVerts], na, nb;
     uint32_t ca = 0, cb = 0;
