@@ -650,7 +650,7 @@ struct EpaCoop {
 // ---------------------------------------------------------------------------------------------
 constexpr uint32_t kMaxFaceVerts = 16;
 
-__device__ inline bool shape_face(const ShapeTables& T, const Body& b, const Vec3& wdir, Vec3* out, uint32_t& cnt,
+static __device__ __noinline__ bool shape_face(const ShapeTables& T, const Body& b, const Vec3& wdir, Vec3* out, uint32_t& cnt,
                                   Vec3& nworld) {
     const ShapeDev* s = b.s;
     if (s->type == kBox) {
@@ -876,7 +876,7 @@ __device__ inline uint32_t collide_sphere_sphere(const Body& A, const Body& B, f
     return m.n;
 }
 
-__device__ inline uint32_t collide_plane_convex(const ShapeTables& T, const Body& P, const Body& B, float max_sep,
+static __device__ __noinline__ uint32_t collide_plane_convex(const ShapeTables& T, const Body& P, const Body& B, float max_sep,
                                                 Manifold& m) {
     Vec3 pn = P.q.rotate(Vec3(P.s->p[0], P.s->p[1], P.s->p[2]));
     float pd = P.s->p[3] + pn.dot(P.t);
