@@ -432,13 +432,23 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
             const uint32_t np = md & 15u, x0 = xx & 0xFFFFu, x1 = xx >> 16;
             const int hub = (int)((md >> 4) & 3u) - 1;
             const uint32_t hflag = hub == 0 ? kFfH0 : (hub == 1 ? kFfH1 : 0u);
+            // the next constraint's fields, fetched up front so that its fits overlap this one's
+            const uint32_t kB = k + 1 < m ? k + 1 : k;
+            const uint32_t mdB = __shfl_sync(full, meta, kB);
+            const uint32_t cB = __shfl_sync(full, mc, kB), xxB = __shfl_sync(full, dx, kB);
+            const bool canB = k + 1 < m && !(mdB & 64u);
+            const uint32_t npB = mdB & 15u, x0B = xxB & 0xFFFFu, x1B = xxB >> 16;
+            const uint32_t hB = (mdB >> 4) & 3u;
+            const uint32_t hfB = hB == 1u ? kFfH0 : (hB == 2u ? kFfH1 : 0u);
             // ---- fast path: the first np lanes of the held window that take a point (sliding the
             // window once past its full batches if it has to)
             bool done = false;
             for (int attempt = 0; attempt < 2; ++attempt) {
                 if (!win) win_load();
                 const bool ok = win_fits(x0, x1, hflag);
+                const bool okBl = win_fits(x0B, x1B, hfB);  // on the state before this constraint
                 const unsigned okm = __ballot_sync(full, ok);
+                const unsigned okBraw = __ballot_sync(full, okBl);
                 if ((uint32_t)__popc(okm) >= np) {
                     const uint32_t rank = __popc(okm & lt);
                     const bool sel = ok && rank < np;
@@ -449,24 +459,13 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
                     // on the same window state, minus the lanes this one fills up and, if they share a
                     // body or a hub, the lanes this one takes.
                     bool pair = false;
-                    uint32_t cB = 0, x0B = 0, x1B = 0, npB = 0, hfB = 0;
                     unsigned okB = 0;
-                    if (k + 1 < m) {
-                        const uint32_t mdB = __shfl_sync(full, meta, k + 1);
-                        const uint32_t cBs = __shfl_sync(full, mc, k + 1), xxB = __shfl_sync(full, dx, k + 1);
-                        if (!(mdB & 64u)) {
-                            cB = cBs;
-                            npB = mdB & 15u;
-                            x0B = xxB & 0xFFFFu;
-                            x1B = xxB >> 16;
-                            const uint32_t hB = (mdB >> 4) & 3u;
-                            hfB = hB == 1u ? kFfH0 : (hB == 2u ? kFfH1 : 0u);
-                            const bool share = x0 == x0B || x0 == x1B || x1 == x0B || x1 == x1B || (hfB & hflag);
-                            const unsigned selm = __ballot_sync(full, sel);
-                            const unsigned fullm = __ballot_sync(full, sel && (wcnt & 7u) + 1u == 4u);
-                            okB = __ballot_sync(full, win_fits(x0B, x1B, hfB)) & ~fullm & (share ? ~selm : ~0u);
-                            pair = (uint32_t)__popc(okB) >= npB;
-                        }
+                    if (canB) {
+                        const bool share = x0 == x0B || x0 == x1B || x1 == x0B || x1 == x1B || (hfB & hflag);
+                        const unsigned selm = __ballot_sync(full, sel);
+                        const unsigned fullm = __ballot_sync(full, sel && (wcnt & 7u) + 1u == 4u);
+                        okB = okBraw & ~fullm & (share ? ~selm : ~0u);
+                        pair = (uint32_t)__popc(okB) >= npB;
                     }
                     if (sel) {
                         if (lane >= vfirst) wbid = nbt + (lane - vfirst);
