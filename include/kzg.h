@@ -46,6 +46,7 @@ typedef int kzg_status;
 
 #define KZG_BODY_SENSOR 1u         /* BodySettings::isSensor */
 #define KZG_BODY_ALLOW_SLEEPING 2u /* BodySettings::allowSleeping */
+#define KZG_BODY_LINEAR_CAST 4u    /* BodySettings::motionQuality = MotionQuality::LinearCast (Body.h:46-67) */
 
 /* Broad-phase pair order of kzg_step (production mode). */
 #define KZG_PAIRS_CANONICAL 0 /* every overlapping pair, sorted by MakePairKey (PhysicsWorld.cpp:13-18) */
@@ -90,6 +91,8 @@ typedef struct {
     float fixed_timestep;   /* used for the broad-phase displacement, PhysicsWorld.cpp:342 */
     int allow_sleeping;     /* must be 0: sleeping is outside the accelerated path */
     int warm_start;         /* 0 reproduces the reference's KZ_NOWS switch (PhysicsWorld.cpp:493) */
+    int use_ccd;            /* WorldSettings::useCCD: clamp LinearCast bodies' motion (PhysicsWorld.cpp:785-852) */
+    float ccd_max_penetration; /* WorldSettings::ccdMaxPenetration */
 } kzg_world_settings;
 
 /* One shape. params: sphere {r}; box {hx,hy,hz}; capsule {halfHeight, radius}

@@ -38,7 +38,7 @@ class KzgSolverSettings(ctypes.Structure):
 
 class KzgWorldSettings(ctypes.Structure):
     _fields_ = [("gravity", f32 * 3), ("fixed_timestep", f32), ("allow_sleeping", ctypes.c_int),
-                ("warm_start", ctypes.c_int)]
+                ("warm_start", ctypes.c_int), ("use_ccd", ctypes.c_int), ("ccd_max_penetration", f32)]
 
 
 class KzgShapeDesc(ctypes.Structure):

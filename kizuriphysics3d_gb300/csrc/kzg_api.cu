@@ -35,7 +35,7 @@ kzg_status alloc_all(Ctx* ctx) {
     const size_t B = c.max_bodies, P = c.max_pairs, R = 4ull * c.max_pairs, H = c.max_cache_entries;
     DeviceBodies& b = ctx->b;
     float4** f4b[] = {&b.pos, &b.rot, &b.lv, &b.av, &b.plv, &b.pav, &b.force, &b.torque, &b.prm0, &b.prm1,
-                      &b.aabb_mn, &b.aabb_mx};
+                      &b.aabb_mn, &b.aabb_mx, &b.fat_mn, &b.fat_mx};
     for (float4** p : f4b) CK(dalloc(p, B));
     CK(dalloc(&b.iiw, 3 * B));
     CK(dalloc(&b.iil, 3 * B));
@@ -60,6 +60,8 @@ kzg_status alloc_all(Ctx* ctx) {
     CK(dalloc(&ctx->m_data, 12 * P));
     CK(dalloc(&ctx->m_key, P));
     CK(dalloc(&ctx->epa_list, P));
+    CK(dalloc(&ctx->ccd_disp, B));
+    CK(dalloc(&ctx->ccd_list, B));
     CK(dalloc(&ctx->con_flag, P));
     CK(dalloc(&ctx->con_index, P));
     CK(dalloc(&ctx->con_pair, P));
@@ -130,10 +132,10 @@ kzg_status alloc_all(Ctx* ctx) {
 void free_all(Ctx* ctx) {
     DeviceBodies& b = ctx->b;
     void* ptrs[] = {b.pos, b.rot, b.lv, b.av, b.plv, b.pav, b.force, b.torque, b.prm0, b.prm1, b.aabb_mn, b.aabb_mx,
-                    b.iiw, b.iil, b.inv_mass, b.shape, b.motion, b.flags, b.layer, b.mask, b.world, b.packed,
+                    b.iiw, b.iil, b.inv_mass, b.shape, b.motion, b.flags, b.layer, b.mask, b.world, b.packed, b.fat_mn, b.fat_mx,
                     ctx->is_large, ctx->large_list, ctx->large_off, ctx->cell_keys, ctx->cell_keys_sorted,
                     ctx->cell_vals, ctx->cell_vals_sorted, ctx->pair_keys, ctx->pair_keys_sorted, ctx->pairs,
-                    ctx->m_count, ctx->m_data, ctx->m_key, ctx->epa_list, ctx->con_flag, ctx->con_index, ctx->con_pair, ctx->con_a,
+                    ctx->m_count, ctx->m_data, ctx->m_key, ctx->epa_list, ctx->ccd_disp, ctx->ccd_list, ctx->con_flag, ctx->con_index, ctx->con_pair, ctx->con_a,
                     ctx->con_b, ctx->con_np, ctx->con_bits, ctx->con_fr, ctx->con_key, ctx->r.pA, ctx->r.pB, ctx->r.n,
                     ctx->r.t1, ctx->r.t2, ctx->r.rA, ctx->r.rB, ctx->r.rAr, ctx->r.rBr, ctx->r.laA, ctx->r.laB,
                     ctx->r.mass, ctx->r.imp, ctx->r.bias, ctx->uf, ctx->isl_key, ctx->isl_key_sorted,
@@ -234,6 +236,8 @@ void kzg_default_settings(kzg_world_settings* ws, kzg_solver_settings* ss) {
         ws->fixed_timestep = (float)(1.0 / 60.0);
         ws->allow_sleeping = 0;
         ws->warm_start = 1;
+        ws->use_ccd = 1;                 // WorldSettings defaults, PhysicsWorld.h:39-42
+        ws->ccd_max_penetration = 0.01f;
     }
     if (ss) {  // SolverSettings defaults, ContactSolver.h:67-82
         ss->velocity_iterations = 16;
@@ -429,7 +433,7 @@ kzg_status kzg_add_bodies(kzg_ctx* k, uint32_t n, const kzg_body_soa* b, uint32_
             ctx->err = "body " + std::to_string(i) + ": bad shape index or motion type";
             return KZG_ERR_INVALID;
         }
-        if (b->flags && (b->flags[i] & ~(KZG_BODY_SENSOR | KZG_BODY_ALLOW_SLEEPING))) {
+        if (b->flags && (b->flags[i] & ~(KZG_BODY_SENSOR | KZG_BODY_ALLOW_SLEEPING | KZG_BODY_LINEAR_CAST))) {
             ctx->err = "unknown body flag";
             return KZG_ERR_INVALID;
         }
@@ -483,6 +487,14 @@ kzg_status kzg_add_bodies(kzg_ctx* k, uint32_t n, const kzg_body_soa* b, uint32_
     h.shape.insert(h.shape.end(), shape.begin(), shape.end());
     h.motion.insert(h.motion.end(), motion.begin(), motion.end());
     h.world.insert(h.world.end(), world.begin(), world.end());
+    std::vector<uint32_t> cast;
+    for (uint32_t i = 0; i < n; ++i)
+        if (flags[i] & KZG_BODY_LINEAR_CAST) cast.push_back(base + i);
+    if (!cast.empty()) {
+        CK(cudaMemcpy(ctx->ccd_list + ctx->nccd, cast.data(), sizeof(uint32_t) * cast.size(), cudaMemcpyHostToDevice));
+        ctx->nccd += (uint32_t)cast.size();
+    }
+    CK(init_fat_bounds(*ctx, base, n));
     h.dirty = true;
     ctx->nbodies += n;
     if (first_slot) *first_slot = base;
@@ -743,16 +755,16 @@ kzg_status kzg_download_constraints(kzg_ctx* k, uint32_t* hdr, float* fr, float*
 // ---- device snapshots: body state and the manifold cache, for exact resume ------------------
 namespace {
 constexpr uint32_t kSnapMagic = 0x53475A4Bu;  // 'KZGS'
-constexpr uint32_t kSnapVersion = 1;
+constexpr uint32_t kSnapVersion = 2;
 struct SnapHeader {
     uint32_t magic, version, nbodies, cache_cap, cache_entries, cache_used, reserved[2];
 };
-constexpr int kSnapBodyArrays = 8;  // pos, rot, lv, av, plv, pav, force, torque (+ 3 iiw columns)
+constexpr int kSnapBodyArrays = 10;  // pos, rot, lv, av, plv, pav, force, torque, fat bounds (+ 3 iiw columns)
 constexpr size_t kSnapBodyBytes = sizeof(float4) * (kSnapBodyArrays + 3);
 constexpr size_t kSnapCacheBytes = sizeof(uint32_t) + sizeof(unsigned long long) + sizeof(uint32_t) + 8 * sizeof(float4);
 
 float4** snap_body_arrays(DeviceBodies& b, float4** out) {
-    float4* a[kSnapBodyArrays] = {b.pos, b.rot, b.lv, b.av, b.plv, b.pav, b.force, b.torque};
+    float4* a[kSnapBodyArrays] = {b.pos, b.rot, b.lv, b.av, b.plv, b.pav, b.force, b.torque, b.fat_mn, b.fat_mx};
     for (int i = 0; i < kSnapBodyArrays; ++i) out[i] = a[i];
     return out;
 }

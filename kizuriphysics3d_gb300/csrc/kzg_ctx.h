@@ -29,6 +29,7 @@ struct DeviceBodies {
     float* inv_mass;
     uint32_t *shape, *motion, *flags, *layer, *mask, *world, *packed;
     float4 *aabb_mn, *aabb_mx;
+    float4 *fat_mn, *fat_mx;  // broad-phase fat bounds (DynamicAABBTree leaves, BroadPhase.cpp:35-75)
 };
 
 struct DeviceRows {  // per point row, index = 4 * constraint + point
@@ -126,6 +127,9 @@ struct Ctx {
     float4* m_data = nullptr;  // 12 float4 per pair
     unsigned long long* m_key = nullptr;
     uint32_t* epa_list = nullptr;  // pairs whose narrow phase needs EPA (warp pass)
+    float4* ccd_disp = nullptr;    // continuous collision: each LinearCast body's step displacement
+    uint32_t* ccd_list = nullptr;  // slots of the LinearCast bodies, ascending
+    uint32_t nccd = 0;
 
     // constraints
     uint32_t* con_flag = nullptr;    // per pair: 1 if it makes a constraint

@@ -941,4 +941,54 @@ __device__ inline uint32_t collide(const ShapeTables& T, const Body& A, const Bo
     return collide_generic(T, A, B, max_sep, tol, m, epa);
 }
 
+// NarrowPhase::CastShape (CollideShape.cpp:607-661): the first fraction of `max_distance` along `direction` at
+// which A, moving without rotation, touches B, and B's surface normal there.  A plane B is solved
+// in closed form (A's deepest point against the plane); every other pair by conservative
+// advancement: GJK distance at the current translation (tolerance 1e-4, 32 iterations), advance by
+// distance - tolerance, at most 64 steps.
+__device__ inline bool cast_shape(const ShapeTables& T, const Body& A, const Vec3& direction, float max_distance,
+                                  const Body& B, float& fraction, Vec3& normal) {
+    const float dir_len = direction.len();
+    if (dir_len < kEps) return false;
+    const Vec3 dir = direction / dir_len;
+    if (B.s->type == kPlane) {
+        if (A.s->type == kPlane) return false;
+        const Vec3 pn(B.s->p[0], B.s->p[1], B.s->p[2]);
+        const Vec3 nw = B.q.rotate(pn).normalized();
+        const float plane_dist = nw.dot(xform(B.q, B.t, pn * B.s->p[3]));
+        const Vec3 deepest = xform(A.q, A.t, support_local(T, A.s, A.q.inv_rotate(-nw)));
+        const float sd = nw.dot(deepest) - plane_dist;
+        if (sd <= 1.0e-4f) {
+            fraction = 0.0f;
+            normal = nw;
+            return true;
+        }
+        const float rate = nw.dot(dir);
+        if (rate >= -kEps) return false;  // parallel or moving away
+        const float t_hit = sd / (-rate);
+        if (t_hit > max_distance) return false;
+        fraction = t_hit / max_distance;
+        normal = nw;
+        return true;
+    }
+    const float tol = 1.0e-4f;
+    float t = 0.0f;
+    for (uint32_t it = 0; it < 64; ++it) {
+        SupportMap map{&T, Body{A.s, A.q, A.t + dir * t}, B};
+        GjkOut g;
+        gjk(map, tol, 32, g);
+        if (g.intersect || g.distance <= tol) {
+            fraction = t / max_distance;
+            normal = g.normal;
+            return true;
+        }
+        if (t >= max_distance) return false;
+        float advance = g.distance - tol;
+        if (advance <= 0.0f) advance = tol;
+        t += advance;
+        if (t > max_distance) return false;
+    }
+    return false;
+}
+
 }  // namespace kzg

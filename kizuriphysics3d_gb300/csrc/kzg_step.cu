@@ -60,17 +60,53 @@ __device__ __forceinline__ unsigned long long cell_key(uint32_t world, uint32_t 
            ((unsigned long long)iy << 16) | (unsigned long long)iz;
 }
 
-// Tight world AABB of every body (Shape::GetWorldBounds = local bounds transformed, Math.cpp:176)
-// and its grid cell key; bodies that bypass the grid get key ~0.
-__global__ void k_aabb(DeviceBodies b, const ShapeDev* __restrict__ shapes, uint32_t n, float inv_cell,
-                       const uint8_t* __restrict__ is_large, unsigned long long* keys, uint32_t* vals) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ AABB body_bounds(const DeviceBodies& b, const ShapeDev* __restrict__ shapes, uint32_t i) {
     const ShapeDev& s = shapes[b.shape[i]];
     AABB local{Vec3(s.lmn[0], s.lmn[1], s.lmn[2]), Vec3(s.lmx[0], s.lmx[1], s.lmx[2])};
-    AABB w = aabb_transformed(local, Q4(b.rot[i]), V3(b.pos[i]));
+    return aabb_transformed(local, Q4(b.rot[i]), V3(b.pos[i]));
+}
+
+// Fat bounds of a moving body, kept like the tree's leaves (DynamicAABBTree::MoveProxy,
+// BroadPhase.cpp:58-75): unchanged while they contain the tight bounds, else the tight bounds
+// grown by the 0.1 margin and by |velocity x fixed timestep|.  Continuous collision tests them.
+__device__ __forceinline__ void update_fat(const DeviceBodies& b, uint32_t i, const AABB& w, float fixed_dt) {
+    if (b.motion[i] == KZG_MOTION_STATIC) return;
+    const Vec3 fmn = V3(b.fat_mn[i]), fmx = V3(b.fat_mx[i]);
+    if (fmn.x <= w.mn.x && fmx.x >= w.mx.x && fmn.y <= w.mn.y && fmx.y >= w.mx.y && fmn.z <= w.mn.z &&
+        fmx.z >= w.mx.z)
+        return;
+    const Vec3 d = (V3(b.lv[i]) * fixed_dt).abs(), margin(0.1f, 0.1f, 0.1f);
+    b.fat_mn[i] = F4((w.mn - margin) - d, 0.0f);
+    b.fat_mx[i] = F4((w.mx + margin) + d, 0.0f);
+}
+
+__global__ void k_init_fat(DeviceBodies b, const ShapeDev* __restrict__ shapes, uint32_t first, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    i += first;
+    const AABB w = body_bounds(b, shapes, i);
+    const Vec3 margin(0.1f, 0.1f, 0.1f);  // CreateProxy: tight bounds + margin
+    b.fat_mn[i] = F4(w.mn - margin, 0.0f);
+    b.fat_mx[i] = F4(w.mx + margin, 0.0f);
+}
+
+__global__ void k_fat(DeviceBodies b, const ShapeDev* __restrict__ shapes, uint32_t n, float fixed_dt) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    update_fat(b, i, body_bounds(b, shapes, i), fixed_dt);
+}
+
+// Tight world AABB of every body (Shape::GetWorldBounds = local bounds transformed, Math.cpp:176)
+// and its grid cell key; bodies that bypass the grid get key ~0.  Fat bounds follow.
+__global__ void k_aabb(DeviceBodies b, const ShapeDev* __restrict__ shapes, uint32_t n, float inv_cell,
+                       const uint8_t* __restrict__ is_large, unsigned long long* keys, uint32_t* vals,
+                       float fixed_dt) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    AABB w = body_bounds(b, shapes, i);
     b.aabb_mn[i] = F4(w.mn, 0.0f);
     b.aabb_mx[i] = F4(w.mx, 0.0f);
+    update_fat(b, i, w, fixed_dt);
     unsigned long long key = ~0ull;
     if (!is_large[i]) {
         Vec3 c = (w.mn + w.mx) * 0.5f;
@@ -539,7 +575,102 @@ __global__ void k_cache_store(Counters* cnt, const unsigned long long* __restric
     }
 }
 
-__global__ void k_integrate_pos(DeviceBodies b, uint32_t n, float dt, int vel_bias) {
+__device__ __forceinline__ bool casts_linear(const DeviceBodies& b, uint32_t i) {
+    return b.motion[i] == KZG_MOTION_DYNAMIC && (b.flags[i] & KZG_BODY_LINEAR_CAST) != 0u;
+}
+
+// Continuous collision of LinearCast bodies (PhysicsWorld::ClampMotionCCD, PhysicsWorld.cpp:785-802
+// and 804-852; the per-body CCD motion threshold is 0, its default), run where the reference runs it: inside the position loop, body by body in slot
+// order, so a body sees the bodies before it already moved.  One block walks the LinearCast list;
+// per body its threads scan every body for candidates (fat bounds overlapping the swept bounds
+// grown by 0.1, not itself, not a sensor, layer and mask both ways), cast against each, and reduce
+// to the smallest fraction (ties: the smaller slot, the reference's first hit).  The motion stops
+// max_pen short of the hit and the approaching normal velocity is removed.  disp[i] receives the
+// displacement k_integrate_pos applies.
+constexpr uint32_t kCcdThreads = 256;
+__global__ void __launch_bounds__(kCcdThreads) k_ccd(ShapeTables T, DeviceBodies b, uint32_t n,
+                                                     const uint32_t* __restrict__ list, uint32_t nlist, float dt,
+                                                     float max_pen, float4* disp_out) {
+    __shared__ float s_frac[kCcdThreads];
+    __shared__ uint32_t s_slot[kCcdThreads];
+    __shared__ float4 s_norm[kCcdThreads];
+    const uint32_t tid = threadIdx.x;
+    for (uint32_t k = 0; k < nlist; ++k) {
+        const uint32_t i = list[k];
+        if (!casts_linear(b, i)) continue;
+        const Vec3 lv = V3(b.lv[i]);
+        const Vec3 disp = lv * dt;
+        const float dist = disp.len();
+        if (dist <= max_pen) {
+            if (tid == 0) disp_out[i] = F4(disp, 0.0f);
+            continue;
+        }
+        const ShapeDev* sh = &T.shapes[b.shape[i]];
+        const Quat q0 = Q4(b.rot[i]);
+        const Vec3 t0 = V3(b.pos[i]);
+        const Vec3 dir = disp / dist;
+        const AABB local{Vec3(sh->lmn[0], sh->lmn[1], sh->lmn[2]), Vec3(sh->lmx[0], sh->lmx[1], sh->lmx[2])};
+        AABB sweep = aabb_merge(aabb_transformed(local, q0, t0), aabb_transformed(local, q0, t0 + disp));
+        const Vec3 margin(0.1f, 0.1f, 0.1f);
+        sweep = AABB{sweep.mn - margin, sweep.mx + margin};
+        const uint32_t li = b.layer[i], mi = b.mask[i];
+        float best = 1.0f;
+        uint32_t best_j = 0xFFFFFFFFu;
+        Vec3 best_n(0.0f, 1.0f, 0.0f);
+        for (uint32_t j = tid; j < n; j += kCcdThreads) {
+            if (j == i || (b.flags[j] & KZG_BODY_SENSOR)) continue;
+            if ((b.layer[j] & mi) == 0u || (li & b.mask[j]) == 0u) continue;
+            if (!aabb_overlaps(AABB{V3(b.fat_mn[j]), V3(b.fat_mx[j])}, sweep)) continue;
+            Vec3 tj = V3(b.pos[j]);
+            Quat qj = Q4(b.rot[j]);
+            if (j < i && b.motion[j] != KZG_MOTION_STATIC) {  // already integrated this step
+                tj = tj + (casts_linear(b, j) ? V3(disp_out[j]) : V3(b.lv[j]) * dt);
+                const Vec3 avj = V3(b.av[j]);
+                if (avj.len2() > 0.0f) qj = integrate_rotation(qj, avj, dt);
+            }
+            float frac;
+            Vec3 nrm;
+            if (cast_shape(T, Body{sh, q0, t0}, dir, dist, Body{&T.shapes[b.shape[j]], qj, tj}, frac, nrm) &&
+                frac < best) {
+                best = frac;
+                best_j = j;
+                best_n = nrm;
+            }
+        }
+        s_frac[tid] = best;
+        s_slot[tid] = best_j;
+        s_norm[tid] = F4(best_n, 0.0f);
+        __syncthreads();
+        for (uint32_t w = kCcdThreads / 2; w > 0; w >>= 1) {
+            if (tid < w) {
+                const float fo = s_frac[tid + w];
+                const uint32_t jo = s_slot[tid + w];
+                if (jo != 0xFFFFFFFFu && (s_slot[tid] == 0xFFFFFFFFu || fo < s_frac[tid] ||
+                                          (fo == s_frac[tid] && jo < s_slot[tid]))) {
+                    s_frac[tid] = fo;
+                    s_slot[tid] = jo;
+                    s_norm[tid] = s_norm[tid + w];
+                }
+            }
+            __syncthreads();
+        }
+        if (tid == 0) {
+            Vec3 d = disp;
+            if (s_slot[0] != 0xFFFFFFFFu) {
+                float stop = s_frac[0] * dist - max_pen;
+                if (stop < 0.0f) stop = 0.0f;
+                d = dir * stop;
+                const Vec3 hn = V3(s_norm[0]);
+                const float vn = lv.dot(hn);
+                if (vn < 0.0f) b.lv[i] = F4(lv - hn * vn, 0.0f);
+            }
+            disp_out[i] = F4(d, 0.0f);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_integrate_pos(DeviceBodies b, uint32_t n, float dt, int vel_bias, const float4* __restrict__ ccd_disp) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t mt = b.motion[i];
@@ -547,7 +678,7 @@ __global__ void k_integrate_pos(DeviceBodies b, uint32_t n, float dt, int vel_bi
         Vec3 p = V3(b.pos[i]);
         Quat q = Q4(b.rot[i]);
         Vec3 lv = V3(b.lv[i]), av = V3(b.av[i]);
-        p = p + lv * dt;
+        p = p + ((ccd_disp && casts_linear(b, i)) ? V3(ccd_disp[i]) : lv * dt);
         if (av.len2() > 0.0f) q = integrate_rotation(q, av, dt);
         if (!vel_bias) {
             Vec3 pl = V3(b.plv[i]), pa = V3(b.pav[i]);
@@ -744,7 +875,15 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     KZG_CK(mark(ctx, 5));
     k_cache_store<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_key, ctx.con_np, ctx.r, ctx.c_key, ctx.c_np,
                                                       ctx.c_pos, ctx.c_imp, ctx.cfg.max_cache_entries);
-    k_integrate_pos<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, dt, ctx.ss.use_velocity_bias);
+    const bool ccd = ctx.ws.use_ccd && ctx.nccd > 0;
+    if (ccd) {
+        ShapeTables T{ctx.shapes, ctx.hull_verts, ctx.face_sizes, ctx.face_idx};
+        k_ccd<<<1, kCcdThreads, 0, st>>>(T, ctx.b, nb, ctx.ccd_list, ctx.nccd, dt, ctx.ws.ccd_max_penetration,
+                                         ctx.ccd_disp);
+        ++ctx.launches;
+    }
+    k_integrate_pos<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, dt, ctx.ss.use_velocity_bias,
+                                                         ccd ? ctx.ccd_disp : nullptr);
     ctx.launches += 2;
     KZG_CK(mark(ctx, 6));
     KZG_CK(cudaGetLastError());
@@ -798,7 +937,7 @@ static kzg_status record_canonical(Ctx& ctx, float dt) {
     k_begin_step<<<1, 32, 0, st>>>(ctx.dcnt);
     KZG_CK(mark(ctx, 0));
     k_aabb<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, ctx.shapes, nb, 1.0f / ctx.cell_size, ctx.is_large,
-                                                ctx.cell_keys, ctx.cell_vals);
+                                                ctx.cell_keys, ctx.cell_vals, ctx.ws.fixed_timestep);
     size_t tb = ctx.cub_tmp_bytes;
     KZG_CK(cub::DeviceRadixSort::SortPairs(ctx.cub_tmp, tb, ctx.cell_keys, ctx.cell_keys_sorted, ctx.cell_vals,
                                            ctx.cell_vals_sorted, (int)nb, 0, 64, st));
@@ -873,9 +1012,10 @@ kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t np, floa
         return KZG_ERR_CAPACITY;
     }
     ++ctx.frame;
-    ctx.launches = np > 0 ? 2 : 1;
+    ctx.launches = np > 0 ? 3 : 2;
     k_begin_step<<<1, 32, 0, st>>>(ctx.dcnt);
     KZG_CK(cudaEventRecord(ctx.ev[0], st));
+    if (ctx.nbodies) k_fat<<<blocks_for(ctx.nbodies), kThreads, 0, st>>>(ctx.b, ctx.shapes, ctx.nbodies, ctx.ws.fixed_timestep);
     if (np > 0) {
         KZG_CK(cudaMemcpyAsync(ctx.pair_keys, host_pairs, sizeof(uint32_t) * 2 * np, cudaMemcpyHostToDevice, st));
         k_pairs_from_packed<<<blocks_for(np), kThreads, 0, st>>>((const uint32_t*)ctx.pair_keys, np, ctx.b,
@@ -887,6 +1027,13 @@ kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t np, floa
     s = fetch_counters(ctx);
     if (s != KZG_OK) return s;
     return finish_stats(ctx);
+}
+
+cudaError_t init_fat_bounds(Ctx& ctx, uint32_t first, uint32_t n) {
+    if (n == 0) return cudaSuccess;
+    k_init_fat<<<blocks_for(n), kThreads, 0, ctx.stream>>>(ctx.b, ctx.shapes, first, n);
+    cudaError_t e = cudaGetLastError();
+    return e != cudaSuccess ? e : cudaStreamSynchronize(ctx.stream);
 }
 
 kzg_status hash_state(Ctx& ctx, uint64_t* out) {

@@ -66,7 +66,8 @@ def to_kzp1(scene: Scene, state: Optional[np.ndarray] = None) -> bytes:
             pos, rot, vel, ang = st[0:3], st[3:7], st[7:10], st[10:13]
         f = lambda xs: [float(np.float32(x)) for x in xs]
         out += struct.pack("<3f4f3f3f", *f(pos), *f(rot), *f(vel), *f(ang))
-        out += struct.pack("<BBf", b.motion, 0, 0.0)  # motionQuality Discrete, ccdMotionThreshold 0
+        quality = 1 if b.flags & scenes.BODY_FLAG_LINEAR_CAST else 0  # MotionQuality::LinearCast = 1
+        out += struct.pack("<BBf", b.motion, quality, 0.0)  # ccdMotionThreshold 0
         out += struct.pack("<7f", *f([b.friction, b.restitution, b.linear_damping, b.angular_damping,
                                       b.gravity_factor, b.max_linear_velocity, b.max_angular_velocity]))
         out += struct.pack("<II", b.layer & 0xFFFFFFFF, b.mask & 0xFFFFFFFF)
@@ -128,14 +129,15 @@ def from_kzp1(data: bytes, template: Optional[Scene] = None) -> Scene:
         if key not in seen:
             seen[key] = sc.add_shape(sh)
         pos = r.take("<3f"); rot = r.take("<4f"); vel = r.take("<3f"); ang = r.take("<3f")
-        motion, _quality, _ccd = r.take("<BBf")
+        motion, quality, _ccd = r.take("<BBf")
         fr, rs, ld, ad, gf, ml, ma = r.take("<7f")
         layer, mask = r.take("<II")
         sleep, sensor = r.take("<BB")
         r.take("<Q")
         mass_override, density = r.take("<2f")
         r.take("<B")  # active
-        flags = (scenes.BODY_FLAG_ALLOW_SLEEPING if sleep else 0) | (scenes.BODY_FLAG_SENSOR if sensor else 0)
+        flags = ((scenes.BODY_FLAG_ALLOW_SLEEPING if sleep else 0) | (scenes.BODY_FLAG_SENSOR if sensor else 0) |
+                 (scenes.BODY_FLAG_LINEAR_CAST if quality == 1 else 0))
         sc.add_body(Body(shape=seen[key], motion=motion, pos=pos, rot=rot, vel=vel, ang=ang, friction=fr,
                          restitution=rs, linear_damping=ld, angular_damping=ad, gravity_factor=gf,
                          max_linear_velocity=ml, max_angular_velocity=ma, density=density,

@@ -49,6 +49,7 @@ MOTION_DYNAMIC = 2
 
 BODY_FLAG_SENSOR = 1
 BODY_FLAG_ALLOW_SLEEPING = 2
+BODY_FLAG_LINEAR_CAST = 4   # MotionQuality::LinearCast: continuous collision clamps the motion (Body.h:46-67)
 
 WORLD_FLAG_ALLOW_SLEEPING = 1
 WORLD_FLAG_VELOCITY_BIAS = 2

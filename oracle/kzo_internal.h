@@ -36,6 +36,8 @@ typedef struct {
 uint32_t kzo_collide(const kzo_shape* sa, qt ra, v3 ta, const kzo_shape* sb, qt rb, v3 tb,
                      float max_sep, float tol, kzo_manifold* out);
 aabb kzo_world_bounds(const kzo_shape* s, qt r, v3 t);
+int kzo_cast_shape(const kzo_shape* sa, qt ra, v3 ta, v3 direction, float max_distance, const kzo_shape* sb, qt rb,
+                   v3 tb, float* out_fraction, v3* out_normal);
 
 /* GJK / EPA results exposed for the known-answer tests. */
 typedef struct { v3 pA, pB, p; } kzo_sp;

@@ -695,3 +695,52 @@ uint32_t kzo_collide(const kzo_shape* sa, qt ra, v3 ta, const kzo_shape* sb, qt 
     }
     return collide_generic(sa, ra, ta, sb, rb, tb, max_sep, tol, out);
 }
+
+/* NarrowPhase::CastShape (CollideShape.cpp:607-661): conservative advancement of A along
+ * `direction` (up to max_distance) against B with GJK distance; planes analytically. */
+int kzo_cast_shape(const kzo_shape* sa, qt ra, v3 ta, v3 direction, float max_distance, const kzo_shape* sb, qt rb,
+                   v3 tb, float* out_fraction, v3* out_normal) {
+    const float dir_len = vlen(direction);
+    if (dir_len < KZO_EPS) return 0;
+    const v3 dir = vdiv(direction, dir_len);
+    if (sb->type == KZO_PLANE) {
+        if (sa->type == KZO_PLANE) return 0;
+        const v3 pn = V(sb->p[0], sb->p[1], sb->p[2]);
+        const v3 n_world = vnormalized(qrotate(rb, pn));
+        const v3 point_on_plane = xform(rb, tb, vmul(pn, sb->p[3]));
+        const float plane_dist = vdot(n_world, point_on_plane);
+        const v3 local_dir_a = qinv_rotate(ra, vneg(n_world));
+        const v3 deepest = xform(ra, ta, support_local(sa, local_dir_a));
+        const float sd = vdot(n_world, deepest) - plane_dist;
+        if (sd <= 1.0e-4f) {
+            *out_fraction = 0.0f;
+            *out_normal = n_world;
+            return 1;
+        }
+        const float rate = vdot(n_world, dir);
+        if (rate >= -KZO_EPS) return 0; /* moving parallel / away */
+        const float t_hit = sd / (-rate);
+        if (t_hit > max_distance) return 0;
+        *out_fraction = t_hit / max_distance;
+        *out_normal = n_world;
+        return 1;
+    }
+    float t = 0.0f;
+    const float tol = 1.0e-4f;
+    for (uint32_t iter = 0; iter < 64; ++iter) {
+        const v3 cur = vadd(ta, vmul(dir, t));
+        kzo_smap map = {sa, sb, ra, rb, cur, tb};
+        kzo_gjk g = kzo_gjk_closest(&map, tol, 32);
+        if (g.intersect || g.distance <= tol) {
+            *out_fraction = t / max_distance;
+            *out_normal = g.normal;
+            return 1;
+        }
+        if (t >= max_distance) return 0;
+        float advance = g.distance - tol;
+        if (advance <= 0.0f) advance = tol;
+        t += advance;
+        if (t > max_distance) return 0;
+    }
+    return 0;
+}

@@ -76,6 +76,10 @@ struct kzo_world {
     uint32_t *packed, *layer, *mask, *proxy;
     int* shape;
     uint8_t *motion, *sensor;
+    uint8_t* ccd;           /* MotionQuality::LinearCast */
+    aabb* fat;              /* broad-phase fat bounds per body (the tree leaves' bounds, all pair modes) */
+    int use_ccd;            /* WorldSettings::useCCD (default true) */
+    float ccd_max_pen;      /* WorldSettings::ccdMaxPenetration (default 0.01) */
     v3 *pos, *lv, *av, *plv, *pav, *force, *torque;
     qt* rot;
     float *inv_mass, *lin_damp, *ang_damp, *grav, *max_lin, *max_ang, *fric, *rest;
@@ -759,6 +763,44 @@ static void solve_island(kzo_world* w, uint32_t isl, uint32_t* out_batches, uint
 /* ----------------------------------------------------------------------------- */
 /* Step                                                                           */
 /* ----------------------------------------------------------------------------- */
+/* PhysicsWorld::ClampMotionCCD (PhysicsWorld.cpp:804-852) for body i, run inside the position
+ * loop (bodies earlier in the active list already moved).  Candidates are the bodies whose fat
+ * bounds overlap the swept bounds, visited in slot order (the reference visits its tree; the two
+ * differ only when two casts return the same fraction). */
+static void clamp_motion_ccd(kzo_world* w, int i, v3* disp) {
+    const float dist = vlen(*disp);
+    if (dist <= w->ccd_max_pen) return;
+    const kzo_shape* sh = &w->shapes[w->shape[i]];
+    const v3 dir = vdiv(*disp, dist);
+    const qt r0 = w->rot[i];
+    const v3 t0 = w->pos[i];
+    aabb sweep = kzo_world_bounds(sh, r0, t0);
+    sweep = aabb_merge(sweep, kzo_world_bounds(sh, r0, vadd(t0, *disp)));
+    sweep = AB(vsub(sweep.mn, V(0.1f, 0.1f, 0.1f)), vadd(sweep.mx, V(0.1f, 0.1f, 0.1f)));
+    float best = 1.0f;
+    v3 best_n = V(0.0f, 1.0f, 0.0f);
+    int hit = 0;
+    for (int j = 0; j < w->nb; ++j) {
+        if (j == i || w->sensor[j]) continue;
+        if ((w->layer[j] & w->mask[i]) == 0u || (w->layer[i] & w->mask[j]) == 0u) continue;
+        if (!aabb_overlaps(w->fat[j], sweep)) continue;
+        float frac;
+        v3 n;
+        if (kzo_cast_shape(sh, r0, t0, dir, dist, &w->shapes[w->shape[j]], w->rot[j], w->pos[j], &frac, &n) &&
+            frac < best) {
+            best = frac;
+            best_n = n;
+            hit = 1;
+        }
+    }
+    if (!hit) return;
+    float stop = best * dist - w->ccd_max_pen;
+    if (stop < 0.0f) stop = 0.0f;
+    *disp = vmul(dir, stop);
+    const float vn = vdot(w->lv[i], best_n);
+    if (vn < 0.0f) w->lv[i] = vsub(w->lv[i], vmul(best_n, vn));
+}
+
 static uint32_t uf_find(uint32_t* par, uint32_t x) {
     while (par[x] != x) { par[x] = par[par[x]]; x = par[x]; }
     return x;
@@ -914,7 +956,17 @@ int kzo_step(kzo_world* w, float dt) {
     ++w->frame;
     if (w->frame == 0) w->frame = 1;
 
-    /* 1. broad phase */
+    /* 1. broad phase.  Every mode keeps the bodies' fat bounds the way the tree's MoveProxy does
+     * (BroadPhase.cpp:58-75): continuous collision queries them. */
+    for (int k = 0; k < w->nactive; ++k) {
+        int i = w->active[k];
+        if (w->motion[i] == KZO_STATIC) continue;
+        aabb b = kzo_world_bounds(&w->shapes[w->shape[i]], w->rot[i], w->pos[i]);
+        if (aabb_contains(w->fat[i], b)) continue;
+        v3 d = vabs(vmul(w->lv[i], w->fixed_dt));
+        v3 margin = V(0.1f, 0.1f, 0.1f);
+        w->fat[i] = AB(vsub(vsub(b.mn, margin), d), vadd(vadd(b.mx, margin), d));
+    }
     if (w->pair_mode == KZO_PAIRS_TREE) {
         for (int k = 0; k < w->nactive; ++k) {
             int i = w->active[k];
@@ -988,7 +1040,9 @@ int kzo_step(kzo_world* w, float dt) {
     for (int k = 0; k < w->nactive; ++k) {
         int i = w->active[k];
         if (w->motion[i] == KZO_STATIC) continue;
-        w->pos[i] = vadd(w->pos[i], vmul(w->lv[i], dt));
+        v3 disp = vmul(w->lv[i], dt);
+        if (w->use_ccd && w->motion[i] == KZO_DYNAMIC && w->ccd[i]) clamp_motion_ccd(w, i, &disp);
+        w->pos[i] = vadd(w->pos[i], disp);
         if (vlen2(w->av[i]) > 0.0f) w->rot[i] = q_integrate(w->rot[i], w->av[i], dt);
     }
     if (!w->vel_bias) {
@@ -1091,7 +1145,7 @@ kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* res
     w->nb = nb;
 #define ALLOC(f, T) w->f = (T*)calloc((size_t)(nb ? nb : 1), sizeof(T))
     ALLOC(packed, uint32_t); ALLOC(layer, uint32_t); ALLOC(mask, uint32_t); ALLOC(proxy, uint32_t);
-    ALLOC(shape, int); ALLOC(motion, uint8_t); ALLOC(sensor, uint8_t);
+    ALLOC(shape, int); ALLOC(motion, uint8_t); ALLOC(sensor, uint8_t); ALLOC(ccd, uint8_t); ALLOC(fat, aabb);
     ALLOC(pos, v3); ALLOC(lv, v3); ALLOC(av, v3); ALLOC(plv, v3); ALLOC(pav, v3); ALLOC(force, v3); ALLOC(torque, v3);
     ALLOC(rot, qt);
     ALLOC(inv_mass, float); ALLOC(lin_damp, float); ALLOC(ang_damp, float); ALLOC(grav, float);
@@ -1112,6 +1166,7 @@ kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* res
         w->layer[i] = rd_u32(&r); w->mask[i] = rd_u32(&r);
         uint32_t fl = rd_u32(&r);
         w->sensor[i] = (fl & 1u) != 0;
+        w->ccd[i] = (fl & 4u) != 0;
         w->packed[i] = (uint32_t)i; /* BodyID(index, sequence 0).Packed() */
         w->active[i] = i;
         w->inv_mass[i] = rd_f32(&rr);
@@ -1124,7 +1179,10 @@ kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* res
         if (w->motion[i] == KZO_DYNAMIC && w->inv_mass[i] > 0.0f) update_world_inertia(w, i);
         aabb b = kzo_world_bounds(&w->shapes[w->shape[i]], w->rot[i], w->pos[i]);
         w->proxy[i] = create_proxy(w, b, w->packed[i], w->layer[i], w->mask[i]);
+        w->fat[i] = AB(vsub(b.mn, V(0.1f, 0.1f, 0.1f)), vadd(b.mx, V(0.1f, 0.1f, 0.1f)));
     }
+    w->use_ccd = 1;
+    w->ccd_max_pen = 0.01f;
     w->cache_cap = 1024;
     w->cache = (cache_t*)calloc(w->cache_cap, sizeof(cache_t));
     return w;
@@ -1134,7 +1192,7 @@ void kzo_destroy(kzo_world* w) {
     if (!w) return;
     for (int i = 0; i < w->nshapes; ++i) { free(w->shapes[i].verts); free(w->shapes[i].sizes); free(w->shapes[i].idx); }
     free(w->shapes);
-    void* ptrs[] = {w->packed, w->layer, w->mask, w->proxy, w->shape, w->motion, w->sensor, w->pos, w->lv, w->av,
+    void* ptrs[] = {w->packed, w->layer, w->mask, w->proxy, w->shape, w->motion, w->sensor, w->ccd, w->fat, w->pos, w->lv, w->av,
                     w->plv, w->pav, w->force, w->torque, w->rot, w->inv_mass, w->lin_damp, w->ang_damp, w->grav,
                     w->max_lin, w->max_ang, w->fric, w->rest, w->iil, w->iiw, w->active, w->island_index,
                     w->nodes, w->bp_layer, w->bp_mask, w->cache, w->pairs, w->ext_pairs, w->man, w->keys,

@@ -144,6 +144,7 @@ int main(int argc, char** argv) {
         bs.objectLayer = layer; bs.collisionMask = mask;
         bs.isSensor = (flags & 1u) != 0;
         bs.allowSleeping = (flags & 2u) != 0;
+        if (flags & 4u) bs.motionQuality = MotionQuality::LinearCast;
         ids[i] = world.CreateBody(bs);
         if (ids[i].IsInvalid()) { std::fprintf(stderr, "body %u invalid\n", i); return 1; }
     }

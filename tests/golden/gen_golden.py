@@ -6,7 +6,7 @@ computed: the ComputeStateHash value after every step, the full body state at ch
 the broad-phase pair list and contact constraints of the first steps, WorldStats counters, the
 resolved mass properties and every hull as built by ConvexHullShape::Create.
 
-    python tests/golden/gen_golden.py [--ref /root/reference]
+    python tests/golden/gen_golden.py [--ref /root/reference] [--only NAME ...]
 """
 from __future__ import annotations
 
@@ -35,7 +35,41 @@ def fixture_scenes():
     out["stacks2x2x20"] = (scenes.stacks(2, 2, 20), 300, 2, [0, 1, 59, 299])
     out["pile64_nows"] = (_nows(scenes.pile(64, seed=77, extent=1.5, y_range=(1.0, 5.0))), 240, 2, [0, 59, 239])
     out["pyramid4_tests"] = (_reference_test_pyramid(), 240, 2, [0, 239])
+    out["ccd_shots"] = (_ccd_shots(), 120, 2, [0, 1, 29, 59, 119])
     return out
+
+
+def _ccd_shots():
+    """Continuous collision (PhysicsWorld.cpp:804-852): small LinearCast spheres and boxes fired
+    down at a thin static slab and sideways at a static wall fast enough to pass through them in
+    one step, beside a few discrete boxes; ground plane below."""
+    import numpy as np
+    sc = scenes.Scene(name="ccd_shots")
+    scenes._timed_settings(sc, 10, 2)
+    scenes._ground(sc, 0.5)
+    slab = sc.add_shape(scenes.Shape(scenes.SHAPE_BOX, [3.0, 0.05, 3.0, 0.0]))
+    wall = sc.add_shape(scenes.Shape(scenes.SHAPE_BOX, [0.05, 2.0, 3.0, 0.0]))
+    ball = sc.add_shape(scenes.Shape(scenes.SHAPE_SPHERE, [0.1, 0.0, 0.0, 0.0]))
+    cube = sc.add_shape(scenes.Shape(scenes.SHAPE_BOX, [0.12, 0.12, 0.12, 0.0]))
+    big = sc.add_shape(scenes.Shape(scenes.SHAPE_BOX, [0.4, 0.4, 0.4, 0.0]))
+    f = scenes.f32
+    sc.add_body(scenes.Body(slab, scenes.MOTION_STATIC, pos=(0.0, 3.0, 0.0)))
+    sc.add_body(scenes.Body(wall, scenes.MOTION_STATIC, pos=(6.0, 2.0, 0.0)))
+    rng = np.random.default_rng(31)
+    lc = scenes.BODY_FLAG_ALLOW_SLEEPING | scenes.BODY_FLAG_LINEAR_CAST
+    for k in range(12):  # dropped through the slab
+        x, z = rng.uniform(-2.5, 2.5, 2)
+        vy = -f(rng.uniform(25.0, 45.0))
+        sc.add_body(scenes.Body(ball if k % 2 else cube, pos=(f(x), f(rng.uniform(4.0, 6.0)), f(z)),
+                                vel=(0.0, vy, 0.0), flags=lc))
+    for k in range(8):  # fired at the wall
+        y, z = rng.uniform(0.4, 3.5), rng.uniform(-2.5, 2.5)
+        vx = f(rng.uniform(30.0, 60.0))
+        sc.add_body(scenes.Body(cube if k % 2 else ball, pos=(f(rng.uniform(1.0, 3.0)), f(y), f(z)),
+                                vel=(vx, 0.0, 0.0), flags=lc))
+    for k in range(6):  # discrete boxes resting and falling
+        sc.add_body(scenes.Body(big, pos=(f(-4.0 + 1.1 * k), f(0.4 + 0.9 * (k % 2)), f(-4.0))))
+    return sc
 
 
 def _nows(sc):
@@ -56,12 +90,15 @@ def _reference_test_pyramid():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", nargs="*", default=None, help="fixture names to (re)generate (default: all)")
     args = ap.parse_args()
     subprocess.run(["make", "-s", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"), f"REF={args.ref}", "-j8"],
                    check=True)
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_trace")
     with tempfile.TemporaryDirectory() as td:
         for name, (sc, steps, detail, ckpt) in fixture_scenes().items():
+            if args.only and name not in args.only:
+                continue
             sp = os.path.join(td, name + ".kzsc")
             tp = os.path.join(td, name + ".kztr")
             sc.save(sp)

@@ -50,7 +50,8 @@ def test_mode_a_bit_exact_with_reference(name, oracle_lib, kzg_lib):
         assert gw.get_stats()["device_error"] == 0
 
 
-@pytest.mark.parametrize("name,steps", [("pile200", 300), ("stacks2x2x20", 200), ("pyramid20", 200)])
+@pytest.mark.parametrize("name,steps", [("pile200", 300), ("stacks2x2x20", 200), ("pyramid20", 200),
+                                        ("ccd_shots", 120)])
 def test_mode_b_bit_exact_with_oracle(name, steps, oracle_lib, kzg_lib):
     sc, g, ow, gw = _pair_worlds(name, oracle_lib.PAIRS_CANONICAL, oracle_lib)
     with gw:
@@ -123,6 +124,33 @@ def test_residual_terminated_bit_exact_with_oracle(name, steps, oracle_lib, kzg_
             seen_iters.add(st["max_velocity_iterations_used"])
         assert np.array_equal(bits(gw.state()), bits(ow.state()))
         assert len(seen_iters) > 1  # the stopping rule actually varied the iteration count
+
+
+def _bullet_scene(flags):
+    from kizuriphysics3d_gb300 import scenes
+    sc = scenes.Scene(name="bullet")
+    wall = sc.add_shape(scenes.Shape(scenes.SHAPE_BOX, [0.02, 2.0, 2.0, 0.0]))
+    ball = sc.add_shape(scenes.Shape(scenes.SHAPE_SPHERE, [0.1, 0.0, 0.0, 0.0]))
+    sc.gravity = (0.0, 0.0, 0.0)
+    sc.add_body(scenes.Body(shape=wall, motion=scenes.MOTION_STATIC, pos=(0.0, 0.0, 0.0)))
+    sc.add_body(scenes.Body(shape=ball, motion=scenes.MOTION_DYNAMIC, pos=(-3.0, 0.0, 0.0), vel=(120.0, 0.0, 0.0),
+                            flags=flags, max_linear_velocity=500.0))
+    return sc
+
+
+def test_linear_cast_stops_a_bullet_at_a_thin_wall(kzg_lib):
+    """A 0.1 m ball at 120 m/s (2 m per step) against a 4 cm static wall: the discrete body passes
+    through between two steps; the LinearCast body's motion is clamped max_pen short of the cast
+    hit every step (ClampMotionCCD), so it stays in front of the wall (x = -0.130 in the oracle)."""
+    from kizuriphysics3d_gb300 import World, scenes
+    xs = {}
+    for flags in (0, scenes.BODY_FLAG_LINEAR_CAST):
+        with World(_bullet_scene(flags)) as w:
+            w.step_fixed(n=4)
+            xs[flags] = float(w.state()[1][0])
+            assert w.get_stats()["device_error"] == 0
+    assert xs[0] > 2.0
+    assert -0.2 < xs[scenes.BODY_FLAG_LINEAR_CAST] < -0.1
 
 
 def test_graph_stepping_matches_direct_stepping(kzg_lib):

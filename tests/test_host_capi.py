@@ -105,6 +105,7 @@ def test_kzp1_round_trip():
     sc.bodies[3].friction = 0.25
     sc.bodies[4].flags = scenes.BODY_FLAG_SENSOR
     sc.bodies[5].mass_override = 7.5
+    sc.bodies[6].flags |= scenes.BODY_FLAG_LINEAR_CAST  # written as MotionQuality::LinearCast
     data = kzp1.to_kzp1(sc)
     assert struct.unpack_from("<III", data) == (0x31505A4B, 1, len(sc.bodies))
     back = kzp1.from_kzp1(data, template=sc)
