@@ -96,6 +96,54 @@ class Body:
     flags: int = BODY_FLAG_ALLOW_SLEEPING
 
 
+# Joint types (include/Kizuri/Constraint/Constraints.h:41-277)
+JOINT_POINT, JOINT_DISTANCE, JOINT_FIXED, JOINT_HINGE, JOINT_SLIDER, JOINT_SIXDOF = range(6)
+JOINT_FLAG_DISABLED = 1       # Constraint::SetEnabled(false)
+JOINT_FLAG_LIMITS = 2         # Hinge/SliderConstraint::SetLimits(lower, upper)
+JOINT_FLAG_MOTOR = 4          # Hinge/SliderConstraint::SetMotor(target, max)
+JOINT_FLAG_LOCAL_ANCHORS = 8  # PointConstraint(a, b, localAnchorA, localAnchorB)
+AXIS_FREE, AXIS_LIMITED, AXIS_FIXED = 0, 1, 2  # SixDOFConstraint::AxisMode
+JOINT_RECORD = struct.Struct("<4I21f2I12f")
+
+
+@dataclass
+class Joint:
+    """One joint as the reference's constructors take it: world-space anchors and axes at the
+    bodies' creation poses.  anchor_b is DistanceConstraint's second anchor (or PointConstraint's
+    local anchor B with JOINT_FLAG_LOCAL_ANCHORS); axis_b is HingeConstraint's axis on B; rotation
+    is SixDOFConstraint's world frame; axis_modes packs 2 bits per axis (linear x,y,z then
+    angular x,y,z); motor_mask bit k / 3+k enables SixDOF linear / angular motor k."""
+    type: int
+    body_a: int
+    body_b: int
+    anchor_a: tuple = (0.0, 0.0, 0.0)
+    anchor_b: tuple = (0.0, 0.0, 0.0)
+    axis_a: tuple = (0.0, 1.0, 0.0)
+    axis_b: tuple = (0.0, 1.0, 0.0)
+    rotation: tuple = (0.0, 0.0, 0.0, 1.0)
+    distance: float = 0.0
+    lower: float = 0.0
+    upper: float = 0.0
+    motor_target: float = 0.0
+    motor_max: float = 0.0
+    flags: int = 0
+    axis_modes: int = 0
+    motor_mask: int = 0
+    six_motor: tuple = (0.0,) * 12  # linear targets[3], linear max[3], angular targets[3], angular max[3]
+
+    def to_bytes(self) -> bytes:
+        fl = [f32(x) for x in (*self.anchor_a, *self.anchor_b, *self.axis_a, *self.axis_b, *self.rotation,
+                               self.distance, self.lower, self.upper, self.motor_target, self.motor_max)]
+        return JOINT_RECORD.pack(self.type, self.body_a, self.body_b, self.flags, *fl, self.axis_modes,
+                                 self.motor_mask, *[f32(x) for x in self.six_motor])
+
+    @staticmethod
+    def from_values(v) -> "Joint":
+        f = v[4:25]
+        return Joint(v[0], v[1], v[2], tuple(f[0:3]), tuple(f[3:6]), tuple(f[6:9]), tuple(f[9:12]),
+                     tuple(f[12:16]), f[16], f[17], f[18], f[19], f[20], v[3], v[25], v[26], tuple(v[27:39]))
+
+
 @dataclass
 class Scene:
     """World settings + shapes + bodies.  Settings defaults are WorldSettings /
@@ -114,6 +162,7 @@ class Scene:
     warm_start_factor: float = 1.0
     shapes: List[Shape] = field(default_factory=list)
     bodies: List[Body] = field(default_factory=list)
+    joints: List[Joint] = field(default_factory=list)
 
     # -- construction helpers -------------------------------------------------
     def add_shape(self, shape: Shape) -> int:
@@ -151,6 +200,10 @@ class Scene:
                 b.friction, b.restitution, b.linear_damping, b.angular_damping, b.gravity_factor,
                 b.max_linear_velocity, b.max_angular_velocity, b.density, b.mass_override)])
             out += struct.pack("<III", b.layer & 0xFFFFFFFF, b.mask & 0xFFFFFFFF, b.flags)
+        if self.joints:  # optional trailing section
+            out += struct.pack("<I", len(self.joints))
+            for j in self.joints:
+                out += j.to_bytes()
         return bytes(out)
 
     def save(self, path: str) -> None:
@@ -192,6 +245,11 @@ class Scene:
             layer, mask, flags = take("<III")
             sc.bodies.append(Body(shape, motion, v[0:3], v[3:7], v[7:10], v[10:13], *m,
                                   layer=layer, mask=mask, flags=flags))
+        if off < len(data):
+            (nj,) = take("<I")
+            for _ in range(nj):
+                sc.joints.append(Joint.from_values(JOINT_RECORD.unpack_from(data, off)))
+                off += JOINT_RECORD.size
         return sc
 
 

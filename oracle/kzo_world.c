@@ -57,6 +57,22 @@ typedef struct {
     float ni[KZO_MAX_MANIFOLD], ti1[KZO_MAX_MANIFOLD], ti2[KZO_MAX_MANIFOLD];
 } cache_t;
 
+/* One joint (Constraints.h:41-277): its creation data, prepared state and accumulated impulses. */
+typedef struct {
+    uint32_t type, a, b, flags;
+    v3 la, lb, lax, lbx, lpa[2], lpb[2];
+    qt relrot;
+    m3 crot;
+    float target, lower, upper, motor_target, motor_max;
+    uint32_t modes, motors;
+    float six[12];
+    /* prepared state and accumulated impulses */
+    v3 r0, r1, axis, imp1, imp2;
+    m3 m1, m2;
+    float sm[2], simp[2], limit_mass, limit_imp, motor_imp, axial_mass, axial_imp, dmass, dimp;
+    v3 lin_imp[3], ang_imp[3], axes[3];
+} joint_t;
+
 typedef struct { int con; uint32_t pt; } pref_t;
 typedef struct { pref_t ref[4]; int a[4], b[4]; uint32_t count; } batch_t;
 
@@ -109,6 +125,10 @@ struct kzo_world {
     uint32_t* isl_off; /* nislands+1 */
     uint32_t* isl_con;
     int* island_index;
+    /* joints (PhysicsWorld::mConstraints) and their islands */
+    joint_t* joints;
+    uint32_t njoints;
+    uint32_t *isl_joff, *isl_joint; /* nislands+1 offsets, joint indices in joint order */
     /* stats */
     uint32_t st_points, st_batches, st_max_vl, st_max_bl, st_max_isl_pts, st_sum_vl, st_max_open;
     uint32_t st_max_iters, st_pt_iters;
@@ -650,12 +670,458 @@ static void solve_bias(kzo_world* w, con_t* c) {
 }
 
 /* SolveIsland, PhysicsWorld.cpp:666-743 (SIMD path, no joints). */
+/* ----------------------------------------------------------------------------- */
+/* Joints (Constraints.cpp:1-597, Constraints.h:41-277)                           */
+/* ----------------------------------------------------------------------------- */
+static m3 m_diag(float s) {
+    m3 r;
+    r.c[0] = V(1.0f * s, 0.0f * s, 0.0f * s);
+    r.c[1] = V(0.0f * s, 1.0f * s, 0.0f * s);
+    r.c[2] = V(0.0f * s, 0.0f * s, 1.0f * s);
+    return r;
+}
+static m3 m_skew(v3 v) { /* Mat3::Skew (Math.h:193-197) */
+    m3 r;
+    r.c[0] = V(0.0f, v.z, -v.y);
+    r.c[1] = V(-v.z, 0.0f, v.x);
+    r.c[2] = V(v.y, -v.x, 0.0f);
+    return r;
+}
+static m3 m_add(m3 a, m3 b) { m3 r; for (int k = 0; k < 3; ++k) r.c[k] = vadd(a.c[k], b.c[k]); return r; }
+static m3 m_sub(m3 a, m3 b) { m3 r; for (int k = 0; k < 3; ++k) r.c[k] = vsub(a.c[k], b.c[k]); return r; }
+static m3 m_zero(void) { m3 r; r.c[0] = r.c[1] = r.c[2] = V(0, 0, 0); return r; }
+static m3 m_inverse(m3 m) { /* Mat3::Inversed (Math.cpp:27-43): adjugate / determinant */
+    v3 r0 = vcross(m.c[1], m.c[2]), r1 = vcross(m.c[2], m.c[0]), r2 = vcross(m.c[0], m.c[1]);
+    float det = vdot(m.c[0], r0);
+    float inv = det != 0.0f ? 1.0f / det : 0.0f;
+    m3 o;
+    o.c[0] = vmul(V(r0.x, r1.x, r2.x), inv);
+    o.c[1] = vmul(V(r0.y, r1.y, r2.y), inv);
+    o.c[2] = vmul(V(r0.z, r1.z, r2.z), inv);
+    return o;
+}
+static void v_basis(v3 n, v3* b, v3* c) { /* Vec3::GetBasis (Math.cpp:9-22) */
+    if (n.z < -0.9999999f) {
+        *b = V(0.0f, -1.0f, 0.0f);
+        *c = V(-1.0f, 0.0f, 0.0f);
+    } else {
+        const float a = 1.0f / (1.0f + n.z);
+        const float bb = -n.x * n.y * a;
+        *b = V(1.0f - n.x * n.x * a, bb, -n.x);
+        *c = V(bb, 1.0f - n.y * n.y * a, -n.y);
+    }
+}
+static qt q_conj(qt q) { return Q(-q.x, -q.y, -q.z, q.w); }
+
+
+static m3 point_mass(const kzo_world* w, int a, int b, v3 ra, v3 rb) { /* Constraints.cpp:23-33 */
+    m3 K = m_diag(w->inv_mass[a] + w->inv_mass[b]);
+    m3 sa = m_skew(ra), sb = m_skew(rb);
+    m3 t = mmul(&w->iiw[a], &sa);
+    t = mmul(&sa, &t);
+    K = m_sub(K, t);
+    t = mmul(&w->iiw[b], &sb);
+    t = mmul(&sb, &t);
+    return m_sub(K, t);
+}
+static float angular_mass(const kzo_world* w, int a, int b, v3 axis) { /* :35-41 */
+    float k = vdot(axis, mmulv(&w->iiw[a], axis)) + vdot(axis, mmulv(&w->iiw[b], axis));
+    return k > KZO_EPS ? 1.0f / k : 0.0f;
+}
+static float linear_mass(const kzo_world* w, int a, int b, v3 ra, v3 rb, v3 axis) { /* :43-52 */
+    v3 ca = vcross(ra, axis), cb = vcross(rb, axis);
+    float k = w->inv_mass[a] + w->inv_mass[b];
+    k += vdot(ca, mmulv(&w->iiw[a], ca));
+    k += vdot(cb, mmulv(&w->iiw[b], cb));
+    return k > KZO_EPS ? 1.0f / k : 0.0f;
+}
+static void apply_impulse(kzo_world* w, int a, int b, v3 ra, v3 rb, v3 imp) { /* :8-15 */
+    w->lv[a] = vadd(w->lv[a], vmul(imp, w->inv_mass[a]));
+    w->av[a] = vadd(w->av[a], mmulv(&w->iiw[a], vcross(ra, imp)));
+    w->lv[b] = vsub(w->lv[b], vmul(imp, w->inv_mass[b]));
+    w->av[b] = vsub(w->av[b], mmulv(&w->iiw[b], vcross(rb, imp)));
+}
+static void apply_angular(kzo_world* w, int a, int b, v3 ang) { /* :17-20 */
+    w->av[a] = vadd(w->av[a], mmulv(&w->iiw[a], ang));
+    w->av[b] = vsub(w->av[b], mmulv(&w->iiw[b], ang));
+}
+static qt rotate_by(qt q, v3 dw) { /* IntegrateRotation(q, dw) (:54-59) with Quat::AxisAngle (Math.cpp:78-83) */
+    float a2 = vlen2(dw);
+    if (a2 < 1.0e-12f) return q;
+    float a = sqrtf(a2);
+    v3 ax = vnormalized(vdiv(dw, a));
+    float half = a * 0.5f;
+    float s = sinf(half);
+    qt r = Q(ax.x * s, ax.y * s, ax.z * s, cosf(half));
+    return qnormalized(qmul(r, q));
+}
+static void apply_positional(kzo_world* w, int a, int b, v3 lin, v3 ang) { /* :62-71 */
+    w->pos[a] = vadd(w->pos[a], vmul(lin, w->inv_mass[a]));
+    w->rot[a] = rotate_by(w->rot[a], mmulv(&w->iiw[a], ang));
+    w->pos[b] = vsub(w->pos[b], vmul(lin, w->inv_mass[b]));
+    w->rot[b] = rotate_by(w->rot[b], vneg(mmulv(&w->iiw[b], ang)));
+}
+static v3 rel_vel(const kzo_world* w, const joint_t* j) {
+    return vsub(vadd(w->lv[j->a], vcross(w->av[j->a], j->r0)), vadd(w->lv[j->b], vcross(w->av[j->b], j->r1)));
+}
+static float hinge_angle(const kzo_world* w, const joint_t* j) { /* HingeConstraint::GetAngle (:361-368) */
+    v3 axis = qrotate(w->rot[j->a], j->lax);
+    v3 pa = qrotate(w->rot[j->a], j->lpa[0]), pb = qrotate(w->rot[j->b], j->lpb[0]);
+    return atan2f(vdot(axis, vcross(pa, pb)), vdot(pa, pb));
+}
+
+/* Constructors: world anchors and axes at the bodies' current poses. */
+static void joint_init(const kzo_world* w, joint_t* j, const float* f, uint32_t modes, uint32_t motors, const float* six) {
+    const int a = (int)j->a, b = (int)j->b;
+    v3 anA = V(f[0], f[1], f[2]), anB = V(f[3], f[4], f[5]), axA = V(f[6], f[7], f[8]), axB = V(f[9], f[10], f[11]);
+    qt rot = Q(f[12], f[13], f[14], f[15]);
+    j->target = f[16]; j->lower = f[17]; j->upper = f[18]; j->motor_target = f[19]; j->motor_max = f[20];
+    j->modes = modes; j->motors = motors;
+    for (int k = 0; k < 12; ++k) j->six[k] = six[k];
+    if (j->type == 0 && (j->flags & 8u)) {
+        j->la = anA; j->lb = anB;
+    } else if (j->type == 1) {
+        j->la = qinv_rotate(w->rot[a], vsub(anA, w->pos[a]));
+        j->lb = qinv_rotate(w->rot[b], vsub(anB, w->pos[b]));
+    } else {
+        j->la = qinv_rotate(w->rot[a], vsub(anA, w->pos[a]));
+        j->lb = qinv_rotate(w->rot[b], vsub(anA, w->pos[b]));
+    }
+    if (j->type == 2) j->relrot = qmul(q_conj(w->rot[a]), w->rot[b]);
+    if (j->type == 3) {
+        j->lax = qinv_rotate(w->rot[a], vnormalized(axA));
+        j->lbx = qinv_rotate(w->rot[b], vnormalized(axB));
+        v_basis(j->lax, &j->lpa[0], &j->lpa[1]);
+        v_basis(j->lbx, &j->lpb[0], &j->lpb[1]);
+        if (!(j->flags & 2u)) { j->lower = -3.14159265358979323846f; j->upper = 3.14159265358979323846f; }
+    }
+    if (j->type == 4) {
+        j->lax = qinv_rotate(w->rot[a], vnormalized(axA));
+        j->lbx = qinv_rotate(w->rot[b], vnormalized(axA));
+        if (!(j->flags & 2u)) { j->lower = 0.0f; j->upper = 0.0f; }
+    }
+    if (j->type == 5) j->crot = qtomat(rot);
+}
+
+static void joint_prepare(const kzo_world* w, joint_t* j) {
+    const int a = (int)j->a, b = (int)j->b;
+    j->r0 = qrotate(w->rot[a], j->la);
+    j->r1 = qrotate(w->rot[b], j->lb);
+    switch (j->type) {
+        case 0: j->m1 = m_inverse(point_mass(w, a, b, j->r0, j->r1)); break;
+        case 1: {
+            v3 d = vsub(vadd(w->pos[b], j->r1), vadd(w->pos[a], j->r0));
+            float dist = vlen(d);
+            j->axis = dist > KZO_EPS ? vdiv(d, dist) : V(0.0f, 1.0f, 0.0f);
+            j->dmass = linear_mass(w, a, b, j->r0, j->r1, j->axis);
+            break;
+        }
+        case 2:
+            j->m1 = m_inverse(point_mass(w, a, b, j->r0, j->r1));
+            j->m2 = m_inverse(m_add(w->iiw[a], w->iiw[b]));
+            break;
+        case 3: {
+            j->m1 = m_inverse(point_mass(w, a, b, j->r0, j->r1));
+            v3 pa[2] = {qrotate(w->rot[a], j->lpa[0]), qrotate(w->rot[a], j->lpa[1])};
+            v3 pb[2] = {qrotate(w->rot[b], j->lpb[0]), qrotate(w->rot[b], j->lpb[1])};
+            for (int i = 0; i < 2; ++i) {
+                v3 axis = vnormalized_or(vadd(pa[i], pb[i]), pa[i]);
+                j->sm[i] = angular_mass(w, a, b, axis);
+                j->lpa[i] = qinv_rotate(w->rot[a], axis);
+            }
+            j->limit_mass = angular_mass(w, a, b, qrotate(w->rot[a], j->lax));
+            break;
+        }
+        case 4: {
+            v3 axis = qrotate(w->rot[a], j->lax), p[2];
+            v_basis(axis, &p[0], &p[1]);
+            j->axial_mass = linear_mass(w, a, b, j->r0, j->r1, axis);
+            m3 K = point_mass(w, a, b, j->r0, j->r1);
+            float k00 = vdot(p[0], mmulv(&K, p[0]));
+            float k01 = vdot(p[0], mmulv(&K, p[1]));
+            float k11 = vdot(p[1], mmulv(&K, p[1]));
+            float det = k00 * k11 - k01 * k01;
+            if (fabs_r(det) > 1.0e-12f) {
+                float inv = 1.0f / det;
+                j->m1.c[0] = vadd(vmul(p[0], k11 * inv), vmul(p[1], -k01 * inv));
+                j->m1.c[1] = vadd(vmul(p[0], -k01 * inv), vmul(p[1], k00 * inv));
+                j->m1.c[2] = V(0, 0, 0);
+            } else {
+                j->m1 = m_zero();
+            }
+            j->m2 = m_inverse(m_add(w->iiw[a], w->iiw[b]));
+            break;
+        }
+        case 5: {
+            m3 ra = qtomat(w->rot[a]);
+            m3 r = mmul(&ra, &j->crot);
+            for (int i = 0; i < 3; ++i) j->axes[i] = r.c[i];
+            break;
+        }
+    }
+}
+
+static void joint_warm(kzo_world* w, joint_t* j) {
+    const int a = (int)j->a, b = (int)j->b;
+    switch (j->type) {
+        case 0: apply_impulse(w, a, b, j->r0, j->r1, j->imp1); break;
+        case 1: apply_impulse(w, a, b, j->r0, j->r1, vmul(j->axis, j->dimp)); break;
+        case 2:
+            apply_impulse(w, a, b, j->r0, j->r1, j->imp1);
+            apply_angular(w, a, b, j->imp2);
+            break;
+        case 3:
+            apply_impulse(w, a, b, j->r0, j->r1, j->imp1);
+            for (int i = 0; i < 2; ++i) apply_angular(w, a, b, vmul(qrotate(w->rot[a], j->lpa[i]), j->simp[i]));
+            apply_angular(w, a, b, vmul(qrotate(w->rot[a], j->lax), j->limit_imp + j->motor_imp));
+            break;
+        case 4:
+            apply_impulse(w, a, b, j->r0, j->r1, j->imp1);
+            apply_angular(w, a, b, j->imp2);
+            apply_impulse(w, a, b, j->r0, j->r1, vmul(qrotate(w->rot[a], j->lax), j->axial_imp));
+            break;
+        case 5:
+            for (int i = 0; i < 3; ++i) {
+                apply_impulse(w, a, b, j->r0, j->r1, j->lin_imp[i]);
+                apply_angular(w, a, b, j->ang_imp[i]);
+            }
+            break;
+    }
+}
+
+static void joint_velocity(kzo_world* w, joint_t* j) {
+    const int a = (int)j->a, b = (int)j->b;
+    switch (j->type) {
+        case 0: {
+            v3 imp = mmulv(&j->m1, vneg(rel_vel(w, j)));
+            j->imp1 = vadd(j->imp1, imp);
+            apply_impulse(w, a, b, j->r0, j->r1, imp);
+            break;
+        }
+        case 1: {
+            float lambda = -j->dmass * vdot(rel_vel(w, j), j->axis);
+            j->dimp += lambda;
+            apply_impulse(w, a, b, j->r0, j->r1, vmul(j->axis, lambda));
+            break;
+        }
+        case 2: {
+            v3 li = mmulv(&j->m1, vneg(rel_vel(w, j)));
+            j->imp1 = vadd(j->imp1, li);
+            apply_impulse(w, a, b, j->r0, j->r1, li);
+            v3 ai = mmulv(&j->m2, vneg(vsub(w->av[a], w->av[b])));
+            j->imp2 = vadd(j->imp2, ai);
+            apply_angular(w, a, b, ai);
+            break;
+        }
+        case 3: {
+            v3 li = mmulv(&j->m1, vneg(rel_vel(w, j)));
+            j->imp1 = vadd(j->imp1, li);
+            apply_impulse(w, a, b, j->r0, j->r1, li);
+            v3 wrel = vsub(w->av[a], w->av[b]);
+            for (int i = 0; i < 2; ++i) {
+                v3 axis = qrotate(w->rot[a], j->lpa[i]);
+                float lambda = -j->sm[i] * vdot(wrel, axis);
+                j->simp[i] += lambda;
+                apply_angular(w, a, b, vmul(axis, lambda));
+            }
+            if (j->flags & 4u) {
+                v3 ha = qrotate(w->rot[a], j->lax);
+                float rv = vdot(vsub(w->av[a], w->av[b]), ha);
+                float lambda = j->limit_mass * (j->motor_target - rv);
+                float ni = fclamp_r(j->motor_imp + lambda, -j->motor_max, j->motor_max);
+                lambda = ni - j->motor_imp;
+                j->motor_imp = ni;
+                apply_angular(w, a, b, vmul(ha, lambda));
+            }
+            if (j->flags & 2u) {
+                v3 ha = qrotate(w->rot[a], j->lax);
+                float angle = hinge_angle(w, j);
+                float rv = vdot(vsub(w->av[a], w->av[b]), ha);
+                float lambda = 0.0f;
+                if (angle <= j->lower) {
+                    lambda = j->limit_mass * (-rv);
+                    j->limit_imp = fmax_r(j->limit_imp + lambda, 0.0f);
+                    lambda = j->limit_imp;
+                } else if (angle >= j->upper) {
+                    lambda = j->limit_mass * (-rv);
+                    j->limit_imp = fmin_r(j->limit_imp + lambda, 0.0f);
+                    lambda = j->limit_imp;
+                } else {
+                    j->limit_imp = 0.0f;
+                    lambda = 0.0f;
+                }
+                if (lambda != 0.0f) apply_angular(w, a, b, vmul(ha, lambda));
+            }
+            break;
+        }
+        case 4: {
+            v3 axis = qrotate(w->rot[a], j->lax);
+            v3 vr = rel_vel(w, j);
+            v3 vp = vsub(vr, vmul(axis, vdot(vr, axis)));
+            v3 pi = vneg(mmulv(&j->m1, vp));
+            j->imp1 = vadd(j->imp1, pi);
+            apply_impulse(w, a, b, j->r0, j->r1, pi);
+            v3 ai = mmulv(&j->m2, vneg(vsub(w->av[a], w->av[b])));
+            j->imp2 = vadd(j->imp2, ai);
+            apply_angular(w, a, b, ai);
+            float rel = vdot(vsub(w->lv[a], w->lv[b]), axis);
+            if (j->flags & 4u) {
+                float lambda = j->axial_mass * (j->motor_target - rel);
+                float ni = fclamp_r(j->motor_imp + lambda, -j->motor_max, j->motor_max);
+                lambda = ni - j->motor_imp;
+                j->motor_imp = ni;
+                apply_impulse(w, a, b, j->r0, j->r1, vmul(axis, lambda));
+            } else if (j->flags & 2u) {
+                v3 ra = qrotate(w->rot[a], j->la), rb = qrotate(w->rot[b], j->lb);
+                float pos = vdot(vsub(vadd(w->pos[b], rb), vadd(w->pos[a], ra)), axis);
+                float lambda = 0.0f;
+                if (pos <= j->lower) {
+                    lambda = j->axial_mass * (-rel);
+                    j->axial_imp = fmax_r(j->axial_imp + lambda, 0.0f);
+                    lambda = j->axial_imp;
+                } else if (pos >= j->upper) {
+                    lambda = j->axial_mass * (-rel);
+                    j->axial_imp = fmin_r(j->axial_imp + lambda, 0.0f);
+                    lambda = j->axial_imp;
+                } else {
+                    j->axial_imp = 0.0f;
+                }
+                if (lambda != 0.0f) apply_impulse(w, a, b, j->r0, j->r1, vmul(axis, lambda));
+            }
+            break;
+        }
+        case 5: {
+            for (int k = 0; k < 3; ++k) { /* SolveLinearAxis (:503-536) */
+                const uint32_t mode = (j->modes >> (2 * k)) & 3u;
+                const int motor = (j->motors >> k) & 1u;
+                if (mode == 0u && !motor) continue;
+                v3 dir = j->axes[k];
+                float rel = vdot(rel_vel(w, j), dir);
+                float mass = linear_mass(w, a, b, j->r0, j->r1, dir);
+                float target = 0.0f;
+                float lambda = mass * (target - rel);
+                if (motor) {
+                    target = j->six[k];
+                    lambda = mass * (target - rel);
+                    float mx = j->six[3 + k];
+                    float acc = vdot(j->lin_imp[k], dir);
+                    float na = fclamp_r(acc + lambda, -mx, mx);
+                    lambda = na - acc;
+                } else if (mode == 2u) {
+                    lambda = mass * (-rel);
+                }
+                v3 imp = vmul(dir, lambda);
+                j->lin_imp[k] = vadd(j->lin_imp[k], imp);
+                apply_impulse(w, a, b, j->r0, j->r1, imp);
+            }
+            for (int k = 0; k < 3; ++k) { /* SolveAngularAxis (:538-557) */
+                const uint32_t mode = (j->modes >> (2 * k + 6)) & 3u;
+                const int motor = (j->motors >> (3 + k)) & 1u;
+                if (mode == 0u && !motor) continue;
+                v3 dir = j->axes[k];
+                float rel = vdot(vsub(w->av[a], w->av[b]), dir);
+                float mass = angular_mass(w, a, b, dir);
+                float lambda;
+                if (motor) {
+                    lambda = mass * (j->six[6 + k] - rel);
+                    float acc = vdot(j->ang_imp[k], dir);
+                    float na = fclamp_r(acc + lambda, -j->six[9 + k], j->six[9 + k]);
+                    lambda = na - acc;
+                } else {
+                    lambda = mass * (-rel);
+                }
+                v3 imp = vmul(dir, lambda);
+                j->ang_imp[k] = vadd(j->ang_imp[k], imp);
+                apply_angular(w, a, b, imp);
+            }
+            break;
+        }
+    }
+}
+
+static void joint_position(kzo_world* w, joint_t* j) {
+    const int a = (int)j->a, b = (int)j->b;
+    v3 ra = qrotate(w->rot[a], j->la), rb = qrotate(w->rot[b], j->lb);
+    switch (j->type) {
+        case 0: {
+            v3 err = vsub(vadd(w->pos[a], ra), vadd(w->pos[b], rb));
+            const float slop = 0.001f;
+            if (vlen2(err) < slop * slop) return;
+            m3 K = m_inverse(point_mass(w, a, b, ra, rb));
+            v3 imp = mmulv(&K, vneg(err));
+            apply_positional(w, a, b, imp, vcross(ra, imp));
+            break;
+        }
+        case 1: {
+            v3 d = vsub(vadd(w->pos[b], rb), vadd(w->pos[a], ra));
+            float dist = vlen(d);
+            if (dist < KZO_EPS) return;
+            v3 axis = vdiv(d, dist);
+            float err = dist - j->target;
+            float k = linear_mass(w, a, b, ra, rb, axis);
+            float lambda = -k * err * 0.2f;
+            apply_positional(w, a, b, vmul(axis, lambda), V(0, 0, 0));
+            break;
+        }
+        case 2: case 3: {
+            v3 err = vsub(vadd(w->pos[a], ra), vadd(w->pos[b], rb));
+            if (vlen2(err) > 1.0e-8f) {
+                m3 K = m_inverse(point_mass(w, a, b, ra, rb));
+                v3 imp = vmul(mmulv(&K, vneg(err)), 0.2f);
+                apply_positional(w, a, b, imp, vcross(ra, imp));
+            }
+            if (j->type == 3) break;
+            qt cur = qmul(q_conj(w->rot[a]), w->rot[b]);
+            qt diff = qmul(cur, q_conj(j->relrot));
+            if (diff.w < 0.0f) diff = Q(-diff.x, -diff.y, -diff.z, -diff.w);
+            float s = sqrtf(fmax_r(0.0f, 1.0f - diff.w * diff.w));
+            v3 axis = s >= KZO_EPS ? vdiv(V(diff.x, diff.y, diff.z), s) : V(1.0f, 0.0f, 0.0f);
+            float angle = 2.0f * acosf(fclamp_r(diff.w, -1.0f, 1.0f));
+            if (fabs_r(angle) > 1.0e-4f) {
+                v3 ae = vmul(axis, angle);
+                m3 K = m_inverse(m_add(w->iiw[a], w->iiw[b]));
+                v3 imp = vmul(mmulv(&K, vneg(ae)), 0.2f);
+                apply_positional(w, a, b, V(0, 0, 0), imp);
+            }
+            break;
+        }
+        case 4: {
+            v3 axis = qrotate(w->rot[a], j->lax);
+            v3 err = vsub(vadd(w->pos[a], ra), vadd(w->pos[b], rb));
+            err = vsub(err, vmul(axis, vdot(err, axis)));
+            if (vlen2(err) > 1.0e-8f) {
+                m3 K = m_inverse(point_mass(w, a, b, ra, rb));
+                v3 imp = vmul(mmulv(&K, vneg(err)), 0.2f);
+                imp = vsub(imp, vmul(axis, vdot(imp, axis)));
+                apply_positional(w, a, b, imp, vcross(ra, imp));
+            }
+            break;
+        }
+        case 5: {
+            v3 err = vsub(vadd(w->pos[a], ra), vadd(w->pos[b], rb));
+            for (int k = 0; k < 3; ++k) {
+                if (((j->modes >> (2 * k)) & 3u) != 2u) continue;
+                v3 dir = j->axes[k];
+                float e = vdot(err, dir);
+                if (fabs_r(e) < 1.0e-4f) continue;
+                float mass = linear_mass(w, a, b, ra, rb, dir);
+                v3 imp = vmul(dir, -mass * e * 0.2f);
+                apply_positional(w, a, b, imp, vcross(ra, imp));
+            }
+            break;
+        }
+    }
+}
+
 static void solve_island(kzo_world* w, uint32_t isl, uint32_t* out_batches, uint32_t* out_vl, uint32_t* out_bl,
                          uint32_t* out_pts, uint32_t* out_iters, uint32_t* out_pt_iters, float* out_res) {
     const uint32_t* list = w->isl_con + w->isl_off[isl];
     uint32_t nc = w->isl_off[isl + 1] - w->isl_off[isl];
-    if (nc == 0) return;
+    const uint32_t* jl = w->isl_joint + w->isl_joff[isl];
+    const uint32_t nj = w->isl_joff[isl + 1] - w->isl_joff[isl];
+    if (nc == 0 && nj == 0) return;
     for (uint32_t i = 0; i < nc; ++i) warm_start(w, &w->cons[list[i]]);
+    for (uint32_t i = 0; i < nj; ++i) joint_warm(w, &w->joints[jl[i]]);
 
     uint32_t npts = 0;
     for (uint32_t i = 0; i < nc; ++i) npts += w->cons[list[i]].npts;
@@ -716,6 +1182,9 @@ static void solve_island(kzo_world* w, uint32_t isl, uint32_t* out_batches, uint
     *out_iters = used;
     *out_pt_iters = nbp * used;
     *out_res = res;
+    /* joint velocity iterations: the configured count (the residual rule stops contacts only) */
+    for (uint32_t it = 0; it < w->vel_iters; ++it)
+        for (uint32_t i = 0; i < nj; ++i) joint_velocity(w, &w->joints[jl[i]]);
     if (!w->vel_bias)
         for (uint32_t it = 0; it < w->pos_iters; ++it)
             for (uint32_t i = 0; i < nc; ++i) solve_bias(w, &w->cons[list[i]]);
@@ -831,6 +1300,13 @@ static void build_islands(kzo_world* w) {
         int ia = w->island_index[c->a], ib = w->island_index[c->b];
         if (ia >= 0 && ib >= 0) uf_union(par, rank, (uint32_t)ia, (uint32_t)ib);
     }
+    for (uint32_t ji = 0; ji < w->njoints; ++ji) { /* joints join islands too (PhysicsWorld.cpp:625-633) */
+        const joint_t* j = &w->joints[ji];
+        if (j->flags & 1u) continue;
+        if (w->motion[j->a] != KZO_DYNAMIC || w->motion[j->b] != KZO_DYNAMIC) continue;
+        int ia = w->island_index[j->a], ib = w->island_index[j->b];
+        if (ia >= 0 && ib >= 0) uf_union(par, rank, (uint32_t)ia, (uint32_t)ib);
+    }
     uint32_t* r2i = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * numDyn);
     for (uint32_t i = 0; i < numDyn; ++i) r2i[i] = NUL;
     uint32_t ni = 0;
@@ -857,6 +1333,27 @@ static void build_islands(kzo_world* w) {
     for (uint32_t i = 0; i < ni; ++i) fill[i] = w->isl_off[i];
     for (uint32_t ci = 0; ci < w->ncons; ++ci)
         if (isl[ci] != NUL) w->isl_con[fill[isl[ci]]++] = ci;
+    /* joints of each island in joint order (PhysicsWorld.cpp:656-661) */
+    w->isl_joff = (uint32_t*)xrealloc(w->isl_joff, sizeof(uint32_t) * (ni + 1));
+    memset(w->isl_joff, 0, sizeof(uint32_t) * (ni + 1));
+    uint32_t* jis = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * (w->njoints ? w->njoints : 1));
+    for (uint32_t ji = 0; ji < w->njoints; ++ji) {
+        const joint_t* j = &w->joints[ji];
+        uint32_t is = NUL;
+        if (!(j->flags & 1u)) {
+            if (w->motion[j->a] == KZO_DYNAMIC && w->island_index[j->a] >= 0) is = r2i[uf_find(par, (uint32_t)w->island_index[j->a])];
+            if (is == NUL && w->motion[j->b] == KZO_DYNAMIC && w->island_index[j->b] >= 0)
+                is = r2i[uf_find(par, (uint32_t)w->island_index[j->b])];
+        }
+        jis[ji] = is;
+        if (is != NUL) w->isl_joff[is + 1]++;
+    }
+    for (uint32_t i = 0; i < ni; ++i) w->isl_joff[i + 1] += w->isl_joff[i];
+    w->isl_joint = (uint32_t*)xrealloc(w->isl_joint, sizeof(uint32_t) * (w->njoints ? w->njoints : 1));
+    for (uint32_t i = 0; i < ni; ++i) fill[i] = w->isl_joff[i];
+    for (uint32_t ji = 0; ji < w->njoints; ++ji)
+        if (jis[ji] != NUL) w->isl_joint[fill[jis[ji]]++] = ji;
+    free(jis);
     free(fill);
     free(isl);
     free(r2i);
@@ -1000,6 +1497,8 @@ int kzo_step(kzo_world* w, float dt) {
     integrate_velocities(w, dt);
     /* 5. solve */
     for (uint32_t ci = 0; ci < w->ncons; ++ci) prepare(w, &w->cons[ci], dt);
+    for (uint32_t ji = 0; ji < w->njoints; ++ji)
+        if (!(w->joints[ji].flags & 1u)) joint_prepare(w, &w->joints[ji]);
     build_islands(w);
     w->st_batches = w->st_max_vl = w->st_max_bl = w->st_max_isl_pts = w->st_sum_vl = w->st_max_open = 0;
     int ni = (int)w->nislands;
@@ -1059,6 +1558,10 @@ int kzo_step(kzo_world* w, float dt) {
         int i = w->active[k];
         if (w->motion[i] == KZO_DYNAMIC) update_world_inertia(w, i);
     }
+    /* 7. joint position correction per island (PhysicsWorld.cpp:293-306, 745-752) */
+    for (uint32_t is = 0; is < w->nislands; ++is)
+        for (uint32_t it = 0; it < w->pos_iters; ++it)
+            for (uint32_t k = w->isl_joff[is]; k < w->isl_joff[is + 1]; ++k) joint_position(w, &w->joints[w->isl_joint[k]]);
     /* 9. clear forces */
     for (int i = 0; i < w->nb; ++i) { w->force[i] = V(0, 0, 0); w->torque[i] = V(0, 0, 0); }
     uint32_t pts = 0;
@@ -1181,6 +1684,27 @@ kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* res
         w->proxy[i] = create_proxy(w, b, w->packed[i], w->layer[i], w->mask[i]);
         w->fat[i] = AB(vsub(b.mn, V(0.1f, 0.1f, 0.1f)), vadd(b.mx, V(0.1f, 0.1f, 0.1f)));
     }
+    /* optional joint section, created after every body (PhysicsWorld::AddConstraint) */
+    if (r.off < r.n) {
+        uint32_t nj = rd_u32(&r);
+        if (nj > (uint32_t)(r.n / 156u)) { set_err("bad joint count"); kzo_destroy(w); return NULL; }
+        w->joints = (joint_t*)calloc(nj ? nj : 1, sizeof(joint_t));
+        for (uint32_t k = 0; k < nj; ++k) {
+            joint_t* j = &w->joints[k];
+            j->type = rd_u32(&r); j->a = rd_u32(&r); j->b = rd_u32(&r); j->flags = rd_u32(&r);
+            float f[21], six[12];
+            for (int q = 0; q < 21; ++q) f[q] = rd_f32(&r);
+            uint32_t modes = rd_u32(&r), motors = rd_u32(&r);
+            for (int q = 0; q < 12; ++q) six[q] = rd_f32(&r);
+            if (r.bad || j->type > 5u || j->a >= (uint32_t)nb || j->b >= (uint32_t)nb) {
+                set_err("bad joint record");
+                kzo_destroy(w);
+                return NULL;
+            }
+            joint_init(w, j, f, modes, motors, six);
+            w->njoints = k + 1;
+        }
+    }
     w->use_ccd = 1;
     w->ccd_max_pen = 0.01f;
     w->cache_cap = 1024;
@@ -1196,7 +1720,7 @@ void kzo_destroy(kzo_world* w) {
                     w->plv, w->pav, w->force, w->torque, w->rot, w->inv_mass, w->lin_damp, w->ang_damp, w->grav,
                     w->max_lin, w->max_ang, w->fric, w->rest, w->iil, w->iiw, w->active, w->island_index,
                     w->nodes, w->bp_layer, w->bp_mask, w->cache, w->pairs, w->ext_pairs, w->man, w->keys,
-                    w->cons, w->isl_off, w->isl_con};
+                    w->cons, w->isl_off, w->isl_con, w->joints, w->isl_joff, w->isl_joint};
     for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; ++i) free(ptrs[i]);
     free(w);
 }

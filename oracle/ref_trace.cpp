@@ -17,6 +17,7 @@
 #include <cstring>
 #include <cstdint>
 #include <chrono>
+#include <memory>
 #include <vector>
 
 using namespace kizuri;
@@ -147,6 +148,60 @@ int main(int argc, char** argv) {
         if (flags & 4u) bs.motionQuality = MotionQuality::LinearCast;
         ids[i] = world.CreateBody(bs);
         if (ids[i].IsInvalid()) { std::fprintf(stderr, "body %u invalid\n", i); return 1; }
+    }
+
+    // Optional joint section: count, then per joint {type, body A, body B, flags, anchor A/B,
+    // axis A/B, rotation, distance, limits, motor, axis modes, motor mask, six-dof motors}, created
+    // through the reference's constructors and PhysicsWorld::AddConstraint.
+    uint32_t nj = rd.off < rd.buf.size() ? rd.get<uint32_t>() : 0u;
+    for (uint32_t j = 0; j < nj; ++j) {
+        uint32_t type = rd.get<uint32_t>(), ia = rd.get<uint32_t>(), ib = rd.get<uint32_t>(), fl = rd.get<uint32_t>();
+        float f[21];
+        for (float& x : f) x = rd.get<float>();
+        uint32_t modes = rd.get<uint32_t>(), motors = rd.get<uint32_t>();
+        float sm[12];
+        for (float& x : sm) x = rd.get<float>();
+        Body* a = world.GetBody(ids[ia]);
+        Body* b = world.GetBody(ids[ib]);
+        const Vec3 anA(f[0], f[1], f[2]), anB(f[3], f[4], f[5]), axA(f[6], f[7], f[8]), axB(f[9], f[10], f[11]);
+        const Quat rot(f[12], f[13], f[14], f[15]);
+        std::unique_ptr<Constraint> c;
+        switch (type) {
+            case 0:
+                if (fl & 8u) c = std::make_unique<PointConstraint>(a, b, anA, anB);
+                else c = std::make_unique<PointConstraint>(a, b, anA);
+                break;
+            case 1: c = std::make_unique<DistanceConstraint>(a, b, anA, anB, f[16]); break;
+            case 2: c = std::make_unique<FixedConstraint>(a, b, anA); break;
+            case 3: {
+                auto h = std::make_unique<HingeConstraint>(a, b, anA, axA, axB);
+                if (fl & 2u) h->SetLimits(f[17], f[18]);
+                if (fl & 4u) h->SetMotor(f[19], f[20]);
+                c = std::move(h);
+                break;
+            }
+            case 4: {
+                auto sl = std::make_unique<SliderConstraint>(a, b, anA, axA);
+                if (fl & 2u) sl->SetLimits(f[17], f[18]);
+                if (fl & 4u) sl->SetMotor(f[19], f[20]);
+                c = std::move(sl);
+                break;
+            }
+            case 5: {
+                auto d = std::make_unique<SixDOFConstraint>(a, b, anA, rot);
+                for (uint32_t k = 0; k < 3; ++k) {
+                    d->SetLinearAxisMode(k, SixDOFConstraint::AxisMode((modes >> (2 * k)) & 3u));
+                    d->SetAngularAxisMode(k, SixDOFConstraint::AxisMode((modes >> (2 * k + 6)) & 3u));
+                    if (motors & (1u << k)) d->SetLinearMotor(k, sm[k], sm[3 + k]);
+                    if (motors & (8u << k)) d->SetAngularMotor(k, sm[6 + k], sm[9 + k]);
+                }
+                c = std::move(d);
+                break;
+            }
+            default: std::fprintf(stderr, "joint type %u unsupported\n", type); return 1;
+        }
+        if (fl & 1u) c->SetEnabled(false);
+        world.AddConstraint(std::move(c));
     }
 
     FILE* f = std::fopen(outPath, "wb");

@@ -11,6 +11,7 @@ resolved mass properties and every hull as built by ConvexHullShape::Create.
 from __future__ import annotations
 
 import argparse
+import math
 import os
 import subprocess
 import sys
@@ -36,7 +37,76 @@ def fixture_scenes():
     out["pile64_nows"] = (_nows(scenes.pile(64, seed=77, extent=1.5, y_range=(1.0, 5.0))), 240, 2, [0, 59, 239])
     out["pyramid4_tests"] = (_reference_test_pyramid(), 240, 2, [0, 239])
     out["ccd_shots"] = (_ccd_shots(), 120, 2, [0, 1, 29, 59, 119])
+    out["joints_mix"] = (_joints_mix(), 180, 2, [0, 1, 59, 179])
     return out
+
+
+def _joints_mix():
+    """Every joint type (Constraints.h:41-277) beside contacts: a point-joint chain hanging from
+    a static post, a motorised hinge door with limits, sliders with limits and with a motor, a
+    fixed pair and a distance pair falling onto the ground (contacts and joints in one island), a
+    six-dof joint with fixed, limited and motorised axes, and a disabled joint."""
+    S = scenes
+    sc = S.Scene(name="joints_mix")
+    S._timed_settings(sc, 10, 2)
+    S._ground(sc, 0.6)
+    post = sc.add_shape(S.Shape(S.SHAPE_BOX, [0.1, 2.0, 0.1, 0.0]))
+    link = sc.add_shape(S.Shape(S.SHAPE_BOX, [0.1, 0.25, 0.1, 0.0]))
+    door = sc.add_shape(S.Shape(S.SHAPE_BOX, [0.5, 0.8, 0.05, 0.0]))
+    cube = sc.add_shape(S.Shape(S.SHAPE_BOX, [0.3, 0.3, 0.3, 0.0]))
+    ball = sc.add_shape(S.Shape(S.SHAPE_SPHERE, [0.25, 0.0, 0.0, 0.0]))
+    cap = sc.add_shape(S.Shape(S.SHAPE_CAPSULE, [0.3, 0.15, 0.0, 0.0]))
+    st = S.MOTION_STATIC
+    J = []
+    # chain: static post at x=0 (top at y=4), 6 links hanging beside it from x=0.4, swinging
+    p0 = sc.add_body(S.Body(post, st, pos=(0.0, 2.0, 0.0)))
+    prev, anchor = p0, (0.4, 4.0, 0.0)
+    for k in range(6):
+        y = 4.0 - 0.5 * k - 0.25
+        b = sc.add_body(S.Body(link, pos=(0.4, y, 0.0), vel=(1.5 if k == 5 else 0.0, 0.0, 0.5)))
+        J.append(S.Joint(S.JOINT_POINT, prev, b, anchor_a=anchor))
+        prev, anchor = b, (0.4, y - 0.25, 0.0)
+    # hinge door on a second post, limited to +-1 rad, motor driving it
+    p1 = sc.add_body(S.Body(post, st, pos=(3.0, 2.0, 0.0)))
+    d = sc.add_body(S.Body(door, pos=(3.6, 2.0, 0.0)))
+    J.append(S.Joint(S.JOINT_HINGE, p1, d, anchor_a=(3.1, 2.0, 0.0), axis_a=(0.0, 1.0, 0.0), axis_b=(0.0, 1.0, 0.0),
+                     lower=-1.0, upper=1.0, motor_target=2.0, motor_max=5.0,
+                     flags=S.JOINT_FLAG_LIMITS | S.JOINT_FLAG_MOTOR))
+    # second door: limits only, pushed
+    p2 = sc.add_body(S.Body(post, st, pos=(-3.0, 2.0, 0.0)))
+    d2 = sc.add_body(S.Body(door, pos=(-2.4, 2.0, 0.0), ang=(0.0, 3.0, 0.0)))
+    J.append(S.Joint(S.JOINT_HINGE, p2, d2, anchor_a=(-2.9, 2.0, 0.0), axis_a=(0.0, 1.0, 0.0),
+                     axis_b=(0.0, 1.0, 0.0), lower=-0.5, upper=0.5, flags=S.JOINT_FLAG_LIMITS))
+    # sliders along x from a static post: one limited, one motorised
+    p3 = sc.add_body(S.Body(post, st, pos=(0.0, 2.0, 3.0)))
+    s1 = sc.add_body(S.Body(cube, pos=(0.8, 3.0, 3.0), vel=(2.0, 0.0, 0.0)))
+    J.append(S.Joint(S.JOINT_SLIDER, p3, s1, anchor_a=(0.8, 3.0, 3.0), axis_a=(1.0, 0.0, 0.0), lower=-0.5,
+                     upper=0.6, flags=S.JOINT_FLAG_LIMITS))
+    s2 = sc.add_body(S.Body(cube, pos=(-0.8, 1.5, 3.0)))
+    J.append(S.Joint(S.JOINT_SLIDER, p3, s2, anchor_a=(-0.8, 1.5, 3.0), axis_a=(-1.0, 0.2, 0.0), motor_target=1.0,
+                     motor_max=20.0, flags=S.JOINT_FLAG_MOTOR))
+    # fixed pair and distance pair dropped onto the ground
+    f1 = sc.add_body(S.Body(cube, pos=(5.0, 1.5, 3.0), ang=(0.3, 0.0, 0.2)))
+    f2 = sc.add_body(S.Body(cube, pos=(5.62, 1.6, 3.0)))
+    J.append(S.Joint(S.JOINT_FIXED, f1, f2, anchor_a=(5.31, 1.55, 3.0)))
+    b1 = sc.add_body(S.Body(ball, pos=(-5.0, 2.0, 3.0), vel=(0.0, 0.0, 1.0)))
+    b2 = sc.add_body(S.Body(cap, pos=(-4.0, 2.5, 3.0)))
+    J.append(S.Joint(S.JOINT_DISTANCE, b1, b2, anchor_a=(-5.0, 2.0, 3.0), anchor_b=(-4.0, 2.5, 3.0), distance=1.2))
+    # point joint with local anchors between a cube and the second chain link
+    c3 = sc.add_body(S.Body(cube, pos=(1.3, 3.2, -0.2)))
+    J.append(S.Joint(S.JOINT_POINT, 3, c3, anchor_a=(0.1, 0.0, 0.0), anchor_b=(-0.4, 0.0, 0.0),
+                     flags=S.JOINT_FLAG_LOCAL_ANCHORS))
+    # six-dof: linear x,y fixed, z limited, angular x fixed; linear z motor, angular y motor
+    p4 = sc.add_body(S.Body(post, st, pos=(3.0, 2.0, -3.0)))
+    x6 = sc.add_body(S.Body(cube, pos=(3.0, 3.0, -2.4), ang=(0.5, 1.0, 0.0)))
+    c, s_ = math.cos(0.3), math.sin(0.3)
+    J.append(S.Joint(S.JOINT_SIXDOF, p4, x6, anchor_a=(3.0, 3.0, -2.4), rotation=(0.0, s_, 0.0, c),
+                     axis_modes=(2 << 0) | (2 << 2) | (1 << 4) | (2 << 6), motor_mask=(1 << 2) | (1 << 4),
+                     six_motor=(0.0, 0.0, 0.5, 0.0, 0.0, 3.0, 0.0, 1.5, 0.0, 0.0, 2.0, 0.0)))
+    # a disabled joint (never prepared, solved or islanded)
+    J.append(S.Joint(S.JOINT_POINT, f1, b1, anchor_a=(0.0, 1.0, 3.0), flags=S.JOINT_FLAG_DISABLED))
+    sc.joints = J
+    return sc
 
 
 def _ccd_shots():
