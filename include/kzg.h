@@ -63,6 +63,7 @@ typedef struct {
     uint32_t max_pairs;         /* broad-phase pairs per step */
     uint32_t max_cache_entries; /* manifold cache slots (power of two; entries are never evicted) */
     int device;                 /* CUDA ordinal */
+    uint32_t max_joints;        /* joints (0: none) */
 } kzg_config;
 
 /* Mirrors SolverSettings (reference include/Kizuri/Solver/ContactSolver.h:67-82). */
@@ -180,6 +181,33 @@ kzg_status kzg_upload_shapes(kzg_ctx* ctx, const kzg_shape_desc* shapes, uint32_
                              uint32_t num_faces, const uint32_t* face_indices, uint32_t num_indices);
 /* Appends bodies; *first_slot receives the slot (BodyID index) of the first one. */
 kzg_status kzg_add_bodies(kzg_ctx* ctx, uint32_t n, const kzg_body_soa* bodies, uint32_t* first_slot);
+
+/* ---- joints (Constraints.h:41-277, PhysicsWorld::AddConstraint, PhysicsWorld.cpp:210-212) --- */
+#define KZG_JOINT_POINT 0u    /* PointConstraint */
+#define KZG_JOINT_DISTANCE 1u /* DistanceConstraint */
+#define KZG_JOINT_FIXED 2u    /* FixedConstraint */
+#define KZG_JOINT_HINGE 3u    /* HingeConstraint */
+#define KZG_JOINT_SLIDER 4u   /* SliderConstraint */
+#define KZG_JOINT_SIXDOF 5u   /* SixDOFConstraint */
+#define KZG_JOINT_DISABLED 1u      /* Constraint::SetEnabled(false) */
+#define KZG_JOINT_LIMITS 2u        /* Hinge/SliderConstraint::SetLimits(lower, upper) */
+#define KZG_JOINT_MOTOR 4u         /* Hinge/SliderConstraint::SetMotor(motor_target, motor_max) */
+#define KZG_JOINT_LOCAL_ANCHORS 8u /* PointConstraint(a, b, localAnchorA = anchor_a, localAnchorB = anchor_b) */
+/* One joint as the reference's constructors take it: anchors and axes in world space at the
+ * bodies' poses when kzg_add_joints is called.  anchor_b: DistanceConstraint's second anchor;
+ * axis_b: HingeConstraint's axis on B; rotation (x, y, z, w): SixDOFConstraint's world frame;
+ * axis_modes: 2 bits per axis (SixDOFConstraint::AxisMode; linear x, y, z in bits 0-5, angular in
+ * bits 6-11); motor_mask: bit k = SetLinearMotor(k), bit 3+k = SetAngularMotor(k), with
+ * six_motor = linear targets[3], linear max[3], angular targets[3], angular max[3]. */
+typedef struct {
+    uint32_t type, body_a, body_b, flags;
+    float anchor_a[3], anchor_b[3], axis_a[3], axis_b[3], rotation[4];
+    float distance, lower, upper, motor_target, motor_max;
+    uint32_t axis_modes, motor_mask;
+    float six_motor[12];
+} kzg_joint_desc;
+/* Appends joints (slots of existing bodies); *first_index receives the first one's index. */
+kzg_status kzg_add_joints(kzg_ctx* ctx, uint32_t n, const kzg_joint_desc* joints, uint32_t* first_index);
 
 /* ---- stepping (PhysicsWorld::StepFixed, PhysicsWorld.cpp:245-329) --------------------------- */
 /* nsteps fixed steps with the GPU broad phase (canonical pair order). */

@@ -26,7 +26,8 @@ u32, f32, vp = ctypes.c_uint32, ctypes.c_float, ctypes.c_void_p
 
 class KzgConfig(ctypes.Structure):
     _fields_ = [("max_bodies", u32), ("max_shapes", u32), ("max_hull_vertices", u32), ("max_hull_indices", u32),
-                ("max_pairs", u32), ("max_cache_entries", u32), ("device", ctypes.c_int)]
+                ("max_pairs", u32), ("max_cache_entries", u32), ("device", ctypes.c_int),
+                ("max_joints", u32)]
 
 
 class KzgSolverSettings(ctypes.Structure):
@@ -67,9 +68,16 @@ class KzgStats(ctypes.Structure):
                                    "integrate_ms", "step_ms", "final_residual")]
 
 
+class KzgJointDesc(ctypes.Structure):
+    _fields_ = [("type", u32), ("body_a", u32), ("body_b", u32), ("flags", u32), ("anchor_a", f32 * 3),
+                ("anchor_b", f32 * 3), ("axis_a", f32 * 3), ("axis_b", f32 * 3), ("rotation", f32 * 4),
+                ("distance", f32), ("lower", f32), ("upper", f32), ("motor_target", f32), ("motor_max", f32),
+                ("axis_modes", u32), ("motor_mask", u32), ("six_motor", f32 * 12)]
+
+
 EXPORTS = ["kzg_create", "kzg_destroy", "kzg_last_error", "kzg_set_stream", "kzg_synchronize",
            "kzg_set_world_settings", "kzg_set_solver_settings", "kzg_default_settings", "kzg_upload_shapes",
-           "kzg_add_bodies", "kzg_step", "kzg_step_with_pairs", "kzg_download_state", "kzg_upload_state",
+           "kzg_add_bodies", "kzg_add_joints", "kzg_step", "kzg_step_with_pairs", "kzg_download_state", "kzg_upload_state",
            "kzg_download_transforms", "kzg_upload_forces", "kzg_download_mass", "kzg_state_hash", "kzg_get_stats",
            "kzg_num_pairs", "kzg_download_pairs", "kzg_num_constraints", "kzg_download_constraints",
            "kzg_hull_build", "kzg_mass_properties"]
@@ -107,6 +115,7 @@ def load(build_if_missing: bool = True):
     L.kzg_default_settings.restype = None
     L.kzg_upload_shapes.argtypes = [vp, P(KzgShapeDesc), u32, vp, u32, vp, u32, vp, u32]
     L.kzg_add_bodies.argtypes = [vp, u32, P(KzgBodySoa), P(u32)]
+    L.kzg_add_joints.argtypes = [vp, u32, P(KzgJointDesc), P(u32)]
     L.kzg_step.argtypes = [vp, f32, u32]
     L.kzg_step_with_pairs.argtypes = [vp, vp, u32, f32]
     L.kzg_download_state.argtypes = [vp, vp, u32, u32]

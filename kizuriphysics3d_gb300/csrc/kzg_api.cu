@@ -62,6 +62,15 @@ kzg_status alloc_all(Ctx* ctx) {
     CK(dalloc(&ctx->epa_list, P));
     CK(dalloc(&ctx->ccd_disp, B));
     CK(dalloc(&ctx->ccd_list, B));
+    if (c.max_joints) {
+        CK(cudaMalloc((void**)&ctx->joints, joint_record_bytes() * c.max_joints));
+        CK(dalloc(&ctx->joint_stage, c.max_joints));
+        CK(dalloc(&ctx->jkeys, c.max_joints));
+        CK(dalloc(&ctx->jkeys_sorted, c.max_joints));
+        CK(dalloc(&ctx->jisl, c.max_joints));
+        CK(dalloc(&ctx->jisl_cisl, c.max_joints));
+        CK(dalloc(&ctx->jflag, P + 1));
+    }
     CK(dalloc(&ctx->con_flag, P));
     CK(dalloc(&ctx->con_index, P));
     CK(dalloc(&ctx->con_pair, P));
@@ -135,7 +144,8 @@ void free_all(Ctx* ctx) {
                     b.iiw, b.iil, b.inv_mass, b.shape, b.motion, b.flags, b.layer, b.mask, b.world, b.packed, b.fat_mn, b.fat_mx,
                     ctx->is_large, ctx->large_list, ctx->large_off, ctx->cell_keys, ctx->cell_keys_sorted,
                     ctx->cell_vals, ctx->cell_vals_sorted, ctx->pair_keys, ctx->pair_keys_sorted, ctx->pairs,
-                    ctx->m_count, ctx->m_data, ctx->m_key, ctx->epa_list, ctx->ccd_disp, ctx->ccd_list, ctx->con_flag, ctx->con_index, ctx->con_pair, ctx->con_a,
+                    ctx->m_count, ctx->m_data, ctx->m_key, ctx->epa_list, ctx->ccd_disp, ctx->ccd_list, ctx->joints, ctx->joint_stage, ctx->jkeys,
+                    ctx->jkeys_sorted, ctx->jisl, ctx->jisl_cisl, ctx->jflag, ctx->con_flag, ctx->con_index, ctx->con_pair, ctx->con_a,
                     ctx->con_b, ctx->con_np, ctx->con_bits, ctx->con_fr, ctx->con_key, ctx->r.pA, ctx->r.pB, ctx->r.n,
                     ctx->r.t1, ctx->r.t2, ctx->r.rA, ctx->r.rB, ctx->r.rAr, ctx->r.rBr, ctx->r.laA, ctx->r.laB,
                     ctx->r.mass, ctx->r.imp, ctx->r.bias, ctx->uf, ctx->isl_key, ctx->isl_key_sorted,
@@ -501,6 +511,28 @@ kzg_status kzg_add_bodies(kzg_ctx* k, uint32_t n, const kzg_body_soa* b, uint32_
     return KZG_OK;
 }
 
+kzg_status kzg_add_joints(kzg_ctx* k, uint32_t n, const kzg_joint_desc* j, uint32_t* first_index) {
+    if (check(k) || (!j && n)) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    if (ctx->njoints + n > ctx->cfg.max_joints) { ctx->err = "kzg_config.max_joints exceeded"; return KZG_ERR_CAPACITY; }
+    if (ctx->njoints + n > ctx->cfg.max_pairs) { ctx->err = "more joints than kzg_config.max_pairs"; return KZG_ERR_CAPACITY; }
+    for (uint32_t i = 0; i < n; ++i) {
+        if (j[i].type > KZG_JOINT_SIXDOF || j[i].body_a >= ctx->nbodies || j[i].body_b >= ctx->nbodies ||
+            (j[i].flags & ~(KZG_JOINT_DISABLED | KZG_JOINT_LIMITS | KZG_JOINT_MOTOR | KZG_JOINT_LOCAL_ANCHORS))) {
+            ctx->err = "joint " + std::to_string(i) + ": bad type, body slot or flag";
+            return KZG_ERR_INVALID;
+        }
+    }
+    if (n) {
+        CK(cudaMemcpy(ctx->joint_stage, j, sizeof(kzg_joint_desc) * n, cudaMemcpyHostToDevice));
+        CK(create_joints(*ctx, ctx->njoints, n));
+    }
+    if (first_index) *first_index = ctx->njoints;
+    ctx->njoints += n;
+    ctx->graph_dirty = true;
+    return KZG_OK;
+}
+
 kzg_status kzg_step(kzg_ctx* k, float dt, uint32_t nsteps) {
     if (check(k)) return KZG_ERR_INVALID;
     Ctx* ctx = &k->c;
@@ -752,12 +784,12 @@ kzg_status kzg_download_constraints(kzg_ctx* k, uint32_t* hdr, float* fr, float*
     return KZG_OK;
 }
 
-// ---- device snapshots: body state and the manifold cache, for exact resume ------------------
+// ---- device snapshots: body state, the manifold cache and the joints, for exact resume -------
 namespace {
 constexpr uint32_t kSnapMagic = 0x53475A4Bu;  // 'KZGS'
-constexpr uint32_t kSnapVersion = 2;
+constexpr uint32_t kSnapVersion = 3;
 struct SnapHeader {
-    uint32_t magic, version, nbodies, cache_cap, cache_entries, cache_used, reserved[2];
+    uint32_t magic, version, nbodies, cache_cap, cache_entries, cache_used, njoints, reserved;
 };
 constexpr int kSnapBodyArrays = 10;  // pos, rot, lv, av, plv, pav, force, torque, fat bounds (+ 3 iiw columns)
 constexpr size_t kSnapBodyBytes = sizeof(float4) * (kSnapBodyArrays + 3);
@@ -780,7 +812,8 @@ kzg_status kzg_snapshot_size(kzg_ctx* k, size_t* bytes) {
     CK(cudaMemcpy(keys.data(), ctx->c_key, sizeof(unsigned long long) * H, cudaMemcpyDeviceToHost));
     size_t used = 0;
     for (unsigned long long key : keys) used += key != 0ull;
-    *bytes = sizeof(SnapHeader) + kSnapBodyBytes * ctx->nbodies + kSnapCacheBytes * used;
+    *bytes = sizeof(SnapHeader) + kSnapBodyBytes * ctx->nbodies + kSnapCacheBytes * used +
+             joint_record_bytes() * ctx->njoints;
     return KZG_OK;
 }
 
@@ -799,13 +832,15 @@ kzg_status kzg_snapshot_save(kzg_ctx* k, void* out, size_t capacity) {
     CK(cudaMemcpy(imp.data(), ctx->c_imp, sizeof(float4) * 4 * H, cudaMemcpyDeviceToHost));
     size_t used = 0;
     for (unsigned long long key : keys) used += key != 0ull;
-    const size_t need = sizeof(SnapHeader) + kSnapBodyBytes * nb + kSnapCacheBytes * used;
+    const size_t JB = joint_record_bytes() * ctx->njoints;
+    const size_t need = sizeof(SnapHeader) + kSnapBodyBytes * nb + kSnapCacheBytes * used + JB;
     if (capacity < need) {
         ctx->err = "kzg_snapshot_save: buffer smaller than kzg_snapshot_size";
         return KZG_ERR_CAPACITY;
     }
     uint8_t* p = static_cast<uint8_t*>(out);
-    SnapHeader h{kSnapMagic, kSnapVersion, (uint32_t)nb, (uint32_t)H, ctx->hcnt->cache_entries, (uint32_t)used, {0, 0}};
+    SnapHeader h{kSnapMagic, kSnapVersion, (uint32_t)nb, (uint32_t)H, ctx->hcnt->cache_entries, (uint32_t)used,
+                 ctx->njoints, 0u};
     CK(cudaMemcpy(&h.cache_entries, &ctx->dcnt->cache_entries, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     std::memcpy(p, &h, sizeof(h));
     p += sizeof(h);
@@ -826,6 +861,7 @@ kzg_status kzg_snapshot_save(kzg_ctx* k, void* out, size_t capacity) {
         std::memcpy(p, &pos[4 * slot], 4 * sizeof(float4)); p += 4 * sizeof(float4);
         std::memcpy(p, &imp[4 * slot], 4 * sizeof(float4)); p += 4 * sizeof(float4);
     }
+    if (JB) CK(cudaMemcpy(p, ctx->joints, JB, cudaMemcpyDeviceToHost));
     return KZG_OK;
 }
 
@@ -838,9 +874,11 @@ kzg_status kzg_snapshot_load(kzg_ctx* k, const void* in, size_t size) {
     SnapHeader h;
     std::memcpy(&h, in, sizeof(h));
     const size_t H = ctx->cfg.max_cache_entries, nb = ctx->nbodies;
+    const size_t JB = joint_record_bytes() * ctx->njoints;
     if (h.magic != kSnapMagic || h.version != kSnapVersion || h.nbodies != nb || h.cache_cap != H ||
-        size != sizeof(SnapHeader) + kSnapBodyBytes * nb + kSnapCacheBytes * (size_t)h.cache_used) {
-        ctx->err = "kzg_snapshot_load: snapshot does not match this context (bodies, cache capacity or size)";
+        h.njoints != ctx->njoints ||
+        size != sizeof(SnapHeader) + kSnapBodyBytes * nb + kSnapCacheBytes * (size_t)h.cache_used + JB) {
+        ctx->err = "kzg_snapshot_load: snapshot does not match this context (bodies, joints, cache capacity or size)";
         return KZG_ERR_INVALID;
     }
     CK(cudaStreamSynchronize(ctx->stream));
@@ -873,6 +911,7 @@ kzg_status kzg_snapshot_load(kzg_ctx* k, const void* in, size_t size) {
     CK(cudaMemcpy(ctx->c_pos, pos.data(), sizeof(float4) * 4 * H, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->c_imp, imp.data(), sizeof(float4) * 4 * H, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(&ctx->dcnt->cache_entries, &h.cache_entries, sizeof(uint32_t), cudaMemcpyHostToDevice));
+    if (JB) CK(cudaMemcpy(ctx->joints, p, JB, cudaMemcpyHostToDevice));
     return KZG_OK;
 }
 

@@ -60,6 +60,7 @@ struct Counters {  // device-side counters, copied back after each stage that si
     uint32_t pt_iters;   // sum of batched points x iterations
     uint32_t res_bits;   // largest final residual (float bits, >= 0)
     uint32_t nmiss;      // contact points without a cached warm start (learned warm start / logging)
+    uint32_t njisl;      // islands holding joints
     uint32_t cache_entries;  // persists across steps
     uint32_t frame;          // step counter, advanced on the device by k_begin_step
 };
@@ -86,6 +87,8 @@ struct MlpState {
     float* out = nullptr;
     uint32_t out_cap = 0;
 };
+
+struct JointDev;  // kzg_joint.cuh
 
 struct Ctx {
     kzg_config cfg{};
@@ -130,6 +133,14 @@ struct Ctx {
     float4* ccd_disp = nullptr;    // continuous collision: each LinearCast body's step displacement
     uint32_t* ccd_list = nullptr;  // slots of the LinearCast bodies, ascending
     uint32_t nccd = 0;
+    // joints (kzg_joint.cuh): records, creation staging, per-step island grouping
+    JointDev* joints = nullptr;
+    kzg_joint_desc* joint_stage = nullptr;
+    unsigned long long *jkeys = nullptr, *jkeys_sorted = nullptr;  // island root << 32 | joint index
+    uint2* jisl = nullptr;           // per joint island: range in jkeys_sorted
+    uint32_t* jisl_cisl = nullptr;   // per joint island: its contact island, or ~0
+    uint32_t* jflag = nullptr;       // per contact island: 1 when a joint island owns it
+    uint32_t njoints = 0;
 
     // constraints
     uint32_t* con_flag = nullptr;    // per pair: 1 if it makes a constraint

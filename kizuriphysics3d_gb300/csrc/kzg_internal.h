@@ -19,6 +19,8 @@ cudaError_t configure_kernels();  // per-device kernel attributes (large dynamic
 size_t pack_elements(uint32_t points, uint32_t* cap);
 size_t cluster_id_words(uint32_t max_cons);  // local-id scratch of the cluster solve
 cudaError_t init_fat_bounds(Ctx& ctx, uint32_t first, uint32_t n);  // broad-phase fat bounds of new bodies
+cudaError_t create_joints(Ctx& ctx, uint32_t first, uint32_t n);     // joint records from ctx.joint_stage
+size_t joint_record_bytes();
 kzg_status step_canonical(Ctx& ctx, float dt, uint32_t nsteps);
 kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t num_pairs, float dt);
 kzg_status hash_state(Ctx& ctx, uint64_t* out);

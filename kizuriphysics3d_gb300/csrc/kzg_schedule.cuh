@@ -51,6 +51,7 @@ struct SchedBufs {
     uint32_t *small_list, *large_list;
     uint32_t small_cons;   // islands with at most this many constraints: warp schedule (<= kSchedSmallCons)
     uint32_t warp_bodies;  // islands with at most this many dynamic bodies: warp solve (<= kWarpBodies)
+    const uint32_t* jflag; // per island: 1 when joints share it (solved with them by k_solve_big), or null
 };
 
 struct SchedShared {  // per island scratch living in shared memory
@@ -992,8 +993,12 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
         S.meta[4 * isl + 1] = nv;
         S.meta[4 * isl + 2] = nb;
         S.meta[4 * isl + 3] = nloc;
-        if (nloc <= S.warp_bodies) S.small_list[atomicAdd(&cnt->nsmall, 1u)] = isl;
-        else S.large_list[atomicAdd(&cnt->nlarge, 1u)] = isl;
+        if (S.jflag && S.jflag[isl]) {
+        } else if (nloc <= S.warp_bodies) {
+            S.small_list[atomicAdd(&cnt->nsmall, 1u)] = isl;
+        } else {
+            S.large_list[atomicAdd(&cnt->nlarge, 1u)] = isl;
+        }
         atomicAdd(&cnt->batches, nbt);
         atomicMax(&cnt->max_vlev, nv);
         atomicMax(&cnt->max_blev, nb);

@@ -14,6 +14,7 @@
 #include <cooperative_groups.h>
 
 #include "kzg_schedule.cuh"
+#include "kzg_joint.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -42,6 +43,10 @@ struct SolveBufs {
     uint32_t* cl_ids;  // cluster islands: per cluster 2 x kClusterBodies words (new local id of each
                        // local body; body of each new id), then the permuted local ids of A and B
                        // per constraint (2 x max_pairs)
+    JointDev* joints;                  // null without joints
+    const unsigned long long* jkeys;   // joints sorted by island root, then joint index
+    const uint2* jisl;                 // per joint island: its range of jkeys
+    const uint32_t* jisl_cisl;         // per joint island: its contact island, or kNone
 };
 
 // Velocity storage of one island: staged in shared memory (local index) or read/written in place
@@ -423,8 +428,13 @@ constexpr uint32_t kBigOffs = 8192;  // velocity level offsets staged in shared 
 // Warm start + velocity sweeps of a big island.  Each velocity item is one 16-byte record
 // {row, A, B, dynamic flags}, and every thread loads its record of the next level before it solves
 // the current one, so after a barrier only the row and body loads stand between it and its math.
+struct NoHook {
+    __device__ void operator()() const {}
+};
+// after_warm runs on every thread between the warm-start sweep and the velocity sweeps.
+template <typename AfterWarm = NoHook>
 __device__ void solve_velocity_big(const SolveBufs& S, uint32_t isl, uint32_t* soff, unsigned long long* red,
-                                   Counters* cnt) {
+                                   Counters* cnt, AfterWarm after_warm = AfterWarm{}) {
     const uint32_t tid = threadIdx.x, nthreads = blockDim.x;
     const uint32_t base = 4u * S.isl_start[isl], loff = base + isl;
     const uint32_t nw = S.meta[4 * isl], nv = S.meta[4 * isl + 1];
@@ -445,6 +455,7 @@ __device__ void solve_velocity_big(const SolveBufs& S, uint32_t isl, uint32_t* s
         for (uint32_t k = S.wl_off[loff + l] + tid; k < e; k += nthreads) warm_point(S, V, S.wl_list[base + k]);
         sync();
     }
+    after_warm();
     auto off = [&](uint32_t l) -> uint32_t { return staged ? soff[l] : S.vl_off[loff + l]; };
     auto item = [&](const uint4& r) -> float2 {
         return velocity_point_ab(S, V, r.x, r.y, r.z, (r.w & 1u) ? 0u : kNone, (r.w & 2u) ? 0u : kNone);
@@ -492,6 +503,43 @@ __device__ void solve_velocity_big(const SolveBufs& S, uint32_t isl, uint32_t* s
 
 __device__ __forceinline__ bool cluster_island(const SolveBufs& S, uint32_t isl, uint32_t smem_bodies);
 
+// An island holding joints, in the reference's order (PhysicsWorld.cpp:666-743): contact warm start,
+// joint warm starts, contact velocity sweeps, the joints' velocity iterations (the configured count;
+// the residual rule stops the contact sweeps only), contact bias sweeps.  The contact parts run
+// level-parallel on the CTA (as in k_solve_big), the joint parts on thread 0 in joint order.
+// Called functions, so that the register allocation of k_solve_big's own contact sweeps stays as
+// it is without joints.
+static __device__ __noinline__ void joints_warm(const DeviceBodies b, JointDev* J, const unsigned long long* jk,
+                                                uint2 r) {
+    const JBodies B{b};
+    for (uint32_t s = r.x; s < r.y; ++s) joint_warm(B, J[(uint32_t)jk[s]]);
+}
+static __device__ __noinline__ void joints_velocity(const DeviceBodies b, JointDev* J, const unsigned long long* jk,
+                                                    uint2 r, uint32_t iters) {
+    const JBodies B{b};
+    for (uint32_t it = 0; it < iters; ++it)
+        for (uint32_t s = r.x; s < r.y; ++s) joint_velocity(B, J[(uint32_t)jk[s]]);
+}
+
+__device__ __forceinline__ void solve_joint_island(const SolveBufs& S, uint32_t k, uint32_t* soff,
+                                                   unsigned long long* red, Counters* cnt) {
+    const uint2 r = S.jisl[k];
+    const uint32_t cisl = S.jisl_cisl[k];
+    auto warm = [&]() {
+        if (threadIdx.x == 0) joints_warm(S.b, S.joints, S.jkeys, r);
+        __syncthreads();
+    };
+    if (cisl != kNone) solve_velocity_big(S, cisl, soff, red, cnt, warm);
+    else warm();
+    if (threadIdx.x == 0) joints_velocity(S.b, S.joints, S.jkeys, r, S.vel_iters);
+    __syncthreads();
+    if (cisl != kNone) {
+        const VelView P{S.b.plv, S.b.pav, S.b.lv, S.b.av, false};
+        solve_bias(S, cisl, P, threadIdx.x, blockDim.x, CtaSync{red});
+    }
+    __syncthreads();
+}
+
 // Large islands that neither one CTA's shared memory nor (when S.pk_cap > 0) a cluster takes.
 __global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
     __shared__ unsigned long long red[6];
@@ -505,6 +553,14 @@ __global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, Count
         solve_bias(S, isl, P, threadIdx.x, blockDim.x, CtaSync{red});
         __syncthreads();
     }
+}
+
+// Islands that hold joints (launched only when the world has joints): one CTA each.
+__global__ void __launch_bounds__(kBigThreads, 1) k_solve_joint(SolveBufs S, Counters* cnt) {
+    __shared__ unsigned long long red[6];
+    __shared__ uint32_t soff[kBigOffs + 1];
+    const uint32_t nj = cnt->njisl;
+    for (uint32_t idx = blockIdx.x; idx < nj; idx += gridDim.x) solve_joint_island(S, idx, soff, red, cnt);
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -544,7 +544,100 @@ __global__ void k_island_starts(Counters* cnt, const uint32_t* __restrict__ head
 
 #include "kzg_solver.cuh"
 
+
 namespace kzg {
+
+// ---------------------------------------------------------------------------------------------
+// Joints: creation, Prepare, island membership and position correction (the velocity part runs in
+// k_solve_big, kzg_solver.cuh)
+// ---------------------------------------------------------------------------------------------
+__global__ void k_joint_create(DeviceBodies b, JointDev* J, const kzg_joint_desc* __restrict__ d, uint32_t first,
+                               uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) joint_create(JBodies{b}, J[first + i], d[i]);
+}
+
+// Constraint::Prepare of every enabled joint (PhysicsWorld.cpp:547-548), after the contacts'.
+__global__ void k_joint_prepare(DeviceBodies b, JointDev* J, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && !(J[i].flags & kJointDisabled)) joint_prepare(JBodies{b}, J[i]);
+}
+
+// Joints between two dynamic bodies join their islands (PhysicsWorld.cpp:625-633).
+__global__ void k_joint_union(DeviceBodies b, const JointDev* __restrict__ J, uint32_t n, uint32_t* uf) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || (J[i].flags & kJointDisabled)) return;
+    uint32_t a = J[i].a, bb = J[i].b;
+    if (b.motion[a] != KZG_MOTION_DYNAMIC || b.motion[bb] != KZG_MOTION_DYNAMIC) return;
+    for (;;) {
+        a = uf_find(uf, a);
+        bb = uf_find(uf, bb);
+        if (a == bb) return;
+        if (a > bb) { uint32_t t = a; a = bb; bb = t; }
+        uint32_t old = atomicCAS(&uf[bb], bb, a);
+        if (old == bb) return;
+        bb = old;
+    }
+}
+
+// Island of each joint: islandOf(A), else islandOf(B) (PhysicsWorld.cpp:656-661), as the root of its
+// dynamic body, keyed root << 32 | joint index so that a sort groups islands in joint order; a
+// joint with no dynamic body or disabled gets ~0 (sorted last, never solved).
+__global__ void k_joint_keys(DeviceBodies b, const JointDev* __restrict__ J, uint32_t n, uint32_t* uf,
+                             unsigned long long* keys) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned long long key = ~0ull;
+    if (!(J[i].flags & kJointDisabled)) {
+        const uint32_t a = J[i].a, bb = J[i].b;
+        const uint32_t d = b.motion[a] == KZG_MOTION_DYNAMIC ? a : (b.motion[bb] == KZG_MOTION_DYNAMIC ? bb : kNone);
+        if (d != kNone) key = ((unsigned long long)uf_find(uf, d) << 32) | i;
+    }
+    keys[i] = key;
+}
+
+// One joint island per run of equal roots; its contact island (contact islands are sorted by root)
+// is flagged so that the schedule hands it to k_solve_big's joint pass instead of the other solvers.
+__global__ void k_joint_islands(const unsigned long long* __restrict__ sk, uint32_t n, Counters* cnt,
+                                const uint32_t* __restrict__ isl_key, const uint32_t* __restrict__ isl_start,
+                                uint2* jisl, uint32_t* jisl_cisl, uint32_t* jflag) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || sk[s] == ~0ull) return;
+    const uint32_t root = (uint32_t)(sk[s] >> 32);
+    if (s > 0 && (uint32_t)(sk[s - 1] >> 32) == root) return;
+    uint32_t e = s + 1;
+    while (e < n && sk[e] != ~0ull && (uint32_t)(sk[e] >> 32) == root) ++e;
+    const uint32_t k = atomicAdd(&cnt->njisl, 1u);
+    jisl[k] = make_uint2(s, e);
+    const uint32_t ni = cnt->nislands;
+    uint32_t lo = 0, hi = ni;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (isl_key[isl_start[mid]] < root) lo = mid + 1;
+        else hi = mid;
+    }
+    const uint32_t c = (lo < ni && isl_key[isl_start[lo]] == root) ? lo : kNone;
+    jisl_cisl[k] = c;
+    if (c != kNone) jflag[c] = 1u;
+}
+
+// SolveIslandPositions (PhysicsWorld.cpp:745-752): each island's joints, position_iterations times.
+__global__ void k_joint_positions(DeviceBodies b, JointDev* J, const unsigned long long* __restrict__ sk,
+                                  const uint2* __restrict__ jisl, const Counters* cnt, uint32_t iters) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= cnt->njisl) return;
+    const uint2 r = jisl[k];
+    const JBodies B{b};
+    for (uint32_t it = 0; it < iters; ++it)
+        for (uint32_t s = r.x; s < r.y; ++s) joint_position(B, J[(uint32_t)sk[s]]);
+}
+
+cudaError_t create_joints(Ctx& ctx, uint32_t first, uint32_t n) {
+    k_joint_create<<<blocks_for(n), kThreads, 0, ctx.stream>>>(ctx.b, ctx.joints, ctx.joint_stage, first, n);
+    cudaError_t e = cudaGetLastError();
+    return e != cudaSuccess ? e : cudaStreamSynchronize(ctx.stream);
+}
+size_t joint_record_bytes() { return sizeof(JointDev); }
 
 // ---------------------------------------------------------------------------------------------
 // cache store (:568-581) and position integration (:276-290, 785-802, 854-861)
@@ -833,8 +926,11 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     PrepParams pp{dt, ctx.ss.baumgarte, ctx.ss.penetration_slop, ctx.ss.restitution_threshold, ctx.ss.max_bias_velocity};
     k_prepare<<<blocks_for(R), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_np, ctx.r, pp);
     ctx.launches += mlp_after_prepare(ctx, dt);
+    const uint32_t nj = ctx.njoints;
+    if (nj) k_joint_prepare<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, nj);
     k_uf_init<<<blocks_for(nb), kThreads, 0, st>>>(ctx.uf, nb);
     k_uf_union<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf);
+    if (nj) k_joint_union<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, nj, ctx.uf);
     const int kbits = bits_for(nb);
     k_island_keys<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf,
                                                       ctx.isl_key, ctx.isl_con_in, P, (1u << kbits) - 1u);
@@ -845,13 +941,22 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     tb = ctx.cub_tmp_bytes;
     KZG_CK(cub::DeviceScan::ExclusiveSum(ctx.cub_tmp, tb, ctx.isl_head, ctx.isl_pts, (int)P, st));
     k_island_starts<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_head, ctx.isl_pts, ctx.isl_start);
+    if (nj) {
+        k_joint_keys<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, nj, ctx.uf, ctx.jkeys);
+        tb = ctx.cub_tmp_bytes;
+        KZG_CK(cub::DeviceRadixSort::SortKeys(ctx.cub_tmp, tb, ctx.jkeys, ctx.jkeys_sorted, (int)nj, 0, 64, st));
+        KZG_CK(cudaMemsetAsync(ctx.jflag, 0, sizeof(uint32_t) * (P + 1), st));
+        k_joint_islands<<<blocks_for(nj), kThreads, 0, st>>>(ctx.jkeys_sorted, nj, ctx.dcnt, ctx.isl_key_sorted,
+                                                             ctx.isl_start, ctx.jisl, ctx.jisl_cisl, ctx.jflag);
+        ctx.launches += 8;  // prepare, union, keys, sort (4 passes), islands
+    }
     SchedBufs SB{ctx.isl_start, ctx.isl_con, ctx.con_a, ctx.con_b, ctx.con_np, ctx.con_bits, ctx.r.bias,
                  ctx.b.inv_mass, ctx.is_large, ctx.brec, ctx.body_stamp, ctx.body_loc, ctx.isl_bodies,
                  ctx.last_g, 2u * ctx.cfg.max_pairs, ctx.con_la, ctx.con_lb, ctx.first_w, ctx.first_b,
                  ctx.ids_tmp, ctx.lvl_tmp, ctx.lvl_count, ctx.wl_list, ctx.vl_list, ctx.bl_list, ctx.wl_off,
                  ctx.vl_off, ctx.bl_off, ctx.isl_meta, ctx.isl_small, ctx.isl_large,
                  std::min(ctx.tune.small_island_constraints, kSchedSmallCons),
-                 std::min(ctx.tune.warp_island_bodies, kWarpBodies)};
+                 std::min(ctx.tune.warp_island_bodies, kWarpBodies), nj ? ctx.jflag : nullptr};
     k_schedule_warp<<<152u * 16u, 128, 0, st>>>(SB, ctx.dcnt);
     k_schedule_cta<<<152u * 2u, 256, 3 * kSchedCtaBodies * sizeof(uint32_t), st>>>(SB, ctx.dcnt);
     ctx.launches += 17;  // prepare, union-find (3), island sort (4 CUB passes), heads, scan (2), starts, schedule (2)
@@ -861,7 +966,8 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
                  ctx.isl_small, ctx.isl_large, ctx.r, ctx.b, ctx.ss.velocity_iterations,
                  ctx.ss.position_iterations, ctx.ss.warm_start_factor, ctx.ss.use_velocity_bias,
                  ctx.ss.residual_tolerance, ctx.ss.max_velocity_iterations, ctx.brec, ctx.pk,
-                 g_cluster_ok ? ctx.pk_cap : 0u, ctx.isl_con, ctx.cfg.max_pairs, ctx.cl_ids};
+                 g_cluster_ok ? ctx.pk_cap : 0u, ctx.isl_con, ctx.cfg.max_pairs, ctx.cl_ids,
+                 nj ? ctx.joints : nullptr, ctx.jkeys_sorted, ctx.jisl, ctx.jisl_cisl};
     k_solve_warp<<<152u * 16u, kWarpsPerBlock * 32, kWarpsPerBlock * 2 * kWarpBodies * sizeof(float4), st>>>(SV, ctx.dcnt);
     k_solve_cta<<<152u * 2u, kCtaThreads, 2 * kCtaBodiesMax * sizeof(float4), st>>>(SV, ctx.dcnt, kCtaBodiesMax);
     if (g_cluster_ok) {
@@ -871,6 +977,10 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     }
     k_solve_big<<<152u, kBigThreads, 0, st>>>(SV, ctx.dcnt, kCtaBodiesMax);
     ctx.launches += 3;
+    if (nj) {
+        k_solve_joint<<<152u, kBigThreads, 0, st>>>(SV, ctx.dcnt);
+        ++ctx.launches;
+    }
     ctx.launches += mlp_after_solve(ctx, dt);
     KZG_CK(mark(ctx, 5));
     k_cache_store<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_key, ctx.con_np, ctx.r, ctx.c_key, ctx.c_np,
@@ -885,6 +995,11 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     k_integrate_pos<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, dt, ctx.ss.use_velocity_bias,
                                                          ccd ? ctx.ccd_disp : nullptr);
     ctx.launches += 2;
+    if (nj) {
+        k_joint_positions<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, ctx.jkeys_sorted, ctx.jisl,
+                                                               ctx.dcnt, ctx.ss.position_iterations);
+        ++ctx.launches;
+    }
     KZG_CK(mark(ctx, 6));
     KZG_CK(cudaGetLastError());
     return KZG_OK;

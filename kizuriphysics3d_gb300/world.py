@@ -117,6 +117,7 @@ class World:
         cache = int(max_cache_entries or 1 << max(12, int(np.ceil(np.log2(max(64 * n, 4096))))))
         cfg.max_cache_entries = cache
         cfg.device = device
+        cfg.max_joints = len(getattr(scene, "joints", []))
         h = ctypes.c_void_p()
         capi.check(L.kzg_create(ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h
@@ -169,7 +170,29 @@ class World:
         soa.world_id = col("world", world_ids if world_ids is not None else np.zeros(n), np.uint32)
         first = ctypes.c_uint32()
         self._check(L.kzg_add_bodies(h, n, ctypes.byref(soa), ctypes.byref(first)))
+        if getattr(scene, "joints", None):
+            self.add_joints(scene.joints)
         self.dt = float(np.float32(scene.dt))
+
+    def add_joints(self, joints) -> int:
+        """Create joints (scenes.Joint records) at the bodies' current poses (PhysicsWorld::AddConstraint);
+        returns the first one's index."""
+        arr = (capi.KzgJointDesc * len(joints))()
+        for d, j in zip(arr, joints):
+            d.type, d.body_a, d.body_b, d.flags = j.type, j.body_a, j.body_b, j.flags
+            for k in range(3):
+                d.anchor_a[k], d.anchor_b[k] = j.anchor_a[k], j.anchor_b[k]
+                d.axis_a[k], d.axis_b[k] = j.axis_a[k], j.axis_b[k]
+            for k in range(4):
+                d.rotation[k] = j.rotation[k]
+            d.distance, d.lower, d.upper, d.motor_target, d.motor_max = (j.distance, j.lower, j.upper,
+                                                                         j.motor_target, j.motor_max)
+            d.axis_modes, d.motor_mask = j.axis_modes, j.motor_mask
+            for k in range(12):
+                d.six_motor[k] = j.six_motor[k]
+        first = ctypes.c_uint32()
+        self._check(capi.load().kzg_add_joints(self._h, len(joints), arr, ctypes.byref(first)))
+        return first.value
 
     # -- settings ----------------------------------------------------------------------------
     def set_solver(self, **fields):

@@ -43,6 +43,9 @@ void kzo_set_schedule_stats(kzo_world* w, int enabled);
  * sum|dImpulse| / sum|impulse| over its batched points (2^-20 N s fixed-point sums), is <= tol,
  * after at most cap iterations; tol = 0 restores the fixed count. */
 void kzo_set_residual(kzo_world* w, float tol, uint32_t cap);
+/* Joint trigonometry: 0 (default) the C library's float sinf/cosf/acosf/atan2f, as the reference
+ * calls them; 1 the double-precision functions rounded to float, as the GPU evaluates them. */
+void kzo_set_trig_mode(kzo_world* w, int mode);
 
 int kzo_step(kzo_world* w, float dt);
 

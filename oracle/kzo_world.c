@@ -129,6 +129,7 @@ struct kzo_world {
     joint_t* joints;
     uint32_t njoints;
     uint32_t *isl_joff, *isl_joint; /* nislands+1 offsets, joint indices in joint order */
+    int trig_mode;                  /* kzo_set_trig_mode */
     /* stats */
     uint32_t st_points, st_batches, st_max_vl, st_max_bl, st_max_isl_pts, st_sum_vl, st_max_open;
     uint32_t st_max_iters, st_pt_iters;
@@ -745,21 +746,27 @@ static void apply_angular(kzo_world* w, int a, int b, v3 ang) { /* :17-20 */
     w->av[a] = vadd(w->av[a], mmulv(&w->iiw[a], ang));
     w->av[b] = vsub(w->av[b], mmulv(&w->iiw[b], ang));
 }
-static qt rotate_by(qt q, v3 dw) { /* IntegrateRotation(q, dw) (:54-59) with Quat::AxisAngle (Math.cpp:78-83) */
+static float j_sin(const kzo_world* w, float x) { return w->trig_mode ? (float)sin((double)x) : sinf(x); }
+static float j_cos(const kzo_world* w, float x) { return w->trig_mode ? (float)cos((double)x) : cosf(x); }
+static float j_acos(const kzo_world* w, float x) { return w->trig_mode ? (float)acos((double)x) : acosf(x); }
+static float j_atan2(const kzo_world* w, float y, float x) {
+    return w->trig_mode ? (float)atan2((double)y, (double)x) : atan2f(y, x);
+}
+static qt rotate_by(const kzo_world* w, qt q, v3 dw) { /* IntegrateRotation(q, dw) (:54-59) with Quat::AxisAngle (Math.cpp:78-83) */
     float a2 = vlen2(dw);
     if (a2 < 1.0e-12f) return q;
     float a = sqrtf(a2);
     v3 ax = vnormalized(vdiv(dw, a));
     float half = a * 0.5f;
-    float s = sinf(half);
-    qt r = Q(ax.x * s, ax.y * s, ax.z * s, cosf(half));
+    float s = j_sin(w, half);
+    qt r = Q(ax.x * s, ax.y * s, ax.z * s, j_cos(w, half));
     return qnormalized(qmul(r, q));
 }
 static void apply_positional(kzo_world* w, int a, int b, v3 lin, v3 ang) { /* :62-71 */
     w->pos[a] = vadd(w->pos[a], vmul(lin, w->inv_mass[a]));
-    w->rot[a] = rotate_by(w->rot[a], mmulv(&w->iiw[a], ang));
+    w->rot[a] = rotate_by(w, w->rot[a], mmulv(&w->iiw[a], ang));
     w->pos[b] = vsub(w->pos[b], vmul(lin, w->inv_mass[b]));
-    w->rot[b] = rotate_by(w->rot[b], vneg(mmulv(&w->iiw[b], ang)));
+    w->rot[b] = rotate_by(w, w->rot[b], vneg(mmulv(&w->iiw[b], ang)));
 }
 static v3 rel_vel(const kzo_world* w, const joint_t* j) {
     return vsub(vadd(w->lv[j->a], vcross(w->av[j->a], j->r0)), vadd(w->lv[j->b], vcross(w->av[j->b], j->r1)));
@@ -767,7 +774,7 @@ static v3 rel_vel(const kzo_world* w, const joint_t* j) {
 static float hinge_angle(const kzo_world* w, const joint_t* j) { /* HingeConstraint::GetAngle (:361-368) */
     v3 axis = qrotate(w->rot[j->a], j->lax);
     v3 pa = qrotate(w->rot[j->a], j->lpa[0]), pb = qrotate(w->rot[j->b], j->lpb[0]);
-    return atan2f(vdot(axis, vcross(pa, pb)), vdot(pa, pb));
+    return j_atan2(w, vdot(axis, vcross(pa, pb)), vdot(pa, pb));
 }
 
 /* Constructors: world anchors and axes at the bodies' current poses. */
@@ -1076,7 +1083,7 @@ static void joint_position(kzo_world* w, joint_t* j) {
             if (diff.w < 0.0f) diff = Q(-diff.x, -diff.y, -diff.z, -diff.w);
             float s = sqrtf(fmax_r(0.0f, 1.0f - diff.w * diff.w));
             v3 axis = s >= KZO_EPS ? vdiv(V(diff.x, diff.y, diff.z), s) : V(1.0f, 0.0f, 0.0f);
-            float angle = 2.0f * acosf(fclamp_r(diff.w, -1.0f, 1.0f));
+            float angle = 2.0f * j_acos(w, fclamp_r(diff.w, -1.0f, 1.0f));
             if (fabs_r(angle) > 1.0e-4f) {
                 v3 ae = vmul(axis, angle);
                 m3 K = m_inverse(m_add(w->iiw[a], w->iiw[b]));
@@ -1711,6 +1718,8 @@ kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* res
     w->cache = (cache_t*)calloc(w->cache_cap, sizeof(cache_t));
     return w;
 }
+
+void kzo_set_trig_mode(kzo_world* w, int mode) { w->trig_mode = mode; }
 
 void kzo_destroy(kzo_world* w) {
     if (!w) return;

@@ -43,6 +43,7 @@ def lib():
         L.kzo_set_pair_mode.argtypes = [vp, ctypes.c_int]
         L.kzo_set_schedule_stats.argtypes = [vp, ctypes.c_int]
         L.kzo_set_residual.argtypes = [vp, f32, u32]
+        L.kzo_set_trig_mode.argtypes = [vp, ctypes.c_int]
         L.kzo_set_external_pairs.argtypes = [vp, vp, u32]
         L.kzo_step.argtypes = [vp, f32]
         L.kzo_num_bodies.restype = u32
@@ -100,6 +101,11 @@ class OracleWorld:
 
     def set_schedule_stats(self, on: bool):
         lib().kzo_set_schedule_stats(self._w, int(on))
+
+    def set_trig_mode(self, mode: int):
+        """0: the C library's float trigonometry (the reference's); 1: double precision rounded to
+        float (the GPU's joint kernels)."""
+        lib().kzo_set_trig_mode(self._w, int(mode))
 
     def set_residual(self, tol: float, cap: int = 64):
         lib().kzo_set_residual(self._w, np.float32(tol), cap)
