@@ -66,6 +66,18 @@ def make_workload(name: str):
                         "pyramids, odd worlds convex piles with xz extent scaled by sqrt(N/20000), each with its own "
                         "plane; 10 velocity + 2 position iterations, dt 1/60; one context, steps replayed from a "
                         "captured CUDA graph, launch shapes autotuned", "bodies": len(sc.bodies), "worlds": 4096}
+    if name == "chains":
+        sc = scenes.chains(40, 40, 10)
+        return sc, 0, {
+            "workload": "joint field: 1600 chains x 10 boxes on static hooks (point joints, every third a limited "
+                        "hinge), seed 5 pushes, 10 velocity + 2 position iterations, dt 1/60",
+            "bodies": len(sc.bodies), "joints": len(sc.joints)}
+    if name == "projectiles":
+        sc = scenes.projectiles(2000, 4000)
+        return sc, 0, {
+            "workload": "continuous collision: 2000 LinearCast spheres/boxes at 40-80 m/s, 8 thin static walls, "
+                        "4000 resting boxes, seed 9, 10 velocity + 2 position iterations, dt 1/60",
+            "bodies": len(sc.bodies), "linear_cast": 2000}
     raise SystemExit(f"unknown workload {name}")
 
 

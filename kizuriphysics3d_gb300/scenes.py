@@ -304,6 +304,64 @@ def stacks(nx: int = 20, nz: int = 20, height: int = 500, pitch: float = 2.0, se
     return sc
 
 
+def chains(nx: int = 40, nz: int = 40, links: int = 10, pitch: float = 1.5, seed: int = 5,
+           vel_iters: int = 10, pos_iters: int = 2) -> Scene:
+    """A joint workload: nx*nz static hooks 6 m up, each holding a chain of ``links`` boxes
+    (0.2 x 0.5 x 0.2 m) joined by point joints, every third joint a hinge about z with +-0.8 rad
+    limits; the chains start straight down with a random push, swing, and hit their neighbours
+    and the ground plane."""
+    sc = Scene(name=f"chains{nx}x{nz}x{links}")
+    _timed_settings(sc, vel_iters, pos_iters)
+    _ground(sc, 0.6)
+    hook = sc.add_shape(Shape(SHAPE_BOX, [0.1, 0.1, 0.1, 0.0]))
+    link = sc.add_shape(Shape(SHAPE_BOX, [0.1, 0.25, 0.1, 0.0]))
+    rng = np.random.RandomState(seed)
+    push = rng.uniform(-2.0, 2.0, (nx * nz, 2))
+    top = 6.0
+    for ix in range(nx):
+        for iz in range(nz):
+            c = ix * nz + iz
+            x = f32((ix - (nx - 1) * 0.5) * pitch)
+            z = f32((iz - (nz - 1) * 0.5) * pitch)
+            prev = sc.add_body(Body(hook, MOTION_STATIC, pos=(x, f32(top + 0.1), z)))
+            anchor = (x, f32(top), z)
+            for k in range(links):
+                y = f32(top - 0.5 * k - 0.25)
+                b = sc.add_body(Body(link, pos=(x, y, z), vel=(f32(push[c, 0] * (k + 1) / links), 0.0,
+                                                                f32(push[c, 1] * (k + 1) / links))))
+                if k % 3 == 2:
+                    sc.joints.append(Joint(JOINT_HINGE, prev, b, anchor_a=anchor, axis_a=(0.0, 0.0, 1.0),
+                                           axis_b=(0.0, 0.0, 1.0), lower=-0.8, upper=0.8, flags=JOINT_FLAG_LIMITS))
+                else:
+                    sc.joints.append(Joint(JOINT_POINT, prev, b, anchor_a=anchor))
+                prev, anchor = b, (x, f32(y - 0.25), z)
+    return sc
+
+
+def projectiles(n_shots: int = 2000, n_boxes: int = 4000, seed: int = 9) -> Scene:
+    """A continuous-collision workload: LinearCast spheres and small boxes fired at 40-80 m/s at
+    thin static walls (5 cm) beside a field of resting boxes, ground plane below."""
+    sc = Scene(name=f"projectiles{n_shots}")
+    _timed_settings(sc, 10, 2)
+    _ground(sc, 0.6)
+    wall = sc.add_shape(Shape(SHAPE_BOX, [0.025, 2.0, 8.0, 0.0]))
+    ball = sc.add_shape(Shape(SHAPE_SPHERE, [0.1, 0.0, 0.0, 0.0]))
+    cube = sc.add_shape(Shape(SHAPE_BOX, [0.1, 0.1, 0.1, 0.0]))
+    box = sc.add_shape(Shape(SHAPE_BOX, [0.4, 0.4, 0.4, 0.0]))
+    rng = np.random.RandomState(seed)
+    for k in range(8):
+        sc.add_body(Body(wall, MOTION_STATIC, pos=(f32(-28.0 + 8.0 * k), 2.0, 0.0)))
+    side = int(math.ceil(math.sqrt(n_boxes)))
+    for i in range(n_boxes):
+        sc.add_body(Body(box, pos=(f32(-30.0 + 60.0 * (i % side) / side), 0.4, f32(10.0 + 40.0 * (i // side) / side))))
+    lc = BODY_FLAG_ALLOW_SLEEPING | BODY_FLAG_LINEAR_CAST
+    for i in range(n_shots):
+        x = f32(rng.uniform(-30.0, 30.0))
+        sc.add_body(Body(ball if i % 2 else cube, pos=(x, f32(rng.uniform(0.5, 3.5)), f32(rng.uniform(-7.0, 7.0))),
+                         vel=(f32(rng.choice([-1.0, 1.0]) * rng.uniform(40.0, 80.0)), 0.0, 0.0), flags=lc))
+    return sc
+
+
 def _shoemake(u1: float, u2: float, u3: float) -> tuple:
     """Uniform random rotation (Shoemake 1992), returned as float32 (x, y, z, w)."""
     a = math.sqrt(1.0 - u1)

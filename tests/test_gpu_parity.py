@@ -239,6 +239,23 @@ def test_snapshot_resumes_bit_exactly(kzg_lib):
         assert c.compute_state_hash() != a.compute_state_hash()
 
 
+def test_snapshot_with_joints_and_ccd_resumes_bit_exactly(kzg_lib):
+    """The snapshot also carries the joints' accumulated impulses and prepared frames and the
+    bodies' broad-phase fat bounds (continuous collision reads them): a world of joints resumes
+    bit-exactly, and so does the CCD fixture."""
+    from kizuriphysics3d_gb300 import World, resolve
+    for name in ("joints_mix", "ccd_shots"):
+        sc = FIXTURES[name][0]
+        res = resolve(sc)
+        with World(sc, resolved=res) as a, World(sc, resolved=res) as b:
+            a.step_fixed(n=30)
+            snap = a.snapshot()
+            a.step_fixed(n=30)
+            b.restore(snap)
+            b.step_fixed(n=30)
+            assert np.array_equal(bits(b.state()), bits(a.state())), name
+
+
 def test_kzp1_world_steps_like_the_scene(kzg_lib):
     """A world loaded from KZP1 bytes of a box scene (no hulls to rebuild) steps to the same state
     as the scene it was written from."""
