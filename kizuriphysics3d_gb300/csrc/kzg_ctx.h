@@ -132,6 +132,7 @@ struct Ctx {
     uint32_t* epa_list = nullptr;  // pairs whose narrow phase needs EPA (warp pass)
     float4* ccd_disp = nullptr;    // continuous collision: each LinearCast body's step displacement
     uint32_t* ccd_list = nullptr;  // slots of the LinearCast bodies, ascending
+    uint32_t* ccd_state = nullptr; // per body slot: CCD round that finished it (LinearCast bodies)
     uint32_t nccd = 0;
     // joints (kzg_joint.cuh): records, creation staging, per-step island grouping
     JointDev* joints = nullptr;

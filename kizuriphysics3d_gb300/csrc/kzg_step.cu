@@ -673,93 +673,194 @@ __device__ __forceinline__ bool casts_linear(const DeviceBodies& b, uint32_t i) 
 }
 
 // Continuous collision of LinearCast bodies (PhysicsWorld::ClampMotionCCD, PhysicsWorld.cpp:785-802
-// and 804-852; the per-body CCD motion threshold is 0, its default), run where the reference runs it: inside the position loop, body by body in slot
-// order, so a body sees the bodies before it already moved.  One block walks the LinearCast list;
-// per body its threads scan every body for candidates (fat bounds overlapping the swept bounds
-// grown by 0.1, not itself, not a sensor, layer and mask both ways), cast against each, and reduce
-// to the smallest fraction (ties: the smaller slot, the reference's first hit).  The motion stops
-// max_pen short of the hit and the approaching normal velocity is removed.  disp[i] receives the
-// displacement k_integrate_pos applies.
+// and 804-852; the per-body CCD motion threshold is 0, its default).  The reference runs it inside
+// the position loop, body by body in slot order, so a body sees the bodies before it already
+// moved.  Per body: candidates are the bodies whose fat bounds overlap the swept bounds grown by
+// 0.1 (not itself, not a sensor, layer and mask both ways), each placed where that loop has it at
+// that moment (lower slots moved: LinearCast ones by their clamped displacement, others by v dt
+// with their rotation integrated), cast against, and the smallest fraction wins (ties: the smaller
+// slot, the reference's first hit).  The motion stops max_pen short of the hit and the approaching
+// normal velocity is removed.
+//
+// Order only matters through a LinearCast candidate of lower slot whose own motion may be clamped
+// (displacement above max_pen).  k_ccd_init writes the displacement of every LinearCast body with
+// nothing to clamp (round[slot] = 0) and marks the others pending (kPending); a body's velocity
+// may change when it is clamped, so "clampable" is read from the round stamp, never from the
+// velocity.  Round r (k_ccd_round, one warp per body, r = 1..kCcdRounds) solves every pending body
+// whose clampable lower-slot candidates all finished in an earlier round, so each sees final
+// displacements, and stamps it r; k_ccd_serial walks what is left in slot order on one block.  The
+// result is the sequential one.
 constexpr uint32_t kCcdThreads = 256;
-__global__ void __launch_bounds__(kCcdThreads) k_ccd(ShapeTables T, DeviceBodies b, uint32_t n,
-                                                     const uint32_t* __restrict__ list, uint32_t nlist, float dt,
-                                                     float max_pen, float4* disp_out) {
+constexpr uint32_t kNoHit = 0xFFFFFFFFu;
+
+struct CcdBody {
+    const ShapeDev* sh;
+    Quat q0;
+    Vec3 t0, lv, disp, dir;
+    float dist;
+    AABB sweep;
+    uint32_t li, mi;
+};
+
+__device__ __forceinline__ CcdBody ccd_body(const ShapeTables& T, const DeviceBodies& b, uint32_t i, float dt) {
+    CcdBody c;
+    c.sh = &T.shapes[b.shape[i]];
+    c.q0 = Q4(b.rot[i]);
+    c.t0 = V3(b.pos[i]);
+    c.lv = V3(b.lv[i]);
+    c.disp = c.lv * dt;
+    c.dist = c.disp.len();
+    c.dir = c.disp / c.dist;
+    const AABB local{Vec3(c.sh->lmn[0], c.sh->lmn[1], c.sh->lmn[2]), Vec3(c.sh->lmx[0], c.sh->lmx[1], c.sh->lmx[2])};
+    AABB sweep = aabb_merge(aabb_transformed(local, c.q0, c.t0), aabb_transformed(local, c.q0, c.t0 + c.disp));
+    const Vec3 margin(0.1f, 0.1f, 0.1f);
+    c.sweep = AABB{sweep.mn - margin, sweep.mx + margin};
+    c.li = b.layer[i];
+    c.mi = b.mask[i];
+    return c;
+}
+
+__device__ __forceinline__ bool ccd_candidate(const DeviceBodies& b, const CcdBody& c, uint32_t i, uint32_t j) {
+    if (j == i || (b.flags[j] & KZG_BODY_SENSOR)) return false;
+    if ((b.layer[j] & c.mi) == 0u || (c.li & b.mask[j]) == 0u) return false;
+    return aabb_overlaps(AABB{V3(b.fat_mn[j]), V3(b.fat_mx[j])}, c.sweep);
+}
+
+struct CcdHit {
+    float frac;
+    uint32_t slot;
+    Vec3 n;
+};
+
+// This lane's share of body i's candidates (j = lane, lane + nl, ...): the smallest fraction, the
+// first such j of the lane on a tie.
+__device__ CcdHit ccd_scan(const ShapeTables& T, const DeviceBodies& b, uint32_t n, uint32_t i, const CcdBody& c,
+                           float dt, const float4* disp, uint32_t lane, uint32_t nl) {
+    CcdHit h{1.0f, kNoHit, Vec3(0.0f, 1.0f, 0.0f)};
+    for (uint32_t j = lane; j < n; j += nl) {
+        if (!ccd_candidate(b, c, i, j)) continue;
+        Vec3 tj = V3(b.pos[j]);
+        Quat qj = Q4(b.rot[j]);
+        if (j < i && b.motion[j] != KZG_MOTION_STATIC) {  // already integrated this step
+            tj = tj + (casts_linear(b, j) ? V3(disp[j]) : V3(b.lv[j]) * dt);
+            const Vec3 avj = V3(b.av[j]);
+            if (avj.len2() > 0.0f) qj = integrate_rotation(qj, avj, dt);
+        }
+        float frac;
+        Vec3 nrm;
+        if (cast_shape(T, Body{c.sh, c.q0, c.t0}, c.dir, c.dist, Body{&T.shapes[b.shape[j]], qj, tj}, frac, nrm) &&
+            frac < h.frac) {
+            h.frac = frac;
+            h.slot = j;
+            h.n = nrm;
+        }
+    }
+    return h;
+}
+
+__device__ __forceinline__ bool ccd_better(const CcdHit& o, const CcdHit& m) {
+    return o.slot != kNoHit && (m.slot == kNoHit || o.frac < m.frac || (o.frac == m.frac && o.slot < m.slot));
+}
+
+__device__ __forceinline__ void ccd_finish(const DeviceBodies& b, uint32_t i, const CcdBody& c, const CcdHit& h,
+                                           float max_pen, float4* disp) {
+    Vec3 d = c.disp;
+    if (h.slot != kNoHit) {
+        float stop = h.frac * c.dist - max_pen;
+        if (stop < 0.0f) stop = 0.0f;
+        d = c.dir * stop;
+        const float vn = c.lv.dot(h.n);
+        if (vn < 0.0f) b.lv[i] = F4(c.lv - h.n * vn, 0.0f);
+    }
+    disp[i] = F4(d, 0.0f);
+}
+
+constexpr uint32_t kPending = 0xFFFFFFFFu;
+constexpr uint32_t kCcdRounds = 8;
+
+__global__ void k_ccd_init(DeviceBodies b, uint32_t n, const uint32_t* __restrict__ list, uint32_t nlist, float dt,
+                           float max_pen, float4* disp, uint32_t* round) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nlist) return;
+    const uint32_t i = list[k];
+    const Vec3 d = V3(b.lv[i]) * dt;
+    if (casts_linear(b, i) && d.len() > max_pen) {
+        round[i] = kPending;
+    } else {
+        if (casts_linear(b, i)) disp[i] = F4(d, 0.0f);
+        round[i] = 0u;
+    }
+}
+
+__global__ void k_ccd_round(ShapeTables T, DeviceBodies b, uint32_t n, const uint32_t* __restrict__ list,
+                            uint32_t nlist, float dt, float max_pen, float4* disp, uint32_t* round, uint32_t r) {
+    const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (k >= nlist) return;
+    const uint32_t i = list[k];
+    if (round[i] != kPending) return;
+    const CcdBody c = ccd_body(T, b, i, dt);
+    bool wait = false;
+    for (uint32_t j = lane; j < i && !wait; j += 32u)
+        wait = casts_linear(b, j) && round[j] >= r && ccd_candidate(b, c, i, j);  // clampable, not finished
+    if (__any_sync(0xFFFFFFFFu, wait)) return;
+    CcdHit h = ccd_scan(T, b, n, i, c, dt, disp, lane, 32u);
+    for (uint32_t off = 16; off > 0; off >>= 1) {
+        CcdHit o;
+        o.frac = __shfl_down_sync(0xFFFFFFFFu, h.frac, off);
+        o.slot = __shfl_down_sync(0xFFFFFFFFu, h.slot, off);
+        o.n.x = __shfl_down_sync(0xFFFFFFFFu, h.n.x, off);
+        o.n.y = __shfl_down_sync(0xFFFFFFFFu, h.n.y, off);
+        o.n.z = __shfl_down_sync(0xFFFFFFFFu, h.n.z, off);
+        if (ccd_better(o, h)) h = o;
+    }
+    if (lane == 0) {
+        ccd_finish(b, i, c, h, max_pen, disp);
+        round[i] = r;
+    }
+}
+
+__global__ void __launch_bounds__(kCcdThreads) k_ccd_serial(ShapeTables T, DeviceBodies b, uint32_t n,
+                                                            const uint32_t* __restrict__ list, uint32_t nlist,
+                                                            float dt, float max_pen, float4* disp,
+                                                            const uint32_t* __restrict__ round) {
     __shared__ float s_frac[kCcdThreads];
     __shared__ uint32_t s_slot[kCcdThreads];
     __shared__ float4 s_norm[kCcdThreads];
+    __shared__ uint32_t s_slot_of[kCcdThreads];
     const uint32_t tid = threadIdx.x;
-    for (uint32_t k = 0; k < nlist; ++k) {
-        const uint32_t i = list[k];
-        if (!casts_linear(b, i)) continue;
-        const Vec3 lv = V3(b.lv[i]);
-        const Vec3 disp = lv * dt;
-        const float dist = disp.len();
-        if (dist <= max_pen) {
-            if (tid == 0) disp_out[i] = F4(disp, 0.0f);
-            continue;
-        }
-        const ShapeDev* sh = &T.shapes[b.shape[i]];
-        const Quat q0 = Q4(b.rot[i]);
-        const Vec3 t0 = V3(b.pos[i]);
-        const Vec3 dir = disp / dist;
-        const AABB local{Vec3(sh->lmn[0], sh->lmn[1], sh->lmn[2]), Vec3(sh->lmx[0], sh->lmx[1], sh->lmx[2])};
-        AABB sweep = aabb_merge(aabb_transformed(local, q0, t0), aabb_transformed(local, q0, t0 + disp));
-        const Vec3 margin(0.1f, 0.1f, 0.1f);
-        sweep = AABB{sweep.mn - margin, sweep.mx + margin};
-        const uint32_t li = b.layer[i], mi = b.mask[i];
-        float best = 1.0f;
-        uint32_t best_j = 0xFFFFFFFFu;
-        Vec3 best_n(0.0f, 1.0f, 0.0f);
-        for (uint32_t j = tid; j < n; j += kCcdThreads) {
-            if (j == i || (b.flags[j] & KZG_BODY_SENSOR)) continue;
-            if ((b.layer[j] & mi) == 0u || (li & b.mask[j]) == 0u) continue;
-            if (!aabb_overlaps(AABB{V3(b.fat_mn[j]), V3(b.fat_mx[j])}, sweep)) continue;
-            Vec3 tj = V3(b.pos[j]);
-            Quat qj = Q4(b.rot[j]);
-            if (j < i && b.motion[j] != KZG_MOTION_STATIC) {  // already integrated this step
-                tj = tj + (casts_linear(b, j) ? V3(disp_out[j]) : V3(b.lv[j]) * dt);
-                const Vec3 avj = V3(b.av[j]);
-                if (avj.len2() > 0.0f) qj = integrate_rotation(qj, avj, dt);
-            }
-            float frac;
-            Vec3 nrm;
-            if (cast_shape(T, Body{sh, q0, t0}, dir, dist, Body{&T.shapes[b.shape[j]], qj, tj}, frac, nrm) &&
-                frac < best) {
-                best = frac;
-                best_j = j;
-                best_n = nrm;
-            }
-        }
-        s_frac[tid] = best;
-        s_slot[tid] = best_j;
-        s_norm[tid] = F4(best_n, 0.0f);
+    for (uint32_t k0 = 0; k0 < nlist; k0 += kCcdThreads) {
         __syncthreads();
-        for (uint32_t w = kCcdThreads / 2; w > 0; w >>= 1) {
-            if (tid < w) {
-                const float fo = s_frac[tid + w];
-                const uint32_t jo = s_slot[tid + w];
-                if (jo != 0xFFFFFFFFu && (s_slot[tid] == 0xFFFFFFFFu || fo < s_frac[tid] ||
-                                          (fo == s_frac[tid] && jo < s_slot[tid]))) {
-                    s_frac[tid] = fo;
-                    s_slot[tid] = jo;
-                    s_norm[tid] = s_norm[tid + w];
+        uint32_t mine = kNoHit;
+        if (k0 + tid < nlist) {
+            const uint32_t i = list[k0 + tid];
+            if (round[i] == kPending) mine = i;
+        }
+        s_slot_of[tid] = mine;
+        __syncthreads();
+        for (uint32_t kk = 0; kk < kCcdThreads; ++kk) {
+            const uint32_t i = s_slot_of[kk];
+            if (i == kNoHit) continue;
+            const CcdBody c = ccd_body(T, b, i, dt);
+            const CcdHit h = ccd_scan(T, b, n, i, c, dt, disp, tid, kCcdThreads);
+            s_frac[tid] = h.frac;
+            s_slot[tid] = h.slot;
+            s_norm[tid] = F4(h.n, 0.0f);
+            __syncthreads();
+            for (uint32_t w = kCcdThreads / 2; w > 0; w >>= 1) {
+                if (tid < w) {
+                    const CcdHit o{s_frac[tid + w], s_slot[tid + w], V3(s_norm[tid + w])};
+                    const CcdHit m{s_frac[tid], s_slot[tid], V3(s_norm[tid])};
+                    if (ccd_better(o, m)) {
+                        s_frac[tid] = o.frac;
+                        s_slot[tid] = o.slot;
+                        s_norm[tid] = s_norm[tid + w];
+                    }
                 }
+                __syncthreads();
             }
+            if (tid == 0) ccd_finish(b, i, c, CcdHit{s_frac[0], s_slot[0], V3(s_norm[0])}, max_pen, disp);
             __syncthreads();
         }
-        if (tid == 0) {
-            Vec3 d = disp;
-            if (s_slot[0] != 0xFFFFFFFFu) {
-                float stop = s_frac[0] * dist - max_pen;
-                if (stop < 0.0f) stop = 0.0f;
-                d = dir * stop;
-                const Vec3 hn = V3(s_norm[0]);
-                const float vn = lv.dot(hn);
-                if (vn < 0.0f) b.lv[i] = F4(lv - hn * vn, 0.0f);
-            }
-            disp_out[i] = F4(d, 0.0f);
-        }
-        __syncthreads();
     }
 }
 
@@ -988,9 +1089,15 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     const bool ccd = ctx.ws.use_ccd && ctx.nccd > 0;
     if (ccd) {
         ShapeTables T{ctx.shapes, ctx.hull_verts, ctx.face_sizes, ctx.face_idx};
-        k_ccd<<<1, kCcdThreads, 0, st>>>(T, ctx.b, nb, ctx.ccd_list, ctx.nccd, dt, ctx.ws.ccd_max_penetration,
-                                         ctx.ccd_disp);
-        ++ctx.launches;
+        const float mp = ctx.ws.ccd_max_penetration;
+        k_ccd_init<<<blocks_for(ctx.nccd), kThreads, 0, st>>>(ctx.b, nb, ctx.ccd_list, ctx.nccd, dt, mp, ctx.ccd_disp,
+                                                               ctx.ccd_state);
+        for (uint32_t r = 1; r <= kCcdRounds; ++r)
+            k_ccd_round<<<blocks_for(32u * ctx.nccd), kThreads, 0, st>>>(T, ctx.b, nb, ctx.ccd_list, ctx.nccd, dt, mp,
+                                                                         ctx.ccd_disp, ctx.ccd_state, r);
+        k_ccd_serial<<<1, kCcdThreads, 0, st>>>(T, ctx.b, nb, ctx.ccd_list, ctx.nccd, dt, mp, ctx.ccd_disp,
+                                                ctx.ccd_state);
+        ctx.launches += 2 + kCcdRounds;
     }
     k_integrate_pos<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, dt, ctx.ss.use_velocity_bias,
                                                          ccd ? ctx.ccd_disp : nullptr);

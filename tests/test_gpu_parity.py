@@ -219,6 +219,39 @@ def test_graph_stepping_matches_direct_stepping(kzg_lib):
         assert b.get_stats()["max_velocity_iterations_used"] == a.get_stats()["max_velocity_iterations_used"]
 
 
+def test_many_linear_cast_bodies_bit_exact_with_oracle(oracle_lib, kzg_lib):
+    """400 LinearCast projectiles among walls and boxes (the projectiles workload, scaled down):
+    the GPU resolves the casts of independent bodies in parallel rounds and the ordered remainder in
+    slot order; the result is the oracle's sequential one, bit for bit, for 40 steps."""
+    from kizuriphysics3d_gb300 import World, resolve, scenes
+    sc = scenes.projectiles(400, 600)
+    res = resolve(sc)
+    ow = oracle_lib.OracleWorld(sc.to_bytes(), oracle_blob(sc, res), oracle_lib.PAIRS_CANONICAL)
+    with World(sc, resolved=res) as gw:
+        for s in range(40):
+            ow.step(np.float32(sc.dt))
+            gw.step_fixed()
+            assert np.array_equal(bits(gw.state()), bits(ow.state())), f"state differs at step {s}"
+        assert gw.get_stats()["device_error"] == 0
+
+
+def test_joint_field_bit_exact_with_oracle(oracle_lib, kzg_lib):
+    """A field of 100 ten-link chains (the chains workload, scaled down): hundreds of joint islands
+    with contacts, solved one CTA each, bit-identical to the oracle (correctly rounded trigonometry)
+    for 40 steps."""
+    from kizuriphysics3d_gb300 import World, resolve, scenes
+    sc = scenes.chains(10, 10, 10)
+    res = resolve(sc)
+    ow = oracle_lib.OracleWorld(sc.to_bytes(), oracle_blob(sc, res), oracle_lib.PAIRS_CANONICAL)
+    ow.set_trig_mode(1)
+    with World(sc, resolved=res) as gw:
+        for s in range(40):
+            ow.step(np.float32(sc.dt))
+            gw.step_fixed()
+            assert np.array_equal(bits(gw.state()), bits(ow.state())), f"state differs at step {s}"
+        assert gw.get_stats()["device_error"] == 0
+
+
 def test_snapshot_resumes_bit_exactly(kzg_lib):
     """kzg_snapshot_save / load: a second context restored from a snapshot continues bit-exactly;
     restoring the body state alone (cold manifold cache) does not, which is what the cache part of
