@@ -63,6 +63,8 @@ kzg_status alloc_all(Ctx* ctx) {
     CK(dalloc(&ctx->ccd_disp, B));
     CK(dalloc(&ctx->ccd_list, B));
     CK(dalloc(&ctx->ccd_state, B));
+    CK(dalloc(&ctx->ccd_deps, 8 * B));
+    CK(dalloc(&ctx->ccd_ndeps, B));
     if (c.max_joints) {
         CK(cudaMalloc((void**)&ctx->joints, joint_record_bytes() * c.max_joints));
         CK(dalloc(&ctx->joint_stage, c.max_joints));
@@ -145,7 +147,7 @@ void free_all(Ctx* ctx) {
                     b.iiw, b.iil, b.inv_mass, b.shape, b.motion, b.flags, b.layer, b.mask, b.world, b.packed, b.fat_mn, b.fat_mx,
                     ctx->is_large, ctx->large_list, ctx->large_off, ctx->cell_keys, ctx->cell_keys_sorted,
                     ctx->cell_vals, ctx->cell_vals_sorted, ctx->pair_keys, ctx->pair_keys_sorted, ctx->pairs,
-                    ctx->m_count, ctx->m_data, ctx->m_key, ctx->epa_list, ctx->ccd_disp, ctx->ccd_list, ctx->ccd_state, ctx->joints, ctx->joint_stage, ctx->jkeys,
+                    ctx->m_count, ctx->m_data, ctx->m_key, ctx->epa_list, ctx->ccd_disp, ctx->ccd_list, ctx->ccd_state, ctx->ccd_deps, ctx->ccd_ndeps, ctx->joints, ctx->joint_stage, ctx->jkeys,
                     ctx->jkeys_sorted, ctx->jisl, ctx->jisl_cisl, ctx->jflag, ctx->con_flag, ctx->con_index, ctx->con_pair, ctx->con_a,
                     ctx->con_b, ctx->con_np, ctx->con_bits, ctx->con_fr, ctx->con_key, ctx->r.pA, ctx->r.pB, ctx->r.n,
                     ctx->r.t1, ctx->r.t2, ctx->r.rA, ctx->r.rB, ctx->r.rAr, ctx->r.rBr, ctx->r.laA, ctx->r.laB,

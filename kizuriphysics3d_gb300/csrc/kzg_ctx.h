@@ -133,6 +133,7 @@ struct Ctx {
     float4* ccd_disp = nullptr;    // continuous collision: each LinearCast body's step displacement
     uint32_t* ccd_list = nullptr;  // slots of the LinearCast bodies, ascending
     uint32_t* ccd_state = nullptr; // per body slot: CCD round that finished it (LinearCast bodies)
+    uint32_t *ccd_deps = nullptr, *ccd_ndeps = nullptr;  // per LinearCast body: predecessors (8 max), count
     uint32_t nccd = 0;
     // joints (kzg_joint.cuh): records, creation staging, per-step island grouping
     JointDev* joints = nullptr;

@@ -686,10 +686,11 @@ __device__ __forceinline__ bool casts_linear(const DeviceBodies& b, uint32_t i) 
 // (displacement above max_pen).  k_ccd_init writes the displacement of every LinearCast body with
 // nothing to clamp (round[slot] = 0) and marks the others pending (kPending); a body's velocity
 // may change when it is clamped, so "clampable" is read from the round stamp, never from the
-// velocity.  Round r (k_ccd_round, one warp per body, r = 1..kCcdRounds) solves every pending body
-// whose clampable lower-slot candidates all finished in an earlier round, so each sees final
-// displacements, and stamps it r; k_ccd_serial walks what is left in slot order on one block.  The
-// result is the sequential one.
+// velocity.  k_ccd_deps lists each pending body's predecessors (its clampable lower-slot
+// candidates).  Round r (k_ccd_round, one warp per body, r = 1..kCcdRounds) solves every pending
+// body whose predecessors all finished in an earlier round, so each sees final displacements, and
+// stamps it r; k_ccd_serial walks what is left in slot order on one block.  The result is the
+// sequential one.
 constexpr uint32_t kCcdThreads = 256;
 constexpr uint32_t kNoHit = 0xFFFFFFFFu;
 
@@ -776,7 +777,8 @@ __device__ __forceinline__ void ccd_finish(const DeviceBodies& b, uint32_t i, co
 }
 
 constexpr uint32_t kPending = 0xFFFFFFFFu;
-constexpr uint32_t kCcdRounds = 8;
+constexpr uint32_t kCcdRounds = 64;
+constexpr uint32_t kCcdMaxDeps = 8;  // more predecessors than this: solved by k_ccd_serial
 
 __global__ void k_ccd_init(DeviceBodies b, uint32_t n, const uint32_t* __restrict__ list, uint32_t nlist, float dt,
                            float max_pen, float4* disp, uint32_t* round) {
@@ -792,17 +794,41 @@ __global__ void k_ccd_init(DeviceBodies b, uint32_t n, const uint32_t* __restric
     }
 }
 
-__global__ void k_ccd_round(ShapeTables T, DeviceBodies b, uint32_t n, const uint32_t* __restrict__ list,
-                            uint32_t nlist, float dt, float max_pen, float4* disp, uint32_t* round, uint32_t r) {
+// Each pending body's predecessors: its clampable (pending) LinearCast candidates of lower slot,
+// in slot order, at most kCcdMaxDeps (a count above that sends the body to k_ccd_serial).
+__global__ void k_ccd_deps(DeviceBodies b, const ShapeDev* __restrict__ shapes, uint32_t n,
+                           const uint32_t* __restrict__ list, uint32_t nlist, float dt, const uint32_t* round,
+                           uint32_t* deps, uint32_t* ndeps) {
     const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
     if (k >= nlist) return;
     const uint32_t i = list[k];
     if (round[i] != kPending) return;
+    const ShapeTables T{shapes, nullptr, nullptr, nullptr};
     const CcdBody c = ccd_body(T, b, i, dt);
-    bool wait = false;
-    for (uint32_t j = lane; j < i && !wait; j += 32u)
-        wait = casts_linear(b, j) && round[j] >= r && ccd_candidate(b, c, i, j);  // clampable, not finished
+    uint32_t cnt = 0;
+    for (uint32_t j0 = 0; j0 < i && cnt <= kCcdMaxDeps; j0 += 32u) {
+        const uint32_t j = j0 + lane;
+        const bool dep = j < i && casts_linear(b, j) && round[j] == kPending && ccd_candidate(b, c, i, j);
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, dep);
+        const uint32_t pos = cnt + __popc(m & ((1u << lane) - 1u));
+        if (dep && pos < kCcdMaxDeps) deps[k * kCcdMaxDeps + pos] = j;
+        cnt += __popc(m);
+    }
+    if (lane == 0) ndeps[k] = cnt;
+}
+
+__global__ void k_ccd_round(ShapeTables T, DeviceBodies b, uint32_t n, const uint32_t* __restrict__ list,
+                            uint32_t nlist, float dt, float max_pen, float4* disp, uint32_t* round,
+                            const uint32_t* __restrict__ deps, const uint32_t* __restrict__ ndeps, uint32_t r) {
+    const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (k >= nlist) return;
+    const uint32_t i = list[k];
+    if (round[i] != kPending) return;
+    const uint32_t nd = ndeps[k];
+    if (nd > kCcdMaxDeps) return;
+    const bool wait = lane < nd && round[deps[k * kCcdMaxDeps + lane]] >= r;  // a predecessor not finished
     if (__any_sync(0xFFFFFFFFu, wait)) return;
+    const CcdBody c = ccd_body(T, b, i, dt);
     CcdHit h = ccd_scan(T, b, n, i, c, dt, disp, lane, 32u);
     for (uint32_t off = 16; off > 0; off >>= 1) {
         CcdHit o;
@@ -1092,12 +1118,15 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
         const float mp = ctx.ws.ccd_max_penetration;
         k_ccd_init<<<blocks_for(ctx.nccd), kThreads, 0, st>>>(ctx.b, nb, ctx.ccd_list, ctx.nccd, dt, mp, ctx.ccd_disp,
                                                                ctx.ccd_state);
+        k_ccd_deps<<<blocks_for(32u * ctx.nccd), kThreads, 0, st>>>(ctx.b, ctx.shapes, nb, ctx.ccd_list, ctx.nccd,
+                                                                    dt, ctx.ccd_state, ctx.ccd_deps, ctx.ccd_ndeps);
         for (uint32_t r = 1; r <= kCcdRounds; ++r)
             k_ccd_round<<<blocks_for(32u * ctx.nccd), kThreads, 0, st>>>(T, ctx.b, nb, ctx.ccd_list, ctx.nccd, dt, mp,
-                                                                         ctx.ccd_disp, ctx.ccd_state, r);
+                                                                         ctx.ccd_disp, ctx.ccd_state, ctx.ccd_deps,
+                                                                         ctx.ccd_ndeps, r);
         k_ccd_serial<<<1, kCcdThreads, 0, st>>>(T, ctx.b, nb, ctx.ccd_list, ctx.nccd, dt, mp, ctx.ccd_disp,
                                                 ctx.ccd_state);
-        ctx.launches += 2 + kCcdRounds;
+        ctx.launches += 3 + kCcdRounds;
     }
     k_integrate_pos<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, dt, ctx.ss.use_velocity_bias,
                                                          ccd ? ctx.ccd_disp : nullptr);
