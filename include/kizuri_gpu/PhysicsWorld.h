@@ -8,6 +8,10 @@
 //   BodySettings / BodyID  include/Kizuri/Body/Body.h:14-30, 62-90
 //   shapes                 include/Kizuri/Geometry/Shape.h (Sphere, Box, Capsule(halfHeight, radius),
 //                          ConvexHull, Plane)
+//   joints                 include/Kizuri/Constraint/Constraints.h:41-277 (PointConstraint ...
+//                          SixDOFConstraint as descriptions, SetLimits / SetMotor, AddConstraint)
+//   continuous collision   BodySettings::motionQuality = LinearCast, WorldSettings::useCCD /
+//                          ccdMaxPenetration (PhysicsWorld.cpp:785-852)
 // Differences, by design: shapes are registered with AddShape before the first step (the device
 // shape table is uploaded once); body state is read back with GetBodyState instead of a Body*;
 // errors throw kizuri_gpu::Error carrying the kzg_status and kzg_last_error() text.
@@ -90,6 +94,8 @@ struct BodyID {
     uint32_t Packed() const { return (sequence << 24) | (index & 0x00FFFFFFu); }
 };
 
+enum class MotionQuality : uint8_t { Discrete = 0, LinearCast };  // Body.h:46-49
+
 // BodySettings defaults (Body.h:62-90); `shape` is an index returned by AddShape.
 struct BodySettings {
     Vec3 position;
@@ -101,6 +107,7 @@ struct BodySettings {
     float gravityFactor = 1.0f, maxLinearVelocity = 500.0f, maxAngularVelocity = 50.0f;
     uint32_t objectLayer = 1, collisionMask = 0xFFFFFFFFu;
     bool allowSleeping = true, isSensor = false;
+    MotionQuality motionQuality = MotionQuality::Discrete;
     float massOverride = 0.0f, density = 1000.0f;
     uint32_t worldId = 0;  // independent worlds stepped together (batched scenes)
 };
@@ -120,12 +127,67 @@ struct WorldSettings {  // PhysicsWorld.h:20-43 (the fields the accelerated step
     float fixedTimestep = (float)(1.0 / 60.0);
     uint32_t maxSubSteps = 4;
     bool warmStart = true;
+    bool useCCD = true;               // continuous collision for LinearCast bodies
+    float ccdMaxPenetration = 0.01f;
 };
+
+// Joints (Constraints.h:41-277), built like the reference's constructors: world-space anchors and
+// axes at the bodies' poses when the world next steps; pass the result to AddConstraint.
+inline kzg_joint_desc JointDesc(uint32_t type, BodyID a, BodyID b, const Vec3& anchorA) {
+    kzg_joint_desc d{};
+    d.type = type;
+    d.body_a = a.index;
+    d.body_b = b.index;
+    d.anchor_a[0] = anchorA.x; d.anchor_a[1] = anchorA.y; d.anchor_a[2] = anchorA.z;
+    d.rotation[3] = 1.0f;
+    return d;
+}
+inline kzg_joint_desc PointConstraint(BodyID a, BodyID b, const Vec3& worldAnchor) {
+    return JointDesc(KZG_JOINT_POINT, a, b, worldAnchor);
+}
+inline kzg_joint_desc DistanceConstraint(BodyID a, BodyID b, const Vec3& worldAnchorA, const Vec3& worldAnchorB,
+                                         float distance) {
+    kzg_joint_desc d = JointDesc(KZG_JOINT_DISTANCE, a, b, worldAnchorA);
+    d.anchor_b[0] = worldAnchorB.x; d.anchor_b[1] = worldAnchorB.y; d.anchor_b[2] = worldAnchorB.z;
+    d.distance = distance;
+    return d;
+}
+inline kzg_joint_desc FixedConstraint(BodyID a, BodyID b, const Vec3& worldAnchor) {
+    return JointDesc(KZG_JOINT_FIXED, a, b, worldAnchor);
+}
+inline kzg_joint_desc HingeConstraint(BodyID a, BodyID b, const Vec3& worldAnchor, const Vec3& worldAxisA,
+                                      const Vec3& worldAxisB) {
+    kzg_joint_desc d = JointDesc(KZG_JOINT_HINGE, a, b, worldAnchor);
+    d.axis_a[0] = worldAxisA.x; d.axis_a[1] = worldAxisA.y; d.axis_a[2] = worldAxisA.z;
+    d.axis_b[0] = worldAxisB.x; d.axis_b[1] = worldAxisB.y; d.axis_b[2] = worldAxisB.z;
+    return d;
+}
+inline kzg_joint_desc SliderConstraint(BodyID a, BodyID b, const Vec3& worldAnchor, const Vec3& worldAxis) {
+    kzg_joint_desc d = JointDesc(KZG_JOINT_SLIDER, a, b, worldAnchor);
+    d.axis_a[0] = worldAxis.x; d.axis_a[1] = worldAxis.y; d.axis_a[2] = worldAxis.z;
+    return d;
+}
+inline kzg_joint_desc SixDOFConstraint(BodyID a, BodyID b, const Vec3& worldAnchor, const Quat& worldRotation) {
+    kzg_joint_desc d = JointDesc(KZG_JOINT_SIXDOF, a, b, worldAnchor);
+    d.rotation[0] = worldRotation.x; d.rotation[1] = worldRotation.y; d.rotation[2] = worldRotation.z;
+    d.rotation[3] = worldRotation.w;
+    return d;
+}
+// Hinge/SliderConstraint::SetLimits and SetMotor on a description.
+inline kzg_joint_desc& SetLimits(kzg_joint_desc& d, float lower, float upper) {
+    d.lower = lower; d.upper = upper; d.flags |= KZG_JOINT_LIMITS;
+    return d;
+}
+inline kzg_joint_desc& SetMotor(kzg_joint_desc& d, float target, float maxImpulse) {
+    d.motor_target = target; d.motor_max = maxImpulse; d.flags |= KZG_JOINT_MOTOR;
+    return d;
+}
 
 struct Capacity {
     uint32_t maxBodies = 1u << 16, maxShapes = 1u << 16, maxHullVertices = 1u << 20, maxHullIndices = 1u << 22;
     uint32_t maxPairs = 1u << 20, maxCacheEntries = 1u << 21;
     int device = 0;
+    uint32_t maxJoints = 1u << 16;
 };
 
 struct BodyState {
@@ -138,7 +200,7 @@ class PhysicsWorld {
 public:
     explicit PhysicsWorld(const Capacity& cap = Capacity()) {
         kzg_config c{cap.maxBodies, cap.maxShapes, cap.maxHullVertices, cap.maxHullIndices, cap.maxPairs,
-                     cap.maxCacheEntries, cap.device};
+                     cap.maxCacheEntries, cap.device, cap.maxJoints};
         Check(kzg_create(&c, &ctx_), nullptr);
     }
     ~PhysicsWorld() {
@@ -169,6 +231,13 @@ public:
         iil_.insert(iil_.end(), iil, iil + 9);
         BodyID id{numBodies_++, 0};
         return id;
+    }
+
+    // PhysicsWorld::AddConstraint: created when the world next steps, after the pending bodies, at
+    // their poses then; returns the joint's index.
+    uint32_t AddConstraint(const kzg_joint_desc& d) {
+        pendingJoints_.push_back(d);
+        return numJoints_++;
     }
 
     // PhysicsWorld::StepFixed
@@ -249,6 +318,8 @@ private:
         ws.fixed_timestep = settings_.fixedTimestep;
         ws.allow_sleeping = settings_.allowSleeping ? 1 : 0;
         ws.warm_start = settings_.warmStart ? 1 : 0;
+        ws.use_ccd = settings_.useCCD ? 1 : 0;
+        ws.ccd_max_penetration = settings_.ccdMaxPenetration;
         ss.velocity_iterations = settings_.solver.velocityIterations;
         ss.position_iterations = settings_.solver.positionIterations;
         ss.baumgarte = settings_.solver.baumgarte;
@@ -259,14 +330,23 @@ private:
         ss.use_velocity_bias = settings_.solver.useVelocityBias ? 1 : 0;
         Check(kzg_set_world_settings(ctx_, &ws), ctx_);
         Check(kzg_set_solver_settings(ctx_, &ss), ctx_);
-        if (pending_.empty()) return;
+        if (!pending_.empty()) FlushBodies();
+        if (!pendingJoints_.empty()) {
+            uint32_t first = 0;
+            Check(kzg_add_joints(ctx_, (uint32_t)pendingJoints_.size(), pendingJoints_.data(), &first), ctx_);
+            pendingJoints_.clear();
+        }
+    }
+
+    void FlushBodies() {
         const size_t n = pending_.size();
         std::vector<uint32_t> shape(n), motion(n), flags(n), layer(n), mask(n), world(n);
         std::vector<float> pos(3 * n), rot(4 * n), lv(3 * n), av(3 * n), fr(n), rs(n), ld(n), ad(n), gf(n), ml(n), ma(n);
         for (size_t i = 0; i < n; ++i) {
             const BodySettings& b = pending_[i];
             shape[i] = (uint32_t)b.shape; motion[i] = (uint32_t)b.motionType;
-            flags[i] = (b.isSensor ? KZG_BODY_SENSOR : 0u) | (b.allowSleeping ? KZG_BODY_ALLOW_SLEEPING : 0u);
+            flags[i] = (b.isSensor ? KZG_BODY_SENSOR : 0u) | (b.allowSleeping ? KZG_BODY_ALLOW_SLEEPING : 0u) |
+                       (b.motionQuality == MotionQuality::LinearCast ? KZG_BODY_LINEAR_CAST : 0u);
             layer[i] = b.objectLayer; mask[i] = b.collisionMask; world[i] = b.worldId;
             pos[3 * i] = b.position.x; pos[3 * i + 1] = b.position.y; pos[3 * i + 2] = b.position.z;
             rot[4 * i] = b.rotation.x; rot[4 * i + 1] = b.rotation.y; rot[4 * i + 2] = b.rotation.z; rot[4 * i + 3] = b.rotation.w;
@@ -289,6 +369,8 @@ private:
     WorldSettings settings_;
     std::vector<Shape> shapes_;
     std::vector<BodySettings> pending_;
+    std::vector<kzg_joint_desc> pendingJoints_;
+    uint32_t numJoints_ = 0;
     std::vector<float> invMass_, iil_;
     bool shapesUploaded_ = false;
     uint32_t numBodies_ = 0;
