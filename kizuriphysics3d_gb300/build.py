@@ -61,11 +61,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if force or jobs or not _newer(LIB, objs):
         run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
     # C++ facade example (include/kizuri_gpu/PhysicsWorld.h), linked against the library
-    ex_src = os.path.join(HERE, "cpp", "pyramid_example.cpp")
-    ex = os.path.join(OUT, "pyramid_example")
-    if force or not _newer(ex, [ex_src, LIB, os.path.join(HERE, "..", "include", "kizuri_gpu", "PhysicsWorld.h")]):
-        run(["g++", "-std=c++17", "-O2", "-I", os.path.join(HERE, "..", "include"), ex_src, "-o", ex, "-L", OUT,
-             "-lkzg", f"-Wl,-rpath,{OUT}"])
+    for name in ("pyramid_example", "joints_example"):
+        ex_src = os.path.join(HERE, "cpp", name + ".cpp")
+        ex = os.path.join(OUT, name)
+        if force or not _newer(ex, [ex_src, LIB, os.path.join(HERE, "..", "include", "kizuri_gpu", "PhysicsWorld.h")]):
+            run(["g++", "-std=c++17", "-O2", "-I", os.path.join(HERE, "..", "include"), ex_src, "-o", ex, "-L", OUT,
+                 "-lkzg", f"-Wl,-rpath,{OUT}"])
     return LIB
 
 

@@ -301,6 +301,51 @@ def test_kzp1_world_steps_like_the_scene(kzg_lib):
         assert a.compute_state_hash() == b.compute_state_hash()
 
 
+def _facade_joint_scene(nx, nz, links):
+    """The scene kizuriphysics3d_gb300/cpp/joints_example.cpp builds, through the Python API."""
+    from kizuriphysics3d_gb300 import scenes as S
+    f = S.f32
+    sc = S.Scene(name="facade_joints")
+    S._timed_settings(sc, 10, 2)
+    S._ground(sc, 0.6)
+    hook = sc.add_shape(S.Shape(S.SHAPE_BOX, [0.1, 0.1, 0.1, 0.0]))
+    link = sc.add_shape(S.Shape(S.SHAPE_BOX, [0.1, 0.25, 0.1, 0.0]))
+    ball = sc.add_shape(S.Shape(S.SHAPE_SPHERE, [0.1, 0.0, 0.0, 0.0]))
+    for ix in range(nx):
+        for iz in range(nz):
+            c = ix * nz + iz
+            x, z = f((ix - (nx - 1) * 0.5) * 1.5), f((iz - (nz - 1) * 0.5) * 1.5)
+            prev = sc.add_body(S.Body(hook, S.MOTION_STATIC, pos=(x, f(6.1), z)))
+            anchor = (x, 6.0, z)
+            for k in range(links):
+                y = f(6.0 - 0.5 * k - 0.25)
+                b = sc.add_body(S.Body(link, pos=(x, y, z), vel=(f(((c % 5) - 2) * 0.5 * (k + 1) / links), 0.0,
+                                                                  f(((c % 3) - 1) * 0.7 * (k + 1) / links))))
+                if k % 3 == 2:
+                    sc.joints.append(S.Joint(S.JOINT_HINGE, prev, b, anchor_a=anchor, axis_a=(0.0, 0.0, 1.0),
+                                             axis_b=(0.0, 0.0, 1.0), lower=-0.8, upper=0.8, flags=S.JOINT_FLAG_LIMITS))
+                else:
+                    sc.joints.append(S.Joint(S.JOINT_POINT, prev, b, anchor_a=anchor))
+                prev, anchor = b, (x, f(y - 0.25), z)
+    sc.add_body(S.Body(ball, pos=(-5.0, 5.75, 0.0), vel=(80.0, 0.0, 0.0),
+                       flags=S.BODY_FLAG_ALLOW_SLEEPING | S.BODY_FLAG_LINEAR_CAST))
+    return sc
+
+
+def test_cpp_facade_joints_and_ccd_match_python_api(kzg_lib):
+    """Joints (PointConstraint, HingeConstraint with limits) and a LinearCast body created through
+    the C++ facade step to the same state hash as the same scene through the Python API."""
+    import os
+    import subprocess
+    from kizuriphysics3d_gb300 import World, build
+    exe = os.path.join(build.OUT, "joints_example")
+    out = subprocess.run([exe, "3", "3", "6", "60"], capture_output=True, text=True, check=True).stdout
+    cpp_hash = int(out.split("hash")[1].split()[0], 16)
+    with World(_facade_joint_scene(3, 3, 6)) as w:
+        w.step_fixed(n=60)
+        assert w.compute_state_hash() == cpp_hash
+
+
 def test_hash_identical_run_to_run(kzg_lib):
     from kizuriphysics3d_gb300 import World, resolve, scenes
     sc = scenes.pile(800, seed=5, extent=4.0, y_range=(1.0, 12.0))
