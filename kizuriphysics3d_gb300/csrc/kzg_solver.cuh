@@ -555,8 +555,10 @@ __global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, Count
     }
 }
 
-// Islands that hold joints (launched only when the world has joints): one CTA each.
-__global__ void __launch_bounds__(kBigThreads, 1) k_solve_joint(SolveBufs S, Counters* cnt) {
+// Islands that hold joints (launched only when the world has joints): one CTA each.  Joint islands
+// are usually small (a chain, a ragdoll), so the CTAs are small and several share an SM.
+constexpr uint32_t kJointThreads = 128;
+__global__ void __launch_bounds__(kJointThreads) k_solve_joint(SolveBufs S, Counters* cnt) {
     __shared__ unsigned long long red[6];
     __shared__ uint32_t soff[kBigOffs + 1];
     const uint32_t nj = cnt->njisl;

@@ -1105,7 +1105,7 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     k_solve_big<<<152u, kBigThreads, 0, st>>>(SV, ctx.dcnt, kCtaBodiesMax);
     ctx.launches += 3;
     if (nj) {
-        k_solve_joint<<<152u, kBigThreads, 0, st>>>(SV, ctx.dcnt);
+        k_solve_joint<<<152u * 8u, kJointThreads, 0, st>>>(SV, ctx.dcnt);
         ++ctx.launches;
     }
     ctx.launches += mlp_after_solve(ctx, dt);
