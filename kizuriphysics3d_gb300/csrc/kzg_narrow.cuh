@@ -946,8 +946,13 @@ __device__ inline uint32_t collide(const ShapeTables& T, const Body& A, const Bo
 // in closed form (A's deepest point against the plane); every other pair by conservative
 // advancement: GJK distance at the current translation (tolerance 1e-4, 32 iterations), advance by
 // distance - tolerance, at most 64 steps.
+//
+// `cut` (optional, the bits of a non-negative float that only decreases): the caller keeps only
+// fractions below it, so the advancement stops once t / max_distance exceeds it (t never
+// decreases, so the fraction could only be larger); a kept result is the same as without it.
 __device__ inline bool cast_shape(const ShapeTables& T, const Body& A, const Vec3& direction, float max_distance,
-                                  const Body& B, float& fraction, Vec3& normal) {
+                                  const Body& B, float& fraction, Vec3& normal,
+                                  const volatile int* cut = nullptr) {
     const float dir_len = direction.len();
     if (dir_len < kEps) return false;
     const Vec3 dir = direction / dir_len;
@@ -974,6 +979,7 @@ __device__ inline bool cast_shape(const ShapeTables& T, const Body& A, const Vec
     const float tol = 1.0e-4f;
     float t = 0.0f;
     for (uint32_t it = 0; it < 64; ++it) {
+        if (cut && t / max_distance > __int_as_float(*cut)) return false;
         SupportMap map{&T, Body{A.s, A.q, A.t + dir * t}, B};
         GjkOut g;
         gjk(map, tol, 32, g);

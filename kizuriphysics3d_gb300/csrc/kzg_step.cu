@@ -735,8 +735,10 @@ struct CcdHit {
 
 // This lane's share of body i's candidates (j = lane, lane + nl, ...): the smallest fraction, the
 // first such j of the lane on a tie.
+// `best` (shared by the lanes working on body i): the smallest fraction any of them has found, as
+// int bits (fractions are >= 0), so a lane's advancement stops early once it cannot win.
 __device__ CcdHit ccd_scan(const ShapeTables& T, const DeviceBodies& b, uint32_t n, uint32_t i, const CcdBody& c,
-                           float dt, const float4* disp, uint32_t lane, uint32_t nl) {
+                           float dt, const float4* disp, uint32_t lane, uint32_t nl, int* best) {
     CcdHit h{1.0f, kNoHit, Vec3(0.0f, 1.0f, 0.0f)};
     for (uint32_t j = lane; j < n; j += nl) {
         if (!ccd_candidate(b, c, i, j)) continue;
@@ -749,11 +751,13 @@ __device__ CcdHit ccd_scan(const ShapeTables& T, const DeviceBodies& b, uint32_t
         }
         float frac;
         Vec3 nrm;
-        if (cast_shape(T, Body{c.sh, c.q0, c.t0}, c.dir, c.dist, Body{&T.shapes[b.shape[j]], qj, tj}, frac, nrm) &&
+        if (cast_shape(T, Body{c.sh, c.q0, c.t0}, c.dir, c.dist, Body{&T.shapes[b.shape[j]], qj, tj}, frac, nrm,
+                       best) &&
             frac < h.frac) {
             h.frac = frac;
             h.slot = j;
             h.n = nrm;
+            atomicMin(best, __float_as_int(frac));
         }
     }
     return h;
@@ -828,8 +832,12 @@ __global__ void k_ccd_round(ShapeTables T, DeviceBodies b, uint32_t n, const uin
     if (nd > kCcdMaxDeps) return;
     const bool wait = lane < nd && round[deps[k * kCcdMaxDeps + lane]] >= r;  // a predecessor not finished
     if (__any_sync(0xFFFFFFFFu, wait)) return;
+    __shared__ int s_best[kThreads / 32];
+    int* best = &s_best[threadIdx.x >> 5];
+    if (lane == 0) *best = __float_as_int(1.0f);
+    __syncwarp();
     const CcdBody c = ccd_body(T, b, i, dt);
-    CcdHit h = ccd_scan(T, b, n, i, c, dt, disp, lane, 32u);
+    CcdHit h = ccd_scan(T, b, n, i, c, dt, disp, lane, 32u, best);
     for (uint32_t off = 16; off > 0; off >>= 1) {
         CcdHit o;
         o.frac = __shfl_down_sync(0xFFFFFFFFu, h.frac, off);
@@ -853,6 +861,7 @@ __global__ void __launch_bounds__(kCcdThreads) k_ccd_serial(ShapeTables T, Devic
     __shared__ uint32_t s_slot[kCcdThreads];
     __shared__ float4 s_norm[kCcdThreads];
     __shared__ uint32_t s_slot_of[kCcdThreads];
+    __shared__ int s_best;
     const uint32_t tid = threadIdx.x;
     for (uint32_t k0 = 0; k0 < nlist; k0 += kCcdThreads) {
         __syncthreads();
@@ -866,8 +875,10 @@ __global__ void __launch_bounds__(kCcdThreads) k_ccd_serial(ShapeTables T, Devic
         for (uint32_t kk = 0; kk < kCcdThreads; ++kk) {
             const uint32_t i = s_slot_of[kk];
             if (i == kNoHit) continue;
+            if (tid == 0) s_best = __float_as_int(1.0f);
+            __syncthreads();
             const CcdBody c = ccd_body(T, b, i, dt);
-            const CcdHit h = ccd_scan(T, b, n, i, c, dt, disp, tid, kCcdThreads);
+            const CcdHit h = ccd_scan(T, b, n, i, c, dt, disp, tid, kCcdThreads, &s_best);
             s_frac[tid] = h.frac;
             s_slot[tid] = h.slot;
             s_norm[tid] = F4(h.n, 0.0f);
