@@ -104,7 +104,7 @@ def scene_with_state(sc, state):
 
 
 # ---------------------------------------------------------------------------------------------
-# algorithmic bytes (the roofline model)
+# algorithmic bytes (the roofline model): compulsory bytes per pair, point, constraint and body
 # ---------------------------------------------------------------------------------------------
 SHAPE_BYTES = {0: 4, 1: 12, 2: 8, 4: 192, 8: 16}
 
