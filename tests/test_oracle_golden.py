@@ -118,3 +118,24 @@ def test_known_answer_separated(oracle_lib):
     m = _collide(oracle_lib, _two_body_scene(S.Shape(S.SHAPE_BOX, [1, 1, 1, 0]), (0, 0, 0),
                                              S.Shape(S.SHAPE_BOX, [1, 1, 1, 0]), (10, 0, 0)))
     assert m.shape[0] == 0
+
+
+def test_oracle_joint_trigonometry_modes(oracle_lib):
+    """The oracle's joint trigonometry: the C library's float functions (default) reproduce the
+    reference trace; correctly rounded values (mode 1, the GPU kernels') give the same bits until
+    the first call where the two differ, several steps into the joints fixture.  (After that the
+    trajectories part quickly: the fixture's chain links press against each other.)"""
+    sc, steps, _, _ = FIXTURES["joints_mix"]
+    g = load_golden("joints_mix")
+    blob = oracle_blob(sc, golden_resolved(sc, g))
+    a = oracle_lib.OracleWorld(sc.to_bytes(), blob, oracle_lib.PAIRS_TREE)
+    b = oracle_lib.OracleWorld(sc.to_bytes(), blob, oracle_lib.PAIRS_TREE)
+    b.set_trig_mode(1)
+    first = None
+    for s in range(steps):
+        a.step(np.float32(sc.dt))
+        b.step(np.float32(sc.dt))
+        assert a.hash() == int(g["hashes"][s])
+        if first is None and a.hash() != b.hash():
+            first = s
+    assert first is not None and first >= 5
