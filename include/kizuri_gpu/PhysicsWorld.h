@@ -108,6 +108,7 @@ struct BodySettings {
     uint32_t objectLayer = 1, collisionMask = 0xFFFFFFFFu;
     bool allowSleeping = true, isSensor = false;
     MotionQuality motionQuality = MotionQuality::Discrete;
+    float ccdMotionThreshold = 0.0f;  // Body.h:70
     float massOverride = 0.0f, density = 1000.0f;
     uint32_t worldId = 0;  // independent worlds stepped together (batched scenes)
 };
@@ -116,13 +117,16 @@ struct SolverSettings {  // ContactSolver.h:67-82
     uint32_t velocityIterations = 16, positionIterations = 6;
     float baumgarte = 0.2f, penetrationSlop = 0.005f, restitutionThreshold = 1.0f, maxBiasVelocity = 3.0f;
     float warmStartFactor = 1.0f;
+    bool useSplitImpulse = true;  // read nowhere by the reference; accepted with either value
+    bool useSIMDSolver = true;    // false (scalar constraint-order sweep) is rejected: KZG_ERR_UNSUPPORTED
     bool useVelocityBias = false;
 };
 
 struct WorldSettings {  // PhysicsWorld.h:20-43 (the fields the accelerated step reads)
     Vec3 gravity{0.0f, -9.81f, 0.0f};
     SolverSettings solver;
-    bool allowSleeping = false;  // sleeping is outside the accelerated path
+    bool allowSleeping = true;    // the reference's default (PhysicsWorld.h:24)
+    float sleepTimeThreshold = 0.5f, sleepLinearThreshold = 0.05f, sleepAngularThreshold = 0.1f;
     bool useFixedTimestep = true;
     float fixedTimestep = (float)(1.0 / 60.0);
     uint32_t maxSubSteps = 4;
@@ -320,6 +324,9 @@ private:
         ws.warm_start = settings_.warmStart ? 1 : 0;
         ws.use_ccd = settings_.useCCD ? 1 : 0;
         ws.ccd_max_penetration = settings_.ccdMaxPenetration;
+        ws.sleep_time_threshold = settings_.sleepTimeThreshold;
+        ws.sleep_linear_threshold = settings_.sleepLinearThreshold;
+        ws.sleep_angular_threshold = settings_.sleepAngularThreshold;
         ss.velocity_iterations = settings_.solver.velocityIterations;
         ss.position_iterations = settings_.solver.positionIterations;
         ss.baumgarte = settings_.solver.baumgarte;
@@ -328,6 +335,8 @@ private:
         ss.max_bias_velocity = settings_.solver.maxBiasVelocity;
         ss.warm_start_factor = settings_.solver.warmStartFactor;
         ss.use_velocity_bias = settings_.solver.useVelocityBias ? 1 : 0;
+        ss.use_split_impulse = settings_.solver.useSplitImpulse ? 1 : 0;
+        ss.use_simd_solver = settings_.solver.useSIMDSolver ? 1 : 0;
         Check(kzg_set_world_settings(ctx_, &ws), ctx_);
         Check(kzg_set_solver_settings(ctx_, &ss), ctx_);
         if (!pending_.empty()) FlushBodies();
@@ -341,7 +350,8 @@ private:
     void FlushBodies() {
         const size_t n = pending_.size();
         std::vector<uint32_t> shape(n), motion(n), flags(n), layer(n), mask(n), world(n);
-        std::vector<float> pos(3 * n), rot(4 * n), lv(3 * n), av(3 * n), fr(n), rs(n), ld(n), ad(n), gf(n), ml(n), ma(n);
+        std::vector<float> pos(3 * n), rot(4 * n), lv(3 * n), av(3 * n), fr(n), rs(n), ld(n), ad(n), gf(n), ml(n), ma(n),
+            ccd(n);
         for (size_t i = 0; i < n; ++i) {
             const BodySettings& b = pending_[i];
             shape[i] = (uint32_t)b.shape; motion[i] = (uint32_t)b.motionType;
@@ -354,10 +364,11 @@ private:
             av[3 * i] = b.angularVelocity.x; av[3 * i + 1] = b.angularVelocity.y; av[3 * i + 2] = b.angularVelocity.z;
             fr[i] = b.friction; rs[i] = b.restitution; ld[i] = b.linearDamping; ad[i] = b.angularDamping;
             gf[i] = b.gravityFactor; ml[i] = b.maxLinearVelocity; ma[i] = b.maxAngularVelocity;
+            ccd[i] = b.ccdMotionThreshold;
         }
         kzg_body_soa soa{shape.data(), motion.data(), flags.data(), pos.data(), rot.data(), lv.data(), av.data(),
                          fr.data(), rs.data(), ld.data(), ad.data(), gf.data(), ml.data(), ma.data(), invMass_.data(),
-                         iil_.data(), layer.data(), mask.data(), world.data()};
+                         iil_.data(), layer.data(), mask.data(), world.data(), ccd.data()};
         uint32_t first = 0;
         Check(kzg_add_bodies(ctx_, (uint32_t)n, &soa, &first), ctx_);
         pending_.clear();

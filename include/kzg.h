@@ -78,12 +78,25 @@ typedef struct {
     int use_velocity_bias;
     int schedule; /* KZG_SCHEDULE_* */
     /* Residual-terminated velocity iterations (not in the reference, which always runs
-     * velocity_iterations): with residual_tolerance > 0 an island stops iterating once the largest
-     * velocity change |dImpulse| / effectiveMass that any of its rows applied in an iteration is
-     * <= residual_tolerance (m/s), after at most max_velocity_iterations iterations.  0 keeps the
+     * velocity_iterations).  The residual of one velocity iteration of an island is its relative
+     * impulse change: the sum over the island's batched contact points of |dImpulse| of the
+     * friction 1, friction 2 and normal rows in that iteration, divided by the sum over the same
+     * points of |normalImpulse| + |tangentImpulse1| + |tangentImpulse2| after it (both sums taken
+     * in 2^-20 N s fixed point, so they do not depend on the order of the additions; dimensionless).
+     * With residual_tolerance > 0 an island stops iterating once its residual is <=
+     * residual_tolerance, after at most max_velocity_iterations iterations.  0 keeps the
      * reference's fixed count. */
     float residual_tolerance;
     uint32_t max_velocity_iterations;
+    /* SolverSettings::useSplitImpulse (ContactSolver.h:75).  The reference declares it but reads it
+     * nowhere: the split-impulse bias pass runs whenever use_velocity_bias is 0.  Both values are
+     * accepted and behave the same, as in the reference. */
+    int use_split_impulse;
+    /* SolverSettings::useSIMDSolver (ContactSolver.h:77): 1 solves the velocity iterations over the
+     * reference's 4-wide first-fit batches (PhysicsWorld.cpp:677-722), the path this library
+     * accelerates.  0 (the reference's scalar constraint-order sweep) is rejected with
+     * KZG_ERR_UNSUPPORTED. */
+    int use_simd_solver;
 } kzg_solver_settings;
 
 /* Mirrors the WorldSettings fields the step reads (reference PhysicsWorld.h:20-43). */
@@ -94,6 +107,11 @@ typedef struct {
     int warm_start;         /* 0 reproduces the reference's KZ_NOWS switch (PhysicsWorld.cpp:493) */
     int use_ccd;            /* WorldSettings::useCCD: clamp LinearCast bodies' motion (PhysicsWorld.cpp:785-852) */
     float ccd_max_penetration; /* WorldSettings::ccdMaxPenetration */
+    /* WorldSettings::sleepTimeThreshold (s), sleepLinearThreshold (m/s), sleepAngularThreshold
+     * (rad/s) (PhysicsWorld.h:25-27), read by the sleeping pass when allow_sleeping is set. */
+    float sleep_time_threshold;
+    float sleep_linear_threshold;
+    float sleep_angular_threshold;
 } kzg_world_settings;
 
 /* One shape. params: sphere {r}; box {hx,hy,hz}; capsule {halfHeight, radius}
@@ -131,6 +149,9 @@ typedef struct {
     const uint32_t* object_layer;
     const uint32_t* collision_mask;
     const uint32_t* world_id; /* may be NULL */
+    /* BodySettings::ccdMotionThreshold (Body.h:70; may be NULL = 0): a LinearCast body whose step
+     * displacement is shorter than a positive threshold is not clamped (PhysicsWorld.cpp:807). */
+    const float* ccd_motion_threshold;
 } kzg_body_soa;
 
 /* Counters of the last step (reference WorldStats, PhysicsWorld.h:66-77, with honest stage
@@ -153,14 +174,18 @@ typedef struct {
      * constraint build + velocity integration; prepare + islands + batch schedule; solver kernel;
      * cache store + position integration; whole step. */
     float broadphase_ms, narrowphase_ms, constraints_ms, schedule_ms, solve_ms, integrate_ms, step_ms;
-    float final_residual; /* largest residual of any island's last velocity iteration (m/s) */
+    float final_residual; /* largest residual (relative impulse change, see kzg_solver_settings) of any
+                           * island's last velocity iteration */
 } kzg_stats;
 
 #define KZG_DEVERR_PAIRS 1u     /* pair buffer overflow */
 #define KZG_DEVERR_CACHE 2u     /* cache table full */
 #define KZG_DEVERR_EPA 4u       /* EPA polytope exceeded its face capacity */
 #define KZG_DEVERR_MANIFOLD 8u  /* a manifold produced more than 4 points */
-#define KZG_DEVERR_WAIT 16u     /* a bounded wait between the warps of a kernel gave up (step abandoned) */
+/* A bounded wait between the warps of a kernel gave up.  The waiting warp's work is then redone
+ * by its CTA after the wait, so the step completes with the same result: the bit is reported in
+ * kzg_stats.device_error and the step still returns KZG_OK. */
+#define KZG_DEVERR_WAIT 16u
 
 /* ---- lifecycle (PhysicsWorld ctor/dtor, PhysicsWorld.cpp:64-78) ----------------------------- */
 kzg_status kzg_create(const kzg_config* cfg, kzg_ctx** out);
@@ -224,15 +249,27 @@ kzg_status kzg_set_graph(kzg_ctx* ctx, int enabled);
 /* Launch shapes of the island work, all bit-identical in result: islands with at most
  * small_island_constraints constraints (<= 128) get one warp for their schedule, islands with at
  * most warp_island_bodies dynamic bodies (<= 384) one warp for their solve, larger ones a CTA.
- * kzg_autotune steps the world steps_per_candidate steps with each of a small set of choices,
- * keeps the fastest (by CUDA-event step time) and returns it; the world advances by all those
- * steps, exactly as plain stepping would.  No counterpart in the reference. */
+ * island_order is the island-to-CTA schedule: KZG_ISLANDS_IN_ORDER hands the islands to warps and
+ * CTAs in island order with a fixed stride; KZG_ISLANDS_LARGEST_FIRST hands them out from a shared
+ * counter, largest first (islands binned by the power of two of their constraint count), the
+ * longest-processing-time-first rule that evens out the load of worlds of very uneven size.
+ * kzg_autotune saves the world on the device, steps it steps_per_candidate steps from that same
+ * state with each of a small set of choices, restores it, keeps the fastest choice (by CUDA-event
+ * step time) and returns it: the world is left exactly as it was.  No counterpart in the
+ * reference. */
+#define KZG_ISLANDS_IN_ORDER 0u
+#define KZG_ISLANDS_LARGEST_FIRST 1u
 typedef struct {
     uint32_t small_island_constraints;
     uint32_t warp_island_bodies;
     float step_ms; /* out: mean step time of this choice during kzg_autotune */
+    uint32_t island_order; /* KZG_ISLANDS_* */
 } kzg_tuning;
 kzg_status kzg_set_tuning(kzg_ctx* ctx, const kzg_tuning* t);
+/* Poll limit of the bounded in-kernel waits (default 2^26 polls, over 8 s): past it a wait
+ * gives up and raises KZG_DEVERR_WAIT (see above).  A small limit makes the give-up path run on
+ * purpose, which is how it is tested; 0 restores the default.  No counterpart in the reference. */
+kzg_status kzg_set_wait_limit(kzg_ctx* ctx, uint32_t polls);
 kzg_status kzg_get_tuning(kzg_ctx* ctx, kzg_tuning* t);
 kzg_status kzg_autotune(kzg_ctx* ctx, float dt, uint32_t steps_per_candidate, kzg_tuning* best);
 

@@ -34,12 +34,14 @@ class KzgSolverSettings(ctypes.Structure):
     _fields_ = [("velocity_iterations", u32), ("position_iterations", u32), ("baumgarte", f32),
                 ("penetration_slop", f32), ("restitution_threshold", f32), ("max_bias_velocity", f32),
                 ("warm_start_factor", f32), ("use_velocity_bias", ctypes.c_int), ("schedule", ctypes.c_int),
-                ("residual_tolerance", f32), ("max_velocity_iterations", u32)]
+                ("residual_tolerance", f32), ("max_velocity_iterations", u32), ("use_split_impulse", ctypes.c_int),
+                ("use_simd_solver", ctypes.c_int)]
 
 
 class KzgWorldSettings(ctypes.Structure):
     _fields_ = [("gravity", f32 * 3), ("fixed_timestep", f32), ("allow_sleeping", ctypes.c_int),
-                ("warm_start", ctypes.c_int), ("use_ccd", ctypes.c_int), ("ccd_max_penetration", f32)]
+                ("warm_start", ctypes.c_int), ("use_ccd", ctypes.c_int), ("ccd_max_penetration", f32),
+                ("sleep_time_threshold", f32), ("sleep_linear_threshold", f32), ("sleep_angular_threshold", f32)]
 
 
 class KzgShapeDesc(ctypes.Structure):
@@ -52,11 +54,12 @@ class KzgBodySoa(ctypes.Structure):
                                    "angular_velocity", "friction", "restitution", "linear_damping",
                                    "angular_damping", "gravity_factor", "max_linear_velocity",
                                    "max_angular_velocity", "inv_mass", "inv_inertia_local", "object_layer",
-                                   "collision_mask", "world_id")]
+                                   "collision_mask", "world_id", "ccd_motion_threshold")]
 
 
 class KzgTuning(ctypes.Structure):
-    _fields_ = [("small_island_constraints", u32), ("warp_island_bodies", u32), ("step_ms", f32)]
+    _fields_ = [("small_island_constraints", u32), ("warp_island_bodies", u32), ("step_ms", f32),
+                ("island_order", u32)]
 
 
 class KzgStats(ctypes.Structure):
@@ -139,6 +142,7 @@ def load(build_if_missing: bool = True):
     L.kzg_set_tuning.argtypes = [vp, P(KzgTuning)]
     L.kzg_get_tuning.argtypes = [vp, P(KzgTuning)]
     L.kzg_autotune.argtypes = [vp, f32, u32, P(KzgTuning)]
+    L.kzg_set_wait_limit.argtypes = [vp, u32]
     L.kzg_mlp_set_params.argtypes = [vp, vp, vp, vp]
     L.kzg_mlp_get_params.argtypes = [vp, vp, vp, vp]
     L.kzg_mlp_enable.argtypes = [vp, ctypes.c_int]

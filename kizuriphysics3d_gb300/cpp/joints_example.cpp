@@ -21,6 +21,7 @@ int main(int argc, char** argv) {
         WorldSettings& ws = world.GetSettings();
         ws.solver.velocityIterations = 10;
         ws.solver.positionIterations = 2;
+        ws.allowSleeping = false;  // as the Python API's scenes it is compared with
         const int plane = world.AddShape(Shape::Plane({0, 1, 0}, 0.0f));
         const int hook = world.AddShape(Shape::Box({0.1f, 0.1f, 0.1f}));
         const int link = world.AddShape(Shape::Box({0.1f, 0.25f, 0.1f}));

@@ -122,6 +122,8 @@ kzg_status alloc_all(Ctx* ctx) {
     CK(dalloc(&ctx->con_lb, P));
     CK(dalloc(&ctx->isl_small, P));
     CK(dalloc(&ctx->isl_large, P));
+    CK(dalloc(&ctx->isl_order, P));
+    CK(dalloc(&ctx->isl_bins, 64));
     CK(dalloc(&ctx->miss_rows, R));
     CK(dalloc(&ctx->miss_prior, R));
     CK(configure_kernels());
@@ -157,7 +159,7 @@ void free_all(Ctx* ctx) {
                     ctx->wl_list, ctx->vl_list, ctx->bl_list, ctx->wl_off, ctx->vl_off, ctx->bl_off, ctx->isl_meta,
                     ctx->c_key, ctx->c_np, ctx->c_pos, ctx->c_imp, ctx->dcnt, ctx->cub_tmp, ctx->hash_words,
                     ctx->body_stamp, ctx->body_loc, ctx->isl_bodies, ctx->con_la, ctx->con_lb, ctx->isl_small,
-                    ctx->isl_large, ctx->miss_rows, ctx->miss_prior,
+                    ctx->isl_large, ctx->isl_order, ctx->isl_bins, ctx->miss_rows, ctx->miss_prior,
                     ctx->shapes, ctx->hull_verts, ctx->face_sizes, ctx->face_idx};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -251,6 +253,9 @@ void kzg_default_settings(kzg_world_settings* ws, kzg_solver_settings* ss) {
         ws->warm_start = 1;
         ws->use_ccd = 1;                 // WorldSettings defaults, PhysicsWorld.h:39-42
         ws->ccd_max_penetration = 0.01f;
+        ws->sleep_time_threshold = 0.5f;  // PhysicsWorld.h:25-27
+        ws->sleep_linear_threshold = 0.05f;
+        ws->sleep_angular_threshold = 0.1f;
     }
     if (ss) {  // SolverSettings defaults, ContactSolver.h:67-82
         ss->velocity_iterations = 16;
@@ -264,6 +269,8 @@ void kzg_default_settings(kzg_world_settings* ws, kzg_solver_settings* ss) {
         ss->schedule = KZG_SCHEDULE_REFERENCE;
         ss->residual_tolerance = 0.0f;
         ss->max_velocity_iterations = 64;
+        ss->use_split_impulse = 1;
+        ss->use_simd_solver = 1;
     }
 }
 
@@ -357,6 +364,10 @@ kzg_status kzg_set_solver_settings(kzg_ctx* k, const kzg_solver_settings* s) {
     if (s->schedule != KZG_SCHEDULE_REFERENCE) {
         k->c.err = "unknown solver schedule";
         return KZG_ERR_INVALID;
+    }
+    if (!s->use_simd_solver) {
+        k->c.err = "SolverSettings::useSIMDSolver = false (the scalar constraint-order sweep) is outside the accelerated path";
+        return KZG_ERR_UNSUPPORTED;
     }
     if (!(s->residual_tolerance >= 0.0f) || (s->residual_tolerance > 0.0f && s->max_velocity_iterations == 0)) {
         k->c.err = "residual_tolerance must be >= 0, with max_velocity_iterations >= 1 when it is > 0";
@@ -464,7 +475,7 @@ kzg_status kzg_add_bodies(kzg_ctx* k, uint32_t n, const kzg_body_soa* b, uint32_
         p0[i] = make_float4(f(b->linear_damping, i, 0.05f), f(b->angular_damping, i, 0.05f),
                             f(b->gravity_factor, i, 1.0f), f(b->max_linear_velocity, i, 500.0f));
         p1[i] = make_float4(f(b->max_angular_velocity, i, 50.0f), f(b->friction, i, 0.5f), f(b->restitution, i, 0.0f),
-                            0.0f);
+                            f(b->ccd_motion_threshold, i, 0.0f));
         const float* L = b->inv_inertia_local + 9 * i;
         Mat3 IL{Vec3(L[0], L[1], L[2]), Vec3(L[3], L[4], L[5]), Vec3(L[6], L[7], L[8])};
         for (int c = 0; c < 3; ++c) iil[3 * i + c] = make_float4(L[3 * c], L[3 * c + 1], L[3 * c + 2], 0.0f);
@@ -550,11 +561,19 @@ kzg_status kzg_step(kzg_ctx* k, float dt, uint32_t nsteps) {
 kzg_status kzg_set_tuning(kzg_ctx* k, const kzg_tuning* t) {
     if (check(k) || !t) return KZG_ERR_INVALID;
     if (t->small_island_constraints == 0 || t->small_island_constraints > 128 || t->warp_island_bodies == 0 ||
-        t->warp_island_bodies > 384) {
-        k->c.err = "kzg_tuning: small_island_constraints in [1, 128], warp_island_bodies in [1, 384]";
+        t->warp_island_bodies > 384 || t->island_order > KZG_ISLANDS_LARGEST_FIRST) {
+        k->c.err = "kzg_tuning: small_island_constraints in [1, 128], warp_island_bodies in [1, 384], "
+                   "island_order KZG_ISLANDS_*";
         return KZG_ERR_INVALID;
     }
     k->c.tune = *t;
+    k->c.graph_dirty = true;
+    return KZG_OK;
+}
+
+kzg_status kzg_set_wait_limit(kzg_ctx* k, uint32_t polls) {
+    if (check(k)) return KZG_ERR_INVALID;
+    k->c.wait_limit = polls ? polls : kDefaultWaitLimit;
     k->c.graph_dirty = true;
     return KZG_OK;
 }
@@ -565,38 +584,95 @@ kzg_status kzg_get_tuning(kzg_ctx* k, kzg_tuning* t) {
     return KZG_OK;
 }
 
+namespace {
+// Device copy of everything a step changes that outlives the step (body state, world inertia, fat
+// bounds, the manifold cache and its entry count, the joints), so that the tuner can time every
+// candidate from one state and leave the world as it found it.
+struct DeviceBackup {
+    std::vector<std::pair<void*, size_t>> regions;
+    uint8_t* mem = nullptr;
+
+    cudaError_t save(Ctx& c) {
+        const size_t nb = c.nbodies, H = c.cfg.max_cache_entries;
+        DeviceBodies& b = c.b;
+        for (float4* p : {b.pos, b.rot, b.lv, b.av, b.plv, b.pav, b.force, b.torque, b.fat_mn, b.fat_mx})
+            regions.push_back({p, sizeof(float4) * nb});
+        regions.push_back({b.iiw, sizeof(float4) * 3 * nb});
+        regions.push_back({c.c_key, sizeof(unsigned long long) * H});
+        regions.push_back({c.c_np, sizeof(uint32_t) * H});
+        regions.push_back({c.c_pos, sizeof(float4) * 4 * H});
+        regions.push_back({c.c_imp, sizeof(float4) * 4 * H});
+        regions.push_back({&c.dcnt->cache_entries, sizeof(uint32_t)});
+        if (c.njoints) regions.push_back({c.joints, joint_record_bytes() * c.njoints});
+        size_t total = 0;
+        for (auto& r : regions) total += (r.second + 255) & ~size_t(255);
+        cudaError_t e = cudaMalloc((void**)&mem, total ? total : 1);
+        if (e != cudaSuccess) return e;
+        return copy(c, true);
+    }
+    cudaError_t copy(Ctx& c, bool to_backup) {
+        size_t off = 0;
+        for (auto& r : regions) {
+            void* dst = to_backup ? (void*)(mem + off) : r.first;
+            const void* src = to_backup ? r.first : (const void*)(mem + off);
+            cudaError_t e = cudaMemcpyAsync(dst, src, r.second, cudaMemcpyDeviceToDevice, c.stream);
+            if (e != cudaSuccess) return e;
+            off += (r.second + 255) & ~size_t(255);
+        }
+        return cudaStreamSynchronize(c.stream);
+    }
+    ~DeviceBackup() {
+        if (mem) cudaFree(mem);
+    }
+};
+}  // namespace
+
 kzg_status kzg_autotune(kzg_ctx* k, float dt, uint32_t steps_per_candidate, kzg_tuning* best) {
     if (check(k) || !(dt > 0.0f) || steps_per_candidate == 0) return KZG_ERR_INVALID;
     Ctx* ctx = &k->c;
     CK(cudaSetDevice(ctx->device));
     kzg_status s = finalize_bodies(k);
     if (s != KZG_OK) return s;
+    const kzg_tuning before = ctx->tune;
+    const bool logging = ctx->mlp.logging;
+    ctx->mlp.logging = false;  // the tuning steps are not part of the world's history
+    DeviceBackup backup;
+    CK(backup.save(*ctx));
     const uint32_t small[3] = {32u, 64u, 128u}, warp[3] = {128u, 256u, 384u};
+    const uint32_t orders[2] = {KZG_ISLANDS_IN_ORDER, KZG_ISLANDS_LARGEST_FIRST};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    kzg_tuning win{128u, 384u, 1e30f};
-    for (uint32_t a = 0; a < 3 && s == KZG_OK; ++a)
-        for (uint32_t b = 0; b < 3 && s == KZG_OK; ++b) {
-            kzg_tuning t{small[a], warp[b], 0.0f};
-            ctx->tune = t;
-            ctx->graph_dirty = true;
-            s = step_canonical(*ctx, dt, 1);  // first step of a choice: graph capture, not timed
-            if (s != KZG_OK) break;
-            cudaEventRecord(e0, ctx->stream);
-            s = step_canonical(*ctx, dt, steps_per_candidate);
-            cudaEventRecord(e1, ctx->stream);
-            cudaEventSynchronize(e1);
-            float ms = 0.0f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            t.step_ms = ms / (float)steps_per_candidate;
-            if (t.step_ms < win.step_ms) win = t;
-        }
+    kzg_tuning win{before.small_island_constraints, before.warp_island_bodies, 1e30f, before.island_order};
+    for (uint32_t o = 0; o < 2 && s == KZG_OK; ++o)
+        for (uint32_t a = 0; a < 3 && s == KZG_OK; ++a)
+            for (uint32_t b = 0; b < 3 && s == KZG_OK; ++b) {
+                kzg_tuning t{small[a], warp[b], 0.0f, orders[o]};
+                ctx->tune = t;
+                ctx->graph_dirty = true;
+                if (backup.copy(*ctx, false) != cudaSuccess) { s = KZG_ERR_CUDA; break; }
+                s = step_canonical(*ctx, dt, 1);  // first step of a choice: graph capture, not timed
+                if (s != KZG_OK) break;
+                cudaEventRecord(e0, ctx->stream);
+                s = step_canonical(*ctx, dt, steps_per_candidate);
+                cudaEventRecord(e1, ctx->stream);
+                cudaEventSynchronize(e1);
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                t.step_ms = ms / (float)steps_per_candidate;
+                if (t.step_ms < win.step_ms) win = t;
+            }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (s != KZG_OK) return s;
-    ctx->tune = win;
+    const cudaError_t restored = backup.copy(*ctx, false);
+    ctx->mlp.logging = logging;
     ctx->graph_dirty = true;
+    if (s != KZG_OK) {
+        ctx->tune = before;
+        return s;
+    }
+    CK(restored);
+    ctx->tune = win;
     if (best) *best = win;
     return KZG_OK;
 }

@@ -25,7 +25,7 @@ namespace kzg {
 struct DeviceBodies {
     float4 *pos, *rot, *lv, *av, *plv, *pav, *force, *torque;
     float4 *iiw, *iil;    // 3 columns per body
-    float4 *prm0, *prm1;  // (linDamp, angDamp, gravityFactor, maxLin), (maxAng, friction, restitution, -)
+    float4 *prm0, *prm1;  // (linDamp, angDamp, gravityFactor, maxLin), (maxAng, friction, restitution, ccdMotionThreshold)
     float* inv_mass;
     uint32_t *shape, *motion, *flags, *layer, *mask, *world, *packed;
     float4 *aabb_mn, *aabb_mx;
@@ -61,6 +61,7 @@ struct Counters {  // device-side counters, copied back after each stage that si
     uint32_t res_bits;   // largest final residual (float bits, >= 0)
     uint32_t nmiss;      // contact points without a cached warm start (learned warm start / logging)
     uint32_t njisl;      // islands holding joints
+    uint32_t nx_sched_w, nx_sched_c, nx_solve_w, nx_solve_c;  // largest-first island order: next island to take
     uint32_t cache_entries;  // persists across steps
     uint32_t frame;          // step counter, advanced on the device by k_begin_step
 };
@@ -89,6 +90,8 @@ struct MlpState {
 };
 
 struct JointDev;  // kzg_joint.cuh
+
+constexpr uint32_t kDefaultWaitLimit = 1u << 26;
 
 struct Ctx {
     kzg_config cfg{};
@@ -177,6 +180,8 @@ struct Ctx {
     uint32_t* isl_bodies = nullptr;                             // per island dynamic bodies
     uint32_t *con_la = nullptr, *con_lb = nullptr;             // per constraint local body indices
     uint32_t *isl_small = nullptr, *isl_large = nullptr;       // islands by solve kernel
+    uint32_t* isl_order = nullptr;   // largest-first island order (KZG_ISLANDS_LARGEST_FIRST)
+    uint32_t* isl_bins = nullptr;    // its 32 size bins: counts, then cursors (64 words)
     uint32_t* miss_rows = nullptr;                              // rows without a cached warm start
     float4* miss_prior = nullptr;  // per miss: nearest cached point's impulses, pair's cached normal impulse per point
     MlpState mlp;
@@ -199,7 +204,8 @@ struct Ctx {
     uint32_t launches = 0;
 
     // launch-shape choices (kzg_set_tuning / kzg_autotune); every choice gives identical results
-    kzg_tuning tune{128u, 384u, 0.0f};
+    kzg_tuning tune{128u, 384u, 0.0f, KZG_ISLANDS_IN_ORDER};
+    uint32_t wait_limit = kDefaultWaitLimit;  // polls of the bounded in-kernel waits (kzg_set_wait_limit)
 
     // CUDA graph of one canonical step (kzg_set_graph); recaptured when dt or the configuration changes
     bool use_graph = false, graph_dirty = true, capturing = false;

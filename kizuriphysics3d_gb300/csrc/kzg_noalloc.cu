@@ -70,13 +70,16 @@ kzg_status fail(const char** error, const char* msg, kzg_status code) {
     return code;
 }
 
-bool device_readable(const void* p) {
+// Memory this device's kernels may read: device memory of this very device, or managed memory.
+// Device memory of another GPU is refused (without peer access a kernel reading it would fault).
+bool device_readable(const void* p, int dev) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 }  // namespace
@@ -107,18 +110,31 @@ extern "C" kzg_status kzg_state_hash_noalloc(const float* state, const uint32_t*
         }
         scratch = g_scratch_ptr[dev];
     }
-    if (n && (!state || !packed_ids || !device_readable(state) || !device_readable(packed_ids)))
-        return fail(error, "kzg_state_hash_noalloc: state and packed_ids must be device pointers", KZG_ERR_INVALID);
+    if (n && (!state || !packed_ids || !device_readable(state, dev) || !device_readable(packed_ids, dev)))
+        return fail(error, "kzg_state_hash_noalloc: state and packed_ids must be device pointers of the current device",
+                    KZG_ERR_INVALID);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (n) k_hash_words_state13<<<(n + 255) / 256, 256, 0, s>>>(state, packed_ids, n, scratch);
-    k_fnv1a_fold<<<1, 32, 0, s>>>(scratch, size_t(kWordsPerBody) * n, scratch + kResult);
-    unsigned long long h = 0;
-    if (cudaGetLastError() != cudaSuccess ||
-        cudaMemcpyAsync(&h, scratch + kResult, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess) {
-        cudaGetLastError();
-        return fail(error, "kzg_state_hash_noalloc: a CUDA launch or copy failed", KZG_ERR_CUDA);
+    // Launched through cudaLaunchKernel so that each launch's own status is checked, not an error an
+    // earlier call left on this thread.
+    cudaError_t e = cudaSuccess;
+    if (n) {
+        uint32_t nn = n;
+        unsigned long long* w = scratch;
+        void* args[] = {(void*)&state, (void*)&packed_ids, (void*)&nn, (void*)&w};
+        e = cudaLaunchKernel((const void*)k_hash_words_state13, dim3((n + 255) / 256), dim3(256), args, 0, s);
     }
+    if (e == cudaSuccess) {
+        const unsigned long long* w = scratch;
+        size_t count = size_t(kWordsPerBody) * n;
+        unsigned long long* res = scratch + kResult;
+        void* args[] = {(void*)&w, (void*)&count, (void*)&res};
+        e = cudaLaunchKernel((const void*)k_fnv1a_fold, dim3(1), dim3(32), args, 0, s);
+    }
+    if (e != cudaSuccess) return fail(error, "kzg_state_hash_noalloc: a kernel launch failed", KZG_ERR_CUDA);
+    unsigned long long h = 0;
+    if (cudaMemcpyAsync(&h, scratch + kResult, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return fail(error, "kzg_state_hash_noalloc: the result copy failed", KZG_ERR_CUDA);
     *out = h;
     return KZG_OK;
 }

@@ -52,6 +52,8 @@ struct SchedBufs {
     uint32_t small_cons;   // islands with at most this many constraints: warp schedule (<= kSchedSmallCons)
     uint32_t warp_bodies;  // islands with at most this many dynamic bodies: warp solve (<= kWarpBodies)
     const uint32_t* jflag; // per island: 1 when joints share it (solved with them by k_solve_big), or null
+    uint32_t spin_limit;   // polls before the streamed velocity sweep's wait gives up
+    const uint32_t* order; // largest-first island order taken from shared counters, or null: island order
 };
 
 struct SchedShared {  // per island scratch living in shared memory
@@ -633,8 +635,8 @@ __device__ void level_sweep(const SchedBufs& S, SchedShared* sh, uint32_t sweep,
 // below sh->ff_final are full and final, so their points sit at 4 * batch + slot in batch order and
 // can be levelled while the first fit goes on; once it is done the rest (batches not full) follow.
 // Returns false - the caller then runs the sweep itself - if the first fit gave up.  The wait is
-// bounded: past kStreamSpins polls it raises KZG_DEVERR_WAIT and gives up.
-constexpr uint32_t kStreamSpins = 1u << 26;
+// bounded: past S.spin_limit polls it raises KZG_DEVERR_WAIT and gives up (the caller's sweep then
+// gives the same levels, so the step's result is unchanged).
 __device__ bool velocity_stream(const SchedBufs& S, Counters* cnt, SchedShared* sh, uint32_t* last, uint32_t rb,
                                 uint32_t base, uint32_t lane) {
     const unsigned full = 0xffffffffu;
@@ -654,7 +656,7 @@ __device__ bool velocity_stream(const SchedBufs& S, Counters* cnt, SchedShared* 
             done = __shfl_sync(full, done, 0);
             fin = __shfl_sync(full, fin, 0);
             if (done || fin >= b + 8) break;
-            if (++spins > kStreamSpins) {
+            if (++spins > S.spin_limit) {
                 if (lane == 0) atomicOr(&cnt->error, KZG_DEVERR_WAIT);
                 return false;
             }
@@ -1020,7 +1022,14 @@ __global__ void __launch_bounds__(128, 8) k_schedule_warp(SchedBufs S, Counters*
     __shared__ uint32_t last[4][kSchedWarpBodies];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t n = cnt->nislands;
-    for (uint32_t isl = blockIdx.x * 4 + warp; isl < n; isl += gridDim.x * 4) {
+    for (uint32_t k = blockIdx.x * 4 + warp;; k += gridDim.x * 4) {
+        if (S.order) {  // largest first: the next island from the shared counter
+            uint32_t t = 0;
+            if (lane == 0) t = atomicAdd(&cnt->nx_sched_w, 1u);
+            k = __shfl_sync(0xffffffffu, t, 0);
+        }
+        if (k >= n) break;
+        const uint32_t isl = S.order ? S.order[k] : k;
         if (S.isl_start[isl + 1] - S.isl_start[isl] > S.small_cons) continue;
         schedule_island(S, cnt, isl, lane, 32u, &sh[warp], tmp[warp], last[warp], kSchedWarpBodies, false,
                         SchedWarpSync{});
@@ -1033,8 +1042,17 @@ __global__ void __launch_bounds__(256, 1) k_schedule_cta(SchedBufs S, Counters* 
     extern __shared__ uint32_t last_sm[];
     __shared__ SchedShared sh;
     __shared__ uint32_t tmp[33];
+    __shared__ uint32_t next;
     const uint32_t n = cnt->nislands;
-    for (uint32_t isl = blockIdx.x; isl < n; isl += gridDim.x) {
+    for (uint32_t k = blockIdx.x;; k += gridDim.x) {
+        if (S.order) {  // largest first: the next island from the shared counter
+            if (threadIdx.x == 0) next = atomicAdd(&cnt->nx_sched_c, 1u);
+            __syncthreads();
+            k = next;
+            __syncthreads();
+        }
+        if (k >= n) break;
+        const uint32_t isl = S.order ? S.order[k] : k;
         if (S.isl_start[isl + 1] - S.isl_start[isl] <= S.small_cons) continue;
         schedule_island(S, cnt, isl, threadIdx.x, blockDim.x, &sh, tmp, last_sm, kSchedCtaBodies, true, SchedCtaSync{});
     }

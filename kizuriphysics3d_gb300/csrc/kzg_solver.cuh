@@ -47,7 +47,19 @@ struct SolveBufs {
     const unsigned long long* jkeys;   // joints sorted by island root, then joint index
     const uint2* jisl;                 // per joint island: its range of jkeys
     const uint32_t* jisl_cisl;         // per joint island: its contact island, or kNone
+    const uint32_t* order;   // largest-first island order taken from shared counters, or null (the lists)
+    const uint32_t* jflag;   // per island: 1 when joints share it, or null
+    uint32_t warp_bodies;    // islands with at most this many dynamic bodies: warp solve
 };
+
+// The solve kernel an island goes to (the lists the schedule appends to follow the same rule).
+__device__ __forceinline__ bool warp_solved(const SolveBufs& S, uint32_t isl) {
+    return !(S.jflag && S.jflag[isl]) && S.meta[4 * isl + 3] <= S.warp_bodies;
+}
+__device__ __forceinline__ bool cta_solved(const SolveBufs& S, uint32_t isl, uint32_t smem_bodies) {
+    const uint32_t nloc = S.meta[4 * isl + 3];
+    return !(S.jflag && S.jflag[isl]) && nloc > S.warp_bodies && nloc <= smem_bodies;
+}
 
 // Velocity storage of one island: staged in shared memory (local index) or read/written in place
 // (global memory, body slot).  Bodies that are not dynamic are never written; their velocity is
@@ -403,6 +415,18 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_solve_warp(SolveBufs S,
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     float4* sv = smem + warp * 2u * kWarpBodies;
     float4* sw = sv + kWarpBodies;
+    if (S.order) {  // largest first, from a shared counter
+        const uint32_t n = cnt->nislands;
+        for (;;) {
+            uint32_t k = 0;
+            if (lane == 0) k = atomicAdd(&cnt->nx_solve_w, 1u);
+            k = __shfl_sync(0xffffffffu, k, 0);
+            if (k >= n) break;
+            const uint32_t isl = S.order[k];
+            if (warp_solved(S, isl)) solve_island_shared(S, isl, sv, sw, lane, 32u, WarpSync{}, cnt);
+        }
+        return;
+    }
     const uint32_t n = cnt->nsmall;
     for (uint32_t idx = blockIdx.x * kWarpsPerBlock + warp; idx < n; idx += gridDim.x * kWarpsPerBlock)
         solve_island_shared(S, S.small_list[idx], sv, sw, lane, 32u, WarpSync{}, cnt);
@@ -412,6 +436,21 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_solve_warp(SolveBufs S,
 __global__ void __launch_bounds__(kCtaThreads) k_solve_cta(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
     extern __shared__ float4 smem[];
     __shared__ unsigned long long red[6];
+    __shared__ uint32_t next;
+    if (S.order) {  // largest first, from a shared counter
+        const uint32_t n = cnt->nislands;
+        for (;;) {
+            if (threadIdx.x == 0) next = atomicAdd(&cnt->nx_solve_c, 1u);
+            __syncthreads();
+            const uint32_t k = next;
+            __syncthreads();
+            if (k >= n) break;
+            const uint32_t isl = S.order[k];
+            if (cta_solved(S, isl, smem_bodies))
+                solve_island_shared(S, isl, smem, smem + smem_bodies, threadIdx.x, blockDim.x, CtaSync{red}, cnt);
+        }
+        return;
+    }
     const uint32_t n = cnt->nlarge;
     for (uint32_t idx = blockIdx.x; idx < n; idx += gridDim.x) {
         const uint32_t isl = S.large_list[idx];

@@ -540,6 +540,33 @@ __global__ void k_island_starts(Counters* cnt, const uint32_t* __restrict__ head
     }
 }
 
+
+// Largest-first island order (KZG_ISLANDS_LARGEST_FIRST): islands binned by the power of two of
+// their constraint count and listed bin by bin from the largest down; inside a bin the order is
+// whatever the atomics give (islands share no dynamic body, so any order gives the same bits).
+__global__ void k_island_bin_count(const Counters* cnt, const uint32_t* __restrict__ start, uint32_t* bins) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cnt->nislands) return;
+    atomicAdd(&bins[31 - __clz(start[i + 1] - start[i])], 1u);  // every island has a constraint
+}
+__global__ void k_island_bin_offsets(uint32_t* bins) {  // one warp; cursors in bins[32..64)
+    const uint32_t lane = threadIdx.x;
+    const uint32_t c = bins[31 - lane];  // lane 0: the largest bin
+    uint32_t x = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    bins[32 + 31 - lane] = x - c;
+}
+__global__ void k_island_bin_scatter(const Counters* cnt, const uint32_t* __restrict__ start, uint32_t* bins,
+                                     uint32_t* order) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cnt->nislands) return;
+    order[atomicAdd(&bins[32 + 31 - __clz(start[i + 1] - start[i])], 1u)] = i;
+}
+
 }  // namespace kzg
 
 #include "kzg_solver.cuh"
@@ -673,7 +700,8 @@ __device__ __forceinline__ bool casts_linear(const DeviceBodies& b, uint32_t i) 
 }
 
 // Continuous collision of LinearCast bodies (PhysicsWorld::ClampMotionCCD, PhysicsWorld.cpp:785-802
-// and 804-852; the per-body CCD motion threshold is 0, its default).  The reference runs it inside
+// and 804-852; a displacement shorter than the body's positive ccdMotionThreshold is left as it is).
+// The reference runs it inside
 // the position loop, body by body in slot order, so a body sees the bodies before it already
 // moved.  Per body: candidates are the bodies whose fat bounds overlap the swept bounds grown by
 // 0.1 (not itself, not a sensor, layer and mask both ways), each placed where that loop has it at
@@ -790,7 +818,8 @@ __global__ void k_ccd_init(DeviceBodies b, uint32_t n, const uint32_t* __restric
     if (k >= nlist) return;
     const uint32_t i = list[k];
     const Vec3 d = V3(b.lv[i]) * dt;
-    if (casts_linear(b, i) && d.len() > max_pen) {
+    const float dist = d.len(), thr = b.prm1[i].w;  // per-body ccdMotionThreshold (PhysicsWorld.cpp:806-807)
+    if (casts_linear(b, i) && dist > max_pen && !(thr > 0.0f && dist < thr)) {
         round[i] = kPending;
     } else {
         if (casts_linear(b, i)) disp[i] = F4(d, 0.0f);
@@ -1079,6 +1108,14 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     tb = ctx.cub_tmp_bytes;
     KZG_CK(cub::DeviceScan::ExclusiveSum(ctx.cub_tmp, tb, ctx.isl_head, ctx.isl_pts, (int)P, st));
     k_island_starts<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_head, ctx.isl_pts, ctx.isl_start);
+    const bool lpt = ctx.tune.island_order == KZG_ISLANDS_LARGEST_FIRST;
+    if (lpt) {
+        KZG_CK(cudaMemsetAsync(ctx.isl_bins, 0, sizeof(uint32_t) * 32, st));
+        k_island_bin_count<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_start, ctx.isl_bins);
+        k_island_bin_offsets<<<1, 32, 0, st>>>(ctx.isl_bins);
+        k_island_bin_scatter<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_start, ctx.isl_bins, ctx.isl_order);
+        ctx.launches += 3;
+    }
     if (nj) {
         k_joint_keys<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, nj, ctx.uf, ctx.jkeys);
         tb = ctx.cub_tmp_bytes;
@@ -1094,7 +1131,8 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
                  ctx.ids_tmp, ctx.lvl_tmp, ctx.lvl_count, ctx.wl_list, ctx.vl_list, ctx.bl_list, ctx.wl_off,
                  ctx.vl_off, ctx.bl_off, ctx.isl_meta, ctx.isl_small, ctx.isl_large,
                  std::min(ctx.tune.small_island_constraints, kSchedSmallCons),
-                 std::min(ctx.tune.warp_island_bodies, kWarpBodies), nj ? ctx.jflag : nullptr};
+                 std::min(ctx.tune.warp_island_bodies, kWarpBodies), nj ? ctx.jflag : nullptr, ctx.wait_limit,
+                 lpt ? ctx.isl_order : nullptr};
     k_schedule_warp<<<152u * 16u, 128, 0, st>>>(SB, ctx.dcnt);
     k_schedule_cta<<<152u * 2u, 256, 3 * kSchedCtaBodies * sizeof(uint32_t), st>>>(SB, ctx.dcnt);
     ctx.launches += 17;  // prepare, union-find (3), island sort (4 CUB passes), heads, scan (2), starts, schedule (2)
@@ -1105,7 +1143,9 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
                  ctx.ss.position_iterations, ctx.ss.warm_start_factor, ctx.ss.use_velocity_bias,
                  ctx.ss.residual_tolerance, ctx.ss.max_velocity_iterations, ctx.brec, ctx.pk,
                  g_cluster_ok ? ctx.pk_cap : 0u, ctx.isl_con, ctx.cfg.max_pairs, ctx.cl_ids,
-                 nj ? ctx.joints : nullptr, ctx.jkeys_sorted, ctx.jisl, ctx.jisl_cisl};
+                 nj ? ctx.joints : nullptr, ctx.jkeys_sorted, ctx.jisl, ctx.jisl_cisl,
+                 lpt ? ctx.isl_order : nullptr, nj ? ctx.jflag : nullptr,
+                 std::min(ctx.tune.warp_island_bodies, kWarpBodies)};
     k_solve_warp<<<152u * 16u, kWarpsPerBlock * 32, kWarpsPerBlock * 2 * kWarpBodies * sizeof(float4), st>>>(SV, ctx.dcnt);
     k_solve_cta<<<152u * 2u, kCtaThreads, 2 * kCtaBodiesMax * sizeof(float4), st>>>(SV, ctx.dcnt, kCtaBodiesMax);
     if (g_cluster_ok) {
@@ -1183,7 +1223,8 @@ static kzg_status finish_stats(Ctx& ctx, uint32_t graph_steps = 0) {
         KZG_CK(cudaEventElapsedTime(&s.integrate_ms, ctx.ev[5], ctx.ev[6]));
         KZG_CK(cudaEventElapsedTime(&s.step_ms, ctx.ev[0], ctx.ev[6]));
     }
-    if (h.error) {
+    // A wait that gave up is a warning: its work was redone by the waiting kernel, the step is complete.
+    if (h.error & ~KZG_DEVERR_WAIT) {
         ctx.err = "device error word " + std::to_string(h.error) + " (see KZG_DEVERR_*)";
         return (h.error & (KZG_DEVERR_PAIRS | KZG_DEVERR_CACHE)) ? KZG_ERR_CAPACITY : KZG_ERR_DEVICE;
     }

@@ -56,7 +56,7 @@ WORLD_FLAG_VELOCITY_BIAS = 2
 WORLD_FLAG_NO_WARM_START = 4   # the reference's KZ_NOWS environment switch (PhysicsWorld.cpp:493)
 
 SCENE_MAGIC = 0x4353_5A4B  # 'KZSC'
-SCENE_VERSION = 1
+SCENE_VERSION = 2  # 2 adds the world's sleep thresholds and each body's CCD motion threshold; 1 is still read
 
 F32 = np.float32
 
@@ -94,6 +94,7 @@ class Body:
     layer: int = 1
     mask: int = 0xFFFFFFFF
     flags: int = BODY_FLAG_ALLOW_SLEEPING
+    ccd_motion_threshold: float = 0.0  # BodySettings::ccdMotionThreshold (Body.h:70)
 
 
 # Joint types (include/Kizuri/Constraint/Constraints.h:41-277)
@@ -160,6 +161,10 @@ class Scene:
     restitution_threshold: float = 1.0
     max_bias_velocity: float = 3.0
     warm_start_factor: float = 1.0
+    # WorldSettings sleep thresholds (PhysicsWorld.h:25-27), used with WORLD_FLAG_ALLOW_SLEEPING
+    sleep_time_threshold: float = 0.5
+    sleep_linear_threshold: float = 0.05
+    sleep_angular_threshold: float = 0.1
     shapes: List[Shape] = field(default_factory=list)
     bodies: List[Body] = field(default_factory=list)
     joints: List[Joint] = field(default_factory=list)
@@ -186,6 +191,8 @@ class Scene:
         out += struct.pack("<5f", f32(self.baumgarte), f32(self.penetration_slop),
                            f32(self.restitution_threshold), f32(self.max_bias_velocity),
                            f32(self.warm_start_factor))
+        out += struct.pack("<3f", f32(self.sleep_time_threshold), f32(self.sleep_linear_threshold),
+                           f32(self.sleep_angular_threshold))
         out += struct.pack("<I", len(self.shapes))
         for s in self.shapes:
             p = list(s.params) + [0.0] * (4 - len(s.params))
@@ -200,6 +207,7 @@ class Scene:
                 b.friction, b.restitution, b.linear_damping, b.angular_damping, b.gravity_factor,
                 b.max_linear_velocity, b.max_angular_velocity, b.density, b.mass_override)])
             out += struct.pack("<III", b.layer & 0xFFFFFFFF, b.mask & 0xFFFFFFFF, b.flags)
+            out += struct.pack("<f", f32(b.ccd_motion_threshold))
         if self.joints:  # optional trailing section
             out += struct.pack("<I", len(self.joints))
             for j in self.joints:
@@ -221,14 +229,16 @@ class Scene:
             return vals
 
         magic, version = take("<II")
-        if magic != SCENE_MAGIC or version != SCENE_VERSION:
-            raise ValueError("not a KZSC v1 scene")
+        if magic != SCENE_MAGIC or version not in (1, 2):
+            raise ValueError("not a KZSC v1/v2 scene")
         sc = Scene(name=name)
         gx, gy, gz, dt = take("<3ff")
         sc.gravity, sc.dt = (gx, gy, gz), dt
         sc.velocity_iterations, sc.position_iterations, sc.flags = take("<III")
         (sc.baumgarte, sc.penetration_slop, sc.restitution_threshold,
          sc.max_bias_velocity, sc.warm_start_factor) = take("<5f")
+        if version >= 2:
+            sc.sleep_time_threshold, sc.sleep_linear_threshold, sc.sleep_angular_threshold = take("<3f")
         (ns,) = take("<I")
         for _ in range(ns):
             t, p0, p1, p2, p3, n = take("<I4fI")
@@ -243,8 +253,9 @@ class Scene:
             v = take("<3f4f3f3f")
             m = take("<9f")
             layer, mask, flags = take("<III")
+            (thr,) = take("<f") if version >= 2 else (0.0,)
             sc.bodies.append(Body(shape, motion, v[0:3], v[3:7], v[7:10], v[10:13], *m,
-                                  layer=layer, mask=mask, flags=flags))
+                                  layer=layer, mask=mask, flags=flags, ccd_motion_threshold=thr))
         if off < len(data):
             (nj,) = take("<I")
             for _ in range(nj):
@@ -437,7 +448,8 @@ def merge_worlds(worlds: List[Scene]):
         raise ValueError("no worlds")
     first = worlds[0]
     keys = ("gravity", "dt", "velocity_iterations", "position_iterations", "flags", "baumgarte",
-            "penetration_slop", "restitution_threshold", "max_bias_velocity", "warm_start_factor")
+            "penetration_slop", "restitution_threshold", "max_bias_velocity", "warm_start_factor",
+            "sleep_time_threshold", "sleep_linear_threshold", "sleep_angular_threshold")
     out = Scene(name=f"{len(worlds)} worlds", **{k: getattr(first, k) for k in keys})
     ids = []
     for w, sc in enumerate(worlds):

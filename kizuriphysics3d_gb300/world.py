@@ -127,6 +127,9 @@ class World:
             ws.gravity[k] = float(np.float32(scene.gravity[k]))
         ws.allow_sleeping = int(bool(scene.flags & WORLD_FLAG_ALLOW_SLEEPING))
         ws.warm_start = 0 if scene.flags & WORLD_FLAG_NO_WARM_START else 1
+        ws.sleep_time_threshold = float(np.float32(scene.sleep_time_threshold))
+        ws.sleep_linear_threshold = float(np.float32(scene.sleep_linear_threshold))
+        ws.sleep_angular_threshold = float(np.float32(scene.sleep_angular_threshold))
         ss.velocity_iterations = scene.velocity_iterations
         ss.position_iterations = scene.position_iterations
         ss.baumgarte = scene.baumgarte
@@ -168,6 +171,7 @@ class World:
         soa.object_layer = col("layer", [b.layer for b in bodies], np.uint32)
         soa.collision_mask = col("mask", [b.mask for b in bodies], np.uint32)
         soa.world_id = col("world", world_ids if world_ids is not None else np.zeros(n), np.uint32)
+        soa.ccd_motion_threshold = col("ccdthr", [b.ccd_motion_threshold for b in bodies])
         first = ctypes.c_uint32()
         self._check(L.kzg_add_bodies(h, n, ctypes.byref(soa), ctypes.byref(first)))
         if getattr(scene, "joints", None):
@@ -220,8 +224,10 @@ class World:
         """Step through a captured CUDA graph (step_fixed(n) then launches n steps back to back)."""
         self._check(capi.load().kzg_set_graph(self._h, int(bool(enabled))))
 
-    def set_tuning(self, small_island_constraints: int, warp_island_bodies: int):
-        t = capi.KzgTuning(small_island_constraints, warp_island_bodies, 0.0)
+    def set_tuning(self, small_island_constraints: int, warp_island_bodies: int, island_order: int = 0):
+        """Launch shapes (bit-identical results): warp/CTA split points and the island-to-CTA order
+        (0 island order, 1 largest first)."""
+        t = capi.KzgTuning(small_island_constraints, warp_island_bodies, 0.0, island_order)
         self._check(capi.load().kzg_set_tuning(self._h, ctypes.byref(t)))
 
     def get_tuning(self) -> dict:
@@ -229,15 +235,21 @@ class World:
         self._check(capi.load().kzg_get_tuning(self._h, ctypes.byref(t)))
         return {n: getattr(t, n) for n, _ in capi.KzgTuning._fields_}
 
+    def set_wait_limit(self, polls: int):
+        """Poll limit of the bounded in-kernel waits (0 = the default 2^26)."""
+        self._check(capi.load().kzg_set_wait_limit(self._h, int(polls)))
+
     def autotune(self, steps_per_candidate: int = 3, dt: Optional[float] = None) -> dict:
-        """Pick the fastest launch shapes on the live world (advances it 10 x steps_per_candidate steps)."""
+        """Pick the fastest launch shapes, each timed from the world's current state; the world is
+        restored afterwards, so it does not advance."""
         t = capi.KzgTuning()
         self._check(capi.load().kzg_autotune(self._h, np.float32(self.dt if dt is None else dt),
                                              int(steps_per_candidate), ctypes.byref(t)))
         return {n: getattr(t, n) for n, _ in capi.KzgTuning._fields_}
 
     def set_residual(self, tolerance: float, max_iterations: int = 64):
-        """Residual-terminated velocity iterations (tolerance in m/s; 0 = the fixed count)."""
+        """Residual-terminated velocity iterations: an island stops once its relative impulse change
+        sum|dImpulse| / sum|impulse| of one iteration is <= tolerance (0 = the fixed count)."""
         self.set_solver(residual_tolerance=float(tolerance), max_velocity_iterations=int(max_iterations))
 
     # -- lifetime ----------------------------------------------------------------------------

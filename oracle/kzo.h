@@ -46,6 +46,10 @@ void kzo_set_residual(kzo_world* w, float tol, uint32_t cap);
 /* Joint trigonometry: 0 (default) the C library's float sinf/cosf/acosf/atan2f, as the reference
  * calls them; 1 the double-precision functions rounded to float, as the GPU evaluates them. */
 void kzo_set_trig_mode(kzo_world* w, int mode);
+/* 1: the manifold cache uses a 64-bit mixed slot function instead of the reference's (pa ^ pb) & mask.
+ * Results are identical (entries are found by key and never evicted); large worlds avoid the
+ * reference's clustered probe runs. */
+void kzo_set_cache_hash(kzo_world* w, int mixed);
 
 int kzo_step(kzo_world* w, float dt);
 

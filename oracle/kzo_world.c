@@ -80,6 +80,7 @@ struct kzo_world {
     /* settings (WorldSettings / SolverSettings) */
     v3 gravity;
     float fixed_dt, baumgarte, slop, rest_thresh, max_bias, ws_factor;
+    float sleep_time, sleep_lin, sleep_ang; /* WorldSettings sleep thresholds */
     uint32_t vel_iters, pos_iters;
     int vel_bias, no_ws, threads, pair_mode, sched_stats;
     float res_tol;     /* > 0: velocity iterations stop once the island's residual is <= res_tol */
@@ -93,6 +94,7 @@ struct kzo_world {
     int* shape;
     uint8_t *motion, *sensor;
     uint8_t* ccd;           /* MotionQuality::LinearCast */
+    float* ccd_thr;         /* BodySettings::ccdMotionThreshold (Body.h:70) */
     aabb* fat;              /* broad-phase fat bounds per body (the tree leaves' bounds, all pair modes) */
     int use_ccd;            /* WorldSettings::useCCD (default true) */
     float ccd_max_pen;      /* WorldSettings::ccdMaxPenetration (default 0.01) */
@@ -110,6 +112,7 @@ struct kzo_world {
     /* manifold cache */
     cache_t* cache;
     uint32_t cache_cap, cache_count, frame;
+    int cache_mix;  /* 1: mixed slot function (same results, no clustering) */
     /* per step */
     uint32_t* pairs; /* packed A, packed B */
     uint32_t npairs, pairs_cap;
@@ -470,10 +473,24 @@ static void canonical_pairs(kzo_world* w) {
 /* ----------------------------------------------------------------------------- */
 /* Manifold cache (PhysicsWorld.cpp:405-452)                                       */
 /* ----------------------------------------------------------------------------- */
+/* Home slot of a key: the reference's (pa ^ pb) & mask, or (kzo_set_cache_hash(w, 1)) a 64-bit mix.
+ * Entries are found by key and never evicted, so the slot function changes no result, only the
+ * probe lengths: the reference's one clusters neighbouring ids (long runs of consecutive slots)
+ * and makes large worlds quadratic. */
+static uint32_t cache_home(const kzo_world* w, uint64_t key, uint32_t mask) {
+    if (!w->cache_mix) return (uint32_t)(key ^ (key >> 32)) & mask;
+    key ^= key >> 33;
+    key *= 0xff51afd7ed558ccdull;
+    key ^= key >> 33;
+    key *= 0xc4ceb9fe1a85ec53ull;
+    key ^= key >> 33;
+    return (uint32_t)key & mask;
+}
+
 static cache_t* find_cached(kzo_world* w, uint64_t key) {
     if (w->cache_cap == 0) return NULL;
     uint32_t mask = w->cache_cap - 1;
-    uint32_t slot = (uint32_t)(key ^ (key >> 32)) & mask;
+    uint32_t slot = cache_home(w, key, mask);
     for (uint32_t p = 0; p < w->cache_cap; ++p) {
         cache_t* e = &w->cache[slot];
         if (e->key == key && e->frame != 0) return e;
@@ -491,7 +508,7 @@ static cache_t* get_or_create_cached(kzo_world* w, uint64_t key) {
         for (uint32_t i = 0; i < w->cache_cap; ++i) {
             cache_t* e = &w->cache[i];
             if (e->frame == 0) continue;
-            uint32_t slot = (uint32_t)(e->key ^ (e->key >> 32)) & mask;
+            uint32_t slot = cache_home(w, e->key, mask);
             while (nc[slot].frame != 0) slot = (slot + 1) & mask;
             nc[slot] = *e;
         }
@@ -500,7 +517,7 @@ static cache_t* get_or_create_cached(kzo_world* w, uint64_t key) {
         w->cache_cap = ncap;
     }
     uint32_t mask = w->cache_cap - 1;
-    uint32_t slot = (uint32_t)(key ^ (key >> 32)) & mask;
+    uint32_t slot = cache_home(w, key, mask);
     for (;;) {
         cache_t* e = &w->cache[slot];
         if (e->frame == 0) {
@@ -1246,6 +1263,7 @@ static void solve_island(kzo_world* w, uint32_t isl, uint32_t* out_batches, uint
 static void clamp_motion_ccd(kzo_world* w, int i, v3* disp) {
     const float dist = vlen(*disp);
     if (dist <= w->ccd_max_pen) return;
+    if (w->ccd_thr[i] > 0.0f && dist < w->ccd_thr[i]) return; /* PhysicsWorld.cpp:807 */
     const kzo_shape* sh = &w->shapes[w->shape[i]];
     const v3 dir = vdiv(*disp, dist);
     const qt r0 = w->rot[i];
@@ -1591,7 +1609,9 @@ static float rd_f32(rd_t* r) { float v; rd(r, &v, 4); return v; }
 
 kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* resolved, size_t resolved_len) {
     rd_t r = {scene, scene_len, 0, 0};
-    if (rd_u32(&r) != 0x43535A4Bu || rd_u32(&r) != 1u) { set_err("bad scene header"); return NULL; }
+    if (rd_u32(&r) != 0x43535A4Bu) { set_err("bad scene header"); return NULL; }
+    const uint32_t version = rd_u32(&r);
+    if (version != 1u && version != 2u) { set_err("bad scene version"); return NULL; }
     kzo_world* w = (kzo_world*)calloc(1, sizeof(kzo_world));
     w->gravity.x = rd_f32(&r); w->gravity.y = rd_f32(&r); w->gravity.z = rd_f32(&r);
     (void)rd_f32(&r); /* scene dt: the caller passes dt to kzo_step */
@@ -1603,6 +1623,9 @@ kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* res
     w->rest_thresh = rd_f32(&r);
     w->max_bias = rd_f32(&r);
     w->ws_factor = rd_f32(&r);
+    /* WorldSettings sleep thresholds (PhysicsWorld.h:25-27); version 1 scenes carry the defaults */
+    w->sleep_time = 0.5f; w->sleep_lin = 0.05f; w->sleep_ang = 0.1f;
+    if (version >= 2u) { w->sleep_time = rd_f32(&r); w->sleep_lin = rd_f32(&r); w->sleep_ang = rd_f32(&r); }
     if (wflags & 1u) { set_err("sleeping is not supported by the oracle"); free(w); return NULL; }
     w->vel_bias = (wflags & 2u) != 0;
     w->no_ws = (wflags & 4u) != 0;
@@ -1656,6 +1679,7 @@ kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* res
 #define ALLOC(f, T) w->f = (T*)calloc((size_t)(nb ? nb : 1), sizeof(T))
     ALLOC(packed, uint32_t); ALLOC(layer, uint32_t); ALLOC(mask, uint32_t); ALLOC(proxy, uint32_t);
     ALLOC(shape, int); ALLOC(motion, uint8_t); ALLOC(sensor, uint8_t); ALLOC(ccd, uint8_t); ALLOC(fat, aabb);
+    ALLOC(ccd_thr, float);
     ALLOC(pos, v3); ALLOC(lv, v3); ALLOC(av, v3); ALLOC(plv, v3); ALLOC(pav, v3); ALLOC(force, v3); ALLOC(torque, v3);
     ALLOC(rot, qt);
     ALLOC(inv_mass, float); ALLOC(lin_damp, float); ALLOC(ang_damp, float); ALLOC(grav, float);
@@ -1675,6 +1699,7 @@ kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* res
         (void)rd_f32(&r); (void)rd_f32(&r); /* density, mass override: resolved mass comes in the blob */
         w->layer[i] = rd_u32(&r); w->mask[i] = rd_u32(&r);
         uint32_t fl = rd_u32(&r);
+        w->ccd_thr[i] = version >= 2u ? rd_f32(&r) : 0.0f; /* BodySettings::ccdMotionThreshold */
         w->sensor[i] = (fl & 1u) != 0;
         w->ccd[i] = (fl & 4u) != 0;
         w->packed[i] = (uint32_t)i; /* BodyID(index, sequence 0).Packed() */
@@ -1720,12 +1745,13 @@ kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* res
 }
 
 void kzo_set_trig_mode(kzo_world* w, int mode) { w->trig_mode = mode; }
+void kzo_set_cache_hash(kzo_world* w, int mixed) { w->cache_mix = mixed != 0; }
 
 void kzo_destroy(kzo_world* w) {
     if (!w) return;
     for (int i = 0; i < w->nshapes; ++i) { free(w->shapes[i].verts); free(w->shapes[i].sizes); free(w->shapes[i].idx); }
     free(w->shapes);
-    void* ptrs[] = {w->packed, w->layer, w->mask, w->proxy, w->shape, w->motion, w->sensor, w->ccd, w->fat, w->pos, w->lv, w->av,
+    void* ptrs[] = {w->packed, w->layer, w->mask, w->proxy, w->shape, w->motion, w->sensor, w->ccd, w->ccd_thr, w->fat, w->pos, w->lv, w->av,
                     w->plv, w->pav, w->force, w->torque, w->rot, w->inv_mass, w->lin_damp, w->ang_damp, w->grav,
                     w->max_lin, w->max_ang, w->fric, w->rest, w->iil, w->iiw, w->active, w->island_index,
                     w->nodes, w->bp_layer, w->bp_mask, w->cache, w->pairs, w->ext_pairs, w->man, w->keys,

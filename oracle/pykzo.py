@@ -44,6 +44,7 @@ def lib():
         L.kzo_set_schedule_stats.argtypes = [vp, ctypes.c_int]
         L.kzo_set_residual.argtypes = [vp, f32, u32]
         L.kzo_set_trig_mode.argtypes = [vp, ctypes.c_int]
+        L.kzo_set_cache_hash.argtypes = [vp, ctypes.c_int]
         L.kzo_set_external_pairs.argtypes = [vp, vp, u32]
         L.kzo_step.argtypes = [vp, f32]
         L.kzo_num_bodies.restype = u32
@@ -106,6 +107,10 @@ class OracleWorld:
         """0: the C library's float trigonometry (the reference's); 1: double precision rounded to
         float (the GPU's joint kernels)."""
         lib().kzo_set_trig_mode(self._w, int(mode))
+
+    def set_cache_hash(self, mixed: bool):
+        """Mixed manifold-cache slot function (same results; avoids the reference's clustering)."""
+        lib().kzo_set_cache_hash(self._w, int(mixed))
 
     def set_residual(self, tol: float, cap: int = 64):
         lib().kzo_set_residual(self._w, np.float32(tol), cap)

@@ -73,8 +73,13 @@ int main(int argc, char** argv) {
         if (std::fread(rd.buf.data(), 1, size_t(n), f) != size_t(n)) return 1;
         std::fclose(f);
     }
-    if (rd.get<uint32_t>() != 0x43535A4Bu || rd.get<uint32_t>() != 1u) {
+    if (rd.get<uint32_t>() != 0x43535A4Bu) {
         std::fprintf(stderr, "bad scene\n");
+        return 1;
+    }
+    const uint32_t version = rd.get<uint32_t>();
+    if (version != 1u && version != 2u) {
+        std::fprintf(stderr, "bad scene version\n");
         return 1;
     }
 
@@ -90,6 +95,11 @@ int main(int argc, char** argv) {
     ws.solver.restitutionThreshold = rd.get<float>();
     ws.solver.maxBiasVelocity = rd.get<float>();
     ws.solver.warmStartFactor = rd.get<float>();
+    if (version >= 2u) {
+        ws.sleepTimeThreshold = rd.get<float>();
+        ws.sleepLinearThreshold = rd.get<float>();
+        ws.sleepAngularThreshold = rd.get<float>();
+    }
     ws.allowSleeping = (wflags & 1u) != 0;
     ws.solver.useVelocityBias = (wflags & 2u) != 0;
     ws.useMultithreading = !singleThread;
@@ -133,6 +143,7 @@ int main(int argc, char** argv) {
         float m[9];
         for (float& x : m) x = rd.get<float>();
         uint32_t layer = rd.get<uint32_t>(), mask = rd.get<uint32_t>(), flags = rd.get<uint32_t>();
+        if (version >= 2u) bs.ccdMotionThreshold = rd.get<float>();
         bs.shape = shapes[shape];
         bs.motionType = MotionType(motion);
         bs.position = Vec3(v[0], v[1], v[2]);

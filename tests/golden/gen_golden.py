@@ -6,7 +6,9 @@ computed: the ComputeStateHash value after every step, the full body state at ch
 the broad-phase pair list and contact constraints of the first steps, WorldStats counters, the
 resolved mass properties and every hull as built by ConvexHullShape::Create.
 
-    python tests/golden/gen_golden.py [--ref /root/reference] [--only NAME ...]
+    python tests/golden/gen_golden.py --ref <reference checkout> [--only NAME ...]
+
+(--ref defaults to the KIZURI_REFERENCE environment variable.)
 """
 from __future__ import annotations
 
@@ -38,7 +40,83 @@ def fixture_scenes():
     out["pyramid4_tests"] = (_reference_test_pyramid(), 240, 2, [0, 239])
     out["ccd_shots"] = (_ccd_shots(), 120, 2, [0, 1, 29, 59, 119])
     out["joints_mix"] = (_joints_mix(), 180, 2, [0, 1, 59, 179])
+    out["ccd_threshold"] = (_ccd_threshold(), 90, 2, [0, 1, 29, 89])
+    out["joints_single"] = (_joints_single(), 60, 2, list(range(60)))
     return out
+
+
+def _joints_single(copies: int = 8):
+    """Single-joint systems of every joint type (Constraints.h:41-277), `copies` of each with seeded
+    initial motions: a body on a point joint, a hinge door with limits and a motor, a slider with
+    limits and a six-dof joint hang from static posts; fixed and distance pairs tumble in free
+    flight.  Dynamic bodies collide with the ground layer only and stay clear of it for 60 steps,
+    so no contact appears or vanishes.  Single-joint systems are well conditioned: a one-rounding-
+    step difference in a joint's trigonometry stays a small perturbation, which makes this the
+    scene on which per-step velocities are compared with the reference at 1e-4 relative."""
+    S = scenes
+    sc = S.Scene(name="joints_single")
+    S._timed_settings(sc, 10, 2)
+    S._ground(sc, 0.6)
+    post = sc.add_shape(S.Shape(S.SHAPE_BOX, [0.1, 0.1, 0.1, 0.0]))
+    cube = sc.add_shape(S.Shape(S.SHAPE_BOX, [0.3, 0.2, 0.25, 0.0]))
+    door = sc.add_shape(S.Shape(S.SHAPE_BOX, [0.5, 0.8, 0.05, 0.0]))
+    ball = sc.add_shape(S.Shape(S.SHAPE_SPHERE, [0.25, 0.0, 0.0, 0.0]))
+    st = S.MOTION_STATIC
+    f = scenes.f32
+    rng = np.random.default_rng(2024)
+    J = []
+
+    def dyn(shape, pos, vel=(0.0, 0.0, 0.0), ang=(0.0, 0.0, 0.0)):
+        return sc.add_body(S.Body(shape, pos=tuple(f(x) for x in pos), vel=tuple(f(x) for x in vel),
+                                  ang=tuple(f(x) for x in ang), layer=2, mask=1))
+
+    def fixed_post(pos):
+        return sc.add_body(S.Body(post, st, pos=pos, layer=4))
+
+    for k in range(copies):
+        z = 3.0 * k
+        r = rng.uniform(-1.0, 1.0, 12)
+        p = fixed_post((0.0, 8.0, z))  # pendulum on a point joint, swinging in 3-D
+        b = dyn(cube, (0.9, 7.5, z + 0.2), vel=(0.0, 0.0, 1.2 * r[0]), ang=(0.3 * r[1], 0.0, 0.4 * r[2]))
+        J.append(S.Joint(S.JOINT_POINT, p, b, anchor_a=(0.0, 8.0, z)))
+        p = fixed_post((4.0, 8.0, z))  # hinge door with limits and a motor
+        b = dyn(door, (4.6, 8.0, z), ang=(0.0, 1.5 * r[3], 0.0))
+        J.append(S.Joint(S.JOINT_HINGE, p, b, anchor_a=(4.1, 8.0, z), axis_a=(0.0, 1.0, 0.0),
+                         axis_b=(0.0, 1.0, 0.0), lower=-1.0, upper=1.0, motor_target=f(2.0 * r[4]), motor_max=5.0,
+                         flags=S.JOINT_FLAG_LIMITS | S.JOINT_FLAG_MOTOR))
+        p = fixed_post((8.0, 8.0, z))  # slider with limits along a tilted axis
+        b = dyn(cube, (8.5, 8.0, z), vel=(0.5 * r[5], 0.0, 0.0))
+        J.append(S.Joint(S.JOINT_SLIDER, p, b, anchor_a=(8.5, 8.0, z), axis_a=(0.8, -0.6, 0.0), lower=-0.6,
+                         upper=0.9, flags=S.JOINT_FLAG_LIMITS))
+        p = fixed_post((12.0, 8.0, z))  # six-dof: fixed, limited and motorised axes
+        b = dyn(cube, (12.0, 8.0, z + 0.6), ang=(0.5 * r[6], 1.0 * r[7], 0.0))
+        c, s_ = math.cos(0.3), math.sin(0.3)
+        J.append(S.Joint(S.JOINT_SIXDOF, p, b, anchor_a=(12.0, 8.0, z + 0.6), rotation=(0.0, s_, 0.0, c),
+                         axis_modes=(2 << 0) | (2 << 2) | (1 << 4) | (2 << 6), motor_mask=(1 << 2) | (1 << 4),
+                         six_motor=(0.0, 0.0, 0.5, 0.0, 0.0, 3.0, 0.0, 1.5, 0.0, 0.0, 2.0, 0.0)))
+        f1 = dyn(cube, (16.0, 9.0, z), vel=(0.0, 2.0, 0.0), ang=(0.3 * r[8], 0.0, 0.2))  # fixed pair, tumbling
+        f2 = dyn(cube, (16.62, 9.1, z), vel=(0.0, 2.0, 0.0))
+        J.append(S.Joint(S.JOINT_FIXED, f1, f2, anchor_a=(16.31, 9.05, z)))
+        d1 = dyn(ball, (20.0, 9.0, z), vel=(0.0, 3.0, 1.0 * r[9]))  # distance pair, tumbling
+        d2 = dyn(ball, (21.0, 9.5, z), vel=(0.0, 1.0, -1.0), ang=(0.0, 2.0 * r[10], 0.0))
+        J.append(S.Joint(S.JOINT_DISTANCE, d1, d2, anchor_a=(20.0, 9.0, z), anchor_b=(21.0, 9.5, z), distance=1.2))
+    sc.joints = J
+    return sc
+
+
+def _ccd_threshold():
+    """The CCD shots with BodySettings::ccdMotionThreshold (Body.h:70) set on every other
+    LinearCast body, between the shortest and longest step displacement of the shots: bodies moving
+    less than their threshold in a step are not clamped (PhysicsWorld.cpp:807) and may tunnel."""
+    sc = _ccd_shots()
+    sc.name = "ccd_threshold"
+    k = 0
+    for b in sc.bodies:
+        if b.flags & scenes.BODY_FLAG_LINEAR_CAST:
+            if k % 2:
+                b.ccd_motion_threshold = 0.7
+            k += 1
+    return sc
 
 
 def _joints_mix():
@@ -159,9 +237,12 @@ def _reference_test_pyramid():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("KIZURI_REFERENCE"),
+                    help="the reference's source checkout (default: $KIZURI_REFERENCE)")
     ap.add_argument("--only", nargs="*", default=None, help="fixture names to (re)generate (default: all)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give --ref or set KIZURI_REFERENCE to the reference's source checkout")
     subprocess.run(["make", "-s", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"), f"REF={args.ref}", "-j8"],
                    check=True)
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_trace")

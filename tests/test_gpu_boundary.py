@@ -1,0 +1,75 @@
+"""The C-ABI's settings boundary on the GPU: reference settings the accelerated path cannot honour
+are rejected, settings the reference ignores are accepted, and the bounded in-kernel wait's
+give-up path (a poll limit small enough to run out) completes the step with unchanged results."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import bits
+
+pytestmark = pytest.mark.gpu
+
+KZG_ERR_UNSUPPORTED = -4
+KZG_DEVERR_WAIT = 16
+
+
+def test_scalar_solver_is_rejected(kzg_lib):
+    """SolverSettings::useSIMDSolver = false (ContactSolver.h:77) selects the reference's scalar
+    constraint-order sweep (PhysicsWorld.cpp:723-729), which this library does not implement."""
+    from kizuriphysics3d_gb300 import World, capi, scenes
+    with World(scenes.pyramid(3)) as w:
+        with pytest.raises(capi.KzgError) as e:
+            w.set_solver(use_simd_solver=0)
+        assert e.value.status == KZG_ERR_UNSUPPORTED
+        assert "useSIMDSolver" in str(e.value)
+        w.set_solver(use_simd_solver=1)  # the default is accepted again
+        w.step_fixed()
+
+
+def test_split_impulse_flag_changes_nothing(kzg_lib):
+    """SolverSettings::useSplitImpulse is read nowhere by the reference (ContactSolver.h:75): both
+    values give identical bits."""
+    from kizuriphysics3d_gb300 import World, scenes
+    sc = scenes.pyramid(8)
+    with World(sc) as a, World(sc) as b:
+        a.set_solver(use_split_impulse=1)
+        b.set_solver(use_split_impulse=0)
+        a.step_fixed(n=60)
+        b.step_fixed(n=60)
+        assert np.array_equal(bits(a.state()), bits(b.state()))
+
+
+def _settled_pile():
+    from kizuriphysics3d_gb300 import resolve, scenes
+    snap = os.path.join(os.path.dirname(__file__), "..", "kizuriphysics3d_gb300", "data", "pile20000_step600.npz")
+    sc = scenes.pile(20000, seed=1234)
+    with np.load(snap) as z:
+        state = z["state"]
+    for b, st in zip(sc.bodies, state):
+        b.pos, b.rot, b.vel, b.ang = tuple(st[0:3]), tuple(st[3:7]), tuple(st[7:10]), tuple(st[10:13])
+    return sc, resolve(sc)
+
+
+def test_wait_that_runs_out_completes_the_step(kzg_lib):
+    """The settled 20,000-body pile's giant island streams its velocity level sweep behind the first
+    fit (the one in-kernel wait).  With a poll limit of 1 the wait runs out: KZG_DEVERR_WAIT is
+    reported in the stats, the step still returns KZG_OK, its result is bit-identical to the
+    default limit's, and the next step with the default limit runs clean."""
+    from kizuriphysics3d_gb300 import World
+    sc, res = _settled_pile()
+    with World(sc, resolved=res, max_pairs=48 * len(sc.bodies)) as short, \
+            World(sc, resolved=res, max_pairs=48 * len(sc.bodies)) as normal:
+        short.set_wait_limit(1)
+        short.step_fixed()  # raises on any status but KZG_OK
+        normal.step_fixed()
+        st = short.get_stats()
+        assert st["device_error"] & KZG_DEVERR_WAIT
+        assert st["device_error"] & ~KZG_DEVERR_WAIT == 0
+        assert normal.get_stats()["device_error"] == 0
+        assert np.array_equal(bits(short.state()), bits(normal.state()))
+        short.set_wait_limit(0)  # back to the default
+        short.step_fixed()
+        normal.step_fixed()
+        assert short.get_stats()["device_error"] == 0
+        assert short.compute_state_hash() == normal.compute_state_hash()
