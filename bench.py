@@ -93,6 +93,32 @@ def load_snapshot(name: str, preroll: int):
     return None
 
 
+def resolved_path(name: str) -> str:
+    return os.path.join(SNAP_DIR, f"{name}_resolved.npz")
+
+
+def load_resolved_blob(name: str):
+    """The workload's resolved setup (built hulls and per-body mass properties) in the oracle's
+    input layout, written by `bench.py --workload NAME --write-resolved` with the library's host
+    setup functions (pinned bit-exact to the reference's ConvexHullShape::Create and mass
+    properties by the tests).  Read by the CPU arm so that it never loads the GPU library."""
+    p = resolved_path(name)
+    if not os.path.exists(p):
+        return None
+    with np.load(p) as z:
+        return z["blob"].tobytes()
+
+
+def write_resolved_blob(name: str, sc) -> str:
+    from kizuriphysics3d_gb300 import resolve
+    from oracle import trace
+    res = resolve(sc)
+    hulls = {i: trace.Hull(h.verts, h.sizes, h.idx, 0.0) for i, h in res.hulls.items()}
+    blob = trace.resolved_blob(sc, hulls, res.inv_mass, res.inv_inertia_local)
+    np.savez_compressed(resolved_path(name), blob=np.frombuffer(blob, np.uint8))
+    return resolved_path(name)
+
+
 def scene_with_state(sc, state):
     """The same scene whose bodies start at the given state (pos, rot, linear, angular)."""
     import copy
@@ -192,14 +218,19 @@ class Clocks:
 # ---------------------------------------------------------------------------------------------
 # CPU legs (oracle port of the reference algorithm)
 # ---------------------------------------------------------------------------------------------
-def cpu_leg(sc, res, state, steps_max: int, budget_s: float, threads: int, residual: bool = True):
-    from oracle import pykzo, trace
+def cpu_leg(sc, blob: bytes, state, warmup: int, steps_max: int, budget_s: float, threads: int,
+            residual: bool = True, mixed_hash: bool = False):
+    """The oracle port of the reference step (the reference's tree pair order and manifold cache)
+    from the given state: `warmup` untimed steps, then timed steps until steps_max or the budget.
+    mixed_hash: the cache's slot function without the reference's clustering (same results)."""
+    from oracle import pykzo
     s2 = scene_with_state(sc, state) if state is not None else sc
-    hulls = {i: trace.Hull(h.verts, h.sizes, h.idx, 0.0) for i, h in res.hulls.items()}
-    w = pykzo.OracleWorld(s2.to_bytes(), trace.resolved_blob(s2, hulls, res.inv_mass, res.inv_inertia_local),
-                          pykzo.PAIRS_TREE, threads=threads)
+    w = pykzo.OracleWorld(s2.to_bytes(), blob, pykzo.PAIRS_TREE, threads=threads)
+    w.set_cache_hash(mixed_hash)
     if residual:
         w.set_residual(RESIDUAL_TOL, RESIDUAL_CAP)
+    for _ in range(warmup):
+        w.step(np.float32(sc.dt))
     done, t0 = 0, time.perf_counter()
     while done < steps_max:
         w.step(np.float32(sc.dt))
@@ -209,6 +240,19 @@ def cpu_leg(sc, res, state, steps_max: int, budget_s: float, threads: int, resid
     dt = time.perf_counter() - t0
     w.close()
     return done, dt
+
+
+def cpu_blob(args, sc):
+    """Resolved setup for the CPU legs: the committed file, else built with the library's host
+    setup functions (noted in the output)."""
+    blob = load_resolved_blob(args.workload)
+    if blob is not None:
+        return blob, "committed resolved-setup file"
+    from kizuriphysics3d_gb300 import resolve
+    from oracle import trace
+    res = resolve(sc)
+    hulls = {i: trace.Hull(h.verts, h.sizes, h.idx, 0.0) for i, h in res.hulls.items()}
+    return trace.resolved_blob(sc, hulls, res.inv_mass, res.inv_inertia_local), "built by the library's host setup"
 
 
 # ---------------------------------------------------------------------------------------------
@@ -223,7 +267,12 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--save-snapshot", default=None, help="write the post-preroll state to this .npz path")
+    ap.add_argument("--write-resolved", action="store_true",
+                    help="write the workload's resolved setup (hulls, mass) for the CPU arm and exit")
     args = ap.parse_args()
+    if args.write_resolved:
+        print(write_resolved_blob(args.workload, make_workload(args.workload)[0]))
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world_size = int(os.environ.get("WORLD_SIZE", "1"))
@@ -393,25 +442,36 @@ def main():
     cpu = None
     if not args.no_cpu_baseline and rank == 0 and world_size == 1:
         threads = os.cpu_count() or 1
-        n_steps, secs = cpu_leg(sc, res, snap, 10 ** 6, args.cpu_budget, threads, residual=True)
+        blob, blob_src = cpu_blob(args, sc)
+        cw = 1  # one untimed step warms the manifold cache, as the GPU arm's warm-up does
+        n_steps, secs = cpu_leg(sc, blob, snap, cw, 10 ** 6, args.cpu_budget, threads, residual=True)
+        nf, sf = cpu_leg(sc, blob, snap, cw, 10 ** 6, args.cpu_budget / 2, threads, residual=False)
+        nm, sm = cpu_leg(sc, blob, snap, cw, 10 ** 6, args.cpu_budget / 2, threads, residual=True, mixed_hash=True)
         cpu = {"value": n_dyn * n_steps / secs, "unit": "body-steps/s", "cores": threads, "kind": "port",
-               "sample": f"{n_steps} steps of the same workload from the same starting state (cold manifold "
-                         f"cache), reference pair order, residual {RESIDUAL_TOL:g} / cap {RESIDUAL_CAP}, "
-                         f"{secs:.1f} s"}
+               "sample": f"{n_steps} steps of the same workload from the same starting state after {cw} untimed "
+                         f"step, reference pair order, residual {RESIDUAL_TOL:g} / cap {RESIDUAL_CAP}, "
+                         f"{secs:.1f} s; setup: {blob_src}",
+               "fixed_iterations": {"value": n_dyn * nf / sf, "unit": "body-steps/s",
+                                    "sample": f"{nf} steps at the fixed {sc.velocity_iterations} velocity "
+                                              f"iterations, {sf:.1f} s"},
+               "mixed_cache_hash": {"value": n_dyn * nm / sm, "unit": "body-steps/s",
+                                    "sample": f"{nm} steps, residual-terminated, with the manifold cache's slot "
+                                              f"function mixed instead of the reference's clustering (pa ^ pb) & "
+                                              f"mask: same results, what the reference would reach without "
+                                              f"that pathology, {sm:.1f} s"}}
 
     ms_per_step = total_ms / args.steps
     out = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
-        "config": dict(cfg, window=f"steps {preroll}+ of the run" if preroll else "from the initial scene",
-                       start_state="committed snapshot" if snap is not None else "simulated untimed",
-                       solver=f"plain warm start, velocity iterations until the relative impulse change is "
-                              f"<= {RESIDUAL_TOL:g} (cap {RESIDUAL_CAP}); the reference's 4-wide batch order",
-                       pair_order="canonical (GPU broad phase)", l2="flushed between timed steps (256 MB write)",
-                       parallelism="replicas" if world_size > 1 else "single GPU",
-                       contacts=points, pairs=int(pairs.shape[0]), islands=last["num_islands"],
-                       max_velocity_levels=last["max_velocity_levels"], max_bias_levels=last["max_bias_levels"]),
+        "config": workload_config(cfg, preroll, snap is not None),
+        "pair_order": "canonical: every overlapping pair once, MakePairKey order (GPU broad phase)",
+        "l2": "flushed between timed steps (256 MB write)",
+        "parallelism": "replicas" if world_size > 1 else "single GPU",
+        "measured": {"contacts": points, "pairs": int(pairs.shape[0]), "islands": last["num_islands"],
+                     "max_velocity_levels": last["max_velocity_levels"],
+                     "max_bias_levels": last["max_bias_levels"]},
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": int(ft.nbytes),
                 "d2h_bytes_per_step": int(tr.nbytes)},
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -435,28 +495,38 @@ def main():
         dist.destroy_process_group()
 
 
+def workload_config(cfg: dict, preroll: int, have_snapshot: bool) -> dict:
+    """The workload as both arms run it (identical in the GPU arm's and the reference arm's line)."""
+    return dict(cfg, window=f"steps {preroll}+ of the run" if preroll else "from the initial scene",
+                start_state="committed snapshot" if have_snapshot else "simulated untimed",
+                solver=f"velocity iterations until the relative impulse change is <= {RESIDUAL_TOL:g} "
+                       f"(cap {RESIDUAL_CAP}); the reference's first-fit 4-wide batches")
+
+
 def run_reference(args, sc, cfg, preroll, n_dyn):
+    """The reference's CPU implementation of the step (the oracle port, pinned bit-exact to the
+    reference by the tests) on all host cores, with the reference's own pair order and manifold
+    cache: args.warmup untimed steps, then up to args.steps timed steps within a bounded budget."""
     snap = load_snapshot(args.workload, preroll)
     if preroll and snap is None:
         print(json.dumps({"impl": "reference", "unavailable": "starting-state snapshot for this workload is not "
                                                               "committed; the CPU cannot simulate the untimed "
                                                               "pre-roll within minutes"}))
         return
-    from kizuriphysics3d_gb300 import resolve
-    res = resolve(sc)
+    blob, blob_src = cpu_blob(args, sc)
     threads = os.cpu_count() or 1
-    budget = max(30.0, min(240.0, 8.0 * (args.steps + args.warmup)))
-    n_steps, secs = cpu_leg(sc, res, snap, args.steps, budget, threads, residual=True)
+    budget = max(30.0, min(240.0, 8.0 * args.steps))
+    warm = args.warmup
+    n_steps, secs = cpu_leg(sc, blob, snap, warm, args.steps, budget, threads, residual=True)
     value = n_dyn * n_steps / secs
     out = {"metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": 0, "steps": n_steps,
-           "warmup": 1, "ms_per_step": 1e3 * secs / max(n_steps, 1), "higher_is_better": True, "scaling": "weak",
+           "warmup": warm, "ms_per_step": 1e3 * secs / max(n_steps, 1), "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)", "impl": "reference",
-           "config": dict(cfg, window=f"steps {preroll}+ of the run" if preroll else "from the initial scene",
-                          pair_order="reference dynamic AABB tree",
-                          solver=f"velocity iterations until the relative impulse change is <= {RESIDUAL_TOL:g} "
-                                 f"(cap {RESIDUAL_CAP}); the reference's first-fit 4-wide batches"),
+           "config": workload_config(cfg, preroll, snap is not None),
+           "pair_order": "the reference's dynamic AABB tree order",
            "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port",
-                            "sample": f"{n_steps} of {args.steps} requested steps within a {budget:.0f} s budget"},
+                            "sample": f"{n_steps} of {args.steps} requested steps after {warm} untimed, within a "
+                                      f"{budget:.0f} s budget; setup: {blob_src}"},
            "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 

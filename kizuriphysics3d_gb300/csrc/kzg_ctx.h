@@ -62,6 +62,7 @@ struct Counters {  // device-side counters, copied back after each stage that si
     uint32_t nmiss;      // contact points without a cached warm start (learned warm start / logging)
     uint32_t njisl;      // islands holding joints
     uint32_t nx_sched_w, nx_sched_c, nx_solve_w, nx_solve_c;  // largest-first island order: next island to take
+    uint32_t nroots;     // islands as the reference counts them: every dynamic body's union-find root
     uint32_t cache_entries;  // persists across steps
     uint32_t frame;          // step counter, advanced on the device by k_begin_step
 };

@@ -505,6 +505,15 @@ __global__ void k_uf_union(const Counters* cnt, const uint32_t* __restrict__ con
         bb = old;
     }
 }
+// WorldStats::numIslands (PhysicsWorld.cpp:636-642): one island per union-find root among the
+// dynamic bodies, bodies without a contact included.
+__global__ void k_count_roots(const DeviceBodies b, uint32_t n, const uint32_t* __restrict__ uf, Counters* cnt) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool root = i < n && b.motion[i] == KZG_MOTION_DYNAMIC && __ldcg(&uf[i]) == i;
+    const unsigned m = __ballot_sync(0xffffffffu, root);
+    if ((threadIdx.x & 31u) == 0 && m) atomicAdd(&cnt->nroots, (uint32_t)__popc(m));
+}
+
 // Island of every constraint; slots past the constraint count (up to cap) get a key above every
 // body index so that a capacity-sized sort leaves them at the end.
 __global__ void k_island_keys(const Counters* cnt, const uint32_t* __restrict__ con_a, const uint32_t* __restrict__ con_b,
@@ -1098,6 +1107,8 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     k_uf_init<<<blocks_for(nb), kThreads, 0, st>>>(ctx.uf, nb);
     k_uf_union<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf);
     if (nj) k_joint_union<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, nj, ctx.uf);
+    k_count_roots<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, ctx.uf, ctx.dcnt);
+    ++ctx.launches;
     const int kbits = bits_for(nb);
     k_island_keys<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf,
                                                       ctx.isl_key, ctx.isl_con_in, P, (1u << kbits) - 1u);
@@ -1199,7 +1210,7 @@ static kzg_status finish_stats(Ctx& ctx, uint32_t graph_steps = 0) {
     s.num_broadphase_pairs = h.npairs;
     s.num_contact_constraints = h.ncons;
     s.num_contact_points = h.npoints;
-    s.num_islands = h.nislands;
+    s.num_islands = h.nroots;
     s.num_batches = h.batches;
     s.max_velocity_levels = h.max_vlev;
     s.max_bias_levels = h.max_blev;

@@ -39,6 +39,9 @@ def test_mode_a_bit_exact_with_reference(name, oracle_lib, kzg_lib):
         for s in range(steps):
             ow.step(np.float32(sc.dt))
             gw.step_with_pairs(ow.pairs())
+            gs = gw.get_stats()
+            assert [gs["num_broadphase_pairs"], gs["num_contact_constraints"], gs["num_contact_points"],
+                    gs["num_islands"]] == list(g["stats"][s]), f"{name}: WorldStats differ from the reference at step {s}"
             st = gw.state()
             if not np.array_equal(bits(st), bits(ow.state())):
                 bad = np.argwhere(bits(st) != bits(ow.state()))
