@@ -50,6 +50,12 @@ void kzo_set_trig_mode(kzo_world* w, int mode);
  * Results are identical (entries are found by key and never evicted); large worlds avoid the
  * reference's clustered probe runs. */
 void kzo_set_cache_hash(kzo_world* w, int mixed);
+/* Sleeping state: the active list in order (kzo_num_active entries), per-body activity flags and
+ * sleep timers (each pointer may be NULL). */
+uint32_t kzo_num_active(const kzo_world* w);
+void kzo_get_activity(const kzo_world* w, uint32_t* active_list, uint8_t* active_flags, float* sleep_timers);
+/* Sleeping bodies whose contacts were assigned to two different islands in the last step. */
+uint32_t kzo_shared_sleepers(const kzo_world* w);
 
 int kzo_step(kzo_world* w, float dt);
 

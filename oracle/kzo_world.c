@@ -102,8 +102,14 @@ struct kzo_world {
     qt* rot;
     float *inv_mass, *lin_damp, *ang_damp, *grav, *max_lin, *max_ang, *fric, *rest;
     m3 *iil, *iiw;
-    int* active;
+    int* active;            /* BodyManager::mActiveBodies: the buffer keeps values past nactive (RemoveSwap) */
     int nactive;
+    int allow_sleeping;     /* WorldSettings::allowSleeping */
+    uint8_t* allow_sleep;   /* BodySettings::allowSleeping */
+    uint8_t* is_active;     /* ActivationState::Active */
+    float* sleep_timer;     /* MotionProperties::sleepTimer */
+    uint32_t st_islands;    /* WorldStats::numIslands as the step leaves it */
+    uint32_t st_shared_sleepers; /* sleeping bodies solved by two islands in the last step */
     /* broad phase tree */
     node_t* nodes;
     uint32_t nnodes, node_cap, root, free_list, nproxies;
@@ -127,7 +133,7 @@ struct kzo_world {
     uint32_t nislands;
     uint32_t* isl_off; /* nislands+1 */
     uint32_t* isl_con;
-    int* island_index;
+    uint32_t* island_index; /* Body::mIslandIndex: kept while a body sleeps (stale) */
     /* joints (PhysicsWorld::mConstraints) and their islands */
     joint_t* joints;
     uint32_t njoints;
@@ -1308,13 +1314,25 @@ static void uf_union(uint32_t* par, uint32_t* rank, uint32_t a, uint32_t b) {
     if (rank[a] == rank[b]) ++rank[a];
 }
 
+/* BuildIslands (PhysicsWorld.cpp:587-664).  Active bodies get a compact index in active-list order
+ * (dynamic ones; others 0xFFFFFFFF); a sleeping body keeps whatever index it last had, so its
+ * contacts join (and are solved in) the island of the active body now holding that index, or of
+ * their other body when the index is past the active dynamic count. */
+static uint32_t island_of(const kzo_world* w, uint32_t* par, const uint32_t* r2i, uint32_t numDyn, int b) {
+    if (w->motion[b] != KZO_DYNAMIC) return NUL;
+    const uint32_t idx = w->island_index[b];
+    if (idx >= numDyn) return NUL;
+    return r2i[uf_find(par, idx)];
+}
+
 static void build_islands(kzo_world* w) {
     uint32_t numDyn = 0;
     for (int i = 0; i < w->nactive; ++i) {
         int b = w->active[i];
-        w->island_index[b] = w->motion[b] == KZO_DYNAMIC ? (int)numDyn++ : -1;
+        w->island_index[b] = w->motion[b] == KZO_DYNAMIC ? numDyn++ : 0xFFFFFFFFu;
     }
     w->nislands = 0;
+    w->st_islands = 0;
     if (numDyn == 0) return;
     uint32_t* par = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * numDyn);
     uint32_t* rank = (uint32_t*)calloc(numDyn, sizeof(uint32_t));
@@ -1322,15 +1340,15 @@ static void build_islands(kzo_world* w) {
     for (uint32_t ci = 0; ci < w->ncons; ++ci) {
         con_t* c = &w->cons[ci];
         if (w->motion[c->a] != KZO_DYNAMIC || w->motion[c->b] != KZO_DYNAMIC) continue;
-        int ia = w->island_index[c->a], ib = w->island_index[c->b];
-        if (ia >= 0 && ib >= 0) uf_union(par, rank, (uint32_t)ia, (uint32_t)ib);
+        uint32_t ia = w->island_index[c->a], ib = w->island_index[c->b];
+        if (ia < numDyn && ib < numDyn) uf_union(par, rank, ia, ib);
     }
     for (uint32_t ji = 0; ji < w->njoints; ++ji) { /* joints join islands too (PhysicsWorld.cpp:625-633) */
         const joint_t* j = &w->joints[ji];
         if (j->flags & 1u) continue;
         if (w->motion[j->a] != KZO_DYNAMIC || w->motion[j->b] != KZO_DYNAMIC) continue;
-        int ia = w->island_index[j->a], ib = w->island_index[j->b];
-        if (ia >= 0 && ib >= 0) uf_union(par, rank, (uint32_t)ia, (uint32_t)ib);
+        uint32_t ia = w->island_index[j->a], ib = w->island_index[j->b];
+        if (ia < numDyn && ib < numDyn) uf_union(par, rank, ia, ib);
     }
     uint32_t* r2i = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * numDyn);
     for (uint32_t i = 0; i < numDyn; ++i) r2i[i] = NUL;
@@ -1340,19 +1358,36 @@ static void build_islands(kzo_world* w) {
         if (r2i[r] == NUL) r2i[r] = ni++;
     }
     w->nislands = ni;
+    w->st_islands = ni;
     uint32_t* isl = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * (w->ncons ? w->ncons : 1));
     w->isl_off = (uint32_t*)xrealloc(w->isl_off, sizeof(uint32_t) * (ni + 1));
     memset(w->isl_off, 0, sizeof(uint32_t) * (ni + 1));
     for (uint32_t ci = 0; ci < w->ncons; ++ci) {
         con_t* c = &w->cons[ci];
-        uint32_t is = NUL;
-        if (w->motion[c->a] == KZO_DYNAMIC && w->island_index[c->a] >= 0) is = r2i[uf_find(par, (uint32_t)w->island_index[c->a])];
-        if (is == NUL && w->motion[c->b] == KZO_DYNAMIC && w->island_index[c->b] >= 0)
-            is = r2i[uf_find(par, (uint32_t)w->island_index[c->b])];
+        uint32_t is = island_of(w, par, r2i, numDyn, c->a);
+        if (is == NUL) is = island_of(w, par, r2i, numDyn, c->b);
         isl[ci] = is;
         if (is != NUL) w->isl_off[is + 1]++;
     }
     for (uint32_t i = 0; i < ni; ++i) w->isl_off[i + 1] += w->isl_off[i];
+    /* Sleeping bodies whose contacts landed in two different islands: the reference solves those
+     * islands concurrently (ParallelFor), so such a body's velocity depends on thread timing there. */
+    w->st_shared_sleepers = 0;
+    if (w->allow_sleeping) {
+        uint32_t* seen = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * (size_t)w->nb);
+        for (int b = 0; b < w->nb; ++b) seen[b] = NUL;
+        for (uint32_t ci = 0; ci < w->ncons; ++ci) {
+            if (isl[ci] == NUL) continue;
+            const int ab[2] = {w->cons[ci].a, w->cons[ci].b};
+            for (int q = 0; q < 2; ++q) {
+                const int b = ab[q];
+                if (w->motion[b] != KZO_DYNAMIC || w->is_active[b]) continue;
+                if (seen[b] == NUL) seen[b] = isl[ci];
+                else if (seen[b] != isl[ci] && seen[b] != NUL - 1) { ++w->st_shared_sleepers; seen[b] = NUL - 1; }
+            }
+        }
+        free(seen);
+    }
     w->isl_con = (uint32_t*)xrealloc(w->isl_con, sizeof(uint32_t) * (w->ncons ? w->ncons : 1));
     uint32_t* fill = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * (ni ? ni : 1));
     for (uint32_t i = 0; i < ni; ++i) fill[i] = w->isl_off[i];
@@ -1366,9 +1401,8 @@ static void build_islands(kzo_world* w) {
         const joint_t* j = &w->joints[ji];
         uint32_t is = NUL;
         if (!(j->flags & 1u)) {
-            if (w->motion[j->a] == KZO_DYNAMIC && w->island_index[j->a] >= 0) is = r2i[uf_find(par, (uint32_t)w->island_index[j->a])];
-            if (is == NUL && w->motion[j->b] == KZO_DYNAMIC && w->island_index[j->b] >= 0)
-                is = r2i[uf_find(par, (uint32_t)w->island_index[j->b])];
+            is = island_of(w, par, r2i, numDyn, (int)j->a);
+            if (is == NUL) is = island_of(w, par, r2i, numDyn, (int)j->b);
         }
         jis[ji] = is;
         if (is != NUL) w->isl_joff[is + 1]++;
@@ -1382,6 +1416,99 @@ static void build_islands(kzo_world* w) {
     free(fill);
     free(isl);
     free(r2i);
+    free(rank);
+    free(par);
+}
+
+/* BodyManager::ActivateBody (BodyManager.cpp:133-141): an inactive body becomes active with a zero
+ * sleep timer and is appended to the active list. */
+static void activate_body(kzo_world* w, int b) {
+    if (w->is_active[b]) return;
+    w->is_active[b] = 1;
+    w->sleep_timer[b] = 0.0f;
+    w->active[w->nactive++] = b;
+}
+
+/* BodyManager::DeactivateBody (BodyManager.cpp:143-154): velocities zeroed, swap-removed from the
+ * active list (the last entry moves into its place; the buffer keeps the old last value). */
+static void deactivate_body(kzo_world* w, int b) {
+    if (!w->is_active[b]) return;
+    w->is_active[b] = 0;
+    w->lv[b] = V(0, 0, 0);
+    w->av[b] = V(0, 0, 0);
+    for (int k = 0; k < w->nactive; ++k)
+        if (w->active[k] == b) {
+            w->active[k] = w->active[w->nactive - 1];
+            --w->nactive;
+            break;
+        }
+}
+
+/* The wake rule of BuildContactConstraints (PhysicsWorld.cpp:473-490): a dynamic body is moving
+ * when active, a kinematic one when it has a velocity, a static one never. */
+static int body_moving(const kzo_world* w, int b) {
+    if (w->motion[b] == KZO_DYNAMIC) return w->is_active[b];
+    if (w->motion[b] == KZO_KINEMATIC) return vlen2(w->lv[b]) > 0.0f || vlen2(w->av[b]) > 0.0f;
+    return 0;
+}
+
+/* UpdateSleeping (PhysicsWorld.cpp:866-951).  Runs over the active list as it was when the pass
+ * began (n entries); the deactivation loop reads the list while swap-removals change it, which
+ * still visits every original entry once at its original position, and the island count at the end
+ * reads the list's buffer past its new end. */
+static void update_sleeping(kzo_world* w, float dt) {
+    if (!w->allow_sleeping) return;
+    const uint32_t n = (uint32_t)w->nactive;
+    if (n == 0) return;
+    const float lt = w->sleep_lin * w->sleep_lin, at = w->sleep_ang * w->sleep_ang;
+    for (uint32_t i = 0; i < n; ++i) {
+        const int b = w->active[i];
+        if (w->motion[b] != KZO_DYNAMIC || !w->allow_sleep[b]) { w->sleep_timer[b] = 0.0f; continue; }
+        if (vlen2(w->lv[b]) < lt && vlen2(w->av[b]) < at) w->sleep_timer[b] += dt;
+        else w->sleep_timer[b] = 0.0f;
+    }
+    uint32_t* par = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * n);
+    uint32_t* rank = (uint32_t*)calloc(n, sizeof(uint32_t));
+    for (uint32_t i = 0; i < n; ++i) par[i] = i;
+    for (uint32_t i = 0; i < n; ++i) w->island_index[w->active[i]] = i;
+    for (uint32_t ci = 0; ci < w->ncons; ++ci) {
+        const con_t* c = &w->cons[ci];
+        if (w->motion[c->a] != KZO_DYNAMIC || w->motion[c->b] != KZO_DYNAMIC) continue;
+        const uint32_t ia = w->island_index[c->a], ib = w->island_index[c->b];
+        if (ia < n && ib < n) uf_union(par, rank, ia, ib);
+    }
+    for (uint32_t ji = 0; ji < w->njoints; ++ji) {
+        const joint_t* j = &w->joints[ji];
+        if (j->flags & 1u) continue;
+        if (w->motion[j->a] != KZO_DYNAMIC || w->motion[j->b] != KZO_DYNAMIC) continue;
+        const uint32_t ia = w->island_index[j->a], ib = w->island_index[j->b];
+        if (ia < n && ib < n) uf_union(par, rank, ia, ib);
+    }
+    float* mt = (float*)xrealloc(NULL, sizeof(float) * n);
+    for (uint32_t i = 0; i < n; ++i) mt[i] = 1.0e18f; /* math::kBigNumber (Types.h:44) */
+    for (uint32_t i = 0; i < n; ++i) {
+        const int b = w->active[i];
+        if (w->motion[b] != KZO_DYNAMIC || !w->allow_sleep[b]) continue;
+        const uint32_t r = uf_find(par, i);
+        mt[r] = fmin_r(mt[r], w->sleep_timer[b]);
+    }
+    for (uint32_t i = 0; i < n; ++i) {
+        const int b = w->active[i]; /* the original entry i (see above) */
+        if (w->motion[b] != KZO_DYNAMIC || !w->allow_sleep[b]) continue;
+        if (mt[uf_find(par, i)] >= w->sleep_time) {
+            w->lv[b] = V(0, 0, 0);
+            w->av[b] = V(0, 0, 0);
+            deactivate_body(w, b);
+        }
+    }
+    uint32_t count = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const int b = w->active[i]; /* past the new end: the buffer's leftover values */
+        if (w->motion[b] != KZO_DYNAMIC) continue;
+        if (uf_find(par, i) == i) ++count;
+    }
+    w->st_islands = count;
+    free(mt);
     free(rank);
     free(par);
 }
@@ -1419,6 +1546,9 @@ static void build_constraints(kzo_world* w) {
         int A = body_of(w, w->pairs[2 * i]), B = body_of(w, w->pairs[2 * i + 1]);
         if (A < 0 || B < 0) continue;
         if (w->packed[A] > w->packed[B]) { int t = A; A = B; B = t; }
+        /* wake a sleeping dynamic body touched by a moving one, in pair order (:473-490) */
+        if (w->motion[A] == KZO_DYNAMIC && !w->is_active[A] && body_moving(w, B)) activate_body(w, A);
+        if (w->motion[B] == KZO_DYNAMIC && !w->is_active[B] && body_moving(w, A)) activate_body(w, B);
         cache_t* cached = w->no_ws ? NULL : find_cached(w, key);
         if (w->ncons == w->cons_cap) {
             w->cons_cap = w->cons_cap ? w->cons_cap * 2 : 1024;
@@ -1587,6 +1717,8 @@ int kzo_step(kzo_world* w, float dt) {
     for (uint32_t is = 0; is < w->nislands; ++is)
         for (uint32_t it = 0; it < w->pos_iters; ++it)
             for (uint32_t k = w->isl_joff[is]; k < w->isl_joff[is + 1]; ++k) joint_position(w, &w->joints[w->isl_joint[k]]);
+    /* 8. sleeping */
+    update_sleeping(w, dt);
     /* 9. clear forces */
     for (int i = 0; i < w->nb; ++i) { w->force[i] = V(0, 0, 0); w->torque[i] = V(0, 0, 0); }
     uint32_t pts = 0;
@@ -1626,7 +1758,7 @@ kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* res
     /* WorldSettings sleep thresholds (PhysicsWorld.h:25-27); version 1 scenes carry the defaults */
     w->sleep_time = 0.5f; w->sleep_lin = 0.05f; w->sleep_ang = 0.1f;
     if (version >= 2u) { w->sleep_time = rd_f32(&r); w->sleep_lin = rd_f32(&r); w->sleep_ang = rd_f32(&r); }
-    if (wflags & 1u) { set_err("sleeping is not supported by the oracle"); free(w); return NULL; }
+    w->allow_sleeping = (wflags & 1u) != 0;
     w->vel_bias = (wflags & 2u) != 0;
     w->no_ws = (wflags & 4u) != 0;
     w->fixed_dt = (float)(1.0 / 60.0); /* WorldSettings::fixedTimestep, PhysicsWorld.h:32 */
@@ -1684,7 +1816,8 @@ kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* res
     ALLOC(rot, qt);
     ALLOC(inv_mass, float); ALLOC(lin_damp, float); ALLOC(ang_damp, float); ALLOC(grav, float);
     ALLOC(max_lin, float); ALLOC(max_ang, float); ALLOC(fric, float); ALLOC(rest, float);
-    ALLOC(iil, m3); ALLOC(iiw, m3); ALLOC(active, int); ALLOC(island_index, int);
+    ALLOC(iil, m3); ALLOC(iiw, m3); ALLOC(active, int); ALLOC(island_index, uint32_t);
+    ALLOC(allow_sleep, uint8_t); ALLOC(is_active, uint8_t); ALLOC(sleep_timer, float);
 #undef ALLOC
     for (int i = 0; i < nb; ++i) {
         w->shape[i] = (int)rd_u32(&r);
@@ -1701,6 +1834,9 @@ kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* res
         uint32_t fl = rd_u32(&r);
         w->ccd_thr[i] = version >= 2u ? rd_f32(&r) : 0.0f; /* BodySettings::ccdMotionThreshold */
         w->sensor[i] = (fl & 1u) != 0;
+        w->allow_sleep[i] = (fl & 2u) != 0;
+        w->is_active[i] = 1;            /* BodyManager::CreateBody: active, in the active list */
+        w->island_index[i] = 0xFFFFFFFFu;
         w->ccd[i] = (fl & 4u) != 0;
         w->packed[i] = (uint32_t)i; /* BodyID(index, sequence 0).Packed() */
         w->active[i] = i;
@@ -1754,6 +1890,7 @@ void kzo_destroy(kzo_world* w) {
     void* ptrs[] = {w->packed, w->layer, w->mask, w->proxy, w->shape, w->motion, w->sensor, w->ccd, w->ccd_thr, w->fat, w->pos, w->lv, w->av,
                     w->plv, w->pav, w->force, w->torque, w->rot, w->inv_mass, w->lin_damp, w->ang_damp, w->grav,
                     w->max_lin, w->max_ang, w->fric, w->rest, w->iil, w->iiw, w->active, w->island_index,
+                    w->allow_sleep, w->is_active, w->sleep_timer,
                     w->nodes, w->bp_layer, w->bp_mask, w->cache, w->pairs, w->ext_pairs, w->man, w->keys,
                     w->cons, w->isl_off, w->isl_con, w->joints, w->isl_joff, w->isl_joint};
     for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; ++i) free(ptrs[i]);
@@ -1838,8 +1975,17 @@ void kzo_get_constraints(const kzo_world* w, uint32_t* hdr, float* pts, float* f
     }
 }
 
+uint32_t kzo_num_active(const kzo_world* w) { return (uint32_t)w->nactive; }
+void kzo_get_activity(const kzo_world* w, uint32_t* active_list, uint8_t* active_flags, float* sleep_timers) {
+    if (active_list)
+        for (int k = 0; k < w->nactive; ++k) active_list[k] = (uint32_t)w->active[k];
+    if (active_flags) memcpy(active_flags, w->is_active, (size_t)w->nb);
+    if (sleep_timers) memcpy(sleep_timers, w->sleep_timer, sizeof(float) * (size_t)w->nb);
+}
+uint32_t kzo_shared_sleepers(const kzo_world* w) { return w->st_shared_sleepers; }
+
 void kzo_get_stats(const kzo_world* w, uint32_t* o) {
-    o[0] = w->npairs; o[1] = w->ncons; o[2] = w->st_points; o[3] = w->nislands;
+    o[0] = w->npairs; o[1] = w->ncons; o[2] = w->st_points; o[3] = w->st_islands;
     o[4] = w->st_batches; o[5] = w->st_max_vl; o[6] = w->st_max_bl; o[7] = w->st_max_isl_pts; o[8] = w->st_sum_vl;
     o[9] = w->st_max_open;
     o[10] = w->st_max_iters; o[11] = w->st_pt_iters;

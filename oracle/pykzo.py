@@ -45,6 +45,11 @@ def lib():
         L.kzo_set_residual.argtypes = [vp, f32, u32]
         L.kzo_set_trig_mode.argtypes = [vp, ctypes.c_int]
         L.kzo_set_cache_hash.argtypes = [vp, ctypes.c_int]
+        L.kzo_num_active.restype = u32
+        L.kzo_num_active.argtypes = [vp]
+        L.kzo_get_activity.argtypes = [vp, vp, vp, vp]
+        L.kzo_shared_sleepers.restype = u32
+        L.kzo_shared_sleepers.argtypes = [vp]
         L.kzo_set_external_pairs.argtypes = [vp, vp, u32]
         L.kzo_step.argtypes = [vp, f32]
         L.kzo_num_bodies.restype = u32
@@ -111,6 +116,18 @@ class OracleWorld:
     def set_cache_hash(self, mixed: bool):
         """Mixed manifold-cache slot function (same results; avoids the reference's clustering)."""
         lib().kzo_set_cache_hash(self._w, int(mixed))
+
+    def activity(self):
+        """(active list in order, per-body active flags, per-body sleep timers)."""
+        n = lib().kzo_num_active(self._w)
+        lst = np.zeros(max(n, 1), np.uint32)
+        fl = np.zeros(self.n, np.uint8)
+        tm = np.zeros(self.n, np.float32)
+        lib().kzo_get_activity(self._w, _ptr(lst), _ptr(fl), _ptr(tm))
+        return lst[:n], fl, tm
+
+    def shared_sleepers(self) -> int:
+        return int(lib().kzo_shared_sleepers(self._w))
 
     def set_residual(self, tol: float, cap: int = 64):
         lib().kzo_set_residual(self._w, np.float32(tol), cap)

@@ -42,7 +42,46 @@ def fixture_scenes():
     out["joints_mix"] = (_joints_mix(), 180, 2, [0, 1, 59, 179])
     out["ccd_threshold"] = (_ccd_threshold(), 90, 2, [0, 1, 29, 89])
     out["joints_single"] = (_joints_single(), 60, 2, list(range(60)))
+    out["sleep_wake"] = (_sleep_wake(), 600, 2, [0, 59, 119, 239, 359, 479, 599])
+    out["pile120_sleep"] = (_sleeping(scenes.pile(120, seed=55, extent=2.5, y_range=(1.0, 8.0)), "pile120_sleep"),
+                            480, 2, [0, 119, 239, 479])
     return out
+
+
+def _sleeping(sc, name):
+    sc.flags |= scenes.WORLD_FLAG_ALLOW_SLEEPING
+    sc.name = name
+    return sc
+
+
+def _sleep_wake():
+    """Sleeping on (WorldSettings::allowSleeping, UpdateSleeping PhysicsWorld.cpp:866-951): small
+    structures settle and fall asleep, then are woken - a box dropped onto a sleeping pyramid, a
+    kinematic box pushing into a sleeping stack (a moving kinematic body wakes what it touches,
+    :473-490), a sphere dropped into sleeping spheres - beside a body that may not sleep."""
+    S = scenes
+    sc = S.Scene(name="sleep_wake")
+    S._timed_settings(sc, 10, 2)
+    sc.flags |= S.WORLD_FLAG_ALLOW_SLEEPING
+    S._ground(sc, 0.6)
+    box = sc.add_shape(S.Shape(S.SHAPE_BOX, [0.5, 0.5, 0.5, 0.0]))
+    small = sc.add_shape(S.Shape(S.SHAPE_BOX, [0.3, 0.3, 0.3, 0.0]))
+    ball = sc.add_shape(S.Shape(S.SHAPE_SPHERE, [0.3, 0.0, 0.0, 0.0]))
+    f = S.f32
+    for r in range(4):  # 4-row pyramid (the World_PyramidRest layout)
+        n = 4 - r
+        for i in range(n):
+            sc.add_body(S.Body(box, pos=(f((i - (n - 1) * 0.5) * 1.02), f(0.5 + r * 1.02), 0.0), friction=0.6))
+    for k in range(3):  # a stack
+        sc.add_body(S.Body(box, pos=(8.0, f(0.5 + 1.01 * k), 0.0), friction=0.6))
+    for k in range(5):  # loose spheres in a row
+        sc.add_body(S.Body(ball, pos=(f(-6.0 + 0.61 * k), 0.3, 4.0), friction=0.6))
+    sc.add_body(S.Body(small, pos=(3.0, 0.3, 4.0), friction=0.6, flags=0))  # may not sleep
+    sc.add_body(S.Body(small, pos=(0.05, 22.0, 0.1), friction=0.6))  # lands on the pyramid at ~2.1 s
+    sc.add_body(S.Body(ball, pos=(-4.8, 45.0, 4.0), friction=0.6))  # lands among the spheres at ~3 s
+    # kinematic pusher: reaches the stack after ~4 s
+    sc.add_body(S.Body(small, S.MOTION_KINEMATIC, pos=(4.0, 0.6, 0.0), vel=(0.8, 0.0, 0.0)))
+    return sc
 
 
 def _joints_single(copies: int = 8):
