@@ -29,7 +29,7 @@ typedef int kzg_status;
 #define KZG_ERR_INVALID (-1)     /* bad argument or call order */
 #define KZG_ERR_CUDA (-2)        /* CUDA runtime failure or no usable device */
 #define KZG_ERR_CAPACITY (-3)    /* a device table or buffer is full; raise the kzg_config limit */
-#define KZG_ERR_UNSUPPORTED (-4) /* feature outside the accelerated path (e.g. sleeping) */
+#define KZG_ERR_UNSUPPORTED (-4) /* feature outside the accelerated path (e.g. the scalar solver) */
 #define KZG_ERR_DEVICE (-5)      /* a kernel raised its error word (see kzg_stats.device_error) */
 
 /* Shape types: numbering of ShapeType (reference include/Kizuri/Geometry/Shape.h:13-25). */
@@ -103,7 +103,7 @@ typedef struct {
 typedef struct {
     float gravity[3];
     float fixed_timestep;   /* used for the broad-phase displacement, PhysicsWorld.cpp:342 */
-    int allow_sleeping;     /* must be 0: sleeping is outside the accelerated path */
+    int allow_sleeping;     /* WorldSettings::allowSleeping (default 1, as in the reference) */
     int warm_start;         /* 0 reproduces the reference's KZ_NOWS switch (PhysicsWorld.cpp:493) */
     int use_ccd;            /* WorldSettings::useCCD: clamp LinearCast bodies' motion (PhysicsWorld.cpp:785-852) */
     float ccd_max_penetration; /* WorldSettings::ccdMaxPenetration */
@@ -176,6 +176,7 @@ typedef struct {
     float broadphase_ms, narrowphase_ms, constraints_ms, schedule_ms, solve_ms, integrate_ms, step_ms;
     float final_residual; /* largest residual (relative impulse change, see kzg_solver_settings) of any
                            * island's last velocity iteration */
+    uint32_t num_active_bodies; /* WorldStats::numActiveBodies: the active list's length */
 } kzg_stats;
 
 #define KZG_DEVERR_PAIRS 1u     /* pair buffer overflow */
@@ -283,6 +284,21 @@ kzg_status kzg_download_transforms(kzg_ctx* ctx, float* out, uint32_t first, uin
  * body (force xyz, torque xyz); cleared after every step like Body::ClearForces. */
 kzg_status kzg_upload_forces(kzg_ctx* ctx, const float* force_torque, uint32_t first, uint32_t count);
 kzg_status kzg_download_mass(kzg_ctx* ctx, float* inv_mass, float* inv_inertia_world);
+
+/* ---- sleeping (WorldSettings::allowSleeping; UpdateSleeping, PhysicsWorld.cpp:866-951) --------
+ * With allow_sleeping set, islands whose dynamic bodies stayed below the sleep thresholds for
+ * sleep_time_threshold seconds are deactivated (velocities zeroed, removed from the active list),
+ * and a sleeping dynamic body touched by a moving one is woken (PhysicsWorld.cpp:473-490), with the
+ * reference's active-list order and island numbering.  One difference, by design: the reference
+ * solves concurrently two islands that both hold a contact of one sleeping body whose island index
+ * is stale past the active count (a race on that body's velocity); here such islands are joined and
+ * solved as one, deterministically. */
+/* PhysicsWorld::SetBodyActive / ActivateBody / DeactivateBody (PhysicsWorld.cpp:108-111, 132-133)
+ * for each packed BodyID in order (stale ids skipped). */
+kzg_status kzg_set_bodies_active(kzg_ctx* ctx, const uint32_t* packed_ids, uint32_t n, int active);
+/* BodyManager::GetActiveBodyList (packed BodyIDs in active-list order); *count receives its length,
+ * at most `capacity` ids are written. */
+kzg_status kzg_get_active_bodies(kzg_ctx* ctx, uint32_t* packed_ids, uint32_t capacity, uint32_t* count);
 
 /* ---- diagnostics (ComputeStateHash / GetStats / GetContactConstraints / GetPairs) ----------- */
 kzg_status kzg_state_hash(kzg_ctx* ctx, uint64_t* out); /* PhysicsWorld.cpp:1145-1175 */

@@ -68,7 +68,7 @@ class KzgStats(ctypes.Structure):
                                    "max_bias_levels", "cache_entries", "device_error", "kernel_launches",
                                    "max_velocity_iterations_used", "point_velocity_iterations")] + \
                [(n, f32) for n in ("broadphase_ms", "narrowphase_ms", "constraints_ms", "schedule_ms", "solve_ms",
-                                   "integrate_ms", "step_ms", "final_residual")]
+                                   "integrate_ms", "step_ms", "final_residual")] + [("num_active_bodies", u32)]
 
 
 class KzgJointDesc(ctypes.Structure):
@@ -143,6 +143,8 @@ def load(build_if_missing: bool = True):
     L.kzg_get_tuning.argtypes = [vp, P(KzgTuning)]
     L.kzg_autotune.argtypes = [vp, f32, u32, P(KzgTuning)]
     L.kzg_set_wait_limit.argtypes = [vp, u32]
+    L.kzg_set_bodies_active.argtypes = [vp, vp, u32, ctypes.c_int]
+    L.kzg_get_active_bodies.argtypes = [vp, vp, u32, P(u32)]
     L.kzg_mlp_set_params.argtypes = [vp, vp, vp, vp]
     L.kzg_mlp_get_params.argtypes = [vp, vp, vp, vp]
     L.kzg_mlp_enable.argtypes = [vp, ctypes.c_int]

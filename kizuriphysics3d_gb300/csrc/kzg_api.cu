@@ -40,8 +40,12 @@ kzg_status alloc_all(Ctx* ctx) {
     CK(dalloc(&b.iiw, 3 * B));
     CK(dalloc(&b.iil, 3 * B));
     CK(dalloc(&b.inv_mass, B));
-    uint32_t** u32b[] = {&b.shape, &b.motion, &b.flags, &b.layer, &b.mask, &b.world, &b.packed};
+    uint32_t** u32b[] = {&b.shape, &b.motion, &b.flags, &b.layer, &b.mask, &b.world, &b.packed, &b.act, &b.isl_idx,
+                         &b.apos, &ctx->alist, &ctx->node, &ctx->dyn2slot, &ctx->act_flag, &ctx->act_scan, &ctx->suf,
+                         &ctx->smin, &ctx->smark, &ctx->root_mark, &ctx->ccd_rank_keys, &ctx->ccd_sorted,
+                         &ctx->ccd_keys_sorted};
     for (uint32_t** p : u32b) CK(dalloc(p, B));
+    CK(dalloc(&b.sleep_t, B));
     CK(cudaMemset(b.plv, 0, sizeof(float4) * B));
     CK(cudaMemset(b.pav, 0, sizeof(float4) * B));
     CK(cudaMemset(b.force, 0, sizeof(float4) * B));
@@ -145,7 +149,10 @@ kzg_status alloc_all(Ctx* ctx) {
 
 void free_all(Ctx* ctx) {
     DeviceBodies& b = ctx->b;
-    void* ptrs[] = {b.pos, b.rot, b.lv, b.av, b.plv, b.pav, b.force, b.torque, b.prm0, b.prm1, b.aabb_mn, b.aabb_mx,
+    void* ptrs[] = {b.act, b.sleep_t, b.isl_idx, b.apos, ctx->alist, ctx->node, ctx->dyn2slot, ctx->act_flag,
+                    ctx->act_scan, ctx->suf, ctx->smin, ctx->smark, ctx->root_mark, ctx->ccd_rank_keys,
+                    ctx->ccd_sorted, ctx->ccd_keys_sorted,
+                    b.pos, b.rot, b.lv, b.av, b.plv, b.pav, b.force, b.torque, b.prm0, b.prm1, b.aabb_mn, b.aabb_mx,
                     b.iiw, b.iil, b.inv_mass, b.shape, b.motion, b.flags, b.layer, b.mask, b.world, b.packed, b.fat_mn, b.fat_mx,
                     ctx->is_large, ctx->large_list, ctx->large_off, ctx->cell_keys, ctx->cell_keys_sorted,
                     ctx->cell_vals, ctx->cell_vals_sorted, ctx->pair_keys, ctx->pair_keys_sorted, ctx->pairs,
@@ -249,7 +256,7 @@ void kzg_default_settings(kzg_world_settings* ws, kzg_solver_settings* ss) {
     if (ws) {
         ws->gravity[0] = 0.0f; ws->gravity[1] = -9.81f; ws->gravity[2] = 0.0f;
         ws->fixed_timestep = (float)(1.0 / 60.0);
-        ws->allow_sleeping = 0;
+        ws->allow_sleeping = 1;  // WorldSettings::allowSleeping (PhysicsWorld.h:24)
         ws->warm_start = 1;
         ws->use_ccd = 1;                 // WorldSettings defaults, PhysicsWorld.h:39-42
         ws->ccd_max_penetration = 0.01f;
@@ -350,9 +357,10 @@ kzg_status kzg_synchronize(kzg_ctx* k) {
 kzg_status kzg_set_world_settings(kzg_ctx* k, const kzg_world_settings* s) {
     if (k) k->c.graph_dirty = true;
     if (check(k) || !s) return KZG_ERR_INVALID;
-    if (s->allow_sleeping) {
-        k->c.err = "sleeping (WorldSettings::allowSleeping) is outside the accelerated path";
-        return KZG_ERR_UNSUPPORTED;
+    if (!(s->sleep_time_threshold >= 0.0f) || !(s->sleep_linear_threshold >= 0.0f) ||
+        !(s->sleep_angular_threshold >= 0.0f)) {
+        k->c.err = "sleep thresholds must be >= 0";
+        return KZG_ERR_INVALID;
     }
     k->c.ws = *s;
     return KZG_OK;
@@ -518,7 +526,7 @@ kzg_status kzg_add_bodies(kzg_ctx* k, uint32_t n, const kzg_body_soa* b, uint32_
         CK(cudaMemcpy(ctx->ccd_list + ctx->nccd, cast.data(), sizeof(uint32_t) * cast.size(), cudaMemcpyHostToDevice));
         ctx->nccd += (uint32_t)cast.size();
     }
-    CK(init_fat_bounds(*ctx, base, n));
+    CK(init_new_bodies(*ctx, base, n));
     h.dirty = true;
     ctx->nbodies += n;
     if (first_slot) *first_slot = base;
@@ -603,6 +611,9 @@ struct DeviceBackup {
         regions.push_back({c.c_pos, sizeof(float4) * 4 * H});
         regions.push_back({c.c_imp, sizeof(float4) * 4 * H});
         regions.push_back({&c.dcnt->cache_entries, sizeof(uint32_t)});
+        regions.push_back({&c.dcnt->nact, sizeof(uint32_t)});
+        for (void* p : {(void*)b.act, (void*)b.sleep_t, (void*)b.isl_idx, (void*)b.apos, (void*)c.alist})
+            regions.push_back({p, sizeof(uint32_t) * nb});
         if (c.njoints) regions.push_back({c.joints, joint_record_bytes() * c.njoints});
         size_t total = 0;
         for (auto& r : regions) total += (r.second + 255) & ~size_t(255);
@@ -785,6 +796,34 @@ kzg_status kzg_download_mass(kzg_ctx* k, float* im, float* iw) {
     return KZG_OK;
 }
 
+kzg_status kzg_set_bodies_active(kzg_ctx* k, const uint32_t* packed_ids, uint32_t n, int active) {
+    if (check(k) || (n && !packed_ids)) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    if (n == 0) return KZG_OK;
+    CK(cudaSetDevice(ctx->device));
+    if (n > ctx->cfg.max_pairs) { ctx->err = "more ids than kzg_config.max_pairs per call"; return KZG_ERR_CAPACITY; }
+    CK(cudaMemcpyAsync(ctx->pair_keys, packed_ids, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(set_bodies_active(*ctx, reinterpret_cast<const uint32_t*>(ctx->pair_keys), n, active));
+    return KZG_OK;
+}
+
+kzg_status kzg_get_active_bodies(kzg_ctx* k, uint32_t* packed_ids, uint32_t capacity, uint32_t* count) {
+    if (check(k) || !count) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    CK(cudaSetDevice(ctx->device));
+    uint32_t n = 0;
+    CK(cudaMemcpyAsync(&n, &ctx->dcnt->nact, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    *count = n;
+    if (!packed_ids || capacity == 0 || n == 0) return KZG_OK;
+    const uint32_t m = std::min(n, capacity);
+    std::vector<uint32_t> slots(m), packed(ctx->nbodies);
+    CK(cudaMemcpy(slots.data(), ctx->alist, sizeof(uint32_t) * m, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(packed.data(), ctx->b.packed, sizeof(uint32_t) * ctx->nbodies, cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < m; ++i) packed_ids[i] = packed[slots[i]];
+    return KZG_OK;
+}
+
 kzg_status kzg_state_hash(kzg_ctx* k, uint64_t* out) {
     if (check(k) || !out) return KZG_ERR_INVALID;
     return hash_state(k->c, out);
@@ -866,12 +905,13 @@ kzg_status kzg_download_constraints(kzg_ctx* k, uint32_t* hdr, float* fr, float*
 // ---- device snapshots: body state, the manifold cache and the joints, for exact resume -------
 namespace {
 constexpr uint32_t kSnapMagic = 0x53475A4Bu;  // 'KZGS'
-constexpr uint32_t kSnapVersion = 3;
+constexpr uint32_t kSnapVersion = 4;
 struct SnapHeader {
-    uint32_t magic, version, nbodies, cache_cap, cache_entries, cache_used, njoints, reserved;
+    uint32_t magic, version, nbodies, cache_cap, cache_entries, cache_used, njoints, reserved;  // reserved: active-list length
 };
 constexpr int kSnapBodyArrays = 10;  // pos, rot, lv, av, plv, pav, force, torque, fat bounds (+ 3 iiw columns)
-constexpr size_t kSnapBodyBytes = sizeof(float4) * (kSnapBodyArrays + 3);
+// + per body: activity, sleep timer, island index, active-list position, active-list buffer entry
+constexpr size_t kSnapBodyBytes = sizeof(float4) * (kSnapBodyArrays + 3) + 5 * sizeof(uint32_t);
 constexpr size_t kSnapCacheBytes = sizeof(uint32_t) + sizeof(unsigned long long) + sizeof(uint32_t) + 8 * sizeof(float4);
 
 float4** snap_body_arrays(DeviceBodies& b, float4** out) {
@@ -931,6 +971,12 @@ kzg_status kzg_snapshot_save(kzg_ctx* k, void* out, size_t capacity) {
     }
     CK(cudaMemcpy(p, ctx->b.iiw, sizeof(float4) * 3 * nb, cudaMemcpyDeviceToHost));
     p += sizeof(float4) * 3 * nb;
+    for (void* a : {(void*)ctx->b.act, (void*)ctx->b.sleep_t, (void*)ctx->b.isl_idx, (void*)ctx->b.apos, (void*)ctx->alist}) {
+        CK(cudaMemcpy(p, a, sizeof(uint32_t) * nb, cudaMemcpyDeviceToHost));
+        p += sizeof(uint32_t) * nb;
+    }
+    CK(cudaMemcpy(&h.reserved, &ctx->dcnt->nact, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    std::memcpy(out, &h, sizeof(h));  // header again with the active-list length
     for (size_t slot = 0; slot < H; ++slot) {  // occupied slots of the open-addressing table
         if (!keys[slot]) continue;
         const uint32_t s32 = (uint32_t)slot;
@@ -970,6 +1016,12 @@ kzg_status kzg_snapshot_load(kzg_ctx* k, const void* in, size_t size) {
     }
     CK(cudaMemcpy(ctx->b.iiw, p, sizeof(float4) * 3 * nb, cudaMemcpyHostToDevice));
     p += sizeof(float4) * 3 * nb;
+    for (void* a : {(void*)ctx->b.act, (void*)ctx->b.sleep_t, (void*)ctx->b.isl_idx, (void*)ctx->b.apos, (void*)ctx->alist}) {
+        CK(cudaMemcpy(a, p, sizeof(uint32_t) * nb, cudaMemcpyHostToDevice));
+        p += sizeof(uint32_t) * nb;
+    }
+    if (h.reserved > nb) { ctx->err = "kzg_snapshot_load: active-list length out of range"; return KZG_ERR_INVALID; }
+    CK(cudaMemcpy(&ctx->dcnt->nact, &h.reserved, sizeof(uint32_t), cudaMemcpyHostToDevice));
     std::vector<unsigned long long> keys(H, 0ull);
     std::vector<uint32_t> np(H, 0u);
     std::vector<float4> pos(4 * H, make_float4(0.0f, 0.0f, 0.0f, 0.0f)), imp(4 * H, make_float4(0.0f, 0.0f, 0.0f, 0.0f));

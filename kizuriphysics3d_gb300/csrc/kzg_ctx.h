@@ -30,6 +30,10 @@ struct DeviceBodies {
     uint32_t *shape, *motion, *flags, *layer, *mask, *world, *packed;
     float4 *aabb_mn, *aabb_mx;
     float4 *fat_mn, *fat_mx;  // broad-phase fat bounds (DynamicAABBTree leaves, BroadPhase.cpp:35-75)
+    uint32_t* act;     // 1: ActivationState::Active (every body is active while sleeping is off)
+    float* sleep_t;    // MotionProperties::sleepTimer
+    uint32_t* isl_idx; // Body::mIslandIndex: compact island index or active-list position, stale while asleep
+    uint32_t* apos;    // position in the active list (kNone while asleep)
 };
 
 struct DeviceRows {  // per point row, index = 4 * constraint + point
@@ -63,8 +67,12 @@ struct Counters {  // device-side counters, copied back after each stage that si
     uint32_t njisl;      // islands holding joints
     uint32_t nx_sched_w, nx_sched_c, nx_solve_w, nx_solve_c;  // largest-first island order: next island to take
     uint32_t nroots;     // islands as the reference counts them: every dynamic body's union-find root
+    uint32_t ndyn;       // active dynamic bodies (BuildIslands' compact index range)
+    uint32_t nsleep_n;   // active-list length when the sleeping pass began
+    uint32_t sleep_islands;  // WorldStats::numIslands as the sleeping pass counts it
     uint32_t cache_entries;  // persists across steps
     uint32_t frame;          // step counter, advanced on the device by k_begin_step
+    uint32_t nact;           // active-list length (persists)
 };
 
 // Learned warm start (kzg_mlp.cu): model, optimiser state, training log and dataset.
@@ -182,6 +190,13 @@ struct Ctx {
     uint32_t *con_la = nullptr, *con_lb = nullptr;             // per constraint local body indices
     uint32_t *isl_small = nullptr, *isl_large = nullptr;       // islands by solve kernel
     uint32_t* isl_order = nullptr;   // largest-first island order (KZG_ISLANDS_LARGEST_FIRST)
+    // sleeping: the active list (BodyManager::mActiveBodies; the buffer keeps values past its end, as
+    // the reference's swap-removal does) and per-step scratch
+    uint32_t* alist = nullptr;
+    uint32_t *node = nullptr, *dyn2slot = nullptr, *act_flag = nullptr, *act_scan = nullptr;
+    uint32_t *suf = nullptr, *smin = nullptr, *smark = nullptr, *root_mark = nullptr;
+    uint32_t* ccd_rank_keys = nullptr;  // continuous collision in active-list order
+    uint32_t *ccd_sorted = nullptr, *ccd_keys_sorted = nullptr;
     uint32_t* isl_bins = nullptr;    // its 32 size bins: counts, then cursors (64 words)
     uint32_t* miss_rows = nullptr;                              // rows without a cached warm start
     float4* miss_prior = nullptr;  // per miss: nearest cached point's impulses, pair's cached normal impulse per point

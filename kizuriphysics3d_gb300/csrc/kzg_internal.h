@@ -18,7 +18,8 @@ cudaError_t configure_kernels();  // per-device kernel attributes (large dynamic
 // (cap) and float4 elements to allocate.
 size_t pack_elements(uint32_t points, uint32_t* cap);
 size_t cluster_id_words(uint32_t max_cons);  // local-id scratch of the cluster solve
-cudaError_t init_fat_bounds(Ctx& ctx, uint32_t first, uint32_t n);  // broad-phase fat bounds of new bodies
+cudaError_t init_new_bodies(Ctx& ctx, uint32_t first, uint32_t n);  // fat bounds, activity, active list of new bodies
+cudaError_t set_bodies_active(Ctx& ctx, const uint32_t* dev_ids, uint32_t n, int active);  // in order
 cudaError_t create_joints(Ctx& ctx, uint32_t first, uint32_t n);     // joint records from ctx.joint_stage
 size_t joint_record_bytes();
 kzg_status step_canonical(Ctx& ctx, float dt, uint32_t nsteps);

@@ -70,7 +70,7 @@ __device__ __forceinline__ AABB body_bounds(const DeviceBodies& b, const ShapeDe
 // BroadPhase.cpp:58-75): unchanged while they contain the tight bounds, else the tight bounds
 // grown by the 0.1 margin and by |velocity x fixed timestep|.  Continuous collision tests them.
 __device__ __forceinline__ void update_fat(const DeviceBodies& b, uint32_t i, const AABB& w, float fixed_dt) {
-    if (b.motion[i] == KZG_MOTION_STATIC) return;
+    if (b.motion[i] == KZG_MOTION_STATIC || !b.act[i]) return;  // UpdateBroadPhase walks the active list
     const Vec3 fmn = V3(b.fat_mn[i]), fmx = V3(b.fat_mx[i]);
     if (fmn.x <= w.mn.x && fmx.x >= w.mx.x && fmn.y <= w.mn.y && fmx.y >= w.mx.y && fmn.z <= w.mn.z &&
         fmx.z >= w.mx.z)
@@ -80,15 +80,25 @@ __device__ __forceinline__ void update_fat(const DeviceBodies& b, uint32_t i, co
     b.fat_mx[i] = F4((w.mx + margin) + d, 0.0f);
 }
 
-__global__ void k_init_fat(DeviceBodies b, const ShapeDev* __restrict__ shapes, uint32_t first, uint32_t n) {
+// New bodies (BodyManager::CreateBody, BodyManager.cpp:15-61): fat bounds, active, appended to the
+// active list in creation order, no island index yet.
+__global__ void k_init_bodies(DeviceBodies b, const ShapeDev* __restrict__ shapes, uint32_t first, uint32_t n,
+                              uint32_t* alist, const Counters* cnt) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const uint32_t at = cnt->nact + i;
     i += first;
     const AABB w = body_bounds(b, shapes, i);
     const Vec3 margin(0.1f, 0.1f, 0.1f);  // CreateProxy: tight bounds + margin
     b.fat_mn[i] = F4(w.mn - margin, 0.0f);
     b.fat_mx[i] = F4(w.mx + margin, 0.0f);
+    b.act[i] = 1u;
+    b.sleep_t[i] = 0.0f;
+    b.isl_idx[i] = 0xFFFFFFFFu;
+    b.apos[i] = at;
+    alist[at] = i;
 }
+__global__ void k_grow_active(Counters* cnt, uint32_t n) { cnt->nact += n; }
 
 __global__ void k_fat(DeviceBodies b, const ShapeDev* __restrict__ shapes, uint32_t n, float fixed_dt) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -393,7 +403,7 @@ __global__ void k_build_constraints(const uint2* __restrict__ pairs, const uint3
 // ---------------------------------------------------------------------------------------------
 __global__ void k_integrate_vel(DeviceBodies b, uint32_t n, float3 g, float dt) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || b.motion[i] != KZG_MOTION_DYNAMIC) return;
+    if (i >= n || b.motion[i] != KZG_MOTION_DYNAMIC || !b.act[i]) return;  // the active list's bodies
     float4 p0 = b.prm0[i], p1 = b.prm1[i];
     float im = b.inv_mass[i];
     Vec3 lv = V3(b.lv[i]), av = V3(b.av[i]);
@@ -490,11 +500,7 @@ __device__ __forceinline__ uint32_t uf_find(uint32_t* uf, uint32_t x) {
         x = p;
     }
 }
-__global__ void k_uf_union(const Counters* cnt, const uint32_t* __restrict__ con_a, const uint32_t* __restrict__ con_b,
-                           const uint32_t* __restrict__ con_bits, uint32_t* uf) {
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= cnt->ncons || (con_bits[c] & 6u) != 6u) return;
-    uint32_t a = con_a[c], bb = con_b[c];
+__device__ __forceinline__ void uf_link(uint32_t* uf, uint32_t a, uint32_t bb) {
     for (;;) {
         a = uf_find(uf, a);
         bb = uf_find(uf, bb);
@@ -504,6 +510,32 @@ __global__ void k_uf_union(const Counters* cnt, const uint32_t* __restrict__ con
         if (old == bb) return;
         bb = old;
     }
+}
+
+// The union-find element a dynamic body joins islands through.  Sleeping off (node == null): the
+// body itself.  Sleeping on: an active body itself; a sleeping body the active dynamic body that now
+// holds its stale island index (BuildIslands' compact index, PhysicsWorld.cpp:593-605, 616-623), or
+// none when that index is past the active dynamic count.
+__device__ __forceinline__ uint32_t island_node(const uint32_t* __restrict__ node, uint32_t x) {
+    return node ? node[x] : x;
+}
+
+// Joins two dynamic bodies' islands (BuildIslands' contact and joint unions).  With sleeping on, a
+// sleeping body without a node still links the islands it touches (its own slot as the link):
+// the reference puts each of its contacts in the other body's island and then solves those islands
+// concurrently, a race on the sleeping body; joined, they are solved as one, deterministically.
+__device__ __forceinline__ void island_union(uint32_t* uf, const uint32_t* __restrict__ node, uint32_t a, uint32_t bb) {
+    const uint32_t na = island_node(node, a), nb = island_node(node, bb);
+    if (na != kInvalid && nb != kInvalid) uf_link(uf, na, nb);
+    else if (na != kInvalid) uf_link(uf, na, bb);
+    else if (nb != kInvalid) uf_link(uf, a, nb);
+}
+
+__global__ void k_uf_union(const Counters* cnt, const uint32_t* __restrict__ con_a, const uint32_t* __restrict__ con_b,
+                           const uint32_t* __restrict__ con_bits, const uint32_t* __restrict__ node, uint32_t* uf) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cnt->ncons || (con_bits[c] & 6u) != 6u) return;
+    island_union(uf, node, con_a[c], con_b[c]);
 }
 // WorldStats::numIslands (PhysicsWorld.cpp:636-642): one island per union-find root among the
 // dynamic bodies, bodies without a contact included.
@@ -516,9 +548,13 @@ __global__ void k_count_roots(const DeviceBodies b, uint32_t n, const uint32_t* 
 
 // Island of every constraint; slots past the constraint count (up to cap) get a key above every
 // body index so that a capacity-sized sort leaves them at the end.
+// islandOf(A), else islandOf(B) (PhysicsWorld.cpp:645-650): the root of the first dynamic body with
+// an island node; a constraint with neither (two sleeping bodies, both indices stale) is in no
+// island and is not solved.  Such constraints, and slots past the constraint count (up to cap), get
+// a key above every body index so that a capacity-sized sort leaves them at the end.
 __global__ void k_island_keys(const Counters* cnt, const uint32_t* __restrict__ con_a, const uint32_t* __restrict__ con_b,
-                              const uint32_t* __restrict__ con_bits, uint32_t* uf, uint32_t* key, uint32_t* val,
-                              uint32_t cap, uint32_t pad) {
+                              const uint32_t* __restrict__ con_bits, const uint32_t* __restrict__ node, uint32_t* uf,
+                              uint32_t* key, uint32_t* val, uint32_t cap, uint32_t pad) {
     uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cnt->ncons) {
         if (c < cap) {
@@ -527,28 +563,214 @@ __global__ void k_island_keys(const Counters* cnt, const uint32_t* __restrict__ 
         }
         return;
     }
-    uint32_t d = (con_bits[c] & 2u) ? con_a[c] : con_b[c];  // islandOf(A), else islandOf(B)
-    key[c] = uf_find(uf, d);
+    const uint32_t bits = con_bits[c];
+    const uint32_t na = (bits & 2u) ? island_node(node, con_a[c]) : kInvalid;
+    const uint32_t d = na != kInvalid ? na : ((bits & 4u) ? island_node(node, con_b[c]) : kInvalid);
+    key[c] = d != kInvalid ? uf_find(uf, d) : pad;
     val[c] = c;
 }
-__global__ void k_island_heads(const Counters* cnt, const uint32_t* __restrict__ skey, uint32_t* head) {
+__global__ void k_island_heads(const Counters* cnt, const uint32_t* __restrict__ skey, uint32_t* head, uint32_t pad) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= cnt->ncons) return;
-    head[s] = (s == 0 || skey[s] != skey[s - 1]) ? 1u : 0u;
+    head[s] = (skey[s] != pad && (s == 0 || skey[s] != skey[s - 1])) ? 1u : 0u;
 }
-__global__ void k_island_starts(Counters* cnt, const uint32_t* __restrict__ head, const uint32_t* __restrict__ hscan,
-                                uint32_t* start) {
+// Island ranges of the sorted constraints; the constraints keyed `pad` (in no island) sort last and
+// end the last island.
+__global__ void k_island_starts(Counters* cnt, const uint32_t* __restrict__ skey, const uint32_t* __restrict__ head,
+                                const uint32_t* __restrict__ hscan, uint32_t* start, uint32_t pad) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t n = cnt->ncons;
     if (s >= n) return;
     if (head[s]) start[hscan[s]] = s;
-    if (s == n - 1) {
+    if (skey[s] != pad && (s == n - 1 || skey[s + 1] == pad)) {
         uint32_t ni = hscan[s] + head[s];
-        start[ni] = n;
+        start[ni] = s + 1;
         cnt->nislands = ni;
     }
 }
 
+
+// ---------------------------------------------------------------------------------------------
+// sleeping (WorldSettings::allowSleeping): the wake rule of BuildContactConstraints
+// (PhysicsWorld.cpp:473-490), BuildIslands' compact indices over the active list (:593-605) and
+// UpdateSleeping (:866-951) with the active list of BodyManager (BodyManager.cpp:133-160)
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ bool body_moving(const DeviceBodies& b, uint32_t i) {
+    const uint32_t m = b.motion[i];
+    if (m == KZG_MOTION_DYNAMIC) return __ldcg(&b.act[i]) != 0u;
+    if (m == KZG_MOTION_KINEMATIC) return V3(b.lv[i]).len2() > 0.0f || V3(b.av[i]).len2() > 0.0f;
+    return false;
+}
+
+// One warp walks the constraints in order, 32 at a time, and wakes a sleeping dynamic body touched
+// by a moving one exactly as the sequential loop does: lanes before the first lane that wakes a body
+// are final; that lane's wakes (A, then B, which then sees A moving) are applied - appended to the
+// active list - and the lanes after it are decided again on the new state.
+__global__ void __launch_bounds__(32) k_wake(DeviceBodies b, Counters* cnt, const uint32_t* __restrict__ con_a,
+                                             const uint32_t* __restrict__ con_b, uint32_t* alist) {
+    const uint32_t lane = threadIdx.x;
+    const uint32_t nc = cnt->ncons;
+    for (uint32_t w0 = 0; w0 < nc; w0 += 32) {
+        const uint32_t c = w0 + lane;
+        const bool v = c < nc;
+        const uint32_t A = v ? con_a[c] : 0u, B = v ? con_b[c] : 0u;
+        const bool dA = v && b.motion[A] == KZG_MOTION_DYNAMIC, dB = v && b.motion[B] == KZG_MOTION_DYNAMIC;
+        uint32_t from = 0;
+        for (;;) {
+            bool wa = false, wb = false;
+            if (v && lane >= from) {
+                wa = dA && __ldcg(&b.act[A]) == 0u && body_moving(b, B);
+                wb = dB && __ldcg(&b.act[B]) == 0u && (wa || body_moving(b, A));
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, wa || wb);
+            if (!m) break;
+            const uint32_t f = (uint32_t)(__ffs(m) - 1);
+            if (lane == f) {
+                uint32_t n = cnt->nact;
+                if (wa) { b.act[A] = 1u; b.sleep_t[A] = 0.0f; b.apos[A] = n; alist[n++] = A; }
+                if (wb) { b.act[B] = 1u; b.sleep_t[B] = 0.0f; b.apos[B] = n; alist[n++] = B; }
+                cnt->nact = n;
+                __threadfence_block();
+            }
+            __syncwarp();
+            from = f + 1;
+        }
+    }
+}
+
+// BuildIslands' compact index: active dynamic bodies numbered in active-list order.
+__global__ void k_act_flags(const DeviceBodies b, const Counters* cnt, const uint32_t* __restrict__ alist, uint32_t cap,
+                            uint32_t* flag) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= cap) return;
+    flag[p] = (p < cnt->nact && b.motion[alist[p]] == KZG_MOTION_DYNAMIC) ? 1u : 0u;
+}
+__global__ void k_act_index(DeviceBodies b, Counters* cnt, const uint32_t* __restrict__ alist,
+                            const uint32_t* __restrict__ flag, const uint32_t* __restrict__ scan, uint32_t* dyn2slot) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = cnt->nact;
+    if (p >= n) return;
+    const uint32_t x = alist[p];
+    b.isl_idx[x] = flag[p] ? scan[p] : 0xFFFFFFFFu;
+    if (flag[p]) dyn2slot[scan[p]] = x;
+    if (p == n - 1) cnt->ndyn = scan[p] + flag[p];
+}
+// Island node of every body (see island_node) and the union-find start.
+__global__ void k_nodes(const DeviceBodies b, const Counters* cnt, uint32_t nb, const uint32_t* __restrict__ dyn2slot,
+                        uint32_t* node, uint32_t* uf) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    uint32_t nd = kInvalid;
+    if (b.motion[i] == KZG_MOTION_DYNAMIC) {
+        if (b.act[i]) nd = i;
+        else if (b.isl_idx[i] < cnt->ndyn) nd = dyn2slot[b.isl_idx[i]];
+    }
+    node[i] = nd;
+    uf[i] = i;
+}
+// WorldStats::numIslands of BuildIslands with sleeping on: the sets holding an active dynamic body.
+__global__ void k_mark_roots(const DeviceBodies b, uint32_t nb, uint32_t* uf, uint32_t* mark) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nb && b.motion[i] == KZG_MOTION_DYNAMIC && b.act[i]) mark[uf_find(uf, i)] = 1u;
+}
+__global__ void k_count_marks(const uint32_t* __restrict__ mark, uint32_t nb, Counters* cnt) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned m = __ballot_sync(0xffffffffu, i < nb && mark[i] != 0u);
+    if ((threadIdx.x & 31u) == 0 && m) atomicAdd(&cnt->nroots, (uint32_t)__popc(m));
+}
+
+// UpdateSleeping, pass 1: sleep timers of the active bodies; island index = active-list position;
+// union-find over positions and the islands' smallest timer start.
+__global__ void k_sleep_begin(DeviceBodies b, Counters* cnt, const uint32_t* __restrict__ alist, uint32_t cap,
+                              float lin2, float ang2, float dt, uint32_t* suf, uint32_t* smin) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = cnt->nact;
+    if (p == 0) cnt->nsleep_n = n;
+    if (p >= cap) return;
+    suf[p] = p;
+    smin[p] = __float_as_uint(1.0e18f);  // math::kBigNumber (Types.h:44)
+    if (p >= n) return;
+    const uint32_t x = alist[p];
+    b.isl_idx[x] = p;
+    if (b.motion[x] != KZG_MOTION_DYNAMIC || !(b.flags[x] & KZG_BODY_ALLOW_SLEEPING)) {
+        b.sleep_t[x] = 0.0f;
+        return;
+    }
+    if (V3(b.lv[x]).len2() < lin2 && V3(b.av[x]).len2() < ang2) b.sleep_t[x] = b.sleep_t[x] + dt;
+    else b.sleep_t[x] = 0.0f;
+}
+// pass 2: contacts between dynamic bodies whose island indices are both below n join.
+__global__ void k_sleep_union(const DeviceBodies b, const Counters* cnt, const uint32_t* __restrict__ con_a,
+                              const uint32_t* __restrict__ con_b, const uint32_t* __restrict__ con_bits, uint32_t* suf) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cnt->ncons || (con_bits[c] & 6u) != 6u) return;
+    const uint32_t n = cnt->nsleep_n, ia = b.isl_idx[con_a[c]], ib = b.isl_idx[con_b[c]];
+    if (ia < n && ib < n) uf_link(suf, ia, ib);
+}
+// pass 3: each island's smallest timer (timers are >= 0, so their bits order like the floats).
+__global__ void k_sleep_min(const DeviceBodies b, const Counters* cnt, const uint32_t* __restrict__ alist, uint32_t* suf,
+                            uint32_t* smin) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= cnt->nsleep_n) return;
+    const uint32_t x = alist[p];
+    if (b.motion[x] != KZG_MOTION_DYNAMIC || !(b.flags[x] & KZG_BODY_ALLOW_SLEEPING)) return;
+    atomicMin(&smin[uf_find(suf, p)], __float_as_uint(b.sleep_t[x]));
+}
+// pass 4: bodies of islands quiet for the threshold are deactivated, velocities zeroed (their
+// removal from the active list follows in order).
+__global__ void k_sleep_mark(DeviceBodies b, const Counters* cnt, const uint32_t* __restrict__ alist, uint32_t* suf,
+                             const uint32_t* __restrict__ smin, float threshold, uint32_t* mark) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= cnt->nsleep_n) return;
+    const uint32_t x = alist[p];
+    uint32_t m = kInvalid;
+    if (b.motion[x] == KZG_MOTION_DYNAMIC && (b.flags[x] & KZG_BODY_ALLOW_SLEEPING) &&
+        __uint_as_float(smin[uf_find(suf, p)]) >= threshold) {
+        b.lv[x] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        b.av[x] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        b.act[x] = 0u;
+        m = x;
+    }
+    mark[p] = m;
+}
+// pass 5 (one warp): BodyManager::DeactivateBody's swap-removal, body by body in active-list order:
+// the last entry moves into the removed one's place; the buffer keeps the old last value.
+__global__ void __launch_bounds__(32) k_sleep_remove(DeviceBodies b, Counters* cnt, uint32_t* alist,
+                                                     const uint32_t* __restrict__ mark) {
+    const uint32_t lane = threadIdx.x;
+    const uint32_t n = cnt->nsleep_n;
+    uint32_t size = n;
+    for (uint32_t p0 = 0; p0 < n; p0 += 32) {
+        const uint32_t p = p0 + lane;
+        const uint32_t x = p < n ? mark[p] : kInvalid;
+        unsigned m = __ballot_sync(0xffffffffu, x != kInvalid);
+        while (m) {
+            const uint32_t l = (uint32_t)(__ffs(m) - 1);
+            m &= m - 1u;
+            const uint32_t xb = __shfl_sync(0xffffffffu, x, l);
+            if (lane == 0) {
+                const uint32_t at = b.apos[xb], last = size - 1u;
+                if (at != last) {
+                    const uint32_t moved = alist[last];
+                    alist[at] = moved;
+                    b.apos[moved] = at;
+                }
+                b.apos[xb] = kInvalid;
+                --size;
+            }
+            size = __shfl_sync(0xffffffffu, size, 0);
+        }
+    }
+    if (lane == 0) cnt->nact = size;
+}
+// pass 6: the island count UpdateSleeping leaves in WorldStats, read over the list's buffer after
+// the removals (positions past the new end hold leftover values).
+__global__ void k_sleep_count(const DeviceBodies b, Counters* cnt, const uint32_t* __restrict__ alist, uint32_t* suf) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool c = p < cnt->nsleep_n && b.motion[alist[p]] == KZG_MOTION_DYNAMIC && uf_find(suf, p) == p;
+    const unsigned m = __ballot_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31u) == 0 && m) atomicAdd(&cnt->sleep_islands, (uint32_t)__popc(m));
+}
 
 // Largest-first island order (KZG_ISLANDS_LARGEST_FIRST): islands binned by the power of two of
 // their constraint count and listed bin by bin from the largest down; inside a bin the order is
@@ -600,33 +822,27 @@ __global__ void k_joint_prepare(DeviceBodies b, JointDev* J, uint32_t n) {
 }
 
 // Joints between two dynamic bodies join their islands (PhysicsWorld.cpp:625-633).
-__global__ void k_joint_union(DeviceBodies b, const JointDev* __restrict__ J, uint32_t n, uint32_t* uf) {
+__global__ void k_joint_union(DeviceBodies b, const JointDev* __restrict__ J, uint32_t n,
+                              const uint32_t* __restrict__ node, uint32_t* uf) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || (J[i].flags & kJointDisabled)) return;
-    uint32_t a = J[i].a, bb = J[i].b;
+    const uint32_t a = J[i].a, bb = J[i].b;
     if (b.motion[a] != KZG_MOTION_DYNAMIC || b.motion[bb] != KZG_MOTION_DYNAMIC) return;
-    for (;;) {
-        a = uf_find(uf, a);
-        bb = uf_find(uf, bb);
-        if (a == bb) return;
-        if (a > bb) { uint32_t t = a; a = bb; bb = t; }
-        uint32_t old = atomicCAS(&uf[bb], bb, a);
-        if (old == bb) return;
-        bb = old;
-    }
+    island_union(uf, node, a, bb);
 }
 
 // Island of each joint: islandOf(A), else islandOf(B) (PhysicsWorld.cpp:656-661), as the root of its
 // dynamic body, keyed root << 32 | joint index so that a sort groups islands in joint order; a
 // joint with no dynamic body or disabled gets ~0 (sorted last, never solved).
-__global__ void k_joint_keys(DeviceBodies b, const JointDev* __restrict__ J, uint32_t n, uint32_t* uf,
-                             unsigned long long* keys) {
+__global__ void k_joint_keys(DeviceBodies b, const JointDev* __restrict__ J, uint32_t n,
+                             const uint32_t* __restrict__ node, uint32_t* uf, unsigned long long* keys) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     unsigned long long key = ~0ull;
     if (!(J[i].flags & kJointDisabled)) {
         const uint32_t a = J[i].a, bb = J[i].b;
-        const uint32_t d = b.motion[a] == KZG_MOTION_DYNAMIC ? a : (b.motion[bb] == KZG_MOTION_DYNAMIC ? bb : kNone);
+        const uint32_t na = b.motion[a] == KZG_MOTION_DYNAMIC ? island_node(node, a) : kNone;
+        const uint32_t d = na != kNone ? na : (b.motion[bb] == KZG_MOTION_DYNAMIC ? island_node(node, bb) : kNone);
         if (d != kNone) key = ((unsigned long long)uf_find(uf, d) << 32) | i;
     }
     keys[i] = key;
@@ -668,6 +884,16 @@ __global__ void k_joint_positions(DeviceBodies b, JointDev* J, const unsigned lo
         for (uint32_t s = r.x; s < r.y; ++s) joint_position(B, J[(uint32_t)sk[s]]);
 }
 
+// UpdateSleeping's joint unions (PhysicsWorld.cpp:907-915), beside k_sleep_union.
+__global__ void k_sleep_union_joints(const DeviceBodies b, const Counters* cnt, const JointDev* __restrict__ J,
+                                     uint32_t nj, uint32_t* suf) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nj || (J[i].flags & kJointDisabled)) return;
+    const uint32_t a = J[i].a, bb = J[i].b;
+    if (b.motion[a] != KZG_MOTION_DYNAMIC || b.motion[bb] != KZG_MOTION_DYNAMIC) return;
+    const uint32_t n = cnt->nsleep_n, ia = b.isl_idx[a], ib = b.isl_idx[bb];
+    if (ia < n && ib < n) uf_link(suf, ia, ib);
+}
 cudaError_t create_joints(Ctx& ctx, uint32_t first, uint32_t n) {
     k_joint_create<<<blocks_for(n), kThreads, 0, ctx.stream>>>(ctx.b, ctx.joints, ctx.joint_stage, first, n);
     cudaError_t e = cudaGetLastError();
@@ -774,14 +1000,21 @@ struct CcdHit {
 // first such j of the lane on a tie.
 // `best` (shared by the lanes working on body i): the smallest fraction any of them has found, as
 // int bits (fractions are >= 0), so a lane's advancement stops early once it cannot win.
+// Whether body j's position was already integrated when the position loop reaches body i: the loop
+// walks the active list (PhysicsWorld.cpp:785-802), which is slot order while nothing has slept;
+// with sleeping on, by active-list position, and a sleeping body is never integrated.
+__device__ __forceinline__ bool integrated_before(const DeviceBodies& b, uint32_t j, uint32_t i, bool by_rank) {
+    return by_rank ? (b.act[j] != 0u && b.apos[j] < b.apos[i]) : j < i;
+}
+
 __device__ CcdHit ccd_scan(const ShapeTables& T, const DeviceBodies& b, uint32_t n, uint32_t i, const CcdBody& c,
-                           float dt, const float4* disp, uint32_t lane, uint32_t nl, int* best) {
+                           float dt, const float4* disp, uint32_t lane, uint32_t nl, int* best, bool by_rank) {
     CcdHit h{1.0f, kNoHit, Vec3(0.0f, 1.0f, 0.0f)};
     for (uint32_t j = lane; j < n; j += nl) {
         if (!ccd_candidate(b, c, i, j)) continue;
         Vec3 tj = V3(b.pos[j]);
         Quat qj = Q4(b.rot[j]);
-        if (j < i && b.motion[j] != KZG_MOTION_STATIC) {  // already integrated this step
+        if (b.motion[j] != KZG_MOTION_STATIC && integrated_before(b, j, i, by_rank)) {  // already integrated this step
             tj = tj + (casts_linear(b, j) ? V3(disp[j]) : V3(b.lv[j]) * dt);
             const Vec3 avj = V3(b.av[j]);
             if (avj.len2() > 0.0f) qj = integrate_rotation(qj, avj, dt);
@@ -818,6 +1051,12 @@ __device__ __forceinline__ void ccd_finish(const DeviceBodies& b, uint32_t i, co
 }
 
 constexpr uint32_t kPending = 0xFFFFFFFFu;
+
+// Sort keys of the LinearCast bodies by active-list position (sleeping ones last).
+__global__ void k_ccd_rank_keys(const DeviceBodies b, const uint32_t* __restrict__ list, uint32_t nlist, uint32_t* keys) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nlist) keys[k] = b.act[list[k]] ? b.apos[list[k]] : 0xFFFFFFFFu;
+}
 constexpr uint32_t kCcdRounds = 64;
 constexpr uint32_t kCcdMaxDeps = 8;  // more predecessors than this: solved by k_ccd_serial
 
@@ -826,6 +1065,10 @@ __global__ void k_ccd_init(DeviceBodies b, uint32_t n, const uint32_t* __restric
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nlist) return;
     const uint32_t i = list[k];
+    if (!b.act[i]) {  // asleep: not integrated this step
+        round[i] = 0u;
+        return;
+    }
     const Vec3 d = V3(b.lv[i]) * dt;
     const float dist = d.len(), thr = b.prm1[i].w;  // per-body ccdMotionThreshold (PhysicsWorld.cpp:806-807)
     if (casts_linear(b, i) && dist > max_pen && !(thr > 0.0f && dist < thr)) {
@@ -840,7 +1083,7 @@ __global__ void k_ccd_init(DeviceBodies b, uint32_t n, const uint32_t* __restric
 // in slot order, at most kCcdMaxDeps (a count above that sends the body to k_ccd_serial).
 __global__ void k_ccd_deps(DeviceBodies b, const ShapeDev* __restrict__ shapes, uint32_t n,
                            const uint32_t* __restrict__ list, uint32_t nlist, float dt, const uint32_t* round,
-                           uint32_t* deps, uint32_t* ndeps) {
+                           uint32_t* deps, uint32_t* ndeps, bool by_rank) {
     const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
     if (k >= nlist) return;
     const uint32_t i = list[k];
@@ -848,9 +1091,11 @@ __global__ void k_ccd_deps(DeviceBodies b, const ShapeDev* __restrict__ shapes, 
     const ShapeTables T{shapes, nullptr, nullptr, nullptr};
     const CcdBody c = ccd_body(T, b, i, dt);
     uint32_t cnt = 0;
-    for (uint32_t j0 = 0; j0 < i && cnt <= kCcdMaxDeps; j0 += 32u) {
+    const uint32_t jend = by_rank ? n : i;
+    for (uint32_t j0 = 0; j0 < jend && cnt <= kCcdMaxDeps; j0 += 32u) {
         const uint32_t j = j0 + lane;
-        const bool dep = j < i && casts_linear(b, j) && round[j] == kPending && ccd_candidate(b, c, i, j);
+        const bool dep = j < jend && integrated_before(b, j, i, by_rank) && casts_linear(b, j) &&
+                         round[j] == kPending && ccd_candidate(b, c, i, j);
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, dep);
         const uint32_t pos = cnt + __popc(m & ((1u << lane) - 1u));
         if (dep && pos < kCcdMaxDeps) deps[k * kCcdMaxDeps + pos] = j;
@@ -861,7 +1106,8 @@ __global__ void k_ccd_deps(DeviceBodies b, const ShapeDev* __restrict__ shapes, 
 
 __global__ void k_ccd_round(ShapeTables T, DeviceBodies b, uint32_t n, const uint32_t* __restrict__ list,
                             uint32_t nlist, float dt, float max_pen, float4* disp, uint32_t* round,
-                            const uint32_t* __restrict__ deps, const uint32_t* __restrict__ ndeps, uint32_t r) {
+                            const uint32_t* __restrict__ deps, const uint32_t* __restrict__ ndeps, uint32_t r,
+                            bool by_rank) {
     const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
     if (k >= nlist) return;
     const uint32_t i = list[k];
@@ -875,7 +1121,7 @@ __global__ void k_ccd_round(ShapeTables T, DeviceBodies b, uint32_t n, const uin
     if (lane == 0) *best = __float_as_int(1.0f);
     __syncwarp();
     const CcdBody c = ccd_body(T, b, i, dt);
-    CcdHit h = ccd_scan(T, b, n, i, c, dt, disp, lane, 32u, best);
+    CcdHit h = ccd_scan(T, b, n, i, c, dt, disp, lane, 32u, best, by_rank);
     for (uint32_t off = 16; off > 0; off >>= 1) {
         CcdHit o;
         o.frac = __shfl_down_sync(0xFFFFFFFFu, h.frac, off);
@@ -894,7 +1140,7 @@ __global__ void k_ccd_round(ShapeTables T, DeviceBodies b, uint32_t n, const uin
 __global__ void __launch_bounds__(kCcdThreads) k_ccd_serial(ShapeTables T, DeviceBodies b, uint32_t n,
                                                             const uint32_t* __restrict__ list, uint32_t nlist,
                                                             float dt, float max_pen, float4* disp,
-                                                            const uint32_t* __restrict__ round) {
+                                                            const uint32_t* __restrict__ round, bool by_rank) {
     __shared__ float s_frac[kCcdThreads];
     __shared__ uint32_t s_slot[kCcdThreads];
     __shared__ float4 s_norm[kCcdThreads];
@@ -916,7 +1162,7 @@ __global__ void __launch_bounds__(kCcdThreads) k_ccd_serial(ShapeTables T, Devic
             if (tid == 0) s_best = __float_as_int(1.0f);
             __syncthreads();
             const CcdBody c = ccd_body(T, b, i, dt);
-            const CcdHit h = ccd_scan(T, b, n, i, c, dt, disp, tid, kCcdThreads, &s_best);
+            const CcdHit h = ccd_scan(T, b, n, i, c, dt, disp, tid, kCcdThreads, &s_best, by_rank);
             s_frac[tid] = h.frac;
             s_slot[tid] = h.slot;
             s_norm[tid] = F4(h.n, 0.0f);
@@ -943,7 +1189,7 @@ __global__ void k_integrate_pos(DeviceBodies b, uint32_t n, float dt, int vel_bi
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t mt = b.motion[i];
-    if (mt != KZG_MOTION_STATIC) {
+    if (mt != KZG_MOTION_STATIC && b.act[i]) {  // IntegratePositions and the pseudo-velocity pass walk the active list
         Vec3 p = V3(b.pos[i]);
         Quat q = Q4(b.rot[i]);
         Vec3 lv = V3(b.lv[i]), av = V3(b.av[i]);
@@ -1095,6 +1341,11 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
         ctx.con_a, ctx.con_b, ctx.con_np, ctx.con_bits, ctx.con_fr, ctx.con_key, ctx.r, ctx.c_key, ctx.c_np, ctx.c_pos,
         ctx.c_imp, ctx.cfg.max_cache_entries, ctx.ws.warm_start,
         (ctx.mlp.logging || (ctx.mlp.enabled && ctx.mlp.have)) ? ctx.miss_rows : nullptr, ctx.miss_prior);
+    const bool sleeping = ctx.ws.allow_sleeping != 0;
+    if (sleeping) {
+        k_wake<<<1, 32, 0, st>>>(ctx.b, ctx.dcnt, ctx.con_a, ctx.con_b, ctx.alist);
+        ++ctx.launches;
+    }
     k_integrate_vel<<<blocks_for(nb), kThreads, 0, st>>>(
         ctx.b, nb, make_float3(ctx.ws.gravity[0], ctx.ws.gravity[1], ctx.ws.gravity[2]), dt);
     ctx.launches += 7;  // narrow (2), flags, scan (2), build, integrate
@@ -1104,21 +1355,43 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     ctx.launches += mlp_after_prepare(ctx, dt);
     const uint32_t nj = ctx.njoints;
     if (nj) k_joint_prepare<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, nj);
-    k_uf_init<<<blocks_for(nb), kThreads, 0, st>>>(ctx.uf, nb);
-    k_uf_union<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf);
-    if (nj) k_joint_union<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, nj, ctx.uf);
-    k_count_roots<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, ctx.uf, ctx.dcnt);
-    ++ctx.launches;
+    const uint32_t* node = nullptr;  // island nodes (sleeping on); null: every dynamic body is its own
+    if (sleeping) {
+        k_act_flags<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.alist, nb, ctx.act_flag);
+        tb = ctx.cub_tmp_bytes;
+        KZG_CK(cub::DeviceScan::ExclusiveSum(ctx.cub_tmp, tb, ctx.act_flag, ctx.act_scan, (int)nb, st));
+        k_act_index<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.alist, ctx.act_flag, ctx.act_scan,
+                                                         ctx.dyn2slot);
+        k_nodes<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, ctx.dcnt, nb, ctx.dyn2slot, ctx.node, ctx.uf);
+        node = ctx.node;
+        ctx.launches += 5;  // flags, scan (2), index, nodes
+    } else {
+        k_uf_init<<<blocks_for(nb), kThreads, 0, st>>>(ctx.uf, nb);
+        ++ctx.launches;
+    }
+    k_uf_union<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, node, ctx.uf);
+    if (nj) k_joint_union<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, nj, node, ctx.uf);
+    if (sleeping) {
+        KZG_CK(cudaMemsetAsync(ctx.root_mark, 0, sizeof(uint32_t) * nb, st));
+        k_mark_roots<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, ctx.uf, ctx.root_mark);
+        k_count_marks<<<blocks_for(nb), kThreads, 0, st>>>(ctx.root_mark, nb, ctx.dcnt);
+        ctx.launches += 2;
+    } else {
+        k_count_roots<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, ctx.uf, ctx.dcnt);
+        ++ctx.launches;
+    }
     const int kbits = bits_for(nb);
-    k_island_keys<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.uf,
-                                                      ctx.isl_key, ctx.isl_con_in, P, (1u << kbits) - 1u);
+    const uint32_t pad = (1u << kbits) - 1u;
+    k_island_keys<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, node, ctx.uf,
+                                                      ctx.isl_key, ctx.isl_con_in, P, pad);
     tb = ctx.cub_tmp_bytes;
     KZG_CK(cub::DeviceRadixSort::SortPairs(ctx.cub_tmp, tb, ctx.isl_key, ctx.isl_key_sorted, ctx.isl_con_in,
                                            ctx.isl_con, (int)P, 0, kbits, st));
-    k_island_heads<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_key_sorted, ctx.isl_head);
+    k_island_heads<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_key_sorted, ctx.isl_head, pad);
     tb = ctx.cub_tmp_bytes;
     KZG_CK(cub::DeviceScan::ExclusiveSum(ctx.cub_tmp, tb, ctx.isl_head, ctx.isl_pts, (int)P, st));
-    k_island_starts<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_head, ctx.isl_pts, ctx.isl_start);
+    k_island_starts<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.isl_key_sorted, ctx.isl_head, ctx.isl_pts,
+                                                        ctx.isl_start, pad);
     const bool lpt = ctx.tune.island_order == KZG_ISLANDS_LARGEST_FIRST;
     if (lpt) {
         KZG_CK(cudaMemsetAsync(ctx.isl_bins, 0, sizeof(uint32_t) * 32, st));
@@ -1128,7 +1401,7 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
         ctx.launches += 3;
     }
     if (nj) {
-        k_joint_keys<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, nj, ctx.uf, ctx.jkeys);
+        k_joint_keys<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, nj, node, ctx.uf, ctx.jkeys);
         tb = ctx.cub_tmp_bytes;
         KZG_CK(cub::DeviceRadixSort::SortKeys(ctx.cub_tmp, tb, ctx.jkeys, ctx.jkeys_sorted, (int)nj, 0, 64, st));
         KZG_CK(cudaMemsetAsync(ctx.jflag, 0, sizeof(uint32_t) * (P + 1), st));
@@ -1146,7 +1419,7 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
                  lpt ? ctx.isl_order : nullptr};
     k_schedule_warp<<<152u * 16u, 128, 0, st>>>(SB, ctx.dcnt);
     k_schedule_cta<<<152u * 2u, 256, 3 * kSchedCtaBodies * sizeof(uint32_t), st>>>(SB, ctx.dcnt);
-    ctx.launches += 17;  // prepare, union-find (3), island sort (4 CUB passes), heads, scan (2), starts, schedule (2)
+    ctx.launches += 16;  // prepare, union-find (2), island sort (4 CUB passes), heads, scan (2), starts, schedule (2)
     KZG_CK(mark(ctx, 4));
     SolveBufs SV{ctx.isl_start, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.con_la, ctx.con_lb, ctx.isl_meta,
                  ctx.isl_bodies, ctx.wl_list, ctx.vl_list, ctx.bl_list, ctx.wl_off, ctx.vl_off, ctx.bl_off,
@@ -1178,16 +1451,27 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     if (ccd) {
         ShapeTables T{ctx.shapes, ctx.hull_verts, ctx.face_sizes, ctx.face_idx};
         const float mp = ctx.ws.ccd_max_penetration;
-        k_ccd_init<<<blocks_for(ctx.nccd), kThreads, 0, st>>>(ctx.b, nb, ctx.ccd_list, ctx.nccd, dt, mp, ctx.ccd_disp,
+        // the position loop's order: slot order, or with sleeping on the active list's
+        const uint32_t* list = ctx.ccd_list;
+        if (sleeping) {
+            k_ccd_rank_keys<<<blocks_for(ctx.nccd), kThreads, 0, st>>>(ctx.b, ctx.ccd_list, ctx.nccd, ctx.ccd_rank_keys);
+            size_t tbc = ctx.cub_tmp_bytes;
+            KZG_CK(cub::DeviceRadixSort::SortPairs(ctx.cub_tmp, tbc, ctx.ccd_rank_keys, ctx.ccd_keys_sorted,
+                                                   ctx.ccd_list, ctx.ccd_sorted, (int)ctx.nccd, 0, 32, st));
+            list = ctx.ccd_sorted;
+            ctx.launches += 5;
+        }
+        k_ccd_init<<<blocks_for(ctx.nccd), kThreads, 0, st>>>(ctx.b, nb, list, ctx.nccd, dt, mp, ctx.ccd_disp,
                                                                ctx.ccd_state);
-        k_ccd_deps<<<blocks_for(32u * ctx.nccd), kThreads, 0, st>>>(ctx.b, ctx.shapes, nb, ctx.ccd_list, ctx.nccd,
-                                                                    dt, ctx.ccd_state, ctx.ccd_deps, ctx.ccd_ndeps);
+        k_ccd_deps<<<blocks_for(32u * ctx.nccd), kThreads, 0, st>>>(ctx.b, ctx.shapes, nb, list, ctx.nccd,
+                                                                    dt, ctx.ccd_state, ctx.ccd_deps, ctx.ccd_ndeps,
+                                                                    sleeping);
         for (uint32_t r = 1; r <= kCcdRounds; ++r)
-            k_ccd_round<<<blocks_for(32u * ctx.nccd), kThreads, 0, st>>>(T, ctx.b, nb, ctx.ccd_list, ctx.nccd, dt, mp,
+            k_ccd_round<<<blocks_for(32u * ctx.nccd), kThreads, 0, st>>>(T, ctx.b, nb, list, ctx.nccd, dt, mp,
                                                                          ctx.ccd_disp, ctx.ccd_state, ctx.ccd_deps,
-                                                                         ctx.ccd_ndeps, r);
-        k_ccd_serial<<<1, kCcdThreads, 0, st>>>(T, ctx.b, nb, ctx.ccd_list, ctx.nccd, dt, mp, ctx.ccd_disp,
-                                                ctx.ccd_state);
+                                                                         ctx.ccd_ndeps, r, sleeping);
+        k_ccd_serial<<<1, kCcdThreads, 0, st>>>(T, ctx.b, nb, list, ctx.nccd, dt, mp, ctx.ccd_disp,
+                                                ctx.ccd_state, sleeping);
         ctx.launches += 3 + kCcdRounds;
     }
     k_integrate_pos<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, dt, ctx.ss.use_velocity_bias,
@@ -1197,6 +1481,20 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
         k_joint_positions<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, ctx.jkeys_sorted, ctx.jisl,
                                                                ctx.dcnt, ctx.ss.position_iterations);
         ++ctx.launches;
+    }
+    if (sleeping) {  // UpdateSleeping (PhysicsWorld.cpp:866-951)
+        const float lin2 = ctx.ws.sleep_linear_threshold * ctx.ws.sleep_linear_threshold;
+        const float ang2 = ctx.ws.sleep_angular_threshold * ctx.ws.sleep_angular_threshold;
+        k_sleep_begin<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.alist, nb, lin2, ang2, dt, ctx.suf,
+                                                           ctx.smin);
+        k_sleep_union<<<blocks_for(P), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.suf);
+        if (nj) k_sleep_union_joints<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.joints, nj, ctx.suf);
+        k_sleep_min<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.alist, ctx.suf, ctx.smin);
+        k_sleep_mark<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.alist, ctx.suf, ctx.smin,
+                                                          ctx.ws.sleep_time_threshold, ctx.smark);
+        k_sleep_remove<<<1, 32, 0, st>>>(ctx.b, ctx.dcnt, ctx.alist, ctx.smark);
+        k_sleep_count<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.alist, ctx.suf);
+        ctx.launches += nj ? 7 : 6;
     }
     KZG_CK(mark(ctx, 6));
     KZG_CK(cudaGetLastError());
@@ -1210,7 +1508,9 @@ static kzg_status finish_stats(Ctx& ctx, uint32_t graph_steps = 0) {
     s.num_broadphase_pairs = h.npairs;
     s.num_contact_constraints = h.ncons;
     s.num_contact_points = h.npoints;
-    s.num_islands = h.nroots;
+    // WorldStats::numIslands: BuildIslands' count, replaced by UpdateSleeping's when that pass ran
+    s.num_islands = (ctx.ws.allow_sleeping && h.nsleep_n) ? h.sleep_islands : h.nroots;
+    s.num_active_bodies = h.nact;
     s.num_batches = h.batches;
     s.max_velocity_levels = h.max_vlev;
     s.max_bias_levels = h.max_blev;
@@ -1343,9 +1643,50 @@ kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t np, floa
     return finish_stats(ctx);
 }
 
-cudaError_t init_fat_bounds(Ctx& ctx, uint32_t first, uint32_t n) {
+// PhysicsWorld::SetBodyActive / ActivateBody / DeactivateBody (PhysicsWorld.cpp:108-111, 132-133;
+// BodyManager.cpp:133-160) for a list of packed BodyIDs, one after another in the given order; stale
+// ids are skipped.  One thread: the active list is order-dependent.
+__global__ void k_set_active(DeviceBodies b, Counters* cnt, uint32_t* alist, const uint32_t* __restrict__ ids, uint32_t n,
+                             uint32_t nb, int active) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    uint32_t size = cnt->nact;
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint32_t x = ids[k] & 0x00FFFFFFu;
+        if (x >= nb || b.packed[x] != ids[k]) continue;
+        if (active) {
+            if (b.act[x]) continue;
+            b.act[x] = 1u;
+            b.sleep_t[x] = 0.0f;
+            b.apos[x] = size;
+            alist[size++] = x;
+        } else {
+            if (!b.act[x]) continue;
+            b.act[x] = 0u;
+            b.lv[x] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            b.av[x] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const uint32_t at = b.apos[x], last = size - 1u;
+            if (at != last) {
+                const uint32_t moved = alist[last];
+                alist[at] = moved;
+                b.apos[moved] = at;
+            }
+            b.apos[x] = kInvalid;
+            --size;
+        }
+    }
+    cnt->nact = size;
+}
+
+cudaError_t set_bodies_active(Ctx& ctx, const uint32_t* dev_ids, uint32_t n, int active) {
+    k_set_active<<<1, 1, 0, ctx.stream>>>(ctx.b, ctx.dcnt, ctx.alist, dev_ids, n, ctx.nbodies, active);
+    cudaError_t e = cudaGetLastError();
+    return e != cudaSuccess ? e : cudaStreamSynchronize(ctx.stream);
+}
+
+cudaError_t init_new_bodies(Ctx& ctx, uint32_t first, uint32_t n) {
     if (n == 0) return cudaSuccess;
-    k_init_fat<<<blocks_for(n), kThreads, 0, ctx.stream>>>(ctx.b, ctx.shapes, first, n);
+    k_init_bodies<<<blocks_for(n), kThreads, 0, ctx.stream>>>(ctx.b, ctx.shapes, first, n, ctx.alist, ctx.dcnt);
+    k_grow_active<<<1, 1, 0, ctx.stream>>>(ctx.dcnt, n);
     cudaError_t e = cudaGetLastError();
     return e != cudaSuccess ? e : cudaStreamSynchronize(ctx.stream);
 }

@@ -311,6 +311,21 @@ class World:
         self._check(capi.load().kzg_download_mass(self._h, capi.ptr(im), capi.ptr(iw)))
         return im, iw
 
+    # -- sleeping (PhysicsWorld::SetBodyActive / GetNumActiveBodies) ------------------------------
+    def active_bodies(self) -> np.ndarray:
+        """The active list: packed BodyIDs in the reference's order."""
+        L = capi.load()
+        n = ctypes.c_uint32()
+        self._check(L.kzg_get_active_bodies(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(max(n.value, 1), np.uint32)
+        if n.value:
+            self._check(L.kzg_get_active_bodies(self._h, capi.ptr(out), n.value, ctypes.byref(n)))
+        return out[:n.value]
+
+    def set_bodies_active(self, packed_ids, active: bool):
+        ids = np.ascontiguousarray(packed_ids, np.uint32).reshape(-1)
+        self._check(capi.load().kzg_set_bodies_active(self._h, capi.ptr(ids), ids.size, int(bool(active))))
+
     # -- diagnostics ----------------------------------------------------------------------------
     def compute_state_hash(self) -> int:
         h = ctypes.c_uint64()

@@ -56,6 +56,8 @@ uint32_t kzo_num_active(const kzo_world* w);
 void kzo_get_activity(const kzo_world* w, uint32_t* active_list, uint8_t* active_flags, float* sleep_timers);
 /* Sleeping bodies whose contacts were assigned to two different islands in the last step. */
 uint32_t kzo_shared_sleepers(const kzo_world* w);
+/* PhysicsWorld::SetBodyActive for each packed id in order (stale ids skipped). */
+void kzo_set_bodies_active(kzo_world* w, const uint32_t* ids, uint32_t n, int active);
 
 int kzo_step(kzo_world* w, float dt);
 

@@ -1983,6 +1983,15 @@ void kzo_get_activity(const kzo_world* w, uint32_t* active_list, uint8_t* active
     if (sleep_timers) memcpy(sleep_timers, w->sleep_timer, sizeof(float) * (size_t)w->nb);
 }
 uint32_t kzo_shared_sleepers(const kzo_world* w) { return w->st_shared_sleepers; }
+/* PhysicsWorld::SetBodyActive (PhysicsWorld.cpp:108-111) for packed ids in order. */
+void kzo_set_bodies_active(kzo_world* w, const uint32_t* ids, uint32_t n, int active) {
+    for (uint32_t k = 0; k < n; ++k) {
+        const int b = body_of(w, ids[k]);
+        if (b < 0) continue;
+        if (active) activate_body(w, b);
+        else deactivate_body(w, b);
+    }
+}
 
 void kzo_get_stats(const kzo_world* w, uint32_t* o) {
     o[0] = w->npairs; o[1] = w->ncons; o[2] = w->st_points; o[3] = w->st_islands;

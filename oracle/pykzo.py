@@ -50,6 +50,7 @@ def lib():
         L.kzo_get_activity.argtypes = [vp, vp, vp, vp]
         L.kzo_shared_sleepers.restype = u32
         L.kzo_shared_sleepers.argtypes = [vp]
+        L.kzo_set_bodies_active.argtypes = [vp, vp, u32, ctypes.c_int]
         L.kzo_set_external_pairs.argtypes = [vp, vp, u32]
         L.kzo_step.argtypes = [vp, f32]
         L.kzo_num_bodies.restype = u32
@@ -125,6 +126,10 @@ class OracleWorld:
         tm = np.zeros(self.n, np.float32)
         lib().kzo_get_activity(self._w, _ptr(lst), _ptr(fl), _ptr(tm))
         return lst[:n], fl, tm
+
+    def set_bodies_active(self, packed_ids, active: bool):
+        ids = np.ascontiguousarray(packed_ids, np.uint32).reshape(-1)
+        lib().kzo_set_bodies_active(self._w, _ptr(ids), ids.size, int(bool(active)))
 
     def shared_sleepers(self) -> int:
         return int(lib().kzo_shared_sleepers(self._w))
