@@ -379,8 +379,10 @@ struct CtaSync {
 };
 
 // Stage an island's velocities in shared memory, run the warm-start and velocity sweeps, write
-// them back; then reuse the same buffers for the split-impulse pseudo velocities (zero at the
-// start of every step, PhysicsWorld.cpp:286-287) and the bias sweeps.
+// them back; then reuse the same buffers for the split-impulse pseudo velocities and the bias
+// sweeps.  Pseudo velocities are loaded, not assumed zero: the position pass clears them only for
+// active bodies (PhysicsWorld.cpp:276-290), so a sleeping body solved in an island keeps
+// accumulating them until it wakes.
 template <typename Sync>
 __device__ __forceinline__ void solve_island_shared(const SolveBufs& S, uint32_t isl, float4* sv, float4* sw,
                                                     uint32_t tid, uint32_t nthreads, Sync sync, Counters* cnt) {
@@ -396,8 +398,8 @@ __device__ __forceinline__ void solve_island_shared(const SolveBufs& S, uint32_t
     for (uint32_t k = tid; k < nloc; k += nthreads) {
         S.b.lv[bodies[k]] = sv[k];
         S.b.av[bodies[k]] = sw[k];
-        sv[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        sw[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        sv[k] = S.b.plv[bodies[k]];
+        sw[k] = S.b.pav[bodies[k]];
     }
     sync();
     solve_bias(S, isl, V, tid, nthreads, sync);
@@ -1130,8 +1132,8 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
             const uint32_t b = __ldcg(&body_of[k * kClusterCtas + rank]);
             S.b.lv[b] = sv[k];
             S.b.av[b] = sw[k];
-            sv[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // pseudo velocities start at zero
-            sw[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            sv[k] = S.b.plv[b];  // pseudo velocities (non-zero only for sleeping bodies)
+            sw[k] = S.b.pav[b];
         }
         cl.sync();
         if (!S.vel_bias) {

@@ -109,7 +109,7 @@ struct kzo_world {
     uint8_t* is_active;     /* ActivationState::Active */
     float* sleep_timer;     /* MotionProperties::sleepTimer */
     uint32_t st_islands;    /* WorldStats::numIslands as the step leaves it */
-    uint32_t st_shared_sleepers; /* sleeping bodies solved by two islands in the last step */
+    uint32_t st_shared_sleepers; /* islands joined through a sleeping body in the last step (see build_islands) */
     /* broad phase tree */
     node_t* nodes;
     uint32_t nnodes, node_cap, root, free_list, nproxies;
@@ -1334,22 +1334,42 @@ static void build_islands(kzo_world* w) {
     w->nislands = 0;
     w->st_islands = 0;
     if (numDyn == 0) return;
-    uint32_t* par = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * numDyn);
-    uint32_t* rank = (uint32_t*)calloc(numDyn, sizeof(uint32_t));
-    for (uint32_t i = 0; i < numDyn; ++i) par[i] = i;
-    for (uint32_t ci = 0; ci < w->ncons; ++ci) {
-        con_t* c = &w->cons[ci];
-        if (w->motion[c->a] != KZO_DYNAMIC || w->motion[c->b] != KZO_DYNAMIC) continue;
-        uint32_t ia = w->island_index[c->a], ib = w->island_index[c->b];
-        if (ia < numDyn && ib < numDyn) uf_union(par, rank, ia, ib);
+    /* Elements [0, numDyn) are the compact indices.  A sleeping body whose stale index is past
+     * numDyn gets a link element: the reference puts each of its contacts in the other body's island
+     * and solves those islands concurrently (a race on the sleeping body); linked, they become one
+     * island, solved deterministically.  Without such a body the islands are the reference's. */
+    uint32_t nel = numDyn;
+    uint32_t* link = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * (size_t)w->nb);
+    for (int b = 0; b < w->nb; ++b) {
+        link[b] = NUL;
+        if (w->allow_sleeping && w->motion[b] == KZO_DYNAMIC && !w->is_active[b] && w->island_index[b] >= numDyn)
+            link[b] = nel++;
     }
-    for (uint32_t ji = 0; ji < w->njoints; ++ji) { /* joints join islands too (PhysicsWorld.cpp:625-633) */
-        const joint_t* j = &w->joints[ji];
-        if (j->flags & 1u) continue;
-        if (w->motion[j->a] != KZO_DYNAMIC || w->motion[j->b] != KZO_DYNAMIC) continue;
-        uint32_t ia = w->island_index[j->a], ib = w->island_index[j->b];
-        if (ia < numDyn && ib < numDyn) uf_union(par, rank, ia, ib);
+    uint32_t* par = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * nel);
+    uint32_t* rank = (uint32_t*)calloc(nel, sizeof(uint32_t));
+    for (uint32_t i = 0; i < nel; ++i) par[i] = i;
+    w->st_shared_sleepers = 0;
+    for (uint32_t pass = 0; pass < 2; ++pass) {  /* contacts, then joints (PhysicsWorld.cpp:607-633) */
+        const uint32_t n = pass == 0 ? w->ncons : w->njoints;
+        for (uint32_t k = 0; k < n; ++k) {
+            int a, b;
+            if (pass == 0) { a = w->cons[k].a; b = w->cons[k].b; }
+            else {
+                if (w->joints[k].flags & 1u) continue;
+                a = (int)w->joints[k].a; b = (int)w->joints[k].b;
+            }
+            if (w->motion[a] != KZO_DYNAMIC || w->motion[b] != KZO_DYNAMIC) continue;
+            const uint32_t ia = w->island_index[a], ib = w->island_index[b];
+            if (ia < numDyn && ib < numDyn) { uf_union(par, rank, ia, ib); continue; }
+            const uint32_t x = ia < numDyn ? ia : (ib < numDyn ? ib : NUL);
+            const uint32_t l = ia < numDyn ? link[b] : (ib < numDyn ? link[a] : NUL);
+            if (x == NUL || l == NUL) continue;
+            const uint32_t rl = uf_find(par, l), rx = uf_find(par, x);
+            if (rl != l && rl != rx) ++w->st_shared_sleepers;  /* a second island reached the same body */
+            uf_union(par, rank, x, l);
+        }
     }
+    free(link);
     uint32_t* r2i = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * numDyn);
     for (uint32_t i = 0; i < numDyn; ++i) r2i[i] = NUL;
     uint32_t ni = 0;
@@ -1370,24 +1390,6 @@ static void build_islands(kzo_world* w) {
         if (is != NUL) w->isl_off[is + 1]++;
     }
     for (uint32_t i = 0; i < ni; ++i) w->isl_off[i + 1] += w->isl_off[i];
-    /* Sleeping bodies whose contacts landed in two different islands: the reference solves those
-     * islands concurrently (ParallelFor), so such a body's velocity depends on thread timing there. */
-    w->st_shared_sleepers = 0;
-    if (w->allow_sleeping) {
-        uint32_t* seen = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * (size_t)w->nb);
-        for (int b = 0; b < w->nb; ++b) seen[b] = NUL;
-        for (uint32_t ci = 0; ci < w->ncons; ++ci) {
-            if (isl[ci] == NUL) continue;
-            const int ab[2] = {w->cons[ci].a, w->cons[ci].b};
-            for (int q = 0; q < 2; ++q) {
-                const int b = ab[q];
-                if (w->motion[b] != KZO_DYNAMIC || w->is_active[b]) continue;
-                if (seen[b] == NUL) seen[b] = isl[ci];
-                else if (seen[b] != isl[ci] && seen[b] != NUL - 1) { ++w->st_shared_sleepers; seen[b] = NUL - 1; }
-            }
-        }
-        free(seen);
-    }
     w->isl_con = (uint32_t*)xrealloc(w->isl_con, sizeof(uint32_t) * (w->ncons ? w->ncons : 1));
     uint32_t* fill = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * (ni ? ni : 1));
     for (uint32_t i = 0; i < ni; ++i) fill[i] = w->isl_off[i];
