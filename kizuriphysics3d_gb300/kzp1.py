@@ -47,8 +47,14 @@ def _shape_bytes(sh: Shape, hull_vertices) -> bytes:
     return out
 
 
-def to_kzp1(scene: Scene, state: Optional[np.ndarray] = None) -> bytes:
-    """KZP1 bytes of a scene's bodies (at `state`, 13 floats per body, when given)."""
+def to_kzp1(scene: Scene, state: Optional[np.ndarray] = None, active: Optional[np.ndarray] = None,
+            inv_mass: Optional[np.ndarray] = None) -> bytes:
+    """KZP1 bytes of a scene's bodies (at `state`, 13 floats per body, when given), as the
+    reference's SerializeWorld writes them: BodySettings captured from the body (Body::CaptureSettings,
+    Body.h:237-262: a dynamic body's mass as its mass override, density 0) and the active flag.
+    `active` (one flag per body; default all active) and `inv_mass` (the resolved inverse masses;
+    default: the scene's own mass override and density are written) make the bytes those of the
+    reference's file for the same world."""
     from .world import build_hull
     hulls = {}
     out = bytearray(struct.pack("<III", MAGIC, VERSION, len(scene.bodies)))
@@ -67,15 +73,20 @@ def to_kzp1(scene: Scene, state: Optional[np.ndarray] = None) -> bytes:
         f = lambda xs: [float(np.float32(x)) for x in xs]
         out += struct.pack("<3f4f3f3f", *f(pos), *f(rot), *f(vel), *f(ang))
         quality = 1 if b.flags & scenes.BODY_FLAG_LINEAR_CAST else 0  # MotionQuality::LinearCast = 1
-        out += struct.pack("<BBf", b.motion, quality, 0.0)  # ccdMotionThreshold 0
+        out += struct.pack("<BBf", b.motion, quality, float(np.float32(b.ccd_motion_threshold)))
         out += struct.pack("<7f", *f([b.friction, b.restitution, b.linear_damping, b.angular_damping,
                                       b.gravity_factor, b.max_linear_velocity, b.max_angular_velocity]))
         out += struct.pack("<II", b.layer & 0xFFFFFFFF, b.mask & 0xFFFFFFFF)
         out += struct.pack("<BB", 1 if b.flags & scenes.BODY_FLAG_ALLOW_SLEEPING else 0,
                            1 if b.flags & scenes.BODY_FLAG_SENSOR else 0)
         out += struct.pack("<Q", 0)  # userData
-        out += struct.pack("<2f", *f([b.mass_override, b.density]))
-        out += struct.pack("<B", 1)  # active
+        if inv_mass is not None:  # GetMass() = 1 / inverseMass of a dynamic body (Body.h:168), else 0
+            im = np.float32(inv_mass[i])
+            mass = float(np.float32(1.0) / im) if b.motion == scenes.MOTION_DYNAMIC and im > 0 else 0.0
+            out += struct.pack("<2f", mass, 0.0)
+        else:
+            out += struct.pack("<2f", *f([b.mass_override, b.density]))
+        out += struct.pack("<B", 1 if active is None or active[i] else 0)
     return bytes(out)
 
 
@@ -94,7 +105,9 @@ class _Reader:
 
 def from_kzp1(data: bytes, template: Optional[Scene] = None) -> Scene:
     """A scene with the file's bodies; world and solver settings come from `template` (defaults:
-    the reference's WorldSettings / SolverSettings).  Identical shapes are shared."""
+    the reference's WorldSettings / SolverSettings).  Identical shapes are shared.  The bodies'
+    active flags are in the returned scene's `active` array; a World built from the scene
+    deactivates the inactive ones in slot order, as DeserializeWorld does (Serializer.cpp:214-232)."""
     r = _Reader(data)
     magic, version, count = r.take("<III")
     if magic != MAGIC or version != VERSION:
@@ -102,6 +115,7 @@ def from_kzp1(data: bytes, template: Optional[Scene] = None) -> Scene:
     sc = copy.copy(template) if template is not None else Scene(name="kzp1")
     sc.shapes, sc.bodies = [], []
     seen = {}
+    active = []
     for _ in range(count):
         (t,) = r.take("<B")
         if t == scenes.SHAPE_SPHERE:
@@ -129,19 +143,22 @@ def from_kzp1(data: bytes, template: Optional[Scene] = None) -> Scene:
         if key not in seen:
             seen[key] = sc.add_shape(sh)
         pos = r.take("<3f"); rot = r.take("<4f"); vel = r.take("<3f"); ang = r.take("<3f")
-        motion, quality, _ccd = r.take("<BBf")
+        motion, quality, ccd = r.take("<BBf")
         fr, rs, ld, ad, gf, ml, ma = r.take("<7f")
         layer, mask = r.take("<II")
         sleep, sensor = r.take("<BB")
         r.take("<Q")
         mass_override, density = r.take("<2f")
-        r.take("<B")  # active
+        (act,) = r.take("<B")
+        active.append(act != 0)
         flags = ((scenes.BODY_FLAG_ALLOW_SLEEPING if sleep else 0) | (scenes.BODY_FLAG_SENSOR if sensor else 0) |
                  (scenes.BODY_FLAG_LINEAR_CAST if quality == 1 else 0))
         sc.add_body(Body(shape=seen[key], motion=motion, pos=pos, rot=rot, vel=vel, ang=ang, friction=fr,
                          restitution=rs, linear_damping=ld, angular_damping=ad, gravity_factor=gf,
                          max_linear_velocity=ml, max_angular_velocity=ma, density=density,
-                         mass_override=mass_override, layer=layer, mask=mask, flags=flags))
+                         mass_override=mass_override, layer=layer, mask=mask, flags=flags,
+                         ccd_motion_threshold=ccd))
     if r.o != len(r.d):
         raise ValueError("trailing bytes after the last KZP1 body")
+    sc.active = np.asarray(active, bool)
     return sc

@@ -176,6 +176,9 @@ class World:
         self._check(L.kzg_add_bodies(h, n, ctypes.byref(soa), ctypes.byref(first)))
         if getattr(scene, "joints", None):
             self.add_joints(scene.joints)
+        inactive = getattr(scene, "active", None)
+        if inactive is not None and not np.all(inactive):  # a loaded KZP1 file's sleeping bodies
+            self.set_bodies_active(np.nonzero(~np.asarray(inactive, bool))[0].astype(np.uint32), False)
         self.dt = float(np.float32(scene.dt))
 
     def add_joints(self, joints) -> int:

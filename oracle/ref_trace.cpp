@@ -7,9 +7,10 @@
 //
 // Built only by oracle/Makefile.ref, from the reference's own sources, into oracle/_ref/.
 //
-// usage: ref_trace <scene.kzsc> <out.kztr> <steps> [detail_steps] [--st]
+// usage: ref_trace <scene.kzsc> <out.kztr> <steps> [detail_steps] [--st] [--kzp1 <path>]
 //   detail_steps : number of leading steps that also dump pairs and contact constraints
 //   --st         : WorldSettings::useMultithreading = false
+//   --kzp1 path  : write the world after the last step with SaveWorldToFile (a KZP1 file)
 #include "Kizuri/Kizuri.h"
 
 #include <cstdio>
@@ -59,8 +60,11 @@ int main(int argc, char** argv) {
     int steps = std::atoi(argv[3]);
     int detail = argc > 4 ? std::atoi(argv[4]) : 0;
     bool singleThread = false;
-    for (int i = 1; i < argc; ++i)
+    const char* kzp1Path = nullptr;  // --kzp1 <path>: SaveWorldToFile after the last step
+    for (int i = 1; i < argc; ++i) {
         if (std::strcmp(argv[i], "--st") == 0) singleThread = true;
+        if (std::strcmp(argv[i], "--kzp1") == 0 && i + 1 < argc) kzp1Path = argv[i + 1];
+    }
 
     Reader rd;
     {
@@ -308,6 +312,10 @@ int main(int argc, char** argv) {
     }
     w.put(totalMs);
     std::fclose(f);
+    if (kzp1Path && !SaveWorldToFile(world, kzp1Path)) {
+        std::fprintf(stderr, "SaveWorldToFile failed\n");
+        return 1;
+    }
     std::fprintf(stderr, "ref_trace: %u bodies, %d steps, %.3f ms/step, hash %016llx\n", nb, steps,
                  steps ? totalMs / steps : 0.0, (unsigned long long)world.ComputeStateHash());
     return 0;

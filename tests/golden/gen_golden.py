@@ -48,6 +48,11 @@ def fixture_scenes():
     return out
 
 
+def kzp1_fixtures():
+    """Fixture scene -> step count after which the reference saves the world as KZP1."""
+    return {"pile200": 0, "sleep_wake": 300, "ccd_threshold": 30}
+
+
 def _sleeping(sc, name):
     sc.flags |= scenes.WORLD_FLAG_ALLOW_SLEEPING
     sc.name = name
@@ -309,6 +314,15 @@ def main():
                 fx[f"d{d}_con_pts"] = det.con_pts
             np.savez_compressed(os.path.join(HERE, name + ".npz"), **fx)
             print(f"{name}: {steps} steps, final hash {int(tr.hashes[-1]):016x}")
+        for name, nsteps in kzp1_fixtures().items():  # worlds saved by the reference's SerializeWorld
+            if args.only and name not in args.only:
+                continue
+            sc = fixture_scenes()[name][0]
+            sp, tp = os.path.join(td, name + ".kzsc"), os.path.join(td, name + ".kztr")
+            sc.save(sp)
+            out = os.path.join(HERE, f"{name}_step{nsteps}.kzp1")
+            subprocess.run([exe, sp, tp, str(nsteps), "0", "--kzp1", out], check=True)
+            print(f"{out}: written by the reference after {nsteps} steps")
 
 
 if __name__ == "__main__":

@@ -96,3 +96,25 @@ def test_sleeping_off_keeps_every_body_active(kzg_lib):
         w.step_fixed(n=120)
         assert len(w.active_bodies()) == len(sc.bodies)
         assert np.array_equal(w.active_bodies(), np.arange(len(sc.bodies), dtype=np.uint32))
+
+
+def test_world_loaded_from_a_reference_kzp1_file(oracle_lib, kzg_lib):
+    """A world the reference saved mid-run with SerializeWorld (sleep_wake after 300 steps, bodies
+    asleep) loads with its sleeping bodies deactivated in slot order, as DeserializeWorld does, and
+    then steps like the oracle loaded the same way."""
+    import os
+    from conftest import GOLDEN
+    from kizuriphysics3d_gb300 import World, kzp1, resolve
+    data = open(os.path.join(GOLDEN, "sleep_wake_step300.kzp1"), "rb").read()
+    sc = kzp1.from_kzp1(data, template=FIXTURES["sleep_wake"][0])
+    assert not sc.active.all()
+    res = resolve(sc)
+    ow = oracle_lib.OracleWorld(sc.to_bytes(), oracle_blob(sc, res), oracle_lib.PAIRS_CANONICAL)
+    ow.set_bodies_active(np.nonzero(~sc.active)[0].astype(np.uint32), False)
+    with World(sc, resolved=res) as gw:
+        assert np.array_equal(gw.active_bodies(), ow.activity()[0])
+        for s in range(150):
+            ow.step(np.float32(sc.dt))
+            gw.step_fixed()
+            assert np.array_equal(bits(gw.state()), bits(ow.state())), f"state differs at step {s}"
+            assert np.array_equal(gw.active_bodies(), ow.activity()[0]), f"active list differs at step {s}"

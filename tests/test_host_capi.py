@@ -131,3 +131,35 @@ def test_kzp1_round_trip():
     assert kzp1.to_kzp1(kzp1.from_kzp1(kzp1.to_kzp1(pyr), template=pyr)) == kzp1.to_kzp1(pyr)
     with pytest.raises(ValueError):
         kzp1.from_kzp1(data[:-3])
+
+
+def _kzp1_reference_cases():
+    from tests.golden.gen_golden import kzp1_fixtures
+    return sorted(kzp1_fixtures().items())
+
+
+@pytest.mark.parametrize("name,nsteps", _kzp1_reference_cases())
+def test_kzp1_matches_files_the_reference_wrote(name, nsteps, oracle_lib):
+    """Worlds saved by the reference's own SerializeWorld (tests/golden/*.kzp1, after `nsteps` steps of
+    a reference-traced fixture): from_kzp1 reads every body with the reference's state bits and
+    active flags, and to_kzp1 of the same world writes the reference's bytes exactly."""
+    import os
+    from conftest import GOLDEN, golden_resolved, load_golden, oracle_blob
+    from kizuriphysics3d_gb300 import kzp1
+    from tests.golden.gen_golden import fixture_scenes
+    sc = fixture_scenes()[name][0]
+    g = load_golden(name)
+    data = open(os.path.join(GOLDEN, f"{name}_step{nsteps}.kzp1"), "rb").read()
+    ow = oracle_lib.OracleWorld(sc.to_bytes(), oracle_blob(sc, golden_resolved(sc, g)), oracle_lib.PAIRS_TREE)
+    for s in range(nsteps):
+        ow.step(np.float32(sc.dt))
+    if nsteps:
+        assert ow.hash() == int(g["hashes"][nsteps - 1])  # the oracle's world is the reference's
+    state = ow.state()
+    _, flags, _ = ow.activity()
+    back = kzp1.from_kzp1(data, template=sc)
+    got = np.array([[*b.pos, *b.rot, *b.vel, *b.ang] for b in back.bodies], np.float32)
+    assert np.array_equal(got.view(np.uint32), state.view(np.uint32))
+    assert np.array_equal(back.active, flags.astype(bool))
+    assert [b.ccd_motion_threshold for b in back.bodies] == [np.float32(b.ccd_motion_threshold) for b in sc.bodies]
+    assert kzp1.to_kzp1(sc, state=state, active=flags.astype(bool), inv_mass=g["inv_mass"]) == data
