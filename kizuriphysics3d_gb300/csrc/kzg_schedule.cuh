@@ -32,7 +32,6 @@ constexpr uint32_t kCtaBodiesMax = 6400;   // island velocities staged per CTA (
 constexpr uint32_t kSchedSmallCons = 128;  // islands with at most this many constraints: warp schedule
 constexpr uint32_t kSchedWarpBodies = 2 * kSchedSmallCons;
 constexpr uint32_t kSchedCtaBodies = 16384;  // per-sweep level table in shared memory (3 x 64 KB)
-constexpr uint32_t kSchedSmem = 224u * 1024u;  // dynamic shared memory of k_schedule_cta
 
 struct SchedBufs {
     const uint32_t *isl_start, *isl_con, *con_a, *con_b, *con_np, *con_bits;
@@ -62,7 +61,6 @@ struct SchedShared {  // per island scratch living in shared memory
     uint32_t ff_final;   // streamed first fit: batches below this are full and their records written
     uint32_t ff_done;    // 0 running, 1 done (nbt set), 2 gave up
     uint32_t stream_ok;  // the velocity level sweep ran behind the first fit
-    uint32_t ff_static;  // batched constraints hold a static or kinematic body that is not a hub
 };
 
 __device__ __forceinline__ uint32_t* rec(const SchedBufs& S, uint32_t r) { return reinterpret_cast<uint32_t*>(S.brec + 4ull * r); }
@@ -208,7 +206,7 @@ __device__ __forceinline__ FfTable ff_table_of(void* smem_v) {
     T.list1 = reinterpret_cast<uint16_t*>(smem + 18u * kFfSlots);
     T.remap = reinterpret_cast<uint16_t*>(smem + 20u * kFfSlots);
     T.cnt = smem + 22u * kFfSlots;
-    T.keys = reinterpret_cast<uint32_t*>(smem + kSchedSmem - kFfCodes * 4u);  // the region's end (see first_fit_bits)
+    T.keys = reinterpret_cast<uint32_t*>(smem + 23u * kFfSlots);
     return T;
 }
 
@@ -585,236 +583,6 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
     return nbt;
 }
 
-// ---------------------------------------------------------------------------------------------
-// Bit-window first fit (CTA islands whose non-dynamic bodies are all hubs; tried before
-// first_fit_warp, which takes over when this returns kNone).
-//
-// The window is the 64 batches from `base`, the first batch that is not full.  Every lane holds
-// the same copy of its state in registers - two bit planes of the point counts, the full mask and a
-// mask per hub - and runs the same serial placement, lane 0 doing the stores.  Each island-local
-// dynamic body has a 64-bit mask of the window batches holding it in shared memory, written
-// relative to the base of its last write (a 16-bit tag) and shifted on read.  A constraint's points
-// take, in order, the lowest bits of ~(full | its bodies | its hub): the reference's first fit
-// (PhysicsWorld.cpp:680-717) restricted to the window, since points of one constraint share their
-// bodies and every batch before the window is full.  Bits past the last batch are the batches it
-// would open next, in order.  Points the window cannot take ("far" points) go to the first later
-// batch that can take them, found by a warp-wide scan of the batch records, or open batches past
-// the last one; far batches keep their point count, hub flags and body codes in their records and
-// are folded into the window (the warp prefetches 32 records at a time) when the base passes
-// them.  Per hub, every batch from base + 64 up to hf[h] holds that hub or is full, so hub points
-// skip those: in an island whose hub is its lowest body (a ground plane created first), the hub
-// constraints come first and each of their points opens a new batch.
-//
-// Batch record words used: [0] hub flags (far batches), [3] points, [4 + 2k], [5 + 2k] body codes of
-// point k (far batches), [12 + k] rows.
-constexpr uint32_t kBitsMaxLocal = (kSchedSmem - kFfCodes * 4u) / 10u;  // 8-byte mask + 2-byte tag per body
-constexpr uint32_t kBitsMaxBatches = 65536u - 256u;                     // 16-bit tags
-
-__device__ __forceinline__ unsigned long long shr64(unsigned long long x, uint32_t s) { return s >= 64u ? 0ull : x >> s; }
-
-__device__ uint32_t first_fit_bits(const SchedBufs& S, uint32_t s0, uint32_t s1, uint32_t rb, uint32_t hub0,
-                                   uint32_t hub1, uint32_t nloc, uint8_t* smem, uint32_t lane,
-                                   volatile uint32_t* pub = nullptr) {
-    const unsigned full = 0xffffffffu;
-    if (nloc > kBitsMaxLocal) return kNone;
-    unsigned long long* bm = reinterpret_cast<unsigned long long*>(smem);
-    uint16_t* bt = reinterpret_cast<uint16_t*>(smem + 8u * nloc);
-    for (uint32_t k = lane; k < nloc; k += 32) { bm[k] = 0ull; bt[k] = 0; }
-    __syncwarp();
-    uint32_t base = 0, nbt = 0, hf0 = 64, hf1 = 64, published = 0;
-    unsigned long long c0 = 0, c1 = 0, fm = 0, hm0 = 0, hm1 = 0;
-    // far-record prefetch: lane L holds batch pf + L (count, hub flags, 8 codes)
-    uint32_t pf = kNone, pcnt = 0, phub = 0, pcode[4] = {0, 0, 0, 0};
-    auto mask_of = [&](uint32_t x) -> unsigned long long {
-        if (x >= nloc) return 0ull;
-        return shr64(bm[x], (base - (uint32_t)bt[x]) & 0xFFFFu);
-    };
-    auto mask_or = [&](uint32_t x, unsigned long long bits) {  // lane 0 stores; callers __syncwarp after
-        if (x >= nloc) return;
-        const unsigned long long m = shr64(bm[x], (base - (uint32_t)bt[x]) & 0xFFFFu) | bits;
-        if (lane == 0) { bm[x] = m; bt[x] = (uint16_t)(base & 0xFFFFu); }
-    };
-    // fold far batch j (entering the window at bit j - base) into the window state
-    auto enter = [&](uint32_t j) {
-        if (pf == kNone || j < pf || j >= pf + 32u) {
-            pf = j;
-            const uint32_t jj = j + lane;
-            pcnt = 0; phub = 0;
-            if (jj < nbt) {
-                const uint32_t* r = rec(S, rb + jj);
-                pcnt = r[3]; phub = r[0];
-                const uint4 cd = *reinterpret_cast<const uint4*>(r + 4), ce = *reinterpret_cast<const uint4*>(r + 8);
-                pcode[0] = cd.x | (cd.y << 16); pcode[1] = cd.z | (cd.w << 16);
-                pcode[2] = ce.x | (ce.y << 16); pcode[3] = ce.z | (ce.w << 16);
-            }
-        }
-        const uint32_t src = j - pf;
-        const uint32_t cn = __shfl_sync(full, pcnt, src), hb = __shfl_sync(full, phub, src);
-        uint32_t cd[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) cd[q] = __shfl_sync(full, pcode[q], src);
-        const unsigned long long bit = 1ull << (j - base);
-        if (cn >= 4u) fm |= bit;
-        else {
-            if (cn & 1u) c0 |= bit;
-            if (cn & 2u) c1 |= bit;
-        }
-        if (hb & 1u) hm0 |= bit;
-        if (hb & 2u) hm1 |= bit;
-        for (uint32_t k = 0; k < cn && k < 4u; ++k) {
-            mask_or(cd[k] & 0xFFFFu, bit);
-            mask_or(cd[k] >> 16, bit);
-        }
-        __syncwarp();
-    };
-    auto slide = [&]() {
-        while (fm & 1ull) {
-            const uint32_t sft = fm == ~0ull ? 64u : (uint32_t)__ffsll((long long)~fm) - 1u;
-            const uint32_t old = base;
-            base += sft;
-            c0 = shr64(c0, sft); c1 = shr64(c1, sft); fm = shr64(fm, sft);
-            hm0 = shr64(hm0, sft); hm1 = shr64(hm1, sft);
-            const uint32_t e = min(base + 64u, nbt);
-            for (uint32_t j = old + 64u; j < e; ++j) enter(j);
-            hf0 = max(hf0, base + 64u);
-            hf1 = max(hf1, base + 64u);
-        }
-        if (pub && base != published) {  // every batch below base is full, its records written
-            __syncwarp();
-            __threadfence_block();
-            if (lane == 0) *pub = base;
-            published = base;
-        }
-    };
-    auto load_id = [&](uint32_t w0) -> uint32_t { return w0 + lane < s1 ? S.isl_con[w0 + lane] : kNone; };
-    uint32_t nx_c = load_id(s0), nx_bits = 1u, nx_a = 0, nx_b = 0, nx_np = 0, nx_la = kNone, nx_lb = kNone;
-    if (nx_c != kNone) {
-        nx_bits = S.con_bits[nx_c]; nx_a = S.con_a[nx_c]; nx_b = S.con_b[nx_c]; nx_np = S.con_np[nx_c];
-        nx_la = S.con_la[nx_c]; nx_lb = S.con_lb[nx_c];
-    }
-    uint32_t id2 = load_id(s0 + 32);
-    for (uint32_t w0 = s0; w0 < s1; w0 += 32) {
-        const uint32_t mc = nx_c, mbits = nx_bits, ma = nx_a, mb = nx_b, mnp = nx_np, mla = nx_la, mlb = nx_lb;
-        nx_c = id2;
-        nx_bits = 1u; nx_np = 0; nx_la = kNone; nx_lb = kNone;
-        if (nx_c != kNone) {
-            nx_bits = S.con_bits[nx_c]; nx_a = S.con_a[nx_c]; nx_b = S.con_b[nx_c]; nx_np = S.con_np[nx_c];
-            nx_la = S.con_la[nx_c]; nx_lb = S.con_lb[nx_c];
-        }
-        id2 = load_id(w0 + 64);
-        // this lane's constraint: body codes (local indices; kFfDead for a hub), hub, point count
-        uint32_t dx = 0, meta = 64u;  // meta: np | hub + 1 << 4 | skip << 6 | unsupported << 7
-        if (mc != kNone) {
-            const int ha = ma == hub0 ? 0 : (ma == hub1 ? 1 : -1);
-            const int hb = mb == hub0 ? 0 : (mb == hub1 ? 1 : -1);
-            const bool sensor = (mbits & 1u) != 0u;
-            const uint32_t ca = ha >= 0 ? kFfDead : mla, cb = hb >= 0 ? kFfDead : mlb;
-            const bool odd = !sensor && ((ha < 0 && ca == kNone) || (hb < 0 && cb == kNone));  // non-hub, non-dynamic
-            const int hub = ha >= 0 ? ha : hb;
-            const uint32_t x0 = hub < 0 ? ca : (ha >= 0 ? cb : ca);
-            const uint32_t x1 = hub < 0 ? cb : kFfDead;
-            dx = (x0 & 0xFFFFu) | (x1 << 16);
-            meta = mnp | ((uint32_t)(hub + 1) << 4) | (sensor ? 64u : 0u) | (odd ? 128u : 0u);
-        }
-        if (__any_sync(full, (meta & 128u) != 0u)) return kNone;
-        const uint32_t m = min(32u, s1 - w0);
-        for (uint32_t k = 0; k < m; ++k) {
-            const uint32_t md = __shfl_sync(full, meta, k);
-            if (md & 64u) continue;  // sensors are never batched (:690)
-            const uint32_t c = __shfl_sync(full, mc, k), xx = __shfl_sync(full, dx, k);
-            const uint32_t np = md & 15u, x0 = xx & 0xFFFFu, x1 = xx >> 16;
-            const int hub = (int)((md >> 4) & 3u) - 1;
-            const unsigned long long hmask = hub == 0 ? hm0 : (hub == 1 ? hm1 : 0ull);
-            unsigned long long avail = ~(fm | mask_of(x0) | mask_of(x1) | hmask), sel = 0ull;
-            uint32_t take = 0;
-            while (take < np && avail) {
-                sel |= avail & (~avail + 1ull);
-                avail &= avail - 1ull;
-                ++take;
-            }
-            if (lane == 0) {  // the rows of the window points
-                uint32_t p = 0;
-                for (unsigned long long t = sel; t; t &= t - 1ull, ++p) {
-                    const uint32_t i = (uint32_t)__ffsll((long long)t) - 1u;
-                    const uint32_t kk = (uint32_t)((c0 >> i) & 1ull) | ((uint32_t)((c1 >> i) & 1ull) << 1);
-                    uint32_t* r = rec(S, rb + base + i);
-                    r[12 + kk] = 4u * c + p;
-                    r[3] = kk + 1u;
-                }
-            }
-            if (sel) {
-                const uint32_t top = base + 64u - (uint32_t)__clzll((long long)sel);  // one past the highest
-                if (top > nbt) nbt = top;
-                const unsigned long long carry = c0 & sel;
-                c0 ^= sel;
-                fm |= c1 & carry;
-                c1 ^= carry;
-                mask_or(x0, sel);
-                if (x1 != x0) mask_or(x1, sel);
-                if (hub == 0) hm0 |= sel;
-                if (hub == 1) hm1 |= sel;
-                __syncwarp();
-            }
-            if (take < np) {  // far points: later batches in order, then new ones
-                uint32_t p = take, rem = np - take;
-                const uint32_t hbit = hub < 0 ? 0u : (1u << hub);
-                const uint32_t c01 = (x0 & 0xFFFFu) | (x1 << 16);
-                uint32_t j0 = max(base + 64u, hub == 0 ? hf0 : (hub == 1 ? hf1 : 0u));
-                pf = kNone;  // records may change below
-                while (rem && j0 < nbt) {
-                    const uint32_t j = j0 + lane;
-                    bool ok = false;
-                    uint32_t cn = 0, hb = 0;
-                    if (j < nbt) {
-                        const uint32_t* r = rec(S, rb + j);
-                        cn = r[3];
-                        hb = r[0];
-                        ok = cn < 4u && !(hb & hbit);
-                        for (uint32_t q = 0; ok && q < cn; ++q) {
-                            const uint32_t ya = r[4 + 2 * q], yb = r[5 + 2 * q];
-                            ok = ya != x0 && yb != x0 && (x1 == kFfDead || (ya != x1 && yb != x1));
-                        }
-                    }
-                    const unsigned okm = __ballot_sync(full, ok);
-                    const uint32_t t = min((uint32_t)__popc(okm), rem);
-                    const uint32_t rank = __popc(okm & ((1u << lane) - 1u));
-                    if (ok && rank < t) {
-                        uint32_t* r = rec(S, rb + j);
-                        r[4 + 2 * cn] = c01 & 0xFFFFu;
-                        r[5 + 2 * cn] = c01 >> 16;
-                        r[12 + cn] = 4u * c + p + rank;
-                        r[3] = cn + 1u;
-                        r[0] = hb | hbit;
-                    }
-                    p += t;
-                    rem -= t;
-                    j0 += 32u;
-                }
-                if (rem) {  // open batches nbt, nbt + 1, ...
-                    if (nbt + rem > kBitsMaxBatches) return kNone;
-                    if (lane < rem) {
-                        uint32_t* r = rec(S, rb + nbt + lane);
-                        r[0] = hbit;
-                        r[3] = 1u;
-                        r[4] = c01 & 0xFFFFu;
-                        r[5] = c01 >> 16;
-                        r[12] = 4u * c + p + lane;
-                    }
-                    const uint32_t old = nbt;
-                    nbt += rem;
-                    if (hub == 0 && hf0 == old) hf0 = nbt;  // the new batches hold the hub
-                    if (hub == 1 && hf1 == old) hf1 = nbt;
-                }
-                __syncwarp();
-                __threadfence_block();
-            }
-            if (nbt > kBitsMaxBatches) return kNone;
-            slide();
-        }
-    }
-    return nbt;
-}
-
 // One level sweep of an island on one warp, with the level table `last` (nloc words, any memory):
 // 0 velocity (batch order, one level per point; local bodies staged per item in vl_list / bl_list),
 // 1 warm start (all points) and 2 bias (points with positionBias > 0) in constraint order, the
@@ -953,7 +721,7 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
     const uint32_t lane = tid & 31u, warp = tid >> 5;
 
     // ---- A: local indices of the island's dynamic bodies, hub candidates (large bodies)
-    if (tid == 0) { sh->nloc = 0; sh->hub0 = kNone; sh->hub1 = kNone; sh->ff_ok = ff_table ? 1u : 0u; sh->ff_static = 0u; }
+    if (tid == 0) { sh->nloc = 0; sh->hub0 = kNone; sh->hub1 = kNone; sh->ff_ok = ff_table ? 1u : 0u; }
     const FfTable T = ff_table_of(last_sm);
     if (ff_table)
         for (uint32_t k = tid; k < kFfCodes; k += nthreads) T.keys[k] = kNone;
@@ -1030,10 +798,7 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
             if (bits & 1u) continue;
             const uint32_t xs[2] = {S.con_a[c], S.con_b[c]};
             for (int q = 0; q < 2; ++q)
-                if (!(bits & (2u << q)) && xs[q] != hub0 && xs[q] != hub1) {
-                    ok = ok && ff_insert(T, xs[q]);
-                    sh->ff_static = 1u;
-                }
+                if (!(bits & (2u << q)) && xs[q] != hub0 && xs[q] != hub1) ok = ok && ff_insert(T, xs[q]);
         }
         if (!ok) sh->ff_ok = 0u;
         sync();
@@ -1054,13 +819,8 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
     }
     sync();
     if (table_ff && warp == 0) {
-        uint32_t r = kNone;
-        if (!sh->ff_static)
-            r = first_fit_bits(S, s0, s1, rb, sh->hub0, sh->hub1, sh->nloc, reinterpret_cast<uint8_t*>(last_sm), lane,
-                               stream ? &sh->ff_final : nullptr);
-        if (r == kNone)
-            r = first_fit_warp(S, s0, s1, rb, sh->hub0, sh->hub1, sh->nloc, reinterpret_cast<uint8_t*>(last_sm),
-                               lane, stream ? &sh->ff_final : nullptr);
+        const uint32_t r = first_fit_warp(S, s0, s1, rb, sh->hub0, sh->hub1, sh->nloc, reinterpret_cast<uint8_t*>(last_sm),
+                                          lane, stream ? &sh->ff_final : nullptr);
         __syncwarp();
         __threadfence_block();
         if (lane == 0) {
@@ -1277,8 +1037,7 @@ __global__ void __launch_bounds__(128, 8) k_schedule_warp(SchedBufs S, Counters*
 }
 
 // Larger islands: one CTA each.
-static_assert(kFfBytes <= kSchedSmem && 3 * kSchedCtaBodies * sizeof(uint32_t) <= kSchedSmem - kFfCodes * 4u,
-              "first-fit table and level tables must fit the schedule's shared memory");
+static_assert(kFfBytes <= 3 * kSchedCtaBodies * sizeof(uint32_t), "first-fit table must fit the level tables' shared memory");
 __global__ void __launch_bounds__(256, 1) k_schedule_cta(SchedBufs S, Counters* cnt) {
     extern __shared__ uint32_t last_sm[];
     __shared__ SchedShared sh;

@@ -1275,7 +1275,8 @@ cudaError_t configure_kernels() {
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_narrow_epa, cudaFuncAttributePreferredSharedMemoryCarveout, 100);  // 4 CTAs per SM
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_schedule_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSchedSmem);
+    e = cudaFuncSetAttribute(k_schedule_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(3 * kSchedCtaBodies * sizeof(uint32_t)));
     if (e != cudaSuccess) return e;
     // the cluster solve needs kClusterCtas co-resident CTAs with 192 KB of shared memory each
     e = cudaFuncSetAttribute(k_solve_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1417,7 +1418,7 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
                  std::min(ctx.tune.warp_island_bodies, kWarpBodies), nj ? ctx.jflag : nullptr, ctx.wait_limit,
                  lpt ? ctx.isl_order : nullptr};
     k_schedule_warp<<<152u * 16u, 128, 0, st>>>(SB, ctx.dcnt);
-    k_schedule_cta<<<152u * 2u, 256, kSchedSmem, st>>>(SB, ctx.dcnt);
+    k_schedule_cta<<<152u * 2u, 256, 3 * kSchedCtaBodies * sizeof(uint32_t), st>>>(SB, ctx.dcnt);
     ctx.launches += 16;  // prepare, union-find (2), island sort (4 CUB passes), heads, scan (2), starts, schedule (2)
     KZG_CK(mark(ctx, 4));
     SolveBufs SV{ctx.isl_start, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.con_la, ctx.con_lb, ctx.isl_meta,
