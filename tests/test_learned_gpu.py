@@ -124,23 +124,28 @@ def test_learned_warm_start_keeps_determinism():
     assert hashes[0] == hashes[1]
 
 
-def test_trained_network_needs_fewer_iterations():
-    """The committed model on the settled 20,000-body pile (the bench workload): velocity iterations
-    until the relative impulse change is <= 3e-3, summed over islands weighted by points, over 8
-    steps.  Measured: plain 29,848,546, learned 29,549,979 (-1.0%).  Small, because only the ~8% of
-    points that miss the cache are warm-started by the network and the giant island's slow modes
-    set the iteration count; on a pile that is still falling the same model needs more iterations
-    than the plain warm start (+14% at 1e-4 on a 4,000-body pile), see the design notes."""
+def test_learned_warm_start_on_held_out_pile_at_the_metric_tolerance():
+    """The committed model on data it was not trained on: the 20,000-body pile of a fresh seed (98765)
+    after 600 steps (committed snapshot), relative impulse change <= 1e-4 with the cap raised to
+    1,024 so that the tolerance is actually reached.  Both warm starts converge to it (the solver's
+    own residual judges the prediction).  Measured on GB300 (6 steps after 2): plain 357,304,682
+    point-iterations (~598 iterations on the giant island), learned 363,093,274 (+1.6%): at this
+    tolerance the learned warm start costs iterations; at 1e-3 it saves 1.0% and at 3e-3 0.35%.
+    The test holds the convergence and bounds the cost."""
     from kizuriphysics3d_gb300 import scenes
     from kizuriphysics3d_gb300.learned import MODEL_PATH, WarmStartModel, evaluate
     model = WarmStartModel.load(MODEL_PATH)
-    snap = os.path.join(os.path.dirname(__file__), "..", "kizuriphysics3d_gb300", "data", "pile20000_step600.npz")
-    sc = scenes.pile(20000, seed=1234)
+    snap = os.path.join(os.path.dirname(__file__), "..", "kizuriphysics3d_gb300", "data",
+                        "pile20000_s98765_step600.npz")
+    sc = scenes.pile(20000, seed=98765)
     with np.load(snap) as z:
         state = z["state"]
     for b, st in zip(sc.bodies, state):
         b.pos, b.rot, b.vel, b.ang = tuple(st[0:3]), tuple(st[3:7]), tuple(st[7:10]), tuple(st[10:13])
-    kw = dict(steps=8, skip=3, tol=3e-3, max_pairs=48 * 20001)
+    kw = dict(steps=4, skip=2, tol=1e-4, cap=1024, max_pairs=48 * 20001)
     plain = evaluate(sc, None, **kw)
     learned = evaluate(sc, model, **kw)
-    assert learned["point_iterations"] < plain["point_iterations"], (plain, learned)
+    for r in (plain, learned):
+        assert r["mean_max_iterations"] < 1024  # reached the tolerance before the cap
+        assert r["mean_final_residual"] <= 1.01e-4
+    assert learned["point_iterations"] <= 1.05 * plain["point_iterations"], (plain, learned)
