@@ -61,7 +61,10 @@ typedef struct {
     uint32_t max_hull_vertices;
     uint32_t max_hull_indices;
     uint32_t max_pairs;         /* broad-phase pairs per step */
-    uint32_t max_cache_entries; /* manifold cache slots (power of two; entries are never evicted) */
+    uint32_t max_cache_entries; /* initial manifold cache slots (power of two).  Entries are never
+                                 * evicted; like PhysicsWorld::GetOrCreateCached's table, this one
+                                 * doubles (entries rehashed, results unchanged) between steps once the
+                                 * coming steps could take it past 0.7 load */
     int device;                 /* CUDA ordinal */
     uint32_t max_joints;        /* joints (0: none) */
 } kzg_config;
@@ -177,6 +180,7 @@ typedef struct {
     float final_residual; /* largest residual (relative impulse change, see kzg_solver_settings) of any
                            * island's last velocity iteration */
     uint32_t num_active_bodies; /* WorldStats::numActiveBodies: the active list's length */
+    uint32_t cache_capacity;    /* manifold cache slots now (kzg_config.max_cache_entries, doubled as it fills) */
 } kzg_stats;
 
 #define KZG_DEVERR_PAIRS 1u     /* pair buffer overflow */

@@ -136,6 +136,8 @@ kzg_status alloc_all(Ctx* ctx) {
     CK(dalloc(&ctx->c_np, H));
     CK(dalloc(&ctx->c_pos, 4 * H));
     CK(dalloc(&ctx->c_imp, 4 * H));
+    CK(cudaMemset(ctx->c_np, 0, sizeof(uint32_t) * H));
+    ctx->cache_cap = (uint32_t)H;
     CK(dalloc(&ctx->dcnt, 1));
     CK(cudaMemset(ctx->dcnt, 0, sizeof(Counters)));
     CK(cudaMallocHost((void**)&ctx->hcnt, sizeof(Counters)));
@@ -601,7 +603,7 @@ struct DeviceBackup {
     uint8_t* mem = nullptr;
 
     cudaError_t save(Ctx& c) {
-        const size_t nb = c.nbodies, H = c.cfg.max_cache_entries;
+        const size_t nb = c.nbodies, H = c.cache_cap;
         DeviceBodies& b = c.b;
         for (float4* p : {b.pos, b.rot, b.lv, b.av, b.plv, b.pav, b.force, b.torque, b.fat_mn, b.fat_mx})
             regions.push_back({p, sizeof(float4) * nb});
@@ -645,10 +647,25 @@ kzg_status kzg_autotune(kzg_ctx* k, float dt, uint32_t steps_per_candidate, kzg_
     kzg_status s = finalize_bodies(k);
     if (s != KZG_OK) return s;
     const kzg_tuning before = ctx->tune;
+    // Every candidate starts from the saved state, so the cache never holds more than the entries
+    // of 1 + steps_per_candidate steps beyond today's: reserve that, and keep the table (whose copy
+    // the backup holds) in place while tuning.
+    uint32_t entries = 0, pairs = 0;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&entries, &ctx->dcnt->cache_entries, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&pairs, &ctx->dcnt->npairs, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    s = cache_reserve(*ctx, (uint64_t)entries + (uint64_t)(steps_per_candidate + 1u) *
+                                                    std::max<uint64_t>(std::max(pairs, ctx->nbodies), 1u));
+    if (s != KZG_OK) return s;
     const bool logging = ctx->mlp.logging;
     ctx->mlp.logging = false;  // the tuning steps are not part of the world's history
     DeviceBackup backup;
     CK(backup.save(*ctx));
+    struct FixCache {
+        Ctx* c;
+        ~FixCache() { c->cache_fixed = false; }
+    } fix{ctx};
+    ctx->cache_fixed = true;
     const uint32_t small[3] = {32u, 64u, 128u}, warp[3] = {128u, 256u, 384u};
     const uint32_t orders[2] = {KZG_ISLANDS_IN_ORDER, KZG_ISLANDS_LARGEST_FIRST};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -832,6 +849,7 @@ kzg_status kzg_state_hash(kzg_ctx* k, uint64_t* out) {
 kzg_status kzg_get_stats(kzg_ctx* k, kzg_stats* out) {
     if (check(k) || !out) return KZG_ERR_INVALID;
     *out = k->c.stats;
+    out->cache_capacity = k->c.cache_cap;  // the table as it is now (it may have grown since)
     return KZG_OK;
 }
 
@@ -926,7 +944,7 @@ kzg_status kzg_snapshot_size(kzg_ctx* k, size_t* bytes) {
     Ctx* ctx = &k->c;
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
-    const size_t H = ctx->cfg.max_cache_entries;
+    const size_t H = ctx->cache_cap;
     std::vector<unsigned long long> keys(H);
     CK(cudaMemcpy(keys.data(), ctx->c_key, sizeof(unsigned long long) * H, cudaMemcpyDeviceToHost));
     size_t used = 0;
@@ -941,7 +959,7 @@ kzg_status kzg_snapshot_save(kzg_ctx* k, void* out, size_t capacity) {
     Ctx* ctx = &k->c;
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
-    const size_t H = ctx->cfg.max_cache_entries, nb = ctx->nbodies;
+    const size_t H = ctx->cache_cap, nb = ctx->nbodies;
     std::vector<unsigned long long> keys(H);
     std::vector<uint32_t> np(H);
     std::vector<float4> pos(4 * H), imp(4 * H);
@@ -998,13 +1016,25 @@ kzg_status kzg_snapshot_load(kzg_ctx* k, const void* in, size_t size) {
     if (st != KZG_OK) return st;
     SnapHeader h;
     std::memcpy(&h, in, sizeof(h));
-    const size_t H = ctx->cfg.max_cache_entries, nb = ctx->nbodies;
+    const size_t nb = ctx->nbodies, H = h.cache_cap;  // the table takes the snapshot's capacity
     const size_t JB = joint_record_bytes() * ctx->njoints;
-    if (h.magic != kSnapMagic || h.version != kSnapVersion || h.nbodies != nb || h.cache_cap != H ||
+    if (h.magic != kSnapMagic || h.version != kSnapVersion || h.nbodies != nb || h.cache_cap == 0 ||
+        (h.cache_cap & (h.cache_cap - 1u)) != 0 || h.cache_used > h.cache_cap || h.cache_entries > h.cache_cap ||
         h.njoints != ctx->njoints ||
         size != sizeof(SnapHeader) + kSnapBodyBytes * nb + kSnapCacheBytes * (size_t)h.cache_used + JB) {
-        ctx->err = "kzg_snapshot_load: snapshot does not match this context (bodies, joints, cache capacity or size)";
+        ctx->err = "kzg_snapshot_load: snapshot does not match this context (bodies, joints, cache table or size)";
         return KZG_ERR_INVALID;
+    }
+    {  // every cache slot inside the table, checked before anything is written
+        const uint8_t* q = static_cast<const uint8_t*>(in) + sizeof(h) + kSnapBodyBytes * nb;
+        for (uint32_t e = 0; e < h.cache_used; ++e, q += kSnapCacheBytes) {
+            uint32_t slot;
+            std::memcpy(&slot, q, 4);
+            if (slot >= H) {
+                ctx->err = "kzg_snapshot_load: cache slot out of range";
+                return KZG_ERR_INVALID;
+            }
+        }
     }
     CK(cudaStreamSynchronize(ctx->stream));
     const uint8_t* p = static_cast<const uint8_t*>(in) + sizeof(h);
@@ -1022,25 +1052,21 @@ kzg_status kzg_snapshot_load(kzg_ctx* k, const void* in, size_t size) {
     }
     if (h.reserved > nb) { ctx->err = "kzg_snapshot_load: active-list length out of range"; return KZG_ERR_INVALID; }
     CK(cudaMemcpy(&ctx->dcnt->nact, &h.reserved, sizeof(uint32_t), cudaMemcpyHostToDevice));
-    std::vector<unsigned long long> keys(H, 0ull);
-    std::vector<uint32_t> np(H, 0u);
-    std::vector<float4> pos(4 * H, make_float4(0.0f, 0.0f, 0.0f, 0.0f)), imp(4 * H, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
-    for (uint32_t e = 0; e < h.cache_used; ++e) {
-        uint32_t slot;
-        std::memcpy(&slot, p, 4); p += 4;
-        if (slot >= H) {
-            ctx->err = "kzg_snapshot_load: cache slot out of range";
-            return KZG_ERR_INVALID;
-        }
-        std::memcpy(&keys[slot], p, 8); p += 8;
-        std::memcpy(&np[slot], p, 4); p += 4;
-        std::memcpy(&pos[4 * slot], p, 4 * sizeof(float4)); p += 4 * sizeof(float4);
-        std::memcpy(&imp[4 * slot], p, 4 * sizeof(float4)); p += 4 * sizeof(float4);
+    const size_t used = h.cache_used;
+    std::vector<uint32_t> slots(used), np(used);
+    std::vector<unsigned long long> keys(used);
+    std::vector<float4> pos(4 * used), imp(4 * used);
+    for (size_t e = 0; e < used; ++e) {
+        std::memcpy(&slots[e], p, 4); p += 4;
+        std::memcpy(&keys[e], p, 8); p += 8;
+        std::memcpy(&np[e], p, 4); p += 4;
+        std::memcpy(&pos[4 * e], p, 4 * sizeof(float4)); p += 4 * sizeof(float4);
+        std::memcpy(&imp[4 * e], p, 4 * sizeof(float4)); p += 4 * sizeof(float4);
     }
-    CK(cudaMemcpy(ctx->c_key, keys.data(), sizeof(unsigned long long) * H, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(ctx->c_np, np.data(), sizeof(uint32_t) * H, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(ctx->c_pos, pos.data(), sizeof(float4) * 4 * H, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(ctx->c_imp, imp.data(), sizeof(float4) * 4 * H, cudaMemcpyHostToDevice));
+    st = cache_reset(*ctx, (uint32_t)H);
+    if (st != KZG_OK) return st;
+    st = cache_scatter(*ctx, slots.data(), keys.data(), np.data(), pos.data(), imp.data(), (uint32_t)used);
+    if (st != KZG_OK) return st;
     CK(cudaMemcpy(&ctx->dcnt->cache_entries, &h.cache_entries, sizeof(uint32_t), cudaMemcpyHostToDevice));
     if (JB) CK(cudaMemcpy(ctx->joints, p, JB, cudaMemcpyHostToDevice));
     return KZG_OK;

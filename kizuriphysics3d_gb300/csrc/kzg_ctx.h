@@ -202,11 +202,15 @@ struct Ctx {
     float4* miss_prior = nullptr;  // per miss: nearest cached point's impulses, pair's cached normal impulse per point
     MlpState mlp;
 
-    // cache
+    // manifold cache: open addressing over cache_cap slots (a power of two), doubled between steps
+    // when the coming steps could take it past 0.7 load (PhysicsWorld::GetOrCreateCached grows at
+    // the same load); never evicted
     unsigned long long* c_key = nullptr;
     uint32_t* c_np = nullptr;
     float4* c_pos = nullptr;
     float4* c_imp = nullptr;
+    uint32_t cache_cap = 0;
+    bool cache_fixed = false;  // the tuner holds a copy of the table: no growth while it runs
 
     // misc
     Counters* dcnt = nullptr;

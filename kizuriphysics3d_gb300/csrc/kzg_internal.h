@@ -5,6 +5,7 @@
 #include <cstdint>
 
 #include <cuda_runtime.h>
+#include <vector_types.h>
 
 #include "../../include/kzg.h"
 
@@ -22,6 +23,13 @@ cudaError_t init_new_bodies(Ctx& ctx, uint32_t first, uint32_t n);  // fat bound
 cudaError_t set_bodies_active(Ctx& ctx, const uint32_t* dev_ids, uint32_t n, int active);  // in order
 cudaError_t create_joints(Ctx& ctx, uint32_t first, uint32_t n);     // joint records from ctx.joint_stage
 size_t joint_record_bytes();
+// Manifold cache table: room for `entries` at below 0.7 load (doubling, entries rehashed), and a
+// table of exactly `cap` slots with every entry cleared (snapshot loads).
+kzg_status cache_reserve(Ctx& ctx, uint64_t entries);
+kzg_status cache_reset(Ctx& ctx, uint32_t cap);
+// Entries (slot, key, point count, 4 positions, 4 impulses) written into their slots.
+kzg_status cache_scatter(Ctx& ctx, const uint32_t* slots, const unsigned long long* keys, const uint32_t* np,
+                         const float4* pos, const float4* imp, uint32_t n);
 kzg_status step_canonical(Ctx& ctx, float dt, uint32_t nsteps);
 kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t num_pairs, float dt);
 kzg_status hash_state(Ctx& ctx, uint64_t* out);

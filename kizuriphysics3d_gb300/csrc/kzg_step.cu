@@ -930,6 +930,42 @@ __global__ void k_cache_store(Counters* cnt, const unsigned long long* __restric
     }
 }
 
+// Moves every entry of a cache table into one twice (or more) its size: keys are unique, so an
+// entry only needs a free slot in its new probe sequence.
+__global__ void k_cache_rehash(const unsigned long long* __restrict__ ok, const uint32_t* __restrict__ onp,
+                               const float4* __restrict__ opos, const float4* __restrict__ oimp, uint32_t ocap,
+                               unsigned long long* nk, uint32_t* nnp, float4* npos, float4* nimp, uint32_t ncap,
+                               Counters* cnt) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= ocap) return;
+    const unsigned long long key = ok[s];
+    if (key == 0ull) return;
+    const uint32_t mask = ncap - 1u;
+    uint32_t slot = hash_key(key) & mask;
+    for (uint32_t probes = 0; atomicCAS(&nk[slot], 0ull, key) != 0ull; slot = (slot + 1u) & mask)
+        if (++probes >= ncap) { atomicOr(&cnt->error, KZG_DEVERR_CACHE); return; }
+    nnp[slot] = onp[s];
+    for (uint32_t p = 0; p < 4; ++p) {
+        npos[4u * slot + p] = opos[4u * s + p];
+        nimp[4u * slot + p] = oimp[4u * s + p];
+    }
+}
+
+__global__ void k_cache_scatter(const uint32_t* __restrict__ slots, const unsigned long long* __restrict__ keys,
+                                const uint32_t* __restrict__ np, const float4* __restrict__ pos,
+                                const float4* __restrict__ imp, uint32_t n, unsigned long long* c_key, uint32_t* c_np,
+                                float4* c_pos, float4* c_imp) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const uint32_t s = slots[e];
+    c_key[s] = keys[e];
+    c_np[s] = np[e];
+    for (uint32_t p = 0; p < 4; ++p) {
+        c_pos[4u * s + p] = pos[4u * e + p];
+        c_imp[4u * s + p] = imp[4u * e + p];
+    }
+}
+
 __device__ __forceinline__ bool casts_linear(const DeviceBodies& b, uint32_t i) {
     return b.motion[i] == KZG_MOTION_DYNAMIC && (b.flags[i] & KZG_BODY_LINEAR_CAST) != 0u;
 }
@@ -1238,6 +1274,124 @@ __global__ void k_hash_words(DeviceBodies b, uint32_t n, unsigned long long* out
         }                                                                \
     } while (0)
 
+// ---------------------------------------------------------------------------------------------
+// manifold cache table: growth (PhysicsWorld::GetOrCreateCached, PhysicsWorld.cpp:418-433) and
+// snapshot loads
+// ---------------------------------------------------------------------------------------------
+namespace {
+struct CacheTable {
+    unsigned long long* key = nullptr;
+    uint32_t* np = nullptr;
+    float4 *pos = nullptr, *imp = nullptr;
+    cudaError_t alloc(uint32_t cap, cudaStream_t st) {
+        cudaError_t e = cudaMalloc((void**)&key, sizeof(unsigned long long) * cap);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&np, sizeof(uint32_t) * cap);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&pos, sizeof(float4) * 4 * (size_t)cap);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&imp, sizeof(float4) * 4 * (size_t)cap);
+        if (e == cudaSuccess) e = cudaMemsetAsync(key, 0, sizeof(unsigned long long) * cap, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(np, 0, sizeof(uint32_t) * cap, st);
+        return e;
+    }
+    void release() {
+        for (void* p : {(void*)key, (void*)np, (void*)pos, (void*)imp})
+            if (p) cudaFree(p);
+        key = nullptr; np = nullptr; pos = nullptr; imp = nullptr;
+    }
+};
+void swap_in(Ctx& ctx, CacheTable& t, uint32_t cap) {
+    CacheTable old{ctx.c_key, ctx.c_np, ctx.c_pos, ctx.c_imp};
+    ctx.c_key = t.key; ctx.c_np = t.np; ctx.c_pos = t.pos; ctx.c_imp = t.imp;
+    ctx.cache_cap = cap;
+    ctx.graph_dirty = true;  // the captured step holds the old table's addresses
+    old.release();
+}
+constexpr uint32_t kMaxCacheCap = 1u << 31;
+}  // namespace
+
+kzg_status cache_reserve(Ctx& ctx, uint64_t entries) {
+    uint64_t cap = ctx.cache_cap;
+    while (entries * 10u >= cap * 7u && cap < kMaxCacheCap) cap *= 2u;
+    if (cap == ctx.cache_cap) return KZG_OK;
+    if (ctx.cache_fixed) return KZG_OK;
+    KZG_CK(cudaGetLastError());
+    CacheTable t;
+    cudaError_t e = t.alloc((uint32_t)cap, ctx.stream);
+    if (e != cudaSuccess) {
+        t.release();
+        (void)cudaGetLastError();
+        ctx.err = "manifold cache: cannot grow the table to " + std::to_string(cap) + " slots";
+        return KZG_ERR_CAPACITY;
+    }
+    k_cache_rehash<<<blocks_for(ctx.cache_cap), kThreads, 0, ctx.stream>>>(
+        ctx.c_key, ctx.c_np, ctx.c_pos, ctx.c_imp, ctx.cache_cap, t.key, t.np, t.pos, t.imp, (uint32_t)cap, ctx.dcnt);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx.stream);
+    if (e != cudaSuccess) {
+        t.release();
+        ctx.err = std::string("CUDA error: ") + cudaGetErrorString(e);
+        return KZG_ERR_CUDA;
+    }
+    swap_in(ctx, t, (uint32_t)cap);
+    return KZG_OK;
+}
+
+kzg_status cache_reset(Ctx& ctx, uint32_t cap) {
+    if (cap == 0 || (cap & (cap - 1u)) != 0) {
+        ctx.err = "manifold cache capacity must be a power of two";
+        return KZG_ERR_INVALID;
+    }
+    if (cap == ctx.cache_cap) {
+        KZG_CK(cudaMemsetAsync(ctx.c_key, 0, sizeof(unsigned long long) * cap, ctx.stream));
+        KZG_CK(cudaMemsetAsync(ctx.c_np, 0, sizeof(uint32_t) * cap, ctx.stream));
+        KZG_CK(cudaStreamSynchronize(ctx.stream));
+        return KZG_OK;
+    }
+    CacheTable t;
+    cudaError_t e = t.alloc(cap, ctx.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx.stream);
+    if (e != cudaSuccess) {
+        t.release();
+        (void)cudaGetLastError();
+        ctx.err = "manifold cache: cannot allocate " + std::to_string(cap) + " slots";
+        return KZG_ERR_CAPACITY;
+    }
+    swap_in(ctx, t, cap);
+    return KZG_OK;
+}
+
+kzg_status cache_scatter(Ctx& ctx, const uint32_t* slots, const unsigned long long* keys, const uint32_t* np,
+                         const float4* pos, const float4* imp, uint32_t n) {
+    if (n == 0) return KZG_OK;
+    for (uint32_t e = 0; e < n; ++e)
+        if (slots[e] >= ctx.cache_cap) {
+            ctx.err = "manifold cache: slot out of range";
+            return KZG_ERR_INVALID;
+        }
+    const size_t bytes = n * (sizeof(uint32_t) * 2 + sizeof(unsigned long long) + sizeof(float4) * 8) + 16;
+    uint8_t* tmp = nullptr;
+    KZG_CK(cudaMalloc((void**)&tmp, bytes));
+    unsigned long long* dk = reinterpret_cast<unsigned long long*>(tmp);
+    float4* dpos = reinterpret_cast<float4*>(tmp + sizeof(unsigned long long) * n + (n & 1u ? 8 : 0));
+    float4* dimp = dpos + 4 * (size_t)n;
+    uint32_t* ds = reinterpret_cast<uint32_t*>(dimp + 4 * (size_t)n);
+    uint32_t* dn = ds + n;
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = cudaMemcpy(dk, keys, sizeof(unsigned long long) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dpos, pos, sizeof(float4) * 4 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dimp, imp, sizeof(float4) * 4 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(ds, slots, sizeof(uint32_t) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dn, np, sizeof(uint32_t) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_cache_scatter<<<blocks_for(n), kThreads, 0, ctx.stream>>>(ds, dk, dn, dpos, dimp, n, ctx.c_key, ctx.c_np,
+                                                                   ctx.c_pos, ctx.c_imp);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx.stream);
+    cudaFree(tmp);
+    KZG_CK(e);
+    return KZG_OK;
+}
+
 static kzg_status fetch_counters(Ctx& ctx) {
     KZG_CK(cudaMemcpyAsync(ctx.hcnt, ctx.dcnt, sizeof(Counters), cudaMemcpyDeviceToHost, ctx.stream));
     KZG_CK(cudaStreamSynchronize(ctx.stream));
@@ -1339,7 +1493,7 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     k_build_constraints<<<blocks_for(P), kThreads, 0, st>>>(
         ctx.pairs, ctx.con_flag, ctx.con_index, ctx.m_count, ctx.m_data, ctx.m_key, ctx.b, ctx.dcnt, ctx.con_pair,
         ctx.con_a, ctx.con_b, ctx.con_np, ctx.con_bits, ctx.con_fr, ctx.con_key, ctx.r, ctx.c_key, ctx.c_np, ctx.c_pos,
-        ctx.c_imp, ctx.cfg.max_cache_entries, ctx.ws.warm_start,
+        ctx.c_imp, ctx.cache_cap, ctx.ws.warm_start,
         (ctx.mlp.logging || (ctx.mlp.enabled && ctx.mlp.have)) ? ctx.miss_rows : nullptr, ctx.miss_prior);
     const bool sleeping = ctx.ws.allow_sleeping != 0;
     if (sleeping) {
@@ -1446,7 +1600,7 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     ctx.launches += mlp_after_solve(ctx, dt);
     KZG_CK(mark(ctx, 5));
     k_cache_store<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_key, ctx.con_np, ctx.r, ctx.c_key, ctx.c_np,
-                                                      ctx.c_pos, ctx.c_imp, ctx.cfg.max_cache_entries);
+                                                      ctx.c_pos, ctx.c_imp, ctx.cache_cap);
     const bool ccd = ctx.ws.use_ccd && ctx.nccd > 0;
     if (ccd) {
         ShapeTables T{ctx.shapes, ctx.hull_verts, ctx.face_sizes, ctx.face_idx};
@@ -1511,6 +1665,7 @@ static kzg_status finish_stats(Ctx& ctx, uint32_t graph_steps = 0) {
     // WorldStats::numIslands: BuildIslands' count, replaced by UpdateSleeping's when that pass ran
     s.num_islands = (ctx.ws.allow_sleeping && h.nsleep_n) ? h.sleep_islands : h.nroots;
     s.num_active_bodies = h.nact;
+    s.cache_capacity = ctx.cache_cap;
     s.num_batches = h.batches;
     s.max_velocity_levels = h.max_vlev;
     s.max_bias_levels = h.max_blev;
@@ -1594,12 +1749,35 @@ static kzg_status ensure_graph(Ctx& ctx, float dt) {
     return KZG_OK;
 }
 
+// New cache entries one step may add: at most one per contact constraint, so at most the pair
+// count; the last step's pair count (or the body count, if larger) stands for the next one's.
+static uint64_t cache_step_estimate(const Ctx& ctx) {
+    return std::max<uint64_t>(std::max<uint64_t>(ctx.hcnt->npairs, ctx.nbodies), 1u);
+}
+
 kzg_status step_canonical(Ctx& ctx, float dt, uint32_t nsteps) {
+    kzg_status s = fetch_counters(ctx);  // cache entries as the device holds them
+    if (s != KZG_OK) return s;
     if (ctx.use_graph) {
-        kzg_status s = ensure_graph(ctx, dt);
-        if (s != KZG_OK) return s;
+        // Replayed in runs that fit the cache: before each run the table is grown to hold two
+        // steps' worth of new entries below 0.7 load, and the run is as long as that headroom lasts.
         KZG_CK(cudaEventRecord(ctx.ev[0], ctx.stream));
-        for (uint32_t i = 0; i < nsteps; ++i) KZG_CK(cudaGraphLaunch(ctx.graph_exec, ctx.stream));
+        for (uint32_t done = 0; done < nsteps;) {
+            const uint64_t est = cache_step_estimate(ctx), have = ctx.hcnt->cache_entries;
+            s = cache_reserve(ctx, have + 2u * est);
+            if (s != KZG_OK) return s;
+            s = ensure_graph(ctx, dt);
+            if (s != KZG_OK) return s;
+            const uint64_t room = (uint64_t)ctx.cache_cap * 7u / 10u;
+            uint64_t run = room > have ? (room - have) / est : 0u;
+            run = std::min<uint64_t>(std::max<uint64_t>(run, 1u), nsteps - done);
+            for (uint64_t i = 0; i < run; ++i) KZG_CK(cudaGraphLaunch(ctx.graph_exec, ctx.stream));
+            done += (uint32_t)run;
+            if (done < nsteps) {
+                s = fetch_counters(ctx);
+                if (s != KZG_OK) return s;
+            }
+        }
         KZG_CK(cudaEventRecord(ctx.ev[6], ctx.stream));
         ctx.frame += nsteps;
         ctx.launches = ctx.graph_launches;
@@ -1608,8 +1786,10 @@ kzg_status step_canonical(Ctx& ctx, float dt, uint32_t nsteps) {
         return finish_stats(ctx, nsteps);
     }
     for (uint32_t i = 0; i < nsteps; ++i) {
+        s = cache_reserve(ctx, (uint64_t)ctx.hcnt->cache_entries + cache_step_estimate(ctx));
+        if (s != KZG_OK) return s;
         ++ctx.frame;
-        kzg_status s = record_canonical(ctx, dt);
+        s = record_canonical(ctx, dt);
         if (s != KZG_OK) return s;
         s = fetch_counters(ctx);
         if (s != KZG_OK) return s;
@@ -1625,6 +1805,10 @@ kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t np, floa
         ctx.err = "pair count exceeds kzg_config.max_pairs";
         return KZG_ERR_CAPACITY;
     }
+    kzg_status s = fetch_counters(ctx);
+    if (s != KZG_OK) return s;
+    s = cache_reserve(ctx, (uint64_t)ctx.hcnt->cache_entries + np);  // at most one new entry per pair
+    if (s != KZG_OK) return s;
     ++ctx.frame;
     ctx.launches = np > 0 ? 3 : 2;
     k_begin_step<<<1, 32, 0, st>>>(ctx.dcnt);
@@ -1636,7 +1820,7 @@ kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t np, floa
                                                                  ctx.nbodies, ctx.pairs);
     }
     KZG_CK(cudaMemcpyAsync(&ctx.dcnt->npairs, &np, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    kzg_status s = record_after_pairs(ctx, dt);
+    s = record_after_pairs(ctx, dt);
     if (s != KZG_OK) return s;
     s = fetch_counters(ctx);
     if (s != KZG_OK) return s;

@@ -4,8 +4,8 @@ Worlds never interact (each is its own PhysicsWorld in the reference; here a wor
 broad phase, so a merged context steps them side by side), so splitting a batch of worlds across
 ranks needs no exchange on the step path: each rank steps its own range and only the metrics are
 gathered.  The ranges are contiguous in world order and balanced by summed body count, the
-linear-partition rule (smallest possible largest share); a single world's giant island never
-splits, see the design notes.
+linear-partition rule (smallest possible largest share).  A single world never splits: its giant
+island is one Gauss-Seidel chain with a barrier per dependency level.
 """
 from __future__ import annotations
 
