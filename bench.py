@@ -162,6 +162,13 @@ def schedule_bytes(points: int, constraints: int) -> float:
     return float(16 * constraints + 56 * points)
 
 
+def broad_bytes(bodies: int, pairs: int) -> float:
+    """Broad phase: the bounds read (32 B per body), the cell keys written and sorted (12 B per
+    body, read and written once), the pair keys written and sorted (8 B per pair, twice), the pairs
+    written (8 B each)."""
+    return 32.0 * bodies + 24.0 * bodies + 16.0 * pairs + 8.0 * pairs
+
+
 def step_bytes(n_dyn: int, pair_bytes: float, points: int, constraints: int) -> float:
     """Whole-step compulsory traffic: 236 B per dynamic body + pair bytes + 312 B per point +
     32 B per constraint."""
@@ -470,6 +477,9 @@ def main():
                                              schedule_bytes(points, last["num_contact_constraints"])),
         "k_solve_cluster + k_solve_big + k_solve_cta + k_solve_warp": (acc["solve_ms"] / args.steps, solve_bytes(points, n_dyn)),
     }
+    cand_all = dict(cand)
+    cand_all["k_aabb + cell sort + k_find_pairs + pair sort"] = (acc["broadphase_ms"] / args.steps,
+                                                                 broad_bytes(len(sc.bodies), int(pairs.shape[0])))
     kname = max(cand, key=lambda k: cand[k][0])
     kms, kbytes = cand[kname]
     peaks = {}
@@ -530,6 +540,9 @@ def main():
         "fixed_iterations": legs["fixed"],
         "plain_solver": legs["plain"]["solver"],
         "stage_ms": {k: v / args.steps for k, v in acc.items()},
+        "kernel_gbs": {k: {"ms": ms, "algorithmic_bytes": b, "gbs": b / (ms / 1e3) / 1e9 if ms > 0 else 0.0,
+                           "frac": (b / (ms / 1e3) / 1e9 if ms > 0 else 0.0) / peak}
+                       for k, (ms, b) in cand_all.items()},
         "tuning": tuned.get("choice"),
         "model_gbs_step": step_bytes(n_dyn, nb - 40 * points, points, last["num_contact_constraints"]) /
                           (ms_per_step / 1e3) / 1e9,

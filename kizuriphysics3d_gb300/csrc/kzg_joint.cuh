@@ -9,9 +9,11 @@
 // positions are integrated, k_joint_positions runs each island's joints' position correction
 // (PhysicsWorld.cpp:293-306, 745-752).
 //
-// sin, cos, acos and atan2 are evaluated in double precision and rounded to float, which gives the
-// correctly rounded float value except near rounding midpoints; the reference calls the C
-// library's float functions, so a result can differ from the reference's in the last bit there.
+// sin, cos, acos and atan2 are evaluated in double precision and rounded to float; the reference
+// calls the C library's float functions, so a result can differ from the reference's in the last
+// bit.  The oracle's matching mode (kzo_set_trig_mode 1) does the same with the C library's double
+// functions: the two agree wherever CUDA's and the C library's double results round to the same
+// float, which the joint parity tests check rather than assume.
 #pragma once
 #include "kzg_ctx.h"
 #include "kzg_math.cuh"

@@ -27,7 +27,7 @@ def _pair_worlds(name, mode, oracle_lib, **kw):
     return sc, g, ow, gw
 
 
-# joints_mix: the joint kernels' trigonometry is correctly rounded, the reference's is the C
+# joints_mix: the joint kernels' trigonometry is evaluated in double and rounded to float, the reference's is the C
 # library's float functions; that fixture has its own tests below.
 @pytest.mark.parametrize("name", sorted(n for n in FIXTURES if n != "joints_mix"))
 def test_mode_a_bit_exact_with_reference(name, oracle_lib, kzg_lib):
@@ -162,7 +162,7 @@ def test_joints_bit_exact_with_oracle(mode, oracle_lib, kzg_lib):
 def test_joints_match_reference_until_its_trigonometry_differs(oracle_lib, kzg_lib):
     """Against the reference's own trace: the GPU's state hash equals the reference's at every step
     before the first step where the C library's float sinf / cosf / acosf / atan2f (the reference's)
-    and the correctly rounded values (the GPU's) give different bits, found by running the oracle
+    and the double-evaluated values rounded to float (the GPU's) give different bits, found by running the oracle
     both ways."""
     sc, g, ow, gw = _pair_worlds("joints_mix", oracle_lib.PAIRS_TREE, oracle_lib)
     cw = oracle_lib.OracleWorld(sc.to_bytes(), oracle_blob(sc, golden_resolved(sc, g)), oracle_lib.PAIRS_TREE)
@@ -232,7 +232,7 @@ def test_linear_cast_stops_a_bullet_at_a_thin_wall(kzg_lib):
 
 
 def _run_both(sc, steps, oracle_lib):
-    """Step the GPU world and the oracle (correctly rounded joint trigonometry) side by side;
+    """Step the GPU world and the oracle (joint trigonometry in double, rounded to float) side by side;
     returns the GPU's final state after checking every step bit for bit."""
     from kizuriphysics3d_gb300 import World, resolve
     res = resolve(sc)
@@ -330,7 +330,7 @@ def test_many_linear_cast_bodies_bit_exact_with_oracle(oracle_lib, kzg_lib):
 
 def test_joint_field_bit_exact_with_oracle(oracle_lib, kzg_lib):
     """A field of 100 ten-link chains (the chains workload, scaled down): hundreds of joint islands
-    with contacts, solved one CTA each, bit-identical to the oracle (correctly rounded trigonometry)
+    with contacts, solved one CTA each, bit-identical to the oracle (trigonometry in double, rounded to float)
     for 40 steps."""
     from kizuriphysics3d_gb300 import World, resolve, scenes
     sc = scenes.chains(10, 10, 10)

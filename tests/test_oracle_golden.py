@@ -122,7 +122,7 @@ def test_known_answer_separated(oracle_lib):
 
 def test_oracle_joint_trigonometry_modes(oracle_lib):
     """The oracle's joint trigonometry: the C library's float functions (default) reproduce the
-    reference trace; correctly rounded values (mode 1, the GPU kernels') give the same bits until
+    reference trace; double-evaluated values rounded to float (mode 1, the GPU kernels') give the same bits until
     the first call where the two differ, several steps into the joints fixture.  (After that the
     trajectories part quickly: the fixture's chain links press against each other.)"""
     sc, steps, _, _ = FIXTURES["joints_mix"]
