@@ -21,6 +21,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <initializer_list>
 #include <vector>
 
 #include "../kzg.h"
@@ -194,6 +195,11 @@ struct Capacity {
     uint32_t maxJoints = 1u << 16;
 };
 
+struct Transform {  // Math.h Transform: translation, then rotation
+    Vec3 translation;
+    Quat rotation;
+};
+
 struct BodyState {
     Vec3 position;
     Quat rotation;
@@ -288,6 +294,40 @@ public:
     uint32_t GetNumBodies() const { return numBodies_; }
     kzg_ctx* Handle() { return ctx_; }
 
+    // Activation and the convenience body operations (PhysicsWorld.cpp:109-205), applied on the
+    // device in call order; `wake` activates the body afterwards, as in the reference.
+    void SetBodyActive(BodyID id, bool active) { Edit(active ? KZG_EDIT_ACTIVATE : KZG_EDIT_DEACTIVATE, id, {}, false); }
+    void ActivateBody(BodyID id) { Edit(KZG_EDIT_ACTIVATE, id, {}, false); }
+    void DeactivateBody(BodyID id) { Edit(KZG_EDIT_DEACTIVATE, id, {}, false); }
+    uint32_t GetNumActiveBodies() {
+        Flush();
+        uint32_t n = 0;
+        Check(kzg_get_active_bodies(ctx_, nullptr, 0, &n), ctx_);
+        return n;
+    }
+    void SetBodyPosition(BodyID id, const Vec3& p, bool wake = true) { Edit(KZG_EDIT_SET_POSITION, id, {p.x, p.y, p.z}, wake); }
+    void SetBodyRotation(BodyID id, const Quat& q, bool wake = true) {
+        Edit(KZG_EDIT_SET_ROTATION, id, {q.x, q.y, q.z, q.w}, wake);
+    }
+    void SetBodyTransform(BodyID id, const Transform& t, bool wake = true) {
+        Edit(KZG_EDIT_SET_TRANSFORM, id,
+             {t.translation.x, t.translation.y, t.translation.z, t.rotation.x, t.rotation.y, t.rotation.z, t.rotation.w},
+             wake);
+    }
+    void SetLinearVelocity(BodyID id, const Vec3& v, bool wake = true) { Edit(KZG_EDIT_SET_LINEAR_VELOCITY, id, {v.x, v.y, v.z}, wake); }
+    void SetAngularVelocity(BodyID id, const Vec3& w, bool wake = true) {
+        Edit(KZG_EDIT_SET_ANGULAR_VELOCITY, id, {w.x, w.y, w.z}, wake);
+    }
+    void AddForce(BodyID id, const Vec3& f, bool wake = true) { Edit(KZG_EDIT_ADD_FORCE, id, {f.x, f.y, f.z}, wake); }
+    void AddForceAtPoint(BodyID id, const Vec3& f, const Vec3& p, bool wake = true) {
+        Edit(KZG_EDIT_ADD_FORCE_AT_POINT, id, {f.x, f.y, f.z, p.x, p.y, p.z}, wake);
+    }
+    void AddTorque(BodyID id, const Vec3& t, bool wake = true) { Edit(KZG_EDIT_ADD_TORQUE, id, {t.x, t.y, t.z}, wake); }
+    void AddImpulse(BodyID id, const Vec3& i, bool wake = true) { Edit(KZG_EDIT_ADD_IMPULSE, id, {i.x, i.y, i.z}, wake); }
+    void AddImpulseAtPoint(BodyID id, const Vec3& i, const Vec3& p, bool wake = true) {
+        Edit(KZG_EDIT_ADD_IMPULSE_AT_POINT, id, {i.x, i.y, i.z, p.x, p.y, p.z}, wake);
+    }
+
 private:
     static kzg_shape_desc Desc(const Shape& s, uint32_t fv, uint32_t ff, uint32_t fi) {
         kzg_shape_desc d{};
@@ -297,6 +337,17 @@ private:
         d.first_face = ff; d.num_faces = (uint32_t)s.faceSizes.size();
         d.first_index = fi; d.num_indices = (uint32_t)s.faceIndices.size();
         return d;
+    }
+
+    void Edit(uint32_t op, BodyID id, std::initializer_list<float> v, bool wake) {
+        Flush();
+        kzg_body_edit e{};
+        e.op = op;
+        e.body = id.Packed();
+        e.wake = wake ? 1u : 0u;
+        int k = 0;
+        for (float x : v) e.v[k++] = x;
+        Check(kzg_edit_bodies(ctx_, &e, 1), ctx_);
     }
 
     void Flush() {

@@ -304,6 +304,33 @@ kzg_status kzg_set_bodies_active(kzg_ctx* ctx, const uint32_t* packed_ids, uint3
  * at most `capacity` ids are written. */
 kzg_status kzg_get_active_bodies(kzg_ctx* ctx, uint32_t* packed_ids, uint32_t capacity, uint32_t* count);
 
+/* ---- body edits between steps (PhysicsWorld convenience operations, PhysicsWorld.cpp:109-205) --
+ * Applied in array order on the device, each exactly as the reference's method does it: the
+ * Body::Apply* forms change dynamic bodies only (Body.h:181-203), SetRotation normalises the
+ * quaternion and updates the world inverse inertia, and with `wake` set the body is then activated
+ * (BodyManager::ActivateBody: appended to the active list if it was inactive).  Forces and torques
+ * accumulate until the next step, which clears them (PhysicsWorld.cpp:312). */
+#define KZG_EDIT_SET_POSITION 0u          /* v[0..2]: position (SetBodyPosition) */
+#define KZG_EDIT_SET_ROTATION 1u          /* v[0..3]: quaternion x, y, z, w (SetBodyRotation) */
+#define KZG_EDIT_SET_TRANSFORM 2u         /* v[0..2] position, v[3..6] quaternion, used as given (SetBodyTransform) */
+#define KZG_EDIT_SET_LINEAR_VELOCITY 3u   /* v[0..2] (SetLinearVelocity) */
+#define KZG_EDIT_SET_ANGULAR_VELOCITY 4u  /* v[0..2] (SetAngularVelocity) */
+#define KZG_EDIT_ADD_FORCE 5u             /* v[0..2] at the centre (AddForce) */
+#define KZG_EDIT_ADD_FORCE_AT_POINT 6u    /* v[0..2] force, v[3..5] world point (AddForceAtPoint) */
+#define KZG_EDIT_ADD_TORQUE 7u            /* v[0..2] (AddTorque) */
+#define KZG_EDIT_ADD_IMPULSE 8u           /* v[0..2] at the centre (AddImpulse) */
+#define KZG_EDIT_ADD_IMPULSE_AT_POINT 9u  /* v[0..2] impulse, v[3..5] world point (AddImpulseAtPoint) */
+#define KZG_EDIT_ACTIVATE 10u             /* ActivateBody (wake ignored) */
+#define KZG_EDIT_DEACTIVATE 11u           /* DeactivateBody: velocities zeroed, swap-removed (wake ignored) */
+typedef struct {
+    uint32_t op;      /* KZG_EDIT_* */
+    uint32_t body;    /* packed BodyID; a stale id is skipped, as GetBody's nullptr is */
+    uint32_t wake;    /* the reference's `wake` argument (default true) */
+    uint32_t reserved;
+    float v[8];
+} kzg_body_edit;
+kzg_status kzg_edit_bodies(kzg_ctx* ctx, const kzg_body_edit* edits, uint32_t n);
+
 /* ---- diagnostics (ComputeStateHash / GetStats / GetContactConstraints / GetPairs) ----------- */
 kzg_status kzg_state_hash(kzg_ctx* ctx, uint64_t* out); /* PhysicsWorld.cpp:1145-1175 */
 kzg_status kzg_get_stats(kzg_ctx* ctx, kzg_stats* out);

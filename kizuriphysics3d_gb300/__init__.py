@@ -7,6 +7,6 @@ Public surface:
   * ``build``   - in-tree nvcc build of libkzg.so for sm_103a
 """
 from . import build, capi, scenes  # noqa: F401
-from .world import Resolved, World, build_hull, resolve  # noqa: F401
+from .world import Resolved, World, build_hull, make_edit, resolve  # noqa: F401
 
-__all__ = ["World", "Resolved", "resolve", "build_hull", "scenes", "build", "capi"]
+__all__ = ["World", "Resolved", "resolve", "build_hull", "make_edit", "scenes", "build", "capi"]

@@ -62,6 +62,13 @@ class KzgTuning(ctypes.Structure):
                 ("island_order", u32)]
 
 
+# kzg_body_edit (include/kzg.h) as a numpy record: op, packed BodyID, wake, reserved, 8 operands
+EDIT_DTYPE = np.dtype([("op", "<u4"), ("body", "<u4"), ("wake", "<u4"), ("reserved", "<u4"), ("v", "<f4", (8,))])
+(EDIT_SET_POSITION, EDIT_SET_ROTATION, EDIT_SET_TRANSFORM, EDIT_SET_LINEAR_VELOCITY, EDIT_SET_ANGULAR_VELOCITY,
+ EDIT_ADD_FORCE, EDIT_ADD_FORCE_AT_POINT, EDIT_ADD_TORQUE, EDIT_ADD_IMPULSE, EDIT_ADD_IMPULSE_AT_POINT,
+ EDIT_ACTIVATE, EDIT_DEACTIVATE) = range(12)
+
+
 class KzgStats(ctypes.Structure):
     _fields_ = [(n, u32) for n in ("num_bodies", "num_broadphase_pairs", "num_contact_constraints",
                                    "num_contact_points", "num_islands", "num_batches", "max_velocity_levels",
@@ -145,6 +152,7 @@ def load(build_if_missing: bool = True):
     L.kzg_set_wait_limit.argtypes = [vp, u32]
     L.kzg_set_bodies_active.argtypes = [vp, vp, u32, ctypes.c_int]
     L.kzg_get_active_bodies.argtypes = [vp, vp, u32, P(u32)]
+    L.kzg_edit_bodies.argtypes = [vp, vp, u32]
     L.kzg_mlp_set_params.argtypes = [vp, vp, vp, vp]
     L.kzg_mlp_get_params.argtypes = [vp, vp, vp, vp]
     L.kzg_mlp_enable.argtypes = [vp, ctypes.c_int]

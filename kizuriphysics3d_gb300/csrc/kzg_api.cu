@@ -661,6 +661,7 @@ kzg_status kzg_autotune(kzg_ctx* k, float dt, uint32_t steps_per_candidate, kzg_
     ctx->mlp.logging = false;  // the tuning steps are not part of the world's history
     DeviceBackup backup;
     CK(backup.save(*ctx));
+    const bool all_active = ctx->all_active;
     struct FixCache {
         Ctx* c;
         ~FixCache() { c->cache_fixed = false; }
@@ -678,6 +679,7 @@ kzg_status kzg_autotune(kzg_ctx* k, float dt, uint32_t steps_per_candidate, kzg_
                 kzg_tuning t{small[a], warp[b], 0.0f, orders[o]};
                 ctx->tune = t;
                 ctx->graph_dirty = true;
+                ctx->all_active = all_active;
                 if (backup.copy(*ctx, false) != cudaSuccess) { s = KZG_ERR_CUDA; break; }
                 s = step_canonical(*ctx, dt, 1);  // first step of a choice: graph capture, not timed
                 if (s != KZG_OK) break;
@@ -693,6 +695,7 @@ kzg_status kzg_autotune(kzg_ctx* k, float dt, uint32_t steps_per_candidate, kzg_
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     const cudaError_t restored = backup.copy(*ctx, false);
+    ctx->all_active = all_active;
     ctx->mlp.logging = logging;
     ctx->graph_dirty = true;
     if (s != KZG_OK) {
@@ -821,6 +824,36 @@ kzg_status kzg_set_bodies_active(kzg_ctx* k, const uint32_t* packed_ids, uint32_
     if (n > ctx->cfg.max_pairs) { ctx->err = "more ids than kzg_config.max_pairs per call"; return KZG_ERR_CAPACITY; }
     CK(cudaMemcpyAsync(ctx->pair_keys, packed_ids, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
     CK(set_bodies_active(*ctx, reinterpret_cast<const uint32_t*>(ctx->pair_keys), n, active));
+    if (!active && ctx->all_active) {  // the step now follows the active list
+        ctx->all_active = false;
+        ctx->graph_dirty = true;
+    }
+    return KZG_OK;
+}
+
+kzg_status kzg_edit_bodies(kzg_ctx* k, const kzg_body_edit* edits, uint32_t n) {
+    if (check(k) || (n && !edits)) return KZG_ERR_INVALID;
+    Ctx* ctx = &k->c;
+    for (uint32_t i = 0; i < n; ++i)
+        if (edits[i].op > KZG_EDIT_DEACTIVATE) {
+            ctx->err = "kzg_edit_bodies: edit " + std::to_string(i) + " has an unknown op";
+            return KZG_ERR_INVALID;
+        }
+    if (n == 0) return KZG_OK;
+    CK(cudaSetDevice(ctx->device));
+    kzg_status s = finalize_bodies(k);
+    if (s != KZG_OK) return s;
+    kzg_body_edit* dev = nullptr;
+    CK(cudaMalloc((void**)&dev, sizeof(kzg_body_edit) * n));
+    cudaError_t e = cudaMemcpyAsync(dev, edits, sizeof(kzg_body_edit) * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = edit_bodies(*ctx, dev, n);
+    cudaFree(dev);
+    CK(e);
+    for (uint32_t i = 0; i < n && ctx->all_active; ++i)
+        if (edits[i].op == KZG_EDIT_DEACTIVATE) {  // the step now follows the active list
+            ctx->all_active = false;
+            ctx->graph_dirty = true;
+        }
     return KZG_OK;
 }
 
@@ -1052,6 +1085,8 @@ kzg_status kzg_snapshot_load(kzg_ctx* k, const void* in, size_t size) {
     }
     if (h.reserved > nb) { ctx->err = "kzg_snapshot_load: active-list length out of range"; return KZG_ERR_INVALID; }
     CK(cudaMemcpy(&ctx->dcnt->nact, &h.reserved, sizeof(uint32_t), cudaMemcpyHostToDevice));
+    ctx->all_active = h.reserved == nb;
+    ctx->graph_dirty = true;
     const size_t used = h.cache_used;
     std::vector<uint32_t> slots(used), np(used);
     std::vector<unsigned long long> keys(used);

@@ -21,6 +21,7 @@ size_t pack_elements(uint32_t points, uint32_t* cap);
 size_t cluster_id_words(uint32_t max_cons);  // local-id scratch of the cluster solve
 cudaError_t init_new_bodies(Ctx& ctx, uint32_t first, uint32_t n);  // fat bounds, activity, active list of new bodies
 cudaError_t set_bodies_active(Ctx& ctx, const uint32_t* dev_ids, uint32_t n, int active);  // in order
+cudaError_t edit_bodies(Ctx& ctx, const kzg_body_edit* dev_edits, uint32_t n);  // in order
 cudaError_t create_joints(Ctx& ctx, uint32_t first, uint32_t n);     // joint records from ctx.joint_stage
 size_t joint_record_bytes();
 // Manifold cache table: room for `entries` at below 0.7 load (doubling, entries rehashed), and a

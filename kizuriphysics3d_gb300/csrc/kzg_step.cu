@@ -1495,8 +1495,13 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
         ctx.con_a, ctx.con_b, ctx.con_np, ctx.con_bits, ctx.con_fr, ctx.con_key, ctx.r, ctx.c_key, ctx.c_np, ctx.c_pos,
         ctx.c_imp, ctx.cache_cap, ctx.ws.warm_start,
         (ctx.mlp.logging || (ctx.mlp.enabled && ctx.mlp.have)) ? ctx.miss_rows : nullptr, ctx.miss_prior);
+    // The wake rule, BuildIslands' compact indices over the active list and the active list's order
+    // matter whenever a body may be inactive: with sleeping on, or after a body was deactivated by a
+    // call (SetBodyActive, DeactivateBody, a loaded world).  With every body active they change
+    // nothing, and the step skips them.
     const bool sleeping = ctx.ws.allow_sleeping != 0;
-    if (sleeping) {
+    const bool listed = sleeping || !ctx.all_active;
+    if (listed) {
         k_wake<<<1, 32, 0, st>>>(ctx.b, ctx.dcnt, ctx.con_a, ctx.con_b, ctx.alist);
         ++ctx.launches;
     }
@@ -1509,8 +1514,8 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     ctx.launches += mlp_after_prepare(ctx, dt);
     const uint32_t nj = ctx.njoints;
     if (nj) k_joint_prepare<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, nj);
-    const uint32_t* node = nullptr;  // island nodes (sleeping on); null: every dynamic body is its own
-    if (sleeping) {
+    const uint32_t* node = nullptr;  // island nodes (active list in use); null: every dynamic body is its own
+    if (listed) {
         k_act_flags<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, ctx.dcnt, ctx.alist, nb, ctx.act_flag);
         tb = ctx.cub_tmp_bytes;
         KZG_CK(cub::DeviceScan::ExclusiveSum(ctx.cub_tmp, tb, ctx.act_flag, ctx.act_scan, (int)nb, st));
@@ -1525,7 +1530,7 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     }
     k_uf_union<<<blocks_for(P), kThreads, 0, st>>>(ctx.dcnt, ctx.con_a, ctx.con_b, ctx.con_bits, node, ctx.uf);
     if (nj) k_joint_union<<<blocks_for(nj), kThreads, 0, st>>>(ctx.b, ctx.joints, nj, node, ctx.uf);
-    if (sleeping) {
+    if (listed) {
         KZG_CK(cudaMemsetAsync(ctx.root_mark, 0, sizeof(uint32_t) * nb, st));
         k_mark_roots<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, ctx.uf, ctx.root_mark);
         k_count_marks<<<blocks_for(nb), kThreads, 0, st>>>(ctx.root_mark, nb, ctx.dcnt);
@@ -1605,9 +1610,9 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     if (ccd) {
         ShapeTables T{ctx.shapes, ctx.hull_verts, ctx.face_sizes, ctx.face_idx};
         const float mp = ctx.ws.ccd_max_penetration;
-        // the position loop's order: slot order, or with sleeping on the active list's
+        // the position loop's order: the active list's (slot order while every body is active)
         const uint32_t* list = ctx.ccd_list;
-        if (sleeping) {
+        if (listed) {
             k_ccd_rank_keys<<<blocks_for(ctx.nccd), kThreads, 0, st>>>(ctx.b, ctx.ccd_list, ctx.nccd, ctx.ccd_rank_keys);
             size_t tbc = ctx.cub_tmp_bytes;
             KZG_CK(cub::DeviceRadixSort::SortPairs(ctx.cub_tmp, tbc, ctx.ccd_rank_keys, ctx.ccd_keys_sorted,
@@ -1619,13 +1624,13 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
                                                                ctx.ccd_state);
         k_ccd_deps<<<blocks_for(32u * ctx.nccd), kThreads, 0, st>>>(ctx.b, ctx.shapes, nb, list, ctx.nccd,
                                                                     dt, ctx.ccd_state, ctx.ccd_deps, ctx.ccd_ndeps,
-                                                                    sleeping);
+                                                                    listed);
         for (uint32_t r = 1; r <= kCcdRounds; ++r)
             k_ccd_round<<<blocks_for(32u * ctx.nccd), kThreads, 0, st>>>(T, ctx.b, nb, list, ctx.nccd, dt, mp,
                                                                          ctx.ccd_disp, ctx.ccd_state, ctx.ccd_deps,
-                                                                         ctx.ccd_ndeps, r, sleeping);
+                                                                         ctx.ccd_ndeps, r, listed);
         k_ccd_serial<<<1, kCcdThreads, 0, st>>>(T, ctx.b, nb, list, ctx.nccd, dt, mp, ctx.ccd_disp,
-                                                ctx.ccd_state, sleeping);
+                                                ctx.ccd_state, listed);
         ctx.launches += 3 + kCcdRounds;
     }
     k_integrate_pos<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, dt, ctx.ss.use_velocity_bias,
@@ -1657,6 +1662,10 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
 
 static kzg_status finish_stats(Ctx& ctx, uint32_t graph_steps = 0) {
     Counters& h = *ctx.hcnt;
+    if (!ctx.all_active && h.nact == ctx.nbodies) {  // every body active again: back to the short step
+        ctx.all_active = true;
+        ctx.graph_dirty = true;
+    }
     kzg_stats& s = ctx.stats;
     s.num_bodies = ctx.nbodies;
     s.num_broadphase_pairs = h.npairs;
@@ -1830,35 +1839,116 @@ kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t np, floa
 // PhysicsWorld::SetBodyActive / ActivateBody / DeactivateBody (PhysicsWorld.cpp:108-111, 132-133;
 // BodyManager.cpp:133-160) for a list of packed BodyIDs, one after another in the given order; stale
 // ids are skipped.  One thread: the active list is order-dependent.
+__device__ void activate_slot(DeviceBodies& b, uint32_t* alist, uint32_t& size, uint32_t x) {
+    if (b.act[x]) return;
+    b.act[x] = 1u;
+    b.sleep_t[x] = 0.0f;
+    b.apos[x] = size;
+    alist[size++] = x;
+}
+__device__ void deactivate_slot(DeviceBodies& b, uint32_t* alist, uint32_t& size, uint32_t x) {
+    if (!b.act[x]) return;
+    b.act[x] = 0u;
+    b.lv[x] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    b.av[x] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const uint32_t at = b.apos[x], last = size - 1u;
+    if (at != last) {
+        const uint32_t moved = alist[last];
+        alist[at] = moved;
+        b.apos[moved] = at;
+    }
+    b.apos[x] = kInvalid;
+    --size;
+}
+__device__ __forceinline__ bool live_slot(const DeviceBodies& b, uint32_t id, uint32_t nb, uint32_t* x) {
+    *x = id & 0x00FFFFFFu;
+    return *x < nb && b.packed[*x] == id;
+}
+
 __global__ void k_set_active(DeviceBodies b, Counters* cnt, uint32_t* alist, const uint32_t* __restrict__ ids, uint32_t n,
                              uint32_t nb, int active) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     uint32_t size = cnt->nact;
     for (uint32_t k = 0; k < n; ++k) {
-        const uint32_t x = ids[k] & 0x00FFFFFFu;
-        if (x >= nb || b.packed[x] != ids[k]) continue;
-        if (active) {
-            if (b.act[x]) continue;
-            b.act[x] = 1u;
-            b.sleep_t[x] = 0.0f;
-            b.apos[x] = size;
-            alist[size++] = x;
-        } else {
-            if (!b.act[x]) continue;
-            b.act[x] = 0u;
-            b.lv[x] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            b.av[x] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            const uint32_t at = b.apos[x], last = size - 1u;
-            if (at != last) {
-                const uint32_t moved = alist[last];
-                alist[at] = moved;
-                b.apos[moved] = at;
-            }
-            b.apos[x] = kInvalid;
-            --size;
-        }
+        uint32_t x;
+        if (!live_slot(b, ids[k], nb, &x)) continue;
+        if (active) activate_slot(b, alist, size, x);
+        else deactivate_slot(b, alist, size, x);
     }
     cnt->nact = size;
+}
+
+// PhysicsWorld's convenience body operations (PhysicsWorld.cpp:135-205; Body.h:149-203) in the given
+// order; one thread, since waking appends to the active list.
+__device__ void set_world_inertia(DeviceBodies& b, uint32_t x, const Quat& q) {  // UpdateWorldInertia (Body.h:121-124)
+    const Mat3 R = q.to_mat3();
+    const Mat3 W = (R * M3(&b.iil[3 * x])) * R.transposed();
+    b.iiw[3 * x] = F4(W.c0, 0.0f);
+    b.iiw[3 * x + 1] = F4(W.c1, 0.0f);
+    b.iiw[3 * x + 2] = F4(W.c2, 0.0f);
+}
+__global__ void k_edit_bodies(DeviceBodies b, Counters* cnt, uint32_t* alist, const kzg_body_edit* __restrict__ e,
+                              uint32_t n, uint32_t nb) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    uint32_t size = cnt->nact;
+    for (uint32_t k = 0; k < n; ++k) {
+        const kzg_body_edit ed = e[k];
+        uint32_t x;
+        if (!live_slot(b, ed.body, nb, &x)) continue;
+        const bool dyn = b.motion[x] == KZG_MOTION_DYNAMIC;
+        const Vec3 v0(ed.v[0], ed.v[1], ed.v[2]), v1(ed.v[3], ed.v[4], ed.v[5]);
+        switch (ed.op) {
+            case KZG_EDIT_SET_POSITION: b.pos[x] = F4(v0, 0.0f); break;
+            case KZG_EDIT_SET_ROTATION: {
+                const Quat q = Quat(ed.v[0], ed.v[1], ed.v[2], ed.v[3]).normalized();
+                b.rot[x] = F4q(q);
+                set_world_inertia(b, x, q);
+                break;
+            }
+            case KZG_EDIT_SET_TRANSFORM: {
+                const Quat q(ed.v[3], ed.v[4], ed.v[5], ed.v[6]);
+                b.pos[x] = F4(v0, 0.0f);
+                b.rot[x] = F4q(q);
+                set_world_inertia(b, x, q);
+                break;
+            }
+            case KZG_EDIT_SET_LINEAR_VELOCITY: b.lv[x] = F4(v0, 0.0f); break;
+            case KZG_EDIT_SET_ANGULAR_VELOCITY: b.av[x] = F4(v0, 0.0f); break;
+            case KZG_EDIT_ADD_FORCE:
+                if (dyn) b.force[x] = F4(V3(b.force[x]) + v0, 0.0f);
+                break;
+            case KZG_EDIT_ADD_FORCE_AT_POINT:
+                if (dyn) {
+                    b.force[x] = F4(V3(b.force[x]) + v0, 0.0f);
+                    b.torque[x] = F4(V3(b.torque[x]) + (v1 - V3(b.pos[x])).cross(v0), 0.0f);
+                }
+                break;
+            case KZG_EDIT_ADD_TORQUE:
+                if (dyn) b.torque[x] = F4(V3(b.torque[x]) + v0, 0.0f);
+                break;
+            case KZG_EDIT_ADD_IMPULSE:
+                if (dyn) b.lv[x] = F4(V3(b.lv[x]) + v0 * b.inv_mass[x], 0.0f);
+                break;
+            case KZG_EDIT_ADD_IMPULSE_AT_POINT:
+                if (dyn) {
+                    b.lv[x] = F4(V3(b.lv[x]) + v0 * b.inv_mass[x], 0.0f);
+                    const Vec3 r = v1 - V3(b.pos[x]);
+                    b.av[x] = F4(V3(b.av[x]) + M3(&b.iiw[3 * x]) * r.cross(v0), 0.0f);
+                }
+                break;
+            case KZG_EDIT_ACTIVATE: activate_slot(b, alist, size, x); continue;
+            case KZG_EDIT_DEACTIVATE: deactivate_slot(b, alist, size, x); continue;
+            default: continue;
+        }
+        if (ed.wake) activate_slot(b, alist, size, x);
+    }
+    cnt->nact = size;
+}
+
+cudaError_t edit_bodies(Ctx& ctx, const kzg_body_edit* dev_edits, uint32_t n) {
+    k_edit_bodies<<<1, 1, 0, ctx.stream>>>(ctx.b, ctx.dcnt, ctx.alist, dev_edits, n, ctx.nbodies);
+    cudaError_t e = cudaGetLastError();
+    return e != cudaSuccess ? e : cudaStreamSynchronize(ctx.stream);
 }
 
 cudaError_t set_bodies_active(Ctx& ctx, const uint32_t* dev_ids, uint32_t n, int active) {

@@ -75,6 +75,15 @@ def _shape_table(scene: Scene, hulls: Dict[int, HullData]):
     return descs, np.ascontiguousarray(V), np.ascontiguousarray(S), np.ascontiguousarray(I)
 
 
+def make_edit(op: int, packed_id: int, values=(), wake: bool = True) -> np.ndarray:
+    """One kzg_body_edit record: `values` fills the operands in the order include/kzg.h gives."""
+    e = np.zeros(1, capi.EDIT_DTYPE)
+    e["op"], e["body"], e["wake"] = op, packed_id, int(bool(wake))
+    v = np.asarray(values, np.float32).reshape(-1)
+    e["v"][0, :v.size] = v
+    return e
+
+
 def resolve(scene: Scene) -> Resolved:
     """Build every hull and every body's mass properties on the host (no GPU needed)."""
     L = capi.load()
@@ -328,6 +337,12 @@ class World:
     def set_bodies_active(self, packed_ids, active: bool):
         ids = np.ascontiguousarray(packed_ids, np.uint32).reshape(-1)
         self._check(capi.load().kzg_set_bodies_active(self._h, capi.ptr(ids), ids.size, int(bool(active))))
+
+    def edit_bodies(self, edits: np.ndarray):
+        """kzg_edit_bodies: PhysicsWorld's SetBody*/Add*/Activate/Deactivate operations, applied in
+        order; `edits` is an array of capi.EDIT_DTYPE records (see make_edit)."""
+        e = np.ascontiguousarray(edits, capi.EDIT_DTYPE).reshape(-1)
+        self._check(capi.load().kzg_edit_bodies(self._h, capi.ptr(e), e.size))
 
     # -- diagnostics ----------------------------------------------------------------------------
     def compute_state_hash(self) -> int:

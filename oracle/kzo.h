@@ -58,6 +58,18 @@ void kzo_get_activity(const kzo_world* w, uint32_t* active_list, uint8_t* active
 uint32_t kzo_shared_sleepers(const kzo_world* w);
 /* PhysicsWorld::SetBodyActive for each packed id in order (stale ids skipped). */
 void kzo_set_bodies_active(kzo_world* w, const uint32_t* ids, uint32_t n, int active);
+/* PhysicsWorld's convenience body operations in order; the layout and op numbers are those of the
+ * GPU library's kzg_body_edit. */
+enum {
+    KZO_EDIT_SET_POSITION, KZO_EDIT_SET_ROTATION, KZO_EDIT_SET_TRANSFORM, KZO_EDIT_SET_LINEAR_VELOCITY,
+    KZO_EDIT_SET_ANGULAR_VELOCITY, KZO_EDIT_ADD_FORCE, KZO_EDIT_ADD_FORCE_AT_POINT, KZO_EDIT_ADD_TORQUE,
+    KZO_EDIT_ADD_IMPULSE, KZO_EDIT_ADD_IMPULSE_AT_POINT, KZO_EDIT_ACTIVATE, KZO_EDIT_DEACTIVATE
+};
+typedef struct {
+    uint32_t op, body, wake, reserved;
+    float v[8];
+} kzo_body_edit;
+void kzo_edit_bodies(kzo_world* w, const kzo_body_edit* edits, uint32_t n);
 
 int kzo_step(kzo_world* w, float dt);
 

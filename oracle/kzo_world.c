@@ -1342,7 +1342,7 @@ static void build_islands(kzo_world* w) {
     uint32_t* link = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * (size_t)w->nb);
     for (int b = 0; b < w->nb; ++b) {
         link[b] = NUL;
-        if (w->allow_sleeping && w->motion[b] == KZO_DYNAMIC && !w->is_active[b] && w->island_index[b] >= numDyn)
+        if (w->motion[b] == KZO_DYNAMIC && !w->is_active[b] && w->island_index[b] >= numDyn)
             link[b] = nel++;
     }
     uint32_t* par = (uint32_t*)xrealloc(NULL, sizeof(uint32_t) * nel);
@@ -1992,6 +1992,60 @@ void kzo_set_bodies_active(kzo_world* w, const uint32_t* ids, uint32_t n, int ac
         if (b < 0) continue;
         if (active) activate_body(w, b);
         else deactivate_body(w, b);
+    }
+}
+
+/* PhysicsWorld's convenience body operations, in order (PhysicsWorld.cpp:109-205, Body.h:149-203):
+ * SetBodyPosition/Rotation/Transform, SetLinear/AngularVelocity, AddForce(AtPoint), AddTorque,
+ * AddImpulse(AtPoint), each followed by ActivateBody when `wake` is set; Activate/DeactivateBody.
+ * The Apply* forms change dynamic bodies only; a stale id is skipped (GetBody returns nullptr). */
+void kzo_edit_bodies(kzo_world* w, const kzo_body_edit* e, uint32_t n) {
+    for (uint32_t k = 0; k < n; ++k) {
+        const kzo_body_edit* d = &e[k];
+        const int b = body_of(w, d->body);
+        if (b < 0) continue;
+        const int dyn = w->motion[b] == KZO_DYNAMIC;
+        const v3 v0 = V(d->v[0], d->v[1], d->v[2]), v1 = V(d->v[3], d->v[4], d->v[5]);
+        switch (d->op) {
+            case KZO_EDIT_SET_POSITION: w->pos[b] = v0; break;
+            case KZO_EDIT_SET_ROTATION:
+                w->rot[b] = qnormalized(Q(d->v[0], d->v[1], d->v[2], d->v[3]));
+                update_world_inertia(w, b);
+                break;
+            case KZO_EDIT_SET_TRANSFORM:
+                w->pos[b] = v0;
+                w->rot[b] = Q(d->v[3], d->v[4], d->v[5], d->v[6]);
+                update_world_inertia(w, b);
+                break;
+            case KZO_EDIT_SET_LINEAR_VELOCITY: w->lv[b] = v0; break;
+            case KZO_EDIT_SET_ANGULAR_VELOCITY: w->av[b] = v0; break;
+            case KZO_EDIT_ADD_FORCE:
+                if (dyn) w->force[b] = vadd(w->force[b], v0);
+                break;
+            case KZO_EDIT_ADD_FORCE_AT_POINT:
+                if (dyn) {
+                    w->force[b] = vadd(w->force[b], v0);
+                    w->torque[b] = vadd(w->torque[b], vcross(vsub(v1, w->pos[b]), v0));
+                }
+                break;
+            case KZO_EDIT_ADD_TORQUE:
+                if (dyn) w->torque[b] = vadd(w->torque[b], v0);
+                break;
+            case KZO_EDIT_ADD_IMPULSE:
+                if (dyn) w->lv[b] = vadd(w->lv[b], vmul(v0, w->inv_mass[b]));
+                break;
+            case KZO_EDIT_ADD_IMPULSE_AT_POINT:
+                if (dyn) {
+                    w->lv[b] = vadd(w->lv[b], vmul(v0, w->inv_mass[b]));
+                    const v3 r = vsub(v1, w->pos[b]);
+                    w->av[b] = vadd(w->av[b], mmulv(&w->iiw[b], vcross(r, v0)));
+                }
+                break;
+            case KZO_EDIT_ACTIVATE: activate_body(w, b); continue;
+            case KZO_EDIT_DEACTIVATE: deactivate_body(w, b); continue;
+            default: continue;
+        }
+        if (d->wake) activate_body(w, b);
     }
 }
 

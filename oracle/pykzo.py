@@ -17,6 +17,9 @@ LIB_PATH = os.path.join(HERE, "_build", "libkzo.so")
 PAIRS_TREE = 0
 PAIRS_CANONICAL = 1
 PAIRS_EXTERNAL = 2
+
+# kzo_body_edit (kzo.h): op, packed body id, wake, reserved, 8 operands
+EDIT_DTYPE = np.dtype([("op", "<u4"), ("body", "<u4"), ("wake", "<u4"), ("reserved", "<u4"), ("v", "<f4", (8,))])
 PT_FLOATS = 39
 
 _lib = None
@@ -51,6 +54,7 @@ def lib():
         L.kzo_shared_sleepers.restype = u32
         L.kzo_shared_sleepers.argtypes = [vp]
         L.kzo_set_bodies_active.argtypes = [vp, vp, u32, ctypes.c_int]
+        L.kzo_edit_bodies.argtypes = [vp, vp, u32]
         L.kzo_set_external_pairs.argtypes = [vp, vp, u32]
         L.kzo_step.argtypes = [vp, f32]
         L.kzo_num_bodies.restype = u32
@@ -130,6 +134,11 @@ class OracleWorld:
     def set_bodies_active(self, packed_ids, active: bool):
         ids = np.ascontiguousarray(packed_ids, np.uint32).reshape(-1)
         lib().kzo_set_bodies_active(self._w, _ptr(ids), ids.size, int(bool(active)))
+
+    def edit_bodies(self, edits: np.ndarray):
+        """kzo_edit_bodies: a structured array of EDIT_DTYPE records, applied in order."""
+        e = np.ascontiguousarray(edits, EDIT_DTYPE).reshape(-1)
+        lib().kzo_edit_bodies(self._w, _ptr(e), e.size)
 
     def shared_sleepers(self) -> int:
         return int(lib().kzo_shared_sleepers(self._w))

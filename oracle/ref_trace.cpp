@@ -11,6 +11,10 @@
 //   detail_steps : number of leading steps that also dump pairs and contact constraints
 //   --st         : WorldSettings::useMultithreading = false
 //   --kzp1 path  : write the world after the last step with SaveWorldToFile (a KZP1 file)
+//   --edits path : body operations applied before given steps through PhysicsWorld's own methods
+//                  (SetBodyPosition ... DeactivateBody, PhysicsWorld.cpp:109-205); the file holds
+//                  a u32 count, then per edit u32 step, op, slot (bit 31: use a stale BodyID of
+//                  that slot), wake and 8 floats (op numbers and operands as kzg_body_edit's)
 #include "Kizuri/Kizuri.h"
 
 #include <cstdio>
@@ -42,6 +46,34 @@ struct Writer {
     void putv(const Vec3& v) { put(v.x); put(v.y); put(v.z); }
 };
 
+struct Edit {
+    uint32_t step, op, slot, wake;
+    float v[8];
+};
+
+void apply_edit(PhysicsWorld& world, const std::vector<BodyID>& ids, const Edit& e) {
+    const uint32_t slot = e.slot & 0x7FFFFFFFu;
+    BodyID id = ids[slot];
+    if (e.slot & 0x80000000u) id = BodyID::Unpack(id.Packed() ^ (1u << 24));  // stale: another sequence
+    const Vec3 a(e.v[0], e.v[1], e.v[2]), b(e.v[3], e.v[4], e.v[5]);
+    const bool wake = e.wake != 0;
+    switch (e.op) {
+        case 0: world.SetBodyPosition(id, a, wake); break;
+        case 1: world.SetBodyRotation(id, Quat(e.v[0], e.v[1], e.v[2], e.v[3]), wake); break;
+        case 2: world.SetBodyTransform(id, Transform(Quat(e.v[3], e.v[4], e.v[5], e.v[6]), a), wake); break;
+        case 3: world.SetLinearVelocity(id, a, wake); break;
+        case 4: world.SetAngularVelocity(id, a, wake); break;
+        case 5: world.AddForce(id, a, wake); break;
+        case 6: world.AddForceAtPoint(id, a, b, wake); break;
+        case 7: world.AddTorque(id, a, wake); break;
+        case 8: world.AddImpulse(id, a, wake); break;
+        case 9: world.AddImpulseAtPoint(id, a, b, wake); break;
+        case 10: world.ActivateBody(id); break;
+        case 11: world.DeactivateBody(id); break;
+        default: std::fprintf(stderr, "edit op %u unknown\n", e.op); std::exit(1);
+    }
+}
+
 struct SceneShape {
     uint32_t type;
     float p[4];
@@ -64,6 +96,17 @@ int main(int argc, char** argv) {
     for (int i = 1; i < argc; ++i) {
         if (std::strcmp(argv[i], "--st") == 0) singleThread = true;
         if (std::strcmp(argv[i], "--kzp1") == 0 && i + 1 < argc) kzp1Path = argv[i + 1];
+    }
+    std::vector<Edit> edits;
+    for (int i = 1; i + 1 < argc; ++i) {
+        if (std::strcmp(argv[i], "--edits") != 0) continue;
+        FILE* ef = std::fopen(argv[i + 1], "rb");
+        if (!ef) { std::perror("edits"); return 1; }
+        uint32_t n = 0;
+        if (std::fread(&n, 4, 1, ef) != 1) { std::fprintf(stderr, "edits: short file\n"); return 1; }
+        edits.resize(n);
+        if (n && std::fread(edits.data(), sizeof(Edit), n, ef) != n) { std::fprintf(stderr, "edits: short file\n"); return 1; }
+        std::fclose(ef);
     }
 
     Reader rd;
@@ -271,6 +314,11 @@ int main(int argc, char** argv) {
 
     double totalMs = 0;
     for (int s = 0; s < steps; ++s) {
+        for (const Edit& e : edits)
+            if (e.step == uint32_t(s)) {
+                if ((e.slot & 0x7FFFFFFFu) >= nb) { std::fprintf(stderr, "edit slot out of range\n"); return 1; }
+                apply_edit(world, ids, e);
+            }
         auto t0 = std::chrono::steady_clock::now();
         world.StepFixed(dt);
         auto t1 = std::chrono::steady_clock::now();

@@ -68,3 +68,29 @@ def oracle_blob(scene, resolved) -> bytes:
 
 def bits(a: np.ndarray) -> np.ndarray:
     return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+# kzg_body_edit / kzo_body_edit records: op, packed BodyID, wake, reserved, 8 operands
+BODY_EDIT_DTYPE = np.dtype([("op", "<u4"), ("body", "<u4"), ("wake", "<u4"), ("reserved", "<u4"),
+                            ("v", "<f4", (8,))])
+
+
+def golden_edits(g: dict, step: int) -> np.ndarray:
+    """The body operations a golden fixture's reference run applied before `step`, as edit records
+    with packed ids (a stale id is the slot's id with another sequence number)."""
+    e = g.get("edits")
+    if e is None:
+        return np.zeros(0, BODY_EDIT_DTYPE)
+    e = e[e["step"] == step]
+    out = np.zeros(len(e), BODY_EDIT_DTYPE)
+    slot = e["slot"] & 0x7FFFFFFF
+    out["body"] = g["packed"][slot] ^ np.where(e["slot"] & 0x80000000, np.uint32(1 << 24), np.uint32(0))
+    out["op"], out["wake"], out["v"] = e["op"], e["wake"], e["v"]
+    return out
+
+
+def apply_golden_edits(world, g: dict, step: int) -> None:
+    """Apply golden_edits(g, step) to an oracle or GPU world (both take the same records)."""
+    e = golden_edits(g, step)
+    if len(e):
+        world.edit_bodies(e)

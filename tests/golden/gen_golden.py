@@ -45,7 +45,96 @@ def fixture_scenes():
     out["sleep_wake"] = (_sleep_wake(), 600, 2, [0, 59, 119, 239, 359, 479, 599])
     out["pile120_sleep"] = (_sleeping(scenes.pile(120, seed=55, extent=2.5, y_range=(1.0, 8.0)), "pile120_sleep"),
                             480, 2, [0, 119, 239, 479])
+    out["edits_sleep"] = (_edits_sleep_scene(), 480, 2, [0, 20, 45, 199, 200, 299, 479])
+    out["edits_nosleep"] = (_edits_nosleep_scene(), 240, 2, [0, 40, 41, 119, 120, 239])
     return out
+
+
+# Body operations between steps (PhysicsWorld.cpp:109-205), applied by the reference through its own
+# methods: name -> list of (step, op, slot, wake, operands, stale).  Op numbers are kzg_body_edit's.
+(E_POS, E_ROT, E_XFORM, E_LINV, E_ANGV, E_FORCE, E_FORCE_AT, E_TORQUE, E_IMP, E_IMP_AT, E_ACT, E_DEACT) = range(12)
+EDIT_DTYPE = np.dtype([("step", "<u4"), ("op", "<u4"), ("slot", "<u4"), ("wake", "<u4"), ("v", "<f4", (8,))])
+
+
+def edit_schedules():
+    """Fixture name -> its edit records (EDIT_DTYPE; slot bit 31: a stale BodyID of that slot)."""
+    f = scenes.f32
+    top_y = f(0.5 + 2 * 1.02)
+    sleep = [  # edits_sleep: slots 1-6 pyramid, 7-9 stack, 10-13 spheres, 14 box, 15 kinematic, 16 capsule
+        (20, E_IMP_AT, 6, 1, (2.0, 0.0, 0.0, 0.0, f(top_y + 0.5), 0.3)),
+        (20, E_LINV, 10, 1, (0.0, 4.0, 0.0)),
+        (20, E_FORCE, 7, 1, (0.0, 900.0, 0.0)),
+        (20, E_TORQUE, 8, 1, (0.0, 30.0, 0.0)),
+        (20, E_IMP, 0, 1, (1.0, 0.0, 0.0)),  # static ground: Apply* ignores it, wake keeps it active
+        (45, E_ROT, 14, 1, (0.0, 0.5, 0.0, 1.0)),  # not normalised: SetBodyRotation normalises
+        (45, E_POS, 11, 0, (-5.5, 3.0, 4.0)),
+        (45, E_ANGV, 16, 1, (0.0, 3.0, 0.0)),
+        (45, E_FORCE_AT, 16, 1, (0.0, 0.0, 200.0, -3.7, 0.2, 4.0)),
+        (200, E_DEACT, 12, 0, ()),
+        (200, E_IMP, 13, 0, (0.0, 0.0, 3.0)),  # on a body that may be asleep, without waking it
+        (200, E_XFORM, 2, 1, (f(1.02), f(0.7), 0.0, 0.0, 0.0, 0.0998, 0.995)),
+        (200, E_ACT, 0, 0, ()),  # ActivateBody on a static body: it joins the active list
+        (260, E_LINV, 15, 1, (1.0, 0.0, 0.0)),  # kinematic pusher towards the stack
+        (300, E_DEACT, 15, 0, ()),  # a deactivated kinematic body stops (velocities zeroed)
+        (340, E_LINV, 14, 1, (0.0, 10.0, 0.0), True),  # stale id: skipped
+        (340, E_ACT, 15, 0, ()),
+        (340, E_LINV, 15, 1, (-1.0, 0.0, 0.0)),
+        (400, E_FORCE, 9, 1, (0.0, 2000.0, 0.0)),
+    ]
+    nosleep = [  # edits_nosleep: 80-body pile, sleeping off; deactivated bodies wait until touched
+        (40, E_DEACT, 5, 0, ()),
+        (40, E_DEACT, 17, 0, ()),
+        (40, E_DEACT, 33, 0, ()),
+        (40, E_DEACT, 50, 0, ()),
+        (40, E_LINV, 60, 0, (0.0, 6.0, 0.0)),
+        (120, E_DEACT, 71, 0, ()),
+        (120, E_IMP_AT, 8, 1, (0.0, 3.0, 0.0, 0.0, 0.0, 0.0)),
+        (120, E_ACT, 17, 0, ()),
+        (120, E_XFORM, 40, 1, (0.0, 6.0, 0.0, 0.0, 0.0, 0.0, 1.0)),  # dropped onto the pile again
+    ]
+    out = {}
+    for name, lst in (("edits_sleep", sleep), ("edits_nosleep", nosleep)):
+        e = np.zeros(len(lst), EDIT_DTYPE)
+        for k, rec in enumerate(lst):
+            step, op, slot, wake, vals = rec[:5]
+            stale = len(rec) > 5 and rec[5]
+            e[k]["step"], e[k]["op"], e[k]["wake"] = step, op, wake
+            e[k]["slot"] = slot | (0x80000000 if stale else 0)
+            e[k]["v"][:len(vals)] = np.asarray(vals, np.float32)
+        out[name] = e
+    return out
+
+
+def _edits_sleep_scene():
+    """Sleeping on; a 3-row pyramid, a 3-box stack, four spheres, a free box, a kinematic box and a
+    capsule, poked by the edit schedule while they fall asleep and wake."""
+    S = scenes
+    f = S.f32
+    sc = S.Scene(name="edits_sleep")
+    S._timed_settings(sc, 10, 2)
+    sc.flags |= S.WORLD_FLAG_ALLOW_SLEEPING
+    S._ground(sc, 0.6)
+    box = sc.add_shape(S.Shape(S.SHAPE_BOX, [0.5, 0.5, 0.5, 0.0]))
+    ball = sc.add_shape(S.Shape(S.SHAPE_SPHERE, [0.3, 0.0, 0.0, 0.0]))
+    cap = sc.add_shape(S.Shape(S.SHAPE_CAPSULE, [0.3, 0.2, 0.0, 0.0]))
+    for r in range(3):
+        n = 3 - r
+        for i in range(n):
+            sc.add_body(S.Body(box, pos=(f((i - (n - 1) * 0.5) * 1.02), f(0.5 + r * 1.02), 0.0), friction=0.6))
+    for k in range(3):
+        sc.add_body(S.Body(box, pos=(6.0, f(0.5 + 1.01 * k), -4.0), friction=0.6))
+    for k in range(4):
+        sc.add_body(S.Body(ball, pos=(f(-6.0 + 0.61 * k), 0.3, 4.0), friction=0.6))
+    sc.add_body(S.Body(box, pos=(-6.0, 0.5, -3.0), friction=0.6))
+    sc.add_body(S.Body(box, S.MOTION_KINEMATIC, pos=(3.0, 0.6, -4.0)))
+    sc.add_body(S.Body(cap, pos=(-4.0, 0.2, 4.0), rot=(0.0, 0.0, f(0.7071068), f(0.7071068)), friction=0.6))
+    return sc
+
+
+def _edits_nosleep_scene():
+    sc = scenes.pile(80, seed=909, extent=2.0, y_range=(1.0, 6.0))
+    sc.name = "edits_nosleep"
+    return sc
 
 
 def kzp1_fixtures():
@@ -297,12 +386,21 @@ def main():
             sp = os.path.join(td, name + ".kzsc")
             tp = os.path.join(td, name + ".kztr")
             sc.save(sp)
-            subprocess.run([exe, sp, tp, str(steps), str(detail)], check=True)
+            cmd = [exe, sp, tp, str(steps), str(detail)]
+            edits = edit_schedules().get(name)
+            if edits is not None:
+                ep = os.path.join(td, name + ".edits")
+                with open(ep, "wb") as fh:
+                    fh.write(np.uint32(len(edits)).tobytes() + edits.tobytes())
+                cmd += ["--edits", ep]
+            subprocess.run(cmd, check=True)
             tr = T.read_trace(tp)
             fx = dict(hashes=tr.hashes, stats=tr.stats, packed=tr.packed, inv_mass=tr.inv_mass,
                       inv_inertia_local=tr.inv_inertia_local, inv_inertia_world=tr.inv_inertia_world,
                       state0=tr.state0, ckpt_steps=np.array(ckpt, np.int32),
                       ckpt_states=np.stack([tr.states[s] for s in ckpt]))
+            if edits is not None:
+                fx["edits"] = edits
             for si, hull in tr.hulls.items():
                 fx[f"hull{si}_verts"] = hull.verts
                 fx[f"hull{si}_sizes"] = hull.sizes

@@ -10,7 +10,7 @@ running the same pair order.
 import numpy as np
 import pytest
 
-from conftest import bits, golden_resolved, load_golden, oracle_blob
+from conftest import apply_golden_edits, bits, golden_resolved, load_golden, oracle_blob
 from tests.golden.gen_golden import fixture_scenes
 
 FIXTURES = fixture_scenes()
@@ -37,6 +37,8 @@ def test_mode_a_bit_exact_with_reference(name, oracle_lib, kzg_lib):
         im, iw = gw.mass()
         assert np.array_equal(bits(iw), bits(g["inv_inertia_world"]))
         for s in range(steps):
+            apply_golden_edits(ow, g, s)  # body operations of the reference run (edit fixtures)
+            apply_golden_edits(gw, g, s)
             ow.step(np.float32(sc.dt))
             gw.step_with_pairs(ow.pairs())
             gs = gw.get_stats()
@@ -62,11 +64,13 @@ def test_mode_a_bit_exact_with_reference(name, oracle_lib, kzg_lib):
 
 @pytest.mark.parametrize("name,steps", [("pile200", 300), ("stacks2x2x20", 200), ("pyramid20", 200),
                                         ("ccd_shots", 120), ("ccd_threshold", 90), ("sleep_wake", 600),
-                                        ("pile120_sleep", 480)])
+                                        ("pile120_sleep", 480), ("edits_sleep", 480), ("edits_nosleep", 240)])
 def test_mode_b_bit_exact_with_oracle(name, steps, oracle_lib, kzg_lib):
     sc, g, ow, gw = _pair_worlds(name, oracle_lib.PAIRS_CANONICAL, oracle_lib)
     with gw:
         for s in range(steps):
+            apply_golden_edits(ow, g, s)
+            apply_golden_edits(gw, g, s)
             ow.step(np.float32(sc.dt))
             gw.step_fixed()
             assert np.array_equal(gw.broadphase_pairs(), ow.pairs()), f"pair list differs at step {s}"
@@ -505,3 +509,38 @@ def test_cpp_facade_matches_python_api(kzg_lib):
     with World(scenes.pyramid(8)) as w:
         w.step_fixed(n=60)
         assert w.compute_state_hash() == cpp_hash
+
+
+def test_cpp_facade_body_operations_match_python_api_and_oracle(oracle_lib, kzg_lib):
+    """The facade's reference-named body operations (AddImpulseAtPoint, SetLinearVelocity, AddForce,
+    SetBodyRotation, SetBodyActive) halfway through the pyramid run, against the same edits through
+    the Python API and the oracle."""
+    import os
+    import subprocess
+    from kizuriphysics3d_gb300 import World, build, capi, make_edit, resolve, scenes
+    exe = os.path.join(build.OUT, "pyramid_example")
+    out = subprocess.run([exe, "8", "60", "1"], capture_output=True, text=True, check=True).stdout
+    cpp_hash = int(out.split("hash")[1].split()[0], 16)
+    cpp_active = int(out.split("active")[1].split()[0])
+    sc = scenes.pyramid(8)
+    res = resolve(sc)
+    ow = oracle_lib.OracleWorld(sc.to_bytes(), oracle_blob(sc, res), oracle_lib.PAIRS_CANONICAL)
+    with World(sc, resolved=res) as w:
+        for s in range(60):
+            if s == 30:
+                top = len(sc.bodies) - 1
+                t = w.state()[top]
+                e = np.concatenate([
+                    make_edit(capi.EDIT_ADD_IMPULSE_AT_POINT, top, (3.0, 0.0, 0.0, t[0], np.float32(t[1] + np.float32(0.5)),
+                                                                     np.float32(t[2] + np.float32(0.3)))),
+                    make_edit(capi.EDIT_SET_LINEAR_VELOCITY, 1, (0.0, 2.0, 0.0)),
+                    make_edit(capi.EDIT_ADD_FORCE, 1, (0.0, 150.0, 0.0)),
+                    make_edit(capi.EDIT_SET_ROTATION, 2, (0.0, 0.2, 0.0, 1.0)),
+                    make_edit(capi.EDIT_DEACTIVATE, 3, (), wake=False)])
+                w.edit_bodies(e)
+                ow.edit_bodies(e)
+            w.step_fixed()
+            ow.step(np.float32(sc.dt))
+        assert np.array_equal(bits(w.state()), bits(ow.state()))
+        assert w.compute_state_hash() == cpp_hash == ow.hash()
+        assert len(w.active_bodies()) == cpp_active

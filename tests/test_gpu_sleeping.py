@@ -5,7 +5,7 @@ C-ABI: state bits, the active list in its order, snapshots, SetBodyActive."""
 import numpy as np
 import pytest
 
-from conftest import bits, golden_resolved, load_golden, oracle_blob
+from conftest import apply_golden_edits, bits, golden_resolved, load_golden, oracle_blob
 from tests.golden.gen_golden import fixture_scenes
 
 pytestmark = pytest.mark.gpu
@@ -23,16 +23,20 @@ def _worlds(name, mode):
     return sc, g, res, ow, World(sc, resolved=res)
 
 
-@pytest.mark.parametrize("name", ["sleep_wake", "pile120_sleep"])
+@pytest.mark.parametrize("name", ["sleep_wake", "pile120_sleep", "edits_sleep", "edits_nosleep"])
 @pytest.mark.parametrize("mode", ["A", "B"])
 def test_active_list_and_state_follow_the_oracle(name, mode, oracle_lib, kzg_lib):
     """Every step: the same bodies asleep, the active list in the same order (the reference's
-    appends on waking and swap-removals on falling asleep), identical state bits."""
+    appends on waking and swap-removals on falling asleep), identical state bits.  The edit
+    fixtures add the reference's body operations between steps (SetBodyActive, Add*, Set*), one
+    of them with sleeping off: deactivated bodies there wait until a moving body touches them."""
     sc, g, res, ow, gw = _worlds(name, oracle_lib.PAIRS_TREE if mode == "A" else oracle_lib.PAIRS_CANONICAL)
     slept = woke = 0
     prev = None
     with gw:
         for s in range(FIXTURES[name][1]):
+            apply_golden_edits(ow, g, s)
+            apply_golden_edits(gw, g, s)
             ow.step(np.float32(sc.dt))
             if mode == "A":
                 gw.step_with_pairs(ow.pairs())
@@ -118,3 +122,29 @@ def test_world_loaded_from_a_reference_kzp1_file(oracle_lib, kzg_lib):
             gw.step_fixed()
             assert np.array_equal(bits(gw.state()), bits(ow.state())), f"state differs at step {s}"
             assert np.array_equal(gw.active_bodies(), ow.activity()[0]), f"active list differs at step {s}"
+
+
+@pytest.mark.parametrize("name", ["edits_sleep", "edits_nosleep"])
+def test_edit_fixtures_under_graph_replay(name, oracle_lib, kzg_lib):
+    """The edit fixtures stepped from a captured graph, many steps per call between the edits: a
+    deactivation switches the captured step to the active-list form and back once every body is
+    active again, with the same bits as the oracle stepping one step at a time."""
+    sc, g, res, ow, gw = _worlds(name, oracle_lib.PAIRS_CANONICAL)
+    steps = FIXTURES[name][1]
+    marks = sorted(set(int(s) for s in g["edits"]["step"])) + [steps]
+    with gw:
+        gw.set_graph(True)
+        at = 0
+        for m in marks:
+            if m > at:
+                gw.step_fixed(n=m - at)
+                for s in range(at, m):
+                    apply_golden_edits(ow, g, s)
+                    ow.step(np.float32(sc.dt))
+                at = m
+                assert np.array_equal(bits(gw.state()), bits(ow.state())), f"state differs after step {m - 1}"
+                lst, _, _ = ow.activity()
+                assert np.array_equal(gw.active_bodies(), lst)
+            if m < steps:
+                apply_golden_edits(gw, g, m)
+        assert gw.get_stats()["device_error"] == 0

@@ -3,7 +3,7 @@ reference engine itself produced (tests/golden/gen_golden.py).  CPU only."""
 import numpy as np
 import pytest
 
-from conftest import bits, golden_resolved, load_golden, oracle_blob
+from conftest import apply_golden_edits, bits, golden_resolved, load_golden, oracle_blob
 from tests.golden.gen_golden import fixture_scenes
 
 FIXTURES = fixture_scenes()
@@ -19,6 +19,7 @@ def test_oracle_matches_reference_every_step(name, oracle_lib):
     assert np.array_equal(bits(iw), bits(g["inv_inertia_world"]))
     k = 0
     for s in range(steps):
+        apply_golden_edits(w, g, s)  # body operations the reference run applied before this step
         w.step(np.float32(sc.dt))
         assert w.hash() == int(g["hashes"][s]), f"{name}: state hash differs at step {s}"
         st = w.stats()
