@@ -60,6 +60,10 @@ def make_workload(name: str):
         return scenes.stacks(20, 20, 500), 0, {
             "workload": "large box field, 400 stacks x 500 unit boxes, jitter seed 7, 8 velocity + 2 position "
                         "iterations, dt 1/60", "bodies": 200000}
+    if name == "stacks10k":  # a smaller box field of the same generator (profiling case)
+        return scenes.stacks(10, 10, 100), 0, {
+            "workload": "box field, 100 stacks x 100 unit boxes, jitter seed 7, 8 velocity + 2 position "
+                        "iterations, dt 1/60", "bodies": 10000}
     if name == "pyramid20":
         return scenes.pyramid(20), 0, {
             "workload": "20-row pyramid, 210 unit boxes, 10 velocity + 2 position iterations, dt 1/60", "bodies": 210}
@@ -524,7 +528,8 @@ def main():
         "pair_order": "canonical: every overlapping pair once, MakePairKey order (GPU broad phase)",
         "l2": "flushed between timed steps (256 MB write)",
         "parallelism": ("world ranges" if sharded else "replicas") if world_size > 1 else "single GPU",
-        "measured": {"contacts": points, "pairs": int(pairs.shape[0]), "islands": last["num_islands"],
+        "measured": {"contacts": points, "pairs": int(pairs.shape[0]), "epa_pairs": last.get("num_epa_pairs"),
+                     "islands": last["num_islands"],
                      "max_velocity_levels": last["max_velocity_levels"],
                      "max_bias_levels": last["max_bias_levels"]},
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": int(ft.nbytes),

@@ -181,6 +181,7 @@ typedef struct {
                            * island's last velocity iteration */
     uint32_t num_active_bodies; /* WorldStats::numActiveBodies: the active list's length */
     uint32_t cache_capacity;    /* manifold cache slots now (kzg_config.max_cache_entries, doubled as it fills) */
+    uint32_t num_epa_pairs;     /* pairs of the last step that needed EPA (overlapping convex pairs) */
 } kzg_stats;
 
 #define KZG_DEVERR_PAIRS 1u     /* pair buffer overflow */

@@ -75,7 +75,7 @@ class KzgStats(ctypes.Structure):
                                    "max_bias_levels", "cache_entries", "device_error", "kernel_launches",
                                    "max_velocity_iterations_used", "point_velocity_iterations")] + \
                [(n, f32) for n in ("broadphase_ms", "narrowphase_ms", "constraints_ms", "schedule_ms", "solve_ms",
-                                   "integrate_ms", "step_ms", "final_residual")] + [("num_active_bodies", u32), ("cache_capacity", u32)]
+                                   "integrate_ms", "step_ms", "final_residual")] + [("num_active_bodies", u32), ("cache_capacity", u32), ("num_epa_pairs", u32)]
 
 
 class KzgJointDesc(ctypes.Structure):

@@ -24,6 +24,13 @@ std::string g_create_error;
             return KZG_ERR_CUDA;                                         \
         }                                                                \
     } while (0)
+// The last step's sleeping island count is counted before the stats are read or anything it reads
+// changes (settle_sleep_count).
+#define SETTLE(c)                                        \
+    do {                                                 \
+        const kzg_status st_ = settle_sleep_count(*(c)); \
+        if (st_ != KZG_OK) return st_;                   \
+    } while (0)
 
 template <typename T>
 cudaError_t dalloc(T** p, size_t count) {
@@ -452,6 +459,7 @@ kzg_status kzg_upload_shapes(kzg_ctx* k, const kzg_shape_desc* shapes, uint32_t 
 kzg_status kzg_add_bodies(kzg_ctx* k, uint32_t n, const kzg_body_soa* b, uint32_t* first_slot) {
     if (check(k) || !b) return KZG_ERR_INVALID;
     Ctx* ctx = &k->c;
+    SETTLE(ctx);
     if (!ctx->shapes_uploaded) { ctx->err = "upload shapes before bodies"; return KZG_ERR_INVALID; }
     const uint32_t base = ctx->nbodies;
     if (base + n > ctx->cfg.max_bodies) { ctx->err = "kzg_config.max_bodies exceeded"; return KZG_ERR_CAPACITY; }
@@ -538,6 +546,7 @@ kzg_status kzg_add_bodies(kzg_ctx* k, uint32_t n, const kzg_body_soa* b, uint32_
 kzg_status kzg_add_joints(kzg_ctx* k, uint32_t n, const kzg_joint_desc* j, uint32_t* first_index) {
     if (check(k) || (!j && n)) return KZG_ERR_INVALID;
     Ctx* ctx = &k->c;
+    SETTLE(ctx);
     if (ctx->njoints + n > ctx->cfg.max_joints) { ctx->err = "kzg_config.max_joints exceeded"; return KZG_ERR_CAPACITY; }
     if (ctx->njoints + n > ctx->cfg.max_pairs) { ctx->err = "more joints than kzg_config.max_pairs"; return KZG_ERR_CAPACITY; }
     for (uint32_t i = 0; i < n; ++i) {
@@ -644,6 +653,7 @@ kzg_status kzg_autotune(kzg_ctx* k, float dt, uint32_t steps_per_candidate, kzg_
     if (check(k) || !(dt > 0.0f) || steps_per_candidate == 0) return KZG_ERR_INVALID;
     Ctx* ctx = &k->c;
     CK(cudaSetDevice(ctx->device));
+    SETTLE(ctx);
     kzg_status s = finalize_bodies(k);
     if (s != KZG_OK) return s;
     const kzg_tuning before = ctx->tune;
@@ -821,6 +831,7 @@ kzg_status kzg_set_bodies_active(kzg_ctx* k, const uint32_t* packed_ids, uint32_
     Ctx* ctx = &k->c;
     if (n == 0) return KZG_OK;
     CK(cudaSetDevice(ctx->device));
+    SETTLE(ctx);
     if (n > ctx->cfg.max_pairs) { ctx->err = "more ids than kzg_config.max_pairs per call"; return KZG_ERR_CAPACITY; }
     CK(cudaMemcpyAsync(ctx->pair_keys, packed_ids, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
     CK(set_bodies_active(*ctx, reinterpret_cast<const uint32_t*>(ctx->pair_keys), n, active));
@@ -841,6 +852,7 @@ kzg_status kzg_edit_bodies(kzg_ctx* k, const kzg_body_edit* edits, uint32_t n) {
         }
     if (n == 0) return KZG_OK;
     CK(cudaSetDevice(ctx->device));
+    SETTLE(ctx);
     kzg_status s = finalize_bodies(k);
     if (s != KZG_OK) return s;
     kzg_body_edit* dev = nullptr;
@@ -881,7 +893,12 @@ kzg_status kzg_state_hash(kzg_ctx* k, uint64_t* out) {
 
 kzg_status kzg_get_stats(kzg_ctx* k, kzg_stats* out) {
     if (check(k) || !out) return KZG_ERR_INVALID;
-    *out = k->c.stats;
+    Ctx* ctx = &k->c;
+    if (ctx->sleep_count_pending) {
+        CK(cudaSetDevice(ctx->device));
+        SETTLE(ctx);
+    }
+    *out = ctx->stats;
     out->cache_capacity = k->c.cache_cap;  // the table as it is now (it may have grown since)
     return KZG_OK;
 }
@@ -1045,6 +1062,7 @@ kzg_status kzg_snapshot_load(kzg_ctx* k, const void* in, size_t size) {
     if (check(k) || !in || size < sizeof(SnapHeader)) return KZG_ERR_INVALID;
     Ctx* ctx = &k->c;
     CK(cudaSetDevice(ctx->device));
+    SETTLE(ctx);
     kzg_status st = finalize_bodies(k);
     if (st != KZG_OK) return st;
     SnapHeader h;

@@ -211,6 +211,7 @@ struct Ctx {
     float4* c_imp = nullptr;
     uint32_t cache_cap = 0;
     bool all_active = true;  // every body in the active list (false once a call may have deactivated one)
+    bool sleep_count_pending = false;  // the last step's UpdateSleeping island count is still to be counted
     bool cache_fixed = false;  // the tuner holds a copy of the table: no growth while it runs
 
     // misc

@@ -27,6 +27,9 @@ size_t joint_record_bytes();
 // Manifold cache table: room for `entries` at below 0.7 load (doubling, entries rehashed), and a
 // table of exactly `cap` slots with every entry cleared (snapshot loads).
 kzg_status cache_reserve(Ctx& ctx, uint64_t entries);
+// The last step's WorldStats::numIslands with sleeping on, counted as the reference does; call
+// before reading the stats and before anything changes the active list, the bodies or the joints.
+kzg_status settle_sleep_count(Ctx& ctx);
 kzg_status cache_reset(Ctx& ctx, uint32_t cap);
 // Entries (slot, key, point count, 4 positions, 4 impulses) written into their slots.
 kzg_status cache_scatter(Ctx& ctx, const uint32_t* slots, const unsigned long long* keys, const uint32_t* np,

@@ -894,6 +894,68 @@ __global__ void k_sleep_union_joints(const DeviceBodies b, const Counters* cnt, 
     const uint32_t n = cnt->nsleep_n, ia = b.isl_idx[a], ib = b.isl_idx[bb];
     if (ia < n && ib < n) uf_link(suf, ia, ib);
 }
+// WorldStats::numIslands as UpdateSleeping leaves it (PhysicsWorld.cpp:893-949).  The count reads
+// the active list's buffer after the removals position by position and counts the positions that
+// are their set's root, so it depends on which position the reference's union-by-rank
+// (PhysicsWorld.cpp:38-57; contacts, then joints, in order) makes each root.  One thread replays
+// those unions; parent and rank live in shared memory when they fit, else in global scratch.
+// Run on demand (kzg_get_stats), on the buffers the last step left.
+constexpr uint32_t kSleepCountSmem = 40000;  // positions held in shared memory (5 bytes each)
+__global__ void __launch_bounds__(256) k_sleep_count_ref(const DeviceBodies b, Counters* cnt, const uint32_t* __restrict__ alist,
+                                                        const uint32_t* __restrict__ con_a, const uint32_t* __restrict__ con_b,
+                                                        const uint32_t* __restrict__ con_bits, const JointDev* __restrict__ J,
+                                                        uint32_t nj, uint32_t* gpar, uint8_t* grank) {
+    extern __shared__ uint32_t sm_uf[];
+    __shared__ uint32_t count;
+    const uint32_t n = cnt->nsleep_n;
+    const bool shared = n <= kSleepCountSmem;
+    uint32_t* par = shared ? sm_uf : gpar;
+    uint8_t* rk = shared ? reinterpret_cast<uint8_t*>(sm_uf + kSleepCountSmem) : grank;
+    for (uint32_t p = threadIdx.x; p < n; p += blockDim.x) {
+        par[p] = p;
+        rk[p] = 0;
+    }
+    if (threadIdx.x == 0) count = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        auto find = [&](uint32_t x) {
+            while (par[x] != x) {
+                par[x] = par[par[x]];
+                x = par[x];
+            }
+            return x;
+        };
+        auto unite = [&](uint32_t a, uint32_t c) {
+            a = find(a);
+            c = find(c);
+            if (a == c) return;
+            if (rk[a] < rk[c]) { const uint32_t t = a; a = c; c = t; }
+            par[c] = a;
+            if (rk[a] == rk[c]) ++rk[a];
+        };
+        const uint32_t nc = cnt->ncons;
+        for (uint32_t k = 0; k < nc; ++k) {
+            if ((con_bits[k] & 6u) != 6u) continue;
+            const uint32_t ia = b.isl_idx[con_a[k]], ib = b.isl_idx[con_b[k]];
+            if (ia < n && ib < n) unite(ia, ib);
+        }
+        for (uint32_t k = 0; k < nj; ++k) {
+            if (J[k].flags & kJointDisabled) continue;
+            const uint32_t a = J[k].a, c = J[k].b;
+            if (b.motion[a] != KZG_MOTION_DYNAMIC || b.motion[c] != KZG_MOTION_DYNAMIC) continue;
+            const uint32_t ia = b.isl_idx[a], ib = b.isl_idx[c];
+            if (ia < n && ib < n) unite(ia, ib);
+        }
+    }
+    __syncthreads();
+    uint32_t mine = 0;
+    for (uint32_t p = threadIdx.x; p < n; p += blockDim.x)
+        mine += (b.motion[alist[p]] == KZG_MOTION_DYNAMIC && par[p] == p) ? 1u : 0u;
+    atomicAdd(&count, mine);
+    __syncthreads();
+    if (threadIdx.x == 0) cnt->sleep_islands = count;
+}
+
 cudaError_t create_joints(Ctx& ctx, uint32_t first, uint32_t n) {
     k_joint_create<<<blocks_for(n), kThreads, 0, ctx.stream>>>(ctx.b, ctx.joints, ctx.joint_stage, first, n);
     cudaError_t e = cudaGetLastError();
@@ -1308,6 +1370,20 @@ void swap_in(Ctx& ctx, CacheTable& t, uint32_t cap) {
 constexpr uint32_t kMaxCacheCap = 1u << 31;
 }  // namespace
 
+kzg_status settle_sleep_count(Ctx& ctx) {
+    if (!ctx.sleep_count_pending) return KZG_OK;
+    ctx.sleep_count_pending = false;
+    k_sleep_count_ref<<<1, 256, kSleepCountSmem * (sizeof(uint32_t) + 1), ctx.stream>>>(
+        ctx.b, ctx.dcnt, ctx.alist, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.joints, ctx.njoints, ctx.suf,
+        reinterpret_cast<uint8_t*>(ctx.smin));
+    KZG_CK(cudaGetLastError());
+    KZG_CK(cudaMemcpyAsync(&ctx.hcnt->sleep_islands, &ctx.dcnt->sleep_islands, sizeof(uint32_t),
+                           cudaMemcpyDeviceToHost, ctx.stream));
+    KZG_CK(cudaStreamSynchronize(ctx.stream));
+    ctx.stats.num_islands = ctx.hcnt->sleep_islands;
+    return KZG_OK;
+}
+
 kzg_status cache_reserve(Ctx& ctx, uint64_t entries) {
     uint64_t cap = ctx.cache_cap;
     while (entries * 10u >= cap * 7u && cap < kMaxCacheCap) cap *= 2u;
@@ -1423,6 +1499,9 @@ static bool g_cluster_ok = false;
 cudaError_t configure_kernels() {
     cudaError_t e = cudaFuncSetAttribute(k_solve_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(2 * kCtaBodiesMax * sizeof(float4)));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_sleep_count_ref, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(kSleepCountSmem * (sizeof(uint32_t) + 1)));
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_narrow_epa, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(kEpaWarps * sizeof(EpaWarpSmem)));
@@ -1672,9 +1751,12 @@ static kzg_status finish_stats(Ctx& ctx, uint32_t graph_steps = 0) {
     s.num_contact_constraints = h.ncons;
     s.num_contact_points = h.npoints;
     // WorldStats::numIslands: BuildIslands' count, replaced by UpdateSleeping's when that pass ran
+    // (the exact one is counted on demand, settle_sleep_count)
     s.num_islands = (ctx.ws.allow_sleeping && h.nsleep_n) ? h.sleep_islands : h.nroots;
+    ctx.sleep_count_pending = ctx.ws.allow_sleeping && h.nsleep_n;
     s.num_active_bodies = h.nact;
     s.cache_capacity = ctx.cache_cap;
+    s.num_epa_pairs = h.nepa;
     s.num_batches = h.batches;
     s.max_velocity_levels = h.max_vlev;
     s.max_bias_levels = h.max_blev;
