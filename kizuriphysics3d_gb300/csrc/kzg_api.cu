@@ -71,6 +71,8 @@ kzg_status alloc_all(Ctx* ctx) {
     CK(dalloc(&ctx->m_data, 12 * P));
     CK(dalloc(&ctx->m_key, P));
     CK(dalloc(&ctx->epa_list, P));
+    ctx->epa_gjk_cap = (uint32_t)std::min<size_t>(P, size_t(1) << 20);
+    CK(cudaMalloc(&ctx->epa_gjk, gjk_record_bytes() * std::max<size_t>(ctx->epa_gjk_cap, 1)));
     CK(dalloc(&ctx->ccd_disp, B));
     CK(dalloc(&ctx->ccd_list, B));
     CK(dalloc(&ctx->ccd_state, B));
@@ -165,7 +167,7 @@ void free_all(Ctx* ctx) {
                     b.iiw, b.iil, b.inv_mass, b.shape, b.motion, b.flags, b.layer, b.mask, b.world, b.packed, b.fat_mn, b.fat_mx,
                     ctx->is_large, ctx->large_list, ctx->large_off, ctx->cell_keys, ctx->cell_keys_sorted,
                     ctx->cell_vals, ctx->cell_vals_sorted, ctx->pair_keys, ctx->pair_keys_sorted, ctx->pairs,
-                    ctx->m_count, ctx->m_data, ctx->m_key, ctx->epa_list, ctx->ccd_disp, ctx->ccd_list, ctx->ccd_state, ctx->ccd_deps, ctx->ccd_ndeps, ctx->joints, ctx->joint_stage, ctx->jkeys,
+                    ctx->m_count, ctx->m_data, ctx->m_key, ctx->epa_list, ctx->epa_gjk, ctx->ccd_disp, ctx->ccd_list, ctx->ccd_state, ctx->ccd_deps, ctx->ccd_ndeps, ctx->joints, ctx->joint_stage, ctx->jkeys,
                     ctx->jkeys_sorted, ctx->jisl, ctx->jisl_cisl, ctx->jflag, ctx->con_flag, ctx->con_index, ctx->con_pair, ctx->con_a,
                     ctx->con_b, ctx->con_np, ctx->con_bits, ctx->con_fr, ctx->con_key, ctx->r.pA, ctx->r.pB, ctx->r.n,
                     ctx->r.t1, ctx->r.t2, ctx->r.rA, ctx->r.rB, ctx->r.rAr, ctx->r.rBr, ctx->r.laA, ctx->r.laB,

@@ -142,6 +142,8 @@ struct Ctx {
     float4* m_data = nullptr;  // 12 float4 per pair
     unsigned long long* m_key = nullptr;
     uint32_t* epa_list = nullptr;  // pairs whose narrow phase needs EPA (warp pass)
+    void* epa_gjk = nullptr;       // their GJK results from the thread pass (epa_gjk_cap records)
+    uint32_t epa_gjk_cap = 0;
     float4* ccd_disp = nullptr;    // continuous collision: each LinearCast body's step displacement
     uint32_t* ccd_list = nullptr;  // slots of the LinearCast bodies, ascending
     uint32_t* ccd_state = nullptr; // per body slot: CCD round that finished it (LinearCast bodies)

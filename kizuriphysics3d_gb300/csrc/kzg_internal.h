@@ -24,6 +24,7 @@ cudaError_t set_bodies_active(Ctx& ctx, const uint32_t* dev_ids, uint32_t n, int
 cudaError_t edit_bodies(Ctx& ctx, const kzg_body_edit* dev_edits, uint32_t n);  // in order
 cudaError_t create_joints(Ctx& ctx, uint32_t first, uint32_t n);     // joint records from ctx.joint_stage
 size_t joint_record_bytes();
+size_t gjk_record_bytes();  // one kept GJK result of a pair deferred to the EPA pass
 // Manifold cache table: room for `entries` at below 0.7 load (doubling, entries rehashed), and a
 // table of exactly `cap` slots with every entry cleared (snapshot loads).
 kzg_status cache_reserve(Ctx& ctx, uint64_t entries);

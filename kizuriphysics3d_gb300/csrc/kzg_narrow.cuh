@@ -375,6 +375,7 @@ __device__ inline bool epa_initial_tetra(const SupportMap& map, const GjkOut& g,
     return false;
 }
 
+
 __device__ inline void epa_finish(const EpaFace& f, const SP* vs, EpaOut& r) {
     Vec3 proj = f.n * f.dist;
     Vec3 a = vs[f.a].p, b = vs[f.b].p, c = vs[f.c].p;
@@ -408,6 +409,139 @@ struct EpaWarpSmem {
 };
 
 __device__ __forceinline__ Vec3 sm_vp(const EpaWarpSmem& S, uint32_t i) { return Vec3(S.vp[i][0], S.vp[i][1], S.vp[i][2]); }
+
+// BuildInitialTetra (EPA.cpp:58-147) for the warp EPA, every lane holding the same result.  The
+// simplex-based attempts run on every lane; the fallback - the first tetrahedron, in the order of
+// the reference's four nested loops, of up to 16 distinct candidate points (the simplex and 14
+// support points) that has volume and holds the origin - is searched 32 combinations at a time,
+// each lane testing one (its indices from the combination's rank in that order) and the smallest
+// rank that passes winning.  On touching polyhedra (a box resting on a box) the simplex is
+// degenerate and this search, up to 1,820 tetrahedra, is most of the pair's work.
+struct TetraSmem {
+    float p[18][3], pa[18][3], pb[18][3];  // the 14 support points, then the candidate list
+    float cp[16][3], cpa[16][3], cpb[16][3];
+};
+static_assert(sizeof(TetraSmem) <= sizeof(EpaWarpSmem), "tetrahedron scratch overlays the EPA scratch");
+
+__device__ __forceinline__ uint32_t choose3(uint32_t m) { return m < 3u ? 0u : m * (m - 1u) * (m - 2u) / 6u; }
+__device__ __forceinline__ uint32_t choose2(uint32_t m) { return m < 2u ? 0u : m * (m - 1u) / 2u; }
+
+static __device__ __noinline__ bool epa_initial_tetra_warp(const SupportMap& map, const GjkOut& g, SP* out,
+                                                          EpaWarpSmem& scratch, uint32_t lane) {
+    uint32_t n = 0;
+    for (uint32_t i = 0; i < g.ns && n < 4; ++i) {
+        bool dup = false;
+        for (uint32_t j = 0; j < n; ++j)
+            if ((out[j].p - g.simplex[i].p).len2() < 1.0e-12f) dup = true;
+        if (!dup) out[n++] = g.simplex[i];
+    }
+    if (n == 0) out[n++] = map(Vec3(1.0f, 0.0f, 0.0f));
+    if (n == 4 && !origin_in_tetra(out)) n = 3;
+    if (n == 1) {
+        out[n] = map(-out[0].p);
+        if ((out[1].p - out[0].p).len2() > 1.0e-12f) ++n;
+    }
+    if (n == 2) {
+        Vec3 ab = out[1].p - out[0].p;
+        if (ab.len2() > 1.0e-12f) {
+            Vec3 d1 = epa_perp(ab).normalized();
+            Vec3 d2 = ab.cross(d1).normalized();
+            SP k0 = out[0], k1 = out[1];
+            out[0] = map(d1);
+            out[1] = map(-d1);
+            out[2] = map(d2);
+            out[3] = map(-d2);
+            if (origin_in_tetra(out)) return true;
+            out[0] = k0;
+            out[1] = k1;
+        }
+        SP s = map(epa_perp(ab));
+        if ((s.p - out[0].p).len2() > 1.0e-12f && (s.p - out[1].p).len2() > 1.0e-12f) out[n++] = s;
+    }
+    if (n == 3) {
+        Vec3 tn = (out[1].p - out[0].p).cross(out[2].p - out[0].p);
+        float len = tn.len();
+        if (len > 1.0e-12f) {
+            tn = tn / len;
+            float sd = tn.dot(Vec3() - out[0].p);
+            SP a = map(sd > 0.0f ? -tn : tn);
+            SP b = map(sd > 0.0f ? tn : -tn);
+            out[3] = a;
+            if (!origin_in_tetra(out)) out[3] = b;
+            if (origin_in_tetra(out)) return true;
+        }
+        n = 3;
+    }
+    if (n == 4 && origin_in_tetra(out)) return true;
+
+    TetraSmem& X = *reinterpret_cast<TetraSmem*>(&scratch);
+    const float s = 0.5773502692f;
+    const float D[14][3] = {{1, 0, 0},   {-1, 0, 0},  {0, 1, 0},  {0, -1, 0}, {0, 0, 1},  {0, 0, -1}, {s, s, s},
+                            {s, s, -s},  {s, -s, s},  {-s, s, s}, {-s, -s, s}, {-s, s, -s}, {s, -s, -s}, {-s, -s, -s}};
+    __syncwarp();
+    if (lane < 14u) {
+        const SP sp = map(Vec3(D[lane][0], D[lane][1], D[lane][2]));
+        X.p[lane][0] = sp.p.x; X.p[lane][1] = sp.p.y; X.p[lane][2] = sp.p.z;
+        X.pa[lane][0] = sp.pA.x; X.pa[lane][1] = sp.pA.y; X.pa[lane][2] = sp.pA.z;
+        X.pb[lane][0] = sp.pB.x; X.pb[lane][1] = sp.pB.y; X.pb[lane][2] = sp.pB.z;
+    }
+    __syncwarp();
+    uint32_t nc = 0;
+    if (lane == 0) {  // the candidate list in the reference's order, duplicates dropped
+        auto add = [&](const Vec3& p, const Vec3& pa, const Vec3& pb) {
+            for (uint32_t i = 0; i < nc; ++i)
+                if ((Vec3(X.cp[i][0], X.cp[i][1], X.cp[i][2]) - p).len2() < 1.0e-12f) return;
+            if (nc < 16) {
+                X.cp[nc][0] = p.x; X.cp[nc][1] = p.y; X.cp[nc][2] = p.z;
+                X.cpa[nc][0] = pa.x; X.cpa[nc][1] = pa.y; X.cpa[nc][2] = pa.z;
+                X.cpb[nc][0] = pb.x; X.cpb[nc][1] = pb.y; X.cpb[nc][2] = pb.z;
+                ++nc;
+            }
+        };
+        for (uint32_t i = 0; i < g.ns && i < 4; ++i) add(g.simplex[i].p, g.simplex[i].pA, g.simplex[i].pB);
+        for (uint32_t i = 0; i < 14; ++i)
+            add(Vec3(X.p[i][0], X.p[i][1], X.p[i][2]), Vec3(X.pa[i][0], X.pa[i][1], X.pa[i][2]),
+                Vec3(X.pb[i][0], X.pb[i][1], X.pb[i][2]));
+    }
+    nc = __shfl_sync(0xffffffffu, nc, 0);
+    __syncwarp();
+    auto cand = [&](uint32_t i) {
+        SP r;
+        r.p = Vec3(X.cp[i][0], X.cp[i][1], X.cp[i][2]);
+        r.pA = Vec3(X.cpa[i][0], X.cpa[i][1], X.cpa[i][2]);
+        r.pB = Vec3(X.cpb[i][0], X.cpb[i][1], X.cpb[i][2]);
+        return r;
+    };
+    const uint32_t total = nc >= 4u ? nc * (nc - 1u) * (nc - 2u) * (nc - 3u) / 24u : 0u;
+    for (uint32_t base = 0; base < total; base += 32u) {
+        const uint32_t rank = base + lane;
+        uint32_t i = 0, j = 0, k = 0, l = 0;
+        bool ok = false;
+        if (rank < total) {  // the rank-th (i < j < k < l) in the loops' order
+            uint32_t r = rank;
+            for (;; ++i) { const uint32_t c = choose3(nc - 1u - i); if (r < c) break; r -= c; }
+            for (j = i + 1u;; ++j) { const uint32_t c = choose2(nc - 1u - j); if (r < c) break; r -= c; }
+            for (k = j + 1u;; ++k) { const uint32_t c = nc - 1u - k; if (r < c) break; r -= c; }
+            l = k + 1u + r;
+            SP t[4] = {cand(i), cand(j), cand(k), cand(l)};
+            float vol = (t[1].p - t[0].p).cross(t[2].p - t[0].p).dot(t[3].p - t[0].p);
+            ok = !(rabs(vol) < 1.0e-12f) && origin_in_tetra(t);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, ok);
+        if (m) {
+            const uint32_t w = (uint32_t)(__ffs(m) - 1);
+            const uint32_t idx = __shfl_sync(0xffffffffu, i | (j << 8) | (k << 16) | (l << 24), w);
+            out[0] = cand(idx & 0xFFu);
+            out[1] = cand((idx >> 8) & 0xFFu);
+            out[2] = cand((idx >> 16) & 0xFFu);
+            out[3] = cand(idx >> 24);
+            __syncwarp();
+            return true;
+        }
+    }
+    __syncwarp();
+    return false;
+}
 
 // BuildFace (EPA.cpp:16-31) on vertices held in shared memory.
 __device__ __forceinline__ bool epa_build_face_sm(uint32_t& fa, uint32_t& fb, uint32_t& fc, Vec3& n_out, float& d_out,
@@ -490,7 +624,7 @@ static __device__ __noinline__ void epa_warp(const SupportMap& map, const GjkOut
     r.normal = Vec3(0.0f, 1.0f, 0.0f);
     r.pA = r.pB = Vec3();
     SP tet[4];
-    if (!epa_initial_tetra(map, g, tet)) return;  // identical on every lane
+    if (!epa_initial_tetra_warp(map, g, tet, S, lane)) return;  // identical on every lane
     if (lane < 4) {
         const SP& t = tet[lane];
         S.vp[lane][0] = t.p.x; S.vp[lane][1] = t.p.y; S.vp[lane][2] = t.p.z;
@@ -627,23 +761,47 @@ static __device__ __noinline__ void epa_warp(const SupportMap& map, const GjkOut
 // How the pair routines obtain EPA results: the thread-per-pair pass defers pairs that need EPA
 // to a worklist; the warp-per-pair pass runs them cooperatively.
 struct EpaDefer {
+    static constexpr bool kWarp = false;
+    uint32_t* nepa;     // worklist length
+    uint32_t* list;     // worklist of pair indices
+    GjkOut* kept;       // per worklist slot: the GJK result the EPA starts from (first `cap` slots)
+    uint32_t cap;
+    uint32_t pair;
     bool deferred = false;
     __device__ bool solo() const { return true; }
-    __device__ void operator()(const SupportMap&, const GjkOut&, float, uint32_t, EpaOut& e) {
+    __device__ void operator()(const SupportMap&, const GjkOut& g, float, uint32_t, EpaOut& e) {
+        const uint32_t slot = atomicAdd(nepa, 1u);
+        list[slot] = pair;
+        if (slot < cap) kept[slot] = g;
         deferred = true;
         e.valid = false;
     }
 };
 struct EpaCoop {
+    static constexpr bool kWarp = true;
     EpaWarpSmem* S;
     uint32_t lane;
     uint32_t* err;
+    const GjkOut* pre;  // the thread pass's GJK result for this pair (same inputs, same result), or null
     bool deferred = false;
     __device__ bool solo() const { return lane == 0; }  // the lane that stores the manifold
     __device__ void operator()(const SupportMap& m, const GjkOut& g, float tol, uint32_t it, EpaOut& e) {
         epa_warp(m, g, tol, it, *S, e, lane, err);
     }
 };
+
+// GJK of a pair: in the warp pass the thread pass's result when it was kept (the same call on the
+// same inputs), else computed.
+template <typename Epa>
+__device__ __forceinline__ void run_gjk(const SupportMap& map, float tol, GjkOut& g, const Epa& epa) {
+    if constexpr (Epa::kWarp) {
+        if (epa.pre) {
+            g = *epa.pre;
+            return;
+        }
+    }
+    gjk(map, tol, 32, g);
+}
 
 // ---------------------------------------------------------------------------------------------
 // Face clipping (CollideShape.cpp:30-228)
@@ -783,6 +941,185 @@ static __device__ __noinline__ uint32_t collide_polyhedral(const ShapeTables& T,
     return nc;
 }
 
+// ---- the same face clipping on one warp, for the EPA pass (every lane calls it; the result is on
+// every lane).  The float operations are the ones above, vertex by vertex; what is spread over the
+// lanes is the independent work: a hull's face normals (first largest wins, as in the loop), each
+// clip pass (one input vertex per lane; its kept vertex and crossing written at its place in the
+// sequential output order, found by a warp scan, past the 32-vertex cap dropped as add() drops them)
+// and the candidate filter (the first eight kept, in order).  Polygons live in the warp's EPA
+// scratch, free once the EPA result is taken.
+struct ClipWarpSmem {
+    float fa[kMaxFaceVerts][3], fb[kMaxFaceVerts][3];
+    float p0[kMaxFaceVerts * 2][3], p1[kMaxFaceVerts * 2][3];
+    ContactPt cand[8];
+};
+static_assert(sizeof(ClipWarpSmem) <= sizeof(EpaWarpSmem), "clip scratch overlays the EPA scratch");
+
+__device__ __forceinline__ Vec3 ld3(const float (*a)[3], uint32_t i) { return Vec3(a[i][0], a[i][1], a[i][2]); }
+__device__ __forceinline__ void st3(float (*a)[3], uint32_t i, const Vec3& v) { a[i][0] = v.x; a[i][1] = v.y; a[i][2] = v.z; }
+
+__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, uint32_t lane, uint32_t* total) {
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    *total = __shfl_sync(0xffffffffu, x, 31);
+    return x - v;
+}
+
+// shape_face with the hull's face search spread over the lanes; the face's vertices go to `out`.
+static __device__ bool shape_face_warp(const ShapeTables& T, const Body& b, const Vec3& wdir, float (*out)[3], uint32_t& cnt,
+                                Vec3& nworld, uint32_t lane) {
+    const ShapeDev* s = b.s;
+    if (s->type == kBox) {
+        Vec3 ld = b.q.inv_rotate(wdir);
+        int axis = ld.abs().max_comp_index();
+        float sg = ld[axis] >= 0.0f ? 1.0f : -1.0f;
+        Vec3 he(s->p[0], s->p[1], s->p[2]);
+        Vec3 n;
+        n.set(axis, sg);
+        Vec3 c(he.x * n.x, he.y * n.y, he.z * n.z);
+        int a0 = (axis + 1) % 3, a1 = (axis + 2) % 3;
+        float s0 = he[a0], s1 = he[a1];
+        if (lane < 4) {
+            Vec3 cr = c;
+            cr.set(a0, (lane == 0 || lane == 3) ? s0 : -s0);
+            cr.set(a1, lane < 2 ? s1 : -s1);
+            st3(out, lane, xform(b.q, b.t, cr));
+        }
+        cnt = 4;
+        nworld = b.q.rotate(n);
+        return true;
+    }
+    if (s->type == kHull) {
+        const Vec3 ld = b.q.inv_rotate(wdir);
+        float bd = -INFINITY;
+        uint32_t bf = 0xFFFFFFFFu, boff = 0, off = s->ifirst;
+        for (uint32_t base = 0; base < s->fnum; base += 32) {
+            const uint32_t fi = base + lane;
+            const uint32_t n = fi < s->fnum ? T.face_sizes[s->ffirst + fi] : 0u;
+            uint32_t tot;
+            const uint32_t o = off + warp_excl_scan(n, lane, &tot);
+            float d = -INFINITY;
+            if (fi < s->fnum) {
+                Vec3 a = hv(T, s->vfirst + T.face_idx[o]), bb = hv(T, s->vfirst + T.face_idx[o + 1]),
+                     c = hv(T, s->vfirst + T.face_idx[o + 2]);
+                Vec3 fn = (bb - a).cross(c - a).normalized_or(Vec3(0.0f, 1.0f, 0.0f));
+                d = fn.dot(ld);
+            }
+            float md = (d > -INFINITY) ? d : -INFINITY;  // a NaN never wins, as `d > bd` never holds for it
+            uint32_t mf = (d > -INFINITY) ? fi : 0xFFFFFFFFu, mo = o;
+#pragma unroll
+            for (int k = 16; k > 0; k >>= 1) {
+                const float od = __shfl_xor_sync(0xffffffffu, md, k);
+                const uint32_t of = __shfl_xor_sync(0xffffffffu, mf, k), oo = __shfl_xor_sync(0xffffffffu, mo, k);
+                if (of != 0xFFFFFFFFu && (mf == 0xFFFFFFFFu || od > md || (od == md && of < mf))) { md = od; mf = of; mo = oo; }
+            }
+            if (mf != 0xFFFFFFFFu && md > bd) { bd = md; bf = mf; boff = mo; }  // earlier chunks win ties
+            off += tot;
+        }
+        if (bf == 0xFFFFFFFFu) return false;
+        uint32_t n = T.face_sizes[s->ffirst + bf];
+        if (n > kMaxFaceVerts) n = kMaxFaceVerts;
+        if (lane < n) st3(out, lane, xform(b.q, b.t, hv(T, s->vfirst + T.face_idx[boff + lane])));
+        cnt = n;
+        Vec3 a = hv(T, s->vfirst + T.face_idx[boff]), bb = hv(T, s->vfirst + T.face_idx[boff + 1]),
+             c = hv(T, s->vfirst + T.face_idx[boff + 2]);
+        nworld = b.q.rotate((bb - a).cross(c - a).normalized_or(Vec3(0.0f, 1.0f, 0.0f)));
+        return true;
+    }
+    return false;
+}
+
+static __device__ __noinline__ uint32_t collide_polyhedral_warp(const ShapeTables& T, const Body& A, const Body& B, float max_sep,
+                                            Manifold& m, const Vec3& normal, EpaWarpSmem& scratch, uint32_t lane) {
+    __syncwarp();  // the EPA result has been read from the scratch by every lane
+    ClipWarpSmem& C = *reinterpret_cast<ClipWarpSmem*>(&scratch);
+    Vec3 na, nb;
+    uint32_t ca = 0, cb = 0;
+    const bool ha = shape_face_warp(T, A, -normal, C.fa, ca, na, lane);
+    const bool hb = shape_face_warp(T, B, normal, C.fb, cb, nb, lane);
+    __syncwarp();
+    if (!ha || !hb) return 0;
+    float ala = na.dot(-normal), alb = nb.dot(normal);
+    const bool ref_a = ala >= alb;
+    const float (*rv)[3] = ref_a ? C.fa : C.fb;
+    const float (*iv)[3] = ref_a ? C.fb : C.fa;
+    const uint32_t rc = ref_a ? ca : cb, ic = ref_a ? cb : ca;
+    const Vec3 rn = ref_a ? na : nb;
+    const float rd = rn.dot(ld3(rv, 0));
+    float (*src)[3] = C.p0;
+    float (*dst)[3] = C.p1;
+    if (lane < ic) st3(src, lane, ld3(iv, lane));
+    uint32_t count = ic;
+    Vec3 cen;
+    for (uint32_t i = 0; i < rc; ++i) cen = cen + ld3(rv, i);
+    cen = cen / (float)rc;
+    __syncwarp();
+    for (uint32_t i = 0; i < rc; ++i) {
+        const Vec3 v0 = ld3(rv, i), v1 = ld3(rv, i + 1 == rc ? 0 : i + 1);
+        Vec3 sn = (v1 - v0).cross(rn);
+        const float len = sn.len();
+        if (len < 1.0e-9f) continue;
+        sn = sn / len;
+        if (sn.dot(v0 - cen) < 0.0f) sn = -sn;
+        const float sd = sn.dot(v0);
+        bool keep = false, cross = false;
+        Vec3 cur, ip;
+        if (lane < count) {
+            cur = ld3(src, lane);
+            const Vec3 nxt = ld3(src, lane + 1 == count ? 0 : lane + 1);
+            const float dc = sn.dot(cur) - sd, dn = sn.dot(nxt) - sd;
+            keep = dc <= 0.0f;
+            cross = (dc <= 0.0f) != (dn <= 0.0f);
+            if (cross) ip = lerp(cur, nxt, rdiv(dc, dc - dn));
+        }
+        uint32_t tot;
+        const uint32_t pos = warp_excl_scan((keep ? 1u : 0u) + (cross ? 1u : 0u), lane, &tot);
+        if (keep && pos < kMaxFaceVerts * 2) st3(dst, pos, cur);
+        if (cross && pos + (keep ? 1u : 0u) < kMaxFaceVerts * 2) st3(dst, pos + (keep ? 1u : 0u), ip);
+        count = min(tot, kMaxFaceVerts * 2);
+        __syncwarp();
+        float (*t)[3] = src;
+        src = dst;
+        dst = t;
+        if (count == 0) break;
+    }
+    // the first eight vertices within max_sep of the reference face, in order
+    bool keep = false;
+    Vec3 p;
+    float sep = 0.0f;
+    if (lane < count) {
+        p = ld3(src, lane);
+        sep = rn.dot(p) - rd;
+        keep = !(sep > max_sep);
+    }
+    uint32_t nkeep;
+    const uint32_t pos = warp_excl_scan(keep ? 1u : 0u, lane, &nkeep);
+    if (keep && pos < 8u) {
+        const Vec3 proj = p - rn * sep;
+        ContactPt& c = C.cand[pos];
+        c.pA = ref_a ? proj : p;
+        c.pB = ref_a ? p : proj;
+        c.n = normal;
+        c.sep = sep;
+        c.feature = lane;
+    }
+    __syncwarp();
+    uint32_t nc = min(nkeep, 8u);
+    if (nc > 4) {
+        for (uint32_t i = 0; i < 4; ++i) m.pts[i] = C.cand[i * (nc - 1) / 3];
+        nc = 4;
+    } else {
+        for (uint32_t i = 0; i < nc; ++i) m.pts[i] = C.cand[i];
+    }
+    m.n = nc;
+    __syncwarp();
+    return nc;
+}
+
 __device__ __forceinline__ void add_point(Manifold& m, const Vec3& pA, const Vec3& pB, const Vec3& n, float sep) {
     if (m.n < kMaxManifold) {
         ContactPt& c = m.pts[m.n++];
@@ -804,7 +1141,7 @@ __device__ inline uint32_t collide_generic(const ShapeTables& T, const Body& A, 
                                            Manifold& m, Epa& epa) {
     SupportMap map{&T, A, B};
     GjkOut g;
-    gjk(map, tol, 32, g);
+    run_gjk(map, tol, g, epa);
     const bool poly = is_poly(A.s) && is_poly(B.s);
     if (!g.intersect) {
         if (g.distance > max_sep) return 0;
@@ -818,9 +1155,16 @@ __device__ inline uint32_t collide_generic(const ShapeTables& T, const Body& A, 
     if (poly) {
         epa(map, g, tol, 64, e);
         if (epa.deferred) return 0;
+        if (!e.valid) {  // the reference computes the same EPA once more below: same inputs, same result
+            add_point(m, g.pA, g.pB, g.normal.len2() > 0.0f ? g.normal : Vec3(0.0f, 1.0f, 0.0f), 0.0f);
+            return m.n;
+        }
         if (e.valid) {
-            if (!epa.solo()) return 0;  // a cooperative EPA: one lane finishes the manifold
-            if (collide_polyhedral(T, A, B, max_sep, m, e.normal) > 0) return m.n;
+            if constexpr (Epa::kWarp) {  // a cooperative EPA: the warp clips the faces too
+                if (collide_polyhedral_warp(T, A, B, max_sep, m, e.normal, *epa.S, epa.lane) > 0) return m.n;
+            } else {
+                if (collide_polyhedral(T, A, B, max_sep, m, e.normal) > 0) return m.n;
+            }
             add_point(m, e.pA, e.pB, e.normal, -e.depth);
             return m.n;
         }
@@ -844,7 +1188,7 @@ __device__ inline uint32_t collide_sphere_convex(const ShapeTables& T, const Bod
     Body P{&point, S_.q, S_.t};
     SupportMap map{&T, P, B};
     GjkOut g;
-    gjk(map, tol, 32, g);
+    run_gjk(map, tol, g, epa);
     const float radius = S_.s->p[0];
     const Vec3 center = S_.t;
     if (g.intersect) {

@@ -237,7 +237,8 @@ __device__ __forceinline__ void store_manifold(const Manifold& m, uint32_t i, un
 // One thread per pair.  Pairs whose routine needs EPA are deferred to the warp pass below.
 __global__ void __launch_bounds__(128) k_narrow(ShapeTables T, DeviceBodies b, const uint2* __restrict__ pairs,
                                                 Counters* cnt, uint32_t* m_count, float4* m_data,
-                                                unsigned long long* m_key, uint32_t* epa_list) {
+                                                unsigned long long* m_key, uint32_t* epa_list, GjkOut* epa_gjk,
+                                                uint32_t gjk_cap) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cnt->npairs) return;
     uint2 pr = pairs[i];
@@ -252,12 +253,9 @@ __global__ void __launch_bounds__(128) k_narrow(ShapeTables T, DeviceBodies b, c
     Body BA{&T.shapes[b.shape[f]], Q4(b.rot[f]), V3(b.pos[f])};
     Body BB{&T.shapes[b.shape[s]], Q4(b.rot[s]), V3(b.pos[s])};
     Manifold m;
-    EpaDefer ed;
+    EpaDefer ed{&cnt->nepa, epa_list, epa_gjk, gjk_cap, i};
     collide(T, BA, BB, 0.02f, 1.0e-4f, m, ed);
-    if (ed.deferred) {
-        epa_list[atomicAdd(&cnt->nepa, 1u)] = i;
-        return;
-    }
+    if (ed.deferred) return;  // queued for the warp pass
     if (swapped) swap_manifold(m);
     store_manifold(m, i, pair_key(pa, pb), m_count, m_data, m_key);
 }
@@ -266,6 +264,7 @@ __global__ void __launch_bounds__(128) k_narrow(ShapeTables T, DeviceBodies b, c
 constexpr uint32_t kEpaWarps = 4;
 __global__ void __launch_bounds__(kEpaWarps * 32) k_narrow_epa(ShapeTables T, DeviceBodies b, const uint2* __restrict__ pairs,
                                                                Counters* cnt, const uint32_t* __restrict__ epa_list,
+                                                               const GjkOut* __restrict__ epa_gjk, uint32_t gjk_cap,
                                                                uint32_t* m_count, float4* m_data, unsigned long long* m_key,
                                                                uint32_t* err) {
     extern __shared__ EpaWarpSmem epa_smem[];
@@ -286,7 +285,7 @@ __global__ void __launch_bounds__(kEpaWarps * 32) k_narrow_epa(ShapeTables T, De
         Body BA{&T.shapes[b.shape[f]], Q4(b.rot[f]), V3(b.pos[f])};
         Body BB{&T.shapes[b.shape[s]], Q4(b.rot[s]), V3(b.pos[s])};
         Manifold m;
-        EpaCoop ec{&epa_smem[warp], lane, err};
+        EpaCoop ec{&epa_smem[warp], lane, err, idx < gjk_cap ? &epa_gjk[idx] : nullptr};
         collide(T, BA, BB, 0.02f, 1.0e-4f, m, ec);
         if (swapped) swap_manifold(m);
         if (lane == 0) store_manifold(m, i, pair_key(pa, pb), m_count, m_data, m_key);
@@ -962,6 +961,7 @@ cudaError_t create_joints(Ctx& ctx, uint32_t first, uint32_t n) {
     return e != cudaSuccess ? e : cudaStreamSynchronize(ctx.stream);
 }
 size_t joint_record_bytes() { return sizeof(JointDev); }
+size_t gjk_record_bytes() { return sizeof(GjkOut); }
 
 // ---------------------------------------------------------------------------------------------
 // cache store (:568-581) and position integration (:276-290, 785-802, 854-861)
@@ -1562,9 +1562,10 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
     ShapeTables T{ctx.shapes, ctx.hull_verts, ctx.face_sizes, ctx.face_idx};
     KZG_CK(mark(ctx, 1));
     k_narrow<<<blocks_for(P, 128), 128, 0, st>>>(T, ctx.b, ctx.pairs, ctx.dcnt, ctx.m_count, ctx.m_data, ctx.m_key,
-                                                 ctx.epa_list);
+                                                 ctx.epa_list, static_cast<GjkOut*>(ctx.epa_gjk), ctx.epa_gjk_cap);
     k_narrow_epa<<<152u * 8u, kEpaWarps * 32, kEpaWarps * sizeof(EpaWarpSmem), st>>>(
-        T, ctx.b, ctx.pairs, ctx.dcnt, ctx.epa_list, ctx.m_count, ctx.m_data, ctx.m_key, &ctx.dcnt->error);
+        T, ctx.b, ctx.pairs, ctx.dcnt, ctx.epa_list, static_cast<const GjkOut*>(ctx.epa_gjk), ctx.epa_gjk_cap,
+        ctx.m_count, ctx.m_data, ctx.m_key, &ctx.dcnt->error);
     KZG_CK(mark(ctx, 2));
     k_con_flags<<<blocks_for(P), kThreads, 0, st>>>(ctx.m_count, ctx.m_key, ctx.dcnt, ctx.con_flag);
     size_t tb = ctx.cub_tmp_bytes;
