@@ -353,13 +353,23 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
                              (__vcmpeq2(ww0, p1) | __vcmpeq2(ww1, p1) | __vcmpeq2(ww2, p1));
         return (wcnt & 7u) < 4u && !(wcnt & hflag) && hit == 0u;
     };
-    auto win_place = [&](uint32_t x0, uint32_t x1, uint32_t hflag, uint32_t row) {  // one point, this lane
+    // win_place on the lanes with `sel`, written without divergent branches: every lane computes the
+    // new slot state and keeps it only if selected (`opens`: the slot is a batch opened now, `bid`).
+    auto win_place_if = [&](bool sel, uint32_t x0, uint32_t x1, uint32_t hflag, uint32_t row, bool opens, uint32_t bid) {
         const uint32_t kk = wcnt & 7u;
-        if (kk + 1 < 4u) ff_shift_codes(ww0, ww1, ww2, x0, x1, hflag != 0u);  // a full batch's codes are never read again
-        wcnt = (kk + 1) | (wcnt & (kFfH0 | kFfH1)) | hflag;
-        uint32_t* r = rec(S, rb + wbid);
-        r[12 + kk] = row;
-        r[3] = kk + 1;
+        uint32_t n0 = ww0, n1 = ww1, n2 = ww2;
+        ff_shift_codes(n0, n1, n2, x0, x1, hflag != 0u);
+        const bool sh = sel && kk + 1 < 4u;  // a full batch's codes are never read again
+        ww0 = sh ? n0 : ww0;
+        ww1 = sh ? n1 : ww1;
+        ww2 = sh ? n2 : ww2;
+        wbid = (sel && opens) ? bid : wbid;
+        wcnt = sel ? ((kk + 1) | (wcnt & (kFfH0 | kFfH1)) | hflag) : wcnt;
+        if (sel) {
+            uint32_t* r = rec(S, rb + wbid);
+            r[12 + kk] = row;
+            r[3] = kk + 1;
+        }
     };
     auto win_load = [&]() {  // skip the full prefix for good, then hold the next 32 slots
         for (;;) {
@@ -470,10 +480,7 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
                         okB = okBraw & ~fullm & (share ? ~selm : ~0u);
                         pair = (uint32_t)__popc(okB) >= npB;
                     }
-                    if (sel) {
-                        if (lane >= vfirst) wbid = nbt + (lane - vfirst);
-                        win_place(x0, x1, hflag, 4u * c + rank);
-                    }
+                    win_place_if(sel, x0, x1, hflag, 4u * c + rank, lane >= vfirst, nbt + (lane - vfirst));
                     ns += nnew;
                     nbt += nnew;
                     if (pair) {
@@ -481,10 +488,7 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
                         const bool selB = ((okB >> lane) & 1u) && rankB < npB;
                         const uint32_t vB = ns - head;
                         const unsigned newB = __ballot_sync(full, selB && lane >= vB);
-                        if (selB) {
-                            if (lane >= vB) wbid = nbt + (lane - vB);
-                            win_place(x0B, x1B, hfB, 4u * cB + rankB);
-                        }
+                        win_place_if(selB, x0B, x1B, hfB, 4u * cB + rankB, lane >= vB, nbt + (lane - vB));
                         ns += __popc(newB);
                         nbt += __popc(newB);
                         ++k;
