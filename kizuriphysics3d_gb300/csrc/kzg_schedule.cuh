@@ -438,17 +438,29 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
             meta = 64u;
         }
         const uint32_t m = min(32u, s1 - w0);
+        // Constraint fields of window positions k and k + 1 are carried from step to step; those of
+        // k + 2 and k + 3 are shuffled in at the start of each step, off the dependent chain of the
+        // placements, and become the next step's.
+        uint32_t fa_md = __shfl_sync(full, meta, 0), fa_c = __shfl_sync(full, mc, 0), fa_x = __shfl_sync(full, dx, 0);
+        const uint32_t k1 = min(1u, m - 1u);
+        uint32_t fb_md = __shfl_sync(full, meta, k1), fb_c = __shfl_sync(full, mc, k1), fb_x = __shfl_sync(full, dx, k1);
         for (uint32_t k = 0; k < m; ++k) {
-            const uint32_t md = __shfl_sync(full, meta, k);
-            if (md & 64u) continue;  // sensors are never batched (:690)
-            const uint32_t c = __shfl_sync(full, mc, k), xx = __shfl_sync(full, dx, k);
+            const uint32_t k2 = min(k + 2u, m - 1u), k3 = min(k + 3u, m - 1u);
+            const uint32_t fc_md = __shfl_sync(full, meta, k2), fc_c = __shfl_sync(full, mc, k2),
+                           fc_x = __shfl_sync(full, dx, k2);
+            const uint32_t fd_md = __shfl_sync(full, meta, k3), fd_c = __shfl_sync(full, mc, k3),
+                           fd_x = __shfl_sync(full, dx, k3);
+            bool two = false;  // this step placed positions k and k + 1
+            do {
+            const uint32_t md = fa_md;
+            if (md & 64u) break;  // sensors are never batched (:690)
+            const uint32_t c = fa_c, xx = fa_x;
             const uint32_t np = md & 15u, x0 = xx & 0xFFFFu, x1 = xx >> 16;
             const int hub = (int)((md >> 4) & 3u) - 1;
             const uint32_t hflag = hub == 0 ? kFfH0 : (hub == 1 ? kFfH1 : 0u);
             // the next constraint's fields, fetched up front so that its fits overlap this one's
-            const uint32_t kB = k + 1 < m ? k + 1 : k;
-            const uint32_t mdB = __shfl_sync(full, meta, kB);
-            const uint32_t cB = __shfl_sync(full, mc, kB), xxB = __shfl_sync(full, dx, kB);
+            const uint32_t mdB = fb_md;
+            const uint32_t cB = fb_c, xxB = fb_x;
             const bool canB = k + 1 < m && !(mdB & 64u);
             const uint32_t npB = mdB & 15u, x0B = xxB & 0xFFFFu, x1B = xxB >> 16;
             const uint32_t hB = (mdB >> 4) & 3u;
@@ -492,6 +504,7 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
                         ns += __popc(newB);
                         nbt += __popc(newB);
                         ++k;
+                        two = true;
                     }
                     wdirty = true;
                     done = true;
@@ -503,7 +516,7 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
                 }
                 break;
             }
-            if (done) continue;
+            if (done) break;
             win_flush();  // the table is read and written directly below
             const uint16_t* L = hub == 0 ? T.list0 : T.list1;
             const uint32_t nL = hub < 0 ? ns : (hub == 0 ? nl0 : nl1);
@@ -581,6 +594,14 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
                 if (hub != 1) nl1 += rem;
             }
             __syncwarp();
+            } while (false);
+            if (two) {
+                fa_md = fc_md; fa_c = fc_c; fa_x = fc_x;
+                fb_md = fd_md; fb_c = fd_c; fb_x = fd_x;
+            } else {
+                fa_md = fb_md; fa_c = fb_c; fa_x = fb_x;
+                fb_md = fc_md; fb_c = fc_c; fb_x = fc_x;
+            }
         }
     }
     win_flush();
