@@ -795,24 +795,16 @@ kzg_status kzg_download_transforms(kzg_ctx* k, float* out, uint32_t first, uint3
     if (check(k) || !out) return KZG_ERR_INVALID;
     Ctx* ctx = &k->c;
     if (first + count > ctx->nbodies) { ctx->err = "range outside the body array"; return KZG_ERR_INVALID; }
-    // pos.xyz + rot.xyzw: 7 floats per body gathered straight from the float4 arrays
-    CK(cudaMemcpy2DAsync(out, 7 * sizeof(float), ctx->b.pos + first, sizeof(float4), 3 * sizeof(float), count,
-                         cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaMemcpy2DAsync(out + 3, 7 * sizeof(float), ctx->b.rot + first, sizeof(float4), 4 * sizeof(float), count,
-                         cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
-    return KZG_OK;
+    CK(cudaSetDevice(ctx->device));
+    return download_transforms(*ctx, out, first, count);  // pos.xyz + rot.xyzw, 7 floats per body
 }
 
 kzg_status kzg_upload_forces(kzg_ctx* k, const float* ft, uint32_t first, uint32_t count) {
     if (check(k) || !ft) return KZG_ERR_INVALID;
     Ctx* ctx = &k->c;
     if (first + count > ctx->nbodies) { ctx->err = "range outside the body array"; return KZG_ERR_INVALID; }
-    CK(cudaMemcpy2DAsync(ctx->b.force + first, sizeof(float4), ft, 6 * sizeof(float), 3 * sizeof(float), count,
-                         cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpy2DAsync(ctx->b.torque + first, sizeof(float4), ft + 3, 6 * sizeof(float), 3 * sizeof(float), count,
-                         cudaMemcpyHostToDevice, ctx->stream));
-    return KZG_OK;
+    CK(cudaSetDevice(ctx->device));
+    return upload_forces(*ctx, ft, first, count);
 }
 
 kzg_status kzg_download_mass(kzg_ctx* k, float* im, float* iw) {

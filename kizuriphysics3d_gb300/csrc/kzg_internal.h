@@ -35,6 +35,8 @@ kzg_status cache_reset(Ctx& ctx, uint32_t cap);
 // Entries (slot, key, point count, 4 positions, 4 impulses) written into their slots.
 kzg_status cache_scatter(Ctx& ctx, const uint32_t* slots, const unsigned long long* keys, const uint32_t* np,
                          const float4* pos, const float4* imp, uint32_t n);
+kzg_status upload_forces(Ctx& ctx, const float* host_ft, uint32_t first, uint32_t n);          // 6 floats per body
+kzg_status download_transforms(Ctx& ctx, float* host_out, uint32_t first, uint32_t n);      // 7 floats per body
 kzg_status step_canonical(Ctx& ctx, float dt, uint32_t nsteps);
 kzg_status step_external(Ctx& ctx, const uint32_t* host_pairs, uint32_t num_pairs, float dt);
 kzg_status hash_state(Ctx& ctx, uint64_t* out);

@@ -2034,6 +2034,41 @@ cudaError_t edit_bodies(Ctx& ctx, const kzg_body_edit* dev_edits, uint32_t n) {
     return e != cudaSuccess ? e : cudaStreamSynchronize(ctx.stream);
 }
 
+// Host transfers through one contiguous staging buffer (the state-hash scratch, 28 floats per body):
+// one plain copy each way instead of strided copies with 12- and 16-byte rows.
+__global__ void k_scatter_forces(DeviceBodies b, const float* __restrict__ ft, uint32_t first, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* f = ft + 6ull * i;
+    b.force[first + i] = make_float4(f[0], f[1], f[2], 0.0f);
+    b.torque[first + i] = make_float4(f[3], f[4], f[5], 0.0f);
+}
+__global__ void k_gather_transforms(const DeviceBodies b, float* out, uint32_t first, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = b.pos[first + i], q = b.rot[first + i];
+    float* o = out + 7ull * i;
+    o[0] = p.x; o[1] = p.y; o[2] = p.z;
+    o[3] = q.x; o[4] = q.y; o[5] = q.z; o[6] = q.w;
+}
+kzg_status upload_forces(Ctx& ctx, const float* host_ft, uint32_t first, uint32_t n) {
+    if (n == 0) return KZG_OK;
+    float* stage = reinterpret_cast<float*>(ctx.hash_words);
+    KZG_CK(cudaMemcpyAsync(stage, host_ft, sizeof(float) * 6ull * n, cudaMemcpyHostToDevice, ctx.stream));
+    k_scatter_forces<<<blocks_for(n), kThreads, 0, ctx.stream>>>(ctx.b, stage, first, n);
+    KZG_CK(cudaGetLastError());
+    return KZG_OK;
+}
+kzg_status download_transforms(Ctx& ctx, float* host_out, uint32_t first, uint32_t n) {
+    if (n == 0) return KZG_OK;
+    float* stage = reinterpret_cast<float*>(ctx.hash_words);
+    k_gather_transforms<<<blocks_for(n), kThreads, 0, ctx.stream>>>(ctx.b, stage, first, n);
+    KZG_CK(cudaGetLastError());
+    KZG_CK(cudaMemcpyAsync(host_out, stage, sizeof(float) * 7ull * n, cudaMemcpyDeviceToHost, ctx.stream));
+    KZG_CK(cudaStreamSynchronize(ctx.stream));
+    return KZG_OK;
+}
+
 cudaError_t set_bodies_active(Ctx& ctx, const uint32_t* dev_ids, uint32_t n, int active) {
     k_set_active<<<1, 1, 0, ctx.stream>>>(ctx.b, ctx.dcnt, ctx.alist, dev_ids, n, ctx.nbodies, active);
     cudaError_t e = cudaGetLastError();

@@ -73,3 +73,29 @@ def test_wait_that_runs_out_completes_the_step(kzg_lib):
         normal.step_fixed()
         assert short.get_stats()["device_error"] == 0
         assert short.compute_state_hash() == normal.compute_state_hash()
+
+
+def test_host_transfers_through_staging(kzg_lib):
+    """kzg_download_transforms equals the position and rotation columns of the state, and forces
+    uploaded from a host array act exactly as the same forces added through AddForce / AddTorque
+    (a twin world), for a range that starts past slot 0."""
+    from kizuriphysics3d_gb300 import World, capi, make_edit, scenes
+    sc = scenes.pile(300, seed=31, extent=3.0, y_range=(1.0, 10.0))
+    with World(sc) as a, World(sc) as b:
+        a.step_fixed(n=5)
+        b.step_fixed(n=5)
+        tr = a.transforms()
+        st = a.state()
+        assert np.array_equal(bits(tr[:, 0:3]), bits(st[:, 0:3])) and np.array_equal(bits(tr[:, 3:7]), bits(st[:, 3:7]))
+        rng = np.random.default_rng(5)
+        ft = np.zeros((a.n, 6), np.float32)
+        ft[1:] = rng.normal(0.0, 50.0, (a.n - 1, 6)).astype(np.float32)
+        ft[1::7] = 0.0
+        a.upload_forces(ft)
+        edits = np.concatenate([np.concatenate([make_edit(capi.EDIT_ADD_FORCE, i, ft[i, 0:3], wake=False),
+                                                make_edit(capi.EDIT_ADD_TORQUE, i, ft[i, 3:6], wake=False)])
+                                for i in range(1, a.n)])
+        b.edit_bodies(edits)
+        a.step_fixed()
+        b.step_fixed()
+        assert np.array_equal(bits(a.state()), bits(b.state()))
