@@ -146,8 +146,11 @@ __global__ void k_find_pairs(DeviceBodies b, uint32_t n, const unsigned long lon
                              const uint8_t* __restrict__ is_large, const uint32_t* __restrict__ large_list,
                              const uint32_t* __restrict__ large_off, uint32_t nworld_large, unsigned long long* out,
                              Counters* cnt, uint32_t cap) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    // Threads take the bodies in cell order, so that a warp's neighbours, its cell searches and the
+    // bounds it reads are shared (the emitted pairs are sorted afterwards; their order here is free).
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const uint32_t i = svals[t];
     const uint32_t pi = b.packed[i];
     const uint32_t wi = b.world[i];
     // large bodies of this world
