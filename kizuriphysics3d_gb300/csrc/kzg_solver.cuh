@@ -617,6 +617,12 @@ constexpr uint32_t kClusterThreads = 256;
 constexpr uint32_t kClusterSlots = 6144;  // bodies per CTA: 2 x 16 B x 6144 = 192 KB
 constexpr uint32_t kClusterBodies = kClusterCtas * kClusterSlots;
 
+// The two halves of a cluster barrier (every thread of every CTA of the cluster, in order, once each
+// per phase): arrive with release semantics for the shared-memory stores before it, wait with
+// acquire semantics for the loads after it.
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
 // Level barrier and residual sums over the whole cluster: every CTA sums its warps into its own
 // rotating words (as CtaSync does), and after the barrier every thread adds the kClusterCtas partial
 // sums it reads through distributed shared memory.
@@ -940,10 +946,14 @@ __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const Cl
     if (has_cur) load_pack(pk, cap, kc, cur);
     for (uint32_t it = 0; it < iters; ++it) {
         unsigned long long sd = 0, sl = 0;
+        // Levels are separated by a split cluster barrier: a thread arrives (release) once its
+        // level's velocities are stored and waits (acquire) only before it reads velocities again,
+        // with its bookkeeping for the next level in between.
         for (uint32_t l = 0; l < nv; ++l) {
             const uint32_t ln = l + 1 < nv ? l + 1 : 0u;  // after the last level: the next iteration's first
             const uint32_t kn = R + soff[ln] + tid;
             const bool has_nxt = kn < R + soff[ln + 1];
+            if (l > 0) cluster_wait();
             PackVel pv;
             if (has_cur) pv = pack_velocities(V, cur);  // issued first: the level's critical path
             PackItem nxt;
@@ -961,11 +971,12 @@ __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const Cl
                 sd += res_fixed(q.x);
                 sl += res_fixed(q.y);
             }
-            sync();
+            cluster_arrive();
             cur = nxt;
             kc = kn;
             has_cur = has_nxt;
         }
+        if (nv > 0) cluster_wait();
         used = it + 1;
         if (residual || used == iters) {
             sync.sum2(sd, sl, it);
