@@ -110,6 +110,24 @@ struct ClusterView {
         const uint32_t r = loc % kClusterCtas;
         return (r == rank ? w : cg::this_cluster().map_shared_rank(w, r)) + loc / kClusterCtas;
     }
+    // The same slots addressed in the cluster's shared window directly (mapa + ld/st.shared::cluster,
+    // the own CTA included), without generic-address resolution: the hot path of the packed solve.
+    __device__ __forceinline__ uint32_t caddr(const float4* base, uint32_t loc) const {
+        const uint32_t a = (uint32_t)__cvta_generic_to_shared(base) + (loc / kClusterCtas) * 16u;
+        uint32_t r;
+        asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(loc % kClusterCtas));
+        return r;
+    }
+    __device__ __forceinline__ float4 ldc(uint32_t addr) const {
+        float4 x;
+        asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                     : "=f"(x.x), "=f"(x.y), "=f"(x.z), "=f"(x.w) : "r"(addr));
+        return x;
+    }
+    __device__ __forceinline__ void stc(uint32_t addr, const float4& x) const {
+        asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};"
+                     :: "r"(addr), "f"(x.x), "f"(x.y), "f"(x.z), "f"(x.w) : "memory");
+    }
     __device__ __forceinline__ Vec3 lin(uint32_t loc, uint32_t body) const {
         return loc == kNone ? V3(__ldg(&glv[body])) : V3(*rv(loc));
     }
@@ -724,10 +742,10 @@ struct PackVel {
 __device__ __forceinline__ PackVel pack_velocities(const ClusterView& V, const PackItem& it) {
     const uint32_t la = __float_as_uint(it.q[4].w), lb = __float_as_uint(it.q[5].w);
     PackVel p;
-    p.vA = la != kNone ? V3(*V.rv(la)) : V3(it.q[12]);
-    p.wA = la != kNone ? V3(*V.rw(la)) : V3(it.q[13]);
-    p.vB = lb != kNone ? V3(*V.rv(lb)) : V3(it.q[12]);
-    p.wB = lb != kNone ? V3(*V.rw(lb)) : V3(it.q[13]);
+    p.vA = la != kNone ? V3(V.ldc(V.caddr(V.v, la))) : V3(it.q[12]);
+    p.wA = la != kNone ? V3(V.ldc(V.caddr(V.w, la))) : V3(it.q[13]);
+    p.vB = lb != kNone ? V3(V.ldc(V.caddr(V.v, lb))) : V3(it.q[12]);
+    p.wB = lb != kNone ? V3(V.ldc(V.caddr(V.w, lb))) : V3(it.q[13]);
     return p;
 }
 
@@ -742,12 +760,12 @@ __device__ __forceinline__ float2 pack_solve(const ClusterView& V, float4* pk, u
                                    p.wA, p.vB, p.wB, im);
     const uint32_t la = __float_as_uint(q[4].w), lb = __float_as_uint(q[5].w);
     if (la != kNone) {
-        *V.rv(la) = F4(p.vA, 0.0f);
-        *V.rw(la) = F4(p.wA, 0.0f);
+        V.stc(V.caddr(V.v, la), F4(p.vA, 0.0f));
+        V.stc(V.caddr(V.w, la), F4(p.wA, 0.0f));
     }
     if (lb != kNone) {
-        *V.rv(lb) = F4(p.vB, 0.0f);
-        *V.rw(lb) = F4(p.wB, 0.0f);
+        V.stc(V.caddr(V.v, lb), F4(p.vB, 0.0f));
+        V.stc(V.caddr(V.w, lb), F4(p.wB, 0.0f));
     }
     pk[11 * cap + k] = im;
     return r;
