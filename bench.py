@@ -417,9 +417,9 @@ def main():
     value = job_body_steps / (total_ms / 1e3)
     launches = tot["launches"]
 
-    # e2e through the C-ABI with host buffers
-    ft = np.zeros((w.n, 6), np.float32)
-    tr = np.zeros((w.n, 7), np.float32)
+    # e2e through the C-ABI with host buffers (pinned, as a frame loop keeps them)
+    ft = torch.zeros((w.n, 6), dtype=torch.float32).pin_memory().numpy()
+    tr = torch.zeros((w.n, 7), dtype=torch.float32).pin_memory().numpy()
     e2e_s = 0.0
     for i in range(args.steps):
         flush.fill_(float(i))

@@ -749,9 +749,11 @@ __device__ __forceinline__ PackVel pack_velocities(const ClusterView& V, const P
     return p;
 }
 
-// Solves a packed item whose velocities are loaded; stores the velocities and the impulses.
-__device__ __forceinline__ float2 pack_solve(const ClusterView& V, float4* pk, uint32_t cap, uint32_t k,
-                                             const PackItem& it, PackVel& p) {
+// Solves a packed item whose velocities are loaded; stores the velocities and returns the
+// accumulated impulses in `im_out` (stored by the caller: the same thread reads them back next
+// iteration, so they need not be ordered before the level barrier).
+__device__ __forceinline__ float2 pack_solve(const ClusterView& V, uint32_t k, const PackItem& it, PackVel& p,
+                                             float4& im_out) {
     const float4* q = it.q;
     const Mat3 IA{V3(q[6]), Vec3(q[6].w, q[7].x, q[7].y), Vec3(q[7].z, q[7].w, q[8].x)};
     const Mat3 IB{Vec3(q[8].y, q[8].z, q[8].w), V3(q[9]), Vec3(q[9].w, q[10].x, q[10].y)};
@@ -767,7 +769,7 @@ __device__ __forceinline__ float2 pack_solve(const ClusterView& V, float4* pk, u
         V.stc(V.caddr(V.v, lb), F4(p.vB, 0.0f));
         V.stc(V.caddr(V.w, lb), F4(p.wB, 0.0f));
     }
-    pk[11 * cap + k] = im;
+    im_out = im;
     return r;
 }
 
@@ -976,8 +978,9 @@ __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const Cl
             if (has_cur) pv = pack_velocities(V, cur);  // issued first: the level's critical path
             PackItem nxt;
             if (has_nxt) load_pack(pk, cap, kn, nxt);
+            float4 imc;
             if (has_cur) {
-                const float2 q = pack_solve(V, pk, cap, kc, cur, pv);
+                const float2 q = pack_solve(V, kc, cur, pv, imc);
                 sd += res_fixed(q.x);
                 sl += res_fixed(q.y);
             }
@@ -985,11 +988,14 @@ __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const Cl
                 PackItem x;
                 load_pack(pk, cap, k, x);
                 PackVel px = pack_velocities(V, x);
-                const float2 q = pack_solve(V, pk, cap, k, x, px);
+                float4 imx;
+                const float2 q = pack_solve(V, k, x, px, imx);
+                pk[11 * cap + k] = imx;
                 sd += res_fixed(q.x);
                 sl += res_fixed(q.y);
             }
             cluster_arrive();
+            if (has_cur) pk[11 * cap + kc] = imc;  // after the arrive: only this thread reads it again
             cur = nxt;
             kc = kn;
             has_cur = has_nxt;
