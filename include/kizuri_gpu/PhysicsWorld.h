@@ -119,7 +119,7 @@ struct SolverSettings {  // ContactSolver.h:67-82
     float baumgarte = 0.2f, penetrationSlop = 0.005f, restitutionThreshold = 1.0f, maxBiasVelocity = 3.0f;
     float warmStartFactor = 1.0f;
     bool useSplitImpulse = true;  // read nowhere by the reference; accepted with either value
-    bool useSIMDSolver = true;    // false (scalar constraint-order sweep) is rejected: KZG_ERR_UNSUPPORTED
+    bool useSIMDSolver = true;    // false: the scalar constraint-order sweep
     bool useVelocityBias = false;
 };
 

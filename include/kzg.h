@@ -96,9 +96,9 @@ typedef struct {
      * accepted and behave the same, as in the reference. */
     int use_split_impulse;
     /* SolverSettings::useSIMDSolver (ContactSolver.h:77): 1 solves the velocity iterations over the
-     * reference's 4-wide first-fit batches (PhysicsWorld.cpp:677-722), the path this library
-     * accelerates.  0 (the reference's scalar constraint-order sweep) is rejected with
-     * KZG_ERR_UNSUPPORTED. */
+     * reference's 4-wide first-fit batches (PhysicsWorld.cpp:677-722) with SolveVelocityBatchSIMD's
+     * lane math; 0 takes the scalar path, SolveVelocityConstraint over every constraint in island
+     * order (PhysicsWorld.cpp:723-729, ContactSolver.cpp:136-188).  Both are bit-exact. */
     int use_simd_solver;
 } kzg_solver_settings;
 

@@ -384,10 +384,6 @@ kzg_status kzg_set_solver_settings(kzg_ctx* k, const kzg_solver_settings* s) {
         k->c.err = "unknown solver schedule";
         return KZG_ERR_INVALID;
     }
-    if (!s->use_simd_solver) {
-        k->c.err = "SolverSettings::useSIMDSolver = false (the scalar constraint-order sweep) is outside the accelerated path";
-        return KZG_ERR_UNSUPPORTED;
-    }
     if (!(s->residual_tolerance >= 0.0f) || (s->residual_tolerance > 0.0f && s->max_velocity_iterations == 0)) {
         k->c.err = "residual_tolerance must be >= 0, with max_velocity_iterations >= 1 when it is > 0";
         return KZG_ERR_INVALID;

@@ -54,6 +54,8 @@ struct SchedBufs {
     const uint32_t* jflag; // per island: 1 when joints share it (solved with them by k_solve_big), or null
     uint32_t spin_limit;   // polls before the streamed velocity sweep's wait gives up
     const uint32_t* order; // largest-first island order taken from shared counters, or null: island order
+    uint32_t scalar;       // SolverSettings::useSIMDSolver = false: no batches; the velocity sweep visits
+                           // every point in island order, so its levels are the warm start's
 };
 
 struct SchedShared {  // per island scratch living in shared memory
@@ -835,7 +837,7 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
     // Warp 3 then runs the velocity level sweep right behind the first fit (velocity_stream).
     const uint32_t nwarps = (nthreads + 31) >> 5;
     const bool early = nwarps >= 3 && sh->nloc > last_cap;
-    const bool table_ff = ff_table && sh->ff_ok && sh->nloc <= kFfMaxLocal;
+    const bool table_ff = !S.scalar && ff_table && sh->ff_ok && sh->nloc <= kFfMaxLocal;
     const bool stream = early && table_ff && nwarps >= 4;
     if (tid == 0) {
         sh->ff_final = 0;
@@ -863,7 +865,8 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
     const bool batched = table_ff && sh->nbt != kNone;
     const bool streamed = batched && sh->stream_ok != 0u;
     sync();
-    if (!batched && tid == 0) {
+    if (S.scalar && tid == 0) sh->nbt = 0;
+    if (!batched && !S.scalar && tid == 0) {
         const uint32_t hub0 = sh->hub0, hub1 = sh->hub1;
         uint32_t* r0 = rec(S, rb);
         r0[0] = 0; r0[1] = 0; r0[2] = 0;
@@ -938,7 +941,7 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
     const uint32_t nvit = sh->total;
     for (uint32_t sweep = 0; sweep < 3; ++sweep) {
         if (early && sweep != 0) continue;
-        if (streamed && sweep == 0) continue;
+        if ((streamed || S.scalar) && sweep == 0) continue;
         const uint32_t owner = nwarps >= 3 ? sweep : 0;
         if (warp != owner) continue;
         uint32_t* last = (early ? nloc <= 3u * last_cap : nloc <= last_cap)
@@ -949,44 +952,48 @@ __device__ void schedule_island(const SchedBufs& S, Counters* cnt, uint32_t isl,
     sync();
 
     // ---- E: sort each sweep's points by level
-    const uint32_t nv = sh->nv, nw = sh->nw, nb = sh->nb;
+    const uint32_t nw = sh->nw, nb = sh->nb, nv = S.scalar ? nw : sh->nv;
     const uint32_t scap = nthreads >= 64 ? 3u * last_cap : 0u;  // CTA: the level tables' shared memory is free now
     // The emitters walk kU items per thread at once so that their loads overlap.
     constexpr uint32_t kU = 8;
-    level_sort(S, loff, base, nv, tid, nthreads, tmp, S.vl_list, S.vl_off,
-               [&](auto put) {
-                   for (uint32_t i0 = tid; i0 < nvit; i0 += kU * nthreads) {
-                       uint32_t lv[kU], rw[kU];
+    // the warm start's points in constraint order (and, under the scalar solver, the velocity sweep's)
+    auto emit_warm = [&](auto put) {
+        for (uint32_t t0 = s0 + tid; t0 < s1; t0 += kU * nthreads) {
+            uint32_t cc[kU], ff[kU], nn[kU];
 #pragma unroll
-                       for (uint32_t j = 0; j < kU; ++j) {
-                           const uint32_t i = i0 + j * nthreads;
-                           lv[j] = i < nvit ? S.vlev[base + i] : 0u;
-                           rw[j] = i < nvit ? S.vitems[base + i] : 0u;
+            for (uint32_t j = 0; j < kU; ++j) {
+                const uint32_t t = t0 + j * nthreads;
+                cc[j] = t < s1 ? S.isl_con[t] : 0u;
+                ff[j] = t < s1 ? S.first_w[t] : 0u;
+            }
+#pragma unroll
+            for (uint32_t j = 0; j < kU; ++j) nn[j] = t0 + j * nthreads < s1 ? S.con_np[cc[j]] : 0u;
+#pragma unroll
+            for (uint32_t j = 0; j < kU; ++j)
+                for (uint32_t p = 0; p < nn[j]; ++p) put(ff[j] + p, 4u * cc[j] + p);
+        }
+    };
+    if (S.scalar) {
+        level_sort(S, loff, base, nw, tid, nthreads, tmp, S.vl_list, S.vl_off, emit_warm, sync, last_sm, scap);
+    } else {
+        level_sort(S, loff, base, nv, tid, nthreads, tmp, S.vl_list, S.vl_off,
+                   [&](auto put) {
+                       for (uint32_t i0 = tid; i0 < nvit; i0 += kU * nthreads) {
+                           uint32_t lv[kU], rw[kU];
+#pragma unroll
+                           for (uint32_t j = 0; j < kU; ++j) {
+                               const uint32_t i = i0 + j * nthreads;
+                               lv[j] = i < nvit ? S.vlev[base + i] : 0u;
+                               rw[j] = i < nvit ? S.vitems[base + i] : 0u;
+                           }
+#pragma unroll
+                           for (uint32_t j = 0; j < kU; ++j)
+                               if (lv[j]) put(lv[j], rw[j]);
                        }
-#pragma unroll
-                       for (uint32_t j = 0; j < kU; ++j)
-                           if (lv[j]) put(lv[j], rw[j]);
-                   }
-               },
-               sync, last_sm, scap);
-    level_sort(S, loff, base, nw, tid, nthreads, tmp, S.wl_list, S.wl_off,
-               [&](auto put) {
-                   for (uint32_t t0 = s0 + tid; t0 < s1; t0 += kU * nthreads) {
-                       uint32_t cc[kU], ff[kU], nn[kU];
-#pragma unroll
-                       for (uint32_t j = 0; j < kU; ++j) {
-                           const uint32_t t = t0 + j * nthreads;
-                           cc[j] = t < s1 ? S.isl_con[t] : 0u;
-                           ff[j] = t < s1 ? S.first_w[t] : 0u;
-                       }
-#pragma unroll
-                       for (uint32_t j = 0; j < kU; ++j) nn[j] = t0 + j * nthreads < s1 ? S.con_np[cc[j]] : 0u;
-#pragma unroll
-                       for (uint32_t j = 0; j < kU; ++j)
-                           for (uint32_t p = 0; p < nn[j]; ++p) put(ff[j] + p, 4u * cc[j] + p);
-                   }
-               },
-               sync, last_sm, scap);
+                   },
+                   sync, last_sm, scap);
+    }
+    level_sort(S, loff, base, nw, tid, nthreads, tmp, S.wl_list, S.wl_off, emit_warm, sync, last_sm, scap);
     level_sort(S, loff, base, nb, tid, nthreads, tmp, S.bl_list, S.bl_off,
                [&](auto put) {
                    for (uint32_t t0 = s0 + tid; t0 < s1; t0 += kU * nthreads) {

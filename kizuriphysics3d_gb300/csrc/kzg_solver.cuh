@@ -50,6 +50,9 @@ struct SolveBufs {
     const uint32_t* order;   // largest-first island order taken from shared counters, or null (the lists)
     const uint32_t* jflag;   // per island: 1 when joints share it, or null
     uint32_t warp_bodies;    // islands with at most this many dynamic bodies: warp solve
+    uint32_t scalar;         // SolverSettings::useSIMDSolver = false: every point in island order with
+                             // SolveContactVelocity's rows (the schedule's velocity levels are then the
+                             // warm-start levels)
 };
 
 // The solve kernel an island goes to (the lists the schedule appends to follow the same rule).
@@ -166,6 +169,14 @@ __device__ __forceinline__ void warm_point(const SolveBufs& S, const View& V, ui
 // (|n| + |t1|) + |t2| of its accumulated impulses).
 // Everything one velocity point reads besides the body velocities (loaded ahead of time by the
 // prefetching sweep).
+// The normal row's velocity bias: SolveVelocityBatchSIMD adds positionBias or zero to
+// restitutionBias (ContactSolverSIMD.cpp), SolveContactVelocity adds positionBias only under
+// useVelocityBias (ContactSolver.cpp:167-168).
+__device__ __forceinline__ float normal_bias(bool scalar, int vel_bias, const float4& bias) {
+    if (scalar) return vel_bias ? bias.x + bias.y : bias.x;
+    return bias.x + (vel_bias ? bias.y : 0.0f);
+}
+
 struct VelItem {
     uint32_t row, A, B, la, lb;
     float4 rA, rB, n, t1, t2, m, im;  // t1.w = friction
@@ -183,8 +194,7 @@ __device__ __forceinline__ void load_vel_item(const SolveBufs& S, uint32_t row, 
     it.t2 = S.r.t2[row];
     it.m = S.r.mass[row];
     it.im = S.r.imp[row];
-    const float4 bias = S.r.bias[row];
-    it.nb = bias.x + (S.vel_bias ? bias.y : 0.0f);
+    it.nb = normal_bias(S.scalar != 0u, S.vel_bias, S.r.bias[row]);
     it.invA = S.b.inv_mass[A];
     it.invB = S.b.inv_mass[B];
     it.IA = M3(&S.b.iiw[3 * A]);
@@ -237,14 +247,71 @@ __device__ __forceinline__ float2 velocity_rows(const Vec3& rA, const Vec3& rB, 
     return make_float2(dsum, (fabsf(nacc) + fabsf(t1acc)) + fabsf(t2acc));
 }
 
-// One lane of SolveVelocityBatchSIMD on a loaded item.
+// SolveContactVelocity (ContactSolver.cpp:136-181) on loaded data, the scalar solver's point: both
+// friction rows take the relative velocity measured before them, the normal row measures it again;
+// -mass * v, math::Clamp / math::Max, and impulses reach dynamic bodies only (ApplyImpulsePair).
+// Same in-place updates and residual shares as velocity_rows.
+__device__ __forceinline__ float2 velocity_rows_scalar(const Vec3& rA, const Vec3& rB, const float4& n4,
+                                                       const float4& t14, const float4& t24, const float4& m4,
+                                                       float invA, float invB, float nb, const Mat3& IA,
+                                                       const Mat3& IB, bool dynA, bool dynB, Vec3& vA, Vec3& wA,
+                                                       Vec3& vB, Vec3& wB, float4& im) {
+    const float fric = t14.w;
+    float nacc = im.x, t1acc = im.y, t2acc = im.z;
+    float dsum = 0.0f;
+    auto rel = [&]() {
+        const Vec3 wa = wA.cross(rA), wb = wB.cross(rB);
+        return Vec3((vA.x + wa.x) - (vB.x + wb.x), (vA.y + wa.y) - (vB.y + wb.y), (vA.z + wa.z) - (vB.z + wb.z));
+    };
+    auto apply = [&](const Vec3& dir, float dl) {
+        const Vec3 imp(dir.x * dl, dir.y * dl, dir.z * dl);
+        if (dynA) {
+            vA = Vec3(vA.x + imp.x * invA, vA.y + imp.y * invA, vA.z + imp.z * invA);
+            wA = wA + IA * rA.cross(imp);
+        }
+        if (dynB) {
+            vB = Vec3(vB.x - imp.x * invB, vB.y - imp.y * invB, vB.z - imp.z * invB);
+            wB = wB - IB * rB.cross(imp);
+        }
+    };
+    const Vec3 vt = rel();
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        const Vec3 dir = t == 0 ? V3(t14) : V3(t24);
+        const float mass = t == 0 ? m4.y : m4.z;
+        const float acc = t == 0 ? t1acc : t2acc;
+        const float lambda = -mass * vt.dot(dir);
+        const float maxf = fric * nacc;
+        float na = acc + lambda;
+        na = na < -maxf ? -maxf : (na > maxf ? maxf : na);
+        const float dl = na - acc;
+        if (t == 0) t1acc = na; else t2acc = na;
+        dsum += fabsf(dl);
+        apply(dir, dl);
+    }
+    const Vec3 n = V3(n4);
+    const float lambda = -m4.x * (rel().dot(n) - nb);
+    float na = nacc + lambda;
+    na = na > 0.0f ? na : 0.0f;
+    const float dl = na - nacc;
+    nacc = na;
+    dsum += fabsf(dl);
+    apply(n, dl);
+    im = make_float4(nacc, t1acc, t2acc, im.w);
+    return make_float2(dsum, (fabsf(nacc) + fabsf(t1acc)) + fabsf(t2acc));
+}
+
+// One point of the velocity sweep on a loaded item: a lane of SolveVelocityBatchSIMD, or
+// SolveContactVelocity under the scalar solver.
 template <typename View>
 __device__ __forceinline__ float2 velocity_item(const SolveBufs& S, const View& V, const VelItem& it) {
     const uint32_t A = it.A, B = it.B, la = it.la, lb = it.lb;
     Vec3 vA = V.lin(la, A), wA = V.ang(la, A), vB = V.lin(lb, B), wB = V.ang(lb, B);
     float4 im = it.im;
-    const float2 q = velocity_rows(V3(it.rA), V3(it.rB), it.n, it.t1, it.t2, it.m, it.invA, it.invB, it.nb, it.IA,
-                                   it.IB, vA, wA, vB, wB, im);
+    const float2 q = S.scalar ? velocity_rows_scalar(V3(it.rA), V3(it.rB), it.n, it.t1, it.t2, it.m, it.invA, it.invB,
+                                                     it.nb, it.IA, it.IB, la != kNone, lb != kNone, vA, wA, vB, wB, im)
+                              : velocity_rows(V3(it.rA), V3(it.rB), it.n, it.t1, it.t2, it.m, it.invA, it.invB, it.nb,
+                                              it.IA, it.IB, vA, wA, vB, wB, im);
     if (la != kNone) V.put(la, A, vA, wA);
     if (lb != kNone) V.put(lb, B, vB, wB);
     S.r.imp[it.row] = im;
@@ -695,6 +762,7 @@ struct PackItem {
 };
 
 // The fields of a point's packed item, gathered from its row and bodies.
+template <bool kScalar>
 __device__ __forceinline__ void gather_item(const SolveBufs& S, uint32_t row, PackItem& it) {
     const uint32_t c = row >> 2;
     const uint32_t A = S.con_a[c], B = S.con_b[c], la = __ldcg(&S.con_la[c]), lb = __ldcg(&S.con_lb[c]);
@@ -704,7 +772,7 @@ __device__ __forceinline__ void gather_item(const SolveBufs& S, uint32_t row, Pa
     const uint32_t st = la == kNone ? A : (lb == kNone ? B : kNone);
     it.q[0] = make_float4(rA.x, rA.y, rA.z, S.b.inv_mass[A]);
     it.q[1] = make_float4(rB.x, rB.y, rB.z, S.b.inv_mass[B]);
-    it.q[2] = make_float4(n.x, n.y, n.z, bias.x + (S.vel_bias ? bias.y : 0.0f));
+    it.q[2] = make_float4(n.x, n.y, n.z, normal_bias(kScalar, S.vel_bias, bias));
     it.q[3] = S.r.t1[row];
     it.q[4] = make_float4(t2.x, t2.y, t2.z, __uint_as_float(la));
     it.q[5] = make_float4(m.x, m.y, m.z, __uint_as_float(lb));
@@ -753,14 +821,16 @@ __device__ __forceinline__ PackVel pack_velocities(const ClusterView& V, const P
 // accumulated impulses in `im_out` (stored by the caller: the same thread reads them back next
 // iteration, so they need not be ordered before the level barrier).
 __device__ __forceinline__ float2 pack_solve(const ClusterView& V, uint32_t k, const PackItem& it, PackVel& p,
-                                             float4& im_out) {
+                                             float4& im_out, bool scalar) {
     const float4* q = it.q;
     const Mat3 IA{V3(q[6]), Vec3(q[6].w, q[7].x, q[7].y), Vec3(q[7].z, q[7].w, q[8].x)};
     const Mat3 IB{Vec3(q[8].y, q[8].z, q[8].w), V3(q[9]), Vec3(q[9].w, q[10].x, q[10].y)};
     float4 im = q[11];
-    const float2 r = velocity_rows(V3(q[0]), V3(q[1]), q[2], q[3], q[4], q[5], q[0].w, q[1].w, q[2].w, IA, IB, p.vA,
-                                   p.wA, p.vB, p.wB, im);
     const uint32_t la = __float_as_uint(q[4].w), lb = __float_as_uint(q[5].w);
+    const float2 r = scalar ? velocity_rows_scalar(V3(q[0]), V3(q[1]), q[2], q[3], q[4], q[5], q[0].w, q[1].w, q[2].w,
+                                                   IA, IB, la != kNone, lb != kNone, p.vA, p.wA, p.vB, p.wB, im)
+                            : velocity_rows(V3(q[0]), V3(q[1]), q[2], q[3], q[4], q[5], q[0].w, q[1].w, q[2].w, IA,
+                                            IB, p.vA, p.wA, p.vB, p.wB, im);
     if (la != kNone) {
         V.stc(V.caddr(V.v, la), F4(p.vA, 0.0f));
         V.stc(V.caddr(V.w, la), F4(p.wA, 0.0f));
@@ -878,7 +948,7 @@ __device__ __forceinline__ void sweep_prefetched(const uint32_t* list, const uin
 // Before a thread solves its point of a level it loads its packed point of the next one - nothing
 // the current level writes - so after each barrier only the velocity loads stand between it and its
 // math.  Needs at least two velocity levels (the prefetched point must differ from the current one).
-template <typename Sync>
+template <bool kScalar, typename Sync>
 __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const ClusterView& V, float4* pk,
                                       uint32_t* soff, uint32_t* lofs, uint32_t* rall, uint32_t* tmp, uint32_t rank,
                                       uint32_t gtid, uint32_t gthreads, Sync sync, Counters* cnt) {
@@ -948,7 +1018,7 @@ __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const Cl
         const uint32_t row = S.vl_list[base + k], o = point_owner(S, row);
         const uint32_t pos = rall[o] + cl.map_shared_rank(soff, o)[level_of(k)] + S.vrec[base + k].x;
         PackItem x;
-        gather_item(S, row, x);
+        gather_item<kScalar>(S, row, x);
         store_pack(pk, cap, pos, x);
     }
     const uint32_t R = rall[rank];
@@ -980,7 +1050,7 @@ __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const Cl
             if (has_nxt) load_pack(pk, cap, kn, nxt);
             float4 imc;
             if (has_cur) {
-                const float2 q = pack_solve(V, kc, cur, pv, imc);
+                const float2 q = pack_solve(V, kc, cur, pv, imc, kScalar);
                 sd += res_fixed(q.x);
                 sl += res_fixed(q.y);
             }
@@ -989,7 +1059,7 @@ __device__ void solve_velocity_packed(const SolveBufs& S, uint32_t isl, const Cl
                 load_pack(pk, cap, k, x);
                 PackVel px = pack_velocities(V, x);
                 float4 imx;
-                const float2 q = pack_solve(V, k, x, px, imx);
+                const float2 q = pack_solve(V, k, x, px, imx, kScalar);
                 pk[11 * cap + k] = imx;
                 sd += res_fixed(q.x);
                 sl += res_fixed(q.y);
@@ -1127,6 +1197,9 @@ __device__ uint32_t cluster_layout(const SolveBufs& S, const SolveBufs& SC, uint
 }
 
 // Islands with more than smem_bodies and at most kClusterCtas * kClusterSlots dynamic bodies.
+// kScalar: SolveBufs::scalar, fixed at compile time so that the batch solver's level loop carries
+// no second row routine.
+template <bool kScalar>
 __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads, 1)
     k_solve_cluster(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
     extern __shared__ float4 smem[];
@@ -1144,6 +1217,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
     const ClusterView V{sv, sw, S.b.lv, S.b.av, rank};
     const ClusterSync sync{red};
     SolveBufs SC = S;  // the island's constraints with permuted local ids
+    SC.scalar = kScalar ? 1u : 0u;
     SC.con_la = S.cl_ids + 2u * kClusterGrid * kClusterBodies;
     SC.con_lb = SC.con_la + S.max_cons;
     uint32_t* ids = S.cl_ids + 2u * kClusterBodies * cid;
@@ -1159,7 +1233,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
         }
         cl.sync();
         if (S.meta[4 * isl + 1] >= 2)  // prefetching needs two distinct levels
-            solve_velocity_packed(SC, isl, V, S.pk + (size_t)cid * kPackArrays * S.pk_cap, soff, lofs, rall, tmp, rank,
+            solve_velocity_packed<kScalar>(SC, isl, V, S.pk + (size_t)cid * kPackArrays * S.pk_cap, soff, lofs, rall, tmp, rank,
                                   gtid, gthreads, sync, cnt);
         else
             solve_velocity(SC, isl, V, gtid, gthreads, sync, cnt);

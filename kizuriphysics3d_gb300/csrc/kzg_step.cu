@@ -1515,12 +1515,13 @@ cudaError_t configure_kernels() {
                              (int)(3 * kSchedCtaBodies * sizeof(uint32_t)));
     if (e != cudaSuccess) return e;
     // the cluster solve needs kClusterCtas co-resident CTAs with 192 KB of shared memory each
-    e = cudaFuncSetAttribute(k_solve_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)(2 * kClusterSlots * sizeof(float4)));
-    if (e != cudaSuccess) return e;
-    if (kClusterCtas > 8) {
-        e = cudaFuncSetAttribute(k_solve_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    for (const void* f : {(const void*)k_solve_cluster<false>, (const void*)k_solve_cluster<true>}) {
+        e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(2 * kClusterSlots * sizeof(float4)));
         if (e != cudaSuccess) return e;
+        if (kClusterCtas > 8) {
+            e = cudaFuncSetAttribute(f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            if (e != cudaSuccess) return e;
+        }
     }
     {
         cudaLaunchConfig_t lc = {};
@@ -1534,9 +1535,11 @@ cudaError_t configure_kernels() {
         at.val.clusterDim.z = 1;
         lc.attrs = &at;
         lc.numAttrs = 1;
-        int nclusters = 0;
-        g_cluster_ok = cudaOccupancyMaxActiveClusters(&nclusters, (void*)k_solve_cluster, &lc) == cudaSuccess &&
-                       nclusters > 0;
+        int nclusters = 0, nclusters_scalar = 0;
+        g_cluster_ok = cudaOccupancyMaxActiveClusters(&nclusters, (void*)k_solve_cluster<false>, &lc) == cudaSuccess &&
+                       cudaOccupancyMaxActiveClusters(&nclusters_scalar, (void*)k_solve_cluster<true>, &lc) ==
+                           cudaSuccess &&
+                       nclusters > 0 && nclusters_scalar > 0;
         cudaGetLastError();
     }
     return mlp_configure_kernels();
@@ -1658,7 +1661,7 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
                  ctx.vl_off, ctx.bl_off, ctx.isl_meta, ctx.isl_small, ctx.isl_large,
                  std::min(ctx.tune.small_island_constraints, kSchedSmallCons),
                  std::min(ctx.tune.warp_island_bodies, kWarpBodies), nj ? ctx.jflag : nullptr, ctx.wait_limit,
-                 lpt ? ctx.isl_order : nullptr};
+                 lpt ? ctx.isl_order : nullptr, ctx.ss.use_simd_solver ? 0u : 1u};
     k_schedule_warp<<<152u * 16u, 128, 0, st>>>(SB, ctx.dcnt);
     k_schedule_cta<<<152u * 2u, 256, 3 * kSchedCtaBodies * sizeof(uint32_t), st>>>(SB, ctx.dcnt);
     ctx.launches += 16;  // prepare, union-find (2), island sort (4 CUB passes), heads, scan (2), starts, schedule (2)
@@ -1671,11 +1674,12 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
                  g_cluster_ok ? ctx.pk_cap : 0u, ctx.isl_con, ctx.cfg.max_pairs, ctx.cl_ids,
                  nj ? ctx.joints : nullptr, ctx.jkeys_sorted, ctx.jisl, ctx.jisl_cisl,
                  lpt ? ctx.isl_order : nullptr, nj ? ctx.jflag : nullptr,
-                 std::min(ctx.tune.warp_island_bodies, kWarpBodies)};
+                 std::min(ctx.tune.warp_island_bodies, kWarpBodies), ctx.ss.use_simd_solver ? 0u : 1u};
     k_solve_warp<<<152u * 16u, kWarpsPerBlock * 32, kWarpsPerBlock * 2 * kWarpBodies * sizeof(float4), st>>>(SV, ctx.dcnt);
     k_solve_cta<<<152u * 2u, kCtaThreads, 2 * kCtaBodiesMax * sizeof(float4), st>>>(SV, ctx.dcnt, kCtaBodiesMax);
     if (g_cluster_ok) {
-        k_solve_cluster<<<kClusterCtas * kClusterGrid, kClusterThreads, 2 * kClusterSlots * sizeof(float4), st>>>(
+        auto* kern = ctx.ss.use_simd_solver ? k_solve_cluster<false> : k_solve_cluster<true>;
+        kern<<<kClusterCtas * kClusterGrid, kClusterThreads, 2 * kClusterSlots * sizeof(float4), st>>>(
             SV, ctx.dcnt, kCtaBodiesMax);
         ++ctx.launches;
     }

@@ -54,6 +54,7 @@ BODY_FLAG_LINEAR_CAST = 4   # MotionQuality::LinearCast: continuous collision cl
 WORLD_FLAG_ALLOW_SLEEPING = 1
 WORLD_FLAG_VELOCITY_BIAS = 2
 WORLD_FLAG_NO_WARM_START = 4   # the reference's KZ_NOWS environment switch (PhysicsWorld.cpp:493)
+WORLD_FLAG_SCALAR_SOLVER = 8   # SolverSettings::useSIMDSolver = false (ContactSolver.h:77)
 
 SCENE_MAGIC = 0x4353_5A4B  # 'KZSC'
 SCENE_VERSION = 2  # 2 adds the world's sleep thresholds and each body's CCD motion threshold; 1 is still read

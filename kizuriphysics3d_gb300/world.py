@@ -16,7 +16,7 @@ import numpy as np
 
 from . import capi
 from .scenes import (Scene, SHAPE_HULL, WORLD_FLAG_ALLOW_SLEEPING, WORLD_FLAG_NO_WARM_START,
-                     WORLD_FLAG_VELOCITY_BIAS)
+                     WORLD_FLAG_SCALAR_SOLVER, WORLD_FLAG_VELOCITY_BIAS)
 
 PT_FLOATS = 39
 
@@ -147,6 +147,7 @@ class World:
         ss.max_bias_velocity = scene.max_bias_velocity
         ss.warm_start_factor = scene.warm_start_factor
         ss.use_velocity_bias = int(bool(scene.flags & WORLD_FLAG_VELOCITY_BIAS))
+        ss.use_simd_solver = 0 if scene.flags & WORLD_FLAG_SCALAR_SOLVER else 1
         self._check(L.kzg_set_world_settings(h, ctypes.byref(ws)))
         self._check(L.kzg_set_solver_settings(h, ctypes.byref(ss)))
         self._ss = ss

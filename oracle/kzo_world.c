@@ -82,7 +82,7 @@ struct kzo_world {
     float fixed_dt, baumgarte, slop, rest_thresh, max_bias, ws_factor;
     float sleep_time, sleep_lin, sleep_ang; /* WorldSettings sleep thresholds */
     uint32_t vel_iters, pos_iters;
-    int vel_bias, no_ws, threads, pair_mode, sched_stats;
+    int vel_bias, no_ws, threads, pair_mode, sched_stats, scalar_solver;
     float res_tol;     /* > 0: velocity iterations stop once the island's residual is <= res_tol */
     uint32_t res_cap;  /* iteration cap when res_tol > 0 */
     /* shapes */
@@ -667,6 +667,42 @@ static void solve_lane(kzo_world* w, con_t* c, cpc_t* p, uint64_t* sd, uint64_t*
     *sl += res_fixed((fabsf(nacc) + fabsf(t1acc)) + fabsf(t2acc));
 }
 
+/* SolveContactVelocity (ContactSolver.cpp:136-181): the scalar path of SolverSettings::useSIMDSolver
+ * = false.  Both friction rows use the relative velocity taken before them; the normal row takes it
+ * again.  Residual sums as solve_lane's. */
+static void solve_point_scalar(kzo_world* w, con_t* c, cpc_t* p, uint64_t* sd, uint64_t* sl) {
+    const int A = c->a, B = c->b;
+    const v3 rA = qrotate(w->rot[A], p->laA);
+    const v3 rB = qrotate(w->rot[B], p->laB);
+    v3 vrel = vsub(vadd(w->lv[A], vcross(w->av[A], rA)), vadd(w->lv[B], vcross(w->av[B], rB)));
+    float dsum = 0.0f;
+    for (int t = 0; t < 2; ++t) {
+        const v3 tangent = t == 0 ? p->t1 : p->t2;
+        const float mass = t == 0 ? p->tm1 : p->tm2;
+        float* accum = t == 0 ? &p->ti1 : &p->ti2;
+        float lambda = -mass * vdot(vrel, tangent);
+        const float maxf = p->fric * p->ni;
+        float ni = *accum + lambda;
+        ni = ni < -maxf ? -maxf : (ni > maxf ? maxf : ni); /* math::Clamp, Types.h:55 */
+        lambda = ni - *accum;
+        *accum = ni;
+        dsum += fabsf(lambda);
+        apply_pair(w, A, B, rA, rB, vmul(tangent, lambda), c->dynA, c->dynB);
+    }
+    vrel = vsub(vadd(w->lv[A], vcross(w->av[A], rA)), vadd(w->lv[B], vcross(w->av[B], rB)));
+    float bias = p->rbias;
+    if (w->vel_bias) bias += p->pbias;
+    float lambda = -p->nm * (vdot(vrel, p->n) - bias);
+    float ni = p->ni + lambda;
+    ni = ni > 0.0f ? ni : 0.0f; /* math::Max, Types.h:54 */
+    lambda = ni - p->ni;
+    p->ni = ni;
+    dsum += fabsf(lambda);
+    apply_pair(w, A, B, rA, rB, vmul(p->n, lambda), c->dynA, c->dynB);
+    *sd += res_fixed(dsum);
+    *sl += res_fixed((fabsf(p->ni) + fabsf(p->ti1)) + fabsf(p->ti2));
+}
+
 /* SolveBiasConstraint, ContactSolver.cpp:257-290 */
 static void solve_bias(kzo_world* w, con_t* c) {
     int A = c->a, B = c->b;
@@ -1157,7 +1193,7 @@ static void solve_island(kzo_world* w, uint32_t isl, uint32_t* out_batches, uint
     for (uint32_t i = 0; i < nc; ++i) npts += w->cons[list[i]].npts;
     batch_t* bt = (batch_t*)xrealloc(NULL, sizeof(batch_t) * (npts ? npts : 1));
     uint32_t nbt = 0, nopen = 0, max_open = 0;
-    for (uint32_t i = 0; i < nc; ++i) {
+    for (uint32_t i = 0; i < nc && !w->scalar_solver; ++i) {
         con_t* c = &w->cons[list[i]];
         if (c->sensor) continue;
         for (uint32_t p = 0; p < c->npts; ++p) {
@@ -1198,17 +1234,25 @@ static void solve_island(kzo_world* w, uint32_t isl, uint32_t* out_batches, uint
     float res = 0.0f;
     for (uint32_t it = 0; it < iters; ++it) {
         uint64_t sd = 0, sl = 0;
-        for (uint32_t bi = 0; bi < nbt; ++bi)
-            for (uint32_t k = 0; k < bt[bi].count; ++k) {
-                con_t* c = &w->cons[bt[bi].ref[k].con];
-                solve_lane(w, c, &c->p[bt[bi].ref[k].pt], &sd, &sl);
+        if (w->scalar_solver) {  /* every constraint in island order, sensors included (PhysicsWorld.cpp:723-727) */
+            for (uint32_t i = 0; i < nc; ++i) {
+                con_t* c = &w->cons[list[i]];
+                for (uint32_t p = 0; p < c->npts; ++p) solve_point_scalar(w, c, &c->p[p], &sd, &sl);
             }
+        } else {
+            for (uint32_t bi = 0; bi < nbt; ++bi)
+                for (uint32_t k = 0; k < bt[bi].count; ++k) {
+                    con_t* c = &w->cons[bt[bi].ref[k].con];
+                    solve_lane(w, c, &c->p[bt[bi].ref[k].pt], &sd, &sl);
+                }
+        }
         used = it + 1;
         res = sl ? (float)((double)sd / (double)sl) : (sd ? 1.0f : 0.0f);
         if (w->res_tol > 0.0f && (double)sd <= (double)w->res_tol * (double)sl) break;
     }
     uint32_t nbp = 0;
     for (uint32_t bi = 0; bi < nbt; ++bi) nbp += bt[bi].count;
+    if (w->scalar_solver) nbp = npts;
     *out_iters = used;
     *out_pt_iters = nbp * used;
     *out_res = res;
@@ -1223,6 +1267,18 @@ static void solve_island(kzo_world* w, uint32_t isl, uint32_t* out_batches, uint
         /* Dependency levels of the two Gauss-Seidel sweeps, counting only dynamic bodies. */
         uint32_t* last = (uint32_t*)calloc((size_t)w->nb, sizeof(uint32_t));
         uint32_t vl = 0;
+        for (uint32_t i = 0; i < nc && w->scalar_solver; ++i) {  /* the scalar sweep: island order */
+            con_t* c = &w->cons[list[i]];
+            for (uint32_t p = 0; p < c->npts; ++p) {
+                uint32_t l = 0;
+                if (c->dynA && last[c->a] > l) l = last[c->a];
+                if (c->dynB && last[c->b] > l) l = last[c->b];
+                ++l;
+                if (c->dynA) last[c->a] = l;
+                if (c->dynB) last[c->b] = l;
+                if (l > vl) vl = l;
+            }
+        }
         for (uint32_t bi = 0; bi < nbt; ++bi)
             for (uint32_t k = 0; k < bt[bi].count; ++k) {
                 con_t* c = &w->cons[bt[bi].ref[k].con];
@@ -1763,6 +1819,7 @@ kzo_world* kzo_create(const uint8_t* scene, size_t scene_len, const uint8_t* res
     w->allow_sleeping = (wflags & 1u) != 0;
     w->vel_bias = (wflags & 2u) != 0;
     w->no_ws = (wflags & 4u) != 0;
+    w->scalar_solver = (wflags & 8u) != 0;  /* SolverSettings::useSIMDSolver = false */
     w->fixed_dt = (float)(1.0 / 60.0); /* WorldSettings::fixedTimestep, PhysicsWorld.h:32 */
     w->threads = 1;
     w->root = NUL;

@@ -151,6 +151,7 @@ int main(int argc, char** argv) {
     ws.solver.useVelocityBias = (wflags & 2u) != 0;
     ws.useMultithreading = !singleThread;
     if (wflags & 4u) setenv("KZ_NOWS", "1", 1);
+    ws.solver.useSIMDSolver = (wflags & 8u) == 0;
 
     uint32_t ns = rd.get<uint32_t>();
     std::vector<ShapeRef> shapes(ns);

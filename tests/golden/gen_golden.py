@@ -45,6 +45,9 @@ def fixture_scenes():
     out["sleep_wake"] = (_sleep_wake(), 600, 2, [0, 59, 119, 239, 359, 479, 599])
     out["pile120_sleep"] = (_sleeping(scenes.pile(120, seed=55, extent=2.5, y_range=(1.0, 8.0)), "pile120_sleep"),
                             480, 2, [0, 119, 239, 479])
+    out["pyramid20_scalar"] = (_scalar(scenes.pyramid(20), "pyramid20_scalar"), 300, 2, [0, 1, 59, 299])
+    out["pile200_scalar"] = (_scalar(scenes.pile(200, seed=1234, extent=3.0, y_range=(2.0, 12.0)), "pile200_scalar"),
+                             300, 2, [0, 1, 59, 299])
     out["edits_sleep"] = (_edits_sleep_scene(), 480, 2, [0, 20, 45, 199, 200, 299, 479])
     out["edits_nosleep"] = (_edits_nosleep_scene(), 240, 2, [0, 40, 41, 119, 120, 239])
     return out
@@ -140,6 +143,14 @@ def _edits_nosleep_scene():
 def kzp1_fixtures():
     """Fixture scene -> step count after which the reference saves the world as KZP1."""
     return {"pile200": 0, "sleep_wake": 300, "ccd_threshold": 30}
+
+
+def _scalar(sc, name):
+    """SolverSettings::useSIMDSolver = false: velocity iterations over the constraints in order with
+    the scalar SolveContactVelocity (PhysicsWorld.cpp:723-727, ContactSolver.cpp:136-181)."""
+    sc.flags |= scenes.WORLD_FLAG_SCALAR_SOLVER
+    sc.name = name
+    return sc
 
 
 def _sleeping(sc, name):

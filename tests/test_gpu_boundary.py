@@ -10,21 +10,31 @@ from conftest import bits
 
 pytestmark = pytest.mark.gpu
 
-KZG_ERR_UNSUPPORTED = -4
 KZG_DEVERR_WAIT = 16
 
 
-def test_scalar_solver_is_rejected(kzg_lib):
-    """SolverSettings::useSIMDSolver = false (ContactSolver.h:77) selects the reference's scalar
-    constraint-order sweep (PhysicsWorld.cpp:723-729), which this library does not implement."""
-    from kizuriphysics3d_gb300 import World, capi, scenes
-    with World(scenes.pyramid(3)) as w:
-        with pytest.raises(capi.KzgError) as e:
-            w.set_solver(use_simd_solver=0)
-        assert e.value.status == KZG_ERR_UNSUPPORTED
-        assert "useSIMDSolver" in str(e.value)
-        w.set_solver(use_simd_solver=1)  # the default is accepted again
-        w.step_fixed()
+def test_simd_and_scalar_solvers_agree(kzg_lib):
+    """World_SIMDMatchesScalar (reference tests/TestWorld.cpp:302-328): four unit boxes stacked with
+    small offsets on the ground, two seconds, once per SolverSettings::useSIMDSolver value: the box
+    positions agree within 0.05 m, while the bits differ (the two paths are different solvers)."""
+    from kizuriphysics3d_gb300 import World, scenes
+
+    def run(simd):
+        sc = scenes.Scene(name="simd_vs_scalar", flags=scenes.WORLD_FLAG_ALLOW_SLEEPING)
+        plane = sc.add_shape(scenes.Shape(scenes.SHAPE_PLANE, [0.0, 1.0, 0.0, 0.0]))
+        sc.add_body(scenes.Body(plane, scenes.MOTION_STATIC, friction=0.8))
+        box = sc.add_shape(scenes.Shape(scenes.SHAPE_BOX, [0.5, 0.5, 0.5, 0.0]))
+        for i in range(4):
+            sc.add_body(scenes.Body(box, pos=(scenes.f32(i * 0.05), scenes.f32(1.0 + i * 1.02), 0.0), friction=0.6))
+        with World(sc) as w:
+            w.set_solver(use_simd_solver=1 if simd else 0)
+            w.step_fixed(n=int(2.0 / (1.0 / 60.0)))
+            assert w.get_stats()["device_error"] == 0
+            return w.state()[1:, 0:3].copy()
+
+    a, b = run(False), run(True)
+    assert np.all(np.linalg.norm(a.astype(np.float64) - b, axis=1) <= 0.05)
+    assert not np.array_equal(bits(a), bits(b))
 
 
 def test_split_impulse_flag_changes_nothing(kzg_lib):

@@ -62,7 +62,8 @@ def test_mode_a_bit_exact_with_reference(name, oracle_lib, kzg_lib):
 
 @pytest.mark.parametrize("name,steps", [("pile200", 300), ("stacks2x2x20", 200), ("pyramid20", 200),
                                         ("ccd_shots", 120), ("ccd_threshold", 90), ("sleep_wake", 600),
-                                        ("pile120_sleep", 480), ("edits_sleep", 480), ("edits_nosleep", 240)])
+                                        ("pile120_sleep", 480), ("edits_sleep", 480), ("edits_nosleep", 240),
+                                        ("pyramid20_scalar", 300), ("pile200_scalar", 300)])
 def test_mode_b_bit_exact_with_oracle(name, steps, oracle_lib, kzg_lib):
     sc, g, ow, gw = _pair_worlds(name, oracle_lib.PAIRS_CANONICAL, oracle_lib)
     with gw:
@@ -91,7 +92,26 @@ def test_mode_b_larger_pile(oracle_lib, kzg_lib):
         assert gw.compute_state_hash() == ow.hash()
 
 
-def test_mode_b_settled_full_pile(oracle_lib, kzg_lib):
+def test_mode_b_scalar_solver_larger_pile(oracle_lib, kzg_lib):
+    """SolverSettings::useSIMDSolver = false on a 1,500-body pile: islands large enough for the
+    CTA-wide schedule and solve, 150 steps bit-exact against the oracle's scalar sweep."""
+    from kizuriphysics3d_gb300 import World, resolve, scenes
+    sc = scenes.pile(1500, seed=99, extent=6.0, y_range=(1.0, 20.0))
+    sc.flags |= scenes.WORLD_FLAG_SCALAR_SOLVER
+    res = resolve(sc)
+    ow = oracle_lib.OracleWorld(sc.to_bytes(), oracle_blob(sc, res), oracle_lib.PAIRS_CANONICAL, threads=8)
+    with World(sc, resolved=res) as gw:
+        for s in range(150):
+            ow.step(np.float32(sc.dt))
+            gw.step_fixed()
+        assert np.array_equal(bits(gw.state()), bits(ow.state()))
+        st, o = gw.get_stats(), ow.stats()
+        assert st["num_batches"] == 0
+        assert st["point_velocity_iterations"] == o["point_velocity_iterations"]
+
+
+@pytest.mark.parametrize("scalar", [False, True])
+def test_mode_b_settled_full_pile(scalar, oracle_lib, kzg_lib):
     """The 20,000-body random convex pile at its settled state (the bench snapshot): one giant
     island of ~100k contact points, so the schedule's open-batch table compacts and the solve runs
     the in-place big-island kernel.  Two steps, bit-exact against the oracle."""
@@ -99,6 +119,8 @@ def test_mode_b_settled_full_pile(oracle_lib, kzg_lib):
     from kizuriphysics3d_gb300 import World, resolve, scenes
     snap = os.path.join(os.path.dirname(__file__), "..", "kizuriphysics3d_gb300", "data", "pile20000_step600.npz")
     sc = scenes.pile(20000, seed=1234)
+    if scalar:  # the scalar solver's velocity levels through the same kernels
+        sc.flags |= scenes.WORLD_FLAG_SCALAR_SOLVER
     with np.load(snap) as z:
         state = z["state"]
     for b, st in zip(sc.bodies, state):
