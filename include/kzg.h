@@ -192,6 +192,9 @@ typedef struct {
  * by its CTA after the wait, so the step completes with the same result: the bit is reported in
  * kzg_stats.device_error and the step still returns KZG_OK. */
 #define KZG_DEVERR_WAIT 16u
+/* A tensor-core wait of the learned warm start gave up: the tiles it was running got no
+ * prediction (their points keep the plain warm start) and the call returns KZG_ERR_DEVICE. */
+#define KZG_DEVERR_MMA 32u
 
 /* ---- lifecycle (PhysicsWorld ctor/dtor, PhysicsWorld.cpp:64-78) ----------------------------- */
 kzg_status kzg_create(const kzg_config* cfg, kzg_ctx** out);

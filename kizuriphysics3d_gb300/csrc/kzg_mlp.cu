@@ -4,7 +4,9 @@
 // within 0.1 m, else with zero (BuildContactConstraints, PhysicsWorld.cpp:518-529).  With a model
 // loaded and enabled, the zero is replaced by the prediction of a small MLP: 24 features of the
 // prepared contact row -> 64 -> 64 -> 3 (ReLU), BF16 weights and activations, FP32 accumulation on
-// the tensor cores (mma.sync m16n8k16 bf16).  The network predicts the impulses divided by the row
+// the tensor cores: the forward pass of the in-step inference on tcgen05 (UMMA 128 x N x 16, operands
+// in shared memory, accumulators in tensor memory), the training pass on mma.sync m16n8k16.  The
+// network predicts the impulses divided by the row
 // effective masses (a velocity, m/s; learned through asinh, see kTargetScale); the impulse is the
 // prediction times the effective mass, clamped into the friction cone.  The solver then runs unchanged, so the solution still converges
 // to the same tolerance - the prediction only changes where it starts.
@@ -142,6 +144,215 @@ __device__ void forward_rows(bf16* X, bf16* H1, bf16* H2, const bf16* W1, const 
     __syncwarp();
 }
 
+// ---- forward pass on tcgen05 ----------------------------------------------------------------
+// One CTA of 128 threads runs a 128-sample tile: three UMMAs of M = 128 (one sample per TMEM lane)
+// issued by one thread, X (128 x 32) * W1^T -> 64 columns, H1 (128 x 64) * W2^T -> 64 columns,
+// H2 * W3^T -> 16 columns (3 used), bf16 operands, f32 accumulators in 128 TMEM columns (D1 at 0,
+// D2 at 64, D3 at 0 again once D1 is read).  Thread t reads TMEM lane t (warp w owns lanes
+// 32w..32w+31), applies bias and ReLU and writes its row of the next operand.
+//
+// Operands sit in shared memory in the canonical K-major layout without swizzle: 8 x 8 bf16 core
+// matrices of 128 contiguous bytes (8 rows of 16 bytes), the core matrices of one 8-row group
+// adjacent along K (leading byte offset 128), the 8-row groups K / 8 x 128 bytes apart (stride byte
+// offset).  One UMMA consumes K = 16, two core matrices; the next starts 256 bytes further.
+constexpr uint32_t kTmemCols = 128;
+constexpr uint32_t kMmaSpins = 1u << 20;  // mbarrier polls before a tile gives up (KZG_DEVERR_MMA)
+
+struct MlpSmemTc {
+    alignas(128) unsigned char X[kTile * 32 * 2];
+    alignas(128) unsigned char H1[kTile * kH * 2];
+    alignas(128) unsigned char H2[kTile * kH * 2];
+    alignas(128) unsigned char W1[kH * 32 * 2];
+    alignas(128) unsigned char W2[kH * kH * 2];
+    alignas(128) unsigned char W3[16 * kH * 2];
+    float b1[kH], b2[kH], b3[16];
+    alignas(8) unsigned long long mbar;
+    uint32_t tmem;
+};
+
+// Byte offset of element (r, k) of an operand with K columns in the layout above.
+__device__ __forceinline__ uint32_t umma_off(int r, int k, int K) {
+    return (uint32_t)(((((r >> 3) * (K >> 3)) + (k >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1));
+}
+
+// Shared-memory matrix descriptor: start address >> 4 (bits 0-13), leading byte offset >> 4
+// (16-29), stride byte offset >> 4 (32-45), descriptor version 1 (46-47), base offset 0, no
+// swizzle (61-63 = 0).
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, int K) {
+    const uint64_t lbo = 128u, sbo = (uint64_t)(K >> 3) * 128u;
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((lbo >> 4) << 16) | ((sbo >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: D f32 (bits 4-5 = 1), A and B bf16 (7-9 = 1, 10-12 = 1), both
+// K-major (15, 16 = 0), N >> 3 (17-22), M >> 4 (24-28) with M = 128.
+__host__ __device__ constexpr uint32_t umma_idesc(uint32_t n) { return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24); }
+static_assert(umma_idesc(64) == 0x08100490u && umma_idesc(16) == 0x08040490u, "instruction descriptors");
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, bool acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        :: "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(acc ? 1u : 0u) : "memory");
+}
+
+// Operand stores (generic proxy) made visible to the tensor core (async proxy), then a CTA barrier
+// ordered with the tcgen05 operations before and after it.
+__device__ __forceinline__ void tc_sync() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Thread 0 issues one layer's UMMAs (K / 16 of them) and commits them to the CTA's mbarrier.
+__device__ __forceinline__ void tc_layer(uint32_t d_tmem, const unsigned char* A, const unsigned char* W, int K,
+                                         uint32_t n, unsigned long long* mbar) {
+    if (threadIdx.x == 0) {
+        const uint32_t a0 = smem_u32(A), w0 = smem_u32(W);
+        for (int j = 0; j < K / 16; ++j)
+            umma(d_tmem, umma_desc(a0 + 256u * j, K), umma_desc(w0 + 256u * j, K), umma_idesc(n), j > 0);
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                     :: "r"(smem_u32(mbar)) : "memory");
+    }
+}
+
+// Waits for the committed UMMAs (bounded); false when the wait gave up.
+__device__ __forceinline__ bool tc_wait(unsigned long long* mbar, uint32_t& phase) {
+    const uint32_t a = smem_u32(mbar);
+    uint32_t done = 0;
+    for (uint32_t n = 0; n < kMmaSpins && !done; ++n)
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done) : "r"(a), "r"(phase) : "memory");
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    return __syncthreads_and(done != 0) != 0;
+}
+
+// 16 accumulator columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr) : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Epilogue of a hidden layer: this thread's 64 accumulators + bias, ReLU, bf16, into row t of H.
+__device__ __forceinline__ void tc_hidden(uint32_t taddr, const float* bias, unsigned char* H) {
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int c0 = 0; c0 < kH; c0 += 16) {
+        float v[16];
+        tmem_ld16(taddr + (uint32_t)c0, v);
+#pragma unroll
+        for (int h = 0; h < 16; h += 8) {
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const __nv_bfloat162 p = __floats2bfloat162_rn(fmaxf(v[h + 2 * q] + bias[c0 + h + 2 * q], 0.0f),
+                                                               fmaxf(v[h + 2 * q + 1] + bias[c0 + h + 2 * q + 1], 0.0f));
+                w[q] = *reinterpret_cast<const uint32_t*>(&p);
+            }
+            *reinterpret_cast<uint4*>(H + umma_off(t, c0 + h, kH)) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    }
+}
+
+// bf16 weights in the UMMA layout (W1 padded to K = 32, W3 to 16 rows) and the biases.
+__device__ void stage_weights_tc(const float* __restrict__ th, MlpSmemTc& S, int tid) {
+    for (int i = tid; i < kH * 32; i += kMlpThreads) {
+        const int n = i >> 5, k = i & 31;
+        *reinterpret_cast<bf16*>(S.W1 + umma_off(n, k, 32)) = __float2bfloat16_rn(k < kF ? th[kOffW1 + n * kF + k] : 0.0f);
+    }
+    for (int i = tid; i < kH * kH; i += kMlpThreads)
+        *reinterpret_cast<bf16*>(S.W2 + umma_off(i >> 6, i & 63, kH)) = __float2bfloat16_rn(th[kOffW2 + i]);
+    for (int i = tid; i < 16 * kH; i += kMlpThreads) {
+        const int n = i >> 6, k = i & 63;
+        *reinterpret_cast<bf16*>(S.W3 + umma_off(n, k, kH)) = __float2bfloat16_rn(n < kO ? th[kOffW3 + n * kH + k] : 0.0f);
+    }
+    for (int i = tid; i < kH; i += kMlpThreads) {
+        S.b1[i] = th[kOffB1 + i];
+        S.b2[i] = th[kOffB2 + i];
+    }
+    if (tid < 16) S.b3[tid] = tid < kO ? th[kOffB3 + tid] : 0.0f;
+}
+
+// This thread's row of X (24 normalised features, zero-padded to 32; f = nullptr: a zero row).
+__device__ __forceinline__ void tc_stage_row(MlpSmemTc& S, const float* f, const float* __restrict__ norm) {
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int k0 = 0; k0 < 32; k0 += 8) {
+        uint32_t w[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int k = k0 + 2 * q;
+            const float x0 = (f && k < kF) ? (f[k] - norm[k]) * norm[kF + k] : 0.0f;
+            const float x1 = (f && k + 1 < kF) ? (f[k + 1] - norm[k + 1]) * norm[kF + k + 1] : 0.0f;
+            const __nv_bfloat162 p = __floats2bfloat162_rn(x0, x1);
+            w[q] = *reinterpret_cast<const uint32_t*>(&p);
+        }
+        *reinterpret_cast<uint4*>(S.X + umma_off(t, k0, 32)) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
+// TMEM allocation (warp 0) and the mbarrier, once per CTA; returns the TMEM base address.
+__device__ uint32_t tc_begin(MlpSmemTc& S) {
+    if (threadIdx.x < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(&S.tmem)), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&S.mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    return S.tmem;
+}
+
+__device__ void tc_end(MlpSmemTc& S, uint32_t tmem) {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (threadIdx.x < 32)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+// The forward pass of the tile staged in S.X; y: this thread's 3 outputs.  False (the CTA stops
+// using the tensor core) when a wait gave up; the caller then raises KZG_DEVERR_MMA.
+__device__ bool forward_tc(MlpSmemTc& S, uint32_t tmem, uint32_t& phase, float (&y)[kO]) {
+    const uint32_t lane_base = tmem + ((uint32_t)(threadIdx.x & ~31u) << 16);
+    tc_sync();
+    tc_layer(tmem, S.X, S.W1, 32, kH, &S.mbar);
+    if (!tc_wait(&S.mbar, phase)) return false;
+    tc_hidden(lane_base, S.b1, S.H1);
+    tc_sync();
+    tc_layer(tmem + 64u, S.H1, S.W2, kH, kH, &S.mbar);
+    if (!tc_wait(&S.mbar, phase)) return false;
+    tc_hidden(lane_base + 64u, S.b2, S.H2);
+    tc_sync();
+    tc_layer(tmem, S.H2, S.W3, kH, 16, &S.mbar);
+    if (!tc_wait(&S.mbar, phase)) return false;
+    float v[16];
+    tmem_ld16(lane_base, v);
+#pragma unroll
+    for (int q = 0; q < kO; ++q) y[q] = v[q] + S.b3[q];
+    return true;
+}
+
 // ---- features ------------------------------------------------------------------------------
 // 24 features of a prepared contact row that missed the cache, in the contact frame (n, t1, t2):
 //   0 normal velocity  1-2 tangential velocities  3 penetration depth
@@ -199,12 +410,16 @@ struct StepView {
 
 // ---- inference: warm start of the cache misses --------------------------------------------
 __global__ void __launch_bounds__(kMlpThreads) k_mlp_infer(StepView v, const float* __restrict__ theta,
-                                                        const float* __restrict__ norm, float blend_n, float blend_t) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    MlpSmemFwd& S = *reinterpret_cast<MlpSmemFwd*>(smem_raw);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    stage_weights(theta, S.W1, S.W2, S.W3, S.b1, S.b2, S.b3, tid);
+                                                        const float* __restrict__ norm, float blend_n, float blend_t,
+                                                        uint32_t* err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    MlpSmemTc& S = *reinterpret_cast<MlpSmemTc*>(smem_raw);
+    const int tid = threadIdx.x;
     const uint32_t nmiss = v.cnt->nmiss;
+    if (blockIdx.x * kTile >= nmiss) return;  // the whole CTA: no tile, no tensor memory
+    stage_weights_tc(theta, S, tid);
+    const uint32_t tmem = tc_begin(S);
+    uint32_t phase = 0;
     for (uint32_t base = blockIdx.x * kTile; base < nmiss; base += gridDim.x * kTile) {
         const uint32_t k = base + tid;
         uint32_t row = 0;
@@ -213,21 +428,20 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_infer(StepView v, const flo
             const uint32_t c = row >> 2;
             float f[kF];
             row_features(v.b, v.r, v.con_a[c], v.con_b[c], row, v.miss_prior[k], v.g, v.dt, f);
-            for (int i = 0; i < kF; ++i) S.X[tid * SX + i] = __float2bfloat16_rn((f[i] - norm[i]) * norm[kF + i]);
+            tc_stage_row(S, f, norm);
         } else {
-            for (int i = 0; i < kF; ++i) S.X[tid * SX + i] = __float2bfloat16_rn(0.0f);
+            tc_stage_row(S, nullptr, norm);
         }
-        for (int i = kF; i < 32; ++i) S.X[tid * SX + i] = __float2bfloat16_rn(0.0f);
-        __syncthreads();
-        forward_rows(S.X, S.H1, S.H2, S.W1, S.W2, S.W3, S.b1, S.b2, S.b3, S.Y, nullptr, nullptr, warp, lane);
-        __syncthreads();
+        float y[kO];
+        if (!forward_tc(S, tmem, phase, y)) {
+            if (tid == 0) atomicOr(err, KZG_DEVERR_MMA);
+            break;
+        }
         if (k < nmiss) {
             const float4 m = v.r.mass[row];
             const float fric = v.r.t1[row].w;
-            float y[3];
             for (int q = 0; q < 3; ++q)
-                y[q] = (q == 0 ? blend_n : blend_t) * kTargetScale *
-                       sinhf(fminf(fmaxf(S.Y[tid * 4 + q], -kOutLimit), kOutLimit));
+                y[q] = (q == 0 ? blend_n : blend_t) * kTargetScale * sinhf(fminf(fmaxf(y[q], -kOutLimit), kOutLimit));
             const float ni = fmaxf(y[0] * m.x, 0.0f);
             const float mf = fric * ni;
             const float t1 = fminf(fmaxf(y[1] * m.y, -mf), mf);
@@ -235,8 +449,8 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_infer(StepView v, const flo
             const float4 im = v.r.imp[row];
             v.r.imp[row] = make_float4(ni, t1, t2, im.w);
         }
-        __syncthreads();
     }
+    tc_end(S, tmem);
 }
 
 // ---- logging: features before the solve, converged impulses after it ----------------------
@@ -309,7 +523,7 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_train(const float* __restri
                                                         const float* __restrict__ ds, uint32_t first, uint32_t count,
                                                         float inv_nvalid, float tau, float* __restrict__ part,
                                                         float* __restrict__ part_loss) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     MlpSmemTrain& S = *reinterpret_cast<MlpSmemTrain*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
     stage_weights(theta, S.f.W1, S.f.W2, S.f.W3, S.f.b1, S.f.b2, S.f.b3, tid);
@@ -495,24 +709,30 @@ __global__ void k_mlp_adam(float* __restrict__ theta, float* __restrict__ m, flo
     theta[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + 1e-8f);
 }
 
-// Forward only over dataset samples (predictions for tests).
+// Forward only over dataset samples (predictions for tests), on the same tensor-core path.
 __global__ void __launch_bounds__(kMlpThreads) k_mlp_predict(const float* __restrict__ theta, const float* __restrict__ norm,
                                                           const float* __restrict__ ds, uint32_t first, uint32_t count,
-                                                          float* __restrict__ out) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    MlpSmemFwd& S = *reinterpret_cast<MlpSmemFwd*>(smem_raw);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    stage_weights(theta, S.W1, S.W2, S.W3, S.b1, S.b2, S.b3, tid);
+                                                          float* __restrict__ out, uint32_t* err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    MlpSmemTc& S = *reinterpret_cast<MlpSmemTc*>(smem_raw);
+    const int tid = threadIdx.x;
+    stage_weights_tc(theta, S, tid);
+    const uint32_t tmem = tc_begin(S);
+    uint32_t phase = 0;
     const uint32_t s = blockIdx.x * kTile + tid;
     const bool valid = s < count;
+    float f[kF];
     const float* rec = ds + (size_t)(first + (valid ? s : 0)) * kLogFloats;
-    for (int i = 0; i < 32; ++i)
-        S.X[tid * SX + i] = __float2bfloat16_rn((valid && i < kF) ? (rec[i] - norm[i]) * norm[kF + i] : 0.0f);
-    __syncthreads();
-    forward_rows(S.X, S.H1, S.H2, S.W1, S.W2, S.W3, S.b1, S.b2, S.b3, S.Y, nullptr, nullptr, warp, lane);
-    __syncthreads();
-    if (valid)
-        for (int q = 0; q < kO; ++q) out[(size_t)s * kO + q] = S.Y[tid * 4 + q];
+    for (int i = 0; i < kF; ++i) f[i] = rec[i];
+    tc_stage_row(S, valid ? f : nullptr, norm);
+    float y[kO];
+    if (forward_tc(S, tmem, phase, y)) {
+        if (valid)
+            for (int q = 0; q < kO; ++q) out[(size_t)s * kO + q] = y[q];
+    } else if (tid == 0) {
+        atomicOr(err, KZG_DEVERR_MMA);
+    }
+    tc_end(S, tmem);
 }
 
 }  // namespace
@@ -533,9 +753,9 @@ cudaError_t mlp_configure_kernels() {
     cudaError_t e = cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)sizeof(MlpSmemTrain));
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmemFwd));
+    e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmemTc));
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_mlp_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmemFwd));
+    return cudaFuncSetAttribute(k_mlp_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmemTc));
 }
 
 static kzg_status mlp_alloc(Ctx& ctx) {
@@ -701,10 +921,19 @@ kzg_status mlp_predict(Ctx& ctx, uint32_t first, uint32_t count, float* out) {
         M.out_cap = count;
     }
     const uint32_t nblk = (count + kTile - 1) / kTile;
-    k_mlp_predict<<<nblk, kMlpThreads, sizeof(MlpSmemFwd), ctx.stream>>>(M.theta, M.norm, M.ds, first, count, M.out);
+    uint32_t* err = &ctx.dcnt->error;
+    k_mlp_predict<<<nblk, kMlpThreads, sizeof(MlpSmemTc), ctx.stream>>>(M.theta, M.norm, M.ds, first, count, M.out, err);
     MLP_CK(cudaGetLastError());
     MLP_CK(cudaMemcpyAsync(out, M.out, sizeof(float) * kO * (size_t)count, cudaMemcpyDeviceToHost, ctx.stream));
+    uint32_t e = 0;
+    MLP_CK(cudaMemcpyAsync(&e, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx.stream));
     MLP_CK(cudaStreamSynchronize(ctx.stream));
+    if (e & KZG_DEVERR_MMA) {
+        const uint32_t keep = e & ~KZG_DEVERR_MMA;
+        MLP_CK(cudaMemcpy(err, &keep, sizeof(uint32_t), cudaMemcpyHostToDevice));
+        ctx.err = "mlp: a tensor-core wait gave up (KZG_DEVERR_MMA)";
+        return KZG_ERR_DEVICE;
+    }
     return KZG_OK;
 }
 
@@ -724,8 +953,8 @@ uint32_t mlp_after_prepare(Ctx& ctx, float dt) {
     }
     if (M.enabled && M.have) {
         const unsigned grid = std::max(1u, std::min((rows + kTile - 1) / kTile, 152u * 4u));
-        k_mlp_infer<<<grid, kMlpThreads, sizeof(MlpSmemFwd), ctx.stream>>>(step_view(ctx, dt), M.theta, M.norm,
-                                                                          M.blend_n, M.blend_t);
+        k_mlp_infer<<<grid, kMlpThreads, sizeof(MlpSmemTc), ctx.stream>>>(step_view(ctx, dt), M.theta, M.norm,
+                                                                         M.blend_n, M.blend_t, &ctx.dcnt->error);
         ++n;
     }
     return n;
