@@ -403,15 +403,60 @@ __device__ uint32_t first_fit_warp(const SchedBufs& S, uint32_t s0, uint32_t s1,
             if (lane == 0) *pub = fb;
         }
     };
+    // The plane's leading contacts (canonical pair order lists a plane's pairs first): every point
+    // holds hub0, so each opens its own batch, the way the slow path below would open it - placed
+    // here 32 constraints at a time.
+    uint32_t sp = s0;  // the first constraint of the main loop
+    while (hub0 != kNone && sp < s1) {
+        const uint32_t t = sp + lane;
+        uint32_t c = 0, bits = 1u, a = 0, b = 0, np = 0, la = kNone, lb = kNone;
+        if (t < s1) {
+            c = S.isl_con[t]; bits = S.con_bits[c]; a = S.con_a[c]; b = S.con_b[c]; np = S.con_np[c];
+            la = S.con_la[c]; lb = S.con_lb[c];
+        }
+        const bool live = t < s1 && !(bits & 1u);
+        const bool plane = live && (a == hub0 || b == hub0);
+        const unsigned stopm = __ballot_sync(full, t < s1 && live && !plane);
+        const uint32_t e = stopm ? (uint32_t)(__ffs(stopm) - 1) : min(32u, s1 - sp);
+        const uint32_t mine = (plane && lane < e) ? np : 0u;
+        uint32_t x = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(full, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        const uint32_t total = __shfl_sync(full, x, 31);
+        if (ns + total > kFfSlots - 1024u) return kNone;
+        const uint32_t off = x - mine;
+        const uint32_t code = mine ? ff_code(T, a == hub0 ? b : a, a == hub0 ? lb : la, nloc) : 0u;
+        for (uint32_t p = 0; p < mine; ++p) {
+            const uint32_t sl = ns + off + p, j = nbt + off + p;
+            T.bid[sl] = j;
+            T.bod0[sl] = code | 0xFFFF0000u;
+            T.bod1[sl] = 0xFFFFFFFFu;
+            T.bod2[sl] = 0xFFFFFFFFu;
+            T.cnt[sl] = (uint8_t)(1u | kFfH0);
+            uint32_t* r = rec(S, rb + j);
+            r[3] = 1;
+            r[12] = 4u * c + p;
+            T.list1[nl1 + off + p] = (uint16_t)sl;
+        }
+        ns += total;
+        nbt += total;
+        nl1 += total;
+        sp += e;
+        if (stopm) break;
+    }
+    __syncwarp();
     // pipeline: id of the constraint two windows ahead, fields of the next window
     auto load_id = [&](uint32_t w0) -> uint32_t { return w0 + lane < s1 ? S.isl_con[w0 + lane] : kNone; };
-    uint32_t nx_c = load_id(s0), nx_bits = 1u, nx_a = 0, nx_b = 0, nx_np = 0, nx_la = kNone, nx_lb = kNone;
+    uint32_t nx_c = load_id(sp), nx_bits = 1u, nx_a = 0, nx_b = 0, nx_np = 0, nx_la = kNone, nx_lb = kNone;
     if (nx_c != kNone) {
         nx_bits = S.con_bits[nx_c]; nx_a = S.con_a[nx_c]; nx_b = S.con_b[nx_c]; nx_np = S.con_np[nx_c];
         nx_la = S.con_la[nx_c]; nx_lb = S.con_lb[nx_c];
     }
-    uint32_t id2 = load_id(s0 + 32);
-    for (uint32_t w0 = s0; w0 < s1; w0 += 32) {
+    uint32_t id2 = load_id(sp + 32);
+    for (uint32_t w0 = sp; w0 < s1; w0 += 32) {
         const uint32_t mc = nx_c, mbits = nx_bits, ma = nx_a, mb = nx_b, mnp = nx_np, mla = nx_la, mlb = nx_lb;
         nx_c = id2;  // fields of the next window start loading now
         nx_bits = 1u; nx_np = 0; nx_la = kNone; nx_lb = kNone;
