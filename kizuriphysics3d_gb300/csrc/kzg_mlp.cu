@@ -4,12 +4,12 @@
 // within 0.1 m, else with zero (BuildContactConstraints, PhysicsWorld.cpp:518-529).  With a model
 // loaded and enabled, the zero is replaced by the prediction of a small MLP: 24 features of the
 // prepared contact row -> 64 -> 64 -> 3 (ReLU), BF16 weights and activations, FP32 accumulation on
-// the tensor cores: the forward pass of the in-step inference on tcgen05 (UMMA 128 x N x 16, operands
-// in shared memory, accumulators in tensor memory), the training pass on mma.sync m16n8k16.  The
-// network predicts the impulses divided by the row
+// the tensor cores (tcgen05: UMMA 128 x N x 16 from shared-memory operands into tensor memory, for
+// the in-step inference and for training).  The network predicts the impulses divided by the row
 // effective masses (a velocity, m/s; learned through asinh, see kTargetScale); the impulse is the
-// prediction times the effective mass, clamped into the friction cone.  The solver then runs unchanged, so the solution still converges
-// to the same tolerance - the prediction only changes where it starts.
+// prediction times the effective mass, clamped into the friction cone.  The solver then runs
+// unchanged, so the solution still converges to the same tolerance - the prediction only changes
+// where it starts.
 //
 // The same translation unit holds the training path (all on the GPU): logging of features and
 // converged impulses during a step, and one Adam step = forward + backward over a batch of logged
@@ -40,109 +40,7 @@ constexpr int kTile = 128;  // samples per CTA (4 warps x 32 rows)
 constexpr int kMlpThreads = 128;
 constexpr int kLogFloats = KZG_MLP_LOG_FLOATS;  // 24 features + 3 targets + 3 masks
 
-// shared-memory strides (bf16 elements), padded by 8 to spread banks
-constexpr int SX = 40, SH = 72, ST = 136, SY = 24;
-
 typedef __nv_bfloat16 bf16;
-
-__device__ __forceinline__ uint32_t ld2(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
-
-// D(16x8) += A(16x16, row-major) * B(16x8); A rows at a (lda), B stored as 8 rows of K (ldb).
-__device__ __forceinline__ void mma_16x8x16(float c[4], const bf16* a, int lda, const bf16* b, int ldb, int lane) {
-    const int g = lane >> 2, t = lane & 3;
-    const uint32_t a0 = ld2(a + g * lda + 2 * t), a1 = ld2(a + (g + 8) * lda + 2 * t);
-    const uint32_t a2 = ld2(a + g * lda + 2 * t + 8), a3 = ld2(a + (g + 8) * lda + 2 * t + 8);
-    const uint32_t b0 = ld2(b + g * ldb + 2 * t), b1 = ld2(b + g * ldb + 2 * t + 8);
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-// C tile (16 x 8*NT) = A (16 x K) * B^T where B is stored as rows of K; K a multiple of 16.
-template <int NT>
-__device__ __forceinline__ void warp_gemm(float (&c)[NT][4], const bf16* a, int lda, const bf16* b, int ldb, int K,
-                                          int lane) {
-#pragma unroll
-    for (int n = 0; n < NT; ++n) c[n][0] = c[n][1] = c[n][2] = c[n][3] = 0.0f;
-    for (int k = 0; k < K; k += 16)
-#pragma unroll
-        for (int n = 0; n < NT; ++n) mma_16x8x16(c[n], a + k, lda, b + n * 8 * ldb + k, ldb, lane);
-}
-
-struct MlpSmemFwd {
-    bf16 X[kTile * SX];
-    bf16 H1[kTile * SH];
-    bf16 H2[kTile * SH];
-    bf16 W1[kH * SX];
-    bf16 W2[kH * SH];
-    bf16 W3[8 * SH];
-    float b1[kH], b2[kH], b3[8];
-    float Y[kTile * 4];
-};
-
-// Stage the bf16 weights (W1 padded to K = 32, W3 padded to 8 rows) and biases.
-__device__ void stage_weights(const float* __restrict__ th, bf16* W1, bf16* W2, bf16* W3, float* b1, float* b2,
-                              float* b3, int tid) {
-    for (int i = tid; i < kH * 32; i += kMlpThreads) {
-        const int r = i >> 5, k = i & 31;
-        W1[r * SX + k] = __float2bfloat16_rn(k < kF ? th[kOffW1 + r * kF + k] : 0.0f);
-    }
-    for (int i = tid; i < kH * kH; i += kMlpThreads) W2[(i >> 6) * SH + (i & 63)] = __float2bfloat16_rn(th[kOffW2 + i]);
-    for (int i = tid; i < 8 * kH; i += kMlpThreads) {
-        const int r = i >> 6, k = i & 63;
-        W3[r * SH + k] = __float2bfloat16_rn(r < kO ? th[kOffW3 + r * kH + k] : 0.0f);
-    }
-    for (int i = tid; i < kH; i += kMlpThreads) {
-        b1[i] = th[kOffB1 + i];
-        b2[i] = th[kOffB2 + i];
-    }
-    if (tid < 8) b3[tid] = tid < kO ? th[kOffB3 + tid] : 0.0f;
-}
-
-// Forward pass of the warp's 32 rows: X -> H1 -> H2 -> Y (fp32, 3 of 4 columns used).
-// Optional transposed copies (feature-major) of H1/H2 for the weight gradients.
-__device__ void forward_rows(bf16* X, bf16* H1, bf16* H2, const bf16* W1, const bf16* W2, const bf16* W3,
-                             const float* b1, const float* b2, const float* b3, float* Y, bf16* H1t, bf16* H2t,
-                             int warp, int lane) {
-    const int g = lane >> 2, t = lane & 3;
-    for (int layer = 0; layer < 2; ++layer) {
-        const bf16* A = layer == 0 ? X : H1;
-        const int lda = layer == 0 ? SX : SH, K = layer == 0 ? 32 : kH;
-        const bf16* W = layer == 0 ? W1 : W2;
-        const int ldw = layer == 0 ? SX : SH;
-        const float* bias = layer == 0 ? b1 : b2;
-        bf16* Hout = layer == 0 ? H1 : H2;
-        bf16* Ht = layer == 0 ? H1t : H2t;
-        for (int mt = 0; mt < 2; ++mt) {
-            const int r0 = warp * 32 + mt * 16;
-            float c[8][4];
-            warp_gemm<8>(c, A + r0 * lda, lda, W, ldw, K, lane);
-#pragma unroll
-            for (int n = 0; n < 8; ++n)
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int row = r0 + g + (q >> 1) * 8, col = n * 8 + 2 * t + (q & 1);
-                    const bf16 h = __float2bfloat16_rn(fmaxf(c[n][q] + bias[col], 0.0f));
-                    Hout[row * SH + col] = h;
-                    if (Ht) Ht[col * ST + row] = h;
-                }
-        }
-        __syncwarp();
-    }
-    for (int mt = 0; mt < 2; ++mt) {
-        const int r0 = warp * 32 + mt * 16;
-        float c[1][4];
-        warp_gemm<1>(c, H2 + r0 * SH, SH, W3, SH, kH, lane);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int row = r0 + g + (q >> 1) * 8, col = 2 * t + (q & 1);
-            if (col < 4) Y[row * 4 + col] = c[0][q] + b3[col];
-        }
-    }
-    __syncwarp();
-}
 
 // ---- forward pass on tcgen05 ----------------------------------------------------------------
 // One CTA of 128 threads runs a 128-sample tile: three UMMAs of M = 128 (one sample per TMEM lane)
@@ -207,16 +105,28 @@ __device__ __forceinline__ void tc_sync() {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// Thread 0 issues one layer's UMMAs (K / 16 of them) and commits them to the CTA's mbarrier.
-__device__ __forceinline__ void tc_layer(uint32_t d_tmem, const unsigned char* A, const unsigned char* W, int K,
-                                         uint32_t n, unsigned long long* mbar) {
+// Thread 0: the UMMAs of one product D (128 x n, at d_tmem) = A (128 x K) * B^T (B: n rows of K),
+// K / 16 of them, accumulated in order.
+__device__ __forceinline__ void tc_chain(uint32_t d_tmem, const unsigned char* A, const unsigned char* B, int K,
+                                         uint32_t n) {
     if (threadIdx.x == 0) {
-        const uint32_t a0 = smem_u32(A), w0 = smem_u32(W);
+        const uint32_t a0 = smem_u32(A), b0 = smem_u32(B);
         for (int j = 0; j < K / 16; ++j)
-            umma(d_tmem, umma_desc(a0 + 256u * j, K), umma_desc(w0 + 256u * j, K), umma_idesc(n), j > 0);
+            umma(d_tmem, umma_desc(a0 + 256u * j, K), umma_desc(b0 + 256u * j, K), umma_idesc(n), j > 0);
+    }
+}
+
+// Thread 0: the CTA's mbarrier completes once every UMMA it issued so far is done.
+__device__ __forceinline__ void tc_commit(unsigned long long* mbar) {
+    if (threadIdx.x == 0)
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                      :: "r"(smem_u32(mbar)) : "memory");
-    }
+}
+
+__device__ __forceinline__ void tc_layer(uint32_t d_tmem, const unsigned char* A, const unsigned char* W, int K,
+                                         uint32_t n, unsigned long long* mbar) {
+    tc_chain(d_tmem, A, W, K, n);
+    tc_commit(mbar);
 }
 
 // Waits for the committed UMMAs (bounded); false when the wait gave up.
@@ -248,8 +158,10 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Epilogue of a hidden layer: this thread's 64 accumulators + bias, ReLU, bf16, into row t of H.
-__device__ __forceinline__ void tc_hidden(uint32_t taddr, const float* bias, unsigned char* H) {
+// Epilogue of a hidden layer: this thread's 64 accumulators + bias, ReLU, bf16, into row t of H
+// (and, for the weight gradients, into column t of Ht: 64 rows of K = 128 samples).
+__device__ __forceinline__ void tc_hidden(uint32_t taddr, const float* bias, unsigned char* H,
+                                          unsigned char* Ht = nullptr) {
     const int t = threadIdx.x;
 #pragma unroll
     for (int c0 = 0; c0 < kH; c0 += 16) {
@@ -263,6 +175,10 @@ __device__ __forceinline__ void tc_hidden(uint32_t taddr, const float* bias, uns
                 const __nv_bfloat162 p = __floats2bfloat162_rn(fmaxf(v[h + 2 * q] + bias[c0 + h + 2 * q], 0.0f),
                                                                fmaxf(v[h + 2 * q + 1] + bias[c0 + h + 2 * q + 1], 0.0f));
                 w[q] = *reinterpret_cast<const uint32_t*>(&p);
+                if (Ht) {
+                    *reinterpret_cast<__nv_bfloat16*>(Ht + umma_off(c0 + h + 2 * q, t, kTile)) = p.x;
+                    *reinterpret_cast<__nv_bfloat16*>(Ht + umma_off(c0 + h + 2 * q + 1, t, kTile)) = p.y;
+                }
             }
             *reinterpret_cast<uint4*>(H + umma_off(t, c0 + h, kH)) = make_uint4(w[0], w[1], w[2], w[3]);
         }
@@ -306,11 +222,12 @@ __device__ __forceinline__ void tc_stage_row(MlpSmemTc& S, const float* f, const
     }
 }
 
-// TMEM allocation (warp 0) and the mbarrier, once per CTA; returns the TMEM base address.
-__device__ uint32_t tc_begin(MlpSmemTc& S) {
+// TMEM allocation (warp 0; ncols a power of 2 >= 32) and the mbarrier, once per CTA; returns the
+// TMEM base address.
+__device__ uint32_t tc_begin(MlpSmemTc& S, uint32_t ncols = kTmemCols) {
     if (threadIdx.x < 32) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     :: "r"(smem_u32(&S.tmem)), "r"(kTmemCols) : "memory");
+                     :: "r"(smem_u32(&S.tmem)), "r"(ncols) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (threadIdx.x == 0) {
@@ -323,26 +240,28 @@ __device__ uint32_t tc_begin(MlpSmemTc& S) {
     return S.tmem;
 }
 
-__device__ void tc_end(MlpSmemTc& S, uint32_t tmem) {
+__device__ void tc_end(MlpSmemTc& S, uint32_t tmem, uint32_t ncols = kTmemCols) {
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (threadIdx.x < 32)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(ncols) : "memory");
 }
 
 // The forward pass of the tile staged in S.X; y: this thread's 3 outputs.  False (the CTA stops
 // using the tensor core) when a wait gave up; the caller then raises KZG_DEVERR_MMA.
-__device__ bool forward_tc(MlpSmemTc& S, uint32_t tmem, uint32_t& phase, float (&y)[kO]) {
+// H1t, H2t: transposed copies of the hidden layers for the weight gradients, or null.
+__device__ bool forward_tc(MlpSmemTc& S, uint32_t tmem, uint32_t& phase, float (&y)[kO],
+                           unsigned char* H1t = nullptr, unsigned char* H2t = nullptr) {
     const uint32_t lane_base = tmem + ((uint32_t)(threadIdx.x & ~31u) << 16);
     tc_sync();
     tc_layer(tmem, S.X, S.W1, 32, kH, &S.mbar);
     if (!tc_wait(&S.mbar, phase)) return false;
-    tc_hidden(lane_base, S.b1, S.H1);
+    tc_hidden(lane_base, S.b1, S.H1, H1t);
     tc_sync();
     tc_layer(tmem + 64u, S.H1, S.W2, kH, kH, &S.mbar);
     if (!tc_wait(&S.mbar, phase)) return false;
-    tc_hidden(lane_base + 64u, S.b2, S.H2);
+    tc_hidden(lane_base + 64u, S.b2, S.H2, H2t);
     tc_sync();
     tc_layer(tmem, S.H2, S.W3, kH, 16, &S.mbar);
     if (!tc_wait(&S.mbar, phase)) return false;
@@ -487,32 +406,64 @@ __global__ void k_mlp_log_advance(const Counters* cnt, uint32_t* log_n, uint32_t
 }
 
 // ---- training ------------------------------------------------------------------------------
-struct MlpSmemTrain {
-    MlpSmemFwd f;
-    bf16 Xt[32 * ST];
-    bf16 H1t[kH * ST];
-    bf16 H2t[kH * ST];
-    bf16 dZ2[kTile * SH];
-    bf16 dZ2t[kH * ST];
-    bf16 dZ1t[kH * ST];
-    bf16 dY[kTile * SY];
-    bf16 dYt[16 * ST];
-    bf16 W2T[kH * SH];
-    bf16 W3T[kH * SY];
-    float bred[4][kH + kH + 8];
-    float lred[4];
+// ---- training: forward + backward of up to 128 samples per CTA, on tcgen05 -------------------
+// After the forward pass (with transposed copies of X, H1, H2), five more products:
+//   dH2 = dY W3          (128 x 64, K = 16)   -> dZ2 = dH2 * (H2 > 0)
+//   dW3^T = H2^T dY      (64 x 16,  K = 128)
+//   dH1 = dZ2 W2         (128 x 64, K = 64)   -> dZ1 = dH1 * (H1 > 0)
+//   dW2 = dZ2^T H1       (64 x 64,  K = 128)
+//   dW1 = dZ1^T X        (64 x 32,  K = 128)
+// The weight gradients have 64 rows: they run as M = 128 products whose A rows 64-127 are read from
+// the buffer placed after the A operand (their results land in TMEM lanes that are never read).
+// TMEM (256 columns): forward 0-127; dW3^T 0-15, dW1 16-47, dW2 64-127, dH2 128-191, dH1 192-255.
+// Bias gradients and the loss are summed over the samples in a fixed order (deterministic).
+struct MlpSmemTrainTc {
+    MlpSmemTc f;
+    alignas(128) unsigned char dY[kTile * 16 * 2];   // A of dH2 (K = 16)
+    alignas(128) unsigned char W3T[kH * 16 * 2];     // B of dH2: W3^T, 64 rows of K = 16
+    alignas(128) unsigned char dZ2[kTile * kH * 2];  // A of dH1 (K = 64)
+    alignas(128) unsigned char W2T[kH * kH * 2];     // B of dH1: W2^T
+    alignas(128) unsigned char dZ2t[kH * kTile * 2]; // A of dW2 (rows 64-127: dZ1t)
+    alignas(128) unsigned char dZ1t[kH * kTile * 2]; // A of dW1 (rows 64-127: H2t)
+    alignas(128) unsigned char H2t[kH * kTile * 2];  // A of dW3^T (rows 64-127: H1t)
+    alignas(128) unsigned char H1t[kH * kTile * 2];  // B of dW2
+    alignas(128) unsigned char Xt[32 * kTile * 2];   // B of dW1
+    alignas(128) unsigned char dYt[16 * kTile * 2];  // B of dW3^T
+    float col[kTile * (kH + 1)];                     // per-sample values of the bias sums
+    float lred[4], dred[4][kO];
 };
+constexpr uint32_t kTrainTmemCols = 256;
 
-// Column sums over the warp's 16-row tile fragments, in a fixed order (xor tree over the 8 row
-// groups); returns the sum for columns 2t and 2t+1 of n-tile n in lanes with g == 0.
-__device__ __forceinline__ float2 frag_colsum(const float c[4]) {
-    float s0 = c[0] + c[2], s1 = c[1] + c[3];
+__device__ __forceinline__ void st_bf16(unsigned char* base, uint32_t off, float v) {
+    *reinterpret_cast<bf16*>(base + off) = __float2bfloat16_rn(v);
+}
+
+// Epilogue of dH = this thread's 64 accumulators at taddr, masked by the layer's ReLU (H > 0):
+// dZ into row t of dZ (when given), column t of dZt and the bias-sum staging.
+__device__ __forceinline__ void tc_backprop(uint32_t taddr, const unsigned char* H, unsigned char* dZ,
+                                            unsigned char* dZt, float* col) {
+    const int t = threadIdx.x;
 #pragma unroll
-    for (int o = 4; o < 32; o <<= 1) {
-        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    for (int c0 = 0; c0 < kH; c0 += 16) {
+        float v[16];
+        tmem_ld16(taddr + (uint32_t)c0, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int c = c0 + i;
+            const float h = __bfloat162float(*reinterpret_cast<const bf16*>(H + umma_off(t, c, kH)));
+            const float d = h > 0.0f ? v[i] : 0.0f;
+            if (dZ) st_bf16(dZ, umma_off(t, c, kH), d);
+            st_bf16(dZt, umma_off(c, t, kTile), d);
+            col[t * (kH + 1) + c] = d;
+        }
     }
-    return make_float2(s0, s1);
+}
+
+// Fixed-order sum over the 128 samples of column c of the staging (threads 0-63, one column each).
+__device__ __forceinline__ float tc_colsum(const float* col, int c) {
+    float s = 0.0f;
+    for (int t = 0; t < kTile; ++t) s += col[t * (kH + 1) + c];
+    return s;
 }
 
 // One CTA: forward + backward of up to 128 samples; writes its partial gradient (kP floats) and
@@ -522,167 +473,118 @@ __device__ __forceinline__ float2 frag_colsum(const float c[4]) {
 __global__ void __launch_bounds__(kMlpThreads) k_mlp_train(const float* __restrict__ theta, const float* __restrict__ norm,
                                                         const float* __restrict__ ds, uint32_t first, uint32_t count,
                                                         float inv_nvalid, float tau, float* __restrict__ part,
-                                                        float* __restrict__ part_loss) {
+                                                        float* __restrict__ part_loss, uint32_t* err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    MlpSmemTrain& S = *reinterpret_cast<MlpSmemTrain*>(smem_raw);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
-    stage_weights(theta, S.f.W1, S.f.W2, S.f.W3, S.f.b1, S.f.b2, S.f.b3, tid);
-    for (int i = tid; i < kH * kH; i += kMlpThreads) {  // W2T[i][j] = W2[j][i]
-        const int j = i >> 6, ii = i & 63;
-        S.W2T[ii * SH + j] = __float2bfloat16_rn(theta[kOffW2 + i]);
-    }
+    MlpSmemTrainTc& S = *reinterpret_cast<MlpSmemTrainTc*>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    stage_weights_tc(theta, S.f, tid);
+    for (int i = tid; i < kH * kH; i += kMlpThreads)  // W2T[n][k] = W2[k][n]
+        st_bf16(S.W2T, umma_off(i & 63, i >> 6, kH), theta[kOffW2 + i]);
     for (int i = tid; i < kH * 16; i += kMlpThreads) {  // W3T[h][o] = W3[o][h], o padded to 16
         const int h = i >> 4, o = i & 15;
-        S.W3T[h * SY + o] = __float2bfloat16_rn(o < kO ? theta[kOffW3 + o * kH + h] : 0.0f);
+        st_bf16(S.W3T, umma_off(h, o, 16), o < kO ? theta[kOffW3 + o * kH + h] : 0.0f);
     }
+    const uint32_t tmem = tc_begin(S.f, kTrainTmemCols);
+    const uint32_t lane_base = tmem + ((uint32_t)(tid & ~31) << 16);
+    uint32_t phase = 0;
     const uint32_t s = blockIdx.x * kTile + tid;
     const bool valid = s < count;
     const float* rec = ds + (size_t)(first + (valid ? s : 0)) * kLogFloats;
-    float tgt[3] = {0, 0, 0}, msk[3] = {0, 0, 0};
-    for (int i = 0; i < 32; ++i) {
-        const float x = (valid && i < kF) ? (rec[i] - norm[i]) * norm[kF + i] : 0.0f;
-        const bf16 xb = __float2bfloat16_rn(x);
-        S.f.X[tid * SX + i] = xb;
-        S.Xt[i * ST + tid] = xb;
-    }
+    float f[kF], tgt[3] = {0, 0, 0}, msk[3] = {0, 0, 0};
+    for (int i = 0; i < kF; ++i) f[i] = rec[i];
     if (valid)
         for (int q = 0; q < 3; ++q) {
             tgt[q] = rec[kF + q];
             msk[q] = rec[kF + 3 + q];
         }
-    __syncthreads();
-    forward_rows(S.f.X, S.f.H1, S.f.H2, S.f.W1, S.f.W2, S.f.W3, S.f.b1, S.f.b2, S.f.b3, S.f.Y, S.H1t, S.H2t, warp,
-                 lane);
-    __syncthreads();
-    // loss and dY (fp32 -> bf16 for the GEMMs; fp32 for the bias gradient)
-    float loss = 0.0f, dy[3];
-    for (int q = 0; q < 3; ++q) {
-        const float e = S.f.Y[tid * 4 + q] - tgt[q];
-        if (tau > 0.0f) {
-            loss += msk[q] * (e > 0.0f ? (1.0f - tau) * e : -tau * e);
-            dy[q] = msk[q] * (e > 0.0f ? (1.0f - tau) : -tau) * inv_nvalid;
-        } else {
-            loss += msk[q] * e * e;
-            dy[q] = msk[q] * 2.0f * e * inv_nvalid;
-        }
-    }
-    for (int o = 0; o < 16; ++o) {
-        const bf16 v = __float2bfloat16_rn(o < 3 ? dy[o] : 0.0f);
-        S.dY[tid * SY + o] = v;
-        S.dYt[o * ST + tid] = v;
-    }
-    {  // fixed-order block sums: loss, db3
-        float l = loss * inv_nvalid, d0 = dy[0], d1 = dy[1], d2 = dy[2];
-        for (int o = 16; o > 0; o >>= 1) {
-            l += __shfl_xor_sync(0xffffffffu, l, o);
-            d0 += __shfl_xor_sync(0xffffffffu, d0, o);
-            d1 += __shfl_xor_sync(0xffffffffu, d1, o);
-            d2 += __shfl_xor_sync(0xffffffffu, d2, o);
-        }
-        if (lane == 0) {
-            S.lred[warp] = l;
-            S.bred[warp][2 * kH + 0] = d0;
-            S.bred[warp][2 * kH + 1] = d1;
-            S.bred[warp][2 * kH + 2] = d2;
-        }
-    }
-    __syncthreads();
+    tc_stage_row(S.f, valid ? f : nullptr, norm);
+    for (int k = 0; k < 32; ++k)
+        st_bf16(S.Xt, umma_off(k, tid, kTile), (valid && k < kF) ? (f[k] - norm[k]) * norm[kF + k] : 0.0f);
     float* P = part + (size_t)blockIdx.x * kP;
-    // dW3 (3 x 64) = dY^T H2: M = 16 (3 used), N = 64 -> warp w takes n-tiles 2w, 2w+1
-    {
-        float c[2][4];
-        warp_gemm<2>(c, S.dYt, ST, S.H2t + (warp * 16) * ST, ST, kTile, lane);
-        for (int n = 0; n < 2; ++n)
-            for (int q = 0; q < 4; ++q) {
-                const int o = g + (q >> 1) * 8, h = warp * 16 + n * 8 + 2 * t + (q & 1);
-                if (o < kO) P[kOffW3 + o * kH + h] = c[n][q];
-            }
-    }
-    // dH2 = dY W3 -> dZ2 = dH2 * (H2 > 0), own rows
-    for (int mt = 0; mt < 2; ++mt) {
-        const int r0 = warp * 32 + mt * 16;
-        float c[8][4];
-        warp_gemm<8>(c, S.dY + r0 * SY, SY, S.W3T, SY, 16, lane);
-        for (int n = 0; n < 8; ++n)
-            for (int q = 0; q < 4; ++q) {
-                const int row = r0 + g + (q >> 1) * 8, col = n * 8 + 2 * t + (q & 1);
-                const bool on = __bfloat162float(S.f.H2[row * SH + col]) > 0.0f;
-                c[n][q] = on ? c[n][q] : 0.0f;
-                const bf16 v = __float2bfloat16_rn(c[n][q]);
-                S.dZ2[row * SH + col] = v;
-                S.dZ2t[col * ST + row] = v;
-            }
-        for (int n = 0; n < 8; ++n) {  // db2 partial of this 16-row tile
-            const float2 cs = frag_colsum(c[n]);
-            if (g == 0) {
-                if (mt == 0) {
-                    S.bred[warp][kH + n * 8 + 2 * t] = cs.x;
-                    S.bred[warp][kH + n * 8 + 2 * t + 1] = cs.y;
-                } else {
-                    S.bred[warp][kH + n * 8 + 2 * t] += cs.x;
-                    S.bred[warp][kH + n * 8 + 2 * t + 1] += cs.y;
-                }
+    bool ok = false;
+    do {
+        float y[kO];
+        if (!forward_tc(S.f, tmem, phase, y, S.H1t, S.H2t)) break;
+        // loss and dY (fp32 for the bias gradient, bf16 for the products)
+        float loss = 0.0f, dy[3];
+        for (int q = 0; q < 3; ++q) {
+            const float e = y[q] - tgt[q];
+            if (tau > 0.0f) {
+                loss += msk[q] * (e > 0.0f ? (1.0f - tau) * e : -tau * e);
+                dy[q] = msk[q] * (e > 0.0f ? (1.0f - tau) : -tau) * inv_nvalid;
+            } else {
+                loss += msk[q] * e * e;
+                dy[q] = msk[q] * 2.0f * e * inv_nvalid;
             }
         }
-    }
-    __syncthreads();
-    // dW2 (64 x 64) = dZ2^T H1: 4 m-tiles x 8 n-tiles, warp w takes m-tile w
-    {
-        float c[8][4];
-        warp_gemm<8>(c, S.dZ2t + (warp * 16) * ST, ST, S.H1t, ST, kTile, lane);
-        for (int n = 0; n < 8; ++n)
-            for (int q = 0; q < 4; ++q) {
-                const int j = warp * 16 + g + (q >> 1) * 8, i = n * 8 + 2 * t + (q & 1);
-                P[kOffW2 + j * kH + i] = c[n][q];
+        for (int o = 0; o < 16; ++o) {
+            const float v = o < 3 ? dy[o] : 0.0f;
+            st_bf16(S.dY, umma_off(tid, o, 16), v);
+            st_bf16(S.dYt, umma_off(o, tid, kTile), v);
+        }
+        {  // loss and db3: warp sums (xor tree), then the four warps in order
+            float l = loss * inv_nvalid, d0 = dy[0], d1 = dy[1], d2 = dy[2];
+            for (int o = 16; o > 0; o >>= 1) {
+                l += __shfl_xor_sync(0xffffffffu, l, o);
+                d0 += __shfl_xor_sync(0xffffffffu, d0, o);
+                d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+                d2 += __shfl_xor_sync(0xffffffffu, d2, o);
             }
-    }
-    // dH1 = dZ2 W2 -> dZ1 = dH1 * (H1 > 0), own rows (transposed copy only)
-    for (int mt = 0; mt < 2; ++mt) {
-        const int r0 = warp * 32 + mt * 16;
-        float c[8][4];
-        warp_gemm<8>(c, S.dZ2 + r0 * SH, SH, S.W2T, SH, kH, lane);
-        for (int n = 0; n < 8; ++n)
-            for (int q = 0; q < 4; ++q) {
-                const int row = r0 + g + (q >> 1) * 8, col = n * 8 + 2 * t + (q & 1);
-                const bool on = __bfloat162float(S.f.H1[row * SH + col]) > 0.0f;
-                c[n][q] = on ? c[n][q] : 0.0f;
-                S.dZ1t[col * ST + row] = __float2bfloat16_rn(c[n][q]);
-            }
-        for (int n = 0; n < 8; ++n) {
-            const float2 cs = frag_colsum(c[n]);
-            if (g == 0) {
-                if (mt == 0) {
-                    S.bred[warp][n * 8 + 2 * t] = cs.x;
-                    S.bred[warp][n * 8 + 2 * t + 1] = cs.y;
-                } else {
-                    S.bred[warp][n * 8 + 2 * t] += cs.x;
-                    S.bred[warp][n * 8 + 2 * t + 1] += cs.y;
-                }
+            if (lane == 0) {
+                S.lred[warp] = l;
+                S.dred[warp][0] = d0;
+                S.dred[warp][1] = d1;
+                S.dred[warp][2] = d2;
             }
         }
-    }
-    __syncthreads();
-    // dW1 (64 x 24) = dZ1^T X: 4 m-tiles x 4 n-tiles (32 columns, 24 kept), warp w takes m-tile w
-    {
-        float c[4][4];
-        warp_gemm<4>(c, S.dZ1t + (warp * 16) * ST, ST, S.Xt, ST, kTile, lane);
-        for (int n = 0; n < 4; ++n)
-            for (int q = 0; q < 4; ++q) {
-                const int i = warp * 16 + g + (q >> 1) * 8, f = n * 8 + 2 * t + (q & 1);
-                if (f < kF) P[kOffW1 + i * kF + f] = c[n][q];
+        tc_sync();
+        tc_chain(tmem + 128u, S.dY, S.W3T, 16, kH);   // dH2
+        tc_chain(tmem, S.H2t, S.dYt, kTile, 16);      // dW3^T
+        tc_commit(&S.f.mbar);
+        if (!tc_wait(&S.f.mbar, phase)) break;
+        tc_backprop(lane_base + 128u, S.f.H2, S.dZ2, S.dZ2t, S.col);
+        if (warp < 2) {  // dW3^T: row h = TMEM lane h
+            float v[16];
+            tmem_ld16(lane_base, v);
+            for (int o = 0; o < kO; ++o) P[kOffW3 + o * kH + tid] = v[o];
+        }
+        tc_sync();
+        if (tid < kH) P[kOffB2 + tid] = tc_colsum(S.col, tid);
+        tc_chain(tmem + 192u, S.dZ2, S.W2T, kH, kH);  // dH1
+        tc_chain(tmem + 64u, S.dZ2t, S.H1t, kTile, kH);  // dW2
+        tc_commit(&S.f.mbar);
+        if (!tc_wait(&S.f.mbar, phase)) break;
+        tc_backprop(lane_base + 192u, S.f.H1, nullptr, S.dZ1t, S.col);
+        if (warp < 2) {  // dW2: row j = TMEM lane j
+#pragma unroll
+            for (int c0 = 0; c0 < kH; c0 += 16) {
+                float v[16];
+                tmem_ld16(lane_base + 64u + (uint32_t)c0, v);
+                for (int i = 0; i < 16; ++i) P[kOffW2 + tid * kH + c0 + i] = v[i];
             }
-    }
-    // bias gradients and loss: sum the four warps in order
-    for (int i = tid; i < kH + kH + kO; i += kMlpThreads) {
-        const float v = ((S.bred[0][i] + S.bred[1][i]) + S.bred[2][i]) + S.bred[3][i];
-        if (i < kH) P[kOffB1 + i] = v;
-        else if (i < 2 * kH) P[kOffB2 + (i - kH)] = v;
-        else P[kOffB3 + (i - 2 * kH)] = v;
-    }
-    if (tid == 0) part_loss[blockIdx.x] = ((S.lred[0] + S.lred[1]) + S.lred[2]) + S.lred[3];
+        }
+        tc_sync();
+        if (tid < kH) P[kOffB1 + tid] = tc_colsum(S.col, tid);
+        tc_chain(tmem + 16u, S.dZ1t, S.Xt, kTile, 32);  // dW1
+        tc_commit(&S.f.mbar);
+        if (!tc_wait(&S.f.mbar, phase)) break;
+        if (warp < 2) {  // dW1: row i = TMEM lane i, 24 of its 32 columns
+#pragma unroll
+            for (int c0 = 0; c0 < 32; c0 += 16) {
+                float v[16];
+                tmem_ld16(lane_base + 16u + (uint32_t)c0, v);
+                for (int i = 0; i < 16; ++i)
+                    if (c0 + i < kF) P[kOffW1 + tid * kF + c0 + i] = v[i];
+            }
+        }
+        if (tid < kO) P[kOffB3 + tid] = ((S.dred[0][tid] + S.dred[1][tid]) + S.dred[2][tid]) + S.dred[3][tid];
+        if (tid == 0) part_loss[blockIdx.x] = ((S.lred[0] + S.lred[1]) + S.lred[2]) + S.lred[3];
+        ok = true;
+    } while (false);
+    if (!ok && tid == 0) atomicOr(err, KZG_DEVERR_MMA);
+    tc_end(S.f, tmem, kTrainTmemCols);
 }
 
-// grad[i] = sum over CTAs of part[cta][i], in CTA order.
 __global__ void k_mlp_reduce(const float* __restrict__ part, const float* __restrict__ part_loss, uint32_t nblk,
                              float* __restrict__ grad, float* __restrict__ loss) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -751,7 +653,7 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_predict(const float* __rest
 
 cudaError_t mlp_configure_kernels() {
     cudaError_t e = cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(MlpSmemTrain));
+                                         (int)sizeof(MlpSmemTrainTc));
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpSmemTc));
     if (e != cudaSuccess) return e;
@@ -873,8 +775,8 @@ static kzg_status mlp_batch_grad(Ctx& ctx, uint32_t first, uint32_t count, float
     const double nvalid = M.ds_valid_prefix[first + count] - M.ds_valid_prefix[first];
     const float inv = nvalid > 0.0 ? (float)(1.0 / nvalid) : 0.0f;
     float* part_loss = M.part + (size_t)nblk * kP;
-    k_mlp_train<<<nblk, kMlpThreads, sizeof(MlpSmemTrain), ctx.stream>>>(M.theta, M.norm, M.ds, first, count, inv,
-                                                                        M.tau, M.part, part_loss);
+    k_mlp_train<<<nblk, kMlpThreads, sizeof(MlpSmemTrainTc), ctx.stream>>>(M.theta, M.norm, M.ds, first, count, inv,
+                                                                          M.tau, M.part, part_loss, &ctx.dcnt->error);
     k_mlp_reduce<<<(kP + 255) / 256, 256, 0, ctx.stream>>>(M.part, part_loss, nblk, M.grad, M.grad + kP);
     MLP_CK(cudaGetLastError());
     if (loss_out) {
