@@ -50,9 +50,6 @@ struct SolveBufs {
     const uint32_t* order;   // largest-first island order taken from shared counters, or null (the lists)
     const uint32_t* jflag;   // per island: 1 when joints share it, or null
     uint32_t warp_bodies;    // islands with at most this many dynamic bodies: warp solve
-    uint32_t scalar;         // SolverSettings::useSIMDSolver = false: every point in island order with
-                             // SolveContactVelocity's rows (the schedule's velocity levels are then the
-                             // warm-start levels)
 };
 
 // The solve kernel an island goes to (the lists the schedule appends to follow the same rule).
@@ -172,7 +169,7 @@ __device__ __forceinline__ void warm_point(const SolveBufs& S, const View& V, ui
 // The normal row's velocity bias: SolveVelocityBatchSIMD adds positionBias or zero to
 // restitutionBias (ContactSolverSIMD.cpp), SolveContactVelocity adds positionBias only under
 // useVelocityBias (ContactSolver.cpp:167-168).
-__device__ __forceinline__ float normal_bias(bool scalar, int vel_bias, const float4& bias) {
+__device__ __forceinline__ float normal_bias(bool scalar, int vel_bias, const float4 bias) {
     if (scalar) return vel_bias ? bias.x + bias.y : bias.x;
     return bias.x + (vel_bias ? bias.y : 0.0f);
 }
@@ -184,6 +181,7 @@ struct VelItem {
     Mat3 IA, IB;
 };
 
+template <bool kScalar>
 __device__ __forceinline__ void load_vel_item(const SolveBufs& S, uint32_t row, uint32_t A, uint32_t B, uint32_t la,
                                               uint32_t lb, VelItem& it) {
     it.row = row; it.A = A; it.B = B; it.la = la; it.lb = lb;
@@ -194,7 +192,8 @@ __device__ __forceinline__ void load_vel_item(const SolveBufs& S, uint32_t row, 
     it.t2 = S.r.t2[row];
     it.m = S.r.mass[row];
     it.im = S.r.imp[row];
-    it.nb = normal_bias(S.scalar != 0u, S.vel_bias, S.r.bias[row]);
+    const float4 bias = S.r.bias[row];  // one 16-byte load (a reference to it loads x and y apart, slower)
+    it.nb = normal_bias(kScalar, S.vel_bias, bias);
     it.invA = S.b.inv_mass[A];
     it.invB = S.b.inv_mass[B];
     it.IA = M3(&S.b.iiw[3 * A]);
@@ -302,34 +301,38 @@ __device__ __forceinline__ float2 velocity_rows_scalar(const Vec3& rA, const Vec
 }
 
 // One point of the velocity sweep on a loaded item: a lane of SolveVelocityBatchSIMD, or
-// SolveContactVelocity under the scalar solver.
-template <typename View>
+// SolveContactVelocity under the scalar solver (kScalar: SolverSettings::useSIMDSolver = false,
+// fixed at compile time so that the batch solver's kernels carry no second row routine).
+template <bool kScalar, typename View>
 __device__ __forceinline__ float2 velocity_item(const SolveBufs& S, const View& V, const VelItem& it) {
     const uint32_t A = it.A, B = it.B, la = it.la, lb = it.lb;
     Vec3 vA = V.lin(la, A), wA = V.ang(la, A), vB = V.lin(lb, B), wB = V.ang(lb, B);
     float4 im = it.im;
-    const float2 q = S.scalar ? velocity_rows_scalar(V3(it.rA), V3(it.rB), it.n, it.t1, it.t2, it.m, it.invA, it.invB,
-                                                     it.nb, it.IA, it.IB, la != kNone, lb != kNone, vA, wA, vB, wB, im)
-                              : velocity_rows(V3(it.rA), V3(it.rB), it.n, it.t1, it.t2, it.m, it.invA, it.invB, it.nb,
-                                              it.IA, it.IB, vA, wA, vB, wB, im);
+    float2 q;
+    if constexpr (kScalar)
+        q = velocity_rows_scalar(V3(it.rA), V3(it.rB), it.n, it.t1, it.t2, it.m, it.invA, it.invB, it.nb, it.IA, it.IB,
+                                 la != kNone, lb != kNone, vA, wA, vB, wB, im);
+    else
+        q = velocity_rows(V3(it.rA), V3(it.rB), it.n, it.t1, it.t2, it.m, it.invA, it.invB, it.nb, it.IA, it.IB, vA, wA,
+                          vB, wB, im);
     if (la != kNone) V.put(la, A, vA, wA);
     if (lb != kNone) V.put(lb, B, vB, wB);
     S.r.imp[it.row] = im;
     return q;
 }
 
-template <typename View>
+template <bool kScalar, typename View>
 __device__ __forceinline__ float2 velocity_point_ab(const SolveBufs& S, const View& V, uint32_t row, uint32_t A,
                                                    uint32_t B, uint32_t la, uint32_t lb) {
     VelItem it;
-    load_vel_item(S, row, A, B, la, lb, it);
-    return velocity_item(S, V, it);
+    load_vel_item<kScalar>(S, row, A, B, la, lb, it);
+    return velocity_item<kScalar>(S, V, it);
 }
 
-template <typename View>
+template <bool kScalar, typename View>
 __device__ __forceinline__ float2 velocity_point(const SolveBufs& S, const View& V, uint32_t row) {
     const uint32_t c = row >> 2;
-    return velocity_point_ab(S, V, row, S.con_a[c], S.con_b[c], __ldcg(&S.con_la[c]), __ldcg(&S.con_lb[c]));
+    return velocity_point_ab<kScalar>(S, V, row, S.con_a[c], S.con_b[c], __ldcg(&S.con_la[c]), __ldcg(&S.con_lb[c]));
 }
 
 // Fixed-point (2^-20 N s) magnitude for the residual sums: integer sums are exact and independent
@@ -364,7 +367,7 @@ __device__ __forceinline__ void bias_point(const SolveBufs& S, const View& V, ui
 // the fixed count, or - with a residual tolerance - until the island's residual, the relative
 // impulse change sum|dImpulse| / sum|impulse| of an iteration (reduced by sync.sum2), is within
 // it, at most res_cap times.
-template <typename Sync, typename View>
+template <bool kScalar, typename Sync, typename View>
 __device__ __forceinline__ void solve_velocity(const SolveBufs& S, uint32_t isl, const View& V, uint32_t tid,
                                                uint32_t nthreads, Sync sync, Counters* cnt) {
     const uint32_t base = 4u * S.isl_start[isl];
@@ -385,7 +388,7 @@ __device__ __forceinline__ void solve_velocity(const SolveBufs& S, uint32_t isl,
         for (uint32_t l = 0; l < nv; ++l) {
             const uint32_t e = S.vl_off[loff + l + 1];
             for (uint32_t k = S.vl_off[loff + l] + tid; k < e; k += nthreads) {
-                const float2 q = velocity_point(S, V, S.vl_list[base + k]);
+                const float2 q = velocity_point<kScalar>(S, V, S.vl_list[base + k]);
                 sd += res_fixed(q.x);
                 sl += res_fixed(q.y);
             }
@@ -468,7 +471,7 @@ struct CtaSync {
 // sweeps.  Pseudo velocities are loaded, not assumed zero: the position pass clears them only for
 // active bodies (PhysicsWorld.cpp:276-290), so a sleeping body solved in an island keeps
 // accumulating them until it wakes.
-template <typename Sync>
+template <bool kScalar, typename Sync>
 __device__ __forceinline__ void solve_island_shared(const SolveBufs& S, uint32_t isl, float4* sv, float4* sw,
                                                     uint32_t tid, uint32_t nthreads, Sync sync, Counters* cnt) {
     const uint32_t nloc = S.meta[4 * isl + 3];
@@ -479,7 +482,7 @@ __device__ __forceinline__ void solve_island_shared(const SolveBufs& S, uint32_t
     }
     sync();
     const VelView V{sv, sw, S.b.lv, S.b.av, true};
-    solve_velocity(S, isl, V, tid, nthreads, sync, cnt);
+    solve_velocity<kScalar>(S, isl, V, tid, nthreads, sync, cnt);
     for (uint32_t k = tid; k < nloc; k += nthreads) {
         S.b.lv[bodies[k]] = sv[k];
         S.b.av[bodies[k]] = sw[k];
@@ -497,6 +500,7 @@ __device__ __forceinline__ void solve_island_shared(const SolveBufs& S, uint32_t
 }
 
 // Small islands: one warp each.
+template <bool kScalar>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_solve_warp(SolveBufs S, Counters* cnt) {
     extern __shared__ float4 smem[];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -510,16 +514,17 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_solve_warp(SolveBufs S,
             k = __shfl_sync(0xffffffffu, k, 0);
             if (k >= n) break;
             const uint32_t isl = S.order[k];
-            if (warp_solved(S, isl)) solve_island_shared(S, isl, sv, sw, lane, 32u, WarpSync{}, cnt);
+            if (warp_solved(S, isl)) solve_island_shared<kScalar>(S, isl, sv, sw, lane, 32u, WarpSync{}, cnt);
         }
         return;
     }
     const uint32_t n = cnt->nsmall;
     for (uint32_t idx = blockIdx.x * kWarpsPerBlock + warp; idx < n; idx += gridDim.x * kWarpsPerBlock)
-        solve_island_shared(S, S.small_list[idx], sv, sw, lane, 32u, WarpSync{}, cnt);
+        solve_island_shared<kScalar>(S, S.small_list[idx], sv, sw, lane, 32u, WarpSync{}, cnt);
 }
 
 // Large islands whose velocities fit shared memory: one CTA each.
+template <bool kScalar>
 __global__ void __launch_bounds__(kCtaThreads) k_solve_cta(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
     extern __shared__ float4 smem[];
     __shared__ unsigned long long red[6];
@@ -534,7 +539,8 @@ __global__ void __launch_bounds__(kCtaThreads) k_solve_cta(SolveBufs S, Counters
             if (k >= n) break;
             const uint32_t isl = S.order[k];
             if (cta_solved(S, isl, smem_bodies))
-                solve_island_shared(S, isl, smem, smem + smem_bodies, threadIdx.x, blockDim.x, CtaSync{red}, cnt);
+                solve_island_shared<kScalar>(S, isl, smem, smem + smem_bodies, threadIdx.x, blockDim.x, CtaSync{red},
+                                             cnt);
         }
         return;
     }
@@ -542,7 +548,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_solve_cta(SolveBufs S, Counters
     for (uint32_t idx = blockIdx.x; idx < n; idx += gridDim.x) {
         const uint32_t isl = S.large_list[idx];
         if (S.meta[4 * isl + 3] > smem_bodies) continue;
-        solve_island_shared(S, isl, smem, smem + smem_bodies, threadIdx.x, blockDim.x, CtaSync{red}, cnt);
+        solve_island_shared<kScalar>(S, isl, smem, smem + smem_bodies, threadIdx.x, blockDim.x, CtaSync{red}, cnt);
     }
 }
 
@@ -558,7 +564,7 @@ struct NoHook {
     __device__ void operator()() const {}
 };
 // after_warm runs on every thread between the warm-start sweep and the velocity sweeps.
-template <typename AfterWarm = NoHook>
+template <bool kScalar, typename AfterWarm = NoHook>
 __device__ void solve_velocity_big(const SolveBufs& S, uint32_t isl, uint32_t* soff, unsigned long long* red,
                                    Counters* cnt, AfterWarm after_warm = AfterWarm{}) {
     const uint32_t tid = threadIdx.x, nthreads = blockDim.x;
@@ -584,7 +590,7 @@ __device__ void solve_velocity_big(const SolveBufs& S, uint32_t isl, uint32_t* s
     after_warm();
     auto off = [&](uint32_t l) -> uint32_t { return staged ? soff[l] : S.vl_off[loff + l]; };
     auto item = [&](const uint4& r) -> float2 {
-        return velocity_point_ab(S, V, r.x, r.y, r.z, (r.w & 1u) ? 0u : kNone, (r.w & 2u) ? 0u : kNone);
+        return velocity_point_ab<kScalar>(S, V, r.x, r.y, r.z, (r.w & 1u) ? 0u : kNone, (r.w & 2u) ? 0u : kNone);
     };
     const bool residual = S.res_tol > 0.0f;
     const uint32_t iters = residual ? S.res_cap : S.vel_iters;
@@ -647,6 +653,7 @@ static __device__ __noinline__ void joints_velocity(const DeviceBodies b, JointD
         for (uint32_t s = r.x; s < r.y; ++s) joint_velocity(B, J[(uint32_t)jk[s]]);
 }
 
+template <bool kScalar>
 __device__ __forceinline__ void solve_joint_island(const SolveBufs& S, uint32_t k, uint32_t* soff,
                                                    unsigned long long* red, Counters* cnt) {
     const uint2 r = S.jisl[k];
@@ -655,7 +662,7 @@ __device__ __forceinline__ void solve_joint_island(const SolveBufs& S, uint32_t 
         if (threadIdx.x == 0) joints_warm(S.b, S.joints, S.jkeys, r);
         __syncthreads();
     };
-    if (cisl != kNone) solve_velocity_big(S, cisl, soff, red, cnt, warm);
+    if (cisl != kNone) solve_velocity_big<kScalar>(S, cisl, soff, red, cnt, warm);
     else warm();
     if (threadIdx.x == 0) joints_velocity(S.b, S.joints, S.jkeys, r, S.vel_iters);
     __syncthreads();
@@ -667,6 +674,7 @@ __device__ __forceinline__ void solve_joint_island(const SolveBufs& S, uint32_t 
 }
 
 // Large islands that neither one CTA's shared memory nor (when S.pk_cap > 0) a cluster takes.
+template <bool kScalar>
 __global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
     __shared__ unsigned long long red[6];
     __shared__ uint32_t soff[kBigOffs + 1];
@@ -675,7 +683,7 @@ __global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, Count
         const uint32_t isl = S.large_list[idx];
         if (S.meta[4 * isl + 3] <= smem_bodies || (S.pk_cap && cluster_island(S, isl, smem_bodies))) continue;
         const VelView P{S.b.plv, S.b.pav, S.b.lv, S.b.av, false};
-        solve_velocity_big(S, isl, soff, red, cnt);
+        solve_velocity_big<kScalar>(S, isl, soff, red, cnt);
         solve_bias(S, isl, P, threadIdx.x, blockDim.x, CtaSync{red});
         __syncthreads();
     }
@@ -684,11 +692,12 @@ __global__ void __launch_bounds__(kBigThreads, 1) k_solve_big(SolveBufs S, Count
 // Islands that hold joints (launched only when the world has joints): one CTA each.  Joint islands
 // are usually small (a chain, a ragdoll), so the CTAs are small and several share an SM.
 constexpr uint32_t kJointThreads = 128;
+template <bool kScalar>
 __global__ void __launch_bounds__(kJointThreads) k_solve_joint(SolveBufs S, Counters* cnt) {
     __shared__ unsigned long long red[6];
     __shared__ uint32_t soff[kBigOffs + 1];
     const uint32_t nj = cnt->njisl;
-    for (uint32_t idx = blockIdx.x; idx < nj; idx += gridDim.x) solve_joint_island(S, idx, soff, red, cnt);
+    for (uint32_t idx = blockIdx.x; idx < nj; idx += gridDim.x) solve_joint_island<kScalar>(S, idx, soff, red, cnt);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1199,8 +1208,8 @@ __device__ uint32_t cluster_layout(const SolveBufs& S, const SolveBufs& SC, uint
 }
 
 // Islands with more than smem_bodies and at most kClusterCtas * kClusterSlots dynamic bodies.
-// kScalar: SolveBufs::scalar, fixed at compile time so that the batch solver's level loop carries
-// no second row routine.
+// kScalar: SolverSettings::useSIMDSolver = false, fixed at compile time so that the batch
+// solver's level loop carries no second row routine.
 template <bool kScalar>
 __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads, 1)
     k_solve_cluster(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
@@ -1219,7 +1228,6 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
     const ClusterView V{sv, sw, S.b.lv, S.b.av, rank};
     const ClusterSync sync{red};
     SolveBufs SC = S;  // the island's constraints with permuted local ids
-    SC.scalar = kScalar ? 1u : 0u;
     SC.con_la = S.cl_ids + 2u * kClusterGrid * kClusterBodies;
     SC.con_lb = SC.con_la + S.max_cons;
     uint32_t* ids = S.cl_ids + 2u * kClusterBodies * cid;
@@ -1238,7 +1246,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
             solve_velocity_packed<kScalar>(SC, isl, V, S.pk + (size_t)cid * kPackArrays * S.pk_cap, soff, lofs, rall, tmp, rank,
                                   gtid, gthreads, sync, cnt);
         else
-            solve_velocity(SC, isl, V, gtid, gthreads, sync, cnt);
+            solve_velocity<kScalar>(SC, isl, V, gtid, gthreads, sync, cnt);
         for (uint32_t k = tid; k < nown; k += blockDim.x) {
             const uint32_t b = __ldcg(&body_of[k * kClusterCtas + rank]);
             S.b.lv[b] = sv[k];

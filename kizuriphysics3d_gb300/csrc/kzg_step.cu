@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(128) k_narrow(ShapeTables T, DeviceBodies b, c
 }
 
 // One warp per deferred pair: the same routine with the warp-cooperative EPA.
-constexpr uint32_t kEpaWarps = 4;
+constexpr uint32_t kEpaWarps = 5;
 __global__ void __launch_bounds__(kEpaWarps * 32) k_narrow_epa(ShapeTables T, DeviceBodies b, const uint2* __restrict__ pairs,
                                                                Counters* cnt, const uint32_t* __restrict__ epa_list,
                                                                const GjkOut* __restrict__ epa_gjk, uint32_t gjk_cap,
@@ -1500,8 +1500,11 @@ size_t cluster_id_words(uint32_t max_cons) { return 2ull * kClusterGrid * kClust
 static bool g_cluster_ok = false;
 
 cudaError_t configure_kernels() {
-    cudaError_t e = cudaFuncSetAttribute(k_solve_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_solve_cta<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(2 * kCtaBodiesMax * sizeof(float4)));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_solve_cta<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(2 * kCtaBodiesMax * sizeof(float4)));
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_sleep_count_ref, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(kSleepCountSmem * (sizeof(uint32_t) + 1)));
@@ -1674,19 +1677,25 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
                  g_cluster_ok ? ctx.pk_cap : 0u, ctx.isl_con, ctx.cfg.max_pairs, ctx.cl_ids,
                  nj ? ctx.joints : nullptr, ctx.jkeys_sorted, ctx.jisl, ctx.jisl_cisl,
                  lpt ? ctx.isl_order : nullptr, nj ? ctx.jflag : nullptr,
-                 std::min(ctx.tune.warp_island_bodies, kWarpBodies), ctx.ss.use_simd_solver ? 0u : 1u};
-    k_solve_warp<<<152u * 16u, kWarpsPerBlock * 32, kWarpsPerBlock * 2 * kWarpBodies * sizeof(float4), st>>>(SV, ctx.dcnt);
-    k_solve_cta<<<152u * 2u, kCtaThreads, 2 * kCtaBodiesMax * sizeof(float4), st>>>(SV, ctx.dcnt, kCtaBodiesMax);
+                 std::min(ctx.tune.warp_island_bodies, kWarpBodies)};
+    // the batch solver's and the scalar solver's kernels are separate instantiations (kScalar)
+    const bool simd = ctx.ss.use_simd_solver != 0;
+    auto* k_warp = simd ? k_solve_warp<false> : k_solve_warp<true>;
+    auto* k_cta = simd ? k_solve_cta<false> : k_solve_cta<true>;
+    auto* k_big = simd ? k_solve_big<false> : k_solve_big<true>;
+    k_warp<<<152u * 16u, kWarpsPerBlock * 32, kWarpsPerBlock * 2 * kWarpBodies * sizeof(float4), st>>>(SV, ctx.dcnt);
+    k_cta<<<152u * 2u, kCtaThreads, 2 * kCtaBodiesMax * sizeof(float4), st>>>(SV, ctx.dcnt, kCtaBodiesMax);
     if (g_cluster_ok) {
-        auto* kern = ctx.ss.use_simd_solver ? k_solve_cluster<false> : k_solve_cluster<true>;
+        auto* kern = simd ? k_solve_cluster<false> : k_solve_cluster<true>;
         kern<<<kClusterCtas * kClusterGrid, kClusterThreads, 2 * kClusterSlots * sizeof(float4), st>>>(
             SV, ctx.dcnt, kCtaBodiesMax);
         ++ctx.launches;
     }
-    k_solve_big<<<152u, kBigThreads, 0, st>>>(SV, ctx.dcnt, kCtaBodiesMax);
+    k_big<<<152u, kBigThreads, 0, st>>>(SV, ctx.dcnt, kCtaBodiesMax);
     ctx.launches += 3;
     if (nj) {
-        k_solve_joint<<<152u * 8u, kJointThreads, 0, st>>>(SV, ctx.dcnt);
+        auto* k_joint = simd ? k_solve_joint<false> : k_solve_joint<true>;
+        k_joint<<<152u * 8u, kJointThreads, 0, st>>>(SV, ctx.dcnt);
         ++ctx.launches;
     }
     ctx.launches += mlp_after_solve(ctx, dt);
