@@ -1106,16 +1106,45 @@ __device__ __forceinline__ bool cluster_island(const SolveBufs& S, uint32_t isl,
 }
 
 // Spatial ownership of a cluster island's bodies: CTA t holds the bodies whose x-z position falls in
-// tile t of a kTilesX x kTilesZ grid over the island's extent - contacts join near bodies, so most
-// points find both velocities in one CTA's shared memory (8-CTA clusters of 4 x 2 tiles solved the
-// settled pile in 15.1 ms against 11.2 ms for 16 CTAs of 4 x 4).  New local ids are slot * kClusterCtas + tile (the
+// tile t of a kTilesX x kTilesZ grid over the island - contacts join near bodies, so most points
+// find both velocities in one CTA's shared memory (8-CTA clusters of 4 x 2 tiles solved the settled
+// pile in 15.1 ms against 11.2 ms for 16 CTAs of 4 x 4).  The tiles hold equal shares of the
+// bodies: kTilesX strips at the quantiles of x, each cut at the quantiles of its bodies' z
+// (kHistBins-bin histograms over the island's extent, gathered in CTA 0's `hist`).  Equal-area
+// tiles gave the centre of a pile 4.8 times the points of a corner per level, and every level
+// waited for the centre CTAs.  New local ids are slot * kClusterCtas + tile (the
 // ClusterView mapping); if a tile overflows its kClusterSlots slots the island keeps its ids.
 // Writes the new ids of the island's constraints (SC.con_la / SC.con_lb) and its bodies by new id;
 // returns how many bodies this CTA holds.  Every read of what it writes goes through L2.
 constexpr uint32_t kTilesX = 4, kTilesZ = kClusterCtas / kTilesX;
 static_assert(kTilesX * kTilesZ == kClusterCtas, "cluster_layout tiles the island kTilesX x kTilesZ");
+constexpr uint32_t kHistBins = 256;
+constexpr uint32_t kHistWords = kHistBins * (1 + kTilesX) + (kTilesX - 1) + kTilesX * (kTilesZ - 1);
+__device__ __forceinline__ uint32_t hist_bin(float v, float v0, float s) {
+    return min(kHistBins - 1u, (uint32_t)fmaxf(0.0f, (v - v0) * s));
+}
+// The kCuts bins at which the running count of h[0..kHistBins) first reaches q / (kCuts + 1) of n.
+template <uint32_t kCuts>
+__device__ __forceinline__ void hist_cuts(const uint32_t* h, uint32_t n, uint32_t* cut) {
+    uint32_t run = 0, q = 0;
+    for (uint32_t b = 0; b < kHistBins && q < kCuts; ++b) {
+        run += h[b];
+        while (q < kCuts && (uint64_t)run * (kCuts + 1) >= (uint64_t)(q + 1) * n) cut[q++] = b;
+    }
+    while (q < kCuts) cut[q++] = kHistBins - 1u;
+}
+// The piece a bin falls in: how many cuts lie below it.
+template <uint32_t kCuts>
+__device__ __forceinline__ uint32_t hist_piece(const uint32_t* cut, uint32_t b) {
+    uint32_t t = 0;
+#pragma unroll
+    for (uint32_t q = 0; q < kCuts; ++q) t += b > cut[q] ? 1u : 0u;
+    return t;
+}
+
 __device__ uint32_t cluster_layout(const SolveBufs& S, const SolveBufs& SC, uint32_t isl, uint32_t* ids,
-                                   uint32_t* sc, float* sbb, uint32_t rank, uint32_t gtid, uint32_t gthreads) {
+                                   uint32_t* sc, float* sbb, uint32_t* hist, uint32_t rank, uint32_t gtid,
+                                   uint32_t gthreads) {
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const uint32_t nloc = S.meta[4 * isl + 3], s0 = S.isl_start[isl], s1 = S.isl_start[isl + 1];
@@ -1168,16 +1197,51 @@ __device__ uint32_t cluster_layout(const SolveBufs& S, const SolveBufs& SC, uint
             mxz = fmaxf(mxz, o[3]);
         }
         sbb[36] = mnx;
-        sbb[37] = 4.0f / fmaxf(mxx - mnx, 1.0e-6f);
+        sbb[37] = (float)kHistBins / fmaxf(mxx - mnx, 1.0e-6f);
         sbb[38] = mnz;
-        sbb[39] = (float)kTilesZ / fmaxf(mxz - mnz, 1.0e-6f);
+        sbb[39] = (float)kHistBins / fmaxf(mxz - mnz, 1.0e-6f);
     }
+    if (rank == 0)
+        for (uint32_t k = tid; k < kHistWords; k += blockDim.x) hist[k] = 0;
     __syncthreads();
+    cl.sync();
     const float x0 = sbb[36], sx = sbb[37], z0 = sbb[38], sz = sbb[39];
+    uint32_t* h0 = cl.map_shared_rank(hist, 0);  // x histogram, then one z histogram per strip, then the cuts
+    uint32_t* xcut = h0 + kHistBins * (1 + kTilesX);
+    uint32_t* zcut = xcut + (kTilesX - 1);
+    for (uint32_t l = gtid; l < nloc; l += gthreads) atomicAdd(&h0[hist_bin(S.b.pos[bodies[l]].x, x0, sx)], 1u);
+    cl.sync();
+    if (rank == 0 && tid == 0) hist_cuts<kTilesX - 1>(hist, nloc, hist + kHistBins * (1 + kTilesX));
+    cl.sync();
+    uint32_t xc[kTilesX - 1];
+#pragma unroll
+    for (uint32_t q = 0; q < kTilesX - 1; ++q) xc[q] = xcut[q];
     for (uint32_t l = gtid; l < nloc; l += gthreads) {
         const float4 p = S.b.pos[bodies[l]];
-        const uint32_t ix = min(kTilesX - 1u, (uint32_t)fmaxf(0.0f, (p.x - x0) * sx));
-        const uint32_t iz = min(kTilesZ - 1u, (uint32_t)fmaxf(0.0f, (p.z - z0) * sz));
+        const uint32_t ix = hist_piece<kTilesX - 1>(xc, hist_bin(p.x, x0, sx));
+        atomicAdd(&h0[kHistBins * (1 + ix) + hist_bin(p.z, z0, sz)], 1u);
+    }
+    cl.sync();
+    if (rank == 0 && tid < kTilesX) {
+        const uint32_t* hz = hist + kHistBins * (1 + tid);
+        uint32_t n = 0;
+        for (uint32_t b = 0; b < kHistBins; ++b) n += hz[b];
+        hist_cuts<kTilesZ - 1>(hz, n, hist + kHistBins * (1 + kTilesX) + (kTilesX - 1) + tid * (kTilesZ - 1));
+    }
+    cl.sync();
+    uint32_t zc[kTilesX][kTilesZ - 1];
+#pragma unroll
+    for (uint32_t i = 0; i < kTilesX; ++i)
+#pragma unroll
+        for (uint32_t q = 0; q < kTilesZ - 1; ++q) zc[i][q] = zcut[i * (kTilesZ - 1) + q];
+    for (uint32_t l = gtid; l < nloc; l += gthreads) {
+        const float4 p = S.b.pos[bodies[l]];
+        const uint32_t ix = hist_piece<kTilesX - 1>(xc, hist_bin(p.x, x0, sx));
+        uint32_t iz = 0;
+        const uint32_t bz = hist_bin(p.z, z0, sz);
+#pragma unroll
+        for (uint32_t i = 0; i < kTilesX; ++i)
+            if (i == ix) iz = hist_piece<kTilesZ - 1>(zc[i], bz);
         const uint32_t t = ix * kTilesZ + iz;
         const uint32_t slot = atomicAdd(cl.map_shared_rank(sc, t), 1u);
         newid[l] = slot * kClusterCtas + t;
@@ -1215,7 +1279,8 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
     k_solve_cluster(SolveBufs S, Counters* cnt, uint32_t smem_bodies) {
     extern __shared__ float4 smem[];
     __shared__ unsigned long long red[6];
-    __shared__ uint32_t soff[kClusterOffs + 2], lofs[kClusterOffs + 1];
+    __shared__ uint32_t soff[kClusterOffs + 2], lofs[kClusterOffs + 1];  // soff: cluster_layout's histograms first
+    static_assert(kHistWords <= kClusterOffs + 2, "the layout histograms live in soff");
     __shared__ uint32_t rall[kClusterCtas], tmp[33], sc[2];
     __shared__ float sbb[40];
     cg::cluster_group cl = cg::this_cluster();
@@ -1235,7 +1300,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
     for (uint32_t idx = cid; idx < n; idx += ncl) {  // the same islands in every CTA of a cluster
         const uint32_t isl = S.large_list[idx];
         if (!cluster_island(S, isl, smem_bodies)) continue;
-        const uint32_t nown = cluster_layout(S, SC, isl, ids, sc, sbb, rank, gtid, gthreads);
+        const uint32_t nown = cluster_layout(S, SC, isl, ids, sc, sbb, soff, rank, gtid, gthreads);
         for (uint32_t k = tid; k < nown; k += blockDim.x) {
             const uint32_t b = __ldcg(&body_of[k * kClusterCtas + rank]);
             sv[k] = S.b.lv[b];
