@@ -1115,7 +1115,8 @@ __global__ void __launch_bounds__(128, 8) k_schedule_warp(SchedBufs S, Counters*
 
 // Larger islands: one CTA each.
 static_assert(kFfBytes <= 3 * kSchedCtaBodies * sizeof(uint32_t), "first-fit table must fit the level tables' shared memory");
-__global__ void __launch_bounds__(256, 1) k_schedule_cta(SchedBufs S, Counters* cnt) {
+constexpr uint32_t kSchedCtaThreads = 512;  // the parallel stages (local ids, level sorts) scale with it
+__global__ void __launch_bounds__(kSchedCtaThreads, 1) k_schedule_cta(SchedBufs S, Counters* cnt) {
     extern __shared__ uint32_t last_sm[];
     __shared__ SchedShared sh;
     __shared__ uint32_t tmp[33];

@@ -1666,7 +1666,7 @@ static kzg_status record_after_pairs(Ctx& ctx, float dt) {
                  std::min(ctx.tune.warp_island_bodies, kWarpBodies), nj ? ctx.jflag : nullptr, ctx.wait_limit,
                  lpt ? ctx.isl_order : nullptr, ctx.ss.use_simd_solver ? 0u : 1u};
     k_schedule_warp<<<152u * 16u, 128, 0, st>>>(SB, ctx.dcnt);
-    k_schedule_cta<<<152u * 2u, 256, 3 * kSchedCtaBodies * sizeof(uint32_t), st>>>(SB, ctx.dcnt);
+    k_schedule_cta<<<152u * 2u, kSchedCtaThreads, 3 * kSchedCtaBodies * sizeof(uint32_t), st>>>(SB, ctx.dcnt);
     ctx.launches += 16;  // prepare, union-find (2), island sort (4 CUB passes), heads, scan (2), starts, schedule (2)
     KZG_CK(mark(ctx, 4));
     SolveBufs SV{ctx.isl_start, ctx.con_a, ctx.con_b, ctx.con_bits, ctx.con_la, ctx.con_lb, ctx.isl_meta,
