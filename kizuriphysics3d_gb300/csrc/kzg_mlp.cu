@@ -144,6 +144,13 @@ __device__ __forceinline__ bool tc_wait(unsigned long long* mbar, uint32_t& phas
     return __syncthreads_and(done != 0) != 0;
 }
 
+// After a wait that gave up (every thread of the CTA calls it): waits once more, bounded, for the
+// committed UMMAs still in flight, so that the tensor memory they write is not freed under them.
+__device__ __forceinline__ void tc_drain(unsigned long long* mbar, uint32_t phase) {
+    uint32_t p = phase ^ 1u;  // the phase the failed wait polled (tc_wait flips it either way)
+    tc_wait(mbar, p);
+}
+
 // 16 accumulator columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     uint32_t r[16];
@@ -354,6 +361,7 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_infer(StepView v, const flo
         float y[kO];
         if (!forward_tc(S, tmem, phase, y)) {
             if (tid == 0) atomicOr(err, KZG_DEVERR_MMA);
+            tc_drain(&S.mbar, phase);
             break;
         }
         if (k < nmiss) {
@@ -581,7 +589,10 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_train(const float* __restri
         if (tid == 0) part_loss[blockIdx.x] = ((S.lred[0] + S.lred[1]) + S.lred[2]) + S.lred[3];
         ok = true;
     } while (false);
-    if (!ok && tid == 0) atomicOr(err, KZG_DEVERR_MMA);
+    if (!ok) {
+        if (tid == 0) atomicOr(err, KZG_DEVERR_MMA);
+        tc_drain(&S.f.mbar, phase);
+    }
     tc_end(S.f, tmem, kTrainTmemCols);
 }
 
@@ -631,8 +642,9 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_predict(const float* __rest
     if (forward_tc(S, tmem, phase, y)) {
         if (valid)
             for (int q = 0; q < kO; ++q) out[(size_t)s * kO + q] = y[q];
-    } else if (tid == 0) {
-        atomicOr(err, KZG_DEVERR_MMA);
+    } else {
+        if (tid == 0) atomicOr(err, KZG_DEVERR_MMA);
+        tc_drain(&S.mbar, phase);
     }
     tc_end(S, tmem);
 }
