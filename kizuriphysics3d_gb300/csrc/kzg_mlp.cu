@@ -771,6 +771,21 @@ kzg_status mlp_set_dataset(Ctx& ctx, const float* samples, uint32_t n) {
     return KZG_OK;
 }
 
+// Reads the device error word after an MLP launch outside the step: a tensor-core wait that gave up
+// is taken out of the word and returned as KZG_ERR_DEVICE.
+static kzg_status take_mma_error(Ctx& ctx) {
+    uint32_t e = 0;
+    MLP_CK(cudaMemcpyAsync(&e, &ctx.dcnt->error, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx.stream));
+    MLP_CK(cudaStreamSynchronize(ctx.stream));
+    if (e & KZG_DEVERR_MMA) {
+        const uint32_t keep = e & ~KZG_DEVERR_MMA;
+        MLP_CK(cudaMemcpy(&ctx.dcnt->error, &keep, sizeof(uint32_t), cudaMemcpyHostToDevice));
+        ctx.err = "mlp: a tensor-core wait gave up (KZG_DEVERR_MMA)";
+        return KZG_ERR_DEVICE;
+    }
+    return KZG_OK;
+}
+
 static kzg_status mlp_batch_grad(Ctx& ctx, uint32_t first, uint32_t count, float* loss_out) {
     MlpState& M = ctx.mlp;
     if (!M.have || !M.ds || count == 0 || first > M.ds_n || count > M.ds_n - first) {
@@ -791,6 +806,8 @@ static kzg_status mlp_batch_grad(Ctx& ctx, uint32_t first, uint32_t count, float
                                                                           M.tau, M.part, part_loss, &ctx.dcnt->error);
     k_mlp_reduce<<<(kP + 255) / 256, 256, 0, ctx.stream>>>(M.part, part_loss, nblk, M.grad, M.grad + kP);
     MLP_CK(cudaGetLastError());
+    const kzg_status s = take_mma_error(ctx);  // a tile without gradients: no update from this batch
+    if (s != KZG_OK) return s;
     if (loss_out) {
         MLP_CK(cudaMemcpyAsync(loss_out, M.grad + kP, sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
         MLP_CK(cudaStreamSynchronize(ctx.stream));
@@ -839,16 +856,7 @@ kzg_status mlp_predict(Ctx& ctx, uint32_t first, uint32_t count, float* out) {
     k_mlp_predict<<<nblk, kMlpThreads, sizeof(MlpSmemTc), ctx.stream>>>(M.theta, M.norm, M.ds, first, count, M.out, err);
     MLP_CK(cudaGetLastError());
     MLP_CK(cudaMemcpyAsync(out, M.out, sizeof(float) * kO * (size_t)count, cudaMemcpyDeviceToHost, ctx.stream));
-    uint32_t e = 0;
-    MLP_CK(cudaMemcpyAsync(&e, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx.stream));
-    MLP_CK(cudaStreamSynchronize(ctx.stream));
-    if (e & KZG_DEVERR_MMA) {
-        const uint32_t keep = e & ~KZG_DEVERR_MMA;
-        MLP_CK(cudaMemcpy(err, &keep, sizeof(uint32_t), cudaMemcpyHostToDevice));
-        ctx.err = "mlp: a tensor-core wait gave up (KZG_DEVERR_MMA)";
-        return KZG_ERR_DEVICE;
-    }
-    return KZG_OK;
+    return take_mma_error(ctx);
 }
 
 // In-step hooks (kzg_step.cu).  launches: kernels issued.
