@@ -132,9 +132,17 @@ __device__ __forceinline__ bool pair_ok(const DeviceBodies& b, uint32_t i, uint3
     return aabb_overlaps(A, B);
 }
 
-__device__ __forceinline__ void emit_pair(unsigned long long* out, Counters* cnt, uint32_t cap, uint32_t pi, uint32_t pj) {
+// The pair's sort key: lower packed id << kb | higher, kb bits each (packed ids < 2^kb), so that
+// the radix sort only passes over 2 kb bits and orders pairs as MakePairKey's 64-bit keys do.
+__device__ __forceinline__ unsigned long long pair_sort_key(uint32_t pa, uint32_t pb, uint32_t kb) {
+    if (pa > pb) { uint32_t t = pa; pa = pb; pb = t; }
+    return ((unsigned long long)pa << kb) | (unsigned long long)pb;
+}
+
+__device__ __forceinline__ void emit_pair(unsigned long long* out, Counters* cnt, uint32_t cap, uint32_t kb,
+                                          uint32_t pi, uint32_t pj) {
     uint32_t slot = atomicAdd(&cnt->npairs, 1u);
-    if (slot < cap) out[slot] = pair_key(pi, pj);
+    if (slot < cap) out[slot] = pair_sort_key(pi, pj, kb);
     else atomicOr(&cnt->error, KZG_DEVERR_PAIRS);
 }
 
@@ -145,7 +153,7 @@ __global__ void k_find_pairs(DeviceBodies b, uint32_t n, const unsigned long lon
                              const uint32_t* __restrict__ svals, uint32_t nsmall, float inv_cell,
                              const uint8_t* __restrict__ is_large, const uint32_t* __restrict__ large_list,
                              const uint32_t* __restrict__ large_off, uint32_t nworld_large, unsigned long long* out,
-                             Counters* cnt, uint32_t cap) {
+                             Counters* cnt, uint32_t cap, uint32_t kb) {
     // Threads take the bodies in cell order, so that a warp's neighbours, its cell searches and the
     // bounds it reads are shared (the emitted pairs are sorted afterwards; their order here is free).
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -159,7 +167,7 @@ __global__ void k_find_pairs(DeviceBodies b, uint32_t n, const unsigned long lon
             uint32_t j = large_list[k];
             if (j == i) continue;
             if (is_large[i] && b.packed[j] <= pi) continue;  // large-large: owned by the lower id
-            if (pair_ok(b, i, j)) emit_pair(out, cnt, cap, pi, b.packed[j]);
+            if (pair_ok(b, i, j)) emit_pair(out, cnt, cap, kb, pi, b.packed[j]);
         }
     }
     if (is_large[i]) return;
@@ -179,7 +187,7 @@ __global__ void k_find_pairs(DeviceBodies b, uint32_t n, const unsigned long lon
             for (uint32_t s = lo; s < nsmall && skeys[s] <= key_hi; ++s) {
                 uint32_t j = svals[s];
                 if (b.packed[j] <= pi) continue;
-                if (pair_ok(b, i, j)) emit_pair(out, cnt, cap, pi, b.packed[j]);
+                if (pair_ok(b, i, j)) emit_pair(out, cnt, cap, kb, pi, b.packed[j]);
             }
         }
 }
@@ -204,11 +212,12 @@ __global__ void k_pad_keys(unsigned long long* keys, const Counters* cnt, uint32
     if (i >= cnt->npairs && i < cap) keys[i] = ~0ull;
 }
 
-__global__ void k_unpack_pairs(const unsigned long long* __restrict__ keys, const Counters* cnt, uint2* pairs) {
+__global__ void k_unpack_pairs(const unsigned long long* __restrict__ keys, const Counters* cnt, uint2* pairs,
+                               uint32_t kb) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cnt->npairs) return;
     unsigned long long k = keys[i];
-    pairs[i] = make_uint2((uint32_t)(k >> 32) & 0x00FFFFFFu, (uint32_t)k & 0x00FFFFFFu);
+    pairs[i] = make_uint2((uint32_t)(k >> kb) & 0x00FFFFFFu, (uint32_t)(k & ((1ull << kb) - 1ull)) & 0x00FFFFFFu);
 }
 
 // Caller-supplied pairs (packed BodyIDs, broad-phase order) -> slots; stale ids become invalid.
@@ -1810,6 +1819,7 @@ static kzg_status record_canonical(Ctx& ctx, float dt) {
     cudaStream_t st = ctx.stream;
     KZG_CK(cudaPeekAtLastError());
     const uint32_t nb = ctx.nbodies, P = ctx.cfg.max_pairs;
+    const uint32_t kb = (uint32_t)bits_for(nb);  // bits of a packed id (packed ids are slots)
     ctx.launches = 0;
     k_begin_step<<<1, 32, 0, st>>>(ctx.dcnt);
     KZG_CK(mark(ctx, 0));
@@ -1821,12 +1831,13 @@ static kzg_status record_canonical(Ctx& ctx, float dt) {
     const uint32_t nsmall = nb - ctx.nlarge;
     k_find_pairs<<<blocks_for(nb), kThreads, 0, st>>>(ctx.b, nb, ctx.cell_keys_sorted, ctx.cell_vals_sorted, nsmall,
                                                       1.0f / ctx.cell_size, ctx.is_large, ctx.large_list,
-                                                      ctx.large_off, ctx.nworlds, ctx.pair_keys, ctx.dcnt, P);
+                                                      ctx.large_off, ctx.nworlds, ctx.pair_keys, ctx.dcnt, P, kb);
     k_clamp_pairs<<<1, 1, 0, st>>>(ctx.dcnt, P);
     k_pad_keys<<<blocks_for(P), kThreads, 0, st>>>(ctx.pair_keys, ctx.dcnt, P);
     tb = ctx.cub_tmp_bytes;
-    KZG_CK(cub::DeviceRadixSort::SortKeys(ctx.cub_tmp, tb, ctx.pair_keys, ctx.pair_keys_sorted, (int)P, 0, 64, st));
-    k_unpack_pairs<<<blocks_for(P), kThreads, 0, st>>>(ctx.pair_keys_sorted, ctx.dcnt, ctx.pairs);
+    KZG_CK(cub::DeviceRadixSort::SortKeys(ctx.cub_tmp, tb, ctx.pair_keys, ctx.pair_keys_sorted, (int)P, 0, 2 * kb,
+                                          st));
+    k_unpack_pairs<<<blocks_for(P), kThreads, 0, st>>>(ctx.pair_keys_sorted, ctx.dcnt, ctx.pairs, kb);
     ctx.launches += 16;  // begin, aabb, cell sort (4 CUB passes), find pairs, clamp, pad, key sort (4+), unpack
     return record_after_pairs(ctx, dt);
 }
