@@ -255,35 +255,11 @@ constexpr uint32_t kEpaVerts = 68;  // the initial tetrahedron + one vertex per 
 constexpr uint32_t kEpaFaces = 512;
 constexpr uint32_t kEpaHorizon = 256;
 
-struct EpaFace {
-    uint32_t a, b, c;
-    Vec3 n;
-    float dist;
-    uint32_t alive;
-};
-
 struct EpaOut {
     bool valid;
     float depth;
     Vec3 normal, pA, pB;
 };
-
-__device__ __forceinline__ bool epa_build_face(EpaFace& f, const SP* vs) {
-    Vec3 A = vs[f.a].p, B = vs[f.b].p, C = vs[f.c].p;
-    Vec3 n = (B - A).cross(C - A);
-    float len = n.len();
-    if (len < 1.0e-12f) return false;
-    n = n / len;
-    float d = n.dot(A);
-    if (d < 0.0f) {
-        n = -n;
-        d = -d;
-        uint32_t t = f.b; f.b = f.c; f.c = t;
-    }
-    f.n = n;
-    f.dist = d;
-    return true;
-}
 
 __device__ __forceinline__ Vec3 epa_perp(const Vec3& v) {
     if (rabs(v.x) <= rabs(v.y) && rabs(v.x) <= rabs(v.z)) return Vec3(0.0f, -v.z, v.y);
@@ -299,102 +275,6 @@ __device__ __forceinline__ bool tet_face_ok(const Vec3& a, const Vec3& b, const 
 __device__ __forceinline__ bool origin_in_tetra(const SP* v) {
     return tet_face_ok(v[0].p, v[1].p, v[2].p, v[3].p) && tet_face_ok(v[0].p, v[2].p, v[3].p, v[1].p) &&
            tet_face_ok(v[0].p, v[3].p, v[1].p, v[2].p) && tet_face_ok(v[1].p, v[3].p, v[2].p, v[0].p);
-}
-
-__device__ inline bool epa_initial_tetra(const SupportMap& map, const GjkOut& g, SP* out) {
-    uint32_t n = 0;
-    for (uint32_t i = 0; i < g.ns && n < 4; ++i) {
-        bool dup = false;
-        for (uint32_t j = 0; j < n; ++j)
-            if ((out[j].p - g.simplex[i].p).len2() < 1.0e-12f) dup = true;
-        if (!dup) out[n++] = g.simplex[i];
-    }
-    if (n == 0) out[n++] = map(Vec3(1.0f, 0.0f, 0.0f));
-    if (n == 4 && !origin_in_tetra(out)) n = 3;
-    if (n == 1) {
-        out[n] = map(-out[0].p);
-        if ((out[1].p - out[0].p).len2() > 1.0e-12f) ++n;
-    }
-    if (n == 2) {
-        Vec3 ab = out[1].p - out[0].p;
-        if (ab.len2() > 1.0e-12f) {
-            Vec3 d1 = epa_perp(ab).normalized();
-            Vec3 d2 = ab.cross(d1).normalized();
-            SP k0 = out[0], k1 = out[1];
-            out[0] = map(d1);
-            out[1] = map(-d1);
-            out[2] = map(d2);
-            out[3] = map(-d2);
-            if (origin_in_tetra(out)) return true;
-            out[0] = k0;
-            out[1] = k1;
-        }
-        SP s = map(epa_perp(ab));
-        if ((s.p - out[0].p).len2() > 1.0e-12f && (s.p - out[1].p).len2() > 1.0e-12f) out[n++] = s;
-    }
-    if (n == 3) {
-        Vec3 tn = (out[1].p - out[0].p).cross(out[2].p - out[0].p);
-        float len = tn.len();
-        if (len > 1.0e-12f) {
-            tn = tn / len;
-            float sd = tn.dot(Vec3() - out[0].p);
-            SP a = map(sd > 0.0f ? -tn : tn);
-            SP b = map(sd > 0.0f ? tn : -tn);
-            out[3] = a;
-            if (!origin_in_tetra(out)) out[3] = b;
-            if (origin_in_tetra(out)) return true;
-        }
-        n = 3;
-    }
-    if (n == 4 && origin_in_tetra(out)) return true;
-
-    SP cand[16];
-    uint32_t nc = 0;
-    auto add = [&](const SP& sp) {
-        for (uint32_t i = 0; i < nc; ++i)
-            if ((cand[i].p - sp.p).len2() < 1.0e-12f) return;
-        if (nc < 16) cand[nc++] = sp;
-    };
-    for (uint32_t i = 0; i < g.ns && i < 4; ++i) add(g.simplex[i]);
-    const float s = 0.5773502692f;
-    const float D[14][3] = {{1, 0, 0},   {-1, 0, 0},  {0, 1, 0},  {0, -1, 0}, {0, 0, 1},  {0, 0, -1}, {s, s, s},
-                            {s, s, -s},  {s, -s, s},  {-s, s, s}, {-s, -s, s}, {-s, s, -s}, {s, -s, -s}, {-s, -s, -s}};
-    for (int i = 0; i < 14; ++i) add(map(Vec3(D[i][0], D[i][1], D[i][2])));
-    for (uint32_t i = 0; i + 3 < nc; ++i)
-        for (uint32_t j = i + 1; j + 2 < nc; ++j)
-            for (uint32_t k = j + 1; k + 1 < nc; ++k)
-                for (uint32_t l = k + 1; l < nc; ++l) {
-                    SP t[4] = {cand[i], cand[j], cand[k], cand[l]};
-                    float vol = (t[1].p - t[0].p).cross(t[2].p - t[0].p).dot(t[3].p - t[0].p);
-                    if (rabs(vol) < 1.0e-12f) continue;
-                    if (origin_in_tetra(t)) {
-                        for (int m = 0; m < 4; ++m) out[m] = t[m];
-                        return true;
-                    }
-                }
-    return false;
-}
-
-
-__device__ inline void epa_finish(const EpaFace& f, const SP* vs, EpaOut& r) {
-    Vec3 proj = f.n * f.dist;
-    Vec3 a = vs[f.a].p, b = vs[f.b].p, c = vs[f.c].p;
-    Vec3 v0 = b - a, v1 = c - a, v2 = proj - a;
-    float d00 = v0.dot(v0), d01 = v0.dot(v1), d11 = v1.dot(v1);
-    float d20 = v2.dot(v0), d21 = v2.dot(v1);
-    float denom = d00 * d11 - d01 * d01;
-    float u, v, w;
-    if (rabs(denom) < 1.0e-18f) { u = 1.0f; v = 0.0f; w = 0.0f; }
-    else {
-        v = rdiv(d11 * d20 - d01 * d21, denom);
-        w = rdiv(d00 * d21 - d01 * d20, denom);
-        u = 1.0f - v - w;
-    }
-    r.valid = true;
-    r.depth = f.dist;
-    r.normal = -f.n;
-    r.pA = (vs[f.a].pA * u + vs[f.b].pA * v) + vs[f.c].pA * w;
-    r.pB = (vs[f.a].pB * u + vs[f.b].pB * v) + vs[f.c].pB * w;
 }
 
 // Polytope of one EPA run, in shared memory, owned by one warp.
