@@ -1833,12 +1833,25 @@ static kzg_status record_canonical(Ctx& ctx, float dt) {
                                                       1.0f / ctx.cell_size, ctx.is_large, ctx.large_list,
                                                       ctx.large_off, ctx.nworlds, ctx.pair_keys, ctx.dcnt, P, kb);
     k_clamp_pairs<<<1, 1, 0, st>>>(ctx.dcnt, P);
-    k_pad_keys<<<blocks_for(P), kThreads, 0, st>>>(ctx.pair_keys, ctx.dcnt, P);
-    tb = ctx.cub_tmp_bytes;
-    KZG_CK(cub::DeviceRadixSort::SortKeys(ctx.cub_tmp, tb, ctx.pair_keys, ctx.pair_keys_sorted, (int)P, 0, 2 * kb,
-                                          st));
-    k_unpack_pairs<<<blocks_for(P), kThreads, 0, st>>>(ctx.pair_keys_sorted, ctx.dcnt, ctx.pairs, kb);
-    ctx.launches += 16;  // begin, aabb, cell sort (4 CUB passes), find pairs, clamp, pad, key sort (4+), unpack
+    // The pair sort's size: in a captured graph the capacity, the keys past the pair count padded to
+    // sort last; stepped directly, the pair count itself, read back here (one round trip instead of
+    // radix passes over the whole capacity).
+    uint32_t nsort = P;
+    if (ctx.capturing) {
+        k_pad_keys<<<blocks_for(P), kThreads, 0, st>>>(ctx.pair_keys, ctx.dcnt, P);
+        ++ctx.launches;
+    } else {
+        KZG_CK(cudaMemcpyAsync(&ctx.hcnt->npairs, &ctx.dcnt->npairs, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        KZG_CK(cudaStreamSynchronize(st));
+        nsort = std::min(ctx.hcnt->npairs, P);
+    }
+    if (nsort) {
+        tb = ctx.cub_tmp_bytes;
+        KZG_CK(cub::DeviceRadixSort::SortKeys(ctx.cub_tmp, tb, ctx.pair_keys, ctx.pair_keys_sorted, (int)nsort, 0,
+                                              2 * kb, st));
+        k_unpack_pairs<<<blocks_for(nsort), kThreads, 0, st>>>(ctx.pair_keys_sorted, ctx.dcnt, ctx.pairs, kb);
+    }
+    ctx.launches += 15;  // begin, aabb, cell sort (4 CUB passes), find pairs, clamp, key sort (4+), unpack
     return record_after_pairs(ctx, dt);
 }
 
