@@ -1814,7 +1814,8 @@ static kzg_status finish_stats(Ctx& ctx, uint32_t graph_steps = 0) {
     return KZG_OK;
 }
 
-// One canonical step (GPU broad phase), issued without host synchronisation.
+// One canonical step (GPU broad phase).  Stepped directly it reads the pair count back once (the pair
+// sort covers that count); while a graph is captured it issues no host synchronisation.
 static kzg_status record_canonical(Ctx& ctx, float dt) {
     cudaStream_t st = ctx.stream;
     KZG_CK(cudaPeekAtLastError());
